@@ -1,0 +1,244 @@
+/*
+ * sfem.h -- C ABI of the GB300-native matrix-free nonlinear elasticity solver.
+ *
+ * Drop-in boundary for SolidFEM's FemPhysicsMatrixFree / NewtonSolver /
+ * NonlinearCG / ElasticEnergy path.  The reference exposes that path as a C++
+ * class, not as an FFI; every entry point below names the reference member it
+ * replaces (file:line within the SolidFEM project).
+ *
+ * Conventions
+ *  - Plain pointers and sizes; no library types cross the boundary.
+ *  - Node arrays passed in "original order" are N x 3 doubles, row-major.
+ *  - "Free-DOF vectors" are 3*N_f doubles in the reference's reshuffled order:
+ *    fixed nodes first, then free nodes in their original relative order
+ *    (FemPhysicsMatrixFree::ReshuffleFixedNodes, Source/FemPhysicsMatrixFree.cpp:229-263);
+ *    entry i of a free-DOF vector is reshuffled node i + N_bc.
+ *  - Host-pointer entry points copy in and out on the handle's stream and
+ *    return after the result is on the host.  *_dev entry points take device
+ *    pointers and are stream-ordered (asynchronous) on the handle's stream.
+ *  - Every call returns an int status: 0 = OK, > 0 = ran but did not
+ *    converge (see SFEM_*), < 0 = error.  sfem_last_error() gives the message.
+ *  - One handle per host thread; a handle is not thread-safe.
+ */
+#ifndef SFEM_H
+#define SFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SFEM_OK 0
+#define SFEM_NOT_CONVERGED 1      /* iteration cap reached */
+#define SFEM_LINESEARCH_FAILED 2  /* backtracking gave up (reference: NewtonSolver.h:282-292) */
+#define SFEM_ERR_INVALID (-1)
+#define SFEM_ERR_CUDA (-2)
+#define SFEM_ERR_NAN (-3)               /* reference: NewtonSolver.h:313-319 */
+#define SFEM_ERR_INVERTED (-4)          /* reference: FemPhysicsBase::CheckForInversion */
+#define SFEM_ERR_OOM (-5)
+#define SFEM_ERR_BREAKDOWN (-6)         /* CG curvature p.Ap <= 0 */
+#define SFEM_ERR_NO_DEVICE (-7)
+
+/* ---- material models: values of MaterialModelType, Include/FemDataStructures.h:90-105 ---- */
+#define SFEM_MMT_LINEAR 0
+#define SFEM_MMT_STVK 1
+#define SFEM_MMT_COROTATIONAL 2
+#define SFEM_MMT_NEO_HOOKEAN 3
+
+/* ---- precision of the element kernels and the inner Krylov solve ---- */
+#define SFEM_FP64 0
+#define SFEM_FP32 1 /* FP32 element kernels + CG; FP64 Newton residual and convergence test */
+
+/* ---- tangent used by the Hessian-vector product ---- */
+#define SFEM_TANGENT_REFERENCE 0 /* the reference's force differential (FemPhysicsMatrixFree.cpp:436-470) */
+#define SFEM_TANGENT_EXACT 1     /* exact derivative of the force; differs only for corotational,
+                                    whose reference differential assumes a true polar R */
+
+/* ---- preconditioners ---- */
+#define SFEM_PC_NONE 0   /* reference SolveConjugateGradientMF with usePrecond=false */
+#define SFEM_PC_JACOBI 1 /* per-DOF diagonal of the element tangents */
+#define SFEM_PC_LEARNED 2 /* graph-network preconditioner in flexible PCG (sfem_gnn_*) */
+
+/* ---- line-search conditions: values of LSCondition, Include/NewtonSolver.h:54-58, plus one ---- */
+#define SFEM_LSC_ARMIJO 0        /* energy decrease (reference: mOptimizer merit) */
+#define SFEM_LSC_ENGINEERING 1   /* Bonet-Wood condition as coded in NewtonSolver.h:257-261 */
+#define SFEM_LSC_RESIDUAL 2      /* |r(x + a d)| <= (1 - 1e-4 a) |r(x)| */
+
+typedef struct sfem_handle sfem_handle;
+
+/* Replaces FemConfig (Include/FemDataStructures.h:131-156) for this path. */
+typedef struct {
+  double young;       /* mYoungsModulus */
+  double poisson;     /* mPoissonRatio */
+  double density;     /* mDensity */
+  double gravity[3];  /* mGravity as a vector (reference: scalar + mZUpAxis, FemPhysicsBase.cpp:30-33) */
+  int32_t material;   /* SFEM_MMT_* (mMaterial) */
+  int32_t precision;  /* SFEM_FP64 / SFEM_FP32 */
+  int32_t device;     /* CUDA device ordinal */
+  int32_t tangent;    /* SFEM_TANGENT_* */
+} sfem_config;
+
+typedef struct {
+  double rel_tol;     /* stop when |r| <= rel_tol |b| (reference eps on r.z, IterativeSolvers.h:184) */
+  int32_t max_iters;  /* mInnerIterations */
+  int32_t precond;    /* SFEM_PC_* */
+  int32_t check_every;/* host convergence poll interval (iterations); 0 = default */
+  int32_t reserved;
+} sfem_pcg_opts;
+
+typedef struct {
+  int32_t iters;
+  int32_t status;
+  double rel_res;     /* final |r| / |b| of the Krylov recurrence */
+} sfem_pcg_stats;
+
+/* Replaces NewtonSolverBackTrack's fields (Include/NewtonSolver.h:77-93) and
+ * FemPhysicsMatrixFree::SolveNewtonCG's loop (Source/FemPhysicsMatrixFree.cpp:604-628). */
+typedef struct {
+  double rel_tol;        /* converge when |r(x)| <= rel_tol |r(x_0)| (FP64 residual) */
+  double abs_tol;        /* ... or |r(x)| <= abs_tol (mResidualThreshold); 0 disables */
+  int32_t max_newton;    /* mNumIterations */
+  int32_t max_cg;        /* per inner solve (mInnerIterations) */
+  double eta_max;        /* inexact-Newton forcing term cap (0 -> 0.5) */
+  double eta_min;        /* forcing term floor (0 -> 1e-10 FP64, 1e-5 FP32) */
+  int32_t precond;       /* SFEM_PC_* */
+  int32_t ls_condition;  /* SFEM_LSC_* */
+  int32_t max_bisection; /* backtracking halvings (mMaxBisection; 0 -> 30) */
+  int32_t verbose;
+  int32_t load_steps;    /* >1: quasi-static force-fraction ramp (ST_QUASI_STATIC, FemPhysicsMatrixFree.cpp:333-340) */
+  int32_t reserved;
+} sfem_newton_opts;
+
+typedef struct {
+  int32_t newton_iters;
+  int32_t cg_iters;       /* total inner iterations */
+  int32_t status;
+  int32_t line_search_cuts;
+  double r0;              /* |r(x_0)| */
+  double rel_res;         /* |r(x)| / |r(x_0)| at return */
+  double seconds;         /* device time of the solve (CUDA events) */
+} sfem_newton_stats;
+
+/* ---- lifetime ---- */
+
+/* FemPhysicsMatrixFree::FemPhysicsMatrixFree (Source/FemPhysicsMatrixFree.cpp:71-213) with
+ * the orientation fix of FemBody::Prepare (Source/FemBody.cpp:127-156) and the fixed-node
+ * flags of PyNonlinearFEM's constructor (PySolidFEM/PyNonlinearFEM.cpp:48-55).
+ * nodes: N x 3; tets: E x 4 (0-based); fixed: node indices. */
+int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets, int64_t n_tets,
+                const int32_t* fixed, int64_t n_fixed, const sfem_config* cfg, sfem_handle** out);
+int sfem_destroy(sfem_handle* h);
+/* Last error message of this thread (never NULL). */
+const char* sfem_last_error(void);
+
+/* ---- queries ---- */
+/* GetNumNodes / GetNumFreeNodes / GetNumElements (Include/FemPhysicsMatrixFree.h:74-77) */
+int sfem_sizes(const sfem_handle* h, int64_t* n_nodes, int64_t* n_free, int64_t* n_tets);
+/* mReshuffleMap (Include/FemPhysicsBase.h:173): original -> reshuffled node index */
+int sfem_reshuffle_map(const sfem_handle* h, int32_t* map);
+/* the CUDA stream the handle's work is ordered on (cudaStream_t) */
+int sfem_get_stream(const sfem_handle* h, void** stream);
+int sfem_set_stream(sfem_handle* h, void* stream);
+
+/* ---- state ---- */
+/* GetDeformedPosition / SetDeformedPosition for all nodes, original order
+ * (Include/FemPhysicsMatrixFree.h:69-71; PyNonlinearFEM::GetNodes, PyNonlinearFEM.cpp:145-159). */
+int sfem_get_positions(sfem_handle* h, double* pos);
+int sfem_set_positions(sfem_handle* h, const double* pos);
+/* Free-node positions in reshuffled order (UpdatePosAndComputeGradients' input,
+ * Source/FemPhysicsMatrixFree.cpp:562-568). */
+int sfem_get_free_positions(sfem_handle* h, double* pos_free);
+int sfem_set_free_positions(sfem_handle* h, const double* pos_free);
+/* SetLameParams (Include/FemPhysicsBase.h:106-114). */
+int sfem_set_lame_params(sfem_handle* h, double mu, double lambda);
+/* mForceFraction (Include/FemPhysicsBase.h:176). */
+int sfem_set_force_fraction(sfem_handle* h, double f);
+/* Extension (no reference counterpart: material parameters are scalars,
+ * Include/FemPhysicsBase.h:152-155): per-element Young's modulus, original element
+ * order; NULL restores the uniform modulus. */
+int sfem_set_element_youngs(sfem_handle* h, const double* young_e);
+/* Extension (FemPhysicsBase::SetExternalForces is an ASSERT stub, Include/FemPhysicsBase.h:68):
+ * dead nodal loads, N x 3 original order, added to the residual scaled by mForceFraction. */
+int sfem_set_nodal_loads(sfem_handle* h, const double* f);
+
+/* ---- physics ---- */
+/* FemPhysicsMatrixFree::ComputeGradients (Source/FemPhysicsMatrixFree.cpp:536-560), static:
+ * r = f_int + m g ff + f_ext ff over free DOFs.  norm (optional) receives |r|_2 in FP64. */
+int sfem_compute_gradients(sfem_handle* h, double* r, double* norm);
+/* FemPhysicsMatrixFree::MatrixVectorMultiply (Source/FemPhysicsMatrixFree.cpp:523-534),
+ * static: Kd = -ComputeForceDifferential(d) (:406-496).  FP64. */
+int sfem_matvec(sfem_handle* h, const double* d, double* Kd);
+/* FemPhysicsMatrixFree::DotProduct (Include/FemPhysicsMatrixFree.h:89). */
+int sfem_dot(sfem_handle* h, const double* a, const double* b, double* out);
+/* Per-DOF diagonal of the tangent: diagonal of the local stiffness matrices of
+ * ElasticEnergy::ComputeLocalStiffnessMatrixFromDifferential (Source/ElasticEnergy.cpp:493-517)
+ * summed per node (3 N_f). */
+int sfem_jacobi_diagonal(sfem_handle* h, double* diag);
+/* FemPhysicsBase::ComputeElasticEnergy (Source/FemPhysicsBase.cpp:203-212) and the total
+ * potential (elastic - (m g + f_ext) . x, full gravity vector; cf. FemPhysicsMatrixFree::ComputeEnergy
+ * :882-916 which uses g.y only). */
+int sfem_energy(sfem_handle* h, double* elastic, double* total);
+/* FemPhysicsBase::CheckForInversion (Source/FemPhysicsBase.cpp:93-117): elements with det F <= 0. */
+int sfem_count_inverted(sfem_handle* h, int64_t* count);
+/* ElasticEnergy::ComputeElementStress (Source/ElasticEnergy.cpp:114-257): PK1 per element,
+ * E x 9 row-major, original element order. */
+int sfem_element_stress(sfem_handle* h, double* P);
+/* FemPhysicsBase::GetForceParamGrads (Source/FemPhysicsBase.cpp:162-187): free-DOF
+ * d f / d mu, d f / d lambda, d f / d rho. */
+int sfem_force_param_grads(sfem_handle* h, double* gmu, double* glambda, double* grho);
+
+/* ---- solvers ---- */
+/* SolveConjugateGradientMF (Math/IterativeSolvers.h:115-195) on K x = b, zero initial guess,
+ * with the chosen preconditioner, in the handle's precision. b, x: free-DOF vectors. */
+int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* opts, sfem_pcg_stats* stats);
+/* Static equilibrium solve (FemPhysicsMatrixFree::Step(0) -> Solve -> SolveNewtonCG /
+ * SolveNewtonLS, Source/FemPhysicsMatrixFree.cpp:325-331, 604-628, 733-781): globalized inexact
+ * Newton with matrix-free PCG inner solves.  Updates the handle's positions. */
+int sfem_newton_solve(sfem_handle* h, const sfem_newton_opts* opts, sfem_newton_stats* stats);
+/* NonlinearConjugateGradientMinimizer::Solve (Include/NonlinearCG.h:51-114) with the
+ * reference's constants; outer/inner iteration caps and absolute threshold as its fields. */
+int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, double abs_tol,
+                      int32_t* iters_done);
+
+/* ---- differentiation (extension; the reference has only global mu/lambda/rho force
+ * gradients, Source/ElasticEnergy.cpp:284-315) ---- */
+/* Adjoint of the static equilibrium at the current state: solves K lam = dLdu (free DOFs)
+ * and returns dL/dE_e (E x 1, original element order) and dL/df_ext (free DOFs). */
+int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max_cg,
+                 double* dLdE, double* dLdf);
+
+/* ---- instrumentation (no reference counterpart: the reference's PROFILE_SCOPE macros are
+ * empty, Engine/Profiler.h:35-39) ---- */
+typedef struct {
+  double hvp_elem_ms;      /* summed CUDA-event time of sampled element Hessian-vector launches */
+  double hvp_gather_ms;    /* summed time of the matching node gathers */
+  int64_t samples;         /* number of sampled launches */
+  int64_t hvp_launches;    /* all element Hessian-vector launches since profiling was enabled */
+  double algo_bytes_hvp;   /* algorithmic bytes of one launch: E (16 + 10 s) + N (9 s) */
+  int32_t precision;       /* precision of the sampled launches (SFEM_FP64 / SFEM_FP32) */
+  int32_t reserved;
+} sfem_profile;
+/* enable != 0 resets the counters and samples one Hessian-vector product per poll interval
+ * of every Krylov solve, timed with CUDA events on the handle's stream. */
+int sfem_set_profiling(sfem_handle* h, int32_t enable);
+int sfem_get_profile(const sfem_handle* h, sfem_profile* out);
+/* Total number of kernels this library has launched in the process. */
+int sfem_kernel_launches(int64_t* count);
+
+/* ---- device-pointer variants (stream-ordered on the handle's stream) ---- */
+int sfem_compute_gradients_dev(sfem_handle* h, double* r_dev);
+int sfem_matvec_dev(sfem_handle* h, const double* d_dev, double* Kd_dev);
+int sfem_get_free_positions_dev(sfem_handle* h, double* pos_dev);
+int sfem_set_free_positions_dev(sfem_handle* h, const double* pos_dev);
+int sfem_set_element_youngs_dev(sfem_handle* h, const double* young_e_dev);
+int sfem_set_nodal_loads_free_dev(sfem_handle* h, const double* f_free_dev);
+int sfem_adjoint_dev(sfem_handle* h, const double* dLdu_dev, double rel_tol, int32_t max_cg,
+                     double* dLdE_dev, double* dLdf_dev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFEM_H */

@@ -1,0 +1,152 @@
+"""ctypes binding of the C ABI in include/sfem.h (libsfem_gb300.so).
+
+The library is the only compute path: if it cannot be built or loaded this
+module raises, there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+SFEM_OK = 0
+SFEM_NOT_CONVERGED = 1
+SFEM_LINESEARCH_FAILED = 2
+SFEM_ERR_INVALID = -1
+SFEM_ERR_CUDA = -2
+SFEM_ERR_NAN = -3
+SFEM_ERR_INVERTED = -4
+SFEM_ERR_OOM = -5
+SFEM_ERR_BREAKDOWN = -6
+SFEM_ERR_NO_DEVICE = -7
+
+MMT_LINEAR, MMT_STVK, MMT_COROTATIONAL, MMT_NEO_HOOKEAN = 0, 1, 2, 3
+FP64, FP32 = 0, 1
+PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
+LSC_ARMIJO, LSC_ENGINEERING, LSC_RESIDUAL = 0, 1, 2
+TANGENT_REFERENCE, TANGENT_EXACT = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_vp = C.c_void_p
+
+
+class Config(C.Structure):
+    _fields_ = [("young", C.c_double), ("poisson", C.c_double), ("density", C.c_double),
+                ("gravity", C.c_double * 3), ("material", C.c_int32), ("precision", C.c_int32),
+                ("device", C.c_int32), ("tangent", C.c_int32)]
+
+
+class PcgOpts(C.Structure):
+    _fields_ = [("rel_tol", C.c_double), ("max_iters", C.c_int32), ("precond", C.c_int32),
+                ("check_every", C.c_int32), ("reserved", C.c_int32)]
+
+
+class PcgStats(C.Structure):
+    _fields_ = [("iters", C.c_int32), ("status", C.c_int32), ("rel_res", C.c_double)]
+
+
+class NewtonOpts(C.Structure):
+    _fields_ = [("rel_tol", C.c_double), ("abs_tol", C.c_double), ("max_newton", C.c_int32),
+                ("max_cg", C.c_int32), ("eta_max", C.c_double), ("eta_min", C.c_double),
+                ("precond", C.c_int32), ("ls_condition", C.c_int32), ("max_bisection", C.c_int32),
+                ("verbose", C.c_int32), ("load_steps", C.c_int32), ("reserved", C.c_int32)]
+
+
+class NewtonStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int32), ("cg_iters", C.c_int32), ("status", C.c_int32),
+                ("line_search_cuts", C.c_int32), ("r0", C.c_double), ("rel_res", C.c_double),
+                ("seconds", C.c_double)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("hvp_elem_ms", C.c_double), ("hvp_gather_ms", C.c_double), ("samples", C.c_int64),
+                ("hvp_launches", C.c_int64), ("algo_bytes_hvp", C.c_double), ("precision", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class SfemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"sfem error {code}: {msg}")
+        self.code = code
+
+
+# (name, argtypes) of every exported entry point; restype is int unless noted
+SIGNATURES = {
+    "sfem_create": [_dp, C.c_int64, _ip, C.c_int64, _ip, C.c_int64, C.POINTER(Config), C.POINTER(_vp)],
+    "sfem_destroy": [_vp],
+    "sfem_last_error": [],
+    "sfem_sizes": [_vp, _i64p, _i64p, _i64p],
+    "sfem_reshuffle_map": [_vp, _ip],
+    "sfem_get_stream": [_vp, C.POINTER(_vp)],
+    "sfem_set_stream": [_vp, _vp],
+    "sfem_get_positions": [_vp, _dp],
+    "sfem_set_positions": [_vp, _dp],
+    "sfem_get_free_positions": [_vp, _dp],
+    "sfem_set_free_positions": [_vp, _dp],
+    "sfem_set_lame_params": [_vp, C.c_double, C.c_double],
+    "sfem_set_force_fraction": [_vp, C.c_double],
+    "sfem_set_element_youngs": [_vp, _dp],
+    "sfem_set_nodal_loads": [_vp, _dp],
+    "sfem_compute_gradients": [_vp, _dp, _dp],
+    "sfem_matvec": [_vp, _dp, _dp],
+    "sfem_dot": [_vp, _dp, _dp, _dp],
+    "sfem_jacobi_diagonal": [_vp, _dp],
+    "sfem_energy": [_vp, _dp, _dp],
+    "sfem_count_inverted": [_vp, _i64p],
+    "sfem_element_stress": [_vp, _dp],
+    "sfem_force_param_grads": [_vp, _dp, _dp, _dp],
+    "sfem_pcg": [_vp, _dp, _dp, C.POINTER(PcgOpts), C.POINTER(PcgStats)],
+    "sfem_newton_solve": [_vp, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)],
+    "sfem_nonlinear_cg": [_vp, C.c_int32, C.c_int32, C.c_double, _ip],
+    "sfem_adjoint": [_vp, _dp, C.c_double, C.c_int32, _dp, _dp],
+    "sfem_set_profiling": [_vp, C.c_int32],
+    "sfem_get_profile": [_vp, C.POINTER(Profile)],
+    "sfem_kernel_launches": [_i64p],
+    "sfem_compute_gradients_dev": [_vp, _vp],
+    "sfem_matvec_dev": [_vp, _vp, _vp],
+    "sfem_get_free_positions_dev": [_vp, _vp],
+    "sfem_set_free_positions_dev": [_vp, _vp],
+    "sfem_set_element_youngs_dev": [_vp, _vp],
+    "sfem_set_nodal_loads_free_dev": [_vp, _vp],
+    "sfem_adjoint_dev": [_vp, _vp, C.c_double, C.c_int32, _vp, _vp],
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the CUDA library; raises if unavailable."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_missing:
+            try:
+                _build.build(verbose=False)
+            except Exception as e:  # noqa: BLE001 -- re-raised with context
+                if not os.path.exists(_build.LIB):
+                    raise ImportError(f"solidfem_gb300: CUDA library could not be built: {e}") from e
+        if not os.path.exists(_build.LIB):
+            raise ImportError(f"solidfem_gb300: {_build.LIB} missing; run `python -m solidfem_gb300.build`")
+        lib = C.CDLL(_build.LIB)
+        for name, args in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = C.c_char_p if name == "sfem_last_error" else C.c_int
+        _lib = lib
+        return lib
+
+
+def check(code: int, allow_positive: bool = True) -> int:
+    if code < 0 or (code > 0 and not allow_positive):
+        raise SfemError(code, load().sfem_last_error().decode())
+    return code

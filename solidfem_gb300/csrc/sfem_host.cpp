@@ -1,0 +1,1156 @@
+// Host side of the C ABI (include/sfem.h): problem set-up, device memory, and
+// the Krylov / Newton / nonlinear-CG drivers.  All arithmetic on problem data
+// runs in the CUDA kernels of sfem_kernels.cu; the host only sequences launches
+// and reads back a handful of scalars.
+//
+// Set-up mirrors FemPhysicsMatrixFree's constructor (Source/FemPhysicsMatrixFree.cpp:71-213):
+// orientation fix (FemBody::Prepare, Source/FemBody.cpp:127-156), fixed nodes
+// first (ReshuffleFixedNodes :229-263), Dm^-1 / signed volume / lumped masses
+// per element in FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sfem.h"
+#include "sfem_internal.h"
+
+using namespace sfem;
+
+namespace {
+
+// internal status of pcg_device: CG stopped on non-positive curvature (truncated CG)
+constexpr int SFEM_NEGATIVE_CURVATURE = 3;
+
+thread_local std::string g_err = "";
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CU(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) {                                                                    \
+      int code_ = (e_ == cudaErrorMemoryAllocation) ? SFEM_ERR_OOM : SFEM_ERR_CUDA;             \
+      return fail(code_, "%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_));       \
+    }                                                                                           \
+  } while (0)
+
+#define TRY(x)            \
+  do {                    \
+    int s_ = (x);         \
+    if (s_ < 0) return s_; \
+  } while (0)
+
+template <typename T>
+int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess)
+    return fail(e == cudaErrorMemoryAllocation ? SFEM_ERR_OOM : SFEM_ERR_CUDA, "cudaMalloc(%zu bytes): %s",
+                count * sizeof(T), cudaGetErrorString(e));
+  return 0;
+}
+
+template <typename T>
+struct KrylovWs {  // vectors of one precision, full length 3N (fixed-node entries stay 0)
+  T *b = nullptr, *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr, *u = nullptr;
+};
+
+}  // namespace
+
+struct sfem_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int64_t N = 0, E = 0, nbc = 0, nf = 0;
+  int material = SFEM_MMT_NEO_HOOKEAN;
+  int precision = SFEM_FP64;
+  int tangent = SFEM_TANGENT_REFERENCE;
+  double young = 0, poisson = 0, mu = 0, lambda = 0, density = 0, grav[3] = {0, 0, 0}, ff = 1.0;
+  std::vector<int32_t> map;  // original -> reshuffled
+  bool has_scale = false;
+
+  // element data
+  int4* tets = nullptr;
+  double *X64 = nullptr, *vol64 = nullptr, *scale64 = nullptr, *young_e = nullptr;
+  float *X32 = nullptr, *vol32 = nullptr, *scale32 = nullptr;
+  // node data (reshuffled, 3N)
+  double *x0 = nullptr, *u = nullptr, *mass = nullptr, *fext = nullptr, *grav_d = nullptr;
+  int64_t *csr_ptr = nullptr, *csr_ent = nullptr;
+  // scratch
+  double* fe = nullptr;  // 12 E doubles (float passes use it as 12 E floats)
+  double* partials = nullptr;
+  unsigned* counter = nullptr;
+  CgScalars* scal = nullptr;
+  CgScalars* scal_h = nullptr;  // pinned mirror
+  double* dres = nullptr;       // small device result slots
+  double* dres_h = nullptr;     // pinned mirror
+  int* ninv = nullptr;
+  // Newton / misc work vectors (FP64, 3N)
+  double *r64 = nullptr, *ubase = nullptr, *tmp64 = nullptr, *tmp64b = nullptr;
+  KrylovWs<double> k64;
+  KrylovWs<float> k32;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // profiling of the element Hessian-vector kernel inside Krylov solves
+  bool profiling = false;
+  cudaEvent_t pev[3] = {nullptr, nullptr, nullptr};
+  double prof_elem_ms = 0, prof_gather_ms = 0;
+  int64_t prof_samples = 0, prof_launches = 0;
+  int prof_precision = 0;
+
+  Reduce red() const { return Reduce{partials, counter}; }
+  NodeCsr csr() const { return NodeCsr{csr_ptr, csr_ent}; }
+  ElemView<double> ev64() const {
+    return ElemView<double>{tets, X64, vol64, has_scale ? scale64 : nullptr, E, mu, lambda};
+  }
+  ElemView<float> ev32() const {
+    return ElemView<float>{tets, X32, vol32, has_scale ? scale32 : nullptr, E, (float)mu, (float)lambda};
+  }
+};
+
+namespace {
+
+template <typename T>
+int alloc_ws(sfem_handle* h, KrylovWs<T>& w) {
+  if (w.b) return 0;
+  size_t n = 3 * (size_t)h->N;
+  T** ptrs[] = {&w.b, &w.x, &w.r, &w.p, &w.q, &w.dinv, &w.u};
+  for (T** p : ptrs) {
+    TRY(dalloc(p, n));
+    CU(cudaMemsetAsync(*p, 0, n * sizeof(T), h->stream));
+  }
+  return 0;
+}
+
+template <typename T>
+ElemView<T> ev_of(const sfem_handle* h);
+template <>
+ElemView<double> ev_of<double>(const sfem_handle* h) { return h->ev64(); }
+template <>
+ElemView<float> ev_of<float>(const sfem_handle* h) { return h->ev32(); }
+
+template <typename T>
+KrylovWs<T>& ws_of(sfem_handle* h);
+template <>
+KrylovWs<double>& ws_of<double>(sfem_handle* h) { return h->k64; }
+template <>
+KrylovWs<float>& ws_of<float>(sfem_handle* h) { return h->k32; }
+
+template <typename T>
+void element_pass(sfem_handle* h, int mode, const T* u, const T* p, T* fe, double* result, int* ninv,
+                  const CgScalars* s) {
+  const ElemView<T> ev = ev_of<T>(h);
+  const int mat = (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) ? 4 : h->material;
+  switch (mat) {
+    case 0: launch_element<T, 0>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
+    case 1: launch_element<T, 1>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
+    case 2: launch_element<T, 2>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
+    case 3: launch_element<T, 3>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
+    default: launch_element<T, 4>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
+  }
+}
+
+// displacement in precision T for the element passes
+template <typename T>
+const T* disp(sfem_handle* h);
+template <>
+const double* disp<double>(sfem_handle* h) { return h->u; }
+template <>
+const float* disp<float>(sfem_handle* h) {
+  launch_convert<double, float>(3 * h->N, h->u, h->k32.u, h->stream);
+  return h->k32.u;
+}
+
+int sync(sfem_handle* h) {
+  CU(cudaStreamSynchronize(h->stream));
+  CU(cudaGetLastError());
+  return 0;
+}
+
+// FP64 residual r64 = f_int + m g ff + f_ext ff; returns |r| and the number of inverted elements.
+int residual(sfem_handle* h, double* rnorm, int* n_inverted) {
+  CU(cudaMemsetAsync(h->ninv, 0, sizeof(int), h->stream));
+  element_pass<double>(h, MODE_FORCE, h->u, nullptr, h->fe, nullptr, h->ninv, nullptr);
+  launch_gather_force(h->nbc, h->N, h->csr(), h->fe, h->mass, h->fext, h->grav, h->ff, h->r64, h->red(),
+                      h->dres, h->stream);
+  CU(cudaMemcpyAsync(h->dres_h, h->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  int ninv_h = 0;
+  CU(cudaMemcpyAsync(&ninv_h, h->ninv, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  if (rnorm) *rnorm = std::sqrt(h->dres_h[0]);
+  if (n_inverted) *n_inverted = ninv_h;
+  return 0;
+}
+
+// Jacobi diagonal (inverse) of the tangent at the current state, precision T
+template <typename T>
+int jacobi(sfem_handle* h, T* dinv, T* diag) {
+  const T* u = disp<T>(h);
+  T* fe = reinterpret_cast<T*>(h->fe);
+  element_pass<T>(h, MODE_DIAG, u, nullptr, fe, nullptr, nullptr, nullptr);
+  launch_gather_diag<T>(h->nbc, h->N, h->csr(), fe, dinv, diag, h->stream);
+  CU(cudaGetLastError());
+  return 0;
+}
+
+// Preconditioned CG on K x = b (device vectors of the workspace, full length).
+// The displacement used by the HVP must already be in ws.u (FP32) / h->u (FP64).
+template <typename T>
+int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, double tol, int max_it,
+               int check_every, sfem_pcg_stats* st) {
+  KrylovWs<T>& w = ws_of<T>(h);
+  const int64_t o = 3 * h->nbc, n = 3 * h->nf;
+  T* fe = reinterpret_cast<T*>(h->fe);
+  CgScalars s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.tol2 = tol * tol;
+  s0.max_it = max_it;
+  *h->scal_h = s0;
+  CU(cudaMemcpyAsync(h->scal, h->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
+  launch_cg_init<T>(n, b + o, x + o, w.r + o, w.p + o, dinv ? dinv + o : nullptr, h->red(), h->scal, h->stream);
+  if (check_every <= 0) check_every = 32;
+  int it = 0;
+  bool pending = false;
+  if (h->profiling) h->prof_precision = sizeof(T) == 4 ? SFEM_FP32 : SFEM_FP64;
+  for (;;) {
+    CU(cudaMemcpyAsync(h->scal_h, h->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    if (h->scal_h->done || it >= max_it) break;
+    if (pending) {  // events of the previous chunk's sampled iteration have completed
+      float a = 0, b = 0;
+      cudaEventElapsedTime(&a, h->pev[0], h->pev[1]);
+      cudaEventElapsedTime(&b, h->pev[1], h->pev[2]);
+      h->prof_elem_ms += a;
+      h->prof_gather_ms += b;
+      h->prof_samples++;
+      pending = false;
+    }
+    for (int k = 0; k < check_every && it < max_it; k++, it++) {
+      const bool sample = h->profiling && k == 0;
+      if (sample) CU(cudaEventRecord(h->pev[0], h->stream));
+      element_pass<T>(h, MODE_HVP, u, w.p, fe, nullptr, nullptr, h->scal);
+      if (sample) CU(cudaEventRecord(h->pev[1], h->stream));
+      launch_gather_hvp<T>(h->nbc, h->N, h->csr(), fe, w.p, w.q, h->red(), h->scal, h->stream);
+      if (sample) {
+        CU(cudaEventRecord(h->pev[2], h->stream));
+        pending = true;
+      }
+      if (h->profiling) h->prof_launches++;
+      launch_cg_update<T>(n, x + o, w.r + o, w.p + o, w.q + o, dinv ? dinv + o : nullptr, h->red(), h->scal,
+                          h->stream);
+      launch_cg_direction<T>(n, w.r + o, dinv ? dinv + o : nullptr, w.p + o, h->scal, h->stream);
+    }
+  }
+  if (pending) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, h->pev[0], h->pev[1]);
+    cudaEventElapsedTime(&b, h->pev[1], h->pev[2]);
+    h->prof_elem_ms += a;
+    h->prof_gather_ms += b;
+    h->prof_samples++;
+  }
+  const CgScalars& s = *h->scal_h;
+  if (st) {
+    st->iters = s.it;
+    st->status = s.status;
+    st->rel_res = s.bb > 0 ? std::sqrt(s.rr / s.bb) : 0.0;
+  }
+  if (s.status == -3) return fail(SFEM_ERR_NAN, "non-finite value in the Krylov recurrence");
+  if (s.status == 2) {
+    // Negative curvature (truncated CG, as in Newton-CG for minimisation): keep the iterate
+    // reached so far; at the first iteration return the preconditioned residual direction.
+    if (s.it == 0) CU(cudaMemcpyAsync(x + o, w.p + o, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
+    fail(SFEM_ERR_BREAKDOWN, "non-positive curvature p.Ap = %g in CG at iteration %d", s.pq, s.it);
+    return SFEM_NEGATIVE_CURVATURE;
+  }
+  return s.status == 1 ? SFEM_NOT_CONVERGED : SFEM_OK;
+}
+
+int check_handle(const sfem_handle* h) {
+  if (!h) return fail(SFEM_ERR_INVALID, "null handle");
+  return 0;
+}
+
+int set_device(const sfem_handle* h) {
+  CU(cudaSetDevice(h->device));
+  return 0;
+}
+
+// host original-order N x 3 -> device reshuffled 3N
+int upload_nodes(sfem_handle* h, const double* src, double* dst) {
+  std::vector<double> tmp(3 * (size_t)h->N);
+  for (int64_t i = 0; i < h->N; i++)
+    for (int c = 0; c < 3; c++) tmp[3 * (size_t)h->map[i] + c] = src[3 * (size_t)i + c];
+  CU(cudaMemcpyAsync(dst, tmp.data(), tmp.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+const char* sfem_last_error(void) { return g_err.c_str(); }
+
+int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, int64_t n_tets, const int32_t* fixed,
+                int64_t n_fixed, const sfem_config* cfg, sfem_handle** out) {
+  if (!out) return fail(SFEM_ERR_INVALID, "out is null");
+  *out = nullptr;
+  if (!nodes || !tets_in || !cfg || n_nodes <= 0 || n_tets <= 0 || (n_fixed > 0 && !fixed))
+    return fail(SFEM_ERR_INVALID, "invalid arguments to sfem_create");
+  if (n_nodes >= (1ll << 31) || n_tets >= (1ll << 29)) return fail(SFEM_ERR_INVALID, "mesh too large");
+  if (cfg->material < 0 || cfg->material > 3) return fail(SFEM_ERR_INVALID, "unsupported material %d", cfg->material);
+  if (cfg->precision != SFEM_FP64 && cfg->precision != SFEM_FP32)
+    return fail(SFEM_ERR_INVALID, "unsupported precision %d", cfg->precision);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SFEM_ERR_NO_DEVICE, "no CUDA device");
+  for (int64_t i = 0; i < 4 * n_tets; i++)
+    if (tets_in[i] < 0 || tets_in[i] >= n_nodes) return fail(SFEM_ERR_INVALID, "tet index out of range at %lld", (long long)i);
+  for (int64_t i = 0; i < n_fixed; i++)
+    if (fixed[i] < 0 || fixed[i] >= n_nodes) return fail(SFEM_ERR_INVALID, "fixed index out of range");
+
+  sfem_handle* h = new sfem_handle();
+  h->device = cfg->device;
+  h->N = n_nodes;
+  h->E = n_tets;
+  h->material = cfg->material;
+  h->precision = cfg->precision;
+  h->tangent = cfg->tangent;
+  h->young = cfg->young;
+  h->poisson = cfg->poisson;
+  h->density = cfg->density;
+  for (int c = 0; c < 3; c++) h->grav[c] = cfg->gravity[c];
+  // Lame parameters, Source/FemPhysicsBase.cpp:38-39
+  h->lambda = cfg->young * cfg->poisson / (1.0 + cfg->poisson) / (1.0 - 2.0 * cfg->poisson);
+  h->mu = 0.5 * cfg->young / (1.0 + cfg->poisson);
+
+  auto bail = [&](int code) {
+    sfem_destroy(h);
+    return code;
+  };
+  if (cudaSetDevice(h->device) != cudaSuccess) return bail(fail(SFEM_ERR_NO_DEVICE, "cannot select device %d", h->device));
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(SFEM_ERR_CUDA, "stream creation failed"));
+  h->own_stream = true;
+
+  // ---- reshuffle: fixed nodes first ----
+  std::vector<char> isfix(n_nodes, 0);
+  for (int64_t i = 0; i < n_fixed; i++) isfix[fixed[i]] = 1;
+  h->map.resize(n_nodes);
+  int64_t k = 0;
+  for (int64_t i = 0; i < n_nodes; i++)
+    if (isfix[i]) h->map[i] = (int32_t)k++;
+  h->nbc = k;
+  for (int64_t i = 0; i < n_nodes; i++)
+    if (!isfix[i]) h->map[i] = (int32_t)k++;
+  h->nf = h->N - h->nbc;
+  if (h->nf <= 0) return bail(fail(SFEM_ERR_INVALID, "all nodes are fixed"));
+
+  std::vector<double> x0(3 * (size_t)n_nodes);
+  for (int64_t i = 0; i < n_nodes; i++)
+    for (int c = 0; c < 3; c++) x0[3 * (size_t)h->map[i] + c] = nodes[3 * (size_t)i + c];
+
+  // ---- element precompute (FP64) ----
+  const size_t E = (size_t)n_tets;
+  std::vector<int4> tt(E);
+  std::vector<double> X(9 * E), vol(E), mass(n_nodes, 0.0);
+  for (size_t e = 0; e < E; e++) {
+    int32_t t[4] = {tets_in[4 * e], tets_in[4 * e + 1], tets_in[4 * e + 2], tets_in[4 * e + 3]};
+    for (int j = 0; j < 4; j++) t[j] = h->map[t[j]];
+    double D[9];
+    for (int pass = 0; pass < 2; pass++) {
+      const double* a0 = &x0[3 * (size_t)t[0]];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) D[3 * i + j] = x0[3 * (size_t)t[j + 1] + i] - a0[i];
+      double det = D[0] * (D[4] * D[8] - D[5] * D[7]) + D[1] * (D[5] * D[6] - D[3] * D[8]) +
+                   D[2] * (D[3] * D[7] - D[4] * D[6]);
+      if (pass == 0 && det < 0) {
+        std::swap(t[0], t[1]);  // FemBody::Prepare: make the volume positive
+        continue;
+      }
+      if (det == 0) return bail(fail(SFEM_ERR_INVALID, "degenerate element %zu", e));
+      double inv[9];
+      inv[0] = D[4] * D[8] - D[5] * D[7];
+      inv[3] = D[5] * D[6] - D[3] * D[8];
+      inv[6] = D[3] * D[7] - D[4] * D[6];
+      inv[1] = D[2] * D[7] - D[1] * D[8];
+      inv[4] = D[0] * D[8] - D[2] * D[6];
+      inv[7] = D[1] * D[6] - D[0] * D[7];
+      inv[2] = D[1] * D[5] - D[2] * D[4];
+      inv[5] = D[2] * D[3] - D[0] * D[5];
+      inv[8] = D[0] * D[4] - D[1] * D[3];
+      for (int q = 0; q < 9; q++) X[q * E + e] = inv[q] / det;
+      vol[e] = det / 6.0;
+      break;
+    }
+    tt[e] = make_int4(t[0], t[1], t[2], t[3]);
+    double lm = 0.25 * vol[e] * h->density;
+    for (int j = 0; j < 4; j++) mass[t[j]] += lm;
+  }
+  // lumped masses as the reference stores them (mass = 1 / (1 / m)), fixed nodes 0
+  for (int64_t i = 0; i < n_nodes; i++) mass[i] = (i < h->nbc || mass[i] == 0) ? 0.0 : 1.0 / (1.0 / mass[i]);
+
+  // ---- node -> element CSR (entries in element order) ----
+  std::vector<int64_t> ptr(n_nodes + 1, 0), ent(4 * E);
+  for (size_t e = 0; e < E; e++) {
+    ptr[tt[e].x + 1]++; ptr[tt[e].y + 1]++; ptr[tt[e].z + 1]++; ptr[tt[e].w + 1]++;
+  }
+  for (int64_t i = 0; i < n_nodes; i++) ptr[i + 1] += ptr[i];
+  {
+    std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+    for (size_t e = 0; e < E; e++) {
+      const int32_t t[4] = {tt[e].x, tt[e].y, tt[e].z, tt[e].w};
+      for (int j = 0; j < 4; j++) ent[fill[t[j]]++] = ((int64_t)e << 2) | j;
+    }
+  }
+
+  // ---- device buffers ----
+  const size_t N3 = 3 * (size_t)n_nodes;
+  int st = 0;
+  if ((st = dalloc(&h->tets, E)) || (st = dalloc(&h->X64, 9 * E)) || (st = dalloc(&h->vol64, E)) ||
+      (st = dalloc(&h->X32, 9 * E)) || (st = dalloc(&h->vol32, E)) || (st = dalloc(&h->x0, N3)) ||
+      (st = dalloc(&h->u, N3)) || (st = dalloc(&h->mass, (size_t)n_nodes)) || (st = dalloc(&h->fext, N3)) ||
+      (st = dalloc(&h->grav_d, 3)) || (st = dalloc(&h->csr_ptr, (size_t)n_nodes + 1)) ||
+      (st = dalloc(&h->csr_ent, 4 * E)) || (st = dalloc(&h->fe, 12 * E)) ||
+      (st = dalloc(&h->partials, 4 * (size_t)kMaxBlocks)) || (st = dalloc(&h->counter, 1)) ||
+      (st = dalloc(&h->scal, 1)) || (st = dalloc(&h->dres, 8)) || (st = dalloc(&h->ninv, 1)) ||
+      (st = dalloc(&h->r64, N3)) || (st = dalloc(&h->ubase, N3)) || (st = dalloc(&h->tmp64, N3)) ||
+      (st = dalloc(&h->tmp64b, N3)))
+    return bail(st);
+  if (cudaMallocHost((void**)&h->scal_h, sizeof(CgScalars)) != cudaSuccess ||
+      cudaMallocHost((void**)&h->dres_h, 8 * sizeof(double)) != cudaSuccess)
+    return bail(fail(SFEM_ERR_OOM, "pinned allocation failed"));
+  std::vector<float> X32(9 * E), vol32(E);
+  for (size_t i = 0; i < 9 * E; i++) X32[i] = (float)X[i];
+  for (size_t i = 0; i < E; i++) vol32[i] = (float)vol[i];
+  cudaStream_t s = h->stream;
+#define UP(dst, src, bytes)                                                                \
+  if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)          \
+    return bail(fail(SFEM_ERR_CUDA, "upload failed: %s", cudaGetErrorString(cudaGetLastError())));
+  UP(h->tets, tt.data(), E * sizeof(int4));
+  UP(h->X64, X.data(), 9 * E * sizeof(double));
+  UP(h->vol64, vol.data(), E * sizeof(double));
+  UP(h->X32, X32.data(), 9 * E * sizeof(float));
+  UP(h->vol32, vol32.data(), E * sizeof(float));
+  UP(h->x0, x0.data(), N3 * sizeof(double));
+  UP(h->mass, mass.data(), (size_t)n_nodes * sizeof(double));
+  UP(h->grav_d, h->grav, 3 * sizeof(double));
+  UP(h->csr_ptr, ptr.data(), ptr.size() * sizeof(int64_t));
+  UP(h->csr_ent, ent.data(), ent.size() * sizeof(int64_t));
+#undef UP
+  double* zero_bufs[] = {h->u, h->fext, h->r64, h->ubase, h->tmp64, h->tmp64b};
+  for (double* z : zero_bufs)
+    if (cudaMemsetAsync(z, 0, N3 * sizeof(double), s) != cudaSuccess) return bail(fail(SFEM_ERR_CUDA, "memset failed"));
+  if (cudaMemsetAsync(h->counter, 0, sizeof(unsigned), s) != cudaSuccess) return bail(fail(SFEM_ERR_CUDA, "memset failed"));
+  if (alloc_ws(h, h->k64) < 0) return bail(SFEM_ERR_OOM);
+  if (h->precision == SFEM_FP32 && alloc_ws(h, h->k32) < 0) return bail(SFEM_ERR_OOM);
+  if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+    return bail(fail(SFEM_ERR_CUDA, "event creation failed"));
+  if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(SFEM_ERR_CUDA, "set-up failed: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = h;
+  return SFEM_OK;
+}
+
+int sfem_destroy(sfem_handle* h) {
+  if (!h) return SFEM_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void* bufs[] = {h->tets, h->X64, h->vol64, h->scale64, h->young_e, h->X32, h->vol32, h->scale32, h->x0, h->u,
+                  h->mass, h->fext, h->grav_d, h->csr_ptr, h->csr_ent, h->fe, h->partials, h->counter, h->scal,
+                  h->dres, h->ninv, h->r64, h->ubase, h->tmp64, h->tmp64b, h->k64.b, h->k64.x, h->k64.r, h->k64.p,
+                  h->k64.q, h->k64.dinv, h->k64.u, h->k32.b, h->k32.x, h->k32.r, h->k32.p, h->k32.q, h->k32.dinv,
+                  h->k32.u};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (h->scal_h) cudaFreeHost(h->scal_h);
+  if (h->dres_h) cudaFreeHost(h->dres_h);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  for (cudaEvent_t e : h->pev)
+    if (e) cudaEventDestroy(e);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return SFEM_OK;
+}
+
+int sfem_set_profiling(sfem_handle* h, int32_t enable) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (enable && !h->pev[0])
+    for (cudaEvent_t& e : h->pev) CU(cudaEventCreate(&e));
+  h->profiling = enable != 0;
+  h->prof_elem_ms = h->prof_gather_ms = 0;
+  h->prof_samples = h->prof_launches = 0;
+  return SFEM_OK;
+}
+
+int sfem_get_profile(const sfem_handle* h, sfem_profile* out) {
+  TRY(check_handle(h));
+  if (!out) return fail(SFEM_ERR_INVALID, "out is null");
+  out->hvp_elem_ms = h->prof_elem_ms;
+  out->hvp_gather_ms = h->prof_gather_ms;
+  out->samples = h->prof_samples;
+  out->hvp_launches = h->prof_launches;
+  const double sz = h->prof_precision == SFEM_FP32 ? 4.0 : 8.0;
+  out->algo_bytes_hvp = (double)h->E * (16.0 + 10.0 * sz) + (double)h->N * 9.0 * sz;
+  out->precision = h->prof_precision;
+  out->reserved = 0;
+  return SFEM_OK;
+}
+
+int sfem_kernel_launches(int64_t* count) {
+  if (!count) return fail(SFEM_ERR_INVALID, "count is null");
+  *count = (int64_t)sfem::launch_count();
+  return SFEM_OK;
+}
+
+int sfem_sizes(const sfem_handle* h, int64_t* n_nodes, int64_t* n_free, int64_t* n_tets) {
+  TRY(check_handle(h));
+  if (n_nodes) *n_nodes = h->N;
+  if (n_free) *n_free = h->nf;
+  if (n_tets) *n_tets = h->E;
+  return SFEM_OK;
+}
+
+int sfem_reshuffle_map(const sfem_handle* h, int32_t* map) {
+  TRY(check_handle(h));
+  if (!map) return fail(SFEM_ERR_INVALID, "map is null");
+  memcpy(map, h->map.data(), h->map.size() * sizeof(int32_t));
+  return SFEM_OK;
+}
+
+int sfem_get_stream(const sfem_handle* h, void** stream) {
+  TRY(check_handle(h));
+  *stream = (void*)h->stream;
+  return SFEM_OK;
+}
+
+int sfem_set_stream(sfem_handle* h, void* stream) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  CU(cudaStreamSynchronize(h->stream));
+  if (h->own_stream) CU(cudaStreamDestroy(h->stream));
+  h->own_stream = false;
+  h->stream = (cudaStream_t)stream;
+  return SFEM_OK;
+}
+
+int sfem_get_positions(sfem_handle* h, double* pos) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  const size_t N3 = 3 * (size_t)h->N;
+  std::vector<double> x0(N3), u(N3);
+  CU(cudaMemcpyAsync(x0.data(), h->x0, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(u.data(), h->u, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  for (int64_t i = 0; i < h->N; i++)
+    for (int c = 0; c < 3; c++) {
+      size_t g = 3 * (size_t)h->map[i] + c;
+      pos[3 * (size_t)i + c] = x0[g] + u[g];
+    }
+  return SFEM_OK;
+}
+
+int sfem_set_positions(sfem_handle* h, const double* pos) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  const size_t N3 = 3 * (size_t)h->N;
+  std::vector<double> x0(N3), u(N3);
+  CU(cudaMemcpyAsync(x0.data(), h->x0, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  for (int64_t i = 0; i < h->N; i++)
+    for (int c = 0; c < 3; c++) {
+      size_t g = 3 * (size_t)h->map[i] + c;
+      u[g] = pos[3 * (size_t)i + c] - x0[g];
+    }
+  CU(cudaMemcpyAsync(h->u, u.data(), N3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+int sfem_get_free_positions(sfem_handle* h, double* pos_free) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  TRY(sfem_get_free_positions_dev(h, h->tmp64));
+  CU(cudaMemcpyAsync(pos_free, h->tmp64, 3 * (size_t)h->nf * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int sfem_set_free_positions(sfem_handle* h, const double* pos_free) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  CU(cudaMemcpyAsync(h->tmp64b, pos_free, 3 * (size_t)h->nf * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TRY(sfem_set_free_positions_dev(h, h->tmp64b));
+  return sync(h);
+}
+
+int sfem_get_free_positions_dev(sfem_handle* h, double* pos_dev) {
+  TRY(check_handle(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  // pos = x0 + u over the free block
+  launch_axpy_state<double>((int64_t)n, 1.0, h->u + o, h->x0 + o, pos_dev, h->stream);
+  CU(cudaGetLastError());
+  return SFEM_OK;
+}
+
+int sfem_set_free_positions_dev(sfem_handle* h, const double* pos_dev) {
+  TRY(check_handle(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  // u = pos - x0 over the free block
+  launch_axpy_state<double>((int64_t)n, -1.0, h->x0 + o, pos_dev, h->u + o, h->stream);
+  CU(cudaGetLastError());
+  return SFEM_OK;
+}
+
+int sfem_set_lame_params(sfem_handle* h, double mu, double lambda) {
+  TRY(check_handle(h));
+  h->mu = mu;
+  h->lambda = lambda;
+  // SetLameParams, Include/FemPhysicsBase.h:106-114
+  h->young = mu * (3 * lambda + 2 * mu) / (mu + lambda);
+  h->poisson = 0.5 * lambda / (mu + lambda);
+  return SFEM_OK;
+}
+
+int sfem_set_force_fraction(sfem_handle* h, double f) {
+  TRY(check_handle(h));
+  h->ff = f;
+  return SFEM_OK;
+}
+
+int sfem_set_element_youngs(sfem_handle* h, const double* young_e) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!young_e) {
+    h->has_scale = false;
+    return SFEM_OK;
+  }
+  if (!h->young_e) {
+    TRY(dalloc(&h->young_e, (size_t)h->E));
+    TRY(dalloc(&h->scale64, (size_t)h->E));
+    TRY(dalloc(&h->scale32, (size_t)h->E));
+  }
+  CU(cudaMemcpyAsync(h->young_e, young_e, (size_t)h->E * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TRY(sfem_set_element_youngs_dev(h, h->young_e));
+  return sync(h);
+}
+
+int sfem_set_element_youngs_dev(sfem_handle* h, const double* young_e_dev) {
+  TRY(check_handle(h));
+  if (!h->young_e) {
+    TRY(dalloc(&h->young_e, (size_t)h->E));
+    TRY(dalloc(&h->scale64, (size_t)h->E));
+    TRY(dalloc(&h->scale32, (size_t)h->E));
+  }
+  if (young_e_dev != h->young_e)
+    CU(cudaMemcpyAsync(h->young_e, young_e_dev, (size_t)h->E * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  launch_scale_copy(h->E, 1.0 / h->young, h->young_e, h->scale64, h->stream);
+  launch_convert<double, float>(h->E, h->scale64, h->scale32, h->stream);
+  h->has_scale = true;
+  CU(cudaGetLastError());
+  return SFEM_OK;
+}
+
+int sfem_set_nodal_loads(sfem_handle* h, const double* f) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!f) {
+    CU(cudaMemsetAsync(h->fext, 0, 3 * (size_t)h->N * sizeof(double), h->stream));
+    return sync(h);
+  }
+  return upload_nodes(h, f, h->fext);
+}
+
+int sfem_set_nodal_loads_free_dev(sfem_handle* h, const double* f_free_dev) {
+  TRY(check_handle(h));
+  CU(cudaMemcpyAsync(h->fext + 3 * h->nbc, f_free_dev, 3 * (size_t)h->nf * sizeof(double), cudaMemcpyDeviceToDevice,
+                     h->stream));
+  return SFEM_OK;
+}
+
+int sfem_compute_gradients_dev(sfem_handle* h, double* r_dev) {
+  TRY(check_handle(h));
+  double rn;
+  TRY(residual(h, &rn, nullptr));
+  CU(cudaMemcpyAsync(r_dev, h->r64 + 3 * h->nbc, 3 * (size_t)h->nf * sizeof(double), cudaMemcpyDeviceToDevice,
+                     h->stream));
+  return SFEM_OK;
+}
+
+int sfem_compute_gradients(sfem_handle* h, double* r, double* norm) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  double rn;
+  TRY(residual(h, &rn, nullptr));
+  if (r)
+    CU(cudaMemcpyAsync(r, h->r64 + 3 * h->nbc, 3 * (size_t)h->nf * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  if (norm) *norm = rn;
+  return SFEM_OK;
+}
+
+int sfem_matvec_dev(sfem_handle* h, const double* d_dev, double* Kd_dev) {
+  TRY(check_handle(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  // direction with zero fixed-node block
+  CU(cudaMemsetAsync(h->tmp64, 0, o * sizeof(double), h->stream));
+  CU(cudaMemcpyAsync(h->tmp64 + o, d_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  element_pass<double>(h, MODE_HVP, h->u, h->tmp64, h->fe, nullptr, nullptr, nullptr);
+  launch_gather_hvp<double>(h->nbc, h->N, h->csr(), h->fe, h->tmp64, h->tmp64b, h->red(), nullptr, h->stream);
+  CU(cudaMemcpyAsync(Kd_dev, h->tmp64b + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CU(cudaGetLastError());
+  return SFEM_OK;
+}
+
+int sfem_matvec(sfem_handle* h, const double* d, double* Kd) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  double* dbuf = h->k64.b;  // scratch
+  CU(cudaMemcpyAsync(dbuf + o, d, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TRY(sfem_matvec_dev(h, dbuf + o, h->k64.x + o));
+  CU(cudaMemcpyAsync(Kd, h->k64.x + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int sfem_dot(sfem_handle* h, const double* a, const double* b, double* out) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  const size_t n = 3 * (size_t)h->nf;
+  CU(cudaMemcpyAsync(h->tmp64, a, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->tmp64b, b, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_dot((int64_t)n, h->tmp64, h->tmp64b, h->red(), h->dres, h->stream);
+  CU(cudaMemcpyAsync(h->dres_h, h->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  *out = h->dres_h[0];
+  return SFEM_OK;
+}
+
+int sfem_jacobi_diagonal(sfem_handle* h, double* diag) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  TRY(jacobi<double>(h, h->k64.dinv, h->tmp64));
+  CU(cudaMemcpyAsync(diag, h->tmp64 + 3 * h->nbc, 3 * (size_t)h->nf * sizeof(double), cudaMemcpyDeviceToHost,
+                     h->stream));
+  return sync(h);
+}
+
+int sfem_energy(sfem_handle* h, double* elastic, double* total) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  element_pass<double>(h, MODE_ENERGY, h->u, nullptr, h->fe, h->dres, nullptr, nullptr);
+  launch_potential(h->nbc, h->N, h->x0, h->u, h->mass, h->fext, h->grav, h->ff, h->red(), h->dres + 1, h->stream);
+  CU(cudaMemcpyAsync(h->dres_h, h->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  if (elastic) *elastic = h->dres_h[0];
+  if (total) *total = h->dres_h[0] + h->dres_h[1];
+  return SFEM_OK;
+}
+
+int sfem_count_inverted(sfem_handle* h, int64_t* count) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  int n = 0;
+  TRY(residual(h, nullptr, &n));
+  *count = n;
+  return SFEM_OK;
+}
+
+int sfem_element_stress(sfem_handle* h, double* P) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  element_pass<double>(h, MODE_STRESS, h->u, nullptr, h->fe, nullptr, nullptr, nullptr);
+  std::vector<double> tmp(12 * (size_t)h->E);
+  CU(cudaMemcpyAsync(tmp.data(), h->fe, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  for (int64_t e = 0; e < h->E; e++) memcpy(P + 9 * (size_t)e, &tmp[12 * (size_t)e], 9 * sizeof(double));
+  return SFEM_OK;
+}
+
+int sfem_force_param_grads(sfem_handle* h, double* gmu, double* glambda, double* grho) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  const int modes[3] = {MODE_PMU, MODE_PLAMBDA, MODE_NODALVOL};
+  double* outs[3] = {gmu, glambda, grho};
+  std::vector<double> nv(n);
+  for (int m = 0; m < 3; m++) {
+    element_pass<double>(h, modes[m], h->u, nullptr, h->fe, nullptr, nullptr, nullptr);
+    launch_gather_diag<double>(h->nbc, h->N, h->csr(), h->fe, nullptr, h->tmp64, h->stream);
+    CU(cudaMemcpyAsync(m < 2 ? outs[m] : nv.data(), h->tmp64 + o, n * sizeof(double), cudaMemcpyDeviceToHost,
+                       h->stream));
+    TRY(sync(h));
+  }
+  // d f / d rho = (nodal volume) * g: the nodal volume sits in every component slot 0 of the gather
+  for (size_t i = 0; i < (size_t)h->nf; i++)
+    for (int c = 0; c < 3; c++) grho[3 * i + c] = nv[3 * i] * h->grav[c];
+  return SFEM_OK;
+}
+
+int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* opts, sfem_pcg_stats* stats) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!b || !x || !opts) return fail(SFEM_ERR_INVALID, "null argument");
+  if (opts->precond == SFEM_PC_LEARNED) return fail(SFEM_ERR_INVALID, "learned preconditioner: use sfem_newton_solve");
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  const bool pc = opts->precond == SFEM_PC_JACOBI;
+  int st = 0;
+  if (h->precision == SFEM_FP64) {
+    KrylovWs<double>& w = h->k64;
+    CU(cudaMemcpyAsync(w.b + o, b, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (pc) TRY(jacobi<double>(h, w.dinv, nullptr));
+    st = pcg_device<double>(h, h->u, w.b, w.x, pc ? w.dinv : nullptr, opts->rel_tol, opts->max_iters,
+                            opts->check_every, stats);
+    if (st == SFEM_NEGATIVE_CURVATURE) return SFEM_ERR_BREAKDOWN;
+    if (st < 0) return st;
+    CU(cudaMemcpyAsync(x, w.x + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  } else {
+    KrylovWs<float>& w = h->k32;
+    CU(cudaMemcpyAsync(h->tmp64 + o, b, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_convert<double, float>((int64_t)n, h->tmp64 + o, w.b + o, h->stream);
+    const float* u32 = disp<float>(h);
+    if (pc) TRY(jacobi<float>(h, w.dinv, nullptr));
+    st = pcg_device<float>(h, u32, w.b, w.x, pc ? w.dinv : nullptr, opts->rel_tol, opts->max_iters,
+                           opts->check_every, stats);
+    if (st == SFEM_NEGATIVE_CURVATURE) return SFEM_ERR_BREAKDOWN;
+    if (st < 0) return st;
+    launch_convert<float, double>((int64_t)n, w.x + o, h->tmp64 + o, h->stream);
+    CU(cudaMemcpyAsync(x, h->tmp64 + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  }
+  TRY(sync(h));
+  return st;
+}
+
+}  // extern "C"
+
+// -----------------------------------------------------------------------------
+// Newton
+// -----------------------------------------------------------------------------
+namespace {
+
+// one inner solve K dx = r64 at the current state, in the handle's precision;
+// the step ends up in h->tmp64 (FP64, full length).
+int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  const bool pc = precond == SFEM_PC_JACOBI;
+  sfem_pcg_stats ps{};
+  int st;
+  if (h->precision == SFEM_FP64) {
+    KrylovWs<double>& w = h->k64;
+    if (pc) TRY(jacobi<double>(h, w.dinv, nullptr));
+    st = pcg_device<double>(h, h->u, h->r64, w.x, pc ? w.dinv : nullptr, eta, max_cg, 0, &ps);
+    if (st < 0) return st;
+    CU(cudaMemcpyAsync(h->tmp64 + o, w.x + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  } else {
+    KrylovWs<float>& w = h->k32;
+    const float* u32 = disp<float>(h);
+    launch_convert<double, float>((int64_t)n, h->r64 + o, w.b + o, h->stream);
+    if (pc) TRY(jacobi<float>(h, w.dinv, nullptr));
+    st = pcg_device<float>(h, u32, w.b, w.x, pc ? w.dinv : nullptr, eta, max_cg, 0, &ps);
+    if (st < 0) return st;
+    launch_convert<float, double>((int64_t)n, w.x + o, h->tmp64 + o, h->stream);
+  }
+  *its = ps.iters;
+  CU(cudaGetLastError());
+  return 0;
+}
+
+int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, double* rn_io, int* nit, int* cgit,
+                 int* cuts, int max_newton) {
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  double rn = *rn_io, rprev = rn, eta = op.eta_max;
+  const int max_bis = op.max_bisection > 0 ? op.max_bisection : 30;
+  for (int k = 0; k < max_newton; k++) {
+    if (rn <= op.rel_tol * r_ref || (op.abs_tol > 0 && rn <= op.abs_tol)) {
+      *rn_io = rn;
+      return SFEM_OK;
+    }
+    // Eisenstat-Walker forcing term (choice 2, gamma 0.9, exponent 2) with safeguards
+    if (k > 0) {
+      double e2 = 0.9 * (rn / rprev) * (rn / rprev);
+      double sg = 0.9 * eta * eta;
+      if (sg > 0.1 && sg > e2) e2 = sg;
+      eta = std::min(e2, op.eta_max);
+    }
+    eta = std::max(eta, 0.5 * op.rel_tol * r_ref / rn);
+    eta = std::max(eta, op.eta_min);
+    eta = std::min(eta, op.eta_max);
+    int its = 0;
+    TRY(inner_solve(h, eta, op.max_cg, op.precond, &its));
+    *cgit += its;
+    (*nit)++;
+    // backtracking line search on the FP64 residual
+    CU(cudaMemcpyAsync(h->ubase, h->u, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    double e_old = 0, slope = 0;
+    if (op.ls_condition == SFEM_LSC_ARMIJO) {
+      TRY(sfem_energy(h, nullptr, &e_old));
+      // slope = grad E . d = -r . d
+      launch_dot((int64_t)n, h->r64 + o, h->tmp64 + o, h->red(), h->dres + 2, h->stream);
+      CU(cudaMemcpyAsync(h->dres_h + 2, h->dres + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      TRY(sync(h));
+      slope = -h->dres_h[2];
+    }
+    double rd_old = 0;
+    if (op.ls_condition == SFEM_LSC_ENGINEERING) {
+      launch_dot((int64_t)n, h->r64 + o, h->tmp64 + o, h->red(), h->dres + 2, h->stream);
+      CU(cudaMemcpyAsync(h->dres_h + 2, h->dres + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      TRY(sync(h));
+      rd_old = -h->dres_h[2];  // Rold = -delta . rhs
+    }
+    double a = 1.0;
+    bool ok = false;
+    double rnew = rn;
+    if (op.ls_condition == SFEM_LSC_RESIDUAL) {
+      // residual-norm backtracking: halve until |r| decreases sufficiently and no element inverts
+      for (int ls = 0; ls <= max_bis; ls++) {
+        launch_axpy_state<double>((int64_t)n, a, h->tmp64 + o, h->ubase + o, h->u + o, h->stream);
+        int ninv = 0;
+        TRY(residual(h, &rnew, &ninv));
+        if (ninv == 0 && std::isfinite(rnew) && rnew <= (1 - 1e-4 * a) * rn) {
+          ok = true;
+          break;
+        }
+        (*cuts)++;
+        a *= 0.5;
+      }
+    } else {
+      // NewtonSolverBackTrack's bisection (Include/NewtonSolver.h:242-293)
+      double lo = 0.0, hi = 1.0;
+      int bis = 0;
+      for (;;) {
+        launch_axpy_state<double>((int64_t)n, a, h->tmp64 + o, h->ubase + o, h->u + o, h->stream);
+        int ninv = 0;
+        TRY(residual(h, &rnew, &ninv));
+        bool cond = false;
+        if (ninv == 0 && std::isfinite(rnew)) {
+          if (op.ls_condition == SFEM_LSC_ARMIJO) {
+            double e_el = 0, e_new = 0;
+            TRY(sfem_energy(h, &e_el, &e_new));
+            cond = e_new < e_old + 1e-4 * a * slope;  // Armijo, mAlpha = 1e-4
+            // near convergence the energy decrease falls below FP64 resolution of the energy:
+            // then a decrease of the residual norm decides
+            const double res = 1e-12 * (std::fabs(e_old) + std::fabs(e_el));
+            if (!cond && std::fabs(e_new - e_old) <= res && std::fabs(a * slope) <= res) cond = rnew < rn;
+          } else {
+            launch_dot((int64_t)n, h->r64 + o, h->tmp64 + o, h->red(), h->dres + 2, h->stream);
+            CU(cudaMemcpyAsync(h->dres_h + 2, h->dres + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            TRY(sync(h));
+            cond = -h->dres_h[2] < 0.5 * rd_old;  // Bonet-Wood as coded: Rnew < 0.5 Rold
+          }
+        }
+        if (!cond) {
+          hi = a;
+          bis++;
+          (*cuts)++;
+        } else if (bis > 10 || a == 1.0) {
+          ok = true;
+          break;
+        } else {
+          lo = a;
+          bis++;
+        }
+        a = 0.5 * (lo + hi);
+        if (a < 1e-10) break;
+      }
+    }
+    if (op.verbose)
+      fprintf(stderr, "[sfem] newton %d: |r| %.6e -> %.6e  cg %d  eta %.2e  step %.3g\n", *nit, rn, rnew, its, eta, a);
+    if (!ok) {
+      CU(cudaMemcpyAsync(h->u, h->ubase, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+      TRY(residual(h, &rn, nullptr));
+      *rn_io = rn;
+      return SFEM_LINESEARCH_FAILED;
+    }
+    rprev = rn;
+    rn = rnew;
+  }
+  *rn_io = rn;
+  return (rn <= op.rel_tol * r_ref || (op.abs_tol > 0 && rn <= op.abs_tol)) ? SFEM_OK : SFEM_NOT_CONVERGED;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfem_newton_solve(sfem_handle* h, const sfem_newton_opts* opts, sfem_newton_stats* stats) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!opts) return fail(SFEM_ERR_INVALID, "opts is null");
+  if (opts->precond == SFEM_PC_LEARNED) return fail(SFEM_ERR_INVALID, "learned preconditioner not loaded");
+  sfem_newton_opts op = *opts;
+  if (op.eta_max <= 0) op.eta_max = 0.5;
+  if (op.eta_min <= 0) op.eta_min = h->precision == SFEM_FP32 ? 1e-5 : 1e-10;
+  if (op.max_newton <= 0) op.max_newton = 50;
+  if (op.max_cg <= 0) op.max_cg = 100000;
+  if (h->precision == SFEM_FP32) TRY(alloc_ws(h, h->k32));
+  CU(cudaEventRecord(h->ev0, h->stream));
+  const double ff_final = h->ff;
+  int nit = 0, cgit = 0, cuts = 0, st = SFEM_OK;
+  double r0 = 0, rn = 0;
+  const int steps = op.load_steps > 1 ? op.load_steps : 1;
+  // |r(x_0)| of the full load defines the relative tolerance
+  TRY(residual(h, &r0, nullptr));
+  for (int s = 1; s <= steps; s++) {
+    h->ff = ff_final * (double)s / steps;
+    double r_ref = r0;
+    sfem_newton_opts so = op;
+    if (s < steps) {
+      // intermediate load steps of the quasi-static ramp need only a rough equilibrium
+      TRY(residual(h, &rn, nullptr));
+      r_ref = rn;
+      so.rel_tol = 1e-3;
+      so.abs_tol = 0;
+    } else if (steps > 1) {
+      TRY(residual(h, &rn, nullptr));
+    } else {
+      rn = r0;
+    }
+    st = newton_stage(h, so, r_ref, &rn, &nit, &cgit, &cuts, op.max_newton - nit);
+    if (st < 0 || st == SFEM_LINESEARCH_FAILED) break;
+  }
+  h->ff = ff_final;
+  CU(cudaEventRecord(h->ev1, h->stream));
+  TRY(sync(h));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  if (stats) {
+    stats->newton_iters = nit;
+    stats->cg_iters = cgit;
+    stats->status = st;
+    stats->line_search_cuts = cuts;
+    stats->r0 = r0;
+    stats->rel_res = r0 > 0 ? rn / r0 : 0;
+    stats->seconds = ms * 1e-3;
+  }
+  if (st < 0) return st;
+  if (!std::isfinite(rn)) return fail(SFEM_ERR_NAN, "residual is not finite");
+  return st;
+}
+
+// NonlinearConjugateGradientMinimizer::Solve, Include/NonlinearCG.h:51-114 (constants eps = tol = 1e-2f).
+int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, double abs_tol, int32_t* iters_done) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  const double eps2 = (double)(1e-2f * 1e-2f), tol2 = (double)(1e-2f * 1e-2f);
+  double* d = h->k64.p;  // search direction (full length, zero fixed block)
+  double* df = h->k64.q;
+  auto dot = [&](const double* a, const double* b, double* out) -> int {
+    launch_dot((int64_t)n, a + o, b + o, h->red(), h->dres + 3, h->stream);
+    CU(cudaMemcpyAsync(h->dres_h + 3, h->dres + 3, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    *out = h->dres_h[3];
+    return 0;
+  };
+  double rn;
+  TRY(residual(h, &rn, nullptr));
+  CU(cudaMemsetAsync(d, 0, 3 * (size_t)h->N * sizeof(double), h->stream));
+  CU(cudaMemcpyAsync(d + o, h->r64 + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  double delta;
+  TRY(dot(h->r64, h->r64, &delta));
+  const double delta0 = delta;
+  int iter = 0;
+  if (delta != 0) {
+    for (; iter < outer_iters; iter++) {
+      double deltaD;
+      TRY(dot(d, d, &deltaD));
+      for (int inner = 0; inner < inner_iters; inner++) {
+        element_pass<double>(h, MODE_HVP, h->u, d, h->fe, nullptr, nullptr, nullptr);
+        launch_gather_hvp<double>(h->nbc, h->N, h->csr(), h->fe, d, df, h->red(), nullptr, h->stream);
+        double rd, ddf;
+        TRY(dot(h->r64, d, &rd));
+        TRY(dot(d, df, &ddf));
+        const double alpha = rd / ddf;
+        launch_axpy_state<double>((int64_t)n, alpha, d + o, h->u + o, h->u + o, h->stream);
+        TRY(residual(h, &rn, nullptr));
+        if (alpha * alpha * deltaD < tol2) break;
+      }
+      double delta1;
+      TRY(dot(h->r64, h->r64, &delta1));
+      const double beta = delta1 / delta;
+      delta = delta1;
+      if (delta < abs_tol * abs_tol) { iter++; break; }
+      if (delta <= eps2 * delta0) { iter++; break; }
+      // d = r + beta d
+      launch_axpy_state<double>((int64_t)n, beta, d + o, h->r64 + o, d + o, h->stream);
+    }
+  }
+  if (iters_done) *iters_done = iter;
+  TRY(sync(h));
+  return std::isfinite(delta) ? SFEM_OK : fail(SFEM_ERR_NAN, "residual is not finite");
+}
+
+int sfem_adjoint_dev(sfem_handle* h, const double* dLdu_dev, double rel_tol, int32_t max_cg, double* dLdE_dev,
+                     double* dLdf_dev) {
+  TRY(check_handle(h));
+  if (h->material == SFEM_MMT_COROTATIONAL)
+    return fail(SFEM_ERR_INVALID, "adjoint needs a symmetric tangent (the corotational force has none)");
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  KrylovWs<double>& w = h->k64;
+  CU(cudaMemcpyAsync(w.b + o, dLdu_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  TRY(jacobi<double>(h, w.dinv, nullptr));
+  sfem_pcg_stats ps{};
+  int st = pcg_device<double>(h, h->u, w.b, w.x, w.dinv, rel_tol, max_cg > 0 ? max_cg : 100000, 0, &ps);
+  if (st == SFEM_NEGATIVE_CURVATURE) return SFEM_ERR_BREAKDOWN;
+  if (st < 0) return st;
+  // element internal forces at the current state
+  element_pass<double>(h, MODE_FORCE, h->u, nullptr, h->fe, nullptr, nullptr, nullptr);
+  if (!h->young_e) {
+    std::vector<double> ye((size_t)h->E, h->young);
+    TRY(dalloc(&h->young_e, (size_t)h->E));
+    TRY(dalloc(&h->scale64, (size_t)h->E));
+    TRY(dalloc(&h->scale32, (size_t)h->E));
+    CU(cudaMemcpyAsync(h->young_e, ye.data(), ye.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    TRY(sync(h));
+  } else if (!h->has_scale) {
+    std::vector<double> ye((size_t)h->E, h->young);
+    CU(cudaMemcpyAsync(h->young_e, ye.data(), ye.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    TRY(sync(h));
+  }
+  launch_adjoint_elem(h->tets, h->E, h->nbc, h->fe, w.x, h->young_e, dLdE_dev, h->stream);
+  // dL/df = ff * lambda
+  launch_scale_copy((int64_t)n, h->ff, w.x + o, dLdf_dev, h->stream);
+  CU(cudaGetLastError());
+  return st;
+}
+
+int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max_cg, double* dLdE, double* dLdf) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  const size_t n = 3 * (size_t)h->nf;
+  double *du = nullptr, *dE = nullptr, *dfp = nullptr;
+  TRY(dalloc(&du, n));
+  TRY(dalloc(&dE, (size_t)h->E));
+  TRY(dalloc(&dfp, n));
+  int st = 0;
+  if (cudaMemcpyAsync(du, dLdu, n * sizeof(double), cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    st = fail(SFEM_ERR_CUDA, "copy failed");
+  if (st == 0) st = sfem_adjoint_dev(h, du, rel_tol, max_cg, dE, dfp);
+  if (st >= 0) {
+    if (dLdE) cudaMemcpyAsync(dLdE, dE, (size_t)h->E * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (dLdf) cudaMemcpyAsync(dLdf, dfp, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    int s2 = sync(h);
+    if (s2 < 0) st = s2;
+  }
+  cudaFree(du);
+  cudaFree(dE);
+  cudaFree(dfp);
+  return st;
+}
+
+}  // extern "C"

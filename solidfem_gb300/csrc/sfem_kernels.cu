@@ -1,0 +1,1003 @@
+// Element and Krylov kernels of the matrix-free nonlinear elasticity solve.
+//
+// Per-tetrahedron work (SolidFEM: FemPhysicsMatrixFree::ComputeDeformationGradient
+// Source/FemPhysicsMatrixFree.cpp:354-368, ElasticEnergy::ComputeElementStress
+// Source/ElasticEnergy.cpp:114-257, ElasticEnergy::ComputeForces :259-282,
+// FemPhysicsMatrixFree::ComputeForceDifferential Source/FemPhysicsMatrixFree.cpp:406-496,
+// ElasticEnergy::ComputeElementEnergy Source/ElasticEnergy.cpp:40-112) runs one
+// element per thread over structure-of-arrays element data.  The deformation
+// gradient is formed from nodal displacements, F = I + D(u) Dm^-1, which equals
+// the reference's D(x) Dm^-1 but keeps F - I accurate in FP32.
+//
+// Element results (12 nodal values) go to an element-major scratch array and
+// are summed per node through a node->element CSR in element order, so every
+// nodal sum is deterministic (no floating-point atomics).
+//
+// Krylov scalars live on the device (CgScalars); every reduction is a
+// warp-shuffle block sum followed by a fixed-order sum of the block partials in
+// the last block to finish, so results are run-to-run identical.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "sfem_internal.h"
+
+namespace sfem {
+
+// Number of kernels this library has launched (all wrappers below count theirs).
+static unsigned long long g_launches = 0;
+unsigned long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+static inline void count_launch() { __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED); }
+
+// ---------------------------------------------------------------------------
+// 3x3 algebra (row-major a[3*i+j])
+// ---------------------------------------------------------------------------
+template <typename T>
+struct M3 {
+  T a[9];
+};
+
+template <typename T>
+__device__ __forceinline__ M3<T> mul(const M3<T>& A, const M3<T>& B) {
+  M3<T> C;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) C.a[3 * i + j] = A.a[3 * i] * B.a[j] + A.a[3 * i + 1] * B.a[3 + j] + A.a[3 * i + 2] * B.a[6 + j];
+  return C;
+}
+// A^T B
+template <typename T>
+__device__ __forceinline__ M3<T> mulTN(const M3<T>& A, const M3<T>& B) {
+  M3<T> C;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) C.a[3 * i + j] = A.a[i] * B.a[j] + A.a[3 + i] * B.a[3 + j] + A.a[6 + i] * B.a[6 + j];
+  return C;
+}
+// A B^T
+template <typename T>
+__device__ __forceinline__ M3<T> mulNT(const M3<T>& A, const M3<T>& B) {
+  M3<T> C;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) C.a[3 * i + j] = A.a[3 * i] * B.a[3 * j] + A.a[3 * i + 1] * B.a[3 * j + 1] + A.a[3 * i + 2] * B.a[3 * j + 2];
+  return C;
+}
+template <typename T>
+__device__ __forceinline__ T trace(const M3<T>& A) { return A.a[0] + A.a[4] + A.a[8]; }
+template <typename T>
+__device__ __forceinline__ T det(const M3<T>& A) {
+  return A.a[0] * (A.a[4] * A.a[8] - A.a[5] * A.a[7]) + A.a[1] * (A.a[5] * A.a[6] - A.a[3] * A.a[8]) +
+         A.a[2] * (A.a[3] * A.a[7] - A.a[4] * A.a[6]);
+}
+// cofactor inverse (Math/matrix3.h:234-249)
+template <typename T>
+__device__ __forceinline__ M3<T> inverse(const M3<T>& m, T* det_out = nullptr) {
+  M3<T> r;
+  r.a[0] = m.a[4] * m.a[8] - m.a[5] * m.a[7];
+  r.a[3] = m.a[5] * m.a[6] - m.a[3] * m.a[8];
+  r.a[6] = m.a[3] * m.a[7] - m.a[4] * m.a[6];
+  r.a[1] = m.a[2] * m.a[7] - m.a[1] * m.a[8];
+  r.a[4] = m.a[0] * m.a[8] - m.a[2] * m.a[6];
+  r.a[7] = m.a[1] * m.a[6] - m.a[0] * m.a[7];
+  r.a[2] = m.a[1] * m.a[5] - m.a[2] * m.a[4];
+  r.a[5] = m.a[2] * m.a[3] - m.a[0] * m.a[5];
+  r.a[8] = m.a[0] * m.a[4] - m.a[1] * m.a[3];
+  T d = m.a[0] * r.a[0] + m.a[1] * r.a[3] + m.a[2] * r.a[6];
+  T s = T(1) / d;
+#pragma unroll
+  for (int k = 0; k < 9; k++) r.a[k] *= s;
+  if (det_out) *det_out = d;
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T dev_log(T x);
+template <>
+__device__ __forceinline__ double dev_log<double>(double x) { return log(x); }
+template <>
+__device__ __forceinline__ float dev_log<float>(float x) { return logf(x); }
+template <typename T>
+__device__ __forceinline__ T dev_rsqrt(T x);
+template <>
+__device__ __forceinline__ double dev_rsqrt<double>(double x) { return 1.0 / sqrt(x); }
+template <>
+__device__ __forceinline__ float dev_rsqrt<float>(float x) { return 1.0f / sqrtf(x); }
+
+// Gram-Schmidt "polar" decomposition of SolidFEM (Source/PolarDecomposition.cpp:37-47, 269-280):
+// R = [r0 r1 r2] from the first two columns of F, U = sym(R^T F).
+template <typename T>
+__device__ __forceinline__ void polar_qr(const M3<T>& F, M3<T>& R, M3<T>& U) {
+  T c0[3] = {F.a[0], F.a[3], F.a[6]};
+  T c1[3] = {F.a[1], F.a[4], F.a[7]};
+  T s = dev_rsqrt<T>(c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2]);
+  T r0[3] = {c0[0] * s, c0[1] * s, c0[2] * s};
+  T d = c1[0] * r0[0] + c1[1] * r0[1] + c1[2] * r0[2];
+  T r1[3] = {c1[0] - d * r0[0], c1[1] - d * r0[1], c1[2] - d * r0[2]};
+  s = dev_rsqrt<T>(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
+  r1[0] *= s; r1[1] *= s; r1[2] *= s;
+  T r2[3] = {r0[1] * r1[2] - r1[1] * r0[2], -r0[0] * r1[2] + r0[2] * r1[0], r0[0] * r1[1] - r1[0] * r0[1]};
+  s = dev_rsqrt<T>(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+  r2[0] *= s; r2[1] *= s; r2[2] *= s;
+#pragma unroll
+  for (int i = 0; i < 3; i++) { R.a[3 * i] = r0[i]; R.a[3 * i + 1] = r1[i]; R.a[3 * i + 2] = r2[i]; }
+  M3<T> V = mulTN(R, F);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) U.a[3 * i + j] = T(0.5) * (V.a[3 * i + j] + V.a[3 * j + i]);
+}
+
+// ---------------------------------------------------------------------------
+// Constitutive models (material ids of MaterialModelType)
+// ---------------------------------------------------------------------------
+constexpr int kLinear = 0, kStvk = 1, kCorot = 2, kNeoHookean = 3;
+// corotational force with the exact derivative of that force as its tangent
+constexpr int kCorotExact = 4;
+
+// PK1 stress P(F), ElasticEnergy.cpp:132-187
+template <typename T, int MAT>
+__device__ __forceinline__ M3<T> stress(const M3<T>& F, T mu, T la) {
+  M3<T> P;
+  if (MAT == kLinear) {
+    T tr = trace(F) - T(3);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        T eps = T(0.5) * (F.a[3 * i + j] + F.a[3 * j + i]) - (i == j ? T(1) : T(0));
+        P.a[3 * i + j] = T(2) * mu * eps + (i == j ? la * tr : T(0));
+      }
+  } else if (MAT == kCorot || MAT == kCorotExact) {
+    M3<T> R, U;
+    polar_qr(F, R, U);
+    T tr = trace(U) - T(3);
+    M3<T> S;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) S.a[3 * i + j] = T(2) * mu * (U.a[3 * i + j] - (i == j ? T(1) : T(0))) + (i == j ? la * tr : T(0));
+    P = mul(R, S);
+  } else if (MAT == kStvk) {
+    M3<T> C = mulTN(F, F);
+    T trE = T(0.5) * (trace(C) - T(3));
+    M3<T> S;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) S.a[3 * i + j] = mu * (C.a[3 * i + j] - (i == j ? T(1) : T(0))) + (i == j ? la * trE : T(0));
+    P = mul(F, S);
+  } else {
+    T J;
+    M3<T> Fi = inverse(F, &J);
+    T lj = dev_log<T>(J);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) P.a[3 * i + j] = mu * (F.a[3 * i + j] - Fi.a[3 * j + i]) + la * lj * Fi.a[3 * j + i];
+  }
+  return P;
+}
+
+// strain energy density, ElasticEnergy.cpp:52-109
+template <typename T, int MAT>
+__device__ __forceinline__ T energy_density(const M3<T>& F, T mu, T la) {
+  if (MAT == kNeoHookean) {
+    T J = det(F);
+    T I1 = 0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) I1 += F.a[k] * F.a[k];
+    T lj = dev_log<T>(J);
+    return T(0.5) * mu * (I1 - T(3)) - mu * lj + T(0.5) * la * lj * lj;
+  }
+  M3<T> G = F;
+  if (MAT == kCorot || MAT == kCorotExact) {
+    M3<T> R;
+    polar_qr(F, R, G);
+  }
+  M3<T> eps;
+  if (MAT == kStvk) {
+    M3<T> C = mulTN(G, G);
+#pragma unroll
+    for (int k = 0; k < 9; k++) eps.a[k] = T(0.5) * (C.a[k] - ((k % 4) == 0 ? T(1) : T(0)));
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) eps.a[3 * i + j] = T(0.5) * (G.a[3 * i + j] + G.a[3 * j + i]) - (i == j ? T(1) : T(0));
+  }
+  T tr = trace(eps), dd = 0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) dd += eps.a[k] * eps.a[k];
+  return mu * dd + T(0.5) * la * tr * tr;
+}
+
+// Tangent dP(F; dF), FemPhysicsMatrixFree.cpp:436-470: init() once per element,
+// apply() per direction.
+template <typename T, int MAT>
+struct Tangent;
+
+template <typename T>
+struct Tangent<T, kLinear> {
+  T mu, la;
+  __device__ void init(const M3<T>&, T m, T l) { mu = m; la = l; }
+  __device__ M3<T> apply(const M3<T>& dF) const {
+    M3<T> P;
+    T tr = trace(dF);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) P.a[3 * i + j] = mu * (dF.a[3 * i + j] + dF.a[3 * j + i]) + (i == j ? la * tr : T(0));
+    return P;
+  }
+};
+
+template <typename T>
+struct Tangent<T, kNeoHookean> {
+  M3<T> Fit;  // F^-T
+  T mu, la, c1;  // c1 = mu - lambda log J
+  __device__ void init(const M3<T>& F, T m, T l) {
+    mu = m; la = l;
+    T J;
+    M3<T> Fi = inverse(F, &J);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) Fit.a[3 * i + j] = Fi.a[3 * j + i];
+    c1 = mu - la * dev_log<T>(J);
+  }
+  // dP = mu dF + c1 F^-T dF^T F^-T + lambda tr(F^-1 dF) F^-T
+  __device__ M3<T> apply(const M3<T>& dF) const {
+    M3<T> A = mulNT(Fit, dF);  // F^-T dF^T
+    M3<T> B = mul(A, Fit);
+    T tr = 0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) tr += Fit.a[k] * dF.a[k];
+    T c2 = la * tr;
+    M3<T> P;
+#pragma unroll
+    for (int k = 0; k < 9; k++) P.a[k] = mu * dF.a[k] + c1 * B.a[k] + c2 * Fit.a[k];
+    return P;
+  }
+};
+
+template <typename T>
+struct Tangent<T, kCorot> {
+  M3<T> R, Ainv;
+  T mu, la, k;
+  __device__ void init(const M3<T>& F, T m, T l) {
+    mu = m; la = l;
+    M3<T> S;
+    polar_qr(F, R, S);
+    T trS = trace(S);
+    M3<T> A = S;
+    A.a[0] -= trS; A.a[4] -= trS; A.a[8] -= trS;
+    Ainv = inverse(A);
+    k = la * (trS - T(3)) - T(2) * mu;
+  }
+  __device__ M3<T> apply(const M3<T>& dF) const {
+    M3<T> dS = mulTN(R, dF);
+    T w0 = dS.a[5] - dS.a[7], w1 = dS.a[2] - dS.a[6], w2 = dS.a[1] - dS.a[3];
+    T r0 = Ainv.a[0] * w0 + Ainv.a[1] * w1 + Ainv.a[2] * w2;
+    T r1 = Ainv.a[3] * w0 + Ainv.a[4] * w1 + Ainv.a[5] * w2;
+    T r2 = Ainv.a[6] * w0 + Ainv.a[7] * w1 + Ainv.a[8] * w2;
+    // skew(r) = [[0,-r2,r1],[r2,0,-r0],[-r1,r0,0]]
+    M3<T> Sk;
+    Sk.a[0] = 0; Sk.a[1] = -r2; Sk.a[2] = r1;
+    Sk.a[3] = r2; Sk.a[4] = 0; Sk.a[5] = -r0;
+    Sk.a[6] = -r1; Sk.a[7] = r0; Sk.a[8] = 0;
+    M3<T> dR = mul(R, Sk);
+    T c = la * trace(dS);
+    M3<T> P;
+#pragma unroll
+    for (int q = 0; q < 9; q++) P.a[q] = T(2) * mu * dF.a[q] + c * R.a[q] + k * dR.a[q];
+    return P;
+  }
+};
+
+// Exact derivative of the corotational stress P = R S(U) with the Gram-Schmidt R and
+// U = sym(R^T F): differentiates r0 = c0/|c0|, r1 = v1/|v1| (v1 = c1 - (c1.r0) r0),
+// r2 = r0 x r1 / |r0 x r1|, then dU = sym(dR^T F + R^T dF), dP = dR S + R dS.
+// (The reference's differential, FemPhysicsMatrixFree.cpp:441-456, assumes a true polar R.)
+template <typename T>
+struct Tangent<T, kCorotExact> {
+  M3<T> F, R, S;
+  T mu, la, n0, n1, n2, a;
+  __device__ void init(const M3<T>& Fin, T m, T l) {
+    mu = m; la = l; F = Fin;
+    T c0[3] = {F.a[0], F.a[3], F.a[6]}, c1[3] = {F.a[1], F.a[4], F.a[7]};
+    n0 = sqrt(c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2]);
+    T r0[3] = {c0[0] / n0, c0[1] / n0, c0[2] / n0};
+    a = c1[0] * r0[0] + c1[1] * r0[1] + c1[2] * r0[2];
+    T v1[3] = {c1[0] - a * r0[0], c1[1] - a * r0[1], c1[2] - a * r0[2]};
+    n1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+    T r1[3] = {v1[0] / n1, v1[1] / n1, v1[2] / n1};
+    T v2[3] = {r0[1] * r1[2] - r1[1] * r0[2], -r0[0] * r1[2] + r0[2] * r1[0], r0[0] * r1[1] - r1[0] * r0[1]};
+    n2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+#pragma unroll
+    for (int i = 0; i < 3; i++) { R.a[3 * i] = r0[i]; R.a[3 * i + 1] = r1[i]; R.a[3 * i + 2] = v2[i] / n2; }
+    M3<T> V = mulTN(R, F);
+    T tr = T(0);
+#pragma unroll
+    for (int i = 0; i < 3; i++) tr += V.a[4 * i] - T(1);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        S.a[3 * i + j] = mu * (V.a[3 * i + j] + V.a[3 * j + i]) - (i == j ? T(2) * mu - la * tr : T(0));
+  }
+  __device__ M3<T> apply(const M3<T>& dF) const {
+    T r0[3] = {R.a[0], R.a[3], R.a[6]}, r1[3] = {R.a[1], R.a[4], R.a[7]}, r2[3] = {R.a[2], R.a[5], R.a[8]};
+    T c1[3] = {F.a[1], F.a[4], F.a[7]};
+    T dc0[3] = {dF.a[0], dF.a[3], dF.a[6]}, dc1[3] = {dF.a[1], dF.a[4], dF.a[7]};
+    T t = r0[0] * dc0[0] + r0[1] * dc0[1] + r0[2] * dc0[2];
+    T dr0[3], dv1[3], dr1[3], dv2[3], dr2[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) dr0[i] = (dc0[i] - t * r0[i]) / n0;
+    T da = dc1[0] * r0[0] + dc1[1] * r0[1] + dc1[2] * r0[2] + c1[0] * dr0[0] + c1[1] * dr0[1] + c1[2] * dr0[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) dv1[i] = dc1[i] - da * r0[i] - a * dr0[i];
+    t = r1[0] * dv1[0] + r1[1] * dv1[1] + r1[2] * dv1[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) dr1[i] = (dv1[i] - t * r1[i]) / n1;
+    dv2[0] = dr0[1] * r1[2] - dr0[2] * r1[1] + r0[1] * dr1[2] - r0[2] * dr1[1];
+    dv2[1] = dr0[2] * r1[0] - dr0[0] * r1[2] + r0[2] * dr1[0] - r0[0] * dr1[2];
+    dv2[2] = dr0[0] * r1[1] - dr0[1] * r1[0] + r0[0] * dr1[1] - r0[1] * dr1[0];
+    t = r2[0] * dv2[0] + r2[1] * dv2[1] + r2[2] * dv2[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) dr2[i] = (dv2[i] - t * r2[i]) / n2;
+    M3<T> dR;
+#pragma unroll
+    for (int i = 0; i < 3; i++) { dR.a[3 * i] = dr0[i]; dR.a[3 * i + 1] = dr1[i]; dR.a[3 * i + 2] = dr2[i]; }
+    M3<T> dV = mulTN(dR, F), W = mulTN(R, dF);
+    T trdU = T(0);
+#pragma unroll
+    for (int q = 0; q < 9; q++) dV.a[q] += W.a[q];
+#pragma unroll
+    for (int i = 0; i < 3; i++) trdU += dV.a[4 * i];
+    M3<T> dS;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) dS.a[3 * i + j] = mu * (dV.a[3 * i + j] + dV.a[3 * j + i]) + (i == j ? la * trdU : T(0));
+    M3<T> P1 = mul(dR, S), P2 = mul(R, dS);
+#pragma unroll
+    for (int q = 0; q < 9; q++) P1.a[q] += P2.a[q];
+    return P1;
+  }
+};
+
+template <typename T>
+struct Tangent<T, kStvk> {
+  M3<T> F, S;  // S = 2 mu E + lambda tr(E) I
+  T mu, la;
+  __device__ void init(const M3<T>& Fin, T m, T l) {
+    mu = m; la = l; F = Fin;
+    M3<T> C = mulTN(F, F);
+    T trE = T(0.5) * (trace(C) - T(3));
+#pragma unroll
+    for (int q = 0; q < 9; q++) S.a[q] = mu * (C.a[q] - ((q % 4) == 0 ? T(1) : T(0))) + ((q % 4) == 0 ? la * trE : T(0));
+  }
+  // dP = dF S + F (2 mu dE + lambda tr(dE) I), dE = sym(F^T dF)
+  __device__ M3<T> apply(const M3<T>& dF) const {
+    M3<T> W = mulTN(F, dF);
+    T trdE = trace(W);
+    M3<T> dS;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) dS.a[3 * i + j] = mu * (W.a[3 * i + j] + W.a[3 * j + i]) + (i == j ? la * trdE : T(0));
+    M3<T> P1 = mul(dF, S), P2 = mul(F, dS);
+#pragma unroll
+    for (int q = 0; q < 9; q++) P1.a[q] += P2.a[q];
+    return P1;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Reductions
+// ---------------------------------------------------------------------------
+template <typename A, int K>
+__device__ __forceinline__ void block_sum(A (&v)[K]) {
+  __shared__ A sm[K][32];
+#pragma unroll
+  for (int k = 0; k < K; k++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) sm[k][w] = v[k];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      v[k] = lane < nw ? sm[k][lane] : A(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    }
+  }
+  __syncthreads();
+}
+
+// Block partials, then a fixed-order sum in the last block.  Returns true in
+// the last block; tot[] is valid in its thread 0.
+template <typename A, int K>
+__device__ __forceinline__ bool reduce_last(A (&v)[K], Reduce red, A (&tot)[K]) {
+  __shared__ bool is_last;
+  A* P = reinterpret_cast<A*>(red.partials);
+  block_sum<A, K>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) P[k * gridDim.x + blockIdx.x] = v[k];
+    __threadfence();
+    unsigned t = atomicAdd(red.counter, 1u);
+    is_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+  A s[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    s[k] = A(0);
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s[k] += __ldcg(&P[k * gridDim.x + i]);
+  }
+  block_sum<A, K>(s);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) tot[k] = s[k];
+    *red.counter = 0u;
+  }
+  return true;
+}
+
+__host__ __device__ inline int grid_for(int64_t n, int cap = kMaxBlocks) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (int)b;
+}
+
+// ---------------------------------------------------------------------------
+// Element pass
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void load3(const T* __restrict__ a, int g, T* o) {
+  o[0] = a[3 * (int64_t)g];
+  o[1] = a[3 * (int64_t)g + 1];
+  o[2] = a[3 * (int64_t)g + 2];
+}
+
+// D = [v1 - v0, v2 - v0, v3 - v0] (columns), returns D * X
+template <typename T>
+__device__ __forceinline__ M3<T> grad_of(const T* __restrict__ v, int4 t, const M3<T>& X) {
+  T a0[3], a1[3], a2[3], a3[3];
+  load3(v, t.x, a0);
+  load3(v, t.y, a1);
+  load3(v, t.z, a2);
+  load3(v, t.w, a3);
+  M3<T> D;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    D.a[3 * i] = a1[i] - a0[i];
+    D.a[3 * i + 1] = a2[i] - a0[i];
+    D.a[3 * i + 2] = a3[i] - a0[i];
+  }
+  return mul(D, X);
+}
+
+// 12 nodal values of H = s M X^T: f_{k+1} = column k, f_0 = -(f_1 + f_2 + f_3)
+template <typename T>
+__device__ __forceinline__ void nodal_forces(const M3<T>& M, const M3<T>& X, T s, T* f) {
+  M3<T> H = mulNT(M, X);
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    T h0 = s * H.a[3 * c], h1 = s * H.a[3 * c + 1], h2 = s * H.a[3 * c + 2];
+    f[3 + c] = h0;
+    f[6 + c] = h1;
+    f[9 + c] = h2;
+    f[c] = -(h0 + h1 + h2);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void store12(T* __restrict__ fe, int64_t e, const T* f);
+template <>
+__device__ __forceinline__ void store12<double>(double* __restrict__ fe, int64_t e, const double* f) {
+  double2* o = reinterpret_cast<double2*>(fe + 12 * e);
+#pragma unroll
+  for (int k = 0; k < 6; k++) o[k] = make_double2(f[2 * k], f[2 * k + 1]);
+}
+template <>
+__device__ __forceinline__ void store12<float>(float* __restrict__ fe, int64_t e, const float* f) {
+  float4* o = reinterpret_cast<float4*>(fe + 12 * e);
+#pragma unroll
+  for (int k = 0; k < 3; k++) o[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+}
+
+template <typename T, int MAT, int MODE>
+__global__ void __launch_bounds__(kThreads) k_element(ElemView<T> ev, const T* __restrict__ u,
+                                                      const T* __restrict__ p, T* __restrict__ fe, Reduce red,
+                                                      double* result, int* n_inv, const CgScalars* s) {
+  if (MODE == MODE_HVP && s != nullptr && s->done) return;
+  double eacc = 0.0;
+  int ninv = 0;
+  const int64_t E = ev.E;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int4 t = ev.tets[e];
+    M3<T> X;
+#pragma unroll
+    for (int k = 0; k < 9; k++) X.a[k] = ev.X[k * E + e];
+    const T vol = ev.vol[e];
+    T mu = ev.mu, la = ev.lambda;
+    if (ev.scale) {
+      const T sc = ev.scale[e];
+      mu *= sc;
+      la *= sc;
+    }
+    M3<T> F = grad_of(u, t, X);
+    F.a[0] += T(1);
+    F.a[4] += T(1);
+    F.a[8] += T(1);
+    T f[12];
+    if (MODE == MODE_FORCE) {
+      if (det(F) <= T(0)) ninv++;
+      M3<T> P = stress<T, MAT>(F, mu, la);
+      nodal_forces(P, X, -vol, f);
+      store12(fe, e, f);
+    } else if (MODE == MODE_ENERGY) {
+      if (det(F) <= T(0)) ninv++;
+      eacc += (double)(vol * energy_density<T, MAT>(F, mu, la));
+    } else if (MODE == MODE_HVP) {
+      Tangent<T, MAT> tg;
+      tg.init(F, mu, la);
+      M3<T> dF = grad_of(p, t, X);
+      M3<T> dP = tg.apply(dF);
+      nodal_forces(dP, X, -vol, f);
+      store12(fe, e, f);
+    } else if (MODE == MODE_STRESS) {
+      M3<T> P = stress<T, MAT>(F, mu, la);
+#pragma unroll
+      for (int q = 0; q < 9; q++) f[q] = P.a[q];
+      f[9] = f[10] = f[11] = T(0);
+      store12(fe, e, f);
+    } else if (MODE == MODE_PMU || MODE == MODE_PLAMBDA) {
+      // ElasticEnergy::ComputeStress splits the neo-Hookean P = mu Pmu + lambda Plambda
+      // (ElasticEnergy.cpp:183-186); other materials report zero parts.
+      M3<T> Pp;
+#pragma unroll
+      for (int q = 0; q < 9; q++) Pp.a[q] = T(0);
+      if (MAT == kNeoHookean) {
+        T J;
+        M3<T> Fi = inverse(F, &J);
+        const T lj = dev_log<T>(J);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++)
+            Pp.a[3 * i + j] = MODE == MODE_PMU ? F.a[3 * i + j] - Fi.a[3 * j + i] : lj * Fi.a[3 * j + i];
+      }
+      nodal_forces(Pp, X, -vol, f);
+      store12(fe, e, f);
+    } else if (MODE == MODE_NODALVOL) {
+#pragma unroll
+      for (int q = 0; q < 12; q++) f[q] = (q % 3 == 0) ? T(0.25) * vol : T(0);
+      store12(fe, e, f);
+    } else {  // MODE_DIAG: diagonal of the local stiffness, K_aa,cc = -df_{a,c}(e_{a,c})
+      Tangent<T, MAT> tg;
+      tg.init(F, mu, la);
+#pragma unroll 1
+      for (int a = 0; a < 4; a++) {
+        T g[3];
+        if (a == 0) {
+          g[0] = -(X.a[0] + X.a[3] + X.a[6]);
+          g[1] = -(X.a[1] + X.a[4] + X.a[7]);
+          g[2] = -(X.a[2] + X.a[5] + X.a[8]);
+        } else {
+          g[0] = X.a[3 * (a - 1)];
+          g[1] = X.a[3 * (a - 1) + 1];
+          g[2] = X.a[3 * (a - 1) + 2];
+        }
+#pragma unroll 1
+        for (int c = 0; c < 3; c++) {
+          M3<T> dF;
+#pragma unroll
+          for (int q = 0; q < 9; q++) dF.a[q] = T(0);
+          dF.a[3 * c] = g[0];
+          dF.a[3 * c + 1] = g[1];
+          dF.a[3 * c + 2] = g[2];
+          M3<T> dP = tg.apply(dF);
+          // df_a,c = -vol * (dP X^T)_{c, a-1} (a>0), -sum_k(...) (a=0); K = -df.
+          // (dP X^T)_{c,k} = sum_j dP_cj X_kj; df_a,c for node a uses g_a: sum_j dP_cj g_j
+          T hv = dP.a[3 * c] * g[0] + dP.a[3 * c + 1] * g[1] + dP.a[3 * c + 2] * g[2];
+          f[3 * a + c] = vol * hv;
+        }
+      }
+      store12(fe, e, f);
+    }
+  }
+  if (MODE == MODE_ENERGY) {
+    double v[1] = {eacc}, tot[1];
+    if (reduce_last<double, 1>(v, red, tot) && threadIdx.x == 0) *result = tot[0];
+  }
+  if ((MODE == MODE_FORCE || MODE == MODE_ENERGY) && n_inv != nullptr) {
+    int v[1] = {ninv};
+    block_sum<int, 1>(v);
+    if (threadIdx.x == 0 && v[0] != 0) atomicAdd(n_inv, v[0]);
+  }
+}
+
+template <typename T, int MAT>
+void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* fe, Reduce red, double* result,
+                    int* n_inverted, const CgScalars* s, cudaStream_t st) {
+  count_launch();
+  const int grid = grid_for(ev.E, 152 * 12);
+  switch (mode) {
+    case MODE_FORCE:
+      k_element<T, MAT, MODE_FORCE><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    case MODE_HVP:
+      k_element<T, MAT, MODE_HVP><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    case MODE_DIAG:
+      k_element<T, MAT, MODE_DIAG><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    case MODE_ENERGY:
+      k_element<T, MAT, MODE_ENERGY><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    case MODE_STRESS:
+      k_element<T, MAT, MODE_STRESS><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    case MODE_PMU:
+      k_element<T, MAT, MODE_PMU><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    case MODE_PLAMBDA:
+      k_element<T, MAT, MODE_PLAMBDA><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    default:
+      k_element<T, MAT, MODE_NODALVOL><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+  }
+}
+
+#define SFEM_INST_ELEM(T, M)                                                                                   \
+  template void launch_element<T, M>(int, const ElemView<T>&, const T*, const T*, T*, Reduce, double*, int*, \
+                                     const CgScalars*, cudaStream_t);
+SFEM_INST_ELEM(double, 0)
+SFEM_INST_ELEM(double, 1)
+SFEM_INST_ELEM(double, 2)
+SFEM_INST_ELEM(double, 3)
+SFEM_INST_ELEM(float, 0)
+SFEM_INST_ELEM(float, 1)
+SFEM_INST_ELEM(float, 2)
+SFEM_INST_ELEM(float, 3)
+SFEM_INST_ELEM(double, 4)
+SFEM_INST_ELEM(float, 4)
+
+// ---------------------------------------------------------------------------
+// Node gathers
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void gather_node(NodeCsr csr, const T* __restrict__ fe, int64_t g, T* acc) {
+  acc[0] = acc[1] = acc[2] = T(0);
+  const int64_t b = csr.ptr[g], en = csr.ptr[g + 1];
+  for (int64_t k = b; k < en; k++) {
+    const int64_t x = csr.ent[k];
+    const T* src = fe + 12 * (x >> 2) + 3 * (x & 3);
+    acc[0] += src[0];
+    acc[1] += src[1];
+    acc[2] += src[2];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t N, NodeCsr csr,
+                                                           const double* __restrict__ fe,
+                                                           const double* __restrict__ mass,
+                                                           const double* __restrict__ fext, double g0, double g1,
+                                                           double g2, double ff, double* __restrict__ r,
+                                                           Reduce red, double* rr_out) {
+  double acc = 0.0;
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    double f[3];
+    gather_node(csr, fe, g, f);
+    const double mf = mass[g] * ff;
+    const double gr[3] = {g0, g1, g2};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double v = f[c] + mf * gr[c];
+      v += ff * fext[3 * g + c];
+      r[3 * g + c] = v;
+      acc += v * v;
+    }
+  }
+  double v[1] = {acc}, tot[1];
+  if (reduce_last<double, 1>(v, red, tot) && threadIdx.x == 0 && rr_out) *rr_out = tot[0];
+}
+
+void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
+                         const double* fext, const double* grav, double ff, double* r, Reduce red, double* rr_out,
+                         cudaStream_t st) {
+  count_launch();
+  k_gather_force<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, mass, fext, grav[0], grav[1], grav[2], ff,
+                                                        r, red, rr_out);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_gather_hvp(int64_t nbc, int64_t N, NodeCsr csr,
+                                                         const T* __restrict__ fe, const T* __restrict__ p,
+                                                         T* __restrict__ q, Reduce red, CgScalars* s) {
+  if (s != nullptr && s->done) return;
+  T acc = T(0);
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    T f[3];
+    gather_node(csr, fe, g, f);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const T v = -f[c];
+      q[3 * g + c] = v;
+      acc += p[3 * g + c] * v;
+    }
+  }
+  if (s == nullptr) return;
+  T v[1] = {acc}, tot[1];
+  if (reduce_last<T, 1>(v, red, tot) && threadIdx.x == 0) {
+    const double pq = (double)tot[0];
+    s->pq = pq;
+    if (!isfinite(pq)) {
+      s->done = 1;
+      s->status = -3;
+      s->alpha = 0.0;
+    } else if (!(pq > 0.0)) {  // negative curvature: truncated CG stops here (status 2)
+      s->done = 1;
+      s->status = 2;
+      s->alpha = 0.0;
+    } else {
+      s->alpha = s->rz / pq;
+    }
+  }
+}
+
+template <typename T>
+void launch_gather_hvp(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, const T* p, T* q, Reduce red, CgScalars* s,
+                       cudaStream_t st) {
+  count_launch();
+  k_gather_hvp<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, p, q, red, s);
+}
+template void launch_gather_hvp<double>(int64_t, int64_t, NodeCsr, const double*, const double*, double*, Reduce,
+                                        CgScalars*, cudaStream_t);
+template void launch_gather_hvp<float>(int64_t, int64_t, NodeCsr, const float*, const float*, float*, Reduce,
+                                       CgScalars*, cudaStream_t);
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_gather_diag(int64_t nbc, int64_t N, NodeCsr csr,
+                                                          const T* __restrict__ fe, T* __restrict__ dinv,
+                                                          T* __restrict__ diag) {
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    T f[3];
+    gather_node(csr, fe, g, f);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      if (diag) diag[3 * g + c] = f[c];
+      if (dinv) dinv[3 * g + c] = T(1) / f[c];
+    }
+  }
+}
+
+template <typename T>
+void launch_gather_diag(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, T* dinv, T* diag, cudaStream_t st) {
+  count_launch();
+  k_gather_diag<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, dinv, diag);
+}
+template void launch_gather_diag<double>(int64_t, int64_t, NodeCsr, const double*, double*, double*, cudaStream_t);
+template void launch_gather_diag<float>(int64_t, int64_t, NodeCsr, const float*, float*, float*, cudaStream_t);
+
+__global__ void __launch_bounds__(kThreads) k_adjoint_elem(const int4* __restrict__ tets, int64_t E, int64_t nbc,
+                                                           const double* __restrict__ fe,
+                                                           const double* __restrict__ lam,
+                                                           const double* __restrict__ young_e,
+                                                           double* __restrict__ dLdE) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int4 t = tets[e];
+    const int idx[4] = {t.x, t.y, t.z, t.w};
+    double s = 0.0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      if (idx[a] < nbc) continue;
+#pragma unroll
+      for (int c = 0; c < 3; c++) s += lam[3 * (int64_t)idx[a] + c] * fe[12 * e + 3 * a + c];
+    }
+    dLdE[e] = s / young_e[e];
+  }
+}
+
+void launch_adjoint_elem(const int4* tets, int64_t E, int64_t nbc, const double* fe, const double* lam,
+                         const double* young_e, double* dLdE, cudaStream_t st) {
+  count_launch();
+  k_adjoint_elem<<<grid_for(E, 152 * 12), kThreads, 0, st>>>(tets, E, nbc, fe, lam, young_e, dLdE);
+}
+
+// ---------------------------------------------------------------------------
+// Krylov vector kernels over the free-DOF range (pointers pre-offset)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_cg_init(int64_t n, const T* __restrict__ b, T* __restrict__ x,
+                                                      T* __restrict__ r, T* __restrict__ p,
+                                                      const T* __restrict__ dinv, Reduce red, CgScalars* s) {
+  T rz = T(0), bb = T(0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T ri = b[i];
+    const T zi = dinv ? ri * dinv[i] : ri;
+    x[i] = T(0);
+    r[i] = ri;
+    p[i] = zi;
+    rz += ri * zi;
+    bb += ri * ri;
+  }
+  T v[2] = {rz, bb}, tot[2];
+  if (reduce_last<T, 2>(v, red, tot) && threadIdx.x == 0) {
+    s->rz = (double)tot[0];
+    s->bb = (double)tot[1];
+    s->rr = (double)tot[1];
+    s->tol2 = s->tol2 * (double)tot[1];
+    s->it = 0;
+    s->status = 0;
+    s->done = (tot[1] == T(0)) ? 1 : 0;
+    if (!isfinite(s->bb)) {
+      s->done = 1;
+      s->status = -3;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_cg_update(int64_t n, T* __restrict__ x, T* __restrict__ r,
+                                                        const T* __restrict__ p, const T* __restrict__ q,
+                                                        const T* __restrict__ dinv, Reduce red, CgScalars* s) {
+  if (s->done) return;
+  const T a = (T)s->alpha;
+  T rz = T(0), rr = T(0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    const T ri = r[i] - a * q[i];
+    r[i] = ri;
+    const T zi = dinv ? ri * dinv[i] : ri;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  T v[2] = {rz, rr}, tot[2];
+  if (reduce_last<T, 2>(v, red, tot) && threadIdx.x == 0) {
+    const double rzn = (double)tot[0];
+    s->beta = rzn / s->rz;
+    s->rz = rzn;
+    s->rr = (double)tot[1];
+    s->it += 1;
+    if (!isfinite(s->rr)) {
+      s->done = 1;
+      s->status = -3;
+    } else if (s->rr <= s->tol2) {
+      s->done = 1;
+    } else if (s->it >= s->max_it) {
+      s->done = 1;
+      s->status = 1;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_cg_direction(int64_t n, const T* __restrict__ r,
+                                                           const T* __restrict__ dinv, T* __restrict__ p,
+                                                           const CgScalars* s) {
+  if (s->done) return;
+  const T beta = (T)s->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T zi = dinv ? r[i] * dinv[i] : r[i];
+    p[i] = zi + beta * p[i];
+  }
+}
+
+template <typename T>
+void launch_cg_init(int64_t n, const T* b, T* x, T* r, T* p, const T* dinv, Reduce red, CgScalars* s,
+                    cudaStream_t st) {
+  count_launch();
+  k_cg_init<T><<<grid_for(n), kThreads, 0, st>>>(n, b, x, r, p, dinv, red, s);
+}
+template <typename T>
+void launch_cg_update(int64_t n, T* x, T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s,
+                      cudaStream_t st) {
+  count_launch();
+  k_cg_update<T><<<grid_for(n), kThreads, 0, st>>>(n, x, r, p, q, dinv, red, s);
+}
+template <typename T>
+void launch_cg_direction(int64_t n, const T* r, const T* dinv, T* p, const CgScalars* s, cudaStream_t st) {
+  count_launch();
+  k_cg_direction<T><<<grid_for(n), kThreads, 0, st>>>(n, r, dinv, p, s);
+}
+#define SFEM_INST_CG(T)                                                                                        \
+  template void launch_cg_init<T>(int64_t, const T*, T*, T*, T*, const T*, Reduce, CgScalars*, cudaStream_t); \
+  template void launch_cg_update<T>(int64_t, T*, T*, const T*, const T*, const T*, Reduce, CgScalars*,        \
+                                    cudaStream_t);                                                             \
+  template void launch_cg_direction<T>(int64_t, const T*, const T*, T*, const CgScalars*, cudaStream_t);
+SFEM_INST_CG(double)
+SFEM_INST_CG(float)
+
+// ---------------------------------------------------------------------------
+// Misc
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_dot(int64_t n, const double* __restrict__ a,
+                                                  const double* __restrict__ b, Reduce red, double* out) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += a[i] * b[i];
+  double v[1] = {acc}, tot[1];
+  if (reduce_last<double, 1>(v, red, tot) && threadIdx.x == 0) *out = tot[0];
+}
+void launch_dot(int64_t n, const double* a, const double* b, Reduce red, double* out, cudaStream_t st) {
+  count_launch();
+  k_dot<<<grid_for(n), kThreads, 0, st>>>(n, a, b, red, out);
+}
+
+__global__ void __launch_bounds__(kThreads) k_potential(int64_t nbc, int64_t N, const double* __restrict__ x0,
+                                                        const double* __restrict__ u,
+                                                        const double* __restrict__ mass,
+                                                        const double* __restrict__ fext, double g0, double g1,
+                                                        double g2, double ff, Reduce red, double* out) {
+  double acc = 0.0;
+  const double gr[3] = {g0, g1, g2};
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const double x = x0[3 * g + c] + u[3 * g + c];
+      acc -= ff * (mass[g] * gr[c] + fext[3 * g + c]) * x;
+    }
+  }
+  double v[1] = {acc}, tot[1];
+  if (reduce_last<double, 1>(v, red, tot) && threadIdx.x == 0) *out = tot[0];
+}
+void launch_potential(int64_t nbc, int64_t N, const double* x0, const double* u, const double* mass,
+                      const double* fext, const double* grav, double ff, Reduce red, double* out, cudaStream_t st) {
+  count_launch();
+  k_potential<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, x0, u, mass, fext, grav[0], grav[1], grav[2], ff, red,
+                                                     out);
+}
+
+template <typename Tin, typename Tout>
+__global__ void k_convert(int64_t n, const Tin* __restrict__ a, Tout* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (Tout)a[i];
+}
+template <typename Tin, typename Tout>
+void launch_convert(int64_t n, const Tin* a, Tout* b, cudaStream_t st) {
+  count_launch();
+  k_convert<Tin, Tout><<<grid_for(n), kThreads, 0, st>>>(n, a, b);
+}
+template void launch_convert<double, float>(int64_t, const double*, float*, cudaStream_t);
+template void launch_convert<float, double>(int64_t, const float*, double*, cudaStream_t);
+
+template <typename T>
+__global__ void k_axpy_state(int64_t n, double a, const T* __restrict__ d, const double* __restrict__ base,
+                             double* __restrict__ x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = base[i] + a * (double)d[i];
+}
+template <typename T>
+void launch_axpy_state(int64_t n, double a, const T* d, const double* base, double* x, cudaStream_t st) {
+  count_launch();
+  k_axpy_state<T><<<grid_for(n), kThreads, 0, st>>>(n, a, d, base, x);
+}
+template void launch_axpy_state<double>(int64_t, double, const double*, const double*, double*, cudaStream_t);
+template void launch_axpy_state<float>(int64_t, double, const float*, const double*, double*, cudaStream_t);
+
+__global__ void k_scale_copy(int64_t n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i];
+}
+void launch_scale_copy(int64_t n, double a, const double* x, double* y, cudaStream_t st) {
+  count_launch();
+  k_scale_copy<<<grid_for(n), kThreads, 0, st>>>(n, a, x, y);
+}
+
+}  // namespace sfem
