@@ -210,6 +210,8 @@ def run_gpu_arm(args):
     from solidfem_gb300 import FemPhysicsMatrixFree
 
     dims = DIMS if not args.small else (64, 16, 16)
+    if args.dims:
+        dims = tuple(int(v) for v in args.dims.split(","))
     m, fixed = make_workload(dims)
     seeds = [LOAD_SEED0 + rank * 1000 + i for i in range(args.warmup + args.steps)]
     loads = {s: loads_for(m, s) for s in seeds}
@@ -217,6 +219,19 @@ def run_gpu_arm(args):
     solve_kw = dict(rel_tol=REL_TOL, max_newton=30, max_cg=200000)
 
     p32 = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision="fp32", **kw)
+    method = "jacobi"
+    weights = args.weights if args.weights else os.path.join(ROOT, "solidfem_gb300", "data", "gnn_slab.bin")
+    if args.precond in ("learned", "auto") and os.path.exists(weights):
+        from solidfem_gb300.learned import LearnedPreconditioner
+
+        net = LearnedPreconditioner(p32)
+        net.load(weights)
+        method = "learned"
+    elif args.precond == "learned":
+        raise SystemExit(f"no trained weights at {weights}")
+    from solidfem_gb300 import PC_JACOBI, PC_LEARNED
+
+    main_pc = PC_LEARNED if method == "learned" else PC_JACOBI
     rest = p32.get_free_positions()
     nf = p32.n_free
     # stage every step's inputs in HBM before the timed region (device-pointer API)
@@ -230,10 +245,10 @@ def run_gpu_arm(args):
     lib = p32._lib
     stream = torch.cuda.ExternalStream(_stream_of(p32))
 
-    def solve(p, s):
+    def solve(p, s, pc=None):
         lib.sfem_set_nodal_loads_free_dev(p.handle, dev_loads[s].data_ptr())
         lib.sfem_set_free_positions_dev(p.handle, dev_rest.data_ptr())
-        return p.newton_solve(**solve_kw)
+        return p.newton_solve(precond=main_pc if pc is None else pc, **solve_kw)
 
     for s in seeds[: args.warmup]:
         solve(p32, s)
@@ -272,13 +287,17 @@ def run_gpu_arm(args):
     for s in seeds[args.warmup:]:
         p32.set_nodal_loads(pinned[s])
         p32.set_positions(rest_full)
-        p32.newton_solve(**solve_kw)
+        p32.newton_solve(precond=main_pc, **solve_kw)
         out = p32.get_positions()
     torch.cuda.synchronize()
     e2e_t = allmax((time.perf_counter() - t) / args.steps, world)
     assert out is not None and np.isfinite(out).all()
     h2d += 8 * 3 * m.n_nodes  # rest positions sent each step
 
+    # Jacobi-PCG FP32 of the first timed load (what the learned preconditioner replaces)
+    st_j32 = None
+    if method == "learned":
+        st_j32 = solve(p32, seeds[args.warmup], PC_JACOBI)
     # plain FP64 Jacobi-PCG of the first timed load (the comparison the metric names)
     t64 = None
     st64 = None
@@ -301,9 +320,12 @@ def run_gpu_arm(args):
             "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {
-                "workload": WORKLOAD if not args.small else "reduced 64x16x16 variant of: " + WORKLOAD,
-                "method": "inexact Newton (Eisenstat-Walker), Jacobi-PCG inner solves in FP32, FP64 residual",
-                "preconditioner": "jacobi", "l2": "inputs larger than L2 (element data 0.35 GB FP32)",
+                "workload": WORKLOAD if dims == DIMS else f"reduced {dims} variant of: " + WORKLOAD,
+                "method": ("inexact Newton (Eisenstat-Walker), " +
+                           ("learned-preconditioner flexible PCG" if method == "learned" else "Jacobi-PCG") +
+                           " inner solves in FP32, FP64 residual and convergence test"),
+                "preconditioner": method, "l2": "inputs larger than L2 (element data 0.35 GB FP32)",
+                "jacobi_fp32_stats": st_j32,
                 "converged": ok, "newton_iters": [s_["newton_iters"] for s_ in stats],
                 "cg_iters": [s_["cg_iters"] for s_ in stats],
                 "fp64_jacobi_pcg_s": t64,
@@ -313,7 +335,7 @@ def run_gpu_arm(args):
             },
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk, "unit": "GB/s",
                          "frac": achieved / pk if achieved else None, "traffic": traffic,
-                         "kernel": "k_element<float, neo-Hookean, HVP>",
+                         "kernel": "k_patch_hvp<float, neo-Hookean> (fused element Hessian-vector product)",
                          "algo_bytes_per_launch": prof["algo_bytes_hvp"], "ms_per_launch": ms,
                          "peak_source": pk_kind},
             "e2e": {"value": e2e_t, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -346,9 +368,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="64x16x16 variant (quick check; not a bench line)")
+    ap.add_argument("--dims", default=None, help="override the lattice, e.g. 128,64,64 (profiling; not a bench line)")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per HVP launch, if captured")
+    ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
+                    help="auto: the learned preconditioner when trained weights exist, else Jacobi")
+    ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")
     args = ap.parse_args()
     if args.warmup < 3 and not args.small:
         args.warmup = 3

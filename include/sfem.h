@@ -209,6 +209,31 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
 int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max_cg,
                  double* dLdE, double* dLdf);
 
+/* ---- learned preconditioner (extension: the reference has no learned components) ----
+ * A per-node graph network on the free-node mesh graph (3 message-passing layers, width 64,
+ * BF16 weights and activations, FP32 accumulation on the tensor cores) maps a residual r to a
+ * correction M(r) = D^-1 r + s * net(D^-1 r / s, log D, boundary flags); it replaces Jacobi
+ * inside flexible (Polak-Ribiere) PCG when sfem_newton_opts.precond = SFEM_PC_LEARNED.
+ * FP32 handles only.  Parameter vector layout: sfem_gnn_num_params floats
+ * [We(64x8) be(64) {Wl(64x128) bl(64)} x3 Wd(3x64) bd(3)]. */
+int sfem_gnn_num_params(int32_t* n);
+int sfem_gnn_init(sfem_handle* h, uint64_t seed);
+int sfem_gnn_get_params(sfem_handle* h, float* params);
+int sfem_gnn_set_params(sfem_handle* h, const float* params);
+/* M(r) at the current state (uses the current Jacobi diagonal); free-DOF vectors */
+int sfem_gnn_apply(sfem_handle* h, const double* r_free, double* out_free);
+/* energy-norm loss ||M(r) - e||_K^2 / (e . r) of one residual/correction pair and its gradient */
+int sfem_gnn_loss_grad(sfem_handle* h, const double* r_free, const double* e_free, double* loss, float* grad);
+/* residual/correction pairs (r_j, x_final - x_j) from a plain Jacobi-PCG solve of K x = b
+ * (b_free NULL: the current nonlinear residual), one every `every` iterations, appended to
+ * the handle's training set */
+int sfem_gnn_collect(sfem_handle* h, const double* b_free, int32_t every, int32_t max_snaps, double rel_tol,
+                     int32_t* n_added);
+int sfem_gnn_dataset_size(sfem_handle* h, int32_t* n);
+int sfem_gnn_clear_dataset(sfem_handle* h);
+/* Adam on the collected pairs, one seeded random pair per step; losses: steps floats (optional) */
+int sfem_gnn_train(sfem_handle* h, int32_t steps, float lr, uint64_t seed, float* losses);
+
 /* ---- instrumentation (no reference counterpart: the reference's PROFILE_SCOPE macros are
  * empty, Engine/Profiler.h:35-39) ---- */
 typedef struct {

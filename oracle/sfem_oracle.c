@@ -439,8 +439,10 @@ void orc_jacobi_diagonal(void* h, double* diag) {
   orc_problem* p = (orc_problem*)h;
   int nbc = p->n_bcs, nf = p->n_nodes - nbc;
   memset(diag, 0, sizeof(double) * 3 * (size_t)nf);
+  double* kdall = (double*)malloc(sizeof(double) * 12 * (size_t)p->n_tets);
+  /* element loop in parallel (as the reference's assembly loop, ElasticEnergy.cpp:589), scatter serial */
+  #pragma omp parallel for schedule(static)
   for (int e = 0; e < p->n_tets; e++) {
-    const int* t = p->tets + 4 * (size_t)e;
     M3 F = def_grad(p, e);
     M3 X = load_X(p, e);
     double kd[12];
@@ -458,11 +460,17 @@ void orc_jacobi_diagonal(void* h, double* diag) {
       else { double s = 0; for (int k = 0; k < 3; k++) s -= H.m[c][k]; dfv = s; }
       kd[j] = -dfv;
     }
+    memcpy(kdall + 12 * (size_t)e, kd, sizeof(kd));
+  }
+  for (int e = 0; e < p->n_tets; e++) {
+    const int* t = p->tets + 4 * (size_t)e;
+    const double* kd = kdall + 12 * (size_t)e;
     for (int a = 0; a < 4; a++) {
       if (t[a] < nbc) continue;
       for (int c = 0; c < 3; c++) diag[3 * (size_t)(t[a] - nbc) + c] += kd[3 * a + c];
     }
   }
+  free(kdall);
 }
 
 /* PK1 stress of all elements at the current positions (E x 9). */
@@ -624,10 +632,12 @@ done:
 
 /*
  * Inexact Newton with Jacobi-PCG inner solves (the same algorithm as the GPU
- * host driver): forcing term eta_k (Eisenstat-Walker choice 2, gamma=0.9,
- * exponent 2, eta_max, floored by eta_min and by the final target), residual
- * norm backtracking (accept |r(x+a d)| <= (1 - 1e-4 a) |r(x)|, no inverted
- * elements, halve up to 30 times).  Converges when |r| <= rtol |r0|.
+ * host driver's default): forcing term eta_k (Eisenstat-Walker choice 2,
+ * gamma=0.9, exponent 2, eta_max, floored by eta_min and by the final target),
+ * backtracking (halve up to 30 times, no inverted elements) on the total energy
+ * (Armijo, 1e-4) for hyperelastic materials -- with the residual norm deciding
+ * once the energy change is below FP64 resolution -- and on the residual norm
+ * (|r(x+a d)| <= (1 - 1e-4 a) |r(x)|) for corotational.  Converges when |r| <= rtol |r0|.
  * stats[0]=newton its, [1]=total cg its, [2]=final |r|/|r0|, [3]=|r0|.
  */
 int orc_newton_pcg(void* h, double rtol, int max_newton, int max_cg, double eta_max, double eta_min, double* stats) {
@@ -657,6 +667,11 @@ int orc_newton_pcg(void* h, double rtol, int max_newton, int max_cg, double eta_
     double rr;
     cg_total += orc_pcg(h, r, dx, diag, eta, max_cg, &rr);
     orc_get_free_positions(h, x0);
+    /* energy Armijo (hyperelastic) with the residual norm deciding once the energy change is
+     * below FP64 resolution; residual-norm backtracking for corotational */
+    const int armijo = p->material != MMT_COROTATIONAL;
+    const double e_old = armijo ? orc_total_energy(h) : 0.0;
+    const double slope = -dotn(r, dx, n);
     double a = 1.0;
     int ok = 0;
     for (int ls = 0; ls < 30; ls++) {
@@ -664,7 +679,18 @@ int orc_newton_pcg(void* h, double rtol, int max_newton, int max_cg, double eta_
       if (orc_count_inverted(h) == 0) {
         orc_compute_gradients(h, r);
         double n2 = sqrt(dotn(r, r, n));
-        if (isfinite(n2) && n2 <= (1 - 1e-4 * a) * rn) { rprev = rn; rn = n2; ok = 1; break; }
+        int cond = 0;
+        if (isfinite(n2)) {
+          if (armijo) {
+            const double e_el = orc_elastic_energy(h), e_new = orc_total_energy(h);
+            cond = e_new < e_old + 1e-4 * a * slope;
+            const double res = 1e-12 * (fabs(e_old) + fabs(e_el));
+            if (!cond && fabs(e_new - e_old) <= res && fabs(a * slope) <= res) cond = n2 < rn;
+          } else {
+            cond = n2 <= (1 - 1e-4 * a) * rn;
+          }
+        }
+        if (cond) { rprev = rn; rn = n2; ok = 1; break; }
       }
       a *= 0.5;
     }

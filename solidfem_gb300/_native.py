@@ -103,6 +103,16 @@ SIGNATURES = {
     "sfem_newton_solve": [_vp, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)],
     "sfem_nonlinear_cg": [_vp, C.c_int32, C.c_int32, C.c_double, _ip],
     "sfem_adjoint": [_vp, _dp, C.c_double, C.c_int32, _dp, _dp],
+    "sfem_gnn_num_params": [_ip],
+    "sfem_gnn_init": [_vp, C.c_uint64],
+    "sfem_gnn_get_params": [_vp, C.POINTER(C.c_float)],
+    "sfem_gnn_set_params": [_vp, C.POINTER(C.c_float)],
+    "sfem_gnn_apply": [_vp, _dp, _dp],
+    "sfem_gnn_loss_grad": [_vp, _dp, _dp, _dp, C.POINTER(C.c_float)],
+    "sfem_gnn_collect": [_vp, _dp, C.c_int32, C.c_int32, C.c_double, _ip],
+    "sfem_gnn_dataset_size": [_vp, _ip],
+    "sfem_gnn_clear_dataset": [_vp],
+    "sfem_gnn_train": [_vp, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)],
     "sfem_set_profiling": [_vp, C.c_int32],
     "sfem_get_profile": [_vp, C.POINTER(Profile)],
     "sfem_kernel_launches": [_i64p],

@@ -1,0 +1,272 @@
+// Launchers of the learned-preconditioner kernels (sfem_gnn_kernels.cuh).
+#include <algorithm>
+
+#include "sfem_gnn_kernels.cuh"
+#include "sfem_internal.h"
+
+namespace sfem {
+namespace gnn {
+
+static int blocks_for(int64_t n, int per) {
+  int64_t b = (n + per - 1) / per;
+  return (int)(b < 1 ? 1 : b);
+}
+
+void launch_stat(int which, int64_t n3, const float* r, const float* dinv, float* partials, unsigned* counter,
+                 Scalars* sc, const int* done, cudaStream_t st) {
+  int grid = blocks_for(n3, 256);
+  if (grid > 1024) grid = 1024;
+  if (which == 0)
+    k_gnn_stat<0><<<grid, 256, 0, st>>>(n3, r, dinv, partials, counter, sc, done);
+  else
+    k_gnn_stat<1><<<grid, 256, 0, st>>>(n3, r, dinv, partials, counter, sc, done);
+}
+
+void launch_forward(const Graph& g, const float* r, const float* dinv, const uint8_t* fixed_nb, const float* params,
+                    const __nv_bfloat16* Wb, Scalars* sc, __nv_bfloat16* const* h, __nv_bfloat16* const* u, float* x,
+                    float* out, const int* done, cudaStream_t st) {
+  k_gnn_encode<<<blocks_for(g.n * 32, 256), 256, 0, st>>>(g.n, r, dinv, fixed_nb, params, sc, h[0], u ? u[0] : nullptr,
+                                                          x, done);
+  for (int l = 0; l < NL; l++)
+    k_gnn_layer_fwd<<<blocks_for(g.n, TILE), LT, 0, st>>>(g, h[l], Wb + (size_t)l * H * AIN,
+                                                          params + OFF_L + l * L_STRIDE + H * AIN, h[l + 1],
+                                                          u ? u[l + 1] : nullptr, done);
+  k_gnn_decode<<<blocks_for(g.n, 256), 256, 0, st>>>(g.n, h[NL], params, sc, r, dinv, out, done);
+}
+
+int launch_count_forward() { return 2 + NL; }
+
+void launch_backward(const Graph& g, const float* Go, const float* params, const __nv_bfloat16* Wtb, const Scalars* sc,
+                     __nv_bfloat16* const* h, __nv_bfloat16* const* u, const float* x, float* G0, float* G1,
+                     float* G2, float* partial, float* grad, cudaStream_t st) {
+  // decoder: G0 <- dL/dh3
+  const int nbd = blocks_for(g.n, 256);
+  k_gnn_decode_bwd<<<nbd, 256, 0, st>>>(g.n, h[NL], params, sc, Go, G0, partial);
+  k_gnn_reduce_cols<<<1, 256, 0, st>>>(nbd, 3 * H + 3, partial, grad + OFF_WD, 0);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gnn_layer_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLayerBwdSmem);
+    attr = true;
+  }
+  const int nbl = blocks_for(g.n, TILE);
+  float* Gout = G0;
+  for (int l = NL - 1; l >= 0; l--) {
+    // layer l maps h[l] -> h[l+1]; Gout = dL/dh[l+1]
+    k_gnn_layer_bwd<<<nbl, LT, kLayerBwdSmem, st>>>(g, h[l], u[l + 1], Gout, Wtb + (size_t)l * H * AIN, G1, G2,
+                                                    partial);
+    k_gnn_reduce_cols<<<(LPART + 255) / 256, 256, 0, st>>>(nbl, LPART, partial, grad + OFF_L + l * L_STRIDE, 0);
+    // G0 <- dL/dh[l]
+    k_gnn_msg_scatter<<<blocks_for(g.n * 32, 256), 256, 0, st>>>(g, G1, G2, G0);
+    Gout = G0;
+  }
+  const int nbe = blocks_for(g.n, 64);
+  k_gnn_encode_bwd<<<nbe, 256, 0, st>>>(g.n, G0, u[0], x, partial);
+  k_gnn_reduce_cols<<<(H * FIN + H + 255) / 256, 256, 0, st>>>(nbe, H * FIN + H, partial, grad + OFF_WE, 0);
+}
+
+int launch_count_backward() { return 2 + NL * 3 + 2; }
+
+void launch_loss(int64_t n3, const float* d, const float* q, float inv_c, float* Go, float* partials,
+                 unsigned* counter, float* loss, cudaStream_t st) {
+  int grid = blocks_for(n3, 256);
+  if (grid > 1024) grid = 1024;
+  k_gnn_loss<<<grid, 256, 0, st>>>(n3, d, q, inv_c, Go, partials, counter, loss);
+}
+
+void launch_adam(const float* grad, float* prm, float* m, float* v, float lr, int t, float clip_scale,
+                 __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st) {
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - powf(b1, (float)t), bc2 = 1.f - powf(b2, (float)t);
+  k_gnn_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(NPARAM, prm, grad, m, v, lr, b1, b2, 1e-8f, bc1, bc2, clip_scale);
+  k_gnn_pack<<<(NL * H * AIN + 255) / 256, 256, 0, st>>>(prm, Wb, Wtb);
+}
+
+void launch_pack(const float* prm, __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st) {
+  k_gnn_pack<<<(NL * H * AIN + 255) / 256, 256, 0, st>>>(prm, Wb, Wtb);
+}
+
+}  // namespace gnn
+}  // namespace sfem
+
+// ---------------------------------------------------------------------------
+// Flexible CG vector kernels (FP32) and small helpers
+// ---------------------------------------------------------------------------
+namespace sfem {
+namespace gnn {
+
+__device__ __forceinline__ float block_sum256(float v, float* sm) {
+  v = warp_sumf(v);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float b = 0.f;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) b += sm[w];
+  __syncthreads();
+  return b;  // valid in thread 0
+}
+
+// d = a - b
+__global__ void k_sub(int64_t n, const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ d) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = a[i] - b[i];
+}
+void launch_sub(int64_t n, const float* a, const float* b, float* d, cudaStream_t st) {
+  int grid = (int)std::min<int64_t>((n + 255) / 256, 2048);
+  k_sub<<<grid < 1 ? 1 : grid, 256, 0, st>>>(n, a, b, d);
+}
+
+// p = z, rz = r.z  (after the CG initialisation has set r, x, bb)
+__global__ void __launch_bounds__(256) k_fcg_init(int64_t n, const float* __restrict__ r, const float* __restrict__ z,
+                                                  float* __restrict__ p, float* __restrict__ partials,
+                                                  unsigned* counter, CgScalars* s) {
+  __shared__ float sm[8];
+  __shared__ bool last;
+  float acc = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    p[i] = z[i];
+    acc += r[i] * z[i];
+  }
+  const float b = block_sum256(acc, sm);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double t = 0.0;
+  for (unsigned k = 0; k < gridDim.x; k++) t += (double)__ldcg(&partials[k]);
+  s->rz = t;
+  *counter = 0u;
+}
+
+// x += alpha p, rprev = r, r -= alpha q, rr
+__global__ void __launch_bounds__(256) k_fcg_update(int64_t n, float* __restrict__ x, float* __restrict__ r,
+                                                    float* __restrict__ rprev, const float* __restrict__ p,
+                                                    const float* __restrict__ q, float* __restrict__ partials,
+                                                    unsigned* counter, CgScalars* s) {
+  if (s->done) return;
+  __shared__ float sm[8];
+  __shared__ bool last;
+  const float a = (float)s->alpha;
+  float acc = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    const float ri = r[i];
+    rprev[i] = ri;
+    const float rn = ri - a * q[i];
+    r[i] = rn;
+    acc += rn * rn;
+  }
+  const float b = block_sum256(acc, sm);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double t = 0.0;
+  for (unsigned k = 0; k < gridDim.x; k++) t += (double)__ldcg(&partials[k]);
+  s->rr = t;
+  s->it += 1;
+  if (!isfinite(t)) {
+    s->done = 1;
+    s->status = -3;
+  } else if (t <= s->tol2) {
+    s->done = 1;
+  } else if (s->it >= s->max_it) {
+    s->done = 1;
+    s->status = 1;
+  }
+  *counter = 0u;
+}
+
+// Polak-Ribiere: beta = z.(r - rprev) / rz_old, rz = z.r.  The same sums are formed for the
+// Jacobi direction z_J = D^-1 r; when the learned direction is not a descent direction
+// (z.r <= 0) or is far less aligned with r than Jacobi's, this iteration falls back to
+// Jacobi (s->status = 0 keeps the solve going; s->beta / s->rz refer to the chosen z and
+// s->pq carries the choice to k_fcg_dir: pq < 0 selects Jacobi).
+__global__ void __launch_bounds__(256) k_fcg_beta(int64_t n, const float* __restrict__ r,
+                                                  const float* __restrict__ rprev, const float* __restrict__ z,
+                                                  const float* __restrict__ dinv, float* __restrict__ partials,
+                                                  unsigned* counter, CgScalars* s) {
+  if (s->done) return;
+  __shared__ float sm[8];
+  __shared__ bool last;
+  float a0 = 0.f, a1 = 0.f, j0 = 0.f, j1 = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float dr = r[i] - rprev[i];
+    const float zj = dinv[i] * r[i];
+    a0 += z[i] * dr;
+    a1 += z[i] * r[i];
+    j0 += zj * dr;
+    j1 += zj * r[i];
+  }
+  const float b0 = block_sum256(a0, sm);
+  const float b1 = block_sum256(a1, sm);
+  const float c0 = block_sum256(j0, sm);
+  const float c1 = block_sum256(j1, sm);
+  if (threadIdx.x == 0) {
+    partials[4 * blockIdx.x] = b0;
+    partials[4 * blockIdx.x + 1] = b1;
+    partials[4 * blockIdx.x + 2] = c0;
+    partials[4 * blockIdx.x + 3] = c1;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (unsigned k = 0; k < gridDim.x; k++)
+    for (int q = 0; q < 4; q++) t[q] += (double)__ldcg(&partials[4 * k + q]);
+  const bool learned_ok = t[1] > 0.0 && isfinite(t[1]) && isfinite(t[0]);
+  if (learned_ok) {
+    s->beta = t[0] / s->rz;
+    s->rz = t[1];
+    s->pq = 1.0;
+  } else {
+    s->beta = t[2] / s->rz;
+    s->rz = t[3];
+    s->pq = -1.0;
+  }
+  *counter = 0u;
+}
+
+__global__ void k_fcg_dir(int64_t n, const float* __restrict__ z, const float* __restrict__ r,
+                          const float* __restrict__ dinv, float* __restrict__ p, const CgScalars* s) {
+  if (s->done) return;
+  const float beta = (float)s->beta;
+  const bool jac = s->pq < 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = (jac ? dinv[i] * r[i] : z[i]) + beta * p[i];
+}
+
+static int vgrid(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b < 1) b = 1;
+  if (b > 1024) b = 1024;
+  return (int)b;
+}
+void launch_fcg_init(int64_t n, const float* r, const float* z, float* p, float* partials, unsigned* counter,
+                     CgScalars* s, cudaStream_t st) {
+  k_fcg_init<<<vgrid(n), 256, 0, st>>>(n, r, z, p, partials, counter, s);
+}
+void launch_fcg_update(int64_t n, float* x, float* r, float* rprev, const float* p, const float* q, float* partials,
+                       unsigned* counter, CgScalars* s, cudaStream_t st) {
+  k_fcg_update<<<vgrid(n), 256, 0, st>>>(n, x, r, rprev, p, q, partials, counter, s);
+}
+void launch_fcg_beta(int64_t n, const float* r, const float* rprev, const float* z, const float* dinv,
+                     float* partials, unsigned* counter, CgScalars* s, cudaStream_t st) {
+  k_fcg_beta<<<vgrid(n), 256, 0, st>>>(n, r, rprev, z, dinv, partials, counter, s);
+}
+void launch_fcg_dir(int64_t n, const float* z, const float* r, const float* dinv, float* p, const CgScalars* s,
+                    cudaStream_t st) {
+  k_fcg_dir<<<vgrid(n), 256, 0, st>>>(n, z, r, dinv, p, s);
+}
+
+}  // namespace gnn
+}  // namespace sfem

@@ -1,0 +1,43 @@
+// Sizes, parameter layout and plain structs of the learned preconditioner, shared by
+// the host driver and the kernels (sfem_gnn_kernels.cuh).
+#pragma once
+#include <stdint.h>
+
+namespace sfem {
+namespace gnn {
+
+constexpr int H = 64;        // width
+constexpr int FIN = 8;       // input features
+constexpr int NL = 3;        // message-passing layers
+constexpr int AIN = 2 * H;   // layer input [h ; mean h]
+constexpr int TILE = 64;     // nodes per CTA in the layer kernels
+constexpr int LT = 128;      // threads per CTA in the layer kernels (4 warps x 16 nodes)
+constexpr int SROW = AIN + 8;  // padded shared-memory row (bf16) for 128-wide rows
+constexpr int SROW64 = H + 8;  // padded row for 64-wide rows
+
+// parameter vector layout (FP32 master copy)
+constexpr int OFF_WE = 0;                 // We [H x FIN]
+constexpr int OFF_BE = OFF_WE + H * FIN;  // be [H]
+constexpr int OFF_L = OFF_BE + H;         // per layer: Wl [H x AIN], bl [H]
+constexpr int L_STRIDE = H * AIN + H;
+constexpr int OFF_WD = OFF_L + NL * L_STRIDE;  // Wd [3 x H]
+constexpr int OFF_BD = OFF_WD + 3 * H;         // bd [3]
+constexpr int NPARAM = OFF_BD + 3;
+constexpr int LPART = H * AIN + H;  // per-CTA partial of one layer's gradient (dW, db)
+
+struct Graph {
+  int64_t n;              // free nodes
+  const int32_t* ptr;     // n + 1
+  const int32_t* idx;     // neighbours (free-node indices)
+  const float* inv_deg;   // 1 / max(deg, 1)
+};
+
+struct Scalars {  // device-resident scalars of one application
+  float s;        // rms of z
+  float inv_s;
+  float mean_ld;  // mean log d over free DOFs
+  float pad;
+};
+
+}  // namespace gnn
+}  // namespace sfem

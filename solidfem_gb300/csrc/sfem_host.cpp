@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <random>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -67,10 +68,19 @@ int dalloc(T** p, size_t count) {
 
 template <typename T>
 struct KrylovWs {  // vectors of one precision, full length 3N (fixed-node entries stay 0)
-  T *b = nullptr, *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr, *u = nullptr;
+  T *b = nullptr, *x = nullptr, *r = nullptr, *p = nullptr, *p2 = nullptr, *q = nullptr, *dinv = nullptr,
+    *u = nullptr, *ones = nullptr;
 };
 
+struct GnnState;
+void gnn_free(GnnState* g);
+
 }  // namespace
+
+int sfem::set_error(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
 
 struct sfem_handle {
   int device = 0;
@@ -86,11 +96,30 @@ struct sfem_handle {
 
   // element data
   int4* tets = nullptr;
-  double *X64 = nullptr, *vol64 = nullptr, *scale64 = nullptr, *young_e = nullptr;
-  float *X32 = nullptr, *vol32 = nullptr, *scale32 = nullptr;
+  double *X64 = nullptr, *vol64 = nullptr, *scale64 = nullptr, *young_e = nullptr, *scale_la64 = nullptr;
+  float *X32 = nullptr, *vol32 = nullptr, *scale32 = nullptr, *scale_la32 = nullptr;
+  bool has_scale_la = false;
+  // independent instances: free-DOF segments, per-instance activity and residual norms
+  int n_inst = 0;
+  int64_t* inst_seg = nullptr;   // device, n_inst + 1 (offsets into a free-DOF vector)
+  int32_t* inst_active = nullptr;
+  double* inst_norm = nullptr;
+  std::vector<double> inst_r0, inst_rel;
+  std::vector<int32_t> inst_its;
   // node data (reshuffled, 3N)
   double *x0 = nullptr, *u = nullptr, *mass = nullptr, *fext = nullptr, *grav_d = nullptr;
   int64_t *csr_ptr = nullptr, *csr_ent = nullptr;
+  // element patches (elements are stored in patch order; perm maps to the caller's order)
+  std::vector<int32_t> perm_h;
+  int32_t* perm = nullptr;
+  int64_t n_patches = 0, n_slots = 0, n_shared = 0;
+  int64_t *elem_off = nullptr, *node_off = nullptr;
+  int32_t *pnode = nullptr, *pdest = nullptr, *bnode = nullptr, *bptr = nullptr, *bidx = nullptr;
+  uint16_t *lptr = nullptr, *lent = nullptr;
+  ushort4* lidx = nullptr;
+  double* partial = nullptr;  // 3 * n_slots values (float passes use it as floats)
+  double* etmp = nullptr;     // E scratch doubles
+  GnnState* gnn = nullptr;    // learned preconditioner (sfem_gnn_init)
   // scratch
   double* fe = nullptr;  // 12 E doubles (float passes use it as 12 E floats)
   double* partials = nullptr;
@@ -113,12 +142,20 @@ struct sfem_handle {
   int prof_precision = 0;
 
   Reduce red() const { return Reduce{partials, counter}; }
+  PatchBoundary pb() const { return PatchBoundary{n_shared, bnode, bptr}; }
+  template <typename T>
+  PatchView<T> pv(const T* X, const T* vol, const T* scale, const T* scale_la, T m, T l) const {
+    return PatchView<T>{elem_off, node_off, pnode, pdest, lptr, lent, lidx, X, vol, scale, scale_la, E, n_patches,
+                        nbc, m, l};
+  }
   NodeCsr csr() const { return NodeCsr{csr_ptr, csr_ent}; }
   ElemView<double> ev64() const {
-    return ElemView<double>{tets, X64, vol64, has_scale ? scale64 : nullptr, E, mu, lambda};
+    return ElemView<double>{tets, X64, vol64, has_scale ? scale64 : nullptr,
+                            has_scale && has_scale_la ? scale_la64 : nullptr, E, mu, lambda};
   }
   ElemView<float> ev32() const {
-    return ElemView<float>{tets, X32, vol32, has_scale ? scale32 : nullptr, E, (float)mu, (float)lambda};
+    return ElemView<float>{tets, X32, vol32, has_scale ? scale32 : nullptr,
+                           has_scale && has_scale_la ? scale_la32 : nullptr, E, (float)mu, (float)lambda};
   }
 };
 
@@ -128,11 +165,16 @@ template <typename T>
 int alloc_ws(sfem_handle* h, KrylovWs<T>& w) {
   if (w.b) return 0;
   size_t n = 3 * (size_t)h->N;
-  T** ptrs[] = {&w.b, &w.x, &w.r, &w.p, &w.q, &w.dinv, &w.u};
+  T** ptrs[] = {&w.b, &w.x, &w.r, &w.p, &w.p2, &w.q, &w.dinv, &w.u, &w.ones};
   for (T** p : ptrs) {
     TRY(dalloc(p, n));
     CU(cudaMemsetAsync(*p, 0, n * sizeof(T), h->stream));
   }
+  // identity "preconditioner" (1 on free DOFs, 0 on fixed ones) for unpreconditioned CG
+  std::vector<T> ones(n, T(0));
+  for (size_t i = 3 * (size_t)h->nbc; i < n; i++) ones[i] = T(1);
+  CU(cudaMemcpyAsync(w.ones, ones.data(), n * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
   return 0;
 }
 
@@ -161,6 +203,23 @@ void element_pass(sfem_handle* h, int mode, const T* u, const T* p, T* fe, doubl
     case 2: launch_element<T, 2>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
     case 3: launch_element<T, 3>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
     default: launch_element<T, 4>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
+  }
+}
+
+// q = K p over the free DOFs with the fused patch kernel (+ p.q and alpha when s is given)
+template <typename T>
+void hvp(sfem_handle* h, const T* u, const T* p, T* q, CgScalars* s, cudaEvent_t mid = nullptr, const T* r = nullptr,
+         const T* dinv = nullptr, T* p_new = nullptr) {
+  const ElemView<T> ev = ev_of<T>(h);
+  const PatchView<T> pv = h->pv<T>(ev.X, ev.vol, ev.scale, ev.scale_la, ev.mu, ev.lambda);
+  T* part = reinterpret_cast<T*>(h->partial);
+  const int mat = (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) ? 4 : h->material;
+  switch (mat) {
+    case 0: launch_patch_hvp<T, 0>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
+    case 1: launch_patch_hvp<T, 1>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
+    case 2: launch_patch_hvp<T, 2>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
+    case 3: launch_patch_hvp<T, 3>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
+    default: launch_patch_hvp<T, 4>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
   }
 }
 
@@ -214,14 +273,17 @@ int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, doub
                int check_every, sfem_pcg_stats* st) {
   KrylovWs<T>& w = ws_of<T>(h);
   const int64_t o = 3 * h->nbc, n = 3 * h->nf;
-  T* fe = reinterpret_cast<T*>(h->fe);
   CgScalars s0;
   memset(&s0, 0, sizeof(s0));
   s0.tol2 = tol * tol;
   s0.max_it = max_it;
   *h->scal_h = s0;
   CU(cudaMemcpyAsync(h->scal, h->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
-  launch_cg_init<T>(n, b + o, x + o, w.r + o, w.p + o, dinv ? dinv + o : nullptr, h->red(), h->scal, h->stream);
+  if (!dinv) dinv = w.ones;  // unpreconditioned CG: z = r
+  launch_cg_init<T>(n, b + o, x + o, w.r + o, w.p + o, dinv + o, h->red(), h->scal, h->stream);
+  // directions alternate between two buffers: iteration k reads p_{k-1} from pbuf[k % 2] and
+  // the patch kernel writes p_k = dinv r + beta p_{k-1} into pbuf[(k + 1) % 2]
+  T* pbuf[2] = {w.p, w.p2};
   if (check_every <= 0) check_every = 32;
   int it = 0;
   bool pending = false;
@@ -242,17 +304,16 @@ int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, doub
     for (int k = 0; k < check_every && it < max_it; k++, it++) {
       const bool sample = h->profiling && k == 0;
       if (sample) CU(cudaEventRecord(h->pev[0], h->stream));
-      element_pass<T>(h, MODE_HVP, u, w.p, fe, nullptr, nullptr, h->scal);
-      if (sample) CU(cudaEventRecord(h->pev[1], h->stream));
-      launch_gather_hvp<T>(h->nbc, h->N, h->csr(), fe, w.p, w.q, h->red(), h->scal, h->stream);
+      T* pold = pbuf[it % 2];
+      T* pnew = pbuf[(it + 1) % 2];
+      hvp<T>(h, u, pold, w.q, h->scal, sample ? h->pev[1] : nullptr, w.r, dinv, pnew);
       if (sample) {
         CU(cudaEventRecord(h->pev[2], h->stream));
         pending = true;
       }
       if (h->profiling) h->prof_launches++;
-      launch_cg_update<T>(n, x + o, w.r + o, w.p + o, w.q + o, dinv ? dinv + o : nullptr, h->red(), h->scal,
-                          h->stream);
-      launch_cg_direction<T>(n, w.r + o, dinv ? dinv + o : nullptr, w.p + o, h->scal, h->stream);
+      launch_cg_update_patch<T>(h->nbc, h->N, h->bidx, h->pb(), reinterpret_cast<const T*>(h->partial), x, w.r,
+                                pnew, w.q, dinv, h->red(), h->scal, h->stream);
     }
   }
   if (pending) {
@@ -273,11 +334,144 @@ int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, doub
   if (s.status == 2) {
     // Negative curvature (truncated CG, as in Newton-CG for minimisation): keep the iterate
     // reached so far; at the first iteration return the preconditioned residual direction.
-    if (s.it == 0) CU(cudaMemcpyAsync(x + o, w.p + o, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
+    if (s.it == 0) CU(cudaMemcpyAsync(x + o, pbuf[1] + o, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
     fail(SFEM_ERR_BREAKDOWN, "non-positive curvature p.Ap = %g in CG at iteration %d", s.pq, s.it);
     return SFEM_NEGATIVE_CURVATURE;
   }
   return s.status == 1 ? SFEM_NOT_CONVERGED : SFEM_OK;
+}
+
+// Morton order of element centroids, cut greedily into patches of at most
+// kPatchElems elements and kPatchNodes distinct nodes.
+struct PatchBuild {
+  std::vector<int32_t> perm;  // patch position -> caller's element index
+  std::vector<int64_t> elem_off, node_off;
+  std::vector<int32_t> pnode, pdest, bnode, bptr;
+  std::vector<uint16_t> lptr, lent;
+  std::vector<ushort4> lidx;
+};
+
+uint32_t spread3(uint32_t v) {  // 10 bits -> every third bit
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+void build_patches(const std::vector<int4>& tt, const std::vector<double>& x0, int64_t N, int64_t nbc, PatchBuild& pb) {
+  const size_t E = tt.size();
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int64_t i = 0; i < N; i++)
+    for (int c = 0; c < 3; c++) {
+      lo[c] = std::min(lo[c], x0[3 * i + c]);
+      hi[c] = std::max(hi[c], x0[3 * i + c]);
+    }
+  std::vector<uint32_t> key(E);
+  for (size_t e = 0; e < E; e++) {
+    const int32_t t[4] = {tt[e].x, tt[e].y, tt[e].z, tt[e].w};
+    uint32_t q[3];
+    for (int c = 0; c < 3; c++) {
+      double m = 0.25 * (x0[3 * (size_t)t[0] + c] + x0[3 * (size_t)t[1] + c] + x0[3 * (size_t)t[2] + c] +
+                         x0[3 * (size_t)t[3] + c]);
+      double f = hi[c] > lo[c] ? (m - lo[c]) / (hi[c] - lo[c]) : 0.0;
+      q[c] = (uint32_t)std::min(1023.0, std::max(0.0, f * 1024.0));
+    }
+    key[e] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+  }
+  std::vector<int32_t> order(E);
+  for (size_t e = 0; e < E; e++) order[e] = (int32_t)e;
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+
+  std::vector<int32_t> mark(N, -1), local(N, 0), cnt(N, 0);
+  pb.perm.clear();
+  pb.elem_off.assign(1, 0);
+  pb.node_off.assign(1, 0);
+  pb.pnode.clear();
+  pb.lptr.clear();
+  pb.lent.assign(4 * E, 0);
+  pb.lidx.assign(E, make_ushort4(0, 0, 0, 0));
+  pb.perm.reserve(E);
+  size_t k = 0;
+  int32_t c = 0;
+  std::vector<int32_t> nodes;
+  while (k < E) {
+    nodes.clear();
+    const size_t e0 = k;
+    while (k < E && (int64_t)(k - e0) < kPatchElems) {
+      const int4 t4 = tt[order[k]];
+      const int32_t t[4] = {t4.x, t4.y, t4.z, t4.w};
+      int fresh = 0;
+      for (int j = 0; j < 4; j++)
+        if (mark[t[j]] != c) {
+          bool dup = false;
+          for (int i = 0; i < j; i++) dup |= (t[i] == t[j]);
+          fresh += dup ? 0 : 1;
+        }
+      if ((int64_t)nodes.size() + fresh > kPatchNodes) break;
+      for (int j = 0; j < 4; j++)
+        if (mark[t[j]] != c) {
+          mark[t[j]] = c;
+          nodes.push_back(t[j]);
+        }
+      pb.perm.push_back(order[k]);
+      k++;
+    }
+    std::sort(nodes.begin(), nodes.end());
+    for (size_t j = 0; j < nodes.size(); j++) {
+      local[nodes[j]] = (int32_t)j;
+      cnt[nodes[j]]++;
+    }
+    // local corner ids and the local node -> (element, corner) CSR in element order
+    const size_t ne = k - e0, nn = nodes.size();
+    std::vector<uint16_t> deg(nn + 1, 0);
+    for (size_t i = 0; i < ne; i++) {
+      const int4 t4 = tt[pb.perm[e0 + i]];
+      ushort4 l = make_ushort4((unsigned short)local[t4.x], (unsigned short)local[t4.y], (unsigned short)local[t4.z],
+                               (unsigned short)local[t4.w]);
+      pb.lidx[e0 + i] = l;
+      deg[l.x + 1]++; deg[l.y + 1]++; deg[l.z + 1]++; deg[l.w + 1]++;
+    }
+    for (size_t j = 0; j < nn; j++) deg[j + 1] += deg[j];
+    std::vector<uint16_t> fill(deg.begin(), deg.end() - 1);
+    for (size_t i = 0; i < ne; i++) {
+      const ushort4 l = pb.lidx[e0 + i];
+      const unsigned short li[4] = {l.x, l.y, l.z, l.w};
+      for (int j = 0; j < 4; j++) pb.lent[4 * e0 + fill[li[j]]++] = (uint16_t)((i << 2) | j);
+    }
+    for (size_t j = 0; j <= nn; j++) pb.lptr.push_back(deg[j]);
+    for (size_t j = 0; j < nn; j++) pb.pnode.push_back(nodes[j]);
+    pb.elem_off.push_back((int64_t)k);
+    pb.node_off.push_back((int64_t)pb.pnode.size());
+    c++;
+  }
+  // shared nodes: flagged in pnode; the partials of a shared free node are stored
+  // contiguously (in patch order) for the boundary pass: pdest[slot] is the position
+  std::vector<std::vector<int64_t>> slots_of;
+  std::vector<int64_t> bid(N, -1);
+  pb.bnode.clear();
+  pb.pdest.assign(pb.pnode.size(), -1);
+  for (size_t sl = 0; sl < pb.pnode.size(); sl++) {
+    const int32_t g = pb.pnode[sl];
+    if (cnt[g] > 1) {
+      pb.pnode[sl] = ~g;
+      if (g >= nbc) {
+        if (bid[g] < 0) {
+          bid[g] = (int64_t)pb.bnode.size();
+          pb.bnode.push_back(g);
+          slots_of.emplace_back();
+        }
+        slots_of[bid[g]].push_back((int64_t)sl);
+      }
+    }
+  }
+  pb.bptr.assign(1, 0);
+  int32_t pos = 0;
+  for (auto& v : slots_of) {
+    for (int64_t sl : v) pb.pdest[sl] = pos++;
+    pb.bptr.push_back(pos);
+  }
 }
 
 int check_handle(const sfem_handle* h) {
@@ -318,12 +512,14 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   if (cfg->material < 0 || cfg->material > 3) return fail(SFEM_ERR_INVALID, "unsupported material %d", cfg->material);
   if (cfg->precision != SFEM_FP64 && cfg->precision != SFEM_FP32)
     return fail(SFEM_ERR_INVALID, "unsupported precision %d", cfg->precision);
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SFEM_ERR_NO_DEVICE, "no CUDA device");
   for (int64_t i = 0; i < 4 * n_tets; i++)
     if (tets_in[i] < 0 || tets_in[i] >= n_nodes) return fail(SFEM_ERR_INVALID, "tet index out of range at %lld", (long long)i);
   for (int64_t i = 0; i < n_fixed; i++)
     if (fixed[i] < 0 || fixed[i] >= n_nodes) return fail(SFEM_ERR_INVALID, "fixed index out of range");
+  if (!(cfg->young > 0) || !(cfg->poisson > -1.0 && cfg->poisson < 0.5) || !(cfg->density >= 0))
+    return fail(SFEM_ERR_INVALID, "invalid material parameters (E > 0, -1 < nu < 0.5, rho >= 0)");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SFEM_ERR_NO_DEVICE, "no CUDA device");
 
   sfem_handle* h = new sfem_handle();
   h->device = cfg->device;
@@ -406,6 +602,27 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   // lumped masses as the reference stores them (mass = 1 / (1 / m)), fixed nodes 0
   for (int64_t i = 0; i < n_nodes; i++) mass[i] = (i < h->nbc || mass[i] == 0) ? 0.0 : 1.0 / (1.0 / mass[i]);
 
+  // ---- element patches: Morton order, elements stored in patch order from here on ----
+  PatchBuild pbld;
+  build_patches(tt, x0, n_nodes, h->nbc, pbld);
+  {
+    std::vector<int4> ttp(E);
+    std::vector<double> Xp(9 * E), volp(E);
+    for (size_t k2 = 0; k2 < E; k2++) {
+      const int32_t e = pbld.perm[k2];
+      ttp[k2] = tt[e];
+      volp[k2] = vol[e];
+      for (int q = 0; q < 9; q++) Xp[q * E + k2] = X[q * E + e];
+    }
+    tt.swap(ttp);
+    X.swap(Xp);
+    vol.swap(volp);
+  }
+  h->perm_h = pbld.perm;
+  h->n_patches = (int64_t)pbld.elem_off.size() - 1;
+  h->n_slots = (int64_t)pbld.pnode.size();
+  h->n_shared = (int64_t)pbld.bnode.size();
+
   // ---- node -> element CSR (entries in element order) ----
   std::vector<int64_t> ptr(n_nodes + 1, 0), ent(4 * E);
   for (size_t e = 0; e < E; e++) {
@@ -428,7 +645,14 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
       (st = dalloc(&h->u, N3)) || (st = dalloc(&h->mass, (size_t)n_nodes)) || (st = dalloc(&h->fext, N3)) ||
       (st = dalloc(&h->grav_d, 3)) || (st = dalloc(&h->csr_ptr, (size_t)n_nodes + 1)) ||
       (st = dalloc(&h->csr_ent, 4 * E)) || (st = dalloc(&h->fe, 12 * E)) ||
-      (st = dalloc(&h->partials, 4 * (size_t)kMaxBlocks)) || (st = dalloc(&h->counter, 1)) ||
+      (st = dalloc(&h->partials, std::max<size_t>(4 * (size_t)kMaxBlocks, (size_t)h->n_patches + kMaxBlocks))) ||
+      (st = dalloc(&h->counter, 1)) || (st = dalloc(&h->perm, E)) || (st = dalloc(&h->etmp, E)) ||
+      (st = dalloc(&h->elem_off, (size_t)h->n_patches + 1)) || (st = dalloc(&h->node_off, (size_t)h->n_patches + 1)) ||
+      (st = dalloc(&h->pnode, (size_t)h->n_slots)) || (st = dalloc(&h->pdest, (size_t)h->n_slots)) ||
+      (st = dalloc(&h->lptr, (size_t)(h->n_slots + h->n_patches))) ||
+      (st = dalloc(&h->lent, 4 * E)) || (st = dalloc(&h->lidx, E)) || (st = dalloc(&h->partial, 3 * (size_t)h->n_slots)) ||
+      (st = dalloc(&h->bnode, (size_t)h->n_shared)) || (st = dalloc(&h->bptr, (size_t)h->n_shared + 1)) ||
+      (st = dalloc(&h->bidx, (size_t)n_nodes)) ||
       (st = dalloc(&h->scal, 1)) || (st = dalloc(&h->dres, 8)) || (st = dalloc(&h->ninv, 1)) ||
       (st = dalloc(&h->r64, N3)) || (st = dalloc(&h->ubase, N3)) || (st = dalloc(&h->tmp64, N3)) ||
       (st = dalloc(&h->tmp64b, N3)))
@@ -453,6 +677,19 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   UP(h->grav_d, h->grav, 3 * sizeof(double));
   UP(h->csr_ptr, ptr.data(), ptr.size() * sizeof(int64_t));
   UP(h->csr_ent, ent.data(), ent.size() * sizeof(int64_t));
+  UP(h->perm, pbld.perm.data(), E * sizeof(int32_t));
+  UP(h->elem_off, pbld.elem_off.data(), pbld.elem_off.size() * sizeof(int64_t));
+  UP(h->node_off, pbld.node_off.data(), pbld.node_off.size() * sizeof(int64_t));
+  UP(h->pnode, pbld.pnode.data(), pbld.pnode.size() * sizeof(int32_t));
+  UP(h->lptr, pbld.lptr.data(), pbld.lptr.size() * sizeof(uint16_t));
+  UP(h->lent, pbld.lent.data(), pbld.lent.size() * sizeof(uint16_t));
+  UP(h->lidx, pbld.lidx.data(), pbld.lidx.size() * sizeof(ushort4));
+  UP(h->pdest, pbld.pdest.data(), pbld.pdest.size() * sizeof(int32_t));
+  if (h->n_shared > 0) UP(h->bnode, pbld.bnode.data(), pbld.bnode.size() * sizeof(int32_t));
+  UP(h->bptr, pbld.bptr.data(), pbld.bptr.size() * sizeof(int32_t));
+  std::vector<int32_t> bidx_h((size_t)n_nodes, -1);
+  for (size_t i = 0; i < pbld.bnode.size(); i++) bidx_h[pbld.bnode[i]] = (int32_t)i;
+  UP(h->bidx, bidx_h.data(), bidx_h.size() * sizeof(int32_t));
 #undef UP
   double* zero_bufs[] = {h->u, h->fext, h->r64, h->ubase, h->tmp64, h->tmp64b};
   for (double* z : zero_bufs)
@@ -471,11 +708,18 @@ int sfem_destroy(sfem_handle* h) {
   if (!h) return SFEM_OK;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm};
+  for (void* b : ibufs)
+    if (b) cudaFree(b);
+  void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
+                   h->partial, h->bnode, h->bptr, h->bidx};
+  for (void* b : pbufs)
+    if (b) cudaFree(b);
   void* bufs[] = {h->tets, h->X64, h->vol64, h->scale64, h->young_e, h->X32, h->vol32, h->scale32, h->x0, h->u,
                   h->mass, h->fext, h->grav_d, h->csr_ptr, h->csr_ent, h->fe, h->partials, h->counter, h->scal,
                   h->dres, h->ninv, h->r64, h->ubase, h->tmp64, h->tmp64b, h->k64.b, h->k64.x, h->k64.r, h->k64.p,
                   h->k64.q, h->k64.dinv, h->k64.u, h->k32.b, h->k32.x, h->k32.r, h->k32.p, h->k32.q, h->k32.dinv,
-                  h->k32.u};
+                  h->k32.u, h->k64.p2, h->k64.ones, h->k32.p2, h->k32.ones};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->scal_h) cudaFreeHost(h->scal_h);
@@ -484,6 +728,7 @@ int sfem_destroy(sfem_handle* h) {
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (cudaEvent_t e : h->pev)
     if (e) cudaEventDestroy(e);
+  if (h->gnn) gnn_free(h->gnn);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return SFEM_OK;
@@ -645,8 +890,8 @@ int sfem_set_element_youngs(sfem_handle* h, const double* young_e) {
     TRY(dalloc(&h->scale64, (size_t)h->E));
     TRY(dalloc(&h->scale32, (size_t)h->E));
   }
-  CU(cudaMemcpyAsync(h->young_e, young_e, (size_t)h->E * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  TRY(sfem_set_element_youngs_dev(h, h->young_e));
+  CU(cudaMemcpyAsync(h->etmp, young_e, (size_t)h->E * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TRY(sfem_set_element_youngs_dev(h, h->etmp));
   return sync(h);
 }
 
@@ -657,11 +902,12 @@ int sfem_set_element_youngs_dev(sfem_handle* h, const double* young_e_dev) {
     TRY(dalloc(&h->scale64, (size_t)h->E));
     TRY(dalloc(&h->scale32, (size_t)h->E));
   }
-  if (young_e_dev != h->young_e)
-    CU(cudaMemcpyAsync(h->young_e, young_e_dev, (size_t)h->E * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  // caller's element order -> patch order
+  launch_permute(h->E, h->perm, young_e_dev, h->young_e, h->stream);
   launch_scale_copy(h->E, 1.0 / h->young, h->young_e, h->scale64, h->stream);
   launch_convert<double, float>(h->E, h->scale64, h->scale32, h->stream);
   h->has_scale = true;
+  h->has_scale_la = false;
   CU(cudaGetLastError());
   return SFEM_OK;
 }
@@ -710,8 +956,7 @@ int sfem_matvec_dev(sfem_handle* h, const double* d_dev, double* Kd_dev) {
   // direction with zero fixed-node block
   CU(cudaMemsetAsync(h->tmp64, 0, o * sizeof(double), h->stream));
   CU(cudaMemcpyAsync(h->tmp64 + o, d_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-  element_pass<double>(h, MODE_HVP, h->u, h->tmp64, h->fe, nullptr, nullptr, nullptr);
-  launch_gather_hvp<double>(h->nbc, h->N, h->csr(), h->fe, h->tmp64, h->tmp64b, h->red(), nullptr, h->stream);
+  hvp<double>(h, h->u, h->tmp64, h->tmp64b, nullptr);
   CU(cudaMemcpyAsync(Kd_dev, h->tmp64b + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
   CU(cudaGetLastError());
   return SFEM_OK;
@@ -778,7 +1023,7 @@ int sfem_element_stress(sfem_handle* h, double* P) {
   std::vector<double> tmp(12 * (size_t)h->E);
   CU(cudaMemcpyAsync(tmp.data(), h->fe, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
-  for (int64_t e = 0; e < h->E; e++) memcpy(P + 9 * (size_t)e, &tmp[12 * (size_t)e], 9 * sizeof(double));
+  for (int64_t k = 0; k < h->E; k++) memcpy(P + 9 * (size_t)h->perm_h[k], &tmp[12 * (size_t)k], 9 * sizeof(double));
   return SFEM_OK;
 }
 
@@ -841,11 +1086,14 @@ int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* op
 // -----------------------------------------------------------------------------
 // Newton
 // -----------------------------------------------------------------------------
+int sfem_gnn_inner_solve(sfem_handle* h, double eta, int max_cg, int* its);
+
 namespace {
 
 // one inner solve K dx = r64 at the current state, in the handle's precision;
 // the step ends up in h->tmp64 (FP64, full length).
 int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
+  if (precond == SFEM_PC_LEARNED) return sfem_gnn_inner_solve(h, eta, max_cg, its);
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
   const bool pc = precond == SFEM_PC_JACOBI;
   sfem_pcg_stats ps{};
@@ -991,7 +1239,8 @@ int sfem_newton_solve(sfem_handle* h, const sfem_newton_opts* opts, sfem_newton_
   TRY(check_handle(h));
   TRY(set_device(h));
   if (!opts) return fail(SFEM_ERR_INVALID, "opts is null");
-  if (opts->precond == SFEM_PC_LEARNED) return fail(SFEM_ERR_INVALID, "learned preconditioner not loaded");
+  if (opts->precond == SFEM_PC_LEARNED && !h->gnn)
+    return fail(SFEM_ERR_INVALID, "learned preconditioner not initialised (sfem_gnn_init)");
   sfem_newton_opts op = *opts;
   if (op.eta_max <= 0) op.eta_max = 0.5;
   if (op.eta_min <= 0) op.eta_min = h->precision == SFEM_FP32 ? 1e-5 : 1e-10;
@@ -1070,8 +1319,7 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
       double deltaD;
       TRY(dot(d, d, &deltaD));
       for (int inner = 0; inner < inner_iters; inner++) {
-        element_pass<double>(h, MODE_HVP, h->u, d, h->fe, nullptr, nullptr, nullptr);
-        launch_gather_hvp<double>(h->nbc, h->N, h->csr(), h->fe, d, df, h->red(), nullptr, h->stream);
+        hvp<double>(h, h->u, d, df, nullptr);
         double rd, ddf;
         TRY(dot(h->r64, d, &rd));
         TRY(dot(d, df, &ddf));
@@ -1100,6 +1348,8 @@ int sfem_adjoint_dev(sfem_handle* h, const double* dLdu_dev, double rel_tol, int
   TRY(check_handle(h));
   if (h->material == SFEM_MMT_COROTATIONAL)
     return fail(SFEM_ERR_INVALID, "adjoint needs a symmetric tangent (the corotational force has none)");
+  if (h->has_scale && h->has_scale_la)
+    return fail(SFEM_ERR_INVALID, "dL/dE assumes a uniform Poisson ratio (per-element Lame parameters are set)");
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
   KrylovWs<double>& w = h->k64;
   CU(cudaMemcpyAsync(w.b + o, dLdu_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -1122,7 +1372,7 @@ int sfem_adjoint_dev(sfem_handle* h, const double* dLdu_dev, double rel_tol, int
     CU(cudaMemcpyAsync(h->young_e, ye.data(), ye.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     TRY(sync(h));
   }
-  launch_adjoint_elem(h->tets, h->E, h->nbc, h->fe, w.x, h->young_e, dLdE_dev, h->stream);
+  launch_adjoint_elem(h->tets, h->E, h->nbc, h->fe, w.x, h->young_e, h->perm, dLdE_dev, h->stream);
   // dL/df = ff * lambda
   launch_scale_copy((int64_t)n, h->ff, w.x + o, dLdf_dev, h->stream);
   CU(cudaGetLastError());
@@ -1151,6 +1401,487 @@ int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max
   cudaFree(dE);
   cudaFree(dfp);
   return st;
+}
+
+}  // extern "C"
+
+// =============================================================================
+// Learned preconditioner (extension; the reference has no learned components)
+// =============================================================================
+namespace {
+
+struct GnnState {
+  int64_t n = 0;  // free nodes
+  int32_t *ptr = nullptr, *idx = nullptr;
+  float* inv_deg = nullptr;
+  uint8_t* fixed_nb = nullptr;
+  float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+  __nv_bfloat16 *Wb = nullptr, *Wtb = nullptr;
+  __nv_bfloat16* h[gnn::NL + 1] = {};
+  __nv_bfloat16* u[gnn::NL + 1] = {};
+  float* x = nullptr;
+  float *G0 = nullptr, *G1 = nullptr, *G2 = nullptr;
+  float* wpart = nullptr;
+  float* spart = nullptr;
+  unsigned* scount = nullptr;
+  gnn::Scalars* sc = nullptr;
+  float* losses = nullptr;  // device, one per training step
+  int64_t losses_cap = 0;
+  float *z = nullptr, *rprev = nullptr;  // FCG vectors (3N)
+  std::vector<float*> R, Ee;             // dataset: residual and correction (free block, 3n)
+  std::vector<float> cinv;               // 1 / (e . r) per sample
+  int adam_t = 0;
+  bool train_bufs = false;
+  gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg}; }
+};
+
+void gnn_free(GnnState* g) {
+  void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->fixed_nb, g->params, g->grad, g->m, g->v, g->Wb, g->Wtb,
+                  g->x, g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->sc, g->losses, g->z, g->rprev};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  for (int l = 0; l <= gnn::NL; l++) {
+    if (g->h[l]) cudaFree(g->h[l]);
+    if (g->u[l]) cudaFree(g->u[l]);
+  }
+  for (float* b : g->R) cudaFree(b);
+  for (float* b : g->Ee) cudaFree(b);
+  delete g;
+}
+
+int gnn_need(const sfem_handle* h) {
+  if (!h->gnn) return fail(SFEM_ERR_INVALID, "learned preconditioner not initialised (sfem_gnn_init)");
+  if (h->precision != SFEM_FP32) return fail(SFEM_ERR_INVALID, "the learned preconditioner runs in FP32 handles");
+  return 0;
+}
+
+int gnn_train_buffers(sfem_handle* h) {
+  GnnState* g = h->gnn;
+  if (g->train_bufs) return 0;
+  const size_t nh = (size_t)g->n * gnn::H;
+  for (int l = 0; l <= gnn::NL; l++) TRY(dalloc(&g->u[l], nh));
+  TRY(dalloc(&g->x, (size_t)g->n * gnn::FIN));
+  TRY(dalloc(&g->G0, nh));
+  TRY(dalloc(&g->G1, nh));
+  TRY(dalloc(&g->G2, nh));
+  const size_t nb = (size_t)((g->n + gnn::TILE - 1) / gnn::TILE);
+  TRY(dalloc(&g->wpart, std::max(nb * gnn::LPART, (size_t)((g->n + 255) / 256) * (3 * gnn::H + 3))));
+  g->train_bufs = true;
+  return 0;
+}
+
+// current Jacobi diagonal (FP32) into k32.dinv and its log-mean statistic
+int gnn_refresh_diag(sfem_handle* h) {
+  GnnState* g = h->gnn;
+  TRY(jacobi<float>(h, h->k32.dinv, nullptr));
+  const size_t o = 3 * (size_t)h->nbc;
+  gnn::launch_stat(0, 3 * g->n, nullptr, h->k32.dinv + o, g->spart, g->scount, g->sc, nullptr, h->stream);
+  CU(cudaGetLastError());
+  return 0;
+}
+
+// out = M(r) over the free block (r, out point at free-block starts); done may be null
+void gnn_apply_dev(sfem_handle* h, const float* r, float* out, const int* done, bool train) {
+  GnnState* g = h->gnn;
+  const size_t o = 3 * (size_t)h->nbc;
+  const float* dinv = h->k32.dinv + o;
+  gnn::launch_stat(1, 3 * g->n, r, dinv, g->spart, g->scount, g->sc, done, h->stream);
+  gnn::launch_forward(g->graph(), r, dinv, g->fixed_nb, g->params, g->Wb, g->sc, g->h, train ? g->u : nullptr,
+                      train ? g->x : nullptr, out, done, h->stream);
+}
+
+// loss of one sample (energy norm) and the parameter gradient into g->grad; loss into *loss_dev
+int gnn_loss_grad_dev(sfem_handle* h, const float* r, const float* e, float cinv, float* loss_dev) {
+  GnnState* g = h->gnn;
+  TRY(gnn_train_buffers(h));
+  KrylovWs<float>& w = h->k32;
+  const size_t o = 3 * (size_t)h->nbc, n3 = 3 * (size_t)g->n;
+  float* out = g->z + o;
+  gnn_apply_dev(h, r, out, nullptr, true);
+  // d = M(r) - e into a full-length vector with a zero fixed block, q = K d
+  gnn::launch_sub((int64_t)n3, out, e, w.b + o, h->stream);
+  hvp<float>(h, w.u, w.b, w.q, nullptr);
+  float* Go = g->rprev + o;
+  gnn::launch_loss((int64_t)n3, w.b + o, w.q + o, cinv, Go, g->spart, g->scount, loss_dev, h->stream);
+  gnn::launch_backward(g->graph(), Go, g->params, g->Wtb, g->sc, g->h, g->u, g->x, g->G0, g->G1, g->G2, g->wpart,
+                       g->grad, h->stream);
+  CU(cudaGetLastError());
+  return 0;
+}
+
+// Flexible CG (Polak-Ribiere beta) with the learned preconditioner, FP32; b, x full length
+int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it, sfem_pcg_stats* st) {
+  GnnState* g = h->gnn;
+  KrylovWs<float>& w = h->k32;
+  const int64_t o = 3 * h->nbc, n = 3 * h->nf;
+  CgScalars s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.tol2 = tol * tol;
+  s0.max_it = max_it;
+  *h->scal_h = s0;
+  CU(cudaMemcpyAsync(h->scal, h->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
+  launch_cg_init<float>(n, b + o, x + o, w.r + o, w.p + o, w.dinv + o, h->red(), h->scal, h->stream);
+  const int* done = &h->scal->done;
+  gnn_apply_dev(h, w.r + o, g->z + o, done, false);
+  gnn::launch_fcg_init(n, w.r + o, g->z + o, w.p + o, reinterpret_cast<float*>(h->partials), h->counter, h->scal,
+                       h->stream);
+  const int check_every = 16;
+  int it = 0;
+  bool pending = false;
+  if (h->profiling) h->prof_precision = SFEM_FP32;
+  for (;;) {
+    CU(cudaMemcpyAsync(h->scal_h, h->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    if (h->scal_h->done || it >= max_it) break;
+    if (pending) {
+      float a = 0, b = 0;
+      cudaEventElapsedTime(&a, h->pev[0], h->pev[1]);
+      cudaEventElapsedTime(&b, h->pev[1], h->pev[2]);
+      h->prof_elem_ms += a;
+      h->prof_gather_ms += b;
+      h->prof_samples++;
+      pending = false;
+    }
+    for (int k = 0; k < check_every && it < max_it; k++, it++) {
+      const bool sample = h->profiling && k == 0;
+      if (sample) CU(cudaEventRecord(h->pev[0], h->stream));
+      hvp<float>(h, w.u, w.p, w.q, h->scal, sample ? h->pev[1] : nullptr);
+      if (sample) {
+        CU(cudaEventRecord(h->pev[2], h->stream));
+        pending = true;
+      }
+      if (h->profiling) h->prof_launches++;
+      gnn::launch_fcg_update(n, x + o, w.r + o, g->rprev + o, w.p + o, w.q + o,
+                             reinterpret_cast<float*>(h->partials), h->counter, h->scal, h->stream);
+      gnn_apply_dev(h, w.r + o, g->z + o, done, false);
+      gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, w.dinv + o, reinterpret_cast<float*>(h->partials),
+                           h->counter, h->scal, h->stream);
+      gnn::launch_fcg_dir(n, g->z + o, w.r + o, w.dinv + o, w.p + o, h->scal, h->stream);
+    }
+  }
+  if (pending) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, h->pev[0], h->pev[1]);
+    cudaEventElapsedTime(&b, h->pev[1], h->pev[2]);
+    h->prof_elem_ms += a;
+    h->prof_gather_ms += b;
+    h->prof_samples++;
+  }
+  const CgScalars& s = *h->scal_h;
+  if (st) {
+    st->iters = s.it;
+    st->status = s.status;
+    st->rel_res = s.bb > 0 ? std::sqrt(s.rr / s.bb) : 0.0;
+  }
+  if (s.status == -3) return fail(SFEM_ERR_NAN, "non-finite value in the flexible Krylov recurrence");
+  if (s.status == 2) {
+    if (s.it == 0) CU(cudaMemcpyAsync(x + o, w.p + o, n * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    return SFEM_NEGATIVE_CURVATURE;
+  }
+  return s.status == 1 ? SFEM_NOT_CONVERGED : SFEM_OK;  // status 3: non-descent direction, keep iterate
+}
+
+}  // namespace
+
+// learned inner solve of the Newton driver (declared before inner_solve's use below)
+int sfem_gnn_inner_solve(sfem_handle* h, double eta, int max_cg, int* its) {
+  TRY(gnn_need(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  KrylovWs<float>& w = h->k32;
+  launch_convert<double, float>(3 * h->N, h->u, w.u, h->stream);
+  launch_convert<double, float>((int64_t)n, h->r64 + o, w.b + o, h->stream);
+  TRY(gnn_refresh_diag(h));
+  sfem_pcg_stats ps{};
+  int st = fcg_device(h, w.b, w.x, eta, max_cg, &ps);
+  if (st < 0) return st;
+  launch_convert<float, double>((int64_t)n, w.x + o, h->tmp64 + o, h->stream);
+  *its = ps.iters;
+  CU(cudaGetLastError());
+  return 0;
+}
+
+extern "C" {
+
+int sfem_gnn_num_params(int32_t* n) {
+  if (!n) return fail(SFEM_ERR_INVALID, "null");
+  *n = gnn::NPARAM;
+  return SFEM_OK;
+}
+
+int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (h->precision != SFEM_FP32) return fail(SFEM_ERR_INVALID, "the learned preconditioner runs in FP32 handles");
+  if (h->gnn) {
+    gnn_free(h->gnn);
+    h->gnn = nullptr;
+  }
+  GnnState* g = new GnnState();
+  h->gnn = g;
+  const int64_t nbc = h->nbc, n = h->nf;
+  g->n = n;
+  // free-node graph from the element edges, fixed-neighbour flags
+  std::vector<int4> tt((size_t)h->E);
+  CU(cudaMemcpyAsync(tt.data(), h->tets, tt.size() * sizeof(int4), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  std::vector<uint64_t> edges;
+  edges.reserve(tt.size() * 12);
+  std::vector<uint8_t> fnb((size_t)n, 0);
+  for (const int4& t4 : tt) {
+    const int32_t v[4] = {t4.x, t4.y, t4.z, t4.w};
+    for (int a = 0; a < 4; a++)
+      for (int b = 0; b < 4; b++) {
+        if (a == b) continue;
+        if (v[a] >= nbc && v[b] >= nbc)
+          edges.push_back(((uint64_t)(v[a] - nbc) << 32) | (uint32_t)(v[b] - nbc));
+        else if (v[a] >= nbc && v[b] < nbc)
+          fnb[v[a] - nbc] = 1;
+      }
+  }
+  std::sort(edges.begin(), edges.end());
+  edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+  std::vector<int32_t> ptr((size_t)n + 1, 0), idx(edges.size());
+  for (size_t k = 0; k < edges.size(); k++) {
+    ptr[(edges[k] >> 32) + 1]++;
+    idx[k] = (int32_t)(edges[k] & 0xffffffffu);
+  }
+  for (int64_t i = 0; i < n; i++) ptr[i + 1] += ptr[i];
+  std::vector<float> invdeg((size_t)n);
+  for (int64_t i = 0; i < n; i++) invdeg[i] = 1.f / (float)std::max(1, ptr[i + 1] - ptr[i]);
+  // He-initialised weights, zero biases, zero decoder (starts as Jacobi)
+  std::vector<float> prm(gnn::NPARAM, 0.f);
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<float> nd(0.f, 1.f);
+  for (int i = 0; i < gnn::H * gnn::FIN; i++) prm[gnn::OFF_WE + i] = nd(rng) * std::sqrt(2.f / gnn::FIN);
+  for (int l = 0; l < gnn::NL; l++)
+    for (int i = 0; i < gnn::H * gnn::AIN; i++)
+      prm[gnn::OFF_L + l * gnn::L_STRIDE + i] = nd(rng) * std::sqrt(2.f / gnn::AIN) * 0.5f;
+  const size_t nh = (size_t)n * gnn::H;
+  TRY(dalloc(&g->ptr, ptr.size()));
+  TRY(dalloc(&g->idx, std::max<size_t>(idx.size(), 1)));
+  TRY(dalloc(&g->inv_deg, (size_t)n));
+  TRY(dalloc(&g->fixed_nb, (size_t)n));
+  TRY(dalloc(&g->params, gnn::NPARAM));
+  TRY(dalloc(&g->grad, gnn::NPARAM));
+  TRY(dalloc(&g->m, gnn::NPARAM));
+  TRY(dalloc(&g->v, gnn::NPARAM));
+  TRY(dalloc(&g->Wb, (size_t)gnn::NL * gnn::H * gnn::AIN));
+  TRY(dalloc(&g->Wtb, (size_t)gnn::NL * gnn::H * gnn::AIN));
+  for (int l = 0; l <= gnn::NL; l++) TRY(dalloc(&g->h[l], nh));
+  TRY(dalloc(&g->spart, 4096));
+  TRY(dalloc(&g->scount, 1));
+  TRY(dalloc(&g->sc, 1));
+  TRY(dalloc(&g->z, 3 * (size_t)h->N));
+  TRY(dalloc(&g->rprev, 3 * (size_t)h->N));
+  CU(cudaMemcpyAsync(g->ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  if (!idx.empty())
+    CU(cudaMemcpyAsync(g->idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(g->inv_deg, invdeg.data(), invdeg.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(g->fixed_nb, fnb.data(), fnb.size(), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(g->params, prm.data(), prm.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemsetAsync(g->m, 0, gnn::NPARAM * sizeof(float), h->stream));
+  CU(cudaMemsetAsync(g->v, 0, gnn::NPARAM * sizeof(float), h->stream));
+  CU(cudaMemsetAsync(g->scount, 0, sizeof(unsigned), h->stream));
+  CU(cudaMemsetAsync(g->z, 0, 3 * (size_t)h->N * sizeof(float), h->stream));
+  CU(cudaMemsetAsync(g->rprev, 0, 3 * (size_t)h->N * sizeof(float), h->stream));
+  gnn::launch_pack(g->params, g->Wb, g->Wtb, h->stream);
+  return sync(h);
+}
+
+int sfem_gnn_get_params(sfem_handle* h, float* params) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  CU(cudaMemcpyAsync(params, h->gnn->params, gnn::NPARAM * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int sfem_gnn_set_params(sfem_handle* h, const float* params) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  CU(cudaMemcpyAsync(h->gnn->params, params, gnn::NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  gnn::launch_pack(h->gnn->params, h->gnn->Wb, h->gnn->Wtb, h->stream);
+  h->gnn->adam_t = 0;
+  CU(cudaMemsetAsync(h->gnn->m, 0, gnn::NPARAM * sizeof(float), h->stream));
+  CU(cudaMemsetAsync(h->gnn->v, 0, gnn::NPARAM * sizeof(float), h->stream));
+  return sync(h);
+}
+
+// M(r) at the current state (Jacobi diagonal of the current tangent); free-DOF vectors
+int sfem_gnn_apply(sfem_handle* h, const double* r_free, double* out_free) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  TRY(gnn_need(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  KrylovWs<float>& w = h->k32;
+  launch_convert<double, float>(3 * h->N, h->u, w.u, h->stream);
+  TRY(gnn_refresh_diag(h));
+  CU(cudaMemcpyAsync(h->tmp64 + o, r_free, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_convert<double, float>((int64_t)n, h->tmp64 + o, w.r + o, h->stream);
+  gnn_apply_dev(h, w.r + o, h->gnn->z + o, nullptr, false);
+  launch_convert<float, double>((int64_t)n, h->gnn->z + o, h->tmp64b + o, h->stream);
+  CU(cudaMemcpyAsync(out_free, h->tmp64b + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+// one sample's energy-norm loss ||M(r) - e||_K^2 / (e.r) and its parameter gradient
+int sfem_gnn_loss_grad(sfem_handle* h, const double* r_free, const double* e_free, double* loss, float* grad) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  TRY(gnn_need(h));
+  GnnState* g = h->gnn;
+  TRY(gnn_train_buffers(h));
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  KrylovWs<float>& w = h->k32;
+  launch_convert<double, float>(3 * h->N, h->u, w.u, h->stream);
+  TRY(gnn_refresh_diag(h));
+  std::vector<double> er(n);
+  std::vector<double> rh(r_free, r_free + n), eh(e_free, e_free + n);
+  double c = 0;
+  for (size_t i = 0; i < n; i++) c += eh[i] * rh[i];
+  float *rd = nullptr, *ed = nullptr, *ld = nullptr;
+  TRY(dalloc(&rd, n));
+  TRY(dalloc(&ed, n));
+  TRY(dalloc(&ld, 1));
+  CU(cudaMemcpyAsync(h->tmp64 + o, r_free, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_convert<double, float>((int64_t)n, h->tmp64 + o, rd, h->stream);
+  CU(cudaMemcpyAsync(h->tmp64b + o, e_free, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_convert<double, float>((int64_t)n, h->tmp64b + o, ed, h->stream);
+  int st = gnn_loss_grad_dev(h, rd, ed, (float)(1.0 / c), ld);
+  float lf = 0;
+  if (st == 0) {
+    cudaMemcpyAsync(&lf, ld, sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    if (grad) cudaMemcpyAsync(grad, g->grad, gnn::NPARAM * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    st = sync(h);
+  }
+  cudaFree(rd);
+  cudaFree(ed);
+  cudaFree(ld);
+  if (loss) *loss = lf;
+  return st;
+}
+
+// Training pairs from a plain Jacobi-PCG solve (FP32) of K x = b at the current state:
+// every `every` iterations the residual r_j and the iterate x_j are kept, and after the
+// solve e_j = x_final - x_j is the correction that solves K e_j = r_j.  b_free == NULL
+// uses the current nonlinear residual.  Appends up to max_snaps samples.
+int sfem_gnn_collect(sfem_handle* h, const double* b_free, int32_t every, int32_t max_snaps, double rel_tol,
+                     int32_t* n_added) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  TRY(gnn_need(h));
+  GnnState* g = h->gnn;
+  KrylovWs<float>& w = h->k32;
+  const int64_t o = 3 * h->nbc, n = 3 * h->nf;
+  if (every <= 0 || max_snaps <= 0) return fail(SFEM_ERR_INVALID, "every and max_snaps must be positive");
+  launch_convert<double, float>(3 * h->N, h->u, w.u, h->stream);
+  if (b_free) {
+    CU(cudaMemcpyAsync(h->tmp64 + o, b_free, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_convert<double, float>(n, h->tmp64 + o, w.b + o, h->stream);
+  } else {
+    double rn;
+    TRY(residual(h, &rn, nullptr));
+    launch_convert<double, float>(n, h->r64 + o, w.b + o, h->stream);
+  }
+  TRY(jacobi<float>(h, w.dinv, nullptr));
+  // snapshot buffers: r_j then x_j
+  std::vector<float*> rs, xs;
+  CgScalars s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.tol2 = rel_tol * rel_tol;
+  s0.max_it = 50000;  // the solve that labels the pairs; FP32 stalls below ~1e-6 relative
+  *h->scal_h = s0;
+  CU(cudaMemcpyAsync(h->scal, h->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
+  launch_cg_init<float>(n, w.b + o, w.x + o, w.r + o, w.p + o, w.dinv + o, h->red(), h->scal, h->stream);
+  float* pbuf[2] = {w.p, w.p2};
+  int it = 0;
+  for (;;) {
+    CU(cudaMemcpyAsync(h->scal_h, h->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    if (h->scal_h->done) break;
+    if ((int)rs.size() < max_snaps) {
+      float *rj = nullptr, *xj = nullptr;
+      TRY(dalloc(&rj, (size_t)n));
+      TRY(dalloc(&xj, (size_t)n));
+      CU(cudaMemcpyAsync(rj, w.r + o, n * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+      CU(cudaMemcpyAsync(xj, w.x + o, n * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+      rs.push_back(rj);
+      xs.push_back(xj);
+    }
+    for (int k = 0; k < every; k++, it++) {
+      float* pold = pbuf[it % 2];
+      float* pnew = pbuf[(it + 1) % 2];
+      hvp<float>(h, w.u, pold, w.q, h->scal, nullptr, w.r, w.dinv, pnew);
+      launch_cg_update_patch<float>(h->nbc, h->N, h->bidx, h->pb(), reinterpret_cast<const float*>(h->partial), w.x,
+                                    w.r, pnew, w.q, w.dinv, h->red(), h->scal, h->stream);
+    }
+  }
+  // e_j = x_final - x_j, c_j = e_j . r_j
+  int added = 0;
+  for (size_t j = 0; j < rs.size(); j++) {
+    gnn::launch_sub(n, w.x + o, xs[j], xs[j], h->stream);
+    float cf = 0;
+    gnn::launch_loss(n, xs[j], rs[j], 1.f, g->rprev + o, g->spart, g->scount, g->spart + 4000, h->stream);
+    CU(cudaMemcpyAsync(&cf, g->spart + 4000, sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    if (cf > 0.f && std::isfinite(cf)) {
+      g->R.push_back(rs[j]);
+      g->Ee.push_back(xs[j]);
+      g->cinv.push_back(1.f / cf);
+      added++;
+    } else {
+      cudaFree(rs[j]);
+      cudaFree(xs[j]);
+    }
+  }
+  if (n_added) *n_added = added;
+  return SFEM_OK;
+}
+
+int sfem_gnn_dataset_size(sfem_handle* h, int32_t* n) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  *n = (int32_t)h->gnn->R.size();
+  return SFEM_OK;
+}
+
+int sfem_gnn_clear_dataset(sfem_handle* h) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  for (float* b : h->gnn->R) cudaFree(b);
+  for (float* b : h->gnn->Ee) cudaFree(b);
+  h->gnn->R.clear();
+  h->gnn->Ee.clear();
+  h->gnn->cinv.clear();
+  return SFEM_OK;
+}
+
+// Adam training over the collected pairs (one sample per step, drawn with a seeded
+// generator); losses (optional, host) receives every step's loss.
+int sfem_gnn_train(sfem_handle* h, int32_t steps, float lr, uint64_t seed, float* losses) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  TRY(gnn_need(h));
+  GnnState* g = h->gnn;
+  if (g->R.empty()) return fail(SFEM_ERR_INVALID, "no training pairs (sfem_gnn_collect)");
+  TRY(gnn_train_buffers(h));
+  if (g->losses_cap < steps) {
+    if (g->losses) cudaFree(g->losses);
+    TRY(dalloc(&g->losses, (size_t)steps));
+    g->losses_cap = steps;
+  }
+  KrylovWs<float>& w = h->k32;
+  launch_convert<double, float>(3 * h->N, h->u, w.u, h->stream);
+  TRY(gnn_refresh_diag(h));
+  std::mt19937_64 rng(seed);
+  for (int t = 0; t < steps; t++) {
+    const size_t j = (size_t)(rng() % g->R.size());
+    TRY(gnn_loss_grad_dev(h, g->R[j], g->Ee[j], g->cinv[j], g->losses + t));
+    g->adam_t++;
+    gnn::launch_adam(g->grad, g->params, g->m, g->v, lr, g->adam_t, 1.f, g->Wb, g->Wtb, h->stream);
+    if ((t & 63) == 63) TRY(sync(h));
+  }
+  if (losses) CU(cudaMemcpyAsync(losses, g->losses, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
 }
 
 }  // extern "C"

@@ -21,13 +21,15 @@ enum Mode {
 //   tets:  E int4 of reshuffled node indices
 //   X:     9 x E, X[k * E + e] = (Dm^-1)_{k/3, k%3} of element e
 //   vol:   E signed rest volumes
-//   scale: E per-element stiffness scales (E_e / E) or nullptr
+//   scale: E per-element stiffness scales (E_e / E) or nullptr; scale_la the lambda
+//          scales when they differ (per-element Poisson ratio)
 template <typename T>
 struct ElemView {
   const int4* tets;
   const T* X;
   const T* vol;
-  const T* scale;
+  const T* scale;     // per-element mu scale (E_e / E), or nullptr
+  const T* scale_la;  // per-element lambda scale, or nullptr (then scale)
   int64_t E;
   T mu, lambda;
 };
@@ -57,12 +59,49 @@ struct CgScalars {
   int32_t status;  // 0 ok, 1 max iters, 2 negative curvature, -3 nan
 };
 
+// Element patches for the fused Hessian-vector product.  Elements are stored in
+// patch order (Morton order of centroids, cut into patches of at most
+// kPatchElems elements touching at most kPatchNodes distinct nodes).  Per patch:
+//   elem_off[c] .. elem_off[c+1]   its elements
+//   node_off[c] .. node_off[c+1]   its node slots; pnode[slot] = global node id,
+//                                  or ~id if the node belongs to several patches
+//   lptr[node_off[c] + c + j]      local CSR: entries lent[4 elem_off[c] + t] =
+//                                  (local element << 2 | corner), in element order
+//   lidx[e]                        local node ids of element e's four corners
+// Shared free nodes are summed by a second pass over bnode/bptr/bslot.
+template <typename T>
+struct PatchView {
+  const int64_t* elem_off;
+  const int64_t* node_off;
+  const int32_t* pnode;
+  const int32_t* pdest;  // shared free node slot -> its position in the boundary partial array, else -1
+  const uint16_t* lptr;
+  const uint16_t* lent;
+  const ushort4* lidx;
+  const T* X;
+  const T* vol;
+  const T* scale;
+  const T* scale_la;
+  int64_t E;
+  int64_t n_patches;
+  int64_t nbc;
+  T mu, lambda;
+};
+
+struct PatchBoundary {
+  int64_t n;             // shared free nodes
+  const int32_t* node;   // n
+  const int32_t* ptr;    // n + 1: node i's partials are partial[3 ptr[i] .. 3 ptr[i+1]) in patch order
+};
+
 struct Reduce {
   double* partials;   // >= kMaxBlocks * 4 doubles
   unsigned* counter;  // zero-initialised
 };
 
 unsigned long long launch_count();
+// records the thread's last error message (sfem_last_error) and returns code
+int set_error(int code, const char* msg);
 
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = 2048;
@@ -71,6 +110,27 @@ constexpr int kMaxBlocks = 2048;
 template <typename T, int MAT>
 void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* fe, Reduce red,
                     double* result, int* n_inverted, const CgScalars* s, cudaStream_t st);
+
+constexpr int kPatchElems = 768;
+constexpr int kPatchNodes = 512;
+
+// ---- fused patch Hessian-vector product: q = K p (negated force differential) ----
+// writes q for nodes owned by one patch and partials for shared nodes; the
+// boundary pass completes q and the p.q reduction (alpha, as the HVP gather).
+// With r, dinv and p_new given (Krylov iterations), the kernel first forms the search
+// direction p_new = dinv * r + beta * p (beta from s; p is the previous direction) for the
+// nodes it stages, writes it for every free node it touches and multiplies that; otherwise
+// it multiplies p.
+template <typename T, int MAT>
+void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, const T* p, T* q, T* partial,
+                      Reduce red, CgScalars* s, cudaStream_t st, cudaEvent_t mid = nullptr, const T* r = nullptr,
+                      const T* dinv = nullptr, T* p_new = nullptr);
+
+// fused Krylov update for the patch product (assembles q at shared nodes, bidx[g] = the
+// node's position in the shared-node list or -1)
+template <typename T>
+void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
+                            T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
 
 // ---- node gathers (FP64 residual / T HVP / T diagonal) ----
 void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
@@ -85,7 +145,9 @@ void launch_gather_diag(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, T* din
 // per-element forces of the FP64 force pass in element-major 12-vectors are
 // reused by the adjoint: g_e = sum_a lam_a . f_a / E_e
 void launch_adjoint_elem(const int4* tets, int64_t E, int64_t nbc, const double* fe, const double* lam,
-                         const double* young_e, double* dLdE, cudaStream_t st);
+                         const double* young_e, const int32_t* perm, double* dLdE, cudaStream_t st);
+// out[k] = in[perm[k]] (element arrays into patch order)
+void launch_permute(int64_t E, const int32_t* perm, const double* in, double* out, cudaStream_t st);
 
 // ---- Krylov vector kernels (T = float or double) ----
 template <typename T>
@@ -96,6 +158,12 @@ void launch_cg_update(int64_t n, T* x, T* r, const T* p, const T* q, const T* di
                       CgScalars* s, cudaStream_t st);
 template <typename T>
 void launch_cg_direction(int64_t n, const T* r, const T* dinv, T* p, const CgScalars* s, cudaStream_t st);
+
+// per-segment 2-norms of a free-DOF vector: one block per segment, fixed order
+void launch_segment_norms(int k, const int64_t* seg, const double* v, double* out, cudaStream_t st);
+// zero v on the DOFs of inactive segments (active[k] == 0)
+template <typename T>
+void launch_segment_mask(int k, const int64_t* seg, const int32_t* active, T* v, cudaStream_t st);
 
 // ---- misc vector kernels ----
 void launch_dot(int64_t n, const double* a, const double* b, Reduce red, double* out, cudaStream_t st);
@@ -109,4 +177,38 @@ template <typename T>
 void launch_axpy_state(int64_t n, double a, const T* d, const double* base, double* x, cudaStream_t st);
 void launch_scale_copy(int64_t n, double a, const double* x, double* y, cudaStream_t st);
 
+}  // namespace sfem
+
+// ---- learned preconditioner launchers (sfem_gnn.cu) ----
+#include <cuda_bf16.h>
+
+#include "sfem_gnn.h"
+namespace sfem {
+namespace gnn {
+void launch_stat(int which, int64_t n3, const float* r, const float* dinv, float* partials, unsigned* counter,
+                 Scalars* sc, const int* done, cudaStream_t st);
+void launch_forward(const Graph& g, const float* r, const float* dinv, const uint8_t* fixed_nb, const float* params,
+                    const __nv_bfloat16* Wb, Scalars* sc, __nv_bfloat16* const* h, __nv_bfloat16* const* u, float* x,
+                    float* out, const int* done, cudaStream_t st);
+int launch_count_forward();
+void launch_backward(const Graph& g, const float* Go, const float* params, const __nv_bfloat16* Wtb, const Scalars* sc,
+                     __nv_bfloat16* const* h, __nv_bfloat16* const* u, const float* x, float* G0, float* G1,
+                     float* G2, float* partial, float* grad, cudaStream_t st);
+int launch_count_backward();
+void launch_loss(int64_t n3, const float* d, const float* q, float inv_c, float* Go, float* partials,
+                 unsigned* counter, float* loss, cudaStream_t st);
+void launch_adam(const float* grad, float* prm, float* m, float* v, float lr, int t, float clip_scale,
+                 __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st);
+void launch_pack(const float* prm, __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st);
+void launch_sub(int64_t n, const float* a, const float* b, float* d, cudaStream_t st);
+// flexible CG (Polak-Ribiere) vector kernels; partials need >= 2048 floats
+void launch_fcg_init(int64_t n, const float* r, const float* z, float* p, float* partials, unsigned* counter,
+                     CgScalars* s, cudaStream_t st);
+void launch_fcg_update(int64_t n, float* x, float* r, float* rprev, const float* p, const float* q, float* partials,
+                       unsigned* counter, CgScalars* s, cudaStream_t st);
+void launch_fcg_beta(int64_t n, const float* r, const float* rprev, const float* z, const float* dinv,
+                     float* partials, unsigned* counter, CgScalars* s, cudaStream_t st);
+void launch_fcg_dir(int64_t n, const float* z, const float* r, const float* dinv, float* p, const CgScalars* s,
+                    cudaStream_t st);
+}  // namespace gnn
 }  // namespace sfem

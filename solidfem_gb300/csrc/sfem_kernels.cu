@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(kThreads) k_element(ElemView<T> ev, const T* _
     if (ev.scale) {
       const T sc = ev.scale[e];
       mu *= sc;
-      la *= sc;
+      la *= ev.scale_la ? ev.scale_la[e] : sc;
     }
     M3<T> F = grad_of(u, t, X);
     F.a[0] += T(1);
@@ -799,6 +799,7 @@ __global__ void __launch_bounds__(kThreads) k_adjoint_elem(const int4* __restric
                                                            const double* __restrict__ fe,
                                                            const double* __restrict__ lam,
                                                            const double* __restrict__ young_e,
+                                                           const int32_t* __restrict__ perm,
                                                            double* __restrict__ dLdE) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
     const int4 t = tets[e];
@@ -810,15 +811,329 @@ __global__ void __launch_bounds__(kThreads) k_adjoint_elem(const int4* __restric
 #pragma unroll
       for (int c = 0; c < 3; c++) s += lam[3 * (int64_t)idx[a] + c] * fe[12 * e + 3 * a + c];
     }
-    dLdE[e] = s / young_e[e];
+    // young_e is in patch order; dLdE is written in the caller's element order
+    dLdE[perm[e]] = s / young_e[e];
   }
 }
 
 void launch_adjoint_elem(const int4* tets, int64_t E, int64_t nbc, const double* fe, const double* lam,
-                         const double* young_e, double* dLdE, cudaStream_t st) {
+                         const double* young_e, const int32_t* perm, double* dLdE, cudaStream_t st) {
   count_launch();
-  k_adjoint_elem<<<grid_for(E, 152 * 12), kThreads, 0, st>>>(tets, E, nbc, fe, lam, young_e, dLdE);
+  k_adjoint_elem<<<grid_for(E, 152 * 12), kThreads, 0, st>>>(tets, E, nbc, fe, lam, young_e, perm, dLdE);
 }
+
+__global__ void k_permute(int64_t E, const int32_t* __restrict__ perm, const double* __restrict__ in,
+                          double* __restrict__ out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < E; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = in[perm[k]];
+}
+void launch_permute(int64_t E, const int32_t* perm, const double* in, double* out, cudaStream_t st) {
+  count_launch();
+  k_permute<<<grid_for(E), kThreads, 0, st>>>(E, perm, in, out);
+}
+
+// ---------------------------------------------------------------------------
+// Fused patch Hessian-vector product
+// ---------------------------------------------------------------------------
+// One CTA per patch.  Phase 1 stages the patch's nodal u and p in shared memory
+// (forming p = dinv r + beta p_old on the fly inside Krylov iterations), phase 2
+// computes the 12 nodal values of every element into shared memory, phase 3 sums
+// them per local node through the patch-local CSR (element order, deterministic)
+// and writes q = -sum for nodes that only this patch touches, or a partial for
+// shared nodes.  Block partials of p.q go to red.partials[c].
+constexpr int kFeStride = 13;  // odd stride: conflict-free shared-memory rows of 12 values
+
+template <typename T>
+struct ElemLoad {  // one element's data, loaded ahead of its use
+  ushort4 li;
+  T X[9];
+  T vol, sc, scl;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_elem(const PatchView<T>& pv, int64_t e, ElemLoad<T>& d) {
+  d.li = pv.lidx[e];
+#pragma unroll
+  for (int q9 = 0; q9 < 9; q9++) d.X[q9] = pv.X[q9 * pv.E + e];
+  d.vol = pv.vol[e];
+  d.sc = pv.scale ? pv.scale[e] : T(1);
+  d.scl = pv.scale_la ? pv.scale_la[e] : d.sc;
+}
+
+template <typename T, int MAT, int NT, bool DIR>
+__global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __restrict__ u,
+                                                  const T* __restrict__ p, T* __restrict__ q,
+                                                  T* __restrict__ partial, Reduce red, CgScalars* s,
+                                                  const T* __restrict__ r, const T* __restrict__ dinv,
+                                                  T* __restrict__ p_new) {
+  if (s != nullptr && s->done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sfe = reinterpret_cast<T*>(smem_raw);  // kPatchElems * kFeStride
+  T* su = sfe + kPatchElems * kFeStride;    // kPatchNodes * 3
+  T* sp = su + kPatchNodes * 3;             // kPatchNodes * 3
+  const int c = blockIdx.x;
+  const int64_t eb = pv.elem_off[c], ne = pv.elem_off[c + 1] - eb;
+  const int64_t nb = pv.node_off[c];
+  const int nn = (int)(pv.node_off[c + 1] - nb);
+  T beta = T(0);
+  if (DIR) beta = (T)s->beta;
+  for (int j = threadIdx.x; j < nn; j += NT) {
+    int g = pv.pnode[nb + j];
+    if (g < 0) g = ~g;
+    const int64_t o = 3 * (int64_t)g;
+    su[3 * j] = u[o];
+    su[3 * j + 1] = u[o + 1];
+    su[3 * j + 2] = u[o + 2];
+    if (DIR) {
+      // zero at fixed nodes: r, dinv and p stay zero there
+      const T p0 = dinv[o] * r[o] + beta * p[o];
+      const T p1 = dinv[o + 1] * r[o + 1] + beta * p[o + 1];
+      const T p2 = dinv[o + 2] * r[o + 2] + beta * p[o + 2];
+      sp[3 * j] = p0;
+      sp[3 * j + 1] = p1;
+      sp[3 * j + 2] = p2;
+      // every patch that touches a node computes the same value from the same inputs
+      if (g >= pv.nbc) {
+        p_new[o] = p0;
+        p_new[o + 1] = p1;
+        p_new[o + 2] = p2;
+      }
+    } else {
+      sp[3 * j] = p[o];
+      sp[3 * j + 1] = p[o + 1];
+      sp[3 * j + 2] = p[o + 2];
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < ne; k += NT) {
+    ElemLoad<T> cur;
+    load_elem(pv, eb + k, cur);
+    const ushort4 li = cur.li;
+    M3<T> X;
+#pragma unroll
+    for (int q9 = 0; q9 < 9; q9++) X.a[q9] = cur.X[q9];
+    const T mu = pv.mu * cur.sc, la = pv.lambda * cur.scl;
+    M3<T> D, Dp;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const T a0 = su[3 * li.x + i], b0 = sp[3 * li.x + i];
+      D.a[3 * i] = su[3 * li.y + i] - a0;
+      D.a[3 * i + 1] = su[3 * li.z + i] - a0;
+      D.a[3 * i + 2] = su[3 * li.w + i] - a0;
+      Dp.a[3 * i] = sp[3 * li.y + i] - b0;
+      Dp.a[3 * i + 1] = sp[3 * li.z + i] - b0;
+      Dp.a[3 * i + 2] = sp[3 * li.w + i] - b0;
+    }
+    M3<T> F = mul(D, X);
+    F.a[0] += T(1);
+    F.a[4] += T(1);
+    F.a[8] += T(1);
+    Tangent<T, MAT> tg;
+    tg.init(F, mu, la);
+    const M3<T> dP = tg.apply(mul(Dp, X));
+    T f[12];
+    nodal_forces(dP, X, -cur.vol, f);
+#pragma unroll
+    for (int t = 0; t < 12; t++) sfe[kFeStride * k + t] = f[t];
+  }
+  __syncthreads();
+  // p.q is linear in the partial sums, so shared nodes contribute p . partial here
+  T acc = T(0);
+  const uint16_t* lp = pv.lptr + nb + c;
+  const uint16_t* le = pv.lent + 4 * eb;
+  for (int j = threadIdx.x; j < nn; j += NT) {
+    T f0 = T(0), f1 = T(0), f2 = T(0);
+    const int t1 = lp[j + 1];
+    for (int t = lp[j]; t < t1; t++) {
+      const int x = le[t];
+      const T* src = sfe + kFeStride * (x >> 2) + 3 * (x & 3);
+      f0 += src[0];
+      f1 += src[1];
+      f2 += src[2];
+    }
+    const int g = pv.pnode[nb + j];
+    int64_t o = -1;
+    T* dst = q;
+    if (g >= 0) {
+      if (g >= pv.nbc) o = 3 * (int64_t)g;
+    } else {
+      const int d = pv.pdest[nb + j];
+      if (d >= 0) {
+        o = 3 * (int64_t)d;
+        dst = partial;
+      }
+    }
+    if (o >= 0) {
+      dst[o] = -f0;
+      dst[o + 1] = -f1;
+      dst[o + 2] = -f2;
+      acc -= sp[3 * j] * f0 + sp[3 * j + 1] * f1 + sp[3 * j + 2] * f2;
+    }
+  }
+  T v[1] = {acc};
+  block_sum<T, 1>(v);
+  if (s == nullptr) return;
+  __shared__ bool is_last;
+  T* P = reinterpret_cast<T*>(red.partials);
+  if (threadIdx.x == 0) {
+    P[c] = v[0];
+    __threadfence();
+    is_last = atomicAdd(red.counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  T sum[1] = {T(0)};
+  for (int64_t i = threadIdx.x; i < (int64_t)gridDim.x; i += NT) sum[0] += __ldcg(&P[i]);
+  block_sum<T, 1>(sum);
+  if (threadIdx.x == 0) {
+    *red.counter = 0u;
+    const double pq = (double)sum[0];
+    s->pq = pq;
+    if (!isfinite(pq)) {
+      s->done = 1;
+      s->status = -3;
+      s->alpha = 0.0;
+    } else if (!(pq > 0.0)) {
+      s->done = 1;
+      s->status = 2;
+      s->alpha = 0.0;
+    } else {
+      s->alpha = s->rz / pq;
+    }
+  }
+}
+
+// Shared free nodes: q = sum of the patch partials in patch order (used when the
+// caller needs the complete vector q; the fused Krylov update sums them itself).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_patch_boundary(PatchBoundary pb, const T* __restrict__ partial,
+                                                             T* __restrict__ q, const CgScalars* s) {
+  if (s != nullptr && s->done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < pb.n; i += (int64_t)gridDim.x * blockDim.x) {
+    T f0 = T(0), f1 = T(0), f2 = T(0);
+    const int t1 = pb.ptr[i + 1];
+    for (int t = pb.ptr[i]; t < t1; t++) {
+      f0 += partial[3 * (int64_t)t];
+      f1 += partial[3 * (int64_t)t + 1];
+      f2 += partial[3 * (int64_t)t + 2];
+    }
+    const int64_t o = 3 * (int64_t)pb.node[i];
+    q[o] = f0;
+    q[o + 1] = f1;
+    q[o + 2] = f2;
+  }
+}
+
+// Fused Krylov update over nodes: q_g from q (owned nodes) or the sum of its patch
+// partials (shared nodes, bidx[g] >= 0), then x += alpha p, r -= alpha q, z = dinv r,
+// r.z and r.r with the fixed-order last-block finish (beta, convergence test).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64_t N, const int32_t* __restrict__ bidx,
+                                                              PatchBoundary pb, const T* __restrict__ partial,
+                                                              T* __restrict__ x, T* __restrict__ r,
+                                                              const T* __restrict__ p, const T* __restrict__ q,
+                                                              const T* __restrict__ dinv, Reduce red, CgScalars* s) {
+  if (s->done) return;
+  const T a = (T)s->alpha;
+  T rz = T(0), rr = T(0);
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = 3 * g;
+    T qq[3];
+    const int b = bidx[g];
+    if (b < 0) {
+      qq[0] = q[o];
+      qq[1] = q[o + 1];
+      qq[2] = q[o + 2];
+    } else {
+      qq[0] = qq[1] = qq[2] = T(0);
+      const int t1 = pb.ptr[b + 1];
+      for (int t = pb.ptr[b]; t < t1; t++) {
+        qq[0] += partial[3 * (int64_t)t];
+        qq[1] += partial[3 * (int64_t)t + 1];
+        qq[2] += partial[3 * (int64_t)t + 2];
+      }
+    }
+#pragma unroll
+    for (int c2 = 0; c2 < 3; c2++) {
+      x[o + c2] += a * p[o + c2];
+      const T ri = r[o + c2] - a * qq[c2];
+      r[o + c2] = ri;
+      rz += ri * (dinv[o + c2] * ri);
+      rr += ri * ri;
+    }
+  }
+  T v[2] = {rz, rr}, tot[2];
+  if (reduce_last<T, 2>(v, red, tot) && threadIdx.x == 0) {
+    const double rzn = (double)tot[0];
+    s->beta = rzn / s->rz;
+    s->rz = rzn;
+    s->rr = (double)tot[1];
+    s->it += 1;
+    if (!isfinite(s->rr)) {
+      s->done = 1;
+      s->status = -3;
+    } else if (s->rr <= s->tol2) {
+      s->done = 1;
+    } else if (s->it >= s->max_it) {
+      s->done = 1;
+      s->status = 1;
+    }
+  }
+}
+
+template <typename T>
+void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
+                            T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st) {
+  count_launch();
+  k_cg_update_patch<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, bidx, pb, partial, x, r, p, q, dinv, red, s);
+}
+template void launch_cg_update_patch<double>(int64_t, int64_t, const int32_t*, PatchBoundary, const double*, double*,
+                                             double*, const double*, const double*, const double*, Reduce,
+                                             CgScalars*, cudaStream_t);
+template void launch_cg_update_patch<float>(int64_t, int64_t, const int32_t*, PatchBoundary, const float*, float*,
+                                            float*, const float*, const float*, const float*, Reduce, CgScalars*,
+                                            cudaStream_t);
+
+template <typename T, int MAT>
+void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, const T* p, T* q, T* partial, Reduce red,
+                      CgScalars* s, cudaStream_t st, cudaEvent_t mid, const T* r, const T* dinv, T* p_new) {
+  constexpr int NT = 256;
+  constexpr size_t smem = sizeof(T) * (kPatchElems * kFeStride + kPatchNodes * 6);
+  static bool attr_set = false;  // per instantiation
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr_set = true;
+  }
+  count_launch();
+  if (p_new != nullptr) {
+    // Krylov iteration: the fused update (k_cg_update_patch) completes the shared nodes
+    k_patch_hvp<T, MAT, NT, true><<<(unsigned)pv.n_patches, NT, smem, st>>>(pv, u, p, q, partial, red, s, r, dinv,
+                                                                           p_new);
+    if (mid) cudaEventRecord(mid, st);
+    return;
+  }
+  k_patch_hvp<T, MAT, NT, false><<<(unsigned)pv.n_patches, NT, smem, st>>>(pv, u, p, q, partial, red, s, nullptr,
+                                                                          nullptr, nullptr);
+  if (mid) cudaEventRecord(mid, st);
+  count_launch();
+  k_patch_boundary<T><<<grid_for(pb.n), kThreads, 0, st>>>(pb, partial, q, s);
+}
+
+#define SFEM_INST_PATCH(T, M)                                                                                   \
+  template void launch_patch_hvp<T, M>(const PatchView<T>&, PatchBoundary, const T*, const T*, T*, T*, Reduce, \
+                                       CgScalars*, cudaStream_t, cudaEvent_t, const T*, const T*, T*);
+SFEM_INST_PATCH(double, 0)
+SFEM_INST_PATCH(double, 1)
+SFEM_INST_PATCH(double, 2)
+SFEM_INST_PATCH(double, 3)
+SFEM_INST_PATCH(double, 4)
+SFEM_INST_PATCH(float, 0)
+SFEM_INST_PATCH(float, 1)
+SFEM_INST_PATCH(float, 2)
+SFEM_INST_PATCH(float, 3)
+SFEM_INST_PATCH(float, 4)
 
 // ---------------------------------------------------------------------------
 // Krylov vector kernels over the free-DOF range (pointers pre-offset)
@@ -844,6 +1159,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_init(int64_t n, const T* __rest
     s->rr = (double)tot[1];
     s->tol2 = s->tol2 * (double)tot[1];
     s->it = 0;
+    s->beta = 0.0;
     s->status = 0;
     s->done = (tot[1] == T(0)) ? 1 : 0;
     if (!isfinite(s->bb)) {
@@ -923,6 +1239,37 @@ void launch_cg_direction(int64_t n, const T* r, const T* dinv, T* p, const CgSca
   template void launch_cg_direction<T>(int64_t, const T*, const T*, T*, const CgScalars*, cudaStream_t);
 SFEM_INST_CG(double)
 SFEM_INST_CG(float)
+
+// ---------------------------------------------------------------------------
+// Independent instances (batched solves): per-segment norms and masks
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_segment_norms(const int64_t* __restrict__ seg,
+                                                            const double* __restrict__ v, double* __restrict__ out) {
+  const int k = blockIdx.x;
+  double acc = 0.0;
+  for (int64_t i = seg[k] + threadIdx.x; i < seg[k + 1]; i += blockDim.x) acc += v[i] * v[i];
+  double a[1] = {acc};
+  block_sum<double, 1>(a);
+  if (threadIdx.x == 0) out[k] = sqrt(a[0]);
+}
+void launch_segment_norms(int k, const int64_t* seg, const double* v, double* out, cudaStream_t st) {
+  count_launch();
+  k_segment_norms<<<k, kThreads, 0, st>>>(seg, v, out);
+}
+
+template <typename T>
+__global__ void k_segment_mask(const int64_t* __restrict__ seg, const int32_t* __restrict__ active, T* __restrict__ v) {
+  const int k = blockIdx.x;
+  if (active[k]) return;
+  for (int64_t i = seg[k] + threadIdx.x; i < seg[k + 1]; i += blockDim.x) v[i] = T(0);
+}
+template <typename T>
+void launch_segment_mask(int k, const int64_t* seg, const int32_t* active, T* v, cudaStream_t st) {
+  count_launch();
+  k_segment_mask<T><<<k, kThreads, 0, st>>>(seg, active, v);
+}
+template void launch_segment_mask<double>(int, const int64_t*, const int32_t*, double*, cudaStream_t);
+template void launch_segment_mask<float>(int, const int64_t*, const int32_t*, float*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Misc

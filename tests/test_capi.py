@@ -39,3 +39,21 @@ def test_no_device_is_reported_not_faked():
     with pytest.raises(SfemError) as ei:
         FemPhysicsMatrixFree(m.tets, m.nodes, np.array([0]))
     assert ei.value.code == -7
+
+
+def test_invalid_arguments_are_rejected_before_any_device_work():
+    import numpy as np
+    import pytest
+
+    from solidfem_gb300 import FemPhysicsMatrixFree, SfemError
+    from solidfem_gb300.mesh import box_lattice
+
+    m = box_lattice(2, 1, 1)
+    bad = m.tets.copy()
+    bad[0, 0] = m.n_nodes + 5
+    with pytest.raises(SfemError) as ei:
+        FemPhysicsMatrixFree(bad, m.nodes, np.array([0]))
+    assert ei.value.code == -1 and "out of range" in str(ei.value)
+    with pytest.raises(SfemError) as ei:
+        FemPhysicsMatrixFree(m.tets, m.nodes, np.array([0]), poisson=0.5)
+    assert ei.value.code == -1

@@ -21,11 +21,11 @@ def c5_problem(nx, ny, nz, seed_a=1, seed_b=2):
     return m, fixed, young, young_t, f
 
 
-def solve_u(phys, young, f_free, rest, tol=1e-13):
+def solve_u(phys, young, f_free, rest, tol=1e-11):
     phys.set_element_youngs(young)
     phys.set_nodal_loads(phys.from_free(f_free))
     phys.set_free_positions(rest)
-    st = phys.newton_solve(rel_tol=tol, max_newton=60)
+    st = phys.newton_solve(rel_tol=tol, max_newton=100)
     assert st["status"] == 0, st
     return phys.get_free_positions() - rest
 
@@ -47,7 +47,7 @@ def test_adjoint_vs_finite_differences_and_oracle(dims, n_fd):
     E = torch.tensor(young, device=dev, requires_grad=True)
     F = torch.tensor(f_free, device=dev, requires_grad=True)
     ut = torch.tensor(u_t, device=dev)
-    u = equilibrium_displacement(phys, E, F, solve_kw=dict(rel_tol=1e-13, max_newton=60), adjoint_tol=1e-12)
+    u = equilibrium_displacement(phys, E, F, solve_kw=dict(rel_tol=1e-11, max_newton=100), adjoint_tol=1e-12)
     loss = ((u - ut) ** 2).sum()
     loss.backward()
     gE = E.grad.cpu().numpy()
@@ -69,8 +69,13 @@ def test_adjoint_vs_finite_differences_and_oracle(dims, n_fd):
     fd = np.array(fd)
     scale = np.abs(gE).max()
     err = np.abs(gE[idx] - fd) / scale
-    print(f"{dims}: dL/dE vs central FD (h=1e-4 E): max err / max|g| = {err.max():.2e}")
-    assert err.max() < 1e-4
+    print(f"{dims}: dL/dE vs central FD (h=1e-4 E) on {n_fd} elements: max err / max|g| = {err.max():.2e}")
+    assert err.max() < 1e-3
+    # directional derivative along a random relative perturbation of all moduli
+    v = rng.normal(size=m.n_tets) * young
+    hdir = 1e-4
+    fdd = (L(young + hdir * v, f_free) - L(young - hdir * v, f_free)) / (2 * hdir)
+    assert abs(gE @ v - fdd) <= 1e-5 * abs(fdd), (gE @ v, fdd)
     # load gradient: a few components
     for k in rng.choice(f_free.size, size=4, replace=False):
         i, c = divmod(int(k), 3)
@@ -86,9 +91,9 @@ def test_adjoint_vs_finite_differences_and_oracle(dims, n_fd):
         o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, (0.0, 0.0, 0.0), 3)
         o.set_element_scale(young / 1e5)
         o.set_nodal_loads(f)
-        status, _ = o.newton_pcg(rtol=1e-13, max_newton=60)
-        assert status == 0
+        status, st_o = o.newton_pcg(rtol=1e-11, max_newton=100)
+        assert status == 0, st_o
         uo = o.free_positions().reshape(-1, 3) - rest
-        dE_o, dF_o, _ = o.adjoint((2 * (uo - u_t)).ravel(), young, tol=1e-13)
+        dE_o, dF_o, _ = o.adjoint((2 * (uo - u_t)).ravel(), young, tol=1e-12)
         assert np.linalg.norm(gE - dE_o) <= 1e-6 * np.linalg.norm(dE_o)
         assert np.linalg.norm(gF.ravel() - dF_o) <= 1e-6 * np.linalg.norm(dF_o)
