@@ -252,6 +252,19 @@ int sfem_get_profile(const sfem_handle* h, sfem_profile* out);
 /* Total number of kernels this library has launched in the process. */
 int sfem_kernel_launches(int64_t* count);
 
+/* ---- allocation-free reduction (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc where they need a reduction: code running inside a
+ * CUDA stream capture (allocation is not capturable and synchronises the device), control
+ * loops that forbid allocation after start-up, and host applications that plan all device
+ * memory themselves.  Computes out_dev[0] = sum_i a_dev[i] * b_dev[i] (device pointers),
+ * ordered on `stream`, with the same fixed-order reduction as sfem_dot.  Its scratch is a
+ * fixed static device array (one partial per 2048 entries + a counter, 512 KiB), held by every
+ * device that loads this library until the process exits; n above 134,217,728 is rejected
+ * with SFEM_ERR_INVALID.  Every call shares the array and clears its counter first, so calls
+ * that overlap on the GPU race: serialise them.  The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress) and should come before any stream capture. */
+int sfem_dot_noalloc_dev(const double* a_dev, const double* b_dev, int64_t n, double* out_dev, void* stream);
+
 /* ---- device-pointer variants (stream-ordered on the handle's stream) ---- */
 int sfem_compute_gradients_dev(sfem_handle* h, double* r_dev);
 int sfem_matvec_dev(sfem_handle* h, const double* d_dev, double* Kd_dev);

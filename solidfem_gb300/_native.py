@@ -116,6 +116,7 @@ SIGNATURES = {
     "sfem_set_profiling": [_vp, C.c_int32],
     "sfem_get_profile": [_vp, C.POINTER(Profile)],
     "sfem_kernel_launches": [_i64p],
+    "sfem_dot_noalloc_dev": [_vp, _vp, C.c_int64, _vp, _vp],
     "sfem_compute_gradients_dev": [_vp, _vp],
     "sfem_matvec_dev": [_vp, _vp, _vp],
     "sfem_get_free_positions_dev": [_vp, _vp],
