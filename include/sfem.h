@@ -159,6 +159,23 @@ int sfem_set_force_fraction(sfem_handle* h, double f);
  * Include/FemPhysicsBase.h:152-155): per-element Young's modulus, original element
  * order; NULL restores the uniform modulus. */
 int sfem_set_element_youngs(sfem_handle* h, const double* young_e);
+/* FemPhysicsMatrixFree::SetBoundaryConditionsSurface (Source/FemPhysicsMatrixFree.cpp:1051-1060):
+ * follower pressure on triangles (n_tris x 3 original node indices), applied as in
+ * ComputePressureForces (:967-1049): ff * (area/3) * pressure * unit normal per triangle node
+ * at the current positions.  Its stiffness is not part of the Hessian-vector product (as in the
+ * reference's MatrixVectorMultiply).  NULL / 0 removes the surface. */
+int sfem_set_pressure_surface(sfem_handle* h, const int32_t* tris, int64_t n_tris, double pressure);
+/* Extension: per-element Lame parameters (caller's element order), e.g. bodies with their own
+ * Young's modulus and Poisson ratio in one mesh; NULL restores the uniform parameters. */
+int sfem_set_element_lame(sfem_handle* h, const double* mu_e, const double* lambda_e);
+/* Extension: the mesh is a union of k independent bodies; body q owns the caller's nodes
+ * [node_offsets[q], node_offsets[q+1]) (node_offsets[0] = 0, node_offsets[k] = N).  Every kernel
+ * launch still covers all bodies; sfem_newton_solve converges each body against its own initial
+ * residual and masks converged bodies (zero right-hand side and Jacobi inverse) while the others
+ * continue.  k = 0 removes the instances. */
+int sfem_set_instances(sfem_handle* h, int32_t k, const int64_t* node_offsets);
+/* per-body |r_q| / |r_q(x_0)| and Newton iterations of the last sfem_newton_solve */
+int sfem_instance_stats(const sfem_handle* h, double* rel_res, int32_t* newton_iters);
 /* Extension (FemPhysicsBase::SetExternalForces is an ASSERT stub, Include/FemPhysicsBase.h:68):
  * dead nodal loads, N x 3 original order, added to the residual scaled by mForceFraction. */
 int sfem_set_nodal_loads(sfem_handle* h, const double* f);
@@ -222,7 +239,10 @@ int sfem_gnn_get_params(sfem_handle* h, float* params);
 int sfem_gnn_set_params(sfem_handle* h, const float* params);
 /* M(r) at the current state (uses the current Jacobi diagonal); free-DOF vectors */
 int sfem_gnn_apply(sfem_handle* h, const double* r_free, double* out_free);
-/* energy-norm loss ||M(r) - e||_K^2 / (e . r) of one residual/correction pair and its gradient */
+/* training objective: 0 = energy norm of the error ||M(r) - e||_K^2 / (e . r) (default),
+ * 1 = residual norm ||K M(r) - r||^2 / (r . r) */
+int sfem_gnn_set_loss(sfem_handle* h, int32_t mode);
+/* the loss of one residual/correction pair and its parameter gradient */
 int sfem_gnn_loss_grad(sfem_handle* h, const double* r_free, const double* e_free, double* loss, float* grad);
 /* residual/correction pairs (r_j, x_final - x_j) from a plain Jacobi-PCG solve of K x = b
  * (b_free NULL: the current nonlinear residual), one every `every` iterations, appended to

@@ -92,15 +92,22 @@ def forward(p, Am, fixed_nb, r, dinv, bf16_layers=True):
     return z + s * y, cache
 
 
-def loss_grad(p, Am, fixed_nb, r, dinv, e, Kmul, bf16_layers=True):
-    """Energy-norm loss ||M(r) - e||_K^2 / (e.r) and its gradient; Kmul(v) = K v (flat)."""
+def loss_grad(p, Am, fixed_nb, r, dinv, e, Kmul, bf16_layers=True, mode="energy"):
+    """Loss and gradient; Kmul(v) = K v (flat).
+    energy:   ||M(r) - e||_K^2 / (e.r);   residual: ||K M(r) - r||^2 / (r.r)."""
     out, c = forward(p, Am, fixed_nb, r, dinv, bf16_layers)
-    e = e.reshape(-1, 3)
-    d = out - e
-    q = Kmul(d.ravel()).reshape(-1, 3)
-    cc = float(e.ravel() @ r.ravel())
-    L = float(d.ravel() @ q.ravel()) / cc
-    Go = 2.0 * q / cc
+    if mode == "energy":
+        e = e.reshape(-1, 3)
+        d = out - e
+        q = Kmul(d.ravel()).reshape(-1, 3)
+        cc = float(e.ravel() @ r.ravel())
+        L = float(d.ravel() @ q.ravel()) / cc
+        Go = 2.0 * q / cc
+    else:
+        d = Kmul(out.ravel()) - r.ravel()
+        cc = float(r.ravel() @ r.ravel())
+        L = float(d @ d) / cc
+        Go = (2.0 * Kmul(d) / cc).reshape(-1, 3)
     We, be, Ws, bs, Wd, bd = unpack(p, bf16_layers)
     g = np.zeros(NPARAM)
     gy = c["s"] * Go

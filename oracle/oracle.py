@@ -78,6 +78,7 @@ class Oracle:
             lib.orc_set_force_fraction.argtypes = [C.c_void_p, C.c_double]
             lib.orc_set_lame.argtypes = [C.c_void_p, C.c_double, C.c_double]
             lib.orc_set_tangent.argtypes = [C.c_void_p, C.c_int]
+            lib.orc_set_pressure_surface.argtypes = [C.c_void_p, _ip, C.c_int, C.c_double]
             lib.orc_matvec.argtypes = [C.c_void_p, _dp, _dp]
             for name in ["orc_elastic_energy", "orc_total_energy"]:
                 getattr(lib, name).argtypes = [C.c_void_p]
@@ -133,6 +134,10 @@ class Oracle:
 
     def set_tangent(self, mode):
         self.lib().orc_set_tangent(self.h, mode)
+
+    def set_pressure_surface(self, tris, pressure):
+        self._tris = _i32(tris)
+        self.lib().orc_set_pressure_surface(self.h, _p(self._tris, _ip), self._tris.shape[0], pressure)
 
     def set_element_scale(self, s):
         if s is None:
@@ -268,6 +273,7 @@ class RefHarness:
                          "ref_element_stress"]:
                 getattr(lib, name).argtypes = [C.c_void_p, _dp]
             lib.ref_set_force_fraction.argtypes = [C.c_void_p, C.c_double]
+            lib.ref_set_pressure_surface.argtypes = [C.c_void_p, _ip, C.c_int, C.c_double]
             lib.ref_matvec.argtypes = [C.c_void_p, _dp, _dp]
             lib.ref_elastic_energy.argtypes = [C.c_void_p]
             lib.ref_elastic_energy.restype = C.c_double
@@ -318,6 +324,10 @@ class RefHarness:
     def set_nodal_loads(self, f):
         f = _f64(f)
         self.lib().ref_set_nodal_loads(self.h, _p(f))
+
+    def set_pressure_surface(self, tris, pressure):
+        self._tris = _i32(tris)
+        self.lib().ref_set_pressure_surface(self.h, _p(self._tris, _ip), self._tris.shape[0], pressure)
 
     def set_positions_shuffled(self, x):
         x = _f64(x)

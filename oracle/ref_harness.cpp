@@ -135,6 +135,13 @@ void ref_tets(void* hp, int* out_tets) {
 
 void ref_set_force_fraction(void* hp, double f) { ((Handle*)hp)->phys->SetForceFraction(f); }
 
+// FemPhysicsMatrixFree::SetBoundaryConditionsSurface: triangles of original node indices
+void ref_set_pressure_surface(void* hp, const int* tris, int n_tris, double pressure) {
+  std::vector<uint32> tl(3 * (size_t)n_tris);
+  for (size_t i = 0; i < tl.size(); i++) tl[i] = (uint32)tris[i];
+  ((Handle*)hp)->phys->SetBoundaryConditionsSurface(tl, pressure);
+}
+
 // Dead loads given per original node index (only free nodes are used).
 void ref_set_nodal_loads(void* hp, const double* f_orig) {
   RefProblem* p = ((Handle*)hp)->phys;

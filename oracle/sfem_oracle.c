@@ -128,6 +128,9 @@ typedef struct {
   double* pos0;      /* rest positions, reshuffled, 3N */
   double* inv_mass;  /* per reshuffled node */
   double* fext;      /* dead loads, reshuffled, 3N */
+  int n_tris;        /* follower-pressure surface (original node indices), 3 per triangle */
+  int* tris;
+  double pressure;
 } orc_problem;
 
 static M3 load_X(const orc_problem* p, int e) { M3 r; memcpy(r.m, p->X + 9 * (size_t)e, 9 * sizeof(double)); return r; }
@@ -199,6 +202,7 @@ void* orc_create(const double* nodes, int n_nodes, const int* tets, int n_tets,
 
 void orc_destroy(void* h) {
   orc_problem* p = (orc_problem*)h;
+  free(p->tris);
   free(p->map); free(p->tets); free(p->X); free(p->vol); free(p->escale);
   free(p->pos); free(p->pos0); free(p->inv_mass); free(p->fext); free(p);
 }
@@ -281,10 +285,44 @@ static M3 elem_stress(const orc_problem* p, int e, M3 F, M3* Pmu, M3* Plambda) {
   }
 }
 
+/* FemPhysicsMatrixFree::SetBoundaryConditionsSurface (Source/FemPhysicsMatrixFree.cpp:1051-1060):
+ * triangles of original node indices and the applied (follower) pressure. */
+void orc_set_pressure_surface(void* h, const int* tris, int n_tris, double pressure) {
+  orc_problem* p = (orc_problem*)h;
+  free(p->tris);
+  p->tris = NULL;
+  p->n_tris = n_tris;
+  p->pressure = pressure;
+  if (n_tris > 0) {
+    p->tris = (int*)malloc(sizeof(int) * 3 * (size_t)n_tris);
+    memcpy(p->tris, tris, sizeof(int) * 3 * (size_t)n_tris);
+  }
+}
+
+/* FemPhysicsMatrixFree::ComputePressureForces (Source/FemPhysicsMatrixFree.cpp:967-1049), explicit
+ * part: per triangle ff * (area/3) * pressure * unit normal of (p2-p1) x (p3-p1), added to its nodes. */
+static void pressure_forces(const orc_problem* p, double* f) {
+  for (int t = 0; t < p->n_tris; t++) {
+    int i1 = p->map[p->tris[3 * t]], i2 = p->map[p->tris[3 * t + 1]], i3 = p->map[p->tris[3 * t + 2]];
+    V3 p1 = node_v(p->pos, i1), p2 = node_v(p->pos, i2), p3 = node_v(p->pos, i3);
+    V3 a = v3_sub(p2, p1), b = v3_sub(p3, p1);
+    V3 nrm = v3_cross(a, b);
+    double area = 0.5 * sqrt(v3_dot(nrm, nrm));
+    nrm = v3_normalized(nrm);
+    V3 traction = v3_scale(p->pressure, nrm);
+    V3 force = v3_scale(p->force_fraction, v3_scale(area / 3.0, traction));
+    int idx[3] = {i1, i2, i3};
+    for (int k = 0; k < 3; k++)
+      for (int c = 0; c < 3; c++) f[3 * (size_t)idx[k] + c] += force.v[c];
+  }
+}
+
 /* ElasticEnergy::ComputeForces (Source/ElasticEnergy.cpp:259-282) into a full
- * reshuffled node array, serial element-order scatter. */
+ * reshuffled node array, serial element-order scatter, after the pressure forces
+ * (the order of FemPhysicsMatrixFree::ComputeGradients, Source/FemPhysicsMatrixFree.cpp:540-543). */
 static void internal_forces(const orc_problem* p, double* f) {
   memset(f, 0, sizeof(double) * 3 * p->n_nodes);
+  pressure_forces(p, f);
   for (int e = 0; e < p->n_tets; e++) {
     M3 Pmu, Pl;
     M3 F = def_grad(p, e);

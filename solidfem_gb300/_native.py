@@ -91,6 +91,10 @@ SIGNATURES = {
     "sfem_set_force_fraction": [_vp, C.c_double],
     "sfem_set_element_youngs": [_vp, _dp],
     "sfem_set_nodal_loads": [_vp, _dp],
+    "sfem_set_pressure_surface": [_vp, _ip, C.c_int64, C.c_double],
+    "sfem_set_element_lame": [_vp, _dp, _dp],
+    "sfem_set_instances": [_vp, C.c_int32, _i64p],
+    "sfem_instance_stats": [_vp, _dp, _ip],
     "sfem_compute_gradients": [_vp, _dp, _dp],
     "sfem_matvec": [_vp, _dp, _dp],
     "sfem_dot": [_vp, _dp, _dp, _dp],
@@ -105,6 +109,7 @@ SIGNATURES = {
     "sfem_adjoint": [_vp, _dp, C.c_double, C.c_int32, _dp, _dp],
     "sfem_gnn_num_params": [_ip],
     "sfem_gnn_init": [_vp, C.c_uint64],
+    "sfem_gnn_set_loss": [_vp, C.c_int32],
     "sfem_gnn_get_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_set_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_apply": [_vp, _dp, _dp],

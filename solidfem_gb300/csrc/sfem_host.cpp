@@ -120,6 +120,12 @@ struct sfem_handle {
   double* partial = nullptr;  // 3 * n_slots values (float passes use it as floats)
   double* etmp = nullptr;     // E scratch doubles
   GnnState* gnn = nullptr;    // learned preconditioner (sfem_gnn_init)
+  // follower pressure surface (sfem_set_pressure_surface)
+  int64_t n_tris = 0;
+  int32_t *tri = nullptr, *tptr = nullptr, *tent = nullptr;
+  double* ptf = nullptr;
+  double pressure = 0.0;
+  PressureView pres() const { return PressureView{n_tris, tri, tptr, tent, ptf, pressure}; }
   // scratch
   double* fe = nullptr;  // 12 E doubles (float passes use it as 12 E floats)
   double* partials = nullptr;
@@ -244,8 +250,10 @@ int sync(sfem_handle* h) {
 int residual(sfem_handle* h, double* rnorm, int* n_inverted) {
   CU(cudaMemsetAsync(h->ninv, 0, sizeof(int), h->stream));
   element_pass<double>(h, MODE_FORCE, h->u, nullptr, h->fe, nullptr, h->ninv, nullptr);
+  const PressureView pv = h->pres();
+  if (h->n_tris > 0) launch_pressure_tris(pv, h->x0, h->u, h->ff, h->stream);
   launch_gather_force(h->nbc, h->N, h->csr(), h->fe, h->mass, h->fext, h->grav, h->ff, h->r64, h->red(),
-                      h->dres, h->stream);
+                      h->dres, h->stream, h->n_tris > 0 ? &pv : nullptr);
   CU(cudaMemcpyAsync(h->dres_h, h->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   int ninv_h = 0;
   CU(cudaMemcpyAsync(&ninv_h, h->ninv, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -435,10 +443,12 @@ void build_patches(const std::vector<int4>& tt, const std::vector<double>& x0, i
     }
     for (size_t j = 0; j < nn; j++) deg[j + 1] += deg[j];
     std::vector<uint16_t> fill(deg.begin(), deg.end() - 1);
+    // entries are the shared-memory offsets of (element i, corner j) in the kernel's
+    // element-result rows: kFeStride * i + 3 * j
     for (size_t i = 0; i < ne; i++) {
       const ushort4 l = pb.lidx[e0 + i];
       const unsigned short li[4] = {l.x, l.y, l.z, l.w};
-      for (int j = 0; j < 4; j++) pb.lent[4 * e0 + fill[li[j]]++] = (uint16_t)((i << 2) | j);
+      for (int j = 0; j < 4; j++) pb.lent[4 * e0 + fill[li[j]]++] = (uint16_t)(kFeStride * i + 3 * j);
     }
     for (size_t j = 0; j <= nn; j++) pb.lptr.push_back(deg[j]);
     for (size_t j = 0; j < nn; j++) pb.pnode.push_back(nodes[j]);
@@ -708,7 +718,8 @@ int sfem_destroy(sfem_handle* h) {
   if (!h) return SFEM_OK;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm};
+  void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
+                   h->ptf};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
@@ -912,6 +923,121 @@ int sfem_set_element_youngs_dev(sfem_handle* h, const double* young_e_dev) {
   return SFEM_OK;
 }
 
+int sfem_set_element_lame(sfem_handle* h, const double* mu_e, const double* lambda_e) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!mu_e || !lambda_e) {
+    h->has_scale = h->has_scale_la = false;
+    return SFEM_OK;
+  }
+  const size_t E = (size_t)h->E;
+  if (!h->young_e) {
+    TRY(dalloc(&h->young_e, E));
+    TRY(dalloc(&h->scale64, E));
+    TRY(dalloc(&h->scale32, E));
+  }
+  if (!h->scale_la64) {
+    TRY(dalloc(&h->scale_la64, E));
+    TRY(dalloc(&h->scale_la32, E));
+  }
+  std::vector<double> sm(E), sl(E);
+  for (size_t k = 0; k < E; k++) {
+    const int32_t e = h->perm_h[k];
+    sm[k] = mu_e[e] / h->mu;
+    sl[k] = lambda_e[e] / h->lambda;
+  }
+  CU(cudaMemcpyAsync(h->scale64, sm.data(), E * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->scale_la64, sl.data(), E * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_convert<double, float>(h->E, h->scale64, h->scale32, h->stream);
+  launch_convert<double, float>(h->E, h->scale_la64, h->scale_la32, h->stream);
+  h->has_scale = true;
+  h->has_scale_la = true;
+  return sync(h);
+}
+
+int sfem_set_pressure_surface(sfem_handle* h, const int32_t* tris, int64_t n_tris, double pressure) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  int32_t** bufs[] = {&h->tri, &h->tptr, &h->tent};
+  for (int32_t** b : bufs)
+    if (*b) {
+      cudaFree(*b);
+      *b = nullptr;
+    }
+  if (h->ptf) cudaFree(h->ptf);
+  h->ptf = nullptr;
+  h->n_tris = 0;
+  h->pressure = pressure;
+  if (!tris || n_tris <= 0) return SFEM_OK;
+  std::vector<int32_t> t(3 * (size_t)n_tris), ptr((size_t)h->N + 1, 0), ent(3 * (size_t)n_tris);
+  for (int64_t i = 0; i < 3 * n_tris; i++) {
+    if (tris[i] < 0 || tris[i] >= h->N) return fail(SFEM_ERR_INVALID, "pressure triangle index out of range");
+    t[i] = h->map[tris[i]];
+    ptr[t[i] + 1]++;
+  }
+  for (int64_t i = 0; i < h->N; i++) ptr[i + 1] += ptr[i];
+  {
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int64_t i = 0; i < 3 * n_tris; i++) ent[fill[t[i]]++] = (int32_t)(i / 3);
+  }
+  TRY(dalloc(&h->tri, t.size()));
+  TRY(dalloc(&h->tptr, ptr.size()));
+  TRY(dalloc(&h->tent, ent.size()));
+  TRY(dalloc(&h->ptf, 3 * (size_t)n_tris));
+  CU(cudaMemcpyAsync(h->tri, t.data(), t.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->tptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->tent, ent.data(), ent.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  h->n_tris = n_tris;
+  return sync(h);
+}
+
+int sfem_set_instances(sfem_handle* h, int32_t k, const int64_t* node_offsets) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (k <= 0 || !node_offsets) {
+    h->n_inst = 0;
+    return SFEM_OK;
+  }
+  if (node_offsets[0] != 0 || node_offsets[k] != h->N) return fail(SFEM_ERR_INVALID, "instance offsets must span [0, N)");
+  std::vector<int64_t> seg(k + 1, 0);
+  for (int q = 0; q < k; q++) {
+    if (node_offsets[q + 1] < node_offsets[q]) return fail(SFEM_ERR_INVALID, "instance offsets must increase");
+    int64_t nfree = 0;
+    for (int64_t i = node_offsets[q]; i < node_offsets[q + 1]; i++) nfree += h->map[i] >= h->nbc ? 1 : 0;
+    seg[q + 1] = seg[q] + 3 * nfree;
+  }
+  // free nodes keep their relative order, so each instance is one contiguous free-DOF segment
+  for (int q = 0; q < k; q++)
+    for (int64_t i = node_offsets[q]; i < node_offsets[q + 1]; i++)
+      if (h->map[i] >= h->nbc && (3 * (h->map[i] - h->nbc) < seg[q] || 3 * (h->map[i] - h->nbc) >= seg[q + 1]))
+        return fail(SFEM_ERR_INVALID, "instance nodes are not contiguous");
+  if (h->inst_seg) cudaFree(h->inst_seg);
+  if (h->inst_active) cudaFree(h->inst_active);
+  if (h->inst_norm) cudaFree(h->inst_norm);
+  h->inst_seg = nullptr;
+  h->inst_active = nullptr;
+  h->inst_norm = nullptr;
+  TRY(dalloc(&h->inst_seg, (size_t)k + 1));
+  TRY(dalloc(&h->inst_active, (size_t)k));
+  TRY(dalloc(&h->inst_norm, (size_t)k));
+  CU(cudaMemcpyAsync(h->inst_seg, seg.data(), seg.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  std::vector<int32_t> act(k, 1);
+  CU(cudaMemcpyAsync(h->inst_active, act.data(), k * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  h->n_inst = k;
+  h->inst_rel.assign(k, 1.0);
+  h->inst_its.assign(k, 0);
+  return sync(h);
+}
+
+int sfem_instance_stats(const sfem_handle* h, double* rel_res, int32_t* newton_iters) {
+  TRY(check_handle(h));
+  for (int q = 0; q < h->n_inst; q++) {
+    if (rel_res) rel_res[q] = h->inst_rel[q];
+    if (newton_iters) newton_iters[q] = h->inst_its[q];
+  }
+  return SFEM_OK;
+}
+
 int sfem_set_nodal_loads(sfem_handle* h, const double* f) {
   TRY(check_handle(h));
   TRY(set_device(h));
@@ -1098,10 +1224,17 @@ int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
   const bool pc = precond == SFEM_PC_JACOBI;
   sfem_pcg_stats ps{};
   int st;
+  const bool masked = h->n_inst > 0;
+  if (masked) launch_segment_mask<double>(h->n_inst, h->inst_seg, h->inst_active, h->r64 + o, h->stream);
   if (h->precision == SFEM_FP64) {
     KrylovWs<double>& w = h->k64;
     if (pc) TRY(jacobi<double>(h, w.dinv, nullptr));
-    st = pcg_device<double>(h, h->u, h->r64, w.x, pc ? w.dinv : nullptr, eta, max_cg, 0, &ps);
+    if (masked) {
+      // the unpreconditioned case masks a copy of the identity
+      if (!pc) CU(cudaMemcpyAsync(w.dinv, w.ones, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+      launch_segment_mask<double>(h->n_inst, h->inst_seg, h->inst_active, w.dinv + o, h->stream);
+    }
+    st = pcg_device<double>(h, h->u, h->r64, w.x, (pc || masked) ? w.dinv : nullptr, eta, max_cg, 0, &ps);
     if (st < 0) return st;
     CU(cudaMemcpyAsync(h->tmp64 + o, w.x + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
   } else {
@@ -1109,7 +1242,11 @@ int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
     const float* u32 = disp<float>(h);
     launch_convert<double, float>((int64_t)n, h->r64 + o, w.b + o, h->stream);
     if (pc) TRY(jacobi<float>(h, w.dinv, nullptr));
-    st = pcg_device<float>(h, u32, w.b, w.x, pc ? w.dinv : nullptr, eta, max_cg, 0, &ps);
+    if (masked) {
+      if (!pc) CU(cudaMemcpyAsync(w.dinv, w.ones, 3 * (size_t)h->N * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+      launch_segment_mask<float>(h->n_inst, h->inst_seg, h->inst_active, w.dinv + o, h->stream);
+    }
+    st = pcg_device<float>(h, u32, w.b, w.x, (pc || masked) ? w.dinv : nullptr, eta, max_cg, 0, &ps);
     if (st < 0) return st;
     launch_convert<float, double>((int64_t)n, w.x + o, h->tmp64 + o, h->stream);
   }
@@ -1118,13 +1255,50 @@ int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
   return 0;
 }
 
+// Independent instances: per-instance residual norms of r64, activity flags (an instance
+// stays active while |r_k| > rel_tol |r_k(x_0)| and above abs_tol); returns true when all
+// instances have converged.  The first call records |r_k(x_0)|.
+int instances_update(sfem_handle* h, const sfem_newton_opts& op, bool first, bool* all_done) {
+  const size_t o = 3 * (size_t)h->nbc;
+  const int K = h->n_inst;
+  launch_segment_norms(K, h->inst_seg, h->r64 + o, h->inst_norm, h->stream);
+  std::vector<double> nk(K);
+  CU(cudaMemcpyAsync(nk.data(), h->inst_norm, K * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  if (first) {
+    h->inst_r0 = nk;
+    h->inst_its.assign(K, 0);
+  }
+  std::vector<int32_t> act(K);
+  bool done = true;
+  for (int k = 0; k < K; k++) {
+    h->inst_rel[k] = h->inst_r0[k] > 0 ? nk[k] / h->inst_r0[k] : 0.0;
+    const bool conv = !(nk[k] > op.rel_tol * h->inst_r0[k]) || (op.abs_tol > 0 && nk[k] <= op.abs_tol);
+    act[k] = conv ? 0 : 1;
+    if (!conv) done = false;
+  }
+  CU(cudaMemcpyAsync(h->inst_active, act.data(), K * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  TRY(sync(h));
+  *all_done = done;
+  return 0;
+}
+
 int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, double* rn_io, int* nit, int* cgit,
                  int* cuts, int max_newton) {
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
   double rn = *rn_io, rprev = rn, eta = op.eta_max;
   const int max_bis = op.max_bisection > 0 ? op.max_bisection : 30;
+  const bool inst = h->n_inst > 0;
+  if (inst) h->inst_rel.assign(h->n_inst, 1.0);
   for (int k = 0; k < max_newton; k++) {
-    if (rn <= op.rel_tol * r_ref || (op.abs_tol > 0 && rn <= op.abs_tol)) {
+    if (inst) {
+      bool all = false;
+      TRY(instances_update(h, op, k == 0, &all));
+      if (all) {
+        *rn_io = rn;
+        return SFEM_OK;
+      }
+    } else if (rn <= op.rel_tol * r_ref || (op.abs_tol > 0 && rn <= op.abs_tol)) {
       *rn_io = rn;
       return SFEM_OK;
     }
@@ -1226,8 +1400,19 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
     }
     rprev = rn;
     rn = rnew;
+    if (inst) {
+      std::vector<int32_t> act(h->n_inst);
+      CU(cudaMemcpyAsync(act.data(), h->inst_active, h->n_inst * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+      TRY(sync(h));
+      for (int q = 0; q < h->n_inst; q++) h->inst_its[q] += act[q];
+    }
   }
   *rn_io = rn;
+  if (inst) {
+    bool all = false;
+    TRY(instances_update(h, op, false, &all));
+    return all ? SFEM_OK : SFEM_NOT_CONVERGED;
+  }
   return (rn <= op.rel_tol * r_ref || (op.abs_tol > 0 && rn <= op.abs_tol)) ? SFEM_OK : SFEM_NOT_CONVERGED;
 }
 
@@ -1430,6 +1615,9 @@ struct GnnState {
   float *z = nullptr, *rprev = nullptr;  // FCG vectors (3N)
   std::vector<float*> R, Ee;             // dataset: residual and correction (free block, 3n)
   std::vector<float> cinv;               // 1 / (e . r) per sample
+  std::vector<float> rinv;               // 1 / (r . r) per sample
+  float* tmp = nullptr;                  // 3N scratch
+  int loss_mode = 0;                     // 0: energy norm of the error, 1: residual norm
   int adam_t = 0;
   bool train_bufs = false;
   gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg}; }
@@ -1437,7 +1625,8 @@ struct GnnState {
 
 void gnn_free(GnnState* g) {
   void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->fixed_nb, g->params, g->grad, g->m, g->v, g->Wb, g->Wtb,
-                  g->x, g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->sc, g->losses, g->z, g->rprev};
+                  g->x, g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->sc, g->losses, g->z, g->rprev,
+                  g->tmp};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int l = 0; l <= gnn::NL; l++) {
@@ -1490,19 +1679,30 @@ void gnn_apply_dev(sfem_handle* h, const float* r, float* out, const int* done, 
                       train ? g->x : nullptr, out, done, h->stream);
 }
 
-// loss of one sample (energy norm) and the parameter gradient into g->grad; loss into *loss_dev
-int gnn_loss_grad_dev(sfem_handle* h, const float* r, const float* e, float cinv, float* loss_dev) {
+// loss of one sample and the parameter gradient into g->grad; loss into *loss_dev.
+//   energy mode:   d = M(r) - e,      L = d.Kd / (e.r),   dL/dM = 2 K d / (e.r)
+//   residual mode: d = K M(r) - r,    L = d.d / (r.r),    dL/dM = 2 K d / (r.r)
+int gnn_loss_grad_dev(sfem_handle* h, const float* r, const float* e, float cinv, float rinv, float* loss_dev) {
   GnnState* g = h->gnn;
   TRY(gnn_train_buffers(h));
   KrylovWs<float>& w = h->k32;
   const size_t o = 3 * (size_t)h->nbc, n3 = 3 * (size_t)g->n;
   float* out = g->z + o;
   gnn_apply_dev(h, r, out, nullptr, true);
-  // d = M(r) - e into a full-length vector with a zero fixed block, q = K d
-  gnn::launch_sub((int64_t)n3, out, e, w.b + o, h->stream);
-  hvp<float>(h, w.u, w.b, w.q, nullptr);
   float* Go = g->rprev + o;
-  gnn::launch_loss((int64_t)n3, w.b + o, w.q + o, cinv, Go, g->spart, g->scount, loss_dev, h->stream);
+  if (g->loss_mode == 0) {
+    // d = M(r) - e into a full-length vector with a zero fixed block, q = K d
+    gnn::launch_sub((int64_t)n3, out, e, w.b + o, h->stream);
+    hvp<float>(h, w.u, w.b, w.q, nullptr);
+    gnn::launch_loss((int64_t)n3, w.b + o, w.q + o, cinv, Go, g->spart, g->scount, loss_dev, h->stream);
+  } else {
+    CU(cudaMemcpyAsync(w.b + o, out, n3 * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    hvp<float>(h, w.u, w.b, w.q, nullptr);                 // q = K M(r)
+    gnn::launch_sub((int64_t)n3, w.q + o, r, w.b + o, h->stream);  // d = K M(r) - r
+    hvp<float>(h, w.u, w.b, w.q, nullptr);                 // q = K d
+    gnn::launch_loss((int64_t)n3, w.b + o, w.q + o, rinv, Go, g->spart, g->scount, g->spart + 4001, h->stream);
+    gnn::launch_loss((int64_t)n3, w.b + o, w.b + o, rinv, g->tmp + o, g->spart, g->scount, loss_dev, h->stream);
+  }
   gnn::launch_backward(g->graph(), Go, g->params, g->Wtb, g->sc, g->h, g->u, g->x, g->G0, g->G1, g->G2, g->wpart,
                        g->grad, h->stream);
   CU(cudaGetLastError());
@@ -1673,6 +1873,7 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   TRY(dalloc(&g->sc, 1));
   TRY(dalloc(&g->z, 3 * (size_t)h->N));
   TRY(dalloc(&g->rprev, 3 * (size_t)h->N));
+  TRY(dalloc(&g->tmp, 3 * (size_t)h->N));
   CU(cudaMemcpyAsync(g->ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
   if (!idx.empty())
     CU(cudaMemcpyAsync(g->idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
@@ -1686,6 +1887,14 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   CU(cudaMemsetAsync(g->rprev, 0, 3 * (size_t)h->N * sizeof(float), h->stream));
   gnn::launch_pack(g->params, g->Wb, g->Wtb, h->stream);
   return sync(h);
+}
+
+int sfem_gnn_set_loss(sfem_handle* h, int32_t mode) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  if (mode != 0 && mode != 1) return fail(SFEM_ERR_INVALID, "loss mode is 0 (energy) or 1 (residual)");
+  h->gnn->loss_mode = mode;
+  return SFEM_OK;
 }
 
 int sfem_gnn_get_params(sfem_handle* h, float* params) {
@@ -1736,8 +1945,11 @@ int sfem_gnn_loss_grad(sfem_handle* h, const double* r_free, const double* e_fre
   TRY(gnn_refresh_diag(h));
   std::vector<double> er(n);
   std::vector<double> rh(r_free, r_free + n), eh(e_free, e_free + n);
-  double c = 0;
-  for (size_t i = 0; i < n; i++) c += eh[i] * rh[i];
+  double c = 0, rr = 0;
+  for (size_t i = 0; i < n; i++) {
+    c += eh[i] * rh[i];
+    rr += rh[i] * rh[i];
+  }
   float *rd = nullptr, *ed = nullptr, *ld = nullptr;
   TRY(dalloc(&rd, n));
   TRY(dalloc(&ed, n));
@@ -1746,7 +1958,7 @@ int sfem_gnn_loss_grad(sfem_handle* h, const double* r_free, const double* e_fre
   launch_convert<double, float>((int64_t)n, h->tmp64 + o, rd, h->stream);
   CU(cudaMemcpyAsync(h->tmp64b + o, e_free, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   launch_convert<double, float>((int64_t)n, h->tmp64b + o, ed, h->stream);
-  int st = gnn_loss_grad_dev(h, rd, ed, (float)(1.0 / c), ld);
+  int st = gnn_loss_grad_dev(h, rd, ed, (float)(1.0 / c), (float)(1.0 / rr), ld);
   float lf = 0;
   if (st == 0) {
     cudaMemcpyAsync(&lf, ld, sizeof(float), cudaMemcpyDeviceToHost, h->stream);
@@ -1819,14 +2031,17 @@ int sfem_gnn_collect(sfem_handle* h, const double* b_free, int32_t every, int32_
   int added = 0;
   for (size_t j = 0; j < rs.size(); j++) {
     gnn::launch_sub(n, w.x + o, xs[j], xs[j], h->stream);
-    float cf = 0;
+    float cf = 0, rf = 0;
     gnn::launch_loss(n, xs[j], rs[j], 1.f, g->rprev + o, g->spart, g->scount, g->spart + 4000, h->stream);
+    gnn::launch_loss(n, rs[j], rs[j], 1.f, g->rprev + o, g->spart, g->scount, g->spart + 4002, h->stream);
     CU(cudaMemcpyAsync(&cf, g->spart + 4000, sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(&rf, g->spart + 4002, sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     TRY(sync(h));
-    if (cf > 0.f && std::isfinite(cf)) {
+    if (cf > 0.f && std::isfinite(cf) && rf > 0.f && std::isfinite(rf)) {
       g->R.push_back(rs[j]);
       g->Ee.push_back(xs[j]);
       g->cinv.push_back(1.f / cf);
+      g->rinv.push_back(1.f / rf);
       added++;
     } else {
       cudaFree(rs[j]);
@@ -1852,6 +2067,7 @@ int sfem_gnn_clear_dataset(sfem_handle* h) {
   h->gnn->R.clear();
   h->gnn->Ee.clear();
   h->gnn->cinv.clear();
+  h->gnn->rinv.clear();
   return SFEM_OK;
 }
 
@@ -1875,7 +2091,7 @@ int sfem_gnn_train(sfem_handle* h, int32_t steps, float lr, uint64_t seed, float
   std::mt19937_64 rng(seed);
   for (int t = 0; t < steps; t++) {
     const size_t j = (size_t)(rng() % g->R.size());
-    TRY(gnn_loss_grad_dev(h, g->R[j], g->Ee[j], g->cinv[j], g->losses + t));
+    TRY(gnn_loss_grad_dev(h, g->R[j], g->Ee[j], g->cinv[j], g->rinv[j], g->losses + t));
     g->adam_t++;
     gnn::launch_adam(g->grad, g->params, g->m, g->v, lr, g->adam_t, 1.f, g->Wb, g->Wtb, h->stream);
     if ((t & 63) == 63) TRY(sync(h));

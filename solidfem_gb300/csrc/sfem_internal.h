@@ -65,8 +65,8 @@ struct CgScalars {
 //   elem_off[c] .. elem_off[c+1]   its elements
 //   node_off[c] .. node_off[c+1]   its node slots; pnode[slot] = global node id,
 //                                  or ~id if the node belongs to several patches
-//   lptr[node_off[c] + c + j]      local CSR: entries lent[4 elem_off[c] + t] =
-//                                  (local element << 2 | corner), in element order
+//   lptr[node_off[c] + c + j]      local CSR: entries lent[4 elem_off[c] + t] = shared-memory
+//                                  offset kFeStride * local element + 3 * corner, element order
 //   lidx[e]                        local node ids of element e's four corners
 // Shared free nodes are summed by a second pass over bnode/bptr/bslot.
 template <typename T>
@@ -113,6 +113,7 @@ void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* 
 
 constexpr int kPatchElems = 768;
 constexpr int kPatchNodes = 512;
+constexpr int kFeStride = 13;  // odd row stride of the element results in shared memory
 
 // ---- fused patch Hessian-vector product: q = K p (negated force differential) ----
 // writes q for nodes owned by one patch and partials for shared nodes; the
@@ -133,9 +134,20 @@ void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBo
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
 
 // ---- node gathers (FP64 residual / T HVP / T diagonal) ----
+// follower pressure (FemPhysicsMatrixFree::ComputePressureForces): per triangle the force
+// ff * (area / 3) * pressure * unit normal at the current positions, summed per node
+struct PressureView {
+  int64_t n_tris;
+  const int32_t* tri;   // 3 per triangle, reshuffled node indices
+  const int32_t* tptr;  // node -> triangle CSR (N + 1)
+  const int32_t* tent;
+  double* ptf;          // 3 per triangle (scratch)
+  double pressure;
+};
+void launch_pressure_tris(PressureView pv, const double* x0, const double* u, double ff, cudaStream_t st);
 void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
                          const double* fext, const double* grav, double ff, double* r, Reduce red,
-                         double* rr_out, cudaStream_t st);
+                         double* rr_out, cudaStream_t st, const PressureView* pv = nullptr);
 template <typename T>
 void launch_gather_hvp(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, const T* p, T* q, Reduce red,
                        CgScalars* s, cudaStream_t st);

@@ -694,16 +694,48 @@ __device__ __forceinline__ void gather_node(NodeCsr csr, const T* __restrict__ f
   }
 }
 
+__global__ void __launch_bounds__(kThreads) k_pressure_tris(PressureView pv, const double* __restrict__ x0,
+                                                            const double* __restrict__ u, double ff) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < pv.n_tris; t += (int64_t)gridDim.x * blockDim.x) {
+    double p[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int64_t o = 3 * (int64_t)pv.tri[3 * t + k];
+#pragma unroll
+      for (int c = 0; c < 3; c++) p[k][c] = x0[o + c] + u[o + c];
+    }
+    const double a[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+    const double b[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+    const double n[3] = {a[1] * b[2] - b[1] * a[2], -a[0] * b[2] + a[2] * b[0], a[0] * b[1] - b[0] * a[1]};
+    const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double s = ff * (0.5 * len / 3.0) * pv.pressure / len;
+#pragma unroll
+    for (int c = 0; c < 3; c++) pv.ptf[3 * t + c] = s * n[c];
+  }
+}
+void launch_pressure_tris(PressureView pv, const double* x0, const double* u, double ff, cudaStream_t st) {
+  count_launch();
+  k_pressure_tris<<<grid_for(pv.n_tris), kThreads, 0, st>>>(pv, x0, u, ff);
+}
+
 __global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t N, NodeCsr csr,
                                                            const double* __restrict__ fe,
                                                            const double* __restrict__ mass,
                                                            const double* __restrict__ fext, double g0, double g1,
                                                            double g2, double ff, double* __restrict__ r,
-                                                           Reduce red, double* rr_out) {
+                                                           Reduce red, double* rr_out, PressureView pv) {
   double acc = 0.0;
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     double f[3];
     gather_node(csr, fe, g, f);
+    if (pv.n_tris > 0) {
+      for (int k = pv.tptr[g]; k < pv.tptr[g + 1]; k++) {
+        const int64_t t = pv.tent[k];
+        f[0] += pv.ptf[3 * t];
+        f[1] += pv.ptf[3 * t + 1];
+        f[2] += pv.ptf[3 * t + 2];
+      }
+    }
     const double mf = mass[g] * ff;
     const double gr[3] = {g0, g1, g2};
 #pragma unroll
@@ -720,10 +752,11 @@ __global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t 
 
 void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
                          const double* fext, const double* grav, double ff, double* r, Reduce red, double* rr_out,
-                         cudaStream_t st) {
+                         cudaStream_t st, const PressureView* pv) {
   count_launch();
+  PressureView none{0, nullptr, nullptr, nullptr, nullptr, 0.0};
   k_gather_force<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, mass, fext, grav[0], grav[1], grav[2], ff,
-                                                        r, red, rr_out);
+                                                        r, red, rr_out, pv ? *pv : none);
 }
 
 template <typename T>
@@ -841,7 +874,6 @@ void launch_permute(int64_t E, const int32_t* perm, const double* in, double* ou
 // them per local node through the patch-local CSR (element order, deterministic)
 // and writes q = -sum for nodes that only this patch touches, or a partial for
 // shared nodes.  Block partials of p.q go to red.partials[c].
-constexpr int kFeStride = 13;  // odd stride: conflict-free shared-memory rows of 12 values
 
 template <typename T>
 struct ElemLoad {  // one element's data, loaded ahead of its use
@@ -945,8 +977,7 @@ __global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __re
     T f0 = T(0), f1 = T(0), f2 = T(0);
     const int t1 = lp[j + 1];
     for (int t = lp[j]; t < t1; t++) {
-      const int x = le[t];
-      const T* src = sfe + kFeStride * (x >> 2) + 3 * (x & 3);
+      const T* src = sfe + le[t];
       f0 += src[0];
       f1 += src[1];
       f2 += src[2];

@@ -62,6 +62,10 @@ class LearnedPreconditioner:
     def load(self, path: str) -> None:
         self.set_params(np.fromfile(path, dtype=np.float32))
 
+    def set_loss(self, mode: str) -> None:
+        """'energy': ||M(r) - e||_K^2 / (e.r);  'residual': ||K M(r) - r||^2 / (r.r)."""
+        nat.check(self._lib.sfem_gnn_set_loss(self.phys.handle, {"energy": 0, "residual": 1}[mode]))
+
     # ---- inference / gradients ----
     def apply(self, r_free) -> np.ndarray:
         r = np.ascontiguousarray(r_free, dtype=np.float64).ravel()

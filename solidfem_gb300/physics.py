@@ -153,6 +153,36 @@ class FemPhysicsMatrixFree:
             assert y.size == self.n_tets
             nat.check(self._lib.sfem_set_element_youngs(self._h, _dp(y)))
 
+    def SetBoundaryConditionsSurface(self, triangles, pressure):
+        """Follower pressure on a triangle list of original node indices (FemPhysicsMatrixFree.h:100)."""
+        t = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+        self._has_pressure = t.shape[0] > 0
+        nat.check(self._lib.sfem_set_pressure_surface(self._h, t.ctypes.data_as(nat._ip), t.shape[0], float(pressure)))
+
+    def set_element_lame(self, mu_e, lambda_e):
+        """Per-element Lame parameters (caller's element order); None restores the uniform ones."""
+        if mu_e is None:
+            nat.check(self._lib.sfem_set_element_lame(self._h, None, None))
+            return
+        a = _f64(mu_e).ravel()
+        b = _f64(lambda_e).ravel()
+        assert a.size == b.size == self.n_tets
+        nat.check(self._lib.sfem_set_element_lame(self._h, _dp(a), _dp(b)))
+
+    def set_instances(self, node_offsets):
+        """Independent bodies: body q owns the nodes [node_offsets[q], node_offsets[q+1])."""
+        if node_offsets is None:
+            nat.check(self._lib.sfem_set_instances(self._h, 0, None))
+            return
+        o = np.ascontiguousarray(node_offsets, dtype=np.int64)
+        nat.check(self._lib.sfem_set_instances(self._h, o.size - 1, o.ctypes.data_as(nat._i64p)))
+
+    def instance_stats(self, k):
+        rel = np.zeros(k)
+        its = np.zeros(k, dtype=np.int32)
+        nat.check(self._lib.sfem_instance_stats(self._h, _dp(rel), its.ctypes.data_as(nat._ip)))
+        return rel, its
+
     def set_nodal_loads(self, f):
         """Dead loads (N, 3) in original node order (None clears)."""
         if f is None:
@@ -234,7 +264,8 @@ class FemPhysicsMatrixFree:
         hyperelastic materials and residual-norm backtracking for corotational (whose force
         is not the gradient of an energy)."""
         if ls_condition is None:
-            ls_condition = nat.LSC_RESIDUAL if self.material == nat.MMT_COROTATIONAL else nat.LSC_ARMIJO
+            nonconservative = self.material == nat.MMT_COROTATIONAL or getattr(self, "_has_pressure", False)
+            ls_condition = nat.LSC_RESIDUAL if nonconservative else nat.LSC_ARMIJO
         o = nat.NewtonOpts(rel_tol=rel_tol, abs_tol=abs_tol, max_newton=max_newton, max_cg=max_cg, eta_max=eta_max,
                            eta_min=eta_min, precond=precond, ls_condition=ls_condition,
                            max_bisection=max_bisection, verbose=int(verbose), load_steps=load_steps)

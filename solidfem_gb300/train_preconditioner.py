@@ -28,12 +28,14 @@ def slab_mesh(nx, ny, nz, jitter=0.2, seed=0):
     return box_lattice(nx, ny, nz, extent=(nx / 64.0, ny / 64.0, nz / 64.0), jitter=jitter, seed=seed)
 
 
-def train(dims=(64, 16, 16), seeds=256, every=25, max_snaps=12, steps=3000, lr=1e-3, init_seed=0, verbose=True):
+def train(dims=(64, 16, 16), seeds=256, every=25, max_snaps=12, steps=3000, lr=1e-3, init_seed=0, verbose=True,
+          loss="residual"):
     m = slab_mesh(*dims)
     fixed = m.face_nodes(2, 0)
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
                              material=3, precision="fp32")
     net = LearnedPreconditioner(p, seed=init_seed)
+    net.set_loss(loss)
     t0 = time.time()
     for s in range(seeds):
         p.set_nodal_loads(random_top_traction(m, seed=s))
@@ -42,7 +44,7 @@ def train(dims=(64, 16, 16), seeds=256, every=25, max_snaps=12, steps=3000, lr=1
     t0 = time.time()
     losses = net.train(steps=steps, lr=lr, seed=init_seed)
     t_train = time.time() - t0
-    info = {"dims": list(dims), "load_seeds": [0, seeds - 1], "pairs": net.dataset_size(), "every": every,
+    info = {"dims": list(dims), "load_seeds": [0, seeds - 1], "pairs": net.dataset_size(), "every": every, "loss": loss,
             "steps": steps, "lr": lr, "loss_first50": float(np.mean(losses[:50])),
             "loss_last50": float(np.mean(losses[-50:])), "collect_s": t_collect, "train_s": t_train,
             "material": "neo-Hookean E=1e5 nu=0.49, h=1/64, jitter 0.2h, bottom clamped, random top traction"}
@@ -60,9 +62,10 @@ def main():
     ap.add_argument("--max-snaps", type=int, default=12)
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--loss", default="residual", choices=["energy", "residual"])
     a = ap.parse_args()
     dims = tuple(int(v) for v in a.dims.split(","))
-    net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr)
+    net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr, loss=a.loss)
     net.save(a.out, meta=info)
     np.save(a.out.rsplit(".", 1)[0] + "_losses.npy", losses)
 

@@ -24,20 +24,24 @@ def test_graph_is_symmetric_mean_aggregation():
     assert fnb.any() and not fnb.all()
 
 
-def test_oracle_gradient_matches_central_differences():
+import pytest
+
+
+@pytest.mark.parametrize("mode", ["energy", "residual"])
+def test_oracle_gradient_matches_central_differences(mode):
     o, Am, fnb, dinv = small_problem()
     rng = np.random.default_rng(0)
     p = rng.normal(size=go.NPARAM) * 0.1
     r = rng.normal(size=3 * o.n_free)
     e, _, _ = o.pcg(r, diag=1.0 / dinv, tol=1e-12, max_iters=20000)  # a consistent pair: K e = r
     K = o.matvec
-    L, g = go.loss_grad(p, Am, fnb, r, dinv, e, K, bf16_layers=False)
+    L, g = go.loss_grad(p, Am, fnb, r, dinv, e, K, bf16_layers=False, mode=mode)
     idx = rng.choice(go.NPARAM, size=40, replace=False)
     for k in idx:
         h = 1e-5
         pp, pm = p.copy(), p.copy()
         pp[k] += h
         pm[k] -= h
-        fd = (go.loss_grad(pp, Am, fnb, r, dinv, e, K, bf16_layers=False)[0]
-              - go.loss_grad(pm, Am, fnb, r, dinv, e, K, bf16_layers=False)[0]) / (2 * h)
+        fd = (go.loss_grad(pp, Am, fnb, r, dinv, e, K, bf16_layers=False, mode=mode)[0]
+              - go.loss_grad(pm, Am, fnb, r, dinv, e, K, bf16_layers=False, mode=mode)[0]) / (2 * h)
         assert abs(fd - g[k]) <= 1e-6 * np.abs(g).max() + 1e-4 * abs(fd), (k, fd, g[k])

@@ -51,7 +51,8 @@ def test_forward_matches_fp64_oracle():
     assert err < 3e-2
 
 
-def test_gradients_match_fp64_oracle():
+@pytest.mark.parametrize("mode", ["energy", "residual"])
+def test_gradients_match_fp64_oracle(mode):
     m, fixed, _ = slab(24, 8, 8)
     p, net, o, Am, fnb, dinv = gpu_and_oracle(m, fixed, seed=4)
     rng = np.random.default_rng(2)
@@ -60,8 +61,9 @@ def test_gradients_match_fp64_oracle():
     net.set_params(prm)
     r = rng.normal(size=3 * o.n_free)
     e, _, _ = o.pcg(r, diag=1.0 / dinv, tol=1e-10, max_iters=20000)
+    net.set_loss(mode)
     Lg, gg = net.loss_grad(r, e)
-    Lo, go_ = go.loss_grad(net.get_params(), Am, fnb, r, dinv, e, o.matvec)
+    Lo, go_ = go.loss_grad(net.get_params(), Am, fnb, r, dinv, e, o.matvec, mode=mode)
     cos = float(gg @ go_) / (np.linalg.norm(gg) * np.linalg.norm(go_))
     print(f"loss GPU {Lg:.6f} oracle {Lo:.6f}; grad rel err {rel(gg, go_):.2e}, cosine {cos:.5f}")
     assert abs(Lg - Lo) <= 3e-2 * abs(Lo)

@@ -185,3 +185,31 @@ def test_exact_tangent_matches_finite_differences_of_gpu_residual(material):
     p.set_free_positions(x)
     fd = -(rp - rm) / (2 * h)
     assert rel(p.MatrixVectorMultiply(d), fd) <= 1e-7
+
+
+def test_follower_pressure_gradients_vs_oracle():
+    from solidfem_gb300.mesh import box_lattice
+
+    rng = np.random.default_rng(9)
+    m = box_lattice(10, 4, 3, extent=(2.5, 1.0, 0.75), jitter=0.2, seed=6)
+    fixed = m.face_nodes(0, 0)
+    tris = np.concatenate([m.face_triangles(2, 1), m.face_triangles(0, 1)])
+    orc = Oracle(m.nodes, m.tets, fixed, 2e5, 0.42, 1000.0, (0, 0, -9.81), 3)
+    orc.set_pressure_surface(tris, 1500.0)
+    g = dict(tets=m.tets, nodes=m.nodes, fixed=fixed, young=2e5, poisson=0.42, density=1000.0,
+             gravity=np.array([0, 0, -9.81]), material=3)
+    p = gpu_problem(g)
+    p.SetBoundaryConditionsSurface(tris, 1500.0)
+    x = orc.free_positions() + 0.02 * rng.normal(size=3 * orc.n_free)
+    orc.set_free_positions(x)
+    p.set_free_positions(x)
+    assert rel(p.ComputeGradients(), orc.gradients()) <= ELEM_TOL
+    # a static solve with the follower load converges (residual line search; the pressure
+    # stiffness is not in the product, as in the reference, so Newton converges linearly)
+    from solidfem_gb300 import FemPhysicsMatrixFree
+
+    q = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=2e7, poisson=0.42, density=1000.0,
+                             gravity=(0, 0, -9.81), material=3)
+    q.SetBoundaryConditionsSurface(tris, 1500.0)
+    st = q.newton_solve(rel_tol=1e-9, max_newton=100)
+    assert st["status"] == 0, st

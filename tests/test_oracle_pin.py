@@ -39,3 +39,20 @@ def test_oracle_bit_identical_to_reference(material, seed):
     assert ref.elastic_energy() == orc.elastic_energy()
     for a, b in zip(ref.force_param_grads(), orc.force_param_grads()):
         np.testing.assert_array_equal(a, b)
+
+
+def test_follower_pressure_bit_identical_to_reference():
+    rng = np.random.default_rng(5)
+    m = box_lattice(5, 3, 2, extent=(2.0, 1.0, 0.7), jitter=0.25, seed=4)
+    fixed = m.face_nodes(0, 0)
+    tris = np.concatenate([m.face_triangles(2, 1), m.face_triangles(0, 1)])
+    ref = RefHarness(m.nodes, m.tets, fixed, 2e5, 0.42, 1000.0, -9.81, True, 3)
+    orc = Oracle(m.nodes, m.tets, fixed, 2e5, 0.42, 1000.0, (0, 0, -9.81), 3)
+    ref.set_force_fraction(1.0)
+    ref.set_pressure_surface(tris, 1500.0)
+    orc.set_pressure_surface(tris, 1500.0)
+    x = orc.positions_shuffled() + 0.02 * rng.normal(size=(m.n_nodes, 3))
+    x[: orc.n_bcs] = orc.positions_shuffled()[: orc.n_bcs]
+    ref.set_positions_shuffled(x)
+    orc.set_positions_shuffled(x)
+    np.testing.assert_array_equal(ref.gradients(), orc.gradients())
