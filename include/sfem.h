@@ -227,12 +227,12 @@ int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max
                  double* dLdE, double* dLdf);
 
 /* ---- learned preconditioner (extension: the reference has no learned components) ----
- * A per-node graph network on the free-node mesh graph (3 message-passing layers, width 64,
- * BF16 weights and activations, FP32 accumulation on the tensor cores) maps a residual r to a
- * correction M(r) = D^-1 r + s * net(D^-1 r / s, log D, boundary flags); it replaces Jacobi
- * inside flexible (Polak-Ribiere) PCG when sfem_newton_opts.precond = SFEM_PC_LEARNED.
- * FP32 handles only.  Parameter vector layout: sfem_gnn_num_params floats
- * [We(64x8) be(64) {Wl(64x128) bl(64)} x3 Wd(3x64) bd(3)]. */
+ * A linear message-passing network S on the free-node mesh graph (3 layers, width 64, BF16
+ * weights and activations, FP32 accumulation on the tensor cores) defines the symmetric
+ * positive definite preconditioner M(r) = D^-1/2 (c x + S^T S x), x = D^-1/2 r, c > 0; it
+ * replaces Jacobi inside flexible (Polak-Ribiere) PCG when sfem_newton_opts.precond =
+ * SFEM_PC_LEARNED.  FP32 handles only.  Parameter vector layout: sfem_gnn_num_params floats
+ * [We(64x3) {Wl(64x128)} x3 log_c]. */
 int sfem_gnn_num_params(int32_t* n);
 int sfem_gnn_init(sfem_handle* h, uint64_t seed);
 int sfem_gnn_get_params(sfem_handle* h, float* params);
@@ -251,7 +251,10 @@ int sfem_gnn_collect(sfem_handle* h, const double* b_free, int32_t every, int32_
                      int32_t* n_added);
 int sfem_gnn_dataset_size(sfem_handle* h, int32_t* n);
 int sfem_gnn_clear_dataset(sfem_handle* h);
-/* Adam on the collected pairs, one seeded random pair per step; losses: steps floats (optional) */
+/* pairs per Adam step (gradient averaged over them); default 1 */
+int sfem_gnn_set_batch(sfem_handle* h, int32_t batch);
+/* Adam on the collected pairs, `batch` seeded random pairs per step; losses: steps floats
+ * (optional), the first pair's loss of each step */
 int sfem_gnn_train(sfem_handle* h, int32_t steps, float lr, uint64_t seed, float* losses);
 
 /* ---- instrumentation (no reference counterpart: the reference's PROFILE_SCOPE macros are

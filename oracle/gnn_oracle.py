@@ -1,27 +1,28 @@
 """TEST INFRASTRUCTURE ONLY: FP64 numpy restatement of the learned preconditioner
-(forward, energy-norm loss, backward) used to check the CUDA kernels' outputs and
-gradients.  The reference has no learned component, so this oracle is pinned by
-its own central finite differences (tests/test_gnn_oracle.py), not by the reference.
+(forward, loss, backward) used to check the CUDA kernels' outputs and gradients.  The
+reference has no learned component, so this oracle is pinned by its own central finite
+differences and by symmetry / positivity checks (tests/test_gnn_oracle.py), not by the
+reference.
 
-Network (free node i, width 64, 3 layers), the same definition as the library:
-  z = D^-1 r,  s = rms(z),  x_i = [z_i/s, -log D_i^-1 - mean(-log D^-1), fixed_nb_i, 1]
-  h0 = relu(We x + be);  h <- h + relu(Wl [h ; mean_{j~i} h_j] + bl);  M(r) = z + s (Wd h + bd)
-Layer weights may be rounded to BF16 to match the device's weight copies.
+Network, the same definition as the library (free nodes, width 64, 3 layers):
+  x = D^-1/2 r
+  S x:  h0 = x We^T;   h <- h + [h ; A h] Wl^T   (A: mean over mesh-graph neighbours)
+  M(r) = D^-1/2 (c x + S^T S x),   c = exp(log c)
+S is linear, so M is a fixed symmetric positive definite operator.  Layer weights may be
+rounded to BF16 to match the device's weight copies.
 """
 from __future__ import annotations
 
 import numpy as np
 import scipy.sparse as sp
 
-H, FIN, NL = 64, 8, 3
+H, FIN, NL = 64, 3, 3
 AIN = 2 * H
 OFF_WE = 0
-OFF_BE = OFF_WE + H * FIN
-OFF_L = OFF_BE + H
-L_STRIDE = H * AIN + H
-OFF_WD = OFF_L + NL * L_STRIDE
-OFF_BD = OFF_WD + 3 * H
-NPARAM = OFF_BD + 3
+OFF_L = OFF_WE + H * FIN
+L_STRIDE = H * AIN
+OFF_C = OFF_L + NL * L_STRIDE
+NPARAM = OFF_C + 1
 
 
 def bf16_round(a):
@@ -34,95 +35,96 @@ def bf16_round(a):
 
 
 def free_graph(tets_shuffled, n_bcs, n_nodes):
-    """Mean-aggregation matrix over the free-node graph (edges of the tets) and the
-    fixed-neighbour flags, in the reference's reshuffled free-node order."""
+    """Mean-aggregation matrix over the free-node graph (edges of the tets), in the
+    reference's reshuffled free-node order."""
     t = np.asarray(tets_shuffled, dtype=np.int64)
     a = t[:, [0, 0, 0, 1, 1, 2]].ravel()
     b = t[:, [1, 2, 3, 2, 3, 3]].ravel()
     n = n_nodes - n_bcs
-    fixed_nb = np.zeros(n, dtype=bool)
-    af, bf = a >= n_bcs, b >= n_bcs
-    fixed_nb[a[af & ~bf] - n_bcs] = True
-    fixed_nb[b[bf & ~af] - n_bcs] = True
-    keep = af & bf
+    keep = (a >= n_bcs) & (b >= n_bcs)
     i, j = a[keep] - n_bcs, b[keep] - n_bcs
     A = sp.coo_matrix((np.ones(2 * i.size), (np.concatenate([i, j]), np.concatenate([j, i]))), shape=(n, n)).tocsr()
-    A.data[:] = 1.0  # duplicates collapse to one edge
     A.sum_duplicates()
-    A.data[:] = 1.0
+    A.data[:] = 1.0  # duplicates collapse to one edge
     deg = np.asarray(A.sum(axis=1)).ravel()
-    Am = sp.diags(1.0 / np.maximum(deg, 1.0)) @ A
-    return Am.tocsr(), fixed_nb
+    return (sp.diags(1.0 / np.maximum(deg, 1.0)) @ A).tocsr()
 
 
 def unpack(p, bf16_layers=True):
     p = np.asarray(p, dtype=np.float64)
-    We = p[OFF_WE:OFF_BE].reshape(H, FIN)
-    be = p[OFF_BE:OFF_L]
-    Ws, bs = [], []
+    We = p[OFF_WE:OFF_L].reshape(H, FIN)
+    Ws = []
     for l in range(NL):
-        o = OFF_L + l * L_STRIDE
-        W = p[o:o + H * AIN].reshape(H, AIN)
+        W = p[OFF_L + l * L_STRIDE:OFF_L + (l + 1) * L_STRIDE].reshape(H, AIN)
         Ws.append(bf16_round(W) if bf16_layers else W)
-        bs.append(p[o + H * AIN:o + L_STRIDE])
-    Wd = p[OFF_WD:OFF_BD].reshape(3, H)
-    bd = p[OFF_BD:NPARAM]
-    return We, be, Ws, bs, Wd, bd
+    return We, Ws, float(np.exp(p[OFF_C]))
 
 
-def forward(p, Am, fixed_nb, r, dinv, bf16_layers=True):
-    r = r.reshape(-1, 3)
-    dinv = dinv.reshape(-1, 3)
-    We, be, Ws, bs, Wd, bd = unpack(p, bf16_layers)
-    z = r * dinv
-    s = np.sqrt(np.mean(z ** 2))
-    ld = -np.log(dinv)
-    x = np.concatenate([z / s, ld - ld.mean(), fixed_nb[:, None].astype(float), np.ones((z.shape[0], 1))], axis=1)
-    u0 = x @ We.T + be
-    h = np.maximum(u0, 0)
-    cache = {"x": x, "u": [u0], "h": [h], "a": [], "s": s, "z": z}
-    for l in range(NL):
+def s_forward(We, Ws, Am, x):
+    """h3 = S x and the layer inputs a_l = [h_l ; A h_l]."""
+    h = x @ We.T
+    acts = []
+    for W in Ws:
         a = np.concatenate([h, Am @ h], axis=1)
-        u = a @ Ws[l].T + bs[l]
-        h = h + np.maximum(u, 0)
-        cache["a"].append(a)
-        cache["u"].append(u)
-        cache["h"].append(h)
-    y = h @ Wd.T + bd
-    return z + s * y, cache
+        acts.append(a)
+        h = h + a @ W.T
+    return h, acts
 
 
-def loss_grad(p, Am, fixed_nb, r, dinv, e, Kmul, bf16_layers=True, mode="energy"):
+def s_transpose(We, Ws, Am, g):
+    """S^T g (g: n x H) -> n x 3."""
+    for W in reversed(Ws):
+        ga = g @ W
+        g = g + ga[:, :H] + Am.T @ ga[:, H:]
+    return g @ We
+
+
+def s_weight_grad(We, Ws, Am, x, cot):
+    """Gradient of <cot, S x> with respect to (We, W_1..W_NL), flattened like the parameters."""
+    _, acts = s_forward(We, Ws, Am, x)
+    g = np.zeros(OFF_C)
+    G = cot
+    for l in reversed(range(NL)):
+        W = Ws[l]
+        g[OFF_L + l * L_STRIDE:OFF_L + (l + 1) * L_STRIDE] = (G.T @ acts[l]).ravel()
+        ga = G @ W
+        G = G + ga[:, :H] + Am.T @ ga[:, H:]
+    g[OFF_WE:OFF_L] = (G.T @ x).ravel()
+    return g
+
+
+def forward(p, Am, r, dinv, bf16_layers=True):
+    r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
+    sd = np.sqrt(np.asarray(dinv, dtype=np.float64).reshape(-1, 3))
+    We, Ws, c = unpack(p, bf16_layers)
+    x = sd * r
+    h3, _ = s_forward(We, Ws, Am, x)
+    return (sd * (c * x + s_transpose(We, Ws, Am, h3))).ravel()
+
+
+def loss_grad(p, Am, r, dinv, e, Kmul, bf16_layers=True, mode="energy"):
     """Loss and gradient; Kmul(v) = K v (flat).
     energy:   ||M(r) - e||_K^2 / (e.r);   residual: ||K M(r) - r||^2 / (r.r)."""
-    out, c = forward(p, Am, fixed_nb, r, dinv, bf16_layers)
+    r = np.asarray(r, dtype=np.float64).ravel()
+    out = forward(p, Am, r, dinv, bf16_layers)
     if mode == "energy":
-        e = e.reshape(-1, 3)
-        d = out - e
-        q = Kmul(d.ravel()).reshape(-1, 3)
-        cc = float(e.ravel() @ r.ravel())
-        L = float(d.ravel() @ q.ravel()) / cc
+        d = out - np.ravel(e)
+        q = Kmul(d)
+        cc = float(np.ravel(e) @ r)
+        L = float(d @ q) / cc
         Go = 2.0 * q / cc
     else:
-        d = Kmul(out.ravel()) - r.ravel()
-        cc = float(r.ravel() @ r.ravel())
+        d = Kmul(out) - r
+        cc = float(r @ r)
         L = float(d @ d) / cc
-        Go = (2.0 * Kmul(d) / cc).reshape(-1, 3)
-    We, be, Ws, bs, Wd, bd = unpack(p, bf16_layers)
+        Go = 2.0 * Kmul(d) / cc
+    We, Ws, c = unpack(p, bf16_layers)
+    sd = np.sqrt(np.asarray(dinv, dtype=np.float64).reshape(-1, 3))
+    x = sd * r.reshape(-1, 3)
+    gy = sd * Go.reshape(-1, 3)
+    hx, _ = s_forward(We, Ws, Am, x)
+    hg, _ = s_forward(We, Ws, Am, gy)
     g = np.zeros(NPARAM)
-    gy = c["s"] * Go
-    h3 = c["h"][-1]
-    g[OFF_WD:OFF_BD] = (gy.T @ h3).ravel()
-    g[OFF_BD:NPARAM] = gy.sum(axis=0)
-    gh = gy @ Wd
-    for l in reversed(range(NL)):
-        gu = gh * (c["u"][l + 1] > 0)
-        o = OFF_L + l * L_STRIDE
-        g[o:o + H * AIN] = (gu.T @ c["a"][l]).ravel()
-        g[o + H * AIN:o + L_STRIDE] = gu.sum(axis=0)
-        ga = gu @ Ws[l]
-        gh = gh + ga[:, :H] + Am.T @ ga[:, H:]
-    gu0 = gh * (c["u"][0] > 0)
-    g[OFF_WE:OFF_BE] = (gu0.T @ c["x"]).ravel()
-    g[OFF_BE:OFF_L] = gu0.sum(axis=0)
+    g[:OFF_C] = s_weight_grad(We, Ws, Am, x, hg) + s_weight_grad(We, Ws, Am, gy, hx)
+    g[OFF_C] = c * float(np.sum(gy * x))
     return L, g

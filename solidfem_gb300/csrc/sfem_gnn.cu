@@ -12,77 +12,145 @@ static int blocks_for(int64_t n, int per) {
   return (int)(b < 1 ? 1 : b);
 }
 
-void launch_stat(int which, int64_t n3, const float* r, const float* dinv, float* partials, unsigned* counter,
-                 Scalars* sc, const int* done, cudaStream_t st) {
-  int grid = blocks_for(n3, 256);
-  if (grid > 1024) grid = 1024;
-  if (which == 0)
-    k_gnn_stat<0><<<grid, 256, 0, st>>>(n3, r, dinv, partials, counter, sc, done);
-  else
-    k_gnn_stat<1><<<grid, 256, 0, st>>>(n3, r, dinv, partials, counter, sc, done);
-}
-
-void launch_forward(const Graph& g, const float* r, const float* dinv, const uint8_t* fixed_nb, const float* params,
-                    const __nv_bfloat16* Wb, Scalars* sc, __nv_bfloat16* const* h, __nv_bfloat16* const* u, float* x,
-                    float* out, const int* done, cudaStream_t st) {
-  k_gnn_encode<<<blocks_for(g.n * 32, 256), 256, 0, st>>>(g.n, r, dinv, fixed_nb, params, sc, h[0], u ? u[0] : nullptr,
-                                                          x, done);
-  for (int l = 0; l < NL; l++)
-    k_gnn_layer_fwd<<<blocks_for(g.n, TILE), LT, 0, st>>>(g, h[l], Wb + (size_t)l * H * AIN,
-                                                          params + OFF_L + l * L_STRIDE + H * AIN, h[l + 1],
-                                                          u ? u[l + 1] : nullptr, done);
-  k_gnn_decode<<<blocks_for(g.n, 256), 256, 0, st>>>(g.n, h[NL], params, sc, r, dinv, out, done);
-}
-
-int launch_count_forward() { return 2 + NL; }
-
-void launch_backward(const Graph& g, const float* Go, const float* params, const __nv_bfloat16* Wtb, const Scalars* sc,
-                     __nv_bfloat16* const* h, __nv_bfloat16* const* u, const float* x, float* G0, float* G1,
-                     float* G2, float* partial, float* grad, cudaStream_t st) {
-  // decoder: G0 <- dL/dh3
-  const int nbd = blocks_for(g.n, 256);
-  k_gnn_decode_bwd<<<nbd, 256, 0, st>>>(g.n, h[NL], params, sc, Go, G0, partial);
-  k_gnn_reduce_cols<<<1, 256, 0, st>>>(nbd, 3 * H + 3, partial, grad + OFF_WD, 0);
-  static bool attr = false;
+template <bool WGRAD, typename GT>
+static void layer_bwd(const Graph& g, const __nv_bfloat16* hin, const GT* Gout, const __nv_bfloat16* Wt, float* Gself,
+                      float* Gmsg, float* partial, const int* done, cudaStream_t st) {
+  constexpr size_t smem = layer_bwd_smem(WGRAD);
+  static bool attr = false;  // per instantiation
   if (!attr) {
-    cudaFuncSetAttribute(k_gnn_layer_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLayerBwdSmem);
+    cudaFuncSetAttribute(k_gnn_layer_bwd<WGRAD, GT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  const int nbl = blocks_for(g.n, TILE);
-  float* Gout = G0;
-  for (int l = NL - 1; l >= 0; l--) {
-    // layer l maps h[l] -> h[l+1]; Gout = dL/dh[l+1]
-    k_gnn_layer_bwd<<<nbl, LT, kLayerBwdSmem, st>>>(g, h[l], u[l + 1], Gout, Wtb + (size_t)l * H * AIN, G1, G2,
-                                                    partial);
-    k_gnn_reduce_cols<<<(LPART + 255) / 256, 256, 0, st>>>(nbl, LPART, partial, grad + OFF_L + l * L_STRIDE, 0);
-    // G0 <- dL/dh[l]
-    k_gnn_msg_scatter<<<blocks_for(g.n * 32, 256), 256, 0, st>>>(g, G1, G2, G0);
-    Gout = G0;
-  }
-  const int nbe = blocks_for(g.n, 64);
-  k_gnn_encode_bwd<<<nbe, 256, 0, st>>>(g.n, G0, u[0], x, partial);
-  k_gnn_reduce_cols<<<(H * FIN + H + 255) / 256, 256, 0, st>>>(nbe, H * FIN + H, partial, grad + OFF_WE, 0);
+  count_launch();
+  k_gnn_layer_bwd<WGRAD, GT><<<blocks_for(g.n, TILE), LT, smem, st>>>(g, hin, Gout, Wt, Gself, Gmsg, partial, done);
 }
 
-int launch_count_backward() { return 2 + NL * 3 + 2; }
+void launch_encode(const Graph& g, const float* v, const float* dinv, const float* params, __nv_bfloat16* h0,
+                   float* xout, const int* done, cudaStream_t st) {
+  count_launch();
+  k_gnn_encode<<<blocks_for(g.n * 32, 256), 256, 0, st>>>(g.n, v, dinv, params, h0, xout, done);
+}
+
+void launch_layers_fwd(const Graph& g, const __nv_bfloat16* Wb, __nv_bfloat16* const* h, const int* done,
+                       cudaStream_t st) {
+  for (int l = 0; l < NL; l++) {
+    count_launch();
+    k_gnn_layer_fwd<<<blocks_for(g.n, TILE), LT, 0, st>>>(g, h[l], Wb + (size_t)l * H * AIN, h[l + 1], done);
+  }
+}
+
+static int inf_grid(int64_t n) {
+  static int cap = 0;  // resident CTAs of the layer kernel on this device
+  if (cap == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gnn_layer_inf<false, false, false>, LT, 0);
+    cap = std::max(1, sms) * std::max(1, per);
+  }
+  const int64_t tiles = (n + TILE - 1) / TILE;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, cap));
+}
+
+void launch_apply(const Graph& g, const float* r, const float* dinv, const float* params, const __nv_bfloat16* Wb,
+                  __nv_bfloat16* const* h, float* out, const int* done, cudaStream_t st) {
+  const size_t per = (size_t)H * AIN;
+  const __nv_bfloat16* Wsb = Wb + 2 * NL * per;
+  const int grid = inf_grid(g.n);
+  static_assert(NL == 3, "the launch sequence below is written for three layers");
+  // S: h1 = L1(We x), h2, h3
+  count_launch();
+  k_gnn_layer_inf<true, false, false><<<grid, LT, 0, st>>>(g, nullptr, r, dinv, params, Wb, h[1], nullptr, done);
+  count_launch();
+  k_gnn_layer_inf<false, false, false><<<grid, LT, 0, st>>>(g, h[1], r, dinv, params, Wb + per, h[2], nullptr, done);
+  count_launch();
+  k_gnn_layer_inf<false, false, false><<<grid, LT, 0, st>>>(g, h[2], r, dinv, params, Wb + 2 * per, h[3], nullptr,
+                                                              done);
+  // S^T: L3^T h3 -> h[1], L2^T -> h[2], L1^T and We^T -> out
+  count_launch();
+  k_gnn_layer_inf<false, true, false><<<grid, LT, 0, st>>>(g, h[3], r, dinv, params, Wsb + 2 * per, h[1], nullptr,
+                                                             done);
+  count_launch();
+  k_gnn_layer_inf<false, true, false><<<grid, LT, 0, st>>>(g, h[1], r, dinv, params, Wsb + per, h[2], nullptr, done);
+  count_launch();
+  k_gnn_layer_inf<false, true, true><<<grid, LT, 0, st>>>(g, h[2], r, dinv, params, Wsb, nullptr, out, done);
+}
+
+// the training forward: activations h0..h3 of S at x (kept, with x), then S^T through the
+// weight-gradient kernels' propagation; the same M(r) as launch_apply up to BF16 rounding
+void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,
+                        const __nv_bfloat16* Wb, __nv_bfloat16* const* h, float* x, float* G0, float* G1, float* G2,
+                        float* out, cudaStream_t st) {
+  const __nv_bfloat16* Wtb = Wb + (size_t)NL * H * AIN;
+  launch_encode(g, r, dinv, params, h[0], x, nullptr, st);
+  launch_layers_fwd(g, Wb, h, nullptr, st);
+  const int nsc = blocks_for(g.n * 32, 256);
+  layer_bwd<false, __nv_bfloat16>(g, nullptr, h[NL], Wtb + (size_t)(NL - 1) * H * AIN, G1, G2, nullptr, nullptr, st);
+  count_launch();
+  k_gnn_msg_scatter<<<nsc, 256, 0, st>>>(g, G1, G2, G0, nullptr);
+  for (int l = NL - 2; l >= 0; l--) {
+    layer_bwd<false, float>(g, nullptr, G0, Wtb + (size_t)l * H * AIN, G1, G2, nullptr, nullptr, st);
+    count_launch();
+    k_gnn_msg_scatter<<<nsc, 256, 0, st>>>(g, G1, G2, G0, nullptr);
+  }
+  count_launch();
+  k_gnn_decode<<<nsc, 256, 0, st>>>(g.n, G0, params, r, dinv, out, nullptr);
+}
+
+int launch_count_apply() { return 2 * NL; }
+
+void launch_weight_grad(const Graph& g, const __nv_bfloat16* cot, __nv_bfloat16* const* h, const float* x,
+                        const __nv_bfloat16* Wb, float* G0, float* G1, float* G2, float* partial, float* grad,
+                        int accumulate, cudaStream_t st) {
+  const __nv_bfloat16* Wtb = Wb + (size_t)NL * H * AIN;
+  const int nbl = blocks_for(g.n, TILE), nsc = blocks_for(g.n * 32, 256);
+  for (int l = NL - 1; l >= 0; l--) {
+    // layer l maps h[l] -> h[l+1]; the cotangent of h[l+1] is cot (l = NL-1) or G0
+    if (l == NL - 1)
+      layer_bwd<true, __nv_bfloat16>(g, h[l], cot, Wtb + (size_t)l * H * AIN, G1, G2, partial, nullptr, st);
+    else
+      layer_bwd<true, float>(g, h[l], G0, Wtb + (size_t)l * H * AIN, G1, G2, partial, nullptr, st);
+    count_launch();
+    k_gnn_reduce_cols<<<(LPART + 255) / 256, 256, 0, st>>>(nbl, LPART, partial, grad + OFF_L + l * L_STRIDE,
+                                                             accumulate);
+    count_launch();
+    k_gnn_msg_scatter<<<nsc, 256, 0, st>>>(g, G1, G2, G0, nullptr);
+  }
+  const int nbe = blocks_for(g.n, 64);
+  count_launch();
+  k_gnn_encode_bwd<<<nbe, 256, 0, st>>>(g.n, G0, x, partial);
+  count_launch();
+  k_gnn_reduce_cols<<<(H * FIN + 255) / 256, 256, 0, st>>>(nbe, H * FIN, partial, grad + OFF_WE, accumulate);
+}
+
+void launch_cgrad(int64_t n3, const float* Go, const float* r, const float* dinv, const float* params, float* partials,
+                  unsigned* counter, float* grad, int accumulate, cudaStream_t st) {
+  int grid = blocks_for(n3, 256);
+  if (grid > 1024) grid = 1024;
+  count_launch();
+  k_gnn_cgrad<<<grid, 256, 0, st>>>(n3, Go, r, dinv, params, partials, counter, grad, accumulate);
+}
 
 void launch_loss(int64_t n3, const float* d, const float* q, float inv_c, float* Go, float* partials,
                  unsigned* counter, float* loss, cudaStream_t st) {
   int grid = blocks_for(n3, 256);
   if (grid > 1024) grid = 1024;
+  count_launch();
   k_gnn_loss<<<grid, 256, 0, st>>>(n3, d, q, inv_c, Go, partials, counter, loss);
 }
 
 void launch_adam(const float* grad, float* prm, float* m, float* v, float lr, int t, float clip_scale,
-                 __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st) {
+                 __nv_bfloat16* Wb, cudaStream_t st) {
   const float b1 = 0.9f, b2 = 0.999f;
   const float bc1 = 1.f - powf(b1, (float)t), bc2 = 1.f - powf(b2, (float)t);
+  count_launch();
   k_gnn_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(NPARAM, prm, grad, m, v, lr, b1, b2, 1e-8f, bc1, bc2, clip_scale);
-  k_gnn_pack<<<(NL * H * AIN + 255) / 256, 256, 0, st>>>(prm, Wb, Wtb);
+  launch_pack(prm, Wb, st);
 }
 
-void launch_pack(const float* prm, __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st) {
-  k_gnn_pack<<<(NL * H * AIN + 255) / 256, 256, 0, st>>>(prm, Wb, Wtb);
+void launch_pack(const float* prm, __nv_bfloat16* Wb, cudaStream_t st) {
+  count_launch();
+  k_gnn_pack<<<(NL * H * AIN + 255) / 256, 256, 0, st>>>(prm, Wb);
 }
 
 }  // namespace gnn
@@ -112,6 +180,7 @@ __global__ void k_sub(int64_t n, const float* __restrict__ a, const float* __res
 }
 void launch_sub(int64_t n, const float* a, const float* b, float* d, cudaStream_t st) {
   int grid = (int)std::min<int64_t>((n + 255) / 256, 2048);
+  count_launch();
   k_sub<<<grid < 1 ? 1 : grid, 256, 0, st>>>(n, a, b, d);
 }
 
@@ -253,18 +322,22 @@ static int vgrid(int64_t n) {
 }
 void launch_fcg_init(int64_t n, const float* r, const float* z, float* p, float* partials, unsigned* counter,
                      CgScalars* s, cudaStream_t st) {
+  count_launch();
   k_fcg_init<<<vgrid(n), 256, 0, st>>>(n, r, z, p, partials, counter, s);
 }
 void launch_fcg_update(int64_t n, float* x, float* r, float* rprev, const float* p, const float* q, float* partials,
                        unsigned* counter, CgScalars* s, cudaStream_t st) {
+  count_launch();
   k_fcg_update<<<vgrid(n), 256, 0, st>>>(n, x, r, rprev, p, q, partials, counter, s);
 }
 void launch_fcg_beta(int64_t n, const float* r, const float* rprev, const float* z, const float* dinv,
                      float* partials, unsigned* counter, CgScalars* s, cudaStream_t st) {
+  count_launch();
   k_fcg_beta<<<vgrid(n), 256, 0, st>>>(n, r, rprev, z, dinv, partials, counter, s);
 }
 void launch_fcg_dir(int64_t n, const float* z, const float* r, const float* dinv, float* p, const CgScalars* s,
                     cudaStream_t st) {
+  count_launch();
   k_fcg_dir<<<vgrid(n), 256, 0, st>>>(n, z, r, dinv, p, s);
 }
 

@@ -7,7 +7,7 @@ namespace sfem {
 namespace gnn {
 
 constexpr int H = 64;        // width
-constexpr int FIN = 8;       // input features
+constexpr int FIN = 3;       // input channels: D^-1/2 r at one node
 constexpr int NL = 3;        // message-passing layers
 constexpr int AIN = 2 * H;   // layer input [h ; mean h]
 constexpr int TILE = 64;     // nodes per CTA in the layer kernels
@@ -16,14 +16,12 @@ constexpr int SROW = AIN + 8;  // padded shared-memory row (bf16) for 128-wide r
 constexpr int SROW64 = H + 8;  // padded row for 64-wide rows
 
 // parameter vector layout (FP32 master copy)
-constexpr int OFF_WE = 0;                 // We [H x FIN]
-constexpr int OFF_BE = OFF_WE + H * FIN;  // be [H]
-constexpr int OFF_L = OFF_BE + H;         // per layer: Wl [H x AIN], bl [H]
-constexpr int L_STRIDE = H * AIN + H;
-constexpr int OFF_WD = OFF_L + NL * L_STRIDE;  // Wd [3 x H]
-constexpr int OFF_BD = OFF_WD + 3 * H;         // bd [3]
-constexpr int NPARAM = OFF_BD + 3;
-constexpr int LPART = H * AIN + H;  // per-CTA partial of one layer's gradient (dW, db)
+constexpr int OFF_WE = 0;                      // We [H x FIN]
+constexpr int OFF_L = OFF_WE + H * FIN;        // per layer: Wl [H x AIN]
+constexpr int L_STRIDE = H * AIN;
+constexpr int OFF_C = OFF_L + NL * L_STRIDE;   // log c (weight of the Jacobi term)
+constexpr int NPARAM = OFF_C + 1;
+constexpr int LPART = H * AIN;  // per-CTA partial of one layer's weight gradient
 
 struct Graph {
   int64_t n;              // free nodes
@@ -32,12 +30,6 @@ struct Graph {
   const float* inv_deg;   // 1 / max(deg, 1)
 };
 
-struct Scalars {  // device-resident scalars of one application
-  float s;        // rms of z
-  float inv_s;
-  float mean_ld;  // mean log d over free DOFs
-  float pad;
-};
 
 }  // namespace gnn
 }  // namespace sfem

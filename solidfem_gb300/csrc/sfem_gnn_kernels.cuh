@@ -1,13 +1,15 @@
 // Device kernels of the learned graph-network preconditioner (included by sfem_gnn.cu).
 //
-// Network (per free node i, width H = 64, 3 message-passing layers):
-//   x_i   = [z_i / s (3), log d_i - mean log d (3), touches a fixed node (1), 1]   z = D^-1 r, s = rms(z)
-//   h0_i  = relu(We x_i + be)
-//   h_i  <- h_i + relu(Wl [h_i ; mean_{j in N(i)} h_j] + bl)          l = 1..3
-//   M(r)_i = z_i + s (Wd h3_i + bd)
-// Activations are stored in BF16, GEMMs run on the tensor cores (mma.sync m16n8k16,
-// BF16 inputs, FP32 accumulation), everything else in FP32.  Backward kernels write
-// per-CTA weight-gradient partials that are summed in a fixed order (deterministic).
+// The preconditioner is symmetric positive definite by construction:
+//   x      = D^-1/2 r                                        (per free DOF)
+//   S x    : h0_i = We x_i;  h_i <- h_i + Wl [h_i ; mean_{j in N(i)} h_j]   l = 1..3
+//   M(r)   = D^-1/2 (c x + S^T S x),   c = exp(log c) > 0
+// S is a linear message-passing network of width H = 64 on the free-node mesh graph, so
+// M is one fixed SPD operator per tangent (conjugate gradients keep their guarantees);
+// S^T runs the same layers transposed (the input-gradient propagation of S).
+// Activations of S are stored in BF16, GEMMs run on the tensor cores (mma.sync m16n8k16,
+// BF16 inputs, FP32 accumulation), the transposed pass carries FP32 vectors.  Weight-gradient
+// kernels write per-CTA partials that are summed in a fixed order (deterministic).
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -38,100 +40,51 @@ __device__ __forceinline__ uint32_t f2bf(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&v);
 }
 
+// two consecutive features of row `node` (64 wide) as floats, from BF16 or FP32 storage
+__device__ __forceinline__ float2 load2(const __nv_bfloat16* a, int64_t node, int col) {
+  return bf2f(reinterpret_cast<const uint32_t*>(a)[(node * H + col) >> 1]);
+}
+__device__ __forceinline__ float2 load2(const float* a, int64_t node, int col) {
+  return *reinterpret_cast<const float2*>(&a[node * H + col]);
+}
+
 __device__ __forceinline__ float warp_sumf(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-// ---- statistics: mean log d (per Jacobi update) and rms(z) (per application) ----
-// sum over free DOFs of f(i); partials[blockIdx] then the last block finalises into *out
-template <int WHICH>  // 0: log(1/dinv), 1: (r dinv)^2
-__global__ void __launch_bounds__(256) k_gnn_stat(int64_t n3, const float* __restrict__ r,
-                                                  const float* __restrict__ dinv, float* __restrict__ partials,
-                                                  unsigned* counter, Scalars* sc, const int* done) {
-  if (done && *done) return;
-  float acc = 0.f;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
-    if (WHICH == 0) {
-      acc += -logf(dinv[i]);
-    } else {
-      const float z = r[i] * dinv[i];
-      acc += z * z;
-    }
-  }
-  __shared__ float sm[8];
-  __shared__ bool last;
-  acc = warp_sumf(acc);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float b = 0.f;
-    for (int w = 0; w < 8; w++) b += sm[w];
-    partials[blockIdx.x] = b;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    double t = 0.0;  // fixed order
-    for (unsigned b = 0; b < gridDim.x; b++) t += (double)__ldcg(&partials[b]);
-    if (WHICH == 0) {
-      sc->mean_ld = (float)(t / (double)n3);
-    } else {
-      const float s = sqrtf((float)(t / (double)n3)) + 1e-30f;
-      sc->s = s;
-      sc->inv_s = 1.f / s;
-    }
-    *counter = 0u;
-  }
-}
-
-// ---- encoder: one warp per node, lane l computes outputs 2l, 2l+1 ----
-__global__ void __launch_bounds__(256) k_gnn_encode(int64_t n, const float* __restrict__ r,
+// ---- encoder: x = v * D^-1/2, h0 = We x; one warp per node, lane l computes outputs 2l, 2l+1 ----
+__global__ void __launch_bounds__(256) k_gnn_encode(int64_t n, const float* __restrict__ v,
                                                     const float* __restrict__ dinv,
-                                                    const uint8_t* __restrict__ fixed_nb,
-                                                    const float* __restrict__ params, const Scalars* sc,
-                                                    __nv_bfloat16* __restrict__ h0, __nv_bfloat16* __restrict__ u0,
-                                                    float* __restrict__ xout, const int* done) {
+                                                    const float* __restrict__ params,
+                                                    __nv_bfloat16* __restrict__ h0, float* __restrict__ xout,
+                                                    const int* done) {
   if (done && *done) return;
   const int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (node >= n) return;
   float x[FIN];
-  const float inv_s = sc->inv_s, mld = sc->mean_ld;
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    const float di = dinv[3 * node + c];
-    x[c] = r[3 * node + c] * di * inv_s;
-    x[3 + c] = -logf(di) - mld;
-  }
-  x[6] = fixed_nb[node] ? 1.f : 0.f;
-  x[7] = 1.f;
-  if (xout && lane < FIN) xout[node * FIN + lane] = x[lane];
-  float v[2];
+  for (int c = 0; c < FIN; c++) x[c] = v[FIN * node + c] * sqrtf(dinv[FIN * node + c]);
+  if (xout && lane < FIN) xout[FIN * node + lane] = x[lane];
+  float a[2];
 #pragma unroll
   for (int k = 0; k < 2; k++) {
     const int o = 2 * lane + k;
-    float a = params[OFF_BE + o];
+    float acc = 0.f;
 #pragma unroll
-    for (int f = 0; f < FIN; f++) a += params[OFF_WE + o * FIN + f] * x[f];
-    v[k] = a;
+    for (int f = 0; f < FIN; f++) acc += params[OFF_WE + o * FIN + f] * x[f];
+    a[k] = acc;
   }
-  const uint32_t pre = f2bf(v[0], v[1]);
-  reinterpret_cast<uint32_t*>(h0)[node * (H / 2) + lane] = f2bf(fmaxf(v[0], 0.f), fmaxf(v[1], 0.f));
-  if (u0) reinterpret_cast<uint32_t*>(u0)[node * (H / 2) + lane] = pre;
+  reinterpret_cast<uint32_t*>(h0)[node * (H / 2) + lane] = f2bf(a[0], a[1]);
 }
 
-// ---- message-passing layer (forward) ----
+// ---- message-passing layer of S: h_out = h_in + Wl [h_in ; mean_j h_j] ----
 // CTA: 64 nodes, 4 warps x 16 nodes.  Shared A tile [64 x (h ; mean h)] and Wl [64 x 128].
 __global__ void __launch_bounds__(LT) k_gnn_layer_fwd(Graph g, const __nv_bfloat16* __restrict__ hin,
                                                       const __nv_bfloat16* __restrict__ W,  // [H][AIN]
-                                                      const float* __restrict__ bias,
-                                                      __nv_bfloat16* __restrict__ hout, __nv_bfloat16* __restrict__ uout,
-                                                      const int* done) {
+                                                      __nv_bfloat16* __restrict__ hout, const int* done) {
   if (done && *done) return;
   __shared__ __align__(16) __nv_bfloat16 As[TILE * SROW];
   __shared__ __align__(16) __nv_bfloat16 Ws[H * SROW];
@@ -180,7 +133,7 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_fwd(Graph g, const __nv_bfloat
       mma_bf16(acc[j], a0, a1, a2, a3, ld32(Wr), ld32(Wr + 8));
     }
   }
-  // epilogue: h_out = h_in + relu(acc + b); rows gq and gq + 8 of this warp, cols 8j + 2 t4 + {0,1}
+  // epilogue: rows gq and gq + 8 of this warp, cols 8j + 2 t4 + {0,1}
 #pragma unroll
   for (int half = 0; half < 2; half++) {
     const int row = 16 * w + gq + 8 * half;
@@ -189,101 +142,32 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_fwd(Graph g, const __nv_bfloat
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int col = 8 * j + 2 * t4;
-      const float p0 = acc[j][2 * half] + bias[col], p1 = acc[j][2 * half + 1] + bias[col + 1];
       const float2 hs = bf2f(ld32(&As[row * SROW + col]));
-      reinterpret_cast<uint32_t*>(hout)[node * (H / 2) + col / 2] = f2bf(hs.x + fmaxf(p0, 0.f), hs.y + fmaxf(p1, 0.f));
-      if (uout) reinterpret_cast<uint32_t*>(uout)[node * (H / 2) + col / 2] = f2bf(p0, p1);
+      reinterpret_cast<uint32_t*>(hout)[node * (H / 2) + col / 2] =
+          f2bf(hs.x + acc[j][2 * half], hs.y + acc[j][2 * half + 1]);
     }
   }
 }
 
-// ---- decoder: M(r) = z + s (Wd h3 + bd); one thread per node ----
-__global__ void __launch_bounds__(256) k_gnn_decode(int64_t n, const __nv_bfloat16* __restrict__ h3,
-                                                    const float* __restrict__ params, const Scalars* sc,
-                                                    const float* __restrict__ r, const float* __restrict__ dinv,
-                                                    float* __restrict__ out, const int* done) {
-  if (done && *done) return;
-  __shared__ float Wd[3 * H + 3];
-  for (int i = threadIdx.x; i < 3 * H + 3; i += blockDim.x) Wd[i] = params[OFF_WD + i];
-  __syncthreads();
-  const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (node >= n) return;
-  float y0 = Wd[3 * H], y1 = Wd[3 * H + 1], y2 = Wd[3 * H + 2];
-  const uint4* hr = reinterpret_cast<const uint4*>(h3 + node * H);
-#pragma unroll
-  for (int q = 0; q < H / 8; q++) {
-    const uint4 v = hr[q];
-    const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int t = 0; t < 4; t++) {
-      const float2 f = bf2f(vv[t]);
-      const int k = 8 * q + 2 * t;
-      y0 += Wd[k] * f.x + Wd[k + 1] * f.y;
-      y1 += Wd[H + k] * f.x + Wd[H + k + 1] * f.y;
-      y2 += Wd[2 * H + k] * f.x + Wd[2 * H + k + 1] * f.y;
-    }
-  }
-  const float s = sc->s;
-  out[3 * node] = r[3 * node] * dinv[3 * node] + s * y0;
-  out[3 * node + 1] = r[3 * node + 1] * dinv[3 * node + 1] + s * y1;
-  out[3 * node + 2] = r[3 * node + 2] * dinv[3 * node + 2] + s * y2;
-}
-
-// ============================== backward ==============================
-
-// decoder backward for one block of 256 nodes: Go = dL/dM(r) (3 per node)
-//   gy = s Go,  g_h3 = Wd^T gy,  partial dWd = sum gy (x) h3, partial dbd = sum gy
-__global__ void __launch_bounds__(256) k_gnn_decode_bwd(int64_t n, const __nv_bfloat16* __restrict__ h3,
-                                                        const float* __restrict__ params, const Scalars* sc,
-                                                        const float* __restrict__ Go, float* __restrict__ gh3,
-                                                        float* __restrict__ partial /* [grid][3H + 3] */) {
-  __shared__ float gy[256 * 3];
-  __shared__ __nv_bfloat16 hs[256 * H];
-  const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const float s = sc->s;
-  float g0 = 0.f, g1 = 0.f, g2 = 0.f;
-  if (node < n) {
-    g0 = s * Go[3 * node];
-    g1 = s * Go[3 * node + 1];
-    g2 = s * Go[3 * node + 2];
-  }
-  gy[3 * threadIdx.x] = g0;
-  gy[3 * threadIdx.x + 1] = g1;
-  gy[3 * threadIdx.x + 2] = g2;
-  for (int k = 0; k < H; k++) {
-    const float wk = params[OFF_WD + k] * g0 + params[OFF_WD + H + k] * g1 + params[OFF_WD + 2 * H + k] * g2;
-    if (node < n) gh3[node * H + k] = wk;
-    hs[threadIdx.x * H + k] = node < n ? h3[node * H + k] : __float2bfloat16(0.f);
-  }
-  __syncthreads();
-  for (int v = threadIdx.x; v < 3 * H + 3; v += blockDim.x) {
-    float a = 0.f;
-    if (v < 3 * H) {
-      const int c = v / H, k = v % H;
-      for (int i = 0; i < 256; i++) a += gy[3 * i + c] * __bfloat162float(hs[i * H + k]);
-    } else {
-      const int c = v - 3 * H;
-      for (int i = 0; i < 256; i++) a += gy[3 * i + c];
-    }
-    partial[(int64_t)blockIdx.x * (3 * H + 3) + v] = a;
-  }
-}
-
-// layer backward.  h_out = h_in + relu(u), u = Wl a + bl, a = [h_in ; mean h_in].
-//   gu = G_out * (u > 0);  g_a = gu Wl  ->  G_self = G_out + g_a[:, :H],  G_msg = g_a[:, H:] / deg
-//   partial dWl = gu^T a,  partial dbl = sum gu
-// Wt is Wl transposed ([AIN][H], bf16).  Dynamic shared memory.
+// ---- transposed layer (and, with WGRAD, its weight gradient) ----
+// For h_out = h_in + Wl a, a = [h_in ; mean h_in] and a cotangent G_out = dL/dh_out:
+//   g_a = G_out Wl  ->  G_self = G_out + g_a[:, :H],  G_msg = g_a[:, H:] / deg
+//   (dL/dh_in = G_self + mean-aggregation^T of G_msg, formed by k_gnn_msg_scatter)
+//   WGRAD: partial dWl = G_out^T a over the tile's nodes.
+// Wt is Wl transposed ([AIN][H], bf16).  Dynamic shared memory (layer_bwd_smem).
+template <bool WGRAD, typename GT>
 __global__ void __launch_bounds__(LT) k_gnn_layer_bwd(Graph g, const __nv_bfloat16* __restrict__ hin,
-                                                      const __nv_bfloat16* __restrict__ u,
-                                                      const float* __restrict__ Gout,
+                                                      const GT* __restrict__ Gout,
                                                       const __nv_bfloat16* __restrict__ Wt,
                                                       float* __restrict__ Gself, float* __restrict__ Gmsg,
-                                                      float* __restrict__ partial /* [grid][LPART] */) {
+                                                      float* __restrict__ partial /* [grid][LPART] */,
+                                                      const int* done) {
+  if (done && *done) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   __nv_bfloat16* gu = reinterpret_cast<__nv_bfloat16*>(smraw);  // [TILE][SROW64]  node-major
-  __nv_bfloat16* guT = gu + TILE * SROW64;                       // [H][SROW64]     out-major
-  __nv_bfloat16* aT = guT + H * SROW64;                          // [AIN][SROW64]   in-major
-  __nv_bfloat16* Ws = aT + AIN * SROW64;                         // [AIN][SROW64]   = Wt
+  __nv_bfloat16* Ws = gu + TILE * SROW64;                        // [AIN][SROW64]   = Wt
+  __nv_bfloat16* guT = Ws + AIN * SROW64;                        // [H][SROW64]     out-major (WGRAD)
+  __nv_bfloat16* aT = guT + H * SROW64;                          // [AIN][SROW64]   in-major  (WGRAD)
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int64_t base = (int64_t)blockIdx.x * TILE;
   for (int i = tid; i < AIN * (H / 8); i += LT) {
@@ -291,39 +175,37 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_bwd(Graph g, const __nv_bfloat
     *reinterpret_cast<uint4*>(&Ws[row * SROW64 + 8 * c8]) = reinterpret_cast<const uint4*>(Wt)[row * (H / 8) + c8];
   }
   const uint32_t* h32 = reinterpret_cast<const uint32_t*>(hin);
-  const uint32_t* u32 = reinterpret_cast<const uint32_t*>(u);
   for (int rr = 0; rr < 16; rr++) {
     const int row = 16 * w + rr;
     const int64_t node = base + row;
-    float g0 = 0.f, g1 = 0.f;
-    uint32_t self = 0, msg = 0;
-    if (node < g.n) {
-      const float2 gv = *reinterpret_cast<const float2*>(&Gout[node * H + 2 * lane]);
-      const float2 uv = bf2f(u32[node * (H / 2) + lane]);
-      g0 = uv.x > 0.f ? gv.x : 0.f;
-      g1 = uv.y > 0.f ? gv.y : 0.f;
-      self = h32[node * (H / 2) + lane];
-      float m0 = 0.f, m1 = 0.f;
-      const int e1 = g.ptr[node + 1];
-      for (int e = g.ptr[node]; e < e1; e++) {
-        const float2 v = bf2f(h32[(int64_t)g.idx[e] * (H / 2) + lane]);
-        m0 += v.x;
-        m1 += v.y;
-      }
-      const float id = g.inv_deg[node];
-      msg = f2bf(m0 * id, m1 * id);
-    }
-    const uint32_t gb = f2bf(g0, g1);
+    float2 gv = make_float2(0.f, 0.f);
+    if (node < g.n) gv = load2(Gout, node, 2 * lane);
+    const uint32_t gb = f2bf(gv.x, gv.y);
     *reinterpret_cast<uint32_t*>(&gu[row * SROW64 + 2 * lane]) = gb;
-    const __nv_bfloat162 gbb = *reinterpret_cast<const __nv_bfloat162*>(&gb);
-    guT[(2 * lane) * SROW64 + row] = gbb.x;
-    guT[(2 * lane + 1) * SROW64 + row] = gbb.y;
-    const __nv_bfloat162 sb = *reinterpret_cast<const __nv_bfloat162*>(&self);
-    const __nv_bfloat162 mb = *reinterpret_cast<const __nv_bfloat162*>(&msg);
-    aT[(2 * lane) * SROW64 + row] = sb.x;
-    aT[(2 * lane + 1) * SROW64 + row] = sb.y;
-    aT[(H + 2 * lane) * SROW64 + row] = mb.x;
-    aT[(H + 2 * lane + 1) * SROW64 + row] = mb.y;
+    if (WGRAD) {
+      uint32_t self = 0, msg = 0;
+      if (node < g.n) {
+        self = h32[node * (H / 2) + lane];
+        float m0 = 0.f, m1 = 0.f;
+        const int e1 = g.ptr[node + 1];
+        for (int e = g.ptr[node]; e < e1; e++) {
+          const float2 v = bf2f(h32[(int64_t)g.idx[e] * (H / 2) + lane]);
+          m0 += v.x;
+          m1 += v.y;
+        }
+        const float id = g.inv_deg[node];
+        msg = f2bf(m0 * id, m1 * id);
+      }
+      const __nv_bfloat162 gbb = *reinterpret_cast<const __nv_bfloat162*>(&gb);
+      guT[(2 * lane) * SROW64 + row] = gbb.x;
+      guT[(2 * lane + 1) * SROW64 + row] = gbb.y;
+      const __nv_bfloat162 sb = *reinterpret_cast<const __nv_bfloat162*>(&self);
+      const __nv_bfloat162 mb = *reinterpret_cast<const __nv_bfloat162*>(&msg);
+      aT[(2 * lane) * SROW64 + row] = sb.x;
+      aT[(2 * lane + 1) * SROW64 + row] = sb.y;
+      aT[(H + 2 * lane) * SROW64 + row] = mb.x;
+      aT[(H + 2 * lane + 1) * SROW64 + row] = mb.y;
+    }
   }
   __syncthreads();
   const int gq = lane >> 2, t4 = lane & 3;
@@ -355,7 +237,7 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_bwd(Graph g, const __nv_bfloat
         const int col = 8 * j + 2 * t4;
         const float v0 = acc[j][2 * half], v1 = acc[j][2 * half + 1];
         if (col < H) {
-          const float2 go = *reinterpret_cast<const float2*>(&Gout[node * H + col]);
+          const float2 go = load2(Gout, node, col);
           *reinterpret_cast<float2*>(&Gself[node * H + col]) = make_float2(go.x + v0, go.y + v1);
         } else {
           *reinterpret_cast<float2*>(&Gmsg[node * H + col - H]) = make_float2(v0 * id, v1 * id);
@@ -363,46 +245,44 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_bwd(Graph g, const __nv_bfloat
       }
     }
   }
+  if constexpr (WGRAD) {
   // ---- dWl partial [64 out x 128 in] = guT [64 x 64 nodes] . a [64 nodes x 128]; B[k][n] = aT[n][k] ----
-  {
-    float acc[16][4];
+  float acc[16][4];
 #pragma unroll
-    for (int j = 0; j < 16; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-    const __nv_bfloat16* Ar0 = &guT[(16 * w + gq) * SROW64];
-    const __nv_bfloat16* Ar1 = &guT[(16 * w + gq + 8) * SROW64];
+  for (int j = 0; j < 16; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  const __nv_bfloat16* Ar0 = &guT[(16 * w + gq) * SROW64];
+  const __nv_bfloat16* Ar1 = &guT[(16 * w + gq + 8) * SROW64];
 #pragma unroll
-    for (int kk = 0; kk < TILE / 16; kk++) {
-      const int k0 = 16 * kk + 2 * t4;
-      const uint32_t a0 = ld32(Ar0 + k0), a1 = ld32(Ar1 + k0), a2 = ld32(Ar0 + k0 + 8), a3 = ld32(Ar1 + k0 + 8);
+  for (int kk = 0; kk < TILE / 16; kk++) {
+    const int k0 = 16 * kk + 2 * t4;
+    const uint32_t a0 = ld32(Ar0 + k0), a1 = ld32(Ar1 + k0), a2 = ld32(Ar0 + k0 + 8), a3 = ld32(Ar1 + k0 + 8);
 #pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const __nv_bfloat16* Br = &aT[(8 * j + gq) * SROW64 + k0];
-        mma_bf16(acc[j], a0, a1, a2, a3, ld32(Br), ld32(Br + 8));
-      }
-    }
-    float* P = partial + (int64_t)blockIdx.x * LPART;
-#pragma unroll
-    for (int half = 0; half < 2; half++) {
-      const int o = 16 * w + gq + 8 * half;
-#pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int col = 8 * j + 2 * t4;
-        *reinterpret_cast<float2*>(&P[o * AIN + col]) = make_float2(acc[j][2 * half], acc[j][2 * half + 1]);
-      }
-    }
-    // bias partial: sum over the tile's nodes of gu (row of guT), fixed order
-    if (tid < H) {
-      float sb = 0.f;
-      for (int k = 0; k < TILE; k++) sb += __bfloat162float(guT[tid * SROW64 + k]);
-      P[H * AIN + tid] = sb;
+    for (int j = 0; j < 16; j++) {
+      const __nv_bfloat16* Br = &aT[(8 * j + gq) * SROW64 + k0];
+      mma_bf16(acc[j], a0, a1, a2, a3, ld32(Br), ld32(Br + 8));
     }
   }
+  float* P = partial + (int64_t)blockIdx.x * LPART;
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int o = 16 * w + gq + 8 * half;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int col = 8 * j + 2 * t4;
+      *reinterpret_cast<float2*>(&P[o * AIN + col]) = make_float2(acc[j][2 * half], acc[j][2 * half + 1]);
+    }
+  }
+  }
 }
-constexpr size_t kLayerBwdSmem = sizeof(__nv_bfloat16) * (TILE * SROW64 + H * SROW64 + 2 * AIN * SROW64);
+__host__ __device__ constexpr size_t layer_bwd_smem(bool wgrad) {
+  return sizeof(__nv_bfloat16) * (TILE * SROW64 + AIN * SROW64 + (wgrad ? H * SROW64 + AIN * SROW64 : 0));
+}
 
 // G_in[j] = G_self[j] + sum_{i in N(j)} G_msg[i]   (mean aggregation transposed; symmetric graph)
 __global__ void __launch_bounds__(256) k_gnn_msg_scatter(Graph g, const float* __restrict__ Gself,
-                                                         const float* __restrict__ Gmsg, float* __restrict__ Gin) {
+                                                         const float* __restrict__ Gmsg, float* __restrict__ Gin,
+                                                         const int* done) {
+  if (done && *done) return;
   const int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (node >= g.n) return;
@@ -416,45 +296,91 @@ __global__ void __launch_bounds__(256) k_gnn_msg_scatter(Graph g, const float* _
   *reinterpret_cast<float2*>(&Gin[node * H + 2 * lane]) = a;
 }
 
-// encoder backward for one block of 64 nodes: gu0 = G_in0 * (u0 > 0); partial dWe = gu0^T x, dbe = sum gu0
+// ---- output: M(r) = D^-1/2 (c x + We^T G0) with x = D^-1/2 r; one warp per node ----
+__global__ void __launch_bounds__(256) k_gnn_decode(int64_t n, const float* __restrict__ G0,
+                                                    const float* __restrict__ params, const float* __restrict__ r,
+                                                    const float* __restrict__ dinv, float* __restrict__ out,
+                                                    const int* done) {
+  if (done && *done) return;
+  const int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (node >= n) return;
+  const float2 gv = *reinterpret_cast<const float2*>(&G0[node * H + 2 * lane]);
+  float y[FIN];
+#pragma unroll
+  for (int c = 0; c < FIN; c++)
+    y[c] = warp_sumf(gv.x * params[OFF_WE + (2 * lane) * FIN + c] + gv.y * params[OFF_WE + (2 * lane + 1) * FIN + c]);
+  if (lane < FIN) {
+    const int64_t i = FIN * node + lane;
+    const float cc = expf(params[OFF_C]);
+    const float d = dinv[i];
+    out[i] = cc * d * r[i] + sqrtf(d) * (lane == 0 ? y[0] : lane == 1 ? y[1] : y[2]);
+  }
+}
+
+// encoder weight gradient for one block of 64 nodes: partial dWe = G0^T x
 __global__ void __launch_bounds__(256) k_gnn_encode_bwd(int64_t n, const float* __restrict__ Gin,
-                                                        const __nv_bfloat16* __restrict__ u0,
                                                         const float* __restrict__ x,
-                                                        float* __restrict__ partial /* [grid][H*FIN + H] */) {
+                                                        float* __restrict__ partial /* [grid][H*FIN] */) {
   __shared__ float gs[64 * H];
   __shared__ float xs[64 * FIN];
   const int64_t base = (int64_t)blockIdx.x * 64;
   for (int i = threadIdx.x; i < 64 * H; i += blockDim.x) {
     const int64_t node = base + i / H;
-    float v = 0.f;
-    if (node < n && __bfloat162float(u0[node * H + i % H]) > 0.f) v = Gin[node * H + i % H];
-    gs[i] = v;
+    gs[i] = node < n ? Gin[node * H + i % H] : 0.f;
   }
   for (int i = threadIdx.x; i < 64 * FIN; i += blockDim.x) {
     const int64_t node = base + i / FIN;
     xs[i] = node < n ? x[node * FIN + i % FIN] : 0.f;
   }
   __syncthreads();
-  for (int v = threadIdx.x; v < H * FIN + H; v += blockDim.x) {
+  for (int v = threadIdx.x; v < H * FIN; v += blockDim.x) {
+    const int o = v / FIN, f = v % FIN;
     float a = 0.f;
-    if (v < H * FIN) {
-      const int o = v / FIN, f = v % FIN;
-      for (int i = 0; i < 64; i++) a += gs[i * H + o] * xs[i * FIN + f];
-    } else {
-      const int o = v - H * FIN;
-      for (int i = 0; i < 64; i++) a += gs[i * H + o];
-    }
-    partial[(int64_t)blockIdx.x * (H * FIN + H) + v] = a;
+    for (int i = 0; i < 64; i++) a += gs[i * H + o] * xs[i * FIN + f];
+    partial[(int64_t)blockIdx.x * (H * FIN) + v] = a;
   }
 }
 
-// out[off + p] (+)= sum_b partial[b * P + p], b in order
+// out[p] (+)= sum_b partial[b * P + p], b in order
 __global__ void k_gnn_reduce_cols(int64_t nb, int P, const float* __restrict__ partial, float* __restrict__ out,
                                   int accumulate) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
     double a = 0.0;
     for (int64_t b = 0; b < nb; b++) a += (double)partial[b * P + p];
     out[p] = accumulate ? out[p] + (float)a : (float)a;
+  }
+}
+
+// dL/d(log c) = c * sum_i Go_i dinv_i r_i  (the Jacobi term's share of dL/dM), fixed-order finish
+__global__ void __launch_bounds__(256) k_gnn_cgrad(int64_t n3, const float* __restrict__ Go,
+                                                   const float* __restrict__ r, const float* __restrict__ dinv,
+                                                   const float* __restrict__ params, float* __restrict__ partials,
+                                                   unsigned* counter, float* __restrict__ grad, int accumulate) {
+  float acc = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x)
+    acc += Go[i] * dinv[i] * r[i];
+  __shared__ float sm[8];
+  __shared__ bool last;
+  acc = warp_sumf(acc);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.f;
+    for (int w = 0; w < 8; w++) b += sm[w];
+    partials[blockIdx.x] = b;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    double t = 0.0;
+    for (unsigned b = 0; b < gridDim.x; b++) t += (double)__ldcg(&partials[b]);
+    const float v = (float)(t * (double)expf(params[OFF_C]));
+    grad[OFF_C] = accumulate ? grad[OFF_C] + v : v;
+    *counter = 0u;
   }
 }
 
@@ -491,7 +417,7 @@ __global__ void __launch_bounds__(256) k_gnn_loss(int64_t n3, const float* __res
   }
 }
 
-// Adam on the FP32 master parameters, then the BF16 layer weights (row-major and transposed)
+// Adam on the FP32 master parameters
 __global__ void k_gnn_adam(int np, float* __restrict__ prm, const float* __restrict__ grad, float* __restrict__ m,
                            float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1, float bc2,
                            float clip_scale) {
@@ -505,14 +431,181 @@ __global__ void k_gnn_adam(int np, float* __restrict__ prm, const float* __restr
   }
 }
 
-__global__ void k_gnn_pack(const float* __restrict__ prm, __nv_bfloat16* __restrict__ Wb,
-                           __nv_bfloat16* __restrict__ Wtb) {
+// BF16 copies of the layer weights in one array of 3 NL H AIN values:
+//   Wb  [l][o][a] = Wl[o][a]                    (forward layers, [H][AIN])
+//   Wtb [l][a][o] = Wl[o][a]                    (weight-gradient kernels, [AIN][H])
+//   Wsb [l]       = [Wa^T | Wb^T], Wl = [Wa | Wb] (transposed layers run as forward layers, [H][AIN])
+__global__ void k_gnn_pack(const float* __restrict__ prm, __nv_bfloat16* __restrict__ Wb) {
   const int per = H * AIN;
+  __nv_bfloat16* Wtb = Wb + NL * per;
+  __nv_bfloat16* Wsb = Wtb + NL * per;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NL * per; i += gridDim.x * blockDim.x) {
     const int l = i / per, k = i % per, o = k / AIN, a = k % AIN;
     const __nv_bfloat16 v = __float2bfloat16(prm[OFF_L + l * L_STRIDE + k]);
     Wb[i] = v;
     Wtb[l * per + a * H + o] = v;
+    Wsb[l * per + (a < H ? a * AIN + o : (a - H) * AIN + H + o)] = v;
+  }
+}
+
+// ============================== inference ==============================
+// One kernel per layer of S and of S^T.  A transposed layer
+//   g_in = g + g Wa + A^T (g Wb)  =  g + [g ; A^T g] [Wa ; Wb]
+// has the shape of a forward layer with the transposed aggregation (A^T g)_j =
+// sum_{i in N(j)} g_i / deg_i and the weights [Wa^T | Wb^T], so S^T needs no scatter pass.
+// FIRST fuses the encoder (h0 = We x, A h0 = We (A x)), LAST the output
+// M(r) = D^-1/2 (c x + We^T g0).  Persistent CTAs of 64 nodes (4 warps x 16 rows); the
+// neighbour indices of a row are loaded by the lanes in parallel and broadcast with
+// shuffles, so up to 8 neighbour rows are in flight per warp.
+template <bool FIRST, bool TRANS, bool LAST>
+__global__ void __launch_bounds__(LT) k_gnn_layer_inf(Graph g, const __nv_bfloat16* __restrict__ hin,
+                                                      const float* __restrict__ r, const float* __restrict__ dinv,
+                                                      const float* __restrict__ params,
+                                                      const __nv_bfloat16* __restrict__ W,  // [H][AIN]
+                                                      __nv_bfloat16* __restrict__ hout, float* __restrict__ out,
+                                                      const int* done) {
+  if (done && *done) return;
+  __shared__ __align__(16) __nv_bfloat16 As[TILE * SROW];
+  __shared__ __align__(16) __nv_bfloat16 Ws[H * SROW];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int i = tid; i < H * (AIN / 8); i += LT) {
+    const int row = i / (AIN / 8), c8 = i % (AIN / 8);
+    *reinterpret_cast<uint4*>(&Ws[row * SROW + 8 * c8]) = reinterpret_cast<const uint4*>(W)[row * (AIN / 8) + c8];
+  }
+  // encoder weights of this lane's two features (FIRST) / the three output rows (LAST)
+  float we[2][FIN];
+  if (FIRST) {
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+      for (int f = 0; f < FIN; f++) we[k][f] = params[OFF_WE + (2 * lane + k) * FIN + f];
+  }
+  const uint32_t* h32 = reinterpret_cast<const uint32_t*>(hin);
+  const int64_t ntiles = (g.n + TILE - 1) / TILE;
+  const int gq = lane >> 2, t4 = lane & 3;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t base = tile * TILE;
+    for (int rr = 0; rr < 16; rr++) {
+      const int row = 16 * w + rr;
+      const int64_t node = base + row;
+      uint32_t self = 0, msg = 0;
+      if (node < g.n) {
+        const int p0 = g.ptr[node], deg = g.ptr[node + 1] - p0;
+        if (FIRST) {
+          // x = D^-1/2 r at the node and the mean over its neighbours (lanes load neighbours)
+          float xs[FIN], xm[FIN] = {0.f, 0.f, 0.f};
+#pragma unroll
+          for (int c = 0; c < FIN; c++) xs[c] = r[FIN * node + c] * sqrtf(dinv[FIN * node + c]);
+          for (int e0 = 0; e0 < deg; e0 += 32) {
+            if (e0 + lane < deg) {
+              const int64_t j = g.idx[p0 + e0 + lane];
+#pragma unroll
+              for (int c = 0; c < FIN; c++) xm[c] += r[FIN * j + c] * sqrtf(dinv[FIN * j + c]);
+            }
+          }
+          const float id = g.inv_deg[node];
+#pragma unroll
+          for (int c = 0; c < FIN; c++) xm[c] = warp_sumf(xm[c]) * id;
+          float a0 = 0.f, a1 = 0.f, m0 = 0.f, m1 = 0.f;
+#pragma unroll
+          for (int f = 0; f < FIN; f++) {
+            a0 += we[0][f] * xs[f];
+            a1 += we[1][f] * xs[f];
+            m0 += we[0][f] * xm[f];
+            m1 += we[1][f] * xm[f];
+          }
+          self = f2bf(a0, a1);
+          msg = f2bf(m0, m1);
+        } else {
+          self = h32[node * (H / 2) + lane];
+          float m0 = 0.f, m1 = 0.f;
+          for (int e0 = 0; e0 < deg; e0 += 32) {
+            const int cnt = min(32, deg - e0);
+            int jl = 0;
+            float wl = 1.f;
+            if (lane < cnt) {
+              jl = g.idx[p0 + e0 + lane];
+              if (TRANS) wl = g.inv_deg[jl];
+            }
+            for (int e = 0; e < cnt; e += 8) {
+              float2 v[8];
+#pragma unroll
+              for (int u = 0; u < 8; u++) {
+                const int j = __shfl_sync(0xffffffffu, jl, (e + u) & 31);
+                v[u] = (e + u < cnt) ? bf2f(h32[(int64_t)j * (H / 2) + lane]) : make_float2(0.f, 0.f);
+              }
+#pragma unroll
+              for (int u = 0; u < 8; u++) {
+                const float wu = TRANS ? __shfl_sync(0xffffffffu, wl, (e + u) & 31) : 1.f;
+                m0 += wu * v[u].x;
+                m1 += wu * v[u].y;
+              }
+            }
+          }
+          const float id = TRANS ? 1.f : g.inv_deg[node];
+          msg = f2bf(m0 * id, m1 * id);
+        }
+      }
+      *reinterpret_cast<uint32_t*>(&As[row * SROW + 2 * lane]) = self;
+      *reinterpret_cast<uint32_t*>(&As[row * SROW + H + 2 * lane]) = msg;
+    }
+    __syncthreads();
+    float acc[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const __nv_bfloat16* Ar0 = &As[(16 * w + gq) * SROW];
+    const __nv_bfloat16* Ar1 = &As[(16 * w + gq + 8) * SROW];
+#pragma unroll
+    for (int kk = 0; kk < AIN / 16; kk++) {
+      const int k0 = 16 * kk + 2 * t4;
+      const uint32_t a0 = ld32(Ar0 + k0), a1 = ld32(Ar1 + k0), a2 = ld32(Ar0 + k0 + 8), a3 = ld32(Ar1 + k0 + 8);
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const __nv_bfloat16* Wr = &Ws[(8 * j + gq) * SROW + k0];
+        mma_bf16(acc[j], a0, a1, a2, a3, ld32(Wr), ld32(Wr + 8));
+      }
+    }
+    // epilogue: rows gq and gq + 8 of this warp, cols 8j + 2 t4 + {0,1}
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+      const int row = 16 * w + gq + 8 * half;
+      const int64_t node = base + row;
+      if (!LAST) {
+        if (node < g.n) {
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            const int col = 8 * j + 2 * t4;
+            const float2 hs = bf2f(ld32(&As[row * SROW + col]));
+            reinterpret_cast<uint32_t*>(hout)[node * (H / 2) + col / 2] =
+                f2bf(hs.x + acc[j][2 * half], hs.y + acc[j][2 * half + 1]);
+          }
+        }
+      } else {
+        // y = We^T g0 over this thread's 16 columns, then across the 4 lanes of the quad
+        float y[FIN] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int col = 8 * j + 2 * t4;
+          const float2 hs = bf2f(ld32(&As[row * SROW + col]));
+          const float g0 = hs.x + acc[j][2 * half], g1 = hs.y + acc[j][2 * half + 1];
+#pragma unroll
+          for (int c = 0; c < FIN; c++)
+            y[c] += g0 * params[OFF_WE + col * FIN + c] + g1 * params[OFF_WE + (col + 1) * FIN + c];
+        }
+#pragma unroll
+        for (int c = 0; c < FIN; c++) {
+          y[c] += __shfl_xor_sync(0xffffffffu, y[c], 1);
+          y[c] += __shfl_xor_sync(0xffffffffu, y[c], 2);
+        }
+        if (t4 < FIN && node < g.n) {
+          const int64_t i = FIN * node + t4;
+          const float cc = expf(params[OFF_C]);
+          const float d = dinv[i];
+          out[i] = cc * d * r[i] + sqrtf(d) * (t4 == 0 ? y[0] : t4 == 1 ? y[1] : y[2]);
+        }
+      }
+    }
+    __syncthreads();  // As is refilled by the next tile
   }
 }
 

@@ -1599,17 +1599,15 @@ struct GnnState {
   int64_t n = 0;  // free nodes
   int32_t *ptr = nullptr, *idx = nullptr;
   float* inv_deg = nullptr;
-  uint8_t* fixed_nb = nullptr;
   float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
-  __nv_bfloat16 *Wb = nullptr, *Wtb = nullptr;
-  __nv_bfloat16* h[gnn::NL + 1] = {};
-  __nv_bfloat16* u[gnn::NL + 1] = {};
-  float* x = nullptr;
-  float *G0 = nullptr, *G1 = nullptr, *G2 = nullptr;
+  __nv_bfloat16* Wb = nullptr;          // 3 packed BF16 weight sets (k_gnn_pack)
+  __nv_bfloat16* h[gnn::NL + 1] = {};   // activations of S at x = D^-1/2 r
+  __nv_bfloat16* hg[gnn::NL + 1] = {};  // activations of S at D^-1/2 dL/dM (training)
+  float *x = nullptr, *xg = nullptr;    // the two inputs (training)
+  float *G0 = nullptr, *G1 = nullptr, *G2 = nullptr;  // transposed-pass vectors (n x H, training)
   float* wpart = nullptr;
   float* spart = nullptr;
   unsigned* scount = nullptr;
-  gnn::Scalars* sc = nullptr;
   float* losses = nullptr;  // device, one per training step
   int64_t losses_cap = 0;
   float *z = nullptr, *rprev = nullptr;  // FCG vectors (3N)
@@ -1618,20 +1616,20 @@ struct GnnState {
   std::vector<float> rinv;               // 1 / (r . r) per sample
   float* tmp = nullptr;                  // 3N scratch
   int loss_mode = 0;                     // 0: energy norm of the error, 1: residual norm
+  int batch = 1;                         // pairs per Adam step
   int adam_t = 0;
   bool train_bufs = false;
   gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg}; }
 };
 
 void gnn_free(GnnState* g) {
-  void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->fixed_nb, g->params, g->grad, g->m, g->v, g->Wb, g->Wtb,
-                  g->x, g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->sc, g->losses, g->z, g->rprev,
-                  g->tmp};
+  void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->params, g->grad, g->m, g->v, g->Wb, g->x, g->xg,
+                  g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->losses, g->z, g->rprev, g->tmp};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int l = 0; l <= gnn::NL; l++) {
     if (g->h[l]) cudaFree(g->h[l]);
-    if (g->u[l]) cudaFree(g->u[l]);
+    if (g->hg[l]) cudaFree(g->hg[l]);
   }
   for (float* b : g->R) cudaFree(b);
   for (float* b : g->Ee) cudaFree(b);
@@ -1648,45 +1646,50 @@ int gnn_train_buffers(sfem_handle* h) {
   GnnState* g = h->gnn;
   if (g->train_bufs) return 0;
   const size_t nh = (size_t)g->n * gnn::H;
-  for (int l = 0; l <= gnn::NL; l++) TRY(dalloc(&g->u[l], nh));
-  TRY(dalloc(&g->x, (size_t)g->n * gnn::FIN));
+  for (int l = 0; l <= gnn::NL; l++) TRY(dalloc(&g->hg[l], nh));
   TRY(dalloc(&g->G0, nh));
   TRY(dalloc(&g->G1, nh));
   TRY(dalloc(&g->G2, nh));
-  const size_t nb = (size_t)((g->n + gnn::TILE - 1) / gnn::TILE);
-  TRY(dalloc(&g->wpart, std::max(nb * gnn::LPART, (size_t)((g->n + 255) / 256) * (3 * gnn::H + 3))));
+  TRY(dalloc(&g->x, (size_t)g->n * gnn::FIN));
+  TRY(dalloc(&g->xg, (size_t)g->n * gnn::FIN));
+  const size_t nbl = (size_t)((g->n + gnn::TILE - 1) / gnn::TILE), nbe = (size_t)((g->n + 63) / 64);
+  TRY(dalloc(&g->wpart, std::max(nbl * gnn::LPART, nbe * gnn::H * gnn::FIN)));
   g->train_bufs = true;
   return 0;
 }
 
-// current Jacobi diagonal (FP32) into k32.dinv and its log-mean statistic
+// current Jacobi diagonal (FP32) into k32.dinv
 int gnn_refresh_diag(sfem_handle* h) {
-  GnnState* g = h->gnn;
   TRY(jacobi<float>(h, h->k32.dinv, nullptr));
-  const size_t o = 3 * (size_t)h->nbc;
-  gnn::launch_stat(0, 3 * g->n, nullptr, h->k32.dinv + o, g->spart, g->scount, g->sc, nullptr, h->stream);
   CU(cudaGetLastError());
   return 0;
 }
 
-// out = M(r) over the free block (r, out point at free-block starts); done may be null
+// out = M(r) over the free block (r, out point at free-block starts); done may be null.
+// With train, x = D^-1/2 r is kept for the weight gradient.
 void gnn_apply_dev(sfem_handle* h, const float* r, float* out, const int* done, bool train) {
   GnnState* g = h->gnn;
   const size_t o = 3 * (size_t)h->nbc;
   const float* dinv = h->k32.dinv + o;
-  gnn::launch_stat(1, 3 * g->n, r, dinv, g->spart, g->scount, g->sc, done, h->stream);
-  gnn::launch_forward(g->graph(), r, dinv, g->fixed_nb, g->params, g->Wb, g->sc, g->h, train ? g->u : nullptr,
-                      train ? g->x : nullptr, out, done, h->stream);
+  if (train)
+    gnn::launch_apply_train(g->graph(), r, dinv, g->params, g->Wb, g->h, g->x, g->G0, g->G1, g->G2, out, h->stream);
+  else
+    gnn::launch_apply(g->graph(), r, dinv, g->params, g->Wb, g->h, out, done, h->stream);
 }
 
 // loss of one sample and the parameter gradient into g->grad; loss into *loss_dev.
 //   energy mode:   d = M(r) - e,      L = d.Kd / (e.r),   dL/dM = 2 K d / (e.r)
 //   residual mode: d = K M(r) - r,    L = d.d / (r.r),    dL/dM = 2 K d / (r.r)
-int gnn_loss_grad_dev(sfem_handle* h, const float* r, const float* e, float cinv, float rinv, float* loss_dev) {
+// With gy = D^-1/2 dL/dM and x = D^-1/2 r, the S-part of dL is d<S gy, S x>: the weight
+// gradient of <S x, S gy> at input x plus that at input gy (S is linear), and
+// dL/d(log c) = c gy.x.
+int gnn_loss_grad_dev(sfem_handle* h, const float* r, const float* e, float cinv, float rinv, float* loss_dev,
+                      int accumulate = 0) {
   GnnState* g = h->gnn;
   TRY(gnn_train_buffers(h));
   KrylovWs<float>& w = h->k32;
   const size_t o = 3 * (size_t)h->nbc, n3 = 3 * (size_t)g->n;
+  const float* dinv = w.dinv + o;
   float* out = g->z + o;
   gnn_apply_dev(h, r, out, nullptr, true);
   float* Go = g->rprev + o;
@@ -1703,8 +1706,14 @@ int gnn_loss_grad_dev(sfem_handle* h, const float* r, const float* e, float cinv
     gnn::launch_loss((int64_t)n3, w.b + o, w.q + o, rinv, Go, g->spart, g->scount, g->spart + 4001, h->stream);
     gnn::launch_loss((int64_t)n3, w.b + o, w.b + o, rinv, g->tmp + o, g->spart, g->scount, loss_dev, h->stream);
   }
-  gnn::launch_backward(g->graph(), Go, g->params, g->Wtb, g->sc, g->h, g->u, g->x, g->G0, g->G1, g->G2, g->wpart,
-                       g->grad, h->stream);
+  const gnn::Graph gr = g->graph();
+  gnn::launch_encode(gr, Go, dinv, g->params, g->hg[0], g->xg, nullptr, h->stream);
+  gnn::launch_layers_fwd(gr, g->Wb, g->hg, nullptr, h->stream);
+  gnn::launch_weight_grad(gr, g->hg[gnn::NL], g->h, g->x, g->Wb, g->G0, g->G1, g->G2, g->wpart, g->grad,
+                          accumulate, h->stream);
+  gnn::launch_weight_grad(gr, g->h[gnn::NL], g->hg, g->xg, g->Wb, g->G0, g->G1, g->G2, g->wpart, g->grad, 1,
+                          h->stream);
+  gnn::launch_cgrad((int64_t)n3, Go, r, dinv, g->params, g->spart, g->scount, g->grad, accumulate, h->stream);
   CU(cudaGetLastError());
   return 0;
 }
@@ -1820,23 +1829,18 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   h->gnn = g;
   const int64_t nbc = h->nbc, n = h->nf;
   g->n = n;
-  // free-node graph from the element edges, fixed-neighbour flags
+  // free-node graph from the element edges
   std::vector<int4> tt((size_t)h->E);
   CU(cudaMemcpyAsync(tt.data(), h->tets, tt.size() * sizeof(int4), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
   std::vector<uint64_t> edges;
   edges.reserve(tt.size() * 12);
-  std::vector<uint8_t> fnb((size_t)n, 0);
   for (const int4& t4 : tt) {
     const int32_t v[4] = {t4.x, t4.y, t4.z, t4.w};
     for (int a = 0; a < 4; a++)
-      for (int b = 0; b < 4; b++) {
-        if (a == b) continue;
-        if (v[a] >= nbc && v[b] >= nbc)
+      for (int b = 0; b < 4; b++)
+        if (a != b && v[a] >= nbc && v[b] >= nbc)
           edges.push_back(((uint64_t)(v[a] - nbc) << 32) | (uint32_t)(v[b] - nbc));
-        else if (v[a] >= nbc && v[b] < nbc)
-          fnb[v[a] - nbc] = 1;
-      }
   }
   std::sort(edges.begin(), edges.end());
   edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
@@ -1848,29 +1852,26 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   for (int64_t i = 0; i < n; i++) ptr[i + 1] += ptr[i];
   std::vector<float> invdeg((size_t)n);
   for (int64_t i = 0; i < n; i++) invdeg[i] = 1.f / (float)std::max(1, ptr[i + 1] - ptr[i]);
-  // He-initialised weights, zero biases, zero decoder (starts as Jacobi)
+  // seeded normal weights; log c = 0
   std::vector<float> prm(gnn::NPARAM, 0.f);
   std::mt19937_64 rng(seed);
   std::normal_distribution<float> nd(0.f, 1.f);
-  for (int i = 0; i < gnn::H * gnn::FIN; i++) prm[gnn::OFF_WE + i] = nd(rng) * std::sqrt(2.f / gnn::FIN);
+  for (int i = 0; i < gnn::H * gnn::FIN; i++) prm[gnn::OFF_WE + i] = nd(rng) * 0.3f;
   for (int l = 0; l < gnn::NL; l++)
     for (int i = 0; i < gnn::H * gnn::AIN; i++)
-      prm[gnn::OFF_L + l * gnn::L_STRIDE + i] = nd(rng) * std::sqrt(2.f / gnn::AIN) * 0.5f;
+      prm[gnn::OFF_L + l * gnn::L_STRIDE + i] = nd(rng) * (0.5f / std::sqrt((float)gnn::AIN));
   const size_t nh = (size_t)n * gnn::H;
   TRY(dalloc(&g->ptr, ptr.size()));
   TRY(dalloc(&g->idx, std::max<size_t>(idx.size(), 1)));
   TRY(dalloc(&g->inv_deg, (size_t)n));
-  TRY(dalloc(&g->fixed_nb, (size_t)n));
   TRY(dalloc(&g->params, gnn::NPARAM));
   TRY(dalloc(&g->grad, gnn::NPARAM));
   TRY(dalloc(&g->m, gnn::NPARAM));
   TRY(dalloc(&g->v, gnn::NPARAM));
-  TRY(dalloc(&g->Wb, (size_t)gnn::NL * gnn::H * gnn::AIN));
-  TRY(dalloc(&g->Wtb, (size_t)gnn::NL * gnn::H * gnn::AIN));
+  TRY(dalloc(&g->Wb, (size_t)3 * gnn::NL * gnn::H * gnn::AIN));
   for (int l = 0; l <= gnn::NL; l++) TRY(dalloc(&g->h[l], nh));
   TRY(dalloc(&g->spart, 4096));
   TRY(dalloc(&g->scount, 1));
-  TRY(dalloc(&g->sc, 1));
   TRY(dalloc(&g->z, 3 * (size_t)h->N));
   TRY(dalloc(&g->rprev, 3 * (size_t)h->N));
   TRY(dalloc(&g->tmp, 3 * (size_t)h->N));
@@ -1878,14 +1879,13 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   if (!idx.empty())
     CU(cudaMemcpyAsync(g->idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemcpyAsync(g->inv_deg, invdeg.data(), invdeg.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemcpyAsync(g->fixed_nb, fnb.data(), fnb.size(), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemcpyAsync(g->params, prm.data(), prm.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(g->m, 0, gnn::NPARAM * sizeof(float), h->stream));
   CU(cudaMemsetAsync(g->v, 0, gnn::NPARAM * sizeof(float), h->stream));
   CU(cudaMemsetAsync(g->scount, 0, sizeof(unsigned), h->stream));
   CU(cudaMemsetAsync(g->z, 0, 3 * (size_t)h->N * sizeof(float), h->stream));
   CU(cudaMemsetAsync(g->rprev, 0, 3 * (size_t)h->N * sizeof(float), h->stream));
-  gnn::launch_pack(g->params, g->Wb, g->Wtb, h->stream);
+  gnn::launch_pack(g->params, g->Wb, h->stream);
   return sync(h);
 }
 
@@ -1894,6 +1894,14 @@ int sfem_gnn_set_loss(sfem_handle* h, int32_t mode) {
   TRY(gnn_need(h));
   if (mode != 0 && mode != 1) return fail(SFEM_ERR_INVALID, "loss mode is 0 (energy) or 1 (residual)");
   h->gnn->loss_mode = mode;
+  return SFEM_OK;
+}
+
+int sfem_gnn_set_batch(sfem_handle* h, int32_t batch) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  if (batch < 1 || batch > 4096) return fail(SFEM_ERR_INVALID, "batch must be in [1, 4096]");
+  h->gnn->batch = batch;
   return SFEM_OK;
 }
 
@@ -1908,7 +1916,7 @@ int sfem_gnn_set_params(sfem_handle* h, const float* params) {
   TRY(check_handle(h));
   TRY(gnn_need(h));
   CU(cudaMemcpyAsync(h->gnn->params, params, gnn::NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-  gnn::launch_pack(h->gnn->params, h->gnn->Wb, h->gnn->Wtb, h->stream);
+  gnn::launch_pack(h->gnn->params, h->gnn->Wb, h->stream);
   h->gnn->adam_t = 0;
   CU(cudaMemsetAsync(h->gnn->m, 0, gnn::NPARAM * sizeof(float), h->stream));
   CU(cudaMemsetAsync(h->gnn->v, 0, gnn::NPARAM * sizeof(float), h->stream));
@@ -2090,10 +2098,14 @@ int sfem_gnn_train(sfem_handle* h, int32_t steps, float lr, uint64_t seed, float
   TRY(gnn_refresh_diag(h));
   std::mt19937_64 rng(seed);
   for (int t = 0; t < steps; t++) {
-    const size_t j = (size_t)(rng() % g->R.size());
-    TRY(gnn_loss_grad_dev(h, g->R[j], g->Ee[j], g->cinv[j], g->rinv[j], g->losses + t));
+    // gradient summed over `batch` seeded random pairs; losses[t] is the first pair's loss
+    for (int b = 0; b < g->batch; b++) {
+      const size_t j = (size_t)(rng() % g->R.size());
+      TRY(gnn_loss_grad_dev(h, g->R[j], g->Ee[j], g->cinv[j], g->rinv[j], b == 0 ? g->losses + t : g->spart + 4003,
+                            b > 0));
+    }
     g->adam_t++;
-    gnn::launch_adam(g->grad, g->params, g->m, g->v, lr, g->adam_t, 1.f, g->Wb, g->Wtb, h->stream);
+    gnn::launch_adam(g->grad, g->params, g->m, g->v, lr, g->adam_t, 1.f / (float)g->batch, g->Wb, h->stream);
     if ((t & 63) == 63) TRY(sync(h));
   }
   if (losses) CU(cudaMemcpyAsync(losses, g->losses, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost, h->stream));

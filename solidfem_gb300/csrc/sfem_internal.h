@@ -100,6 +100,7 @@ struct Reduce {
 };
 
 unsigned long long launch_count();
+void count_launch();  // every kernel launcher of the library calls this once per launch
 // records the thread's last error message (sfem_last_error) and returns code
 int set_error(int code, const char* msg);
 
@@ -197,21 +198,32 @@ void launch_scale_copy(int64_t n, double a, const double* x, double* y, cudaStre
 #include "sfem_gnn.h"
 namespace sfem {
 namespace gnn {
-void launch_stat(int which, int64_t n3, const float* r, const float* dinv, float* partials, unsigned* counter,
-                 Scalars* sc, const int* done, cudaStream_t st);
-void launch_forward(const Graph& g, const float* r, const float* dinv, const uint8_t* fixed_nb, const float* params,
-                    const __nv_bfloat16* Wb, Scalars* sc, __nv_bfloat16* const* h, __nv_bfloat16* const* u, float* x,
-                    float* out, const int* done, cudaStream_t st);
-int launch_count_forward();
-void launch_backward(const Graph& g, const float* Go, const float* params, const __nv_bfloat16* Wtb, const Scalars* sc,
-                     __nv_bfloat16* const* h, __nv_bfloat16* const* u, const float* x, float* G0, float* G1,
-                     float* G2, float* partial, float* grad, cudaStream_t st);
-int launch_count_backward();
+// M(r) over the free block: NL layers of S then NL transposed layers (encoder and output
+// fused into the first and last); Wb holds the 3 packed BF16 weight sets (k_gnn_pack)
+void launch_apply(const Graph& g, const float* r, const float* dinv, const float* params, const __nv_bfloat16* Wb,
+                  __nv_bfloat16* const* h, float* out, const int* done, cudaStream_t st);
+// the same M(r) keeping the activations h0..h3 of S and x = D^-1/2 r (training)
+void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,
+                        const __nv_bfloat16* Wb, __nv_bfloat16* const* h, float* x, float* G0, float* G1, float* G2,
+                        float* out, cudaStream_t st);
+int launch_count_apply();
+// h0 = We (v D^-1/2) (x = v D^-1/2 kept in xout when given), then the NL layers of S
+void launch_encode(const Graph& g, const float* v, const float* dinv, const float* params, __nv_bfloat16* h0,
+                   float* xout, const int* done, cudaStream_t st);
+void launch_layers_fwd(const Graph& g, const __nv_bfloat16* Wb, __nv_bfloat16* const* h, const int* done,
+                       cudaStream_t st);
+// weight gradient of <cot, S x> for the activations h of S at input x, into (or added to) grad
+void launch_weight_grad(const Graph& g, const __nv_bfloat16* cot, __nv_bfloat16* const* h, const float* x,
+                        const __nv_bfloat16* Wb, float* G0, float* G1, float* G2, float* partial, float* grad,
+                        int accumulate, cudaStream_t st);
+// grad[OFF_C] (+)= dL/d(log c)
+void launch_cgrad(int64_t n3, const float* Go, const float* r, const float* dinv, const float* params, float* partials,
+                  unsigned* counter, float* grad, int accumulate, cudaStream_t st);
 void launch_loss(int64_t n3, const float* d, const float* q, float inv_c, float* Go, float* partials,
                  unsigned* counter, float* loss, cudaStream_t st);
 void launch_adam(const float* grad, float* prm, float* m, float* v, float lr, int t, float clip_scale,
-                 __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st);
-void launch_pack(const float* prm, __nv_bfloat16* Wb, __nv_bfloat16* Wtb, cudaStream_t st);
+                 __nv_bfloat16* Wb, cudaStream_t st);
+void launch_pack(const float* prm, __nv_bfloat16* Wb, cudaStream_t st);
 void launch_sub(int64_t n, const float* a, const float* b, float* d, cudaStream_t st);
 // flexible CG (Polak-Ribiere) vector kernels; partials need >= 2048 floats
 void launch_fcg_init(int64_t n, const float* r, const float* z, float* p, float* partials, unsigned* counter,

@@ -27,7 +27,7 @@ namespace sfem {
 // Number of kernels this library has launched (all wrappers below count theirs).
 static unsigned long long g_launches = 0;
 unsigned long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
-static inline void count_launch() { __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED); }
+void count_launch() { __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED); }
 
 // ---------------------------------------------------------------------------
 // 3x3 algebra (row-major a[3*i+j])

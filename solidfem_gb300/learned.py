@@ -1,6 +1,9 @@
 """Learned graph-network preconditioner (extension; the reference has no learned part).
 
-The network, its training and its inference all run in the CUDA library
+M(r) = D^-1/2 (c x + S^T S x), x = D^-1/2 r, with S a linear 3-layer message-passing
+network of width 64 on the free-node mesh graph: a symmetric positive definite operator
+for every choice of weights, so conjugate gradients stay convergent whatever the training
+reached.  The network, its training and its inference all run in the CUDA library
 (include/sfem.h, sfem_gnn_*); this module is the host-side handle: collect
 residual/correction pairs from plain Jacobi-PCG solves, train with Adam, save and
 load the weights (raw float32 blob + JSON metadata), and use it as the
@@ -29,7 +32,7 @@ class LearnedPreconditioner:
     """Attached to one FP32 ``FemPhysicsMatrixFree``; the weights can be moved between
     handles (the network is independent of the mesh size)."""
 
-    WIDTH, LAYERS, FEATURES = 64, 3, 8
+    WIDTH, LAYERS, FEATURES = 64, 3, 3
 
     def __init__(self, phys, seed: int = 0):
         if phys.precision != "fp32":
@@ -61,6 +64,10 @@ class LearnedPreconditioner:
 
     def load(self, path: str) -> None:
         self.set_params(np.fromfile(path, dtype=np.float32))
+
+    def set_batch(self, batch: int) -> None:
+        """Pairs per Adam step (the gradient is averaged over them)."""
+        nat.check(self._lib.sfem_gnn_set_batch(self.phys.handle, int(batch)))
 
     def set_loss(self, mode: str) -> None:
         """'energy': ||M(r) - e||_K^2 / (e.r);  'residual': ||K M(r) - r||^2 / (r.r)."""

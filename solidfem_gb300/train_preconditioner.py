@@ -9,7 +9,7 @@ load the plain Jacobi-PCG solve of K x = r(x_0) on the GPU labels its own iterat
 (r_j, x_final - x_j) every `every` iterations.  The network is local (3 message-
 passing hops), so weights trained on small slabs apply to the 256x64x64 mesh.
 Training runs on the GPU (the library's BF16 tensor-core forward/backward kernels,
-Adam on FP32 master weights).
+Adam on FP32 master weights, `batch` pairs per step).
 """
 from __future__ import annotations
 
@@ -28,14 +28,15 @@ def slab_mesh(nx, ny, nz, jitter=0.2, seed=0):
     return box_lattice(nx, ny, nz, extent=(nx / 64.0, ny / 64.0, nz / 64.0), jitter=jitter, seed=seed)
 
 
-def train(dims=(64, 16, 16), seeds=256, every=25, max_snaps=12, steps=3000, lr=1e-3, init_seed=0, verbose=True,
-          loss="residual"):
+def train(dims=(64, 16, 16), seeds=64, every=25, max_snaps=40, steps=2000, lr=1e-3, init_seed=0, verbose=True,
+          loss="energy", batch=8):
     m = slab_mesh(*dims)
     fixed = m.face_nodes(2, 0)
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
                              material=3, precision="fp32")
     net = LearnedPreconditioner(p, seed=init_seed)
     net.set_loss(loss)
+    net.set_batch(batch)
     t0 = time.time()
     for s in range(seeds):
         p.set_nodal_loads(random_top_traction(m, seed=s))
@@ -44,7 +45,7 @@ def train(dims=(64, 16, 16), seeds=256, every=25, max_snaps=12, steps=3000, lr=1
     t0 = time.time()
     losses = net.train(steps=steps, lr=lr, seed=init_seed)
     t_train = time.time() - t0
-    info = {"dims": list(dims), "load_seeds": [0, seeds - 1], "pairs": net.dataset_size(), "every": every, "loss": loss,
+    info = {"dims": list(dims), "load_seeds": [0, seeds - 1], "pairs": net.dataset_size(), "every": every, "loss": loss, "batch": batch,
             "steps": steps, "lr": lr, "loss_first50": float(np.mean(losses[:50])),
             "loss_last50": float(np.mean(losses[-50:])), "collect_s": t_collect, "train_s": t_train,
             "material": "neo-Hookean E=1e5 nu=0.49, h=1/64, jitter 0.2h, bottom clamped, random top traction"}
@@ -57,15 +58,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--dims", default="64,16,16")
-    ap.add_argument("--seeds", type=int, default=256)
+    ap.add_argument("--seeds", type=int, default=64)
     ap.add_argument("--every", type=int, default=25)
-    ap.add_argument("--max-snaps", type=int, default=12)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--max-snaps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--loss", default="residual", choices=["energy", "residual"])
+    ap.add_argument("--loss", default="energy", choices=["energy", "residual"])
     a = ap.parse_args()
     dims = tuple(int(v) for v in a.dims.split(","))
-    net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr, loss=a.loss)
+    net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr, loss=a.loss, batch=a.batch)
     net.save(a.out, meta=info)
     np.save(a.out.rsplit(".", 1)[0] + "_losses.npy", losses)
 

@@ -27,9 +27,9 @@ def gpu_and_oracle(m, fixed, seed=0):
                              material=3, precision="fp32")
     net = LearnedPreconditioner(p, seed=seed)
     o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.49, 1070.0, (0, 0, 0), 3)
-    Am, fnb = go.free_graph(o.tets(), o.n_bcs, o.n_nodes)
+    Am = go.free_graph(o.tets(), o.n_bcs, o.n_nodes)
     dinv = 1.0 / o.jacobi_diagonal()
-    return p, net, o, Am, fnb, dinv
+    return p, net, o, Am, dinv
 
 
 def rel(a, b):
@@ -38,38 +38,42 @@ def rel(a, b):
 
 def test_forward_matches_fp64_oracle():
     m, fixed, _ = slab(24, 8, 8)
-    p, net, o, Am, fnb, dinv = gpu_and_oracle(m, fixed, seed=3)
+    p, net, o, Am, dinv = gpu_and_oracle(m, fixed, seed=3)
     rng = np.random.default_rng(1)
-    prm = net.get_params().astype(np.float64)
-    prm[go.OFF_WD:] = rng.normal(size=go.NPARAM - go.OFF_WD) * 0.05  # non-zero decoder
-    net.set_params(prm)
     r = rng.normal(size=3 * o.n_free)
     out_g = net.apply(r)
-    out_o, _ = go.forward(net.get_params(), Am, fnb, r, dinv)
+    out_o = go.forward(net.get_params(), Am, r, dinv)
     err = rel(out_g, out_o)
-    print(f"M(r) GPU (BF16 activations) vs FP64 oracle: rel err {err:.2e}")
-    assert err < 3e-2
+    # the S^T S part alone (c x removed), where the BF16 rounding lives
+    prm = net.get_params().astype(np.float64)
+    c = np.exp(prm[go.OFF_C])
+    ss_g, ss_o = out_g - c * dinv * r, out_o - c * dinv * r
+    err_ss = rel(ss_g, ss_o)
+    print(f"M(r) GPU (BF16 activations) vs FP64 oracle: rel err {err:.2e}; S^T S part {err_ss:.2e}")
+    assert err < 2e-2 and err_ss < 3e-2
+    # linear and symmetric on the device too (up to BF16 rounding of the activations)
+    u, v = rng.normal(size=(2, 3 * o.n_free))
+    Mu, Mv = net.apply(u), net.apply(v)
+    assert abs(u @ Mv - v @ Mu) <= 2e-2 * abs(u @ Mv)
+    assert rel(net.apply(2.0 * u + v), 2.0 * Mu + Mv) < 2e-2
 
 
 @pytest.mark.parametrize("mode", ["energy", "residual"])
 def test_gradients_match_fp64_oracle(mode):
     m, fixed, _ = slab(24, 8, 8)
-    p, net, o, Am, fnb, dinv = gpu_and_oracle(m, fixed, seed=4)
+    p, net, o, Am, dinv = gpu_and_oracle(m, fixed, seed=4)
     rng = np.random.default_rng(2)
-    prm = net.get_params().astype(np.float64)
-    prm[go.OFF_WD:] = rng.normal(size=go.NPARAM - go.OFF_WD) * 0.05
-    net.set_params(prm)
     r = rng.normal(size=3 * o.n_free)
     e, _, _ = o.pcg(r, diag=1.0 / dinv, tol=1e-10, max_iters=20000)
     net.set_loss(mode)
     Lg, gg = net.loss_grad(r, e)
-    Lo, go_ = go.loss_grad(net.get_params(), Am, fnb, r, dinv, e, o.matvec, mode=mode)
+    Lo, go_ = go.loss_grad(net.get_params(), Am, r, dinv, e, o.matvec, mode=mode)
     cos = float(gg @ go_) / (np.linalg.norm(gg) * np.linalg.norm(go_))
     print(f"loss GPU {Lg:.6f} oracle {Lo:.6f}; grad rel err {rel(gg, go_):.2e}, cosine {cos:.5f}")
     assert abs(Lg - Lo) <= 3e-2 * abs(Lo)
     assert rel(gg, go_) < 8e-2 and cos > 0.995
-    for name, a, b in [("We", go.OFF_WE, go.OFF_BE), ("L1", go.OFF_L, go.OFF_L + go.L_STRIDE),
-                       ("L3", go.OFF_L + 2 * go.L_STRIDE, go.OFF_WD), ("Wd", go.OFF_WD, go.NPARAM)]:
+    for name, a, b in [("We", go.OFF_WE, go.OFF_L), ("L1", go.OFF_L, go.OFF_L + go.L_STRIDE),
+                       ("L3", go.OFF_L + 2 * go.L_STRIDE, go.OFF_C), ("log c", go.OFF_C, go.NPARAM)]:
         assert rel(gg[a:b], go_[a:b]) < 1e-1, name
 
 
@@ -90,7 +94,8 @@ def test_trained_network_gain_over_jacobi():
         p.set_nodal_loads(random_top_traction(m, seed=s))
         net.collect(None, every=25, max_snaps=40, rel_tol=1e-6)
     n = net.dataset_size()
-    losses = net.train(steps=1500, lr=1e-3, seed=0)
+    net.set_batch(8)
+    losses = net.train(steps=600, lr=1e-3, seed=0)
     first, last = float(np.mean(losses[:50])), float(np.mean(losses[-50:]))
     print(f"pairs {n}; energy-norm loss {first:.4f} -> {last:.4f}")
     assert last < first
@@ -103,5 +108,6 @@ def test_trained_network_gain_over_jacobi():
         assert st["status"] == 0 and st["rel_res"] <= 1e-8, (name, st)
         res[name] = st
     print("jacobi:", res["jacobi"], "\nlearned:", res["learned"])
-    print(f"learned/jacobi CG iterations {res['learned']['cg_iters'] / res['jacobi']['cg_iters']:.3f}, "
-          f"time {res['learned']['seconds'] / res['jacobi']['seconds']:.3f}")
+    ratio = res["learned"]["cg_iters"] / res["jacobi"]["cg_iters"]
+    print(f"learned/jacobi CG iterations {ratio:.3f}, time {res['learned']['seconds'] / res['jacobi']['seconds']:.3f}")
+    assert ratio < 0.7
