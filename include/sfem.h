@@ -251,6 +251,11 @@ int sfem_gnn_collect(sfem_handle* h, const double* b_free, int32_t every, int32_
                      int32_t* n_added);
 int sfem_gnn_dataset_size(sfem_handle* h, int32_t* n);
 int sfem_gnn_clear_dataset(sfem_handle* h);
+/* how M(r) is evaluated inside the solver and by sfem_gnn_apply: 0 (default) = the network
+ * folded into its polynomial form S^T S x = sum_{j,k} (A^T)^j (A^k x) G_kj with 3x3 blocks
+ * G_kj (exact, since S is linear; six passes over 3-vectors), 1 = the six BF16 tensor-core
+ * layer kernels.  Training always runs the layer kernels. */
+int sfem_gnn_set_inference(sfem_handle* h, int32_t mode);
 /* pairs per Adam step (gradient averaged over them); default 1 */
 int sfem_gnn_set_batch(sfem_handle* h, int32_t batch);
 /* Adam on the collected pairs, `batch` seeded random pairs per step; losses: steps floats

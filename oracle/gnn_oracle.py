@@ -128,3 +128,40 @@ def loss_grad(p, Am, r, dinv, e, Kmul, bf16_layers=True, mode="energy"):
     g[:OFF_C] = s_weight_grad(We, Ws, Am, x, hg) + s_weight_grad(We, Ws, Am, gy, hx)
     g[OFF_C] = c * float(np.sum(gy * x))
     return L, g
+
+
+def poly_coefficients(p, bf16_layers=True):
+    """The network folded into its polynomial form.  S is linear and the feature maps act on
+    the right while A acts on the node index, so they commute:
+        S x = sum_k (A^k x) T_k,   T_k = We^T C_k,   prod_l (P_l + A Q_l) = sum_k A^k C_k,
+        P_l = I + Wa_l^T,  Q_l = Wb_l^T  (Wl = [Wa | Wb]),
+    and  S^T S x = sum_{j,k} (A^T)^j (A^k x) G_kj  with  G_kj = T_k T_j^T  (3 x 3).
+    Returns G (4, 4, 3, 3) and c."""
+    We, Ws, c = unpack(p, bf16_layers)
+    C = [np.eye(H)]
+    for W in Ws:
+        P = np.eye(H) + W[:, :H].T
+        Q = W[:, H:].T
+        nxt = [np.zeros((H, H)) for _ in range(len(C) + 1)]
+        for k, Ck in enumerate(C):
+            nxt[k] += Ck @ P
+            nxt[k + 1] += Ck @ Q
+        C = nxt
+    T = [We.T @ Ck for Ck in C]
+    G = np.array([[T[k] @ T[j].T for j in range(NL + 1)] for k in range(NL + 1)])
+    return G, c
+
+
+def forward_poly(p, Am, r, dinv, bf16_layers=True):
+    """M(r) evaluated through the folded polynomial (equal to ``forward`` in exact arithmetic)."""
+    G, c = poly_coefficients(p, bf16_layers)
+    sd = np.sqrt(np.asarray(dinv, dtype=np.float64).reshape(-1, 3))
+    x = sd * np.asarray(r, dtype=np.float64).reshape(-1, 3)
+    y = [x]
+    for _ in range(NL):
+        y.append(Am @ y[-1])
+    w = [sum(y[k] @ G[k, j] for k in range(NL + 1)) for j in range(NL + 1)]
+    u = w[NL]
+    for j in range(NL - 1, -1, -1):
+        u = Am.T @ u + w[j]
+    return (sd * (c * x + u)).ravel()

@@ -76,6 +76,26 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
   k_gnn_layer_inf<false, true, true><<<grid, LT, 0, st>>>(g, h[2], r, dinv, params, Wsb, nullptr, out, done);
 }
 
+void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
+                       float* w, float* out, const int* done, cudaStream_t st) {
+  static_assert(NL == 3, "the launch sequence below is written for three layers");
+  const int64_t n3 = 3 * g.n;
+  int grid = blocks_for(g.n, 256);
+  count_launch();
+  k_poly_fwd<true><<<grid, 256, 0, st>>>(g, r, dinv, nullptr, y1, done);
+  count_launch();
+  k_poly_fwd<false><<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, done);
+  count_launch();
+  k_poly_mid<<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, pc, w, done);
+  // Horner in A^T: u = w3 -> A^T u + w2 (into y1) -> A^T u + w1 (into y2) -> out
+  count_launch();
+  k_poly_bwd<false><<<grid, 256, 0, st>>>(g, w + 3 * n3, w + 2 * n3, r, dinv, 0.f, y1, done);
+  count_launch();
+  k_poly_bwd<false><<<grid, 256, 0, st>>>(g, y1, w + n3, r, dinv, 0.f, y2, done);
+  count_launch();
+  k_poly_bwd<true><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done);
+}
+
 // the training forward: activations h0..h3 of S at x (kept, with x), then S^T through the
 // weight-gradient kernels' propagation; the same M(r) as launch_apply up to BF16 rounding
 void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,

@@ -23,6 +23,13 @@ constexpr int OFF_C = OFF_L + NL * L_STRIDE;   // log c (weight of the Jacobi te
 constexpr int NPARAM = OFF_C + 1;
 constexpr int LPART = H * AIN;  // per-CTA partial of one layer's weight gradient
 
+// The network folded into its polynomial form (S is linear and its feature maps commute with
+// the node aggregation A):  S^T S x = sum_{j,k} (A^T)^j (A^k x) G[k][j],  G[k][j] 3 x 3.
+struct PolyCoef {
+  float G[NL + 1][NL + 1][9];  // row-major: w_j += y_k G[k][j] (row vector y_k)
+  float c;                     // weight of the Jacobi term
+};
+
 struct Graph {
   int64_t n;              // free nodes
   const int32_t* ptr;     // n + 1

@@ -609,5 +609,111 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_inf(Graph g, const __nv_bfloat
   }
 }
 
+// ======================= inference through the folded polynomial =======================
+// y_{k+1} = A y_k (mean over neighbours), y_0 = x = D^-1/2 r; then w_j = sum_k y_k G[k][j]
+// and M(r) = D^-1/2 (c x + w_0 + A^T (w_1 + A^T (w_2 + A^T w_3)))   (Horner in A^T).
+// Six passes over 3-vectors, one thread per node, fixed-order neighbour sums.
+template <bool FIRST>
+__global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float* __restrict__ r,
+                                                  const float* __restrict__ dinv, const float* __restrict__ yin,
+                                                  float* __restrict__ yout, const int* done) {
+  if (done && *done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    const int e1 = g.ptr[i + 1];
+    for (int e = g.ptr[i]; e < e1; e++) {
+      const int64_t j = 3 * (int64_t)g.idx[e];
+      if (FIRST) {
+        a0 += r[j] * sqrtf(dinv[j]);
+        a1 += r[j + 1] * sqrtf(dinv[j + 1]);
+        a2 += r[j + 2] * sqrtf(dinv[j + 2]);
+      } else {
+        a0 += yin[j];
+        a1 += yin[j + 1];
+        a2 += yin[j + 2];
+      }
+    }
+    const float id = g.inv_deg[i];
+    yout[3 * i] = a0 * id;
+    yout[3 * i + 1] = a1 * id;
+    yout[3 * i + 2] = a2 * id;
+  }
+}
+
+// y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of 3n)
+__global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restrict__ r,
+                                                  const float* __restrict__ dinv, const float* __restrict__ y1,
+                                                  const float* __restrict__ y2, PolyCoef pc, float* __restrict__ w,
+                                                  const int* done) {
+  if (done && *done) return;
+  const int64_t n3 = 3 * g.n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    float y[NL + 1][3];
+    const int64_t o = 3 * i;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      y[0][c] = r[o + c] * sqrtf(dinv[o + c]);
+      y[1][c] = y1[o + c];
+      y[2][c] = y2[o + c];
+      y[3][c] = 0.f;
+    }
+    const int e1 = g.ptr[i + 1];
+    for (int e = g.ptr[i]; e < e1; e++) {
+      const int64_t j = 3 * (int64_t)g.idx[e];
+      y[3][0] += y2[j];
+      y[3][1] += y2[j + 1];
+      y[3][2] += y2[j + 2];
+    }
+    const float id = g.inv_deg[i];
+    y[3][0] *= id;
+    y[3][1] *= id;
+    y[3][2] *= id;
+#pragma unroll
+    for (int jj = 0; jj <= NL; jj++) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        float a = 0.f;
+#pragma unroll
+        for (int k = 0; k <= NL; k++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) a += y[k][b] * pc.G[k][jj][3 * b + c];
+        w[jj * n3 + o + c] = a;
+      }
+    }
+  }
+}
+
+// u_out_i = sum_{j in N(i)} u_in_j / deg_j + wadd_i;  LAST: out = D^-1/2 (c x + that) with x = D^-1/2 r
+template <bool LAST>
+__global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const float* __restrict__ uin,
+                                                  const float* __restrict__ wadd, const float* __restrict__ r,
+                                                  const float* __restrict__ dinv, float cc, float* __restrict__ out,
+                                                  const int* done) {
+  if (done && *done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    const int e1 = g.ptr[i + 1];
+    for (int e = g.ptr[i]; e < e1; e++) {
+      const int jn = g.idx[e];
+      const float wj = g.inv_deg[jn];
+      const int64_t j = 3 * (int64_t)jn;
+      a0 += wj * uin[j];
+      a1 += wj * uin[j + 1];
+      a2 += wj * uin[j + 2];
+    }
+    const int64_t o = 3 * i;
+    const float v[3] = {a0 + wadd[o], a1 + wadd[o + 1], a2 + wadd[o + 2]};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      if (LAST) {
+        const float d = dinv[o + c];
+        out[o + c] = cc * d * r[o + c] + sqrtf(d) * v[c];
+      } else {
+        out[o + c] = v[c];
+      }
+    }
+  }
+}
+
 }  // namespace gnn
 }  // namespace sfem

@@ -1617,6 +1617,10 @@ struct GnnState {
   float* tmp = nullptr;                  // 3N scratch
   int loss_mode = 0;                     // 0: energy norm of the error, 1: residual norm
   int batch = 1;                         // pairs per Adam step
+  int infer_mode = 0;                    // 0: folded polynomial, 1: tensor-core layers
+  gnn::PolyCoef pc{};                    // folded coefficients of the current weights
+  bool pc_dirty = true;
+  float *py1 = nullptr, *py2 = nullptr, *pw = nullptr;  // polynomial-form vectors (3n, 3n, 4 x 3n)
   int adam_t = 0;
   bool train_bufs = false;
   gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg}; }
@@ -1624,7 +1628,8 @@ struct GnnState {
 
 void gnn_free(GnnState* g) {
   void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->params, g->grad, g->m, g->v, g->Wb, g->x, g->xg,
-                  g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->losses, g->z, g->rprev, g->tmp};
+                  g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->losses, g->z, g->rprev, g->tmp,
+                  g->py1, g->py2, g->pw};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int l = 0; l <= gnn::NL; l++) {
@@ -1665,14 +1670,84 @@ int gnn_refresh_diag(sfem_handle* h) {
   return 0;
 }
 
+float bf16_rne(float v) {  // the rounding of __float2bfloat16 for finite values
+  uint32_t u;
+  memcpy(&u, &v, 4);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  u &= 0xffff0000u;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+
+// Fold the current weights into the polynomial coefficients (FP64 on the host, from the same
+// BF16-rounded layer weights the tensor-core kernels use):
+//   prod_l (P_l + A Q_l) = sum_k A^k C_k,  P_l = I + Wa_l^T,  Q_l = Wb_l^T,
+//   T_k = We^T C_k (3 x H),  G[k][j] = T_k T_j^T.
+int gnn_poly_refresh(sfem_handle* h) {
+  GnnState* g = h->gnn;
+  if (!g->pc_dirty) return 0;
+  constexpr int H = gnn::H, K = gnn::NL + 1;
+  std::vector<float> prm(gnn::NPARAM);
+  CU(cudaMemcpyAsync(prm.data(), g->params, gnn::NPARAM * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  std::vector<double> C((size_t)K * H * H, 0.0), N((size_t)K * H * H), P((size_t)H * H), Q((size_t)H * H);
+  for (int a = 0; a < H; a++) C[(size_t)a * H + a] = 1.0;
+  for (int l = 0; l < gnn::NL; l++) {
+    const float* W = prm.data() + gnn::OFF_L + (size_t)l * gnn::L_STRIDE;  // [H][AIN]
+    for (int a = 0; a < H; a++)
+      for (int o = 0; o < H; o++) {
+        P[(size_t)a * H + o] = (a == o ? 1.0 : 0.0) + bf16_rne(W[(size_t)o * gnn::AIN + a]);
+        Q[(size_t)a * H + o] = bf16_rne(W[(size_t)o * gnn::AIN + H + a]);
+      }
+    std::fill(N.begin(), N.end(), 0.0);
+    for (int k = 0; k <= l; k++) {
+      const double* Ck = &C[(size_t)k * H * H];
+      for (int a = 0; a < H; a++)
+        for (int b = 0; b < H; b++) {
+          const double cab = Ck[(size_t)a * H + b];
+          if (cab == 0.0) continue;
+          double* n0 = &N[(size_t)k * H * H + (size_t)a * H];
+          double* n1 = &N[(size_t)(k + 1) * H * H + (size_t)a * H];
+          for (int o = 0; o < H; o++) {
+            n0[o] += cab * P[(size_t)b * H + o];
+            n1[o] += cab * Q[(size_t)b * H + o];
+          }
+        }
+    }
+    C.swap(N);
+  }
+  std::vector<double> T((size_t)K * 3 * H, 0.0);
+  for (int k = 0; k < K; k++)
+    for (int f = 0; f < 3; f++)
+      for (int b = 0; b < H; b++) {
+        const double e = prm[gnn::OFF_WE + (size_t)b * gnn::FIN + f];
+        for (int a = 0; a < H; a++) T[((size_t)k * 3 + f) * H + a] += e * C[(size_t)k * H * H + (size_t)b * H + a];
+      }
+  for (int k = 0; k < K; k++)
+    for (int j = 0; j < K; j++)
+      for (int f = 0; f < 3; f++)
+        for (int q = 0; q < 3; q++) {
+          double a = 0.0;
+          for (int x = 0; x < H; x++) a += T[((size_t)k * 3 + f) * H + x] * T[((size_t)j * 3 + q) * H + x];
+          g->pc.G[k][j][3 * f + q] = (float)a;
+        }
+  g->pc.c = (float)std::exp((double)prm[gnn::OFF_C]);
+  g->pc_dirty = false;
+  return 0;
+}
+
 // out = M(r) over the free block (r, out point at free-block starts); done may be null.
-// With train, x = D^-1/2 r is kept for the weight gradient.
+// With train, x = D^-1/2 r and the activations of S are kept for the weight gradient.
+// Inference uses the folded polynomial (gnn_poly_refresh must have run) or the layers.
 void gnn_apply_dev(sfem_handle* h, const float* r, float* out, const int* done, bool train) {
   GnnState* g = h->gnn;
   const size_t o = 3 * (size_t)h->nbc;
   const float* dinv = h->k32.dinv + o;
   if (train)
     gnn::launch_apply_train(g->graph(), r, dinv, g->params, g->Wb, g->h, g->x, g->G0, g->G1, g->G2, out, h->stream);
+  else if (g->infer_mode == 0)
+    gnn::launch_apply_poly(g->graph(), r, dinv, g->pc, g->py1, g->py2, g->pw, out, done, h->stream);
   else
     gnn::launch_apply(g->graph(), r, dinv, g->params, g->Wb, g->h, out, done, h->stream);
 }
@@ -1729,6 +1804,7 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   s0.max_it = max_it;
   *h->scal_h = s0;
   CU(cudaMemcpyAsync(h->scal, h->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
+  TRY(gnn_poly_refresh(h));
   launch_cg_init<float>(n, b + o, x + o, w.r + o, w.p + o, w.dinv + o, h->red(), h->scal, h->stream);
   const int* done = &h->scal->done;
   gnn_apply_dev(h, w.r + o, g->z + o, done, false);
@@ -1870,6 +1946,9 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   TRY(dalloc(&g->v, gnn::NPARAM));
   TRY(dalloc(&g->Wb, (size_t)3 * gnn::NL * gnn::H * gnn::AIN));
   for (int l = 0; l <= gnn::NL; l++) TRY(dalloc(&g->h[l], nh));
+  TRY(dalloc(&g->py1, 3 * (size_t)n));
+  TRY(dalloc(&g->py2, 3 * (size_t)n));
+  TRY(dalloc(&g->pw, 12 * (size_t)n));
   TRY(dalloc(&g->spart, 4096));
   TRY(dalloc(&g->scount, 1));
   TRY(dalloc(&g->z, 3 * (size_t)h->N));
@@ -1897,6 +1976,14 @@ int sfem_gnn_set_loss(sfem_handle* h, int32_t mode) {
   return SFEM_OK;
 }
 
+int sfem_gnn_set_inference(sfem_handle* h, int32_t mode) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  if (mode != 0 && mode != 1) return fail(SFEM_ERR_INVALID, "inference mode is 0 (folded polynomial) or 1 (layers)");
+  h->gnn->infer_mode = mode;
+  return SFEM_OK;
+}
+
 int sfem_gnn_set_batch(sfem_handle* h, int32_t batch) {
   TRY(check_handle(h));
   TRY(gnn_need(h));
@@ -1917,6 +2004,7 @@ int sfem_gnn_set_params(sfem_handle* h, const float* params) {
   TRY(gnn_need(h));
   CU(cudaMemcpyAsync(h->gnn->params, params, gnn::NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   gnn::launch_pack(h->gnn->params, h->gnn->Wb, h->stream);
+  h->gnn->pc_dirty = true;
   h->gnn->adam_t = 0;
   CU(cudaMemsetAsync(h->gnn->m, 0, gnn::NPARAM * sizeof(float), h->stream));
   CU(cudaMemsetAsync(h->gnn->v, 0, gnn::NPARAM * sizeof(float), h->stream));
@@ -1934,6 +2022,7 @@ int sfem_gnn_apply(sfem_handle* h, const double* r_free, double* out_free) {
   TRY(gnn_refresh_diag(h));
   CU(cudaMemcpyAsync(h->tmp64 + o, r_free, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   launch_convert<double, float>((int64_t)n, h->tmp64 + o, w.r + o, h->stream);
+  TRY(gnn_poly_refresh(h));
   gnn_apply_dev(h, w.r + o, h->gnn->z + o, nullptr, false);
   launch_convert<float, double>((int64_t)n, h->gnn->z + o, h->tmp64b + o, h->stream);
   CU(cudaMemcpyAsync(out_free, h->tmp64b + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -2106,6 +2195,7 @@ int sfem_gnn_train(sfem_handle* h, int32_t steps, float lr, uint64_t seed, float
     }
     g->adam_t++;
     gnn::launch_adam(g->grad, g->params, g->m, g->v, lr, g->adam_t, 1.f / (float)g->batch, g->Wb, h->stream);
+    g->pc_dirty = true;
     if ((t & 63) == 63) TRY(sync(h));
   }
   if (losses) CU(cudaMemcpyAsync(losses, g->losses, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost, h->stream));

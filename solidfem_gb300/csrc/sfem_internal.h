@@ -202,6 +202,9 @@ namespace gnn {
 // fused into the first and last); Wb holds the 3 packed BF16 weight sets (k_gnn_pack)
 void launch_apply(const Graph& g, const float* r, const float* dinv, const float* params, const __nv_bfloat16* Wb,
                   __nv_bfloat16* const* h, float* out, const int* done, cudaStream_t st);
+// the same M(r) through the folded polynomial (six passes over 3-vectors); y1, y2: 3n, w: 4 x 3n
+void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
+                       float* w, float* out, const int* done, cudaStream_t st);
 // the same M(r) keeping the activations h0..h3 of S and x = D^-1/2 r (training)
 void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,
                         const __nv_bfloat16* Wb, __nv_bfloat16* const* h, float* x, float* G0, float* G1, float* G2,

@@ -65,6 +65,11 @@ class LearnedPreconditioner:
     def load(self, path: str) -> None:
         self.set_params(np.fromfile(path, dtype=np.float32))
 
+    def set_inference(self, mode: str) -> None:
+        """'poly': the network folded into 3x3 polynomial coefficients (default, exact since S
+        is linear); 'layers': the BF16 tensor-core layer kernels."""
+        nat.check(self._lib.sfem_gnn_set_inference(self.phys.handle, {"poly": 0, "layers": 1}[mode]))
+
     def set_batch(self, batch: int) -> None:
         """Pairs per Adam step (the gradient is averaged over them)."""
         nat.check(self._lib.sfem_gnn_set_batch(self.phys.handle, int(batch)))

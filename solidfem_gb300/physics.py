@@ -51,6 +51,7 @@ class FemPhysicsMatrixFree:
         nat.check(self._lib.sfem_create(_dp(nodes), nodes.shape[0], tets.ctypes.data_as(nat._ip), tets.shape[0],
                                         fixed.ctypes.data_as(nat._ip), fixed.size, C.byref(cfg), C.byref(h)))
         self._h = h
+        self.tets_original, self.rest_positions = tets.copy(), nodes.copy()  # caller's order
         n, nf, e = C.c_int64(), C.c_int64(), C.c_int64()
         self._lib.sfem_sizes(h, C.byref(n), C.byref(nf), C.byref(e))
         self.n_nodes, self.n_free, self.n_tets = n.value, nf.value, e.value

@@ -59,3 +59,16 @@ def test_oracle_gradient_matches_central_differences(mode):
         fd = (go.loss_grad(pp, Am, r, dinv, e, K, bf16_layers=False, mode=mode)[0]
               - go.loss_grad(pm, Am, r, dinv, e, K, bf16_layers=False, mode=mode)[0]) / (2 * h)
         assert abs(fd - g[k]) <= 1e-6 * np.abs(g).max() + 1e-4 * abs(fd), (k, fd, g[k])
+
+
+def test_folded_polynomial_equals_the_network():
+    o, Am, dinv = small_problem()
+    rng = np.random.default_rng(5)
+    p = rng.normal(size=go.NPARAM) * 0.1
+    r = rng.normal(size=3 * o.n_free)
+    a, b = go.forward(p, Am, r, dinv), go.forward_poly(p, Am, r, dinv)
+    assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a)
+    G, _ = go.poly_coefficients(p)
+    for k in range(go.NL + 1):  # G_kj = T_k T_j^T: G_kj = G_jk^T
+        for j in range(go.NL + 1):
+            np.testing.assert_allclose(G[k, j], G[j, k].T, rtol=1e-12, atol=1e-14 * np.abs(G).max())

@@ -36,9 +36,11 @@ def rel(a, b):
     return np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b))
 
 
-def test_forward_matches_fp64_oracle():
+@pytest.mark.parametrize("mode", ["poly", "layers"])
+def test_forward_matches_fp64_oracle(mode):
     m, fixed, _ = slab(24, 8, 8)
     p, net, o, Am, dinv = gpu_and_oracle(m, fixed, seed=3)
+    net.set_inference(mode)
     rng = np.random.default_rng(1)
     r = rng.normal(size=3 * o.n_free)
     out_g = net.apply(r)
@@ -49,8 +51,10 @@ def test_forward_matches_fp64_oracle():
     c = np.exp(prm[go.OFF_C])
     ss_g, ss_o = out_g - c * dinv * r, out_o - c * dinv * r
     err_ss = rel(ss_g, ss_o)
-    print(f"M(r) GPU (BF16 activations) vs FP64 oracle: rel err {err:.2e}; S^T S part {err_ss:.2e}")
+    print(f"M(r) GPU ({mode}) vs FP64 oracle: rel err {err:.2e}; S^T S part {err_ss:.2e}")
     assert err < 2e-2 and err_ss < 3e-2
+    if mode == "poly":  # FP32 arithmetic on the folded coefficients: no BF16 activations
+        assert err_ss < 1e-4
     # linear and symmetric on the device too (up to BF16 rounding of the activations)
     u, v = rng.normal(size=(2, 3 * o.n_free))
     Mu, Mv = net.apply(u), net.apply(v)
@@ -101,13 +105,15 @@ def test_trained_network_gain_over_jacobi():
     assert last < first
     f_eval = random_top_traction(m, seed=10000)
     res = {}
-    for name, pc in [("jacobi", PC_JACOBI), ("learned", PC_LEARNED)]:
+    for name, pc in [("jacobi", PC_JACOBI), ("learned", PC_LEARNED), ("learned-layers", PC_LEARNED)]:
+        if name == "learned-layers":
+            net.set_inference("layers")
         p.set_nodal_loads(f_eval)
         p.set_positions(m.nodes)
         st = p.newton_solve(rel_tol=1e-8, max_newton=30, precond=pc)
         assert st["status"] == 0 and st["rel_res"] <= 1e-8, (name, st)
         res[name] = st
-    print("jacobi:", res["jacobi"], "\nlearned:", res["learned"])
+    print("jacobi:", res["jacobi"], "\nlearned:", res["learned"], "\nlearned, layer kernels:", res["learned-layers"])
     ratio = res["learned"]["cg_iters"] / res["jacobi"]["cg_iters"]
     print(f"learned/jacobi CG iterations {ratio:.3f}, time {res['learned']['seconds'] / res['jacobi']['seconds']:.3f}")
     assert ratio < 0.7
