@@ -194,7 +194,8 @@ def run_reference_arm(args):
     line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": 0,
             "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "method": "FP64 Jacobi-PCG Newton, oracle CPU port (extrapolated)"},
+            "config": {"workload": WORKLOAD if not args.small else "reduced (64, 16, 16) variant of: " + WORKLOAD,
+                       "method": "FP64 Jacobi-PCG Newton, oracle CPU port (extrapolated)"},
             "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

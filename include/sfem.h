@@ -226,6 +226,26 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
 int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max_cg,
                  double* dLdE, double* dLdf);
 
+/* ---- dynamics (FemPhysicsMatrixFree::Step :297-324, SubStep :371-387, MatrixVectorMultiply
+ * :523-534 and ComputeGradients :536-560 with mTimeStep != 0, Solve :589-597) ----
+ * Time step h of the implicit (backward Euler) terms: with h > 0 the residual gains
+ * (m/h) v - (m/h^2)(x - x_start) and the tangent m/h^2 (lumped masses), as the reference's
+ * matrix-free class does; h = 0 restores the static problem. */
+#define SFEM_SIM_EXPLICIT 2 /* SimulationType ST_EXPLICIT */
+#define SFEM_SIM_IMPLICIT 3 /* SimulationType ST_IMPLICIT */
+int sfem_set_time_step(sfem_handle* h, double dt);
+int sfem_get_time_step(sfem_handle* h, double* dt);
+/* node velocities, original node order (N x 3); fixed nodes stay at rest */
+int sfem_set_velocities(sfem_handle* h, const double* vel);
+int sfem_get_velocities(sfem_handle* h, double* vel);
+/* x_start = current positions (the reference's pos0 = pos at the start of Step) */
+int sfem_begin_step(sfem_handle* h);
+/* Step(dt) with mNumSteps = substeps.  EXPLICIT: symplectic Euler substeps on the elastic forces
+ * and gravity.  IMPLICIT: x_start = x, time step dt/substeps, per substep a Newton solve (opts)
+ * then v = (x - x_start)/h; the time step stays set afterwards, as in the reference. */
+int sfem_step(sfem_handle* h, double dt, int32_t sim_type, int32_t substeps, const sfem_newton_opts* opts,
+              sfem_newton_stats* stats);
+
 /* ---- learned preconditioner (extension: the reference has no learned components) ----
  * A linear message-passing network S on the free-node mesh graph (3 layers, width 64, BF16
  * weights and activations, FP32 accumulation on the tensor cores) defines the symmetric

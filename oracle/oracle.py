@@ -76,6 +76,10 @@ class Oracle:
                          "orc_element_forces", "orc_set_element_scale"]:
                 getattr(lib, name).argtypes = [C.c_void_p, _dp]
             lib.orc_set_force_fraction.argtypes = [C.c_void_p, C.c_double]
+            lib.orc_set_time_step.argtypes = [C.c_void_p, C.c_double]
+            lib.orc_explicit_substep.argtypes = [C.c_void_p, C.c_double]
+            for name in ["orc_set_velocities_shuffled", "orc_get_velocities_shuffled", "orc_set_start_shuffled"]:
+                getattr(lib, name).argtypes = [C.c_void_p, _dp]
             lib.orc_set_lame.argtypes = [C.c_void_p, C.c_double, C.c_double]
             lib.orc_set_tangent.argtypes = [C.c_void_p, C.c_int]
             lib.orc_set_pressure_surface.argtypes = [C.c_void_p, _ip, C.c_int, C.c_double]
@@ -128,6 +132,26 @@ class Oracle:
 
     def set_force_fraction(self, f):
         self.lib().orc_set_force_fraction(self.h, f)
+
+    # ---- dynamics (reshuffled node order) ----
+    def set_time_step(self, dt):
+        self.lib().orc_set_time_step(self.h, float(dt))
+
+    def set_velocities_shuffled(self, v):
+        v = _f64(v).reshape(-1, 3)
+        self.lib().orc_set_velocities_shuffled(self.h, _p(v))
+
+    def velocities_shuffled(self):
+        v = np.zeros((self.n_nodes, 3))
+        self.lib().orc_get_velocities_shuffled(self.h, _p(v))
+        return v
+
+    def set_start_shuffled(self, x):
+        x = _f64(x).reshape(-1, 3)
+        self.lib().orc_set_start_shuffled(self.h, _p(x))
+
+    def explicit_substep(self, hs):
+        self.lib().orc_explicit_substep(self.h, float(hs))
 
     def set_lame(self, mu, lam):
         self.lib().orc_set_lame(self.h, mu, lam)
@@ -279,6 +303,11 @@ class RefHarness:
             lib.ref_elastic_energy.restype = C.c_double
             lib.ref_force_param_grads.argtypes = [C.c_void_p, _dp, _dp, _dp]
             lib.ref_step.argtypes = [C.c_void_p]
+            lib.ref_set_sim.argtypes = [C.c_void_p, C.c_int, C.c_int]
+            lib.ref_set_time_step.argtypes = [C.c_void_p, C.c_double]
+            lib.ref_step_dt.argtypes = [C.c_void_p, C.c_double]
+            for name in ["ref_set_velocities_shuffled", "ref_get_velocities_shuffled", "ref_set_start_shuffled"]:
+                getattr(lib, name).argtypes = [C.c_void_p, _dp]
             lib.ref_newton_direct.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp]
             lib.ref_newton_direct.restype = C.c_int
             lib.ref_newton_fd.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp]
@@ -374,6 +403,29 @@ class RefHarness:
 
     def step(self):
         self.lib().ref_step(self.h)
+
+    # ---- dynamics (reshuffled node order) ----
+    def set_sim(self, simtype, substeps=1):
+        self.lib().ref_set_sim(self.h, int(simtype), int(substeps))
+
+    def set_time_step(self, dt):
+        self.lib().ref_set_time_step(self.h, float(dt))
+
+    def set_velocities_shuffled(self, v):
+        v = _f64(v).reshape(-1, 3)
+        self.lib().ref_set_velocities_shuffled(self.h, _p(v))
+
+    def velocities_shuffled(self):
+        v = np.zeros((self.n_nodes, 3))
+        self.lib().ref_get_velocities_shuffled(self.h, _p(v))
+        return v
+
+    def set_start_shuffled(self, x):
+        x = _f64(x).reshape(-1, 3)
+        self.lib().ref_set_start_shuffled(self.h, _p(x))
+
+    def step_dt(self, dt):
+        self.lib().ref_step_dt(self.h, float(dt))
 
     def newton_fd(self, max_iters=50, rel_tol=1e-12):
         r = np.zeros(1)

@@ -39,6 +39,8 @@ struct RefProblem : public FemPhysicsMatrixFree {
       : FemPhysicsMatrixFree(t, n, c) {}
 
   void SetForceFraction(real f) { mForceFraction = f; }
+  void SetSim(int type, int steps) { mSimType = (SimulationType)type; mNumSteps = steps; }
+  void SetTimeStep(real h) { mTimeStep = h; }
   uint32 NumBCs() const { return mNumBCs; }
   const std::vector<uint32>& Map() const { return mReshuffleMap; }
   std::vector<Node>& Nodes() { return nodes; }
@@ -232,6 +234,28 @@ void ref_force_param_grads(void* hp, double* gmu, double* glambda, double* grho)
 
 // The reference's own static solve: Step(0) dispatching on the configured solver.
 void ref_step(void* hp) { ((Handle*)hp)->phys->Step(0); }
+
+// Dynamics: simulation type / substeps (FemPhysicsBase mSimType, mNumSteps), the time step
+// of the implicit terms (mTimeStep), node velocities and step-start positions (pos0), in
+// reshuffled order, and the reference's own Step(dt).
+void ref_set_sim(void* hp, int type, int steps) { ((Handle*)hp)->phys->SetSim(type, steps); }
+void ref_set_time_step(void* hp, double h) { ((Handle*)hp)->phys->SetTimeStep(h); }
+void ref_set_velocities_shuffled(void* hp, const double* v) {
+  RefProblem* p = ((Handle*)hp)->phys;
+  for (uint32 i = 0; i < p->GetNumNodes(); i++) p->Nodes()[i].vel = Vector3R(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+}
+void ref_get_velocities_shuffled(void* hp, double* v) {
+  RefProblem* p = ((Handle*)hp)->phys;
+  for (uint32 i = 0; i < p->GetNumNodes(); i++) {
+    const Vector3R& a = p->Nodes()[i].vel;
+    v[3 * i] = a.x; v[3 * i + 1] = a.y; v[3 * i + 2] = a.z;
+  }
+}
+void ref_set_start_shuffled(void* hp, const double* x) {
+  RefProblem* p = ((Handle*)hp)->phys;
+  for (uint32 i = 0; i < p->GetNumNodes(); i++) p->Nodes()[i].pos0 = Vector3R(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+}
+void ref_step_dt(void* hp, double dt) { ((Handle*)hp)->phys->Step(dt); }
 
 // Harness Newton with a direct sparse LU inner solve over the assembled
 // reference tangent; includes dead loads.  Residual-norm backtracking.

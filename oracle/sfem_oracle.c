@@ -131,6 +131,9 @@ typedef struct {
   int n_tris;        /* follower-pressure surface (original node indices), 3 per triangle */
   int* tris;
   double pressure;
+  double time_step;  /* mTimeStep: 0 static, h > 0 backward-Euler terms */
+  double* vel;       /* node velocities, reshuffled, 3N */
+  double* xstart;    /* positions at the start of the step (the reference's pos0), reshuffled, 3N */
 } orc_problem;
 
 static M3 load_X(const orc_problem* p, int e) { M3 r; memcpy(r.m, p->X + 9 * (size_t)e, 9 * sizeof(double)); return r; }
@@ -166,6 +169,8 @@ void* orc_create(const double* nodes, int n_nodes, const int* tets, int n_tets,
   p->pos = (double*)malloc(sizeof(double) * 3 * n_nodes);
   p->pos0 = (double*)malloc(sizeof(double) * 3 * n_nodes);
   p->fext = (double*)calloc(3 * (size_t)n_nodes, sizeof(double));
+  p->vel = (double*)calloc(3 * (size_t)n_nodes, sizeof(double));
+  p->xstart = (double*)malloc(sizeof(double) * 3 * n_nodes);
   for (int i = 0; i < n_nodes; i++)
     for (int c = 0; c < 3; c++) p->pos[3 * p->map[i] + c] = p->pos0[3 * p->map[i] + c] = nodes[3 * i + c];
   p->tets = (int*)malloc(sizeof(int) * 4 * (size_t)n_tets);
@@ -197,6 +202,7 @@ void* orc_create(const double* nodes, int n_nodes, const int* tets, int n_tets,
   }
   free(masses);
   free(is_fixed);
+  memcpy(p->xstart, p->pos, sizeof(double) * 3 * n_nodes);
   return p;
 }
 
@@ -204,7 +210,7 @@ void orc_destroy(void* h) {
   orc_problem* p = (orc_problem*)h;
   free(p->tris);
   free(p->map); free(p->tets); free(p->X); free(p->vol); free(p->escale);
-  free(p->pos); free(p->pos0); free(p->inv_mass); free(p->fext); free(p);
+  free(p->pos); free(p->pos0); free(p->inv_mass); free(p->fext); free(p->vel); free(p->xstart); free(p);
 }
 
 int orc_num_bcs(void* h) { return ((orc_problem*)h)->n_bcs; }
@@ -212,6 +218,11 @@ int orc_num_free(void* h) { orc_problem* p = (orc_problem*)h; return p->n_nodes 
 void orc_reshuffle_map(void* h, int* out) { orc_problem* p = (orc_problem*)h; memcpy(out, p->map, sizeof(int) * p->n_nodes); }
 void orc_tets(void* h, int* out) { orc_problem* p = (orc_problem*)h; memcpy(out, p->tets, sizeof(int) * 4 * (size_t)p->n_tets); }
 void orc_set_force_fraction(void* h, double f) { ((orc_problem*)h)->force_fraction = f; }
+/* dynamics: mTimeStep, node velocities and step-start positions (reshuffled order) */
+void orc_set_time_step(void* h, double dt) { ((orc_problem*)h)->time_step = dt; }
+void orc_set_velocities_shuffled(void* h, const double* v) { orc_problem* p = (orc_problem*)h; memcpy(p->vel, v, sizeof(double) * 3 * p->n_nodes); }
+void orc_get_velocities_shuffled(void* h, double* v) { orc_problem* p = (orc_problem*)h; memcpy(v, p->vel, sizeof(double) * 3 * p->n_nodes); }
+void orc_set_start_shuffled(void* h, const double* x) { orc_problem* p = (orc_problem*)h; memcpy(p->xstart, x, sizeof(double) * 3 * p->n_nodes); }
 /* 0: the reference's force differential; 1: exact derivative of the force (differs for corotational). */
 void orc_set_tangent(void* h, int mode) { ((orc_problem*)h)->tangent = mode; }
 void orc_set_lame(void* h, double mu, double lambda) { orc_problem* p = (orc_problem*)h; p->mu = mu; p->lambda = lambda; }
@@ -348,10 +359,18 @@ void orc_compute_gradients(void* h, double* r) {
     int g = i + p->n_bcs;
     double mass = 1.0 / p->inv_mass[g];
     double s = mass * p->force_fraction;
+    /* FemPhysicsMatrixFree.cpp:545-556: invH = 1/h, invHSqr = 1/(h h), both 0 for a static solve */
+    double invH = p->time_step == 0 ? 0 : 1.0 / p->time_step;
+    double invHSqr = p->time_step == 0 ? 0 : 1.0 / (p->time_step * p->time_step);
     for (int c = 0; c < 3; c++) {
-      r[3 * (size_t)i + c] = f[3 * (size_t)g + c];
+      size_t k = 3 * (size_t)g + c;
+      r[3 * (size_t)i + c] = f[k];
       r[3 * (size_t)i + c] += s * p->grav[c];
-      r[3 * (size_t)i + c] += p->force_fraction * p->fext[3 * (size_t)g + c];
+      if (p->time_step != 0) {
+        r[3 * (size_t)i + c] += mass * invH * p->vel[k];
+        r[3 * (size_t)i + c] -= mass * invHSqr * (p->pos[k] - p->xstart[k]);
+      }
+      r[3 * (size_t)i + c] += p->force_fraction * p->fext[k];
     }
   }
   free(f);
@@ -464,9 +483,31 @@ void orc_matvec(void* h, const double* d, double* out) {
     }
     if (t[0] >= nbc) for (int c = 0; c < 3; c++) df[3 * (size_t)(t[0] - nbc) + c] += f3[c];
   }
-  for (size_t i = 0; i < 3 * (size_t)nf; i++) out[i] = -df[i];
+  /* MatrixVectorMultiply (FemPhysicsMatrixFree.cpp:523-534): M d / h^2 - df */
+  double invHSqr = p->time_step == 0 ? 0 : 1.0 / (p->time_step * p->time_step);
+  for (size_t i = 0; i < 3 * (size_t)nf; i++) {
+    double mass = 1.0 / p->inv_mass[nbc + i / 3];
+    out[i] = invHSqr * mass * d[i] - df[i];
+  }
   free(df);
   free(dH);
+}
+
+/* FemPhysicsMatrixFree::SubStep (Source/FemPhysicsMatrixFree.cpp:371-387): elastic forces only,
+ * then for every node with invMass != 0: vel += (h invMass) f + h g, pos += h vel. */
+void orc_explicit_substep(void* h, double hs) {
+  orc_problem* p = (orc_problem*)h;
+  double* f = (double*)malloc(sizeof(double) * 3 * p->n_nodes);
+  internal_forces(p, f);
+  for (int i = 0; i < p->n_nodes; i++) {
+    if (p->inv_mass[i] == 0) continue;
+    for (int c = 0; c < 3; c++) {
+      size_t k = 3 * (size_t)i + c;
+      p->vel[k] += (hs * p->inv_mass[i]) * f[k] + hs * p->grav[c];
+      p->pos[k] += hs * p->vel[k];
+    }
+  }
+  free(f);
 }
 
 /* Per-DOF diagonal of the tangent over free DOFs: the diagonal entries of the
@@ -509,6 +550,11 @@ void orc_jacobi_diagonal(void* h, double* diag) {
     }
   }
   free(kdall);
+  if (p->time_step != 0) {  /* the M / h^2 term of the dynamic tangent */
+    double invHSqr = 1.0 / (p->time_step * p->time_step);
+    for (int i = 0; i < nf; i++)
+      for (int c = 0; c < 3; c++) diag[3 * (size_t)i + c] += invHSqr * (1.0 / p->inv_mass[nbc + i]);
+  }
 }
 
 /* PK1 stress of all elements at the current positions (E x 9). */

@@ -25,6 +25,7 @@ SFEM_ERR_NO_DEVICE = -7
 MMT_LINEAR, MMT_STVK, MMT_COROTATIONAL, MMT_NEO_HOOKEAN = 0, 1, 2, 3
 FP64, FP32 = 0, 1
 PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
+SIM_EXPLICIT, SIM_IMPLICIT = 2, 3
 LSC_ARMIJO, LSC_ENGINEERING, LSC_RESIDUAL = 0, 1, 2
 TANGENT_REFERENCE, TANGENT_EXACT = 0, 1
 
@@ -105,6 +106,12 @@ SIGNATURES = {
     "sfem_force_param_grads": [_vp, _dp, _dp, _dp],
     "sfem_pcg": [_vp, _dp, _dp, C.POINTER(PcgOpts), C.POINTER(PcgStats)],
     "sfem_newton_solve": [_vp, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)],
+    "sfem_set_time_step": [_vp, C.c_double],
+    "sfem_get_time_step": [_vp, _dp],
+    "sfem_set_velocities": [_vp, _dp],
+    "sfem_get_velocities": [_vp, _dp],
+    "sfem_begin_step": [_vp],
+    "sfem_step": [_vp, C.c_double, C.c_int32, C.c_int32, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)],
     "sfem_nonlinear_cg": [_vp, C.c_int32, C.c_int32, C.c_double, _ip],
     "sfem_adjoint": [_vp, _dp, C.c_double, C.c_int32, _dp, _dp],
     "sfem_gnn_num_params": [_ip],

@@ -80,7 +80,7 @@ void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const 
                        float* w, float* out, const int* done, cudaStream_t st) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
   const int64_t n3 = 3 * g.n;
-  int grid = blocks_for(g.n, 256);
+  const int grid = (int)std::min<int64_t>(blocks_for(g.n, 16), 152 * 16);  // 16 nodes per 256-thread block
   count_launch();
   k_poly_fwd<true><<<grid, 256, 0, st>>>(g, r, dinv, nullptr, y1, done);
   count_launch();
@@ -182,17 +182,6 @@ void launch_pack(const float* prm, __nv_bfloat16* Wb, cudaStream_t st) {
 namespace sfem {
 namespace gnn {
 
-__device__ __forceinline__ float block_sum256(float v, float* sm) {
-  v = warp_sumf(v);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float b = 0.f;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) b += sm[w];
-  __syncthreads();
-  return b;  // valid in thread 0
-}
-
 // d = a - b
 __global__ void k_sub(int64_t n, const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ d) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -208,26 +197,13 @@ void launch_sub(int64_t n, const float* a, const float* b, float* d, cudaStream_
 __global__ void __launch_bounds__(256) k_fcg_init(int64_t n, const float* __restrict__ r, const float* __restrict__ z,
                                                   float* __restrict__ p, float* __restrict__ partials,
                                                   unsigned* counter, CgScalars* s) {
-  __shared__ float sm[8];
-  __shared__ bool last;
-  float acc = 0.f;
+  float acc[1] = {0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     p[i] = z[i];
-    acc += r[i] * z[i];
+    acc[0] += r[i] * z[i];
   }
-  const float b = block_sum256(acc, sm);
-  if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last || threadIdx.x != 0) return;
-  __threadfence();
-  double t = 0.0;
-  for (unsigned k = 0; k < gridDim.x; k++) t += (double)__ldcg(&partials[k]);
-  s->rz = t;
-  *counter = 0u;
+  double t[1];
+  if (last_block_sums<1>(acc, partials, counter, t) && threadIdx.x == 0) s->rz = t[0];
 }
 
 // x += alpha p, rprev = r, r -= alpha q, rr
@@ -236,29 +212,19 @@ __global__ void __launch_bounds__(256) k_fcg_update(int64_t n, float* __restrict
                                                     const float* __restrict__ q, float* __restrict__ partials,
                                                     unsigned* counter, CgScalars* s) {
   if (s->done) return;
-  __shared__ float sm[8];
-  __shared__ bool last;
   const float a = (float)s->alpha;
-  float acc = 0.f;
+  float acc[1] = {0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += a * p[i];
     const float ri = r[i];
     rprev[i] = ri;
     const float rn = ri - a * q[i];
     r[i] = rn;
-    acc += rn * rn;
+    acc[0] += rn * rn;
   }
-  const float b = block_sum256(acc, sm);
-  if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last || threadIdx.x != 0) return;
-  __threadfence();
-  double t = 0.0;
-  for (unsigned k = 0; k < gridDim.x; k++) t += (double)__ldcg(&partials[k]);
+  double tt[1];
+  if (!last_block_sums<1>(acc, partials, counter, tt) || threadIdx.x != 0) return;
+  const double t = tt[0];
   s->rr = t;
   s->it += 1;
   if (!isfinite(t)) {
@@ -270,48 +236,29 @@ __global__ void __launch_bounds__(256) k_fcg_update(int64_t n, float* __restrict
     s->done = 1;
     s->status = 1;
   }
-  *counter = 0u;
 }
 
 // Polak-Ribiere: beta = z.(r - rprev) / rz_old, rz = z.r.  The same sums are formed for the
 // Jacobi direction z_J = D^-1 r; when the learned direction is not a descent direction
-// (z.r <= 0) or is far less aligned with r than Jacobi's, this iteration falls back to
-// Jacobi (s->status = 0 keeps the solve going; s->beta / s->rz refer to the chosen z and
+// (z.r <= 0) this iteration falls back to Jacobi (s->beta / s->rz refer to the chosen z and
 // s->pq carries the choice to k_fcg_dir: pq < 0 selects Jacobi).
 __global__ void __launch_bounds__(256) k_fcg_beta(int64_t n, const float* __restrict__ r,
                                                   const float* __restrict__ rprev, const float* __restrict__ z,
                                                   const float* __restrict__ dinv, float* __restrict__ partials,
                                                   unsigned* counter, CgScalars* s) {
   if (s->done) return;
-  __shared__ float sm[8];
-  __shared__ bool last;
-  float a0 = 0.f, a1 = 0.f, j0 = 0.f, j1 = 0.f;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float dr = r[i] - rprev[i];
-    const float zj = dinv[i] * r[i];
-    a0 += z[i] * dr;
-    a1 += z[i] * r[i];
-    j0 += zj * dr;
-    j1 += zj * r[i];
+    const float ri = r[i];
+    const float dr = ri - rprev[i];
+    const float zj = dinv[i] * ri;
+    acc[0] += z[i] * dr;
+    acc[1] += z[i] * ri;
+    acc[2] += zj * dr;
+    acc[3] += zj * ri;
   }
-  const float b0 = block_sum256(a0, sm);
-  const float b1 = block_sum256(a1, sm);
-  const float c0 = block_sum256(j0, sm);
-  const float c1 = block_sum256(j1, sm);
-  if (threadIdx.x == 0) {
-    partials[4 * blockIdx.x] = b0;
-    partials[4 * blockIdx.x + 1] = b1;
-    partials[4 * blockIdx.x + 2] = c0;
-    partials[4 * blockIdx.x + 3] = c1;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last || threadIdx.x != 0) return;
-  __threadfence();
-  double t[4] = {0.0, 0.0, 0.0, 0.0};
-  for (unsigned k = 0; k < gridDim.x; k++)
-    for (int q = 0; q < 4; q++) t[q] += (double)__ldcg(&partials[4 * k + q]);
+  double t[4];
+  if (!last_block_sums<4>(acc, partials, counter, t) || threadIdx.x != 0) return;
   const bool learned_ok = t[1] > 0.0 && isfinite(t[1]) && isfinite(t[0]);
   if (learned_ok) {
     s->beta = t[0] / s->rz;
@@ -322,7 +269,6 @@ __global__ void __launch_bounds__(256) k_fcg_beta(int64_t n, const float* __rest
     s->rz = t[3];
     s->pq = -1.0;
   }
-  *counter = 0u;
 }
 
 __global__ void k_fcg_dir(int64_t n, const float* __restrict__ z, const float* __restrict__ r,

@@ -54,6 +54,60 @@ __device__ __forceinline__ float warp_sumf(float v) {
   return v;
 }
 
+__device__ __forceinline__ double warp_sumd(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sums of K values into partials[k * gridDim.x + blockIdx.x]; the last block to finish
+// adds them in a fixed order (thread t takes blocks t, t + 256, ... in FP64, then a fixed
+// shuffle tree) and returns true with tot[] valid in its thread 0.  256 threads per block.
+template <int K>
+__device__ __forceinline__ bool last_block_sums(float (&v)[K], float* partials, unsigned* counter, double (&tot)[K]) {
+  __shared__ float sm[K][8];
+  __shared__ double sd[K][8];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const float a = warp_sumf(v[k]);
+    if (lane == 0) sm[k][w] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      float b = 0.f;
+      for (int q = 0; q < 8; q++) b += sm[k][q];
+      partials[k * gridDim.x + blockIdx.x] = b;
+    }
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double a = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) a += (double)__ldcg(&partials[k * gridDim.x + b]);
+    a = warp_sumd(a);
+    if (lane == 0) sd[k][w] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      double a = 0.0;
+      for (int q = 0; q < 8; q++) a += sd[k][q];
+      tot[k] = a;
+    }
+    *counter = 0u;
+  }
+  return true;
+}
+
 // ---- encoder: x = v * D^-1/2, h0 = We x; one warp per node, lane l computes outputs 2l, 2l+1 ----
 __global__ void __launch_bounds__(256) k_gnn_encode(int64_t n, const float* __restrict__ v,
                                                     const float* __restrict__ dinv,
@@ -357,31 +411,13 @@ __global__ void __launch_bounds__(256) k_gnn_cgrad(int64_t n3, const float* __re
                                                    const float* __restrict__ r, const float* __restrict__ dinv,
                                                    const float* __restrict__ params, float* __restrict__ partials,
                                                    unsigned* counter, float* __restrict__ grad, int accumulate) {
-  float acc = 0.f;
+  float acc[1] = {0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x)
-    acc += Go[i] * dinv[i] * r[i];
-  __shared__ float sm[8];
-  __shared__ bool last;
-  acc = warp_sumf(acc);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float b = 0.f;
-    for (int w = 0; w < 8; w++) b += sm[w];
-    partials[blockIdx.x] = b;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    double t = 0.0;
-    for (unsigned b = 0; b < gridDim.x; b++) t += (double)__ldcg(&partials[b]);
-    const float v = (float)(t * (double)expf(params[OFF_C]));
-    grad[OFF_C] = accumulate ? grad[OFF_C] + v : v;
-    *counter = 0u;
-  }
+    acc[0] += Go[i] * dinv[i] * r[i];
+  double t[1];
+  if (!last_block_sums<1>(acc, partials, counter, t) || threadIdx.x != 0) return;
+  const float v = (float)(t[0] * (double)expf(params[OFF_C]));
+  grad[OFF_C] = accumulate ? grad[OFF_C] + v : v;
 }
 
 // loss of one sample in the energy norm:  d = M(r) - e,  q = K d,
@@ -389,32 +425,13 @@ __global__ void __launch_bounds__(256) k_gnn_cgrad(int64_t n3, const float* __re
 __global__ void __launch_bounds__(256) k_gnn_loss(int64_t n3, const float* __restrict__ d, const float* __restrict__ q,
                                                   float inv_c, float* __restrict__ Go, float* __restrict__ partials,
                                                   unsigned* counter, float* loss) {
-  float acc = 0.f;
+  float acc[1] = {0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
-    acc += d[i] * q[i];
+    acc[0] += d[i] * q[i];
     Go[i] = 2.f * q[i] * inv_c;
   }
-  __shared__ float sm[8];
-  __shared__ bool last;
-  acc = warp_sumf(acc);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float b = 0.f;
-    for (int w = 0; w < 8; w++) b += sm[w];
-    partials[blockIdx.x] = b;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    double t = 0.0;
-    for (unsigned b = 0; b < gridDim.x; b++) t += (double)__ldcg(&partials[b]);
-    *loss = (float)(t * inv_c);
-    *counter = 0u;
-  }
+  double t[1];
+  if (last_block_sums<1>(acc, partials, counter, t) && threadIdx.x == 0) *loss = (float)(t[0] * inv_c);
 }
 
 // Adam on the FP32 master parameters
@@ -612,74 +629,97 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_inf(Graph g, const __nv_bfloat
 // ======================= inference through the folded polynomial =======================
 // y_{k+1} = A y_k (mean over neighbours), y_0 = x = D^-1/2 r; then w_j = sum_k y_k G[k][j]
 // and M(r) = D^-1/2 (c x + w_0 + A^T (w_1 + A^T (w_2 + A^T w_3)))   (Horner in A^T).
-// Six passes over 3-vectors, one thread per node, fixed-order neighbour sums.
+// Six passes over 3-vectors.  Half a warp per node: its 16 lanes load neighbours e, e + 16,
+// ... in parallel and a fixed shuffle tree adds them (deterministic).
+
+__device__ __forceinline__ float half_sum(float v) {  // over the 16 lanes of a half warp
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// sum over the neighbours j of node of wgt_j * v_j (3-vectors); every lane of the half warp
+// returns the total.  FIRST: v_j = r_j D_j^-1/2; TRANS: wgt_j = 1 / deg_j, else 1.
+template <bool FIRST, bool TRANS>
+__device__ __forceinline__ void half_gather(const Graph& g, int64_t node, bool valid, int l16,
+                                            const float* __restrict__ r, const float* __restrict__ dinv,
+                                            const float* __restrict__ v, float (&a)[3]) {
+  a[0] = a[1] = a[2] = 0.f;
+  int p0 = 0, deg = 0;
+  if (valid) {
+    p0 = g.ptr[node];
+    deg = g.ptr[node + 1] - p0;
+  }
+  for (int e = l16; e < deg; e += 16) {
+    const int jn = g.idx[p0 + e];
+    const int64_t j = 3 * (int64_t)jn;
+    const float wgt = TRANS ? g.inv_deg[jn] : 1.f;
+    if (FIRST) {
+      a[0] += r[j] * sqrtf(dinv[j]);
+      a[1] += r[j + 1] * sqrtf(dinv[j + 1]);
+      a[2] += r[j + 2] * sqrtf(dinv[j + 2]);
+    } else {
+      a[0] += wgt * v[j];
+      a[1] += wgt * v[j + 1];
+      a[2] += wgt * v[j + 2];
+    }
+  }
+  a[0] = half_sum(a[0]);
+  a[1] = half_sum(a[1]);
+  a[2] = half_sum(a[2]);
+}
+
 template <bool FIRST>
 __global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float* __restrict__ r,
                                                   const float* __restrict__ dinv, const float* __restrict__ yin,
                                                   float* __restrict__ yout, const int* done) {
   if (done && *done) return;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    const int e1 = g.ptr[i + 1];
-    for (int e = g.ptr[i]; e < e1; e++) {
-      const int64_t j = 3 * (int64_t)g.idx[e];
-      if (FIRST) {
-        a0 += r[j] * sqrtf(dinv[j]);
-        a1 += r[j + 1] * sqrtf(dinv[j + 1]);
-        a2 += r[j + 2] * sqrtf(dinv[j + 2]);
-      } else {
-        a0 += yin[j];
-        a1 += yin[j + 1];
-        a2 += yin[j + 2];
-      }
-    }
-    const float id = g.inv_deg[i];
-    yout[3 * i] = a0 * id;
-    yout[3 * i + 1] = a1 * id;
-    yout[3 * i + 2] = a2 * id;
+  const int lane = threadIdx.x & 31, l16 = lane & 15;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = warp; 2 * k < g.n; k += nwarps) {
+    const int64_t node = 2 * k + (lane >> 4);
+    const bool valid = node < g.n;
+    float a[3];
+    half_gather<FIRST, false>(g, node, valid, l16, r, dinv, yin, a);
+    if (valid && l16 < 3) yout[3 * node + l16] = (l16 == 0 ? a[0] : l16 == 1 ? a[1] : a[2]) * g.inv_deg[node];
   }
 }
 
-// y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of 3n)
+// y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of 3n);
+// lane t < 12 of the half warp writes w_{t/3}[t%3]
 __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restrict__ r,
                                                   const float* __restrict__ dinv, const float* __restrict__ y1,
                                                   const float* __restrict__ y2, PolyCoef pc, float* __restrict__ w,
                                                   const int* done) {
   if (done && *done) return;
+  const int lane = threadIdx.x & 31, l16 = lane & 15;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t n3 = 3 * g.n;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t k = warp; 2 * k < g.n; k += nwarps) {
+    const int64_t node = 2 * k + (lane >> 4);
+    const bool valid = node < g.n;
+    float a[3];
+    half_gather<false, false>(g, node, valid, l16, r, dinv, y2, a);
+    if (!valid || l16 >= 12) continue;
+    const int64_t o = 3 * node;
+    const float id = g.inv_deg[node];
     float y[NL + 1][3];
-    const int64_t o = 3 * i;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       y[0][c] = r[o + c] * sqrtf(dinv[o + c]);
       y[1][c] = y1[o + c];
       y[2][c] = y2[o + c];
-      y[3][c] = 0.f;
+      y[3][c] = a[c] * id;
     }
-    const int e1 = g.ptr[i + 1];
-    for (int e = g.ptr[i]; e < e1; e++) {
-      const int64_t j = 3 * (int64_t)g.idx[e];
-      y[3][0] += y2[j];
-      y[3][1] += y2[j + 1];
-      y[3][2] += y2[j + 2];
-    }
-    const float id = g.inv_deg[i];
-    y[3][0] *= id;
-    y[3][1] *= id;
-    y[3][2] *= id;
+    const int jj = l16 / 3, c = l16 % 3;
+    float acc = 0.f;
 #pragma unroll
-    for (int jj = 0; jj <= NL; jj++) {
+    for (int kk = 0; kk <= NL; kk++)
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        float a = 0.f;
-#pragma unroll
-        for (int k = 0; k <= NL; k++)
-#pragma unroll
-          for (int b = 0; b < 3; b++) a += y[k][b] * pc.G[k][jj][3 * b + c];
-        w[jj * n3 + o + c] = a;
-      }
-    }
+      for (int b = 0; b < 3; b++) acc += y[kk][b] * pc.G[kk][jj][3 * b + c];
+    w[jj * n3 + o + c] = acc;
   }
 }
 
@@ -690,27 +730,22 @@ __global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const float* __restri
                                                   const float* __restrict__ dinv, float cc, float* __restrict__ out,
                                                   const int* done) {
   if (done && *done) return;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    const int e1 = g.ptr[i + 1];
-    for (int e = g.ptr[i]; e < e1; e++) {
-      const int jn = g.idx[e];
-      const float wj = g.inv_deg[jn];
-      const int64_t j = 3 * (int64_t)jn;
-      a0 += wj * uin[j];
-      a1 += wj * uin[j + 1];
-      a2 += wj * uin[j + 2];
-    }
-    const int64_t o = 3 * i;
-    const float v[3] = {a0 + wadd[o], a1 + wadd[o + 1], a2 + wadd[o + 2]};
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      if (LAST) {
-        const float d = dinv[o + c];
-        out[o + c] = cc * d * r[o + c] + sqrtf(d) * v[c];
-      } else {
-        out[o + c] = v[c];
-      }
+  const int lane = threadIdx.x & 31, l16 = lane & 15;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = warp; 2 * k < g.n; k += nwarps) {
+    const int64_t node = 2 * k + (lane >> 4);
+    const bool valid = node < g.n;
+    float a[3];
+    half_gather<false, true>(g, node, valid, l16, r, dinv, uin, a);
+    if (!valid || l16 >= 3) continue;
+    const int64_t i = 3 * node + l16;
+    const float v = (l16 == 0 ? a[0] : l16 == 1 ? a[1] : a[2]) + wadd[i];
+    if (LAST) {
+      const float d = dinv[i];
+      out[i] = cc * d * r[i] + sqrtf(d) * v;
+    } else {
+      out[i] = v;
     }
   }
 }

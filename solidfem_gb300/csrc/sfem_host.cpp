@@ -108,6 +108,12 @@ struct sfem_handle {
   std::vector<int32_t> inst_its;
   // node data (reshuffled, 3N)
   double *x0 = nullptr, *u = nullptr, *mass = nullptr, *fext = nullptr, *grav_d = nullptr;
+  // dynamics (FemPhysicsMatrixFree mTimeStep, node vel, pos0 at the step start)
+  double dt = 0.0;  // 0: static
+  double *vel = nullptr, *ustart = nullptr;
+  double* pm64 = nullptr;  // per patch-node slot mass share / h^2 (implicit dynamics)
+  float* pm32 = nullptr;
+  DynView dyn() const { return DynView{vel, ustart, 1.0 / dt, 1.0 / (dt * dt)}; }
   int64_t *csr_ptr = nullptr, *csr_ent = nullptr;
   // element patches (elements are stored in patch order; perm maps to the caller's order)
   std::vector<int32_t> perm_h;
@@ -151,8 +157,10 @@ struct sfem_handle {
   PatchBoundary pb() const { return PatchBoundary{n_shared, bnode, bptr}; }
   template <typename T>
   PatchView<T> pv(const T* X, const T* vol, const T* scale, const T* scale_la, T m, T l) const {
+    const T* pm = nullptr;
+    if (dt > 0) pm = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)pm64 : (const void*)pm32);
     return PatchView<T>{elem_off, node_off, pnode, pdest, lptr, lent, lidx, X, vol, scale, scale_la, E, n_patches,
-                        nbc, m, l};
+                        nbc, m, l, pm};
   }
   NodeCsr csr() const { return NodeCsr{csr_ptr, csr_ent}; }
   ElemView<double> ev64() const {
@@ -252,8 +260,9 @@ int residual(sfem_handle* h, double* rnorm, int* n_inverted) {
   element_pass<double>(h, MODE_FORCE, h->u, nullptr, h->fe, nullptr, h->ninv, nullptr);
   const PressureView pv = h->pres();
   if (h->n_tris > 0) launch_pressure_tris(pv, h->x0, h->u, h->ff, h->stream);
+  const DynView dv = h->dyn();
   launch_gather_force(h->nbc, h->N, h->csr(), h->fe, h->mass, h->fext, h->grav, h->ff, h->r64, h->red(),
-                      h->dres, h->stream, h->n_tris > 0 ? &pv : nullptr);
+                      h->dres, h->stream, h->n_tris > 0 ? &pv : nullptr, h->dt > 0 ? &dv : nullptr, h->u);
   CU(cudaMemcpyAsync(h->dres_h, h->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   int ninv_h = 0;
   CU(cudaMemcpyAsync(&ninv_h, h->ninv, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -269,7 +278,8 @@ int jacobi(sfem_handle* h, T* dinv, T* diag) {
   const T* u = disp<T>(h);
   T* fe = reinterpret_cast<T*>(h->fe);
   element_pass<T>(h, MODE_DIAG, u, nullptr, fe, nullptr, nullptr, nullptr);
-  launch_gather_diag<T>(h->nbc, h->N, h->csr(), fe, dinv, diag, h->stream);
+  launch_gather_diag<T>(h->nbc, h->N, h->csr(), fe, dinv, diag, h->stream, h->dt > 0 ? h->mass : nullptr,
+                        h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0);
   CU(cudaGetLastError());
   return 0;
 }
@@ -653,6 +663,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   if ((st = dalloc(&h->tets, E)) || (st = dalloc(&h->X64, 9 * E)) || (st = dalloc(&h->vol64, E)) ||
       (st = dalloc(&h->X32, 9 * E)) || (st = dalloc(&h->vol32, E)) || (st = dalloc(&h->x0, N3)) ||
       (st = dalloc(&h->u, N3)) || (st = dalloc(&h->mass, (size_t)n_nodes)) || (st = dalloc(&h->fext, N3)) ||
+      (st = dalloc(&h->vel, N3)) || (st = dalloc(&h->ustart, N3)) ||
       (st = dalloc(&h->grav_d, 3)) || (st = dalloc(&h->csr_ptr, (size_t)n_nodes + 1)) ||
       (st = dalloc(&h->csr_ent, 4 * E)) || (st = dalloc(&h->fe, 12 * E)) ||
       (st = dalloc(&h->partials, std::max<size_t>(4 * (size_t)kMaxBlocks, (size_t)h->n_patches + kMaxBlocks))) ||
@@ -701,7 +712,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   for (size_t i = 0; i < pbld.bnode.size(); i++) bidx_h[pbld.bnode[i]] = (int32_t)i;
   UP(h->bidx, bidx_h.data(), bidx_h.size() * sizeof(int32_t));
 #undef UP
-  double* zero_bufs[] = {h->u, h->fext, h->r64, h->ubase, h->tmp64, h->tmp64b};
+  double* zero_bufs[] = {h->u, h->fext, h->r64, h->ubase, h->tmp64, h->tmp64b, h->vel, h->ustart};
   for (double* z : zero_bufs)
     if (cudaMemsetAsync(z, 0, N3 * sizeof(double), s) != cudaSuccess) return bail(fail(SFEM_ERR_CUDA, "memset failed"));
   if (cudaMemsetAsync(h->counter, 0, sizeof(unsigned), s) != cudaSuccess) return bail(fail(SFEM_ERR_CUDA, "memset failed"));
@@ -719,7 +730,7 @@ int sfem_destroy(sfem_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
-                   h->ptf};
+                   h->ptf, h->vel, h->ustart, h->pm64, h->pm32};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
@@ -805,6 +816,119 @@ int sfem_set_stream(sfem_handle* h, void* stream) {
   h->own_stream = false;
   h->stream = (cudaStream_t)stream;
   return SFEM_OK;
+}
+
+// ---- dynamics (FemPhysicsMatrixFree::Step :297-324, SubStep :371-387, Solve :589-597) ----
+int sfem_set_time_step(sfem_handle* h, double dt) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!(dt >= 0.0) || !std::isfinite(dt)) return fail(SFEM_ERR_INVALID, "time step must be finite and >= 0");
+  h->dt = dt;
+  if (dt == 0.0) return SFEM_OK;
+  if (!h->pm64) TRY(dalloc(&h->pm64, (size_t)h->n_slots));
+  if (h->precision == SFEM_FP32 && !h->pm32) TRY(dalloc(&h->pm32, (size_t)h->n_slots));
+  const double inv_h2 = 1.0 / (dt * dt);
+  launch_patch_mass<double>(h->n_slots, h->nbc, h->pnode, h->bidx, h->pb(), h->mass, inv_h2, h->pm64, h->stream);
+  if (h->pm32)
+    launch_patch_mass<float>(h->n_slots, h->nbc, h->pnode, h->bidx, h->pb(), h->mass, inv_h2, h->pm32, h->stream);
+  return sync(h);
+}
+
+int sfem_get_time_step(sfem_handle* h, double* dt) {
+  TRY(check_handle(h));
+  if (!dt) return fail(SFEM_ERR_INVALID, "null");
+  *dt = h->dt;
+  return SFEM_OK;
+}
+
+static int node_vec_io(sfem_handle* h, double* dev, const double* in, double* out) {
+  const size_t N3 = 3 * (size_t)h->N;
+  std::vector<double> t(N3, 0.0);
+  if (in) {
+    for (int64_t i = 0; i < h->N; i++)
+      for (int c = 0; c < 3; c++) t[3 * (size_t)h->map[i] + c] = in[3 * (size_t)i + c];
+    for (size_t k = 0; k < 3 * (size_t)h->nbc; k++) t[k] = 0.0;  // fixed nodes do not move
+    CU(cudaMemcpyAsync(dev, t.data(), N3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+  }
+  CU(cudaMemcpyAsync(t.data(), dev, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  for (int64_t i = 0; i < h->N; i++)
+    for (int c = 0; c < 3; c++) out[3 * (size_t)i + c] = t[3 * (size_t)h->map[i] + c];
+  return SFEM_OK;
+}
+
+int sfem_set_velocities(sfem_handle* h, const double* vel) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!vel) return fail(SFEM_ERR_INVALID, "null");
+  return node_vec_io(h, h->vel, vel, nullptr);
+}
+
+int sfem_get_velocities(sfem_handle* h, double* vel) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!vel) return fail(SFEM_ERR_INVALID, "null");
+  return node_vec_io(h, h->vel, nullptr, vel);
+}
+
+int sfem_begin_step(sfem_handle* h) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  CU(cudaMemcpyAsync(h->ustart, h->u, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  return sync(h);
+}
+
+int sfem_step(sfem_handle* h, double dt, int32_t sim_type, int32_t substeps, const sfem_newton_opts* opts,
+              sfem_newton_stats* stats) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (substeps < 1) return fail(SFEM_ERR_INVALID, "substeps must be >= 1");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(SFEM_ERR_INVALID, "dt must be finite and > 0");
+  const double hs = dt / substeps;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (sim_type == SFEM_SIM_EXPLICIT) {
+    // internal forces only (no gravity scaling, no loads), then symplectic Euler with h g
+    const double ff = h->ff;
+    const double dt_keep = h->dt;
+    for (int i = 0; i < substeps; i++) {
+      CU(cudaMemsetAsync(h->ninv, 0, sizeof(int), h->stream));
+      element_pass<double>(h, MODE_FORCE, h->u, nullptr, h->fe, nullptr, h->ninv, nullptr);
+      h->dt = 0.0;
+      launch_gather_force(h->nbc, h->N, h->csr(), h->fe, h->mass, h->fext, h->grav, 0.0, h->r64, h->red(), nullptr,
+                          h->stream);
+      h->dt = dt_keep;
+      launch_explicit_substep(h->nbc, h->N, h->r64, h->mass, h->grav, hs, h->vel, h->u, h->stream);
+    }
+    h->ff = ff;
+    CU(cudaGetLastError());
+    return sync(h);
+  }
+  if (sim_type != SFEM_SIM_IMPLICIT) return fail(SFEM_ERR_INVALID, "sim_type is SFEM_SIM_EXPLICIT or SFEM_SIM_IMPLICIT");
+  if (!opts) return fail(SFEM_ERR_INVALID, "opts is null");
+  // positions at the start of the step (the reference overwrites pos0 once per Step)
+  TRY(sfem_begin_step(h));
+  TRY(sfem_set_time_step(h, hs));
+  h->ff = 1.0;
+  int worst = SFEM_OK;
+  for (int i = 0; i < substeps; i++) {
+    sfem_newton_stats st{};
+    const int rc = sfem_newton_solve(h, opts, &st);
+    if (rc < 0) return rc;
+    if (rc > worst) worst = rc;
+    launch_velocity_update(h->nbc, h->N, h->u, h->ustart, 1.0 / hs, h->vel, h->stream);
+    if (stats) {
+      stats->newton_iters += st.newton_iters;
+      stats->cg_iters += st.cg_iters;
+      stats->line_search_cuts += st.line_search_cuts;
+      stats->status = st.status > stats->status ? st.status : stats->status;
+      stats->r0 = i == 0 ? st.r0 : stats->r0;
+      stats->rel_res = st.rel_res;
+      stats->seconds += st.seconds;
+    }
+  }
+  TRY(sync(h));
+  return worst;
 }
 
 int sfem_get_positions(sfem_handle* h, double* pos) {
@@ -1125,7 +1249,9 @@ int sfem_energy(sfem_handle* h, double* elastic, double* total) {
   TRY(check_handle(h));
   TRY(set_device(h));
   element_pass<double>(h, MODE_ENERGY, h->u, nullptr, h->fe, h->dres, nullptr, nullptr);
-  launch_potential(h->nbc, h->N, h->x0, h->u, h->mass, h->fext, h->grav, h->ff, h->red(), h->dres + 1, h->stream);
+  const DynView dv = h->dyn();
+  launch_potential(h->nbc, h->N, h->x0, h->u, h->mass, h->fext, h->grav, h->ff, h->red(), h->dres + 1, h->stream,
+                   h->dt > 0 ? &dv : nullptr);
   CU(cudaMemcpyAsync(h->dres_h, h->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
   if (elastic) *elastic = h->dres_h[0];

@@ -86,6 +86,15 @@ struct PatchView {
   int64_t n_patches;
   int64_t nbc;
   T mu, lambda;
+  const T* pm;  // implicit dynamics: per slot m_g / (h^2 * patches sharing g), else nullptr
+};
+
+// Implicit-dynamics terms of the residual (FemPhysicsMatrixFree::ComputeGradients :546-557):
+// r += (m/h) v - (m/h^2) (x - x_start); vel == nullptr for static solves
+struct DynView {
+  const double* vel;      // 3N, reshuffled
+  const double* u_start;  // displacement at the start of the step, 3N
+  double inv_h, inv_h2;
 };
 
 struct PatchBoundary {
@@ -148,13 +157,14 @@ struct PressureView {
 void launch_pressure_tris(PressureView pv, const double* x0, const double* u, double ff, cudaStream_t st);
 void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
                          const double* fext, const double* grav, double ff, double* r, Reduce red,
-                         double* rr_out, cudaStream_t st, const PressureView* pv = nullptr);
+                         double* rr_out, cudaStream_t st, const PressureView* pv = nullptr,
+                         const DynView* dv = nullptr, const double* u = nullptr);
 template <typename T>
 void launch_gather_hvp(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, const T* p, T* q, Reduce red,
                        CgScalars* s, cudaStream_t st);
 template <typename T>
 void launch_gather_diag(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, T* dinv, T* diag,
-                        cudaStream_t st);
+                        cudaStream_t st, const double* mass = nullptr, double inv_h2 = 0.0);
 // per-element forces of the FP64 force pass in element-major 12-vectors are
 // reused by the adjoint: g_e = sum_a lam_a . f_a / E_e
 void launch_adjoint_elem(const int4* tets, int64_t E, int64_t nbc, const double* fe, const double* lam,
@@ -182,7 +192,17 @@ void launch_segment_mask(int k, const int64_t* seg, const int32_t* active, T* v,
 void launch_dot(int64_t n, const double* a, const double* b, Reduce red, double* out, cudaStream_t st);
 void launch_potential(int64_t nbc, int64_t N, const double* x0, const double* u, const double* mass,
                       const double* fext, const double* grav, double ff, Reduce red, double* out,
-                      cudaStream_t st);
+                      cudaStream_t st, const DynView* dv = nullptr);
+// implicit dynamics: per patch-node slot mass share m_g / (h^2 k_g) (k_g patches touch g)
+template <typename T>
+void launch_patch_mass(int64_t n_slots, int64_t nbc, const int32_t* pnode, const int32_t* bidx, PatchBoundary pb,
+                       const double* mass, double inv_h2, T* pm, cudaStream_t st);
+// explicit substep (FemPhysicsMatrixFree::SubStep :371-387): v += (h/m) f + h g, u += h v
+void launch_explicit_substep(int64_t nbc, int64_t N, const double* f, const double* mass, const double* grav,
+                             double hs, double* vel, double* u, cudaStream_t st);
+// implicit step end (FemPhysicsMatrixFree::Solve :589-597): v = (u - u_start) / h
+void launch_velocity_update(int64_t nbc, int64_t N, const double* u, const double* u_start, double inv_h,
+                            double* vel, cudaStream_t st);
 template <typename Tin, typename Tout>
 void launch_convert(int64_t n, const Tin* a, Tout* b, cudaStream_t st);
 // x = x + a * d   (FP64 state += precision-T direction)

@@ -723,7 +723,8 @@ __global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t 
                                                            const double* __restrict__ mass,
                                                            const double* __restrict__ fext, double g0, double g1,
                                                            double g2, double ff, double* __restrict__ r,
-                                                           Reduce red, double* rr_out, PressureView pv) {
+                                                           Reduce red, double* rr_out, PressureView pv, DynView dv,
+                                                           const double* __restrict__ u) {
   double acc = 0.0;
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     double f[3];
@@ -741,6 +742,10 @@ __global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t 
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       double v = f[c] + mf * gr[c];
+      if (dv.vel) {
+        v += (mass[g] * dv.inv_h) * dv.vel[3 * g + c];
+        v -= (mass[g] * dv.inv_h2) * (u[3 * g + c] - dv.u_start[3 * g + c]);
+      }
       v += ff * fext[3 * g + c];
       r[3 * g + c] = v;
       acc += v * v;
@@ -752,11 +757,12 @@ __global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t 
 
 void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
                          const double* fext, const double* grav, double ff, double* r, Reduce red, double* rr_out,
-                         cudaStream_t st, const PressureView* pv) {
+                         cudaStream_t st, const PressureView* pv, const DynView* dv, const double* u) {
   count_launch();
   PressureView none{0, nullptr, nullptr, nullptr, nullptr, 0.0};
+  DynView nodyn{nullptr, nullptr, 0.0, 0.0};
   k_gather_force<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, mass, fext, grav[0], grav[1], grav[2], ff,
-                                                        r, red, rr_out, pv ? *pv : none);
+                                                        r, red, rr_out, pv ? *pv : none, dv ? *dv : nodyn, u);
 }
 
 template <typename T>
@@ -808,10 +814,17 @@ template void launch_gather_hvp<float>(int64_t, int64_t, NodeCsr, const float*, 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_gather_diag(int64_t nbc, int64_t N, NodeCsr csr,
                                                           const T* __restrict__ fe, T* __restrict__ dinv,
-                                                          T* __restrict__ diag) {
+                                                          T* __restrict__ diag, const double* __restrict__ mass,
+                                                          double inv_h2) {
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     T f[3];
     gather_node(csr, fe, g, f);
+    if (mass) {
+      const T m = (T)(mass[g] * inv_h2);
+      f[0] += m;
+      f[1] += m;
+      f[2] += m;
+    }
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       if (diag) diag[3 * g + c] = f[c];
@@ -821,12 +834,15 @@ __global__ void __launch_bounds__(kThreads) k_gather_diag(int64_t nbc, int64_t N
 }
 
 template <typename T>
-void launch_gather_diag(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, T* dinv, T* diag, cudaStream_t st) {
+void launch_gather_diag(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, T* dinv, T* diag, cudaStream_t st,
+                        const double* mass, double inv_h2) {
   count_launch();
-  k_gather_diag<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, dinv, diag);
+  k_gather_diag<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, dinv, diag, mass, inv_h2);
 }
-template void launch_gather_diag<double>(int64_t, int64_t, NodeCsr, const double*, double*, double*, cudaStream_t);
-template void launch_gather_diag<float>(int64_t, int64_t, NodeCsr, const float*, float*, float*, cudaStream_t);
+template void launch_gather_diag<double>(int64_t, int64_t, NodeCsr, const double*, double*, double*, cudaStream_t,
+                                         const double*, double);
+template void launch_gather_diag<float>(int64_t, int64_t, NodeCsr, const float*, float*, float*, cudaStream_t,
+                                        const double*, double);
 
 __global__ void __launch_bounds__(kThreads) k_adjoint_elem(const int4* __restrict__ tets, int64_t E, int64_t nbc,
                                                            const double* __restrict__ fe,
@@ -981,6 +997,12 @@ __global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __re
       f0 += src[0];
       f1 += src[1];
       f2 += src[2];
+    }
+    if (pv.pm) {  // implicit dynamics: q = K p + (m / h^2) p (shared nodes: a share per patch)
+      const T m = pv.pm[nb + j];
+      f0 -= m * sp[3 * j];
+      f1 -= m * sp[3 * j + 1];
+      f2 -= m * sp[3 * j + 2];
     }
     const int g = pv.pnode[nb + j];
     int64_t o = -1;
@@ -1322,7 +1344,7 @@ __global__ void __launch_bounds__(kThreads) k_potential(int64_t nbc, int64_t N, 
                                                         const double* __restrict__ u,
                                                         const double* __restrict__ mass,
                                                         const double* __restrict__ fext, double g0, double g1,
-                                                        double g2, double ff, Reduce red, double* out) {
+                                                        double g2, double ff, Reduce red, double* out, DynView dv) {
   double acc = 0.0;
   const double gr[3] = {g0, g1, g2};
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
@@ -1330,16 +1352,83 @@ __global__ void __launch_bounds__(kThreads) k_potential(int64_t nbc, int64_t N, 
     for (int c = 0; c < 3; c++) {
       const double x = x0[3 * g + c] + u[3 * g + c];
       acc -= ff * (mass[g] * gr[c] + fext[3 * g + c]) * x;
+      if (dv.vel) {  // inertia of backward Euler: m / (2 h^2) |x - x_start - h v|^2
+        const double d = u[3 * g + c] - dv.u_start[3 * g + c] - dv.vel[3 * g + c] / dv.inv_h;
+        acc += 0.5 * mass[g] * dv.inv_h2 * d * d;
+      }
     }
   }
   double v[1] = {acc}, tot[1];
   if (reduce_last<double, 1>(v, red, tot) && threadIdx.x == 0) *out = tot[0];
 }
 void launch_potential(int64_t nbc, int64_t N, const double* x0, const double* u, const double* mass,
-                      const double* fext, const double* grav, double ff, Reduce red, double* out, cudaStream_t st) {
+                      const double* fext, const double* grav, double ff, Reduce red, double* out, cudaStream_t st,
+                      const DynView* dv) {
   count_launch();
+  DynView nodyn{nullptr, nullptr, 0.0, 0.0};
   k_potential<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, x0, u, mass, fext, grav[0], grav[1], grav[2], ff, red,
-                                                     out);
+                                                     out, dv ? *dv : nodyn);
+}
+
+template <typename T>
+__global__ void k_patch_mass(int64_t n_slots, int64_t nbc, const int32_t* __restrict__ pnode,
+                             const int32_t* __restrict__ bidx, PatchBoundary pb, const double* __restrict__ mass,
+                             double inv_h2, T* __restrict__ pm) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_slots; s += (int64_t)gridDim.x * blockDim.x) {
+    int g = pnode[s];
+    const bool shared = g < 0;
+    if (shared) g = ~g;
+    double m = 0.0;
+    if (g >= nbc) {
+      m = mass[g] * inv_h2;
+      const int b = shared ? bidx[g] : -1;
+      if (b >= 0) m /= (double)(pb.ptr[b + 1] - pb.ptr[b]);
+    }
+    pm[s] = (T)m;
+  }
+}
+template <typename T>
+void launch_patch_mass(int64_t n_slots, int64_t nbc, const int32_t* pnode, const int32_t* bidx, PatchBoundary pb,
+                       const double* mass, double inv_h2, T* pm, cudaStream_t st) {
+  count_launch();
+  k_patch_mass<T><<<grid_for(n_slots), kThreads, 0, st>>>(n_slots, nbc, pnode, bidx, pb, mass, inv_h2, pm);
+}
+template void launch_patch_mass<double>(int64_t, int64_t, const int32_t*, const int32_t*, PatchBoundary,
+                                        const double*, double, double*, cudaStream_t);
+template void launch_patch_mass<float>(int64_t, int64_t, const int32_t*, const int32_t*, PatchBoundary,
+                                       const double*, double, float*, cudaStream_t);
+
+__global__ void k_explicit_substep(int64_t nbc, int64_t N, const double* __restrict__ f,
+                                   const double* __restrict__ mass, double g0, double g1, double g2, double hs,
+                                   double* __restrict__ vel, double* __restrict__ u) {
+  const double gr[3] = {g0, g1, g2};
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    if (mass[g] == 0.0) continue;
+    const double a = hs * (1.0 / mass[g]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const double v = vel[3 * g + c] + (a * f[3 * g + c] + hs * gr[c]);
+      vel[3 * g + c] = v;
+      u[3 * g + c] += hs * v;
+    }
+  }
+}
+void launch_explicit_substep(int64_t nbc, int64_t N, const double* f, const double* mass, const double* grav,
+                             double hs, double* vel, double* u, cudaStream_t st) {
+  count_launch();
+  k_explicit_substep<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, f, mass, grav[0], grav[1], grav[2], hs, vel, u);
+}
+
+__global__ void k_velocity_update(int64_t nbc, int64_t N, const double* __restrict__ u,
+                                  const double* __restrict__ us, double inv_h, double* __restrict__ vel) {
+  for (int64_t i = 3 * nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * N;
+       i += (int64_t)gridDim.x * blockDim.x)
+    vel[i] = inv_h * (u[i] - us[i]);
+}
+void launch_velocity_update(int64_t nbc, int64_t N, const double* u, const double* u_start, double inv_h,
+                            double* vel, cudaStream_t st) {
+  count_launch();
+  k_velocity_update<<<grid_for(3 * (N - nbc)), kThreads, 0, st>>>(nbc, N, u, u_start, inv_h, vel);
 }
 
 template <typename Tin, typename Tout>

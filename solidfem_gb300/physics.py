@@ -275,9 +275,42 @@ class FemPhysicsMatrixFree:
         return dict(status=code, newton_iters=st.newton_iters, cg_iters=st.cg_iters, r0=st.r0,
                     rel_res=st.rel_res, seconds=st.seconds, line_search_cuts=st.line_search_cuts)
 
-    def Step(self, dt=0.0, **newton_kw):
-        """Static step: FemPhysicsMatrixFree::Step(0) (Source/FemPhysicsMatrixFree.cpp:325-331)."""
-        return self.newton_solve(**newton_kw)
+    def Step(self, dt=0.0, simtype=0, substeps=1, **newton_kw):
+        """FemPhysicsMatrixFree::Step (Source/FemPhysicsMatrixFree.cpp:297-342): static
+        (simtype 0/1: the Newton solve), explicit (2: symplectic Euler substeps on the elastic
+        forces and gravity) or implicit (3: backward Euler, a Newton solve per substep)."""
+        if simtype in (0, 1) or dt == 0:
+            return self.newton_solve(**newton_kw)
+        if simtype == nat.SIM_EXPLICIT:
+            nat.check(self._lib.sfem_step(self._h, float(dt), nat.SIM_EXPLICIT, int(substeps), None, None))
+            return dict(status=0)
+        kw = dict(rel_tol=1e-8, abs_tol=0.0, max_newton=50, max_cg=100000, precond=nat.PC_JACOBI,
+                  ls_condition=nat.LSC_RESIDUAL if self.material == nat.MMT_COROTATIONAL else nat.LSC_ARMIJO,
+                  eta_max=0.5, eta_min=0.0, load_steps=1, verbose=0, max_bisection=0)
+        kw.update(newton_kw)
+        o = nat.NewtonOpts(**kw)
+        st = nat.NewtonStats()
+        code = nat.check(self._lib.sfem_step(self._h, float(dt), nat.SIM_IMPLICIT, int(substeps), C.byref(o),
+                                             C.byref(st)))
+        return dict(status=code, newton_iters=st.newton_iters, cg_iters=st.cg_iters, r0=st.r0, rel_res=st.rel_res,
+                    seconds=st.seconds, line_search_cuts=st.line_search_cuts)
+
+    def set_time_step(self, dt):
+        """mTimeStep: 0 for static, h > 0 adds the backward-Euler inertia terms."""
+        nat.check(self._lib.sfem_set_time_step(self._h, float(dt)))
+
+    def set_velocities(self, vel):
+        v = _f64(vel).reshape(-1, 3)
+        nat.check(self._lib.sfem_set_velocities(self._h, _dp(v)))
+
+    def get_velocities(self):
+        v = np.zeros((self.n_nodes, 3))
+        nat.check(self._lib.sfem_get_velocities(self._h, _dp(v)))
+        return v
+
+    def begin_step(self):
+        """x_start = x (the reference's pos0 = pos at the start of an implicit Step)."""
+        nat.check(self._lib.sfem_begin_step(self._h))
 
     def nonlinear_cg(self, outer_iters=200, inner_iters=10, abs_tol=1e-4):
         it = C.c_int32()

@@ -40,8 +40,6 @@ class NonlinearFEM:
             mat = _MATERIALS[mat.lower()]
         gravity = cfg.get("gravity", -9.8)
         self.simtype = int(cfg.get("simtype", ST_STATIC))
-        if self.simtype in (ST_EXPLICIT, ST_IMPLICIT):
-            raise NotImplementedError("dynamic simulation types are outside the static matrix-free path")
         self.substeps = int(cfg.get("substeps", 1))
         self.maxiter = int(cfg.get("maxiter", 10))  # FemConfig::mOuterIterations default
         self.tol = float(cfg.get("tol", 0.1))  # FemConfig::mAbsNewtonRsidualThreshold default
@@ -70,6 +68,15 @@ class NonlinearFEM:
             if self.force_fraction < 1:
                 self.force_fraction = min(1.0, self.force_fraction + self.force_step)
                 self._solve()
+        elif self.simtype == ST_EXPLICIT:
+            self.phys.Step(dt, simtype=ST_EXPLICIT, substeps=self.substeps)
+        elif self.simtype == ST_IMPLICIT:
+            self.force_fraction = 1.0
+            self.phys.set_force_fraction(1.0)
+            lsc = nat.LSC_ARMIJO if self.optimizer else nat.LSC_ENGINEERING
+            self.last_stats = self.phys.Step(dt, simtype=ST_IMPLICIT, substeps=self.substeps, rel_tol=self.newton_rtol,
+                                             abs_tol=self.tol, max_newton=self.maxiter, precond=self.precond,
+                                             ls_condition=lsc, eta_min=1e-10)
 
     def simulate_static(self):
         while self.force_fraction < 1:

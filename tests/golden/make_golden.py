@@ -17,6 +17,12 @@ Fixtures (npz):
                      gravity -9.81 z, x=0 clamped: the reference's SolveNewtonLS equilibrium.
   c2s_<mat>.npz      8x2x2 box [0,8]x[0,2]x[0,2] (reduced C2), E=1e6 nu=0.4, 500 Pa -z traction
                      on x=8, x=0 clamped: equilibrium from reference assembly + Eigen SparseLU.
+  dyn_nh.npz         8x2x2 cantilever [0,2]x[0,0.5]x[0,0.5], neo-Hookean E=1e5 nu=0.45 rho=1070,
+                     gravity -9.81 z, x=0 clamped, from rest: the reference's own Step(dt):
+                     ST_EXPLICIT (dt 0.01, 10 substeps) x 3 and ST_IMPLICIT with SolveNewtonLS
+                     (dt 0.01, 1 substep) x 3 -> positions and velocities after each step.
+
+    python tests/golden/make_golden.py [--only dyn]
 """
 from __future__ import annotations
 
@@ -69,7 +75,36 @@ def element_outputs(ref, rng, perturb):
     return out
 
 
+def dynamics():
+    m = box_lattice(8, 2, 2, extent=(2.0, 0.5, 0.5))
+    fixed = m.face_nodes(0, 0)
+    out = dict(nodes=m.nodes, tets=m.tets, fixed=fixed, young=1e5, poisson=0.45, density=1070.0,
+               gravity=np.array([0.0, 0.0, -9.81]), material=3, dt=0.01, explicit_substeps=10, steps=3)
+    ref = RefHarness(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, -9.81, True, 3)
+    ref.set_sim(2, 10)  # ST_EXPLICIT, mNumSteps
+    xs, vs = [], []
+    for _ in range(3):
+        ref.step_dt(0.01)
+        xs.append(ref.positions())
+        vs.append(ref.velocities_shuffled()[ref.reshuffle_map()])
+    out.update(explicit_positions=np.array(xs), explicit_velocities=np.array(vs))
+    ref = RefHarness(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, -9.81, True, 3, solver=1, outer_iters=100,
+                     abs_tol=1e-11)
+    ref.set_sim(3, 1)  # ST_IMPLICIT, SolveNewtonLS per step
+    xs, vs = [], []
+    for _ in range(3):
+        ref.step_dt(0.01)
+        xs.append(ref.positions())
+        vs.append(ref.velocities_shuffled()[ref.reshuffle_map()])
+    out.update(implicit_positions=np.array(xs), implicit_velocities=np.array(vs))
+    np.savez_compressed(os.path.join(HERE, "dyn_nh.npz"), **out)
+    print("dyn: implicit tip after 3 steps", xs[-1][m.node_index(8, 2, 2)])
+
+
 def main():
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "dyn":
+        dynamics()
+        return
     if not os.path.isdir(REF):
         sys.exit("reference tree not present; fixtures are generated in the development container")
     rng = np.random.default_rng(20261203)
@@ -133,6 +168,7 @@ def main():
                             young=1e6, poisson=0.4, density=1070.0, gravity=np.zeros(3), material=mat, loads=fl,
                             eq_positions=ref.positions(), r0=r0, r_eq=rn, newton_iters=its)
         print(f"c2s {MATS[mat]}: its={its} |r0|={r0:.3e} |r|={rn:.3e}")
+    dynamics()
 
 
 if __name__ == "__main__":
