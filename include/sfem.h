@@ -226,6 +226,16 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
 int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max_cg,
                  double* dLdE, double* dLdf);
 
+/* ---- assembled tangent (ElasticEnergy::AssembleStiffnessMatrix, Source/ElasticEnergy.cpp:573-635;
+ * FemPhysicsMatrixFree::ComputeSystemMatrix :700-722 adds M/h^2 for implicit dynamics) ----
+ * Block CSR over the free nodes in the reshuffled free order (3 x 3 blocks, row-major), FP64,
+ * at the current state; the element blocks are the tangent's columns in closed form. */
+int sfem_tangent_nnz(sfem_handle* h, int64_t* nnzb);
+/* rowptr: n_free + 1, colidx: nnzb, vals: 9 nnzb */
+int sfem_assemble_tangent(sfem_handle* h, int32_t* rowptr, int32_t* colidx, double* vals);
+/* out = K d with the assembled tangent (checks against sfem_matvec) */
+int sfem_tangent_matvec(sfem_handle* h, const double* d_free, double* out_free);
+
 /* ---- dynamics (FemPhysicsMatrixFree::Step :297-324, SubStep :371-387, MatrixVectorMultiply
  * :523-534 and ComputeGradients :536-560 with mTimeStep != 0, Solve :589-597) ----
  * Time step h of the implicit (backward Euler) terms: with h > 0 the residual gains

@@ -304,6 +304,7 @@ class RefHarness:
             lib.ref_force_param_grads.argtypes = [C.c_void_p, _dp, _dp, _dp]
             lib.ref_step.argtypes = [C.c_void_p]
             lib.ref_set_sim.argtypes = [C.c_void_p, C.c_int, C.c_int]
+            lib.ref_assemble_dense.argtypes = [C.c_void_p, _dp]
             lib.ref_set_time_step.argtypes = [C.c_void_p, C.c_double]
             lib.ref_step_dt.argtypes = [C.c_void_p, C.c_double]
             for name in ["ref_set_velocities_shuffled", "ref_get_velocities_shuffled", "ref_set_start_shuffled"]:
@@ -403,6 +404,12 @@ class RefHarness:
 
     def step(self):
         self.lib().ref_step(self.h)
+
+    def assemble_dense(self):
+        n = 3 * self.n_free
+        K = np.zeros((n, n))
+        self.lib().ref_assemble_dense(self.h, _p(K))
+        return K
 
     # ---- dynamics (reshuffled node order) ----
     def set_sim(self, simtype, substeps=1):

@@ -235,6 +235,20 @@ void ref_force_param_grads(void* hp, double* gmu, double* glambda, double* grho)
 // The reference's own static solve: Step(0) dispatching on the configured solver.
 void ref_step(void* hp) { ((Handle*)hp)->phys->Step(0); }
 
+// The reference's assembled tangent (ElasticEnergy::AssembleStiffnessMatrix,
+// Source/ElasticEnergy.cpp:573-635) at the current positions, dense row-major
+// 3 N_f x 3 N_f (small meshes only).
+void ref_assemble_dense(void* hp, double* out) {
+  RefProblem* p = ((Handle*)hp)->phys;
+  p->ComputeDeformationGradients();
+  SparseMatrix K;
+  ElasticEnergy::AssembleStiffnessMatrix(p, K);
+  const int n = (int)K.rows();
+  EigenMatrix D(K);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) out[(size_t)i * n + j] = D(i, j);
+}
+
 // Dynamics: simulation type / substeps (FemPhysicsBase mSimType, mNumSteps), the time step
 // of the implicit terms (mTimeStep), node velocities and step-start positions (pos0), in
 // reshuffled order, and the reference's own Step(dt).

@@ -106,6 +106,9 @@ SIGNATURES = {
     "sfem_force_param_grads": [_vp, _dp, _dp, _dp],
     "sfem_pcg": [_vp, _dp, _dp, C.POINTER(PcgOpts), C.POINTER(PcgStats)],
     "sfem_newton_solve": [_vp, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)],
+    "sfem_tangent_nnz": [_vp, _i64p],
+    "sfem_assemble_tangent": [_vp, _ip, _ip, _dp],
+    "sfem_tangent_matvec": [_vp, _dp, _dp],
     "sfem_set_time_step": [_vp, C.c_double],
     "sfem_get_time_step": [_vp, _dp],
     "sfem_set_velocities": [_vp, _dp],

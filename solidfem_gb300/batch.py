@@ -40,12 +40,14 @@ def lame(E, nu):
 class BatchedBodies:
     """Union of bodies, each a clamped (x = 0) cantilever box of length L under gravity.
 
-    The tip deflection of such a cantilever relative to its length is about 24 rho g L / E, so
-    for E down to 1e4 Pa the default L = 0.1 m keeps the softest bodies at moderate rotation
-    (a metre-scale body of E = 1e4 Pa folds over under its own weight)."""
+    The tip deflection of such a cantilever (square section L/4) relative to its length is
+    about 24 rho g L / E, so for E down to 1e4 Pa the default L = 0.01 m keeps the softest
+    bodies at a deflection of a quarter of their length (a metre-scale body of E = 1e4 Pa
+    folds over under its own weight)."""
 
-    def __init__(self, specs, precision="fp32", density=1070.0, gravity=(0.0, 0.0, -9.81), length=0.1):
+    def __init__(self, specs, precision="fp32", density=1070.0, gravity=(0.0, 0.0, -9.81), length=0.01):
         spacing = 0.5 * length
+        self.spacing = spacing
         nodes, tets, fixed, mu, lam, offsets = [], [], [], [], [], [0]
         self.meshes = []
         base = 0

@@ -1,8 +1,8 @@
 // Launchers of the learned-preconditioner kernels (sfem_gnn_kernels.cuh).
 #include <algorithm>
 
-#include "sfem_gnn_kernels.cuh"
 #include "sfem_internal.h"
+#include "sfem_gnn_kernels.cuh"
 
 namespace sfem {
 namespace gnn {
@@ -77,10 +77,12 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 }
 
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
-                       float* w, float* out, const int* done, cudaStream_t st) {
+                       float* w, float* out, const int* done, cudaStream_t st, const float* rprev, float* partials,
+                       unsigned* counter, CgScalars* s) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
   const int64_t n3 = 3 * g.n;
-  const int grid = (int)std::min<int64_t>(blocks_for(g.n, 16), 152 * 16);  // 16 nodes per 256-thread block
+  // one node per thread; the partials of the BETA pass hold 4 values per block
+  const int grid = blocks_for(g.n, 256);
   count_launch();
   k_poly_fwd<true><<<grid, 256, 0, st>>>(g, r, dinv, nullptr, y1, done);
   count_launch();
@@ -89,11 +91,17 @@ void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const 
   k_poly_mid<<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, pc, w, done);
   // Horner in A^T: u = w3 -> A^T u + w2 (into y1) -> A^T u + w1 (into y2) -> out
   count_launch();
-  k_poly_bwd<false><<<grid, 256, 0, st>>>(g, w + 3 * n3, w + 2 * n3, r, dinv, 0.f, y1, done);
+  k_poly_bwd<false, false><<<grid, 256, 0, st>>>(g, w + 3 * n3, w + 2 * n3, r, dinv, 0.f, y1, done, nullptr, nullptr,
+                                                 nullptr, nullptr);
   count_launch();
-  k_poly_bwd<false><<<grid, 256, 0, st>>>(g, y1, w + n3, r, dinv, 0.f, y2, done);
+  k_poly_bwd<false, false><<<grid, 256, 0, st>>>(g, y1, w + n3, r, dinv, 0.f, y2, done, nullptr, nullptr, nullptr,
+                                                 nullptr);
   count_launch();
-  k_poly_bwd<true><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done);
+  if (s)
+    k_poly_bwd<true, true><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, rprev, partials, counter, s);
+  else
+    k_poly_bwd<true, false><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, nullptr, nullptr, nullptr,
+                                                  nullptr);
 }
 
 // the training forward: activations h0..h3 of S at x (kept, with x), then S^T through the
@@ -193,55 +201,29 @@ void launch_sub(int64_t n, const float* a, const float* b, float* d, cudaStream_
   k_sub<<<grid < 1 ? 1 : grid, 256, 0, st>>>(n, a, b, d);
 }
 
-// p = z, rz = r.z  (after the CG initialisation has set r, x, bb)
+// rz = r.z, p = 0, beta = 0 (the first direction is z itself), after the CG initialisation
+// has set r, x, bb
 __global__ void __launch_bounds__(256) k_fcg_init(int64_t n, const float* __restrict__ r, const float* __restrict__ z,
                                                   float* __restrict__ p, float* __restrict__ partials,
                                                   unsigned* counter, CgScalars* s) {
   float acc[1] = {0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    p[i] = z[i];
+    p[i] = 0.f;
     acc[0] += r[i] * z[i];
   }
   double t[1];
-  if (last_block_sums<1>(acc, partials, counter, t) && threadIdx.x == 0) s->rz = t[0];
-}
-
-// x += alpha p, rprev = r, r -= alpha q, rr
-__global__ void __launch_bounds__(256) k_fcg_update(int64_t n, float* __restrict__ x, float* __restrict__ r,
-                                                    float* __restrict__ rprev, const float* __restrict__ p,
-                                                    const float* __restrict__ q, float* __restrict__ partials,
-                                                    unsigned* counter, CgScalars* s) {
-  if (s->done) return;
-  const float a = (float)s->alpha;
-  float acc[1] = {0.f};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += a * p[i];
-    const float ri = r[i];
-    rprev[i] = ri;
-    const float rn = ri - a * q[i];
-    r[i] = rn;
-    acc[0] += rn * rn;
-  }
-  double tt[1];
-  if (!last_block_sums<1>(acc, partials, counter, tt) || threadIdx.x != 0) return;
-  const double t = tt[0];
-  s->rr = t;
-  s->it += 1;
-  if (!isfinite(t)) {
-    s->done = 1;
-    s->status = -3;
-  } else if (t <= s->tol2) {
-    s->done = 1;
-  } else if (s->it >= s->max_it) {
-    s->done = 1;
-    s->status = 1;
+  if (last_block_sums<1>(acc, partials, counter, t) && threadIdx.x == 0) {
+    s->rz = t[0];
+    s->beta = 0.0;
+    s->jac = 0;
   }
 }
 
 // Polak-Ribiere: beta = z.(r - rprev) / rz_old, rz = z.r.  The same sums are formed for the
 // Jacobi direction z_J = D^-1 r; when the learned direction is not a descent direction
 // (z.r <= 0) this iteration falls back to Jacobi (s->beta / s->rz refer to the chosen z and
-// s->pq carries the choice to k_fcg_dir: pq < 0 selects Jacobi).
+// s->jac = 1 makes the next fused direction update use D^-1 r).  Used with the layer-kernel
+// inference; the polynomial inference forms these sums in its last pass.
 __global__ void __launch_bounds__(256) k_fcg_beta(int64_t n, const float* __restrict__ r,
                                                   const float* __restrict__ rprev, const float* __restrict__ z,
                                                   const float* __restrict__ dinv, float* __restrict__ partials,
@@ -263,21 +245,12 @@ __global__ void __launch_bounds__(256) k_fcg_beta(int64_t n, const float* __rest
   if (learned_ok) {
     s->beta = t[0] / s->rz;
     s->rz = t[1];
-    s->pq = 1.0;
+    s->jac = 0;
   } else {
     s->beta = t[2] / s->rz;
     s->rz = t[3];
-    s->pq = -1.0;
+    s->jac = 1;
   }
-}
-
-__global__ void k_fcg_dir(int64_t n, const float* __restrict__ z, const float* __restrict__ r,
-                          const float* __restrict__ dinv, float* __restrict__ p, const CgScalars* s) {
-  if (s->done) return;
-  const float beta = (float)s->beta;
-  const bool jac = s->pq < 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = (jac ? dinv[i] * r[i] : z[i]) + beta * p[i];
 }
 
 static int vgrid(int64_t n) {
@@ -291,20 +264,10 @@ void launch_fcg_init(int64_t n, const float* r, const float* z, float* p, float*
   count_launch();
   k_fcg_init<<<vgrid(n), 256, 0, st>>>(n, r, z, p, partials, counter, s);
 }
-void launch_fcg_update(int64_t n, float* x, float* r, float* rprev, const float* p, const float* q, float* partials,
-                       unsigned* counter, CgScalars* s, cudaStream_t st) {
-  count_launch();
-  k_fcg_update<<<vgrid(n), 256, 0, st>>>(n, x, r, rprev, p, q, partials, counter, s);
-}
 void launch_fcg_beta(int64_t n, const float* r, const float* rprev, const float* z, const float* dinv,
                      float* partials, unsigned* counter, CgScalars* s, cudaStream_t st) {
   count_launch();
   k_fcg_beta<<<vgrid(n), 256, 0, st>>>(n, r, rprev, z, dinv, partials, counter, s);
-}
-void launch_fcg_dir(int64_t n, const float* z, const float* r, const float* dinv, float* p, const CgScalars* s,
-                    cudaStream_t st) {
-  count_launch();
-  k_fcg_dir<<<vgrid(n), 256, 0, st>>>(n, z, r, dinv, p, s);
 }
 
 }  // namespace gnn

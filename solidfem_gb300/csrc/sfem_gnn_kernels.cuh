@@ -629,44 +629,44 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_inf(Graph g, const __nv_bfloat
 // ======================= inference through the folded polynomial =======================
 // y_{k+1} = A y_k (mean over neighbours), y_0 = x = D^-1/2 r; then w_j = sum_k y_k G[k][j]
 // and M(r) = D^-1/2 (c x + w_0 + A^T (w_1 + A^T (w_2 + A^T w_3)))   (Horner in A^T).
-// Six passes over 3-vectors.  Half a warp per node: its 16 lanes load neighbours e, e + 16,
-// ... in parallel and a fixed shuffle tree adds them (deterministic).
+// Six passes over 3-vectors, one thread per node; the neighbour loop is unrolled by four so
+// that four neighbour loads are in flight, and adds in neighbour order (deterministic).
 
-__device__ __forceinline__ float half_sum(float v) {  // over the 16 lanes of a half warp
-#pragma unroll
-  for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// sum over the neighbours j of node of wgt_j * v_j (3-vectors); every lane of the half warp
-// returns the total.  FIRST: v_j = r_j D_j^-1/2; TRANS: wgt_j = 1 / deg_j, else 1.
+// sum over the neighbours j of node i of wgt_j * v_j (3-vectors).
+// FIRST: v_j = r_j D_j^-1/2; TRANS: wgt_j = 1 / deg_j, else 1.
 template <bool FIRST, bool TRANS>
-__device__ __forceinline__ void half_gather(const Graph& g, int64_t node, bool valid, int l16,
-                                            const float* __restrict__ r, const float* __restrict__ dinv,
-                                            const float* __restrict__ v, float (&a)[3]) {
+__device__ __forceinline__ void node_gather(const Graph& g, int64_t i, const float* __restrict__ r,
+                                            const float* __restrict__ dinv, const float* __restrict__ v,
+                                            float (&a)[3]) {
   a[0] = a[1] = a[2] = 0.f;
-  int p0 = 0, deg = 0;
-  if (valid) {
-    p0 = g.ptr[node];
-    deg = g.ptr[node + 1] - p0;
-  }
-  for (int e = l16; e < deg; e += 16) {
-    const int jn = g.idx[p0 + e];
-    const int64_t j = 3 * (int64_t)jn;
-    const float wgt = TRANS ? g.inv_deg[jn] : 1.f;
-    if (FIRST) {
-      a[0] += r[j] * sqrtf(dinv[j]);
-      a[1] += r[j + 1] * sqrtf(dinv[j + 1]);
-      a[2] += r[j + 2] * sqrtf(dinv[j + 2]);
-    } else {
-      a[0] += wgt * v[j];
-      a[1] += wgt * v[j + 1];
-      a[2] += wgt * v[j + 2];
+  const int p1 = g.ptr[i + 1];
+  int e = g.ptr[i];
+  auto val = [&](int jn, int c) -> float {
+    const int64_t j = 3 * (int64_t)jn + c;
+    return FIRST ? r[j] * sqrtf(dinv[j]) : v[j];
+  };
+  for (; e + 4 <= p1; e += 4) {
+    int jn[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) jn[u] = g.idx[e + u];
+    float x[4][3], wg[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      wg[u] = TRANS ? g.inv_deg[jn[u]] : 1.f;
+#pragma unroll
+      for (int c = 0; c < 3; c++) x[u][c] = val(jn[u], c);
     }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) a[c] += wg[u] * x[u][c];
   }
-  a[0] = half_sum(a[0]);
-  a[1] = half_sum(a[1]);
-  a[2] = half_sum(a[2]);
+  for (; e < p1; e++) {
+    const int jn = g.idx[e];
+    const float wg = TRANS ? g.inv_deg[jn] : 1.f;
+#pragma unroll
+    for (int c = 0; c < 3; c++) a[c] += wg * val(jn, c);
+  }
 }
 
 template <bool FIRST>
@@ -674,37 +674,28 @@ __global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float* __restri
                                                   const float* __restrict__ dinv, const float* __restrict__ yin,
                                                   float* __restrict__ yout, const int* done) {
   if (done && *done) return;
-  const int lane = threadIdx.x & 31, l16 = lane & 15;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t k = warp; 2 * k < g.n; k += nwarps) {
-    const int64_t node = 2 * k + (lane >> 4);
-    const bool valid = node < g.n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     float a[3];
-    half_gather<FIRST, false>(g, node, valid, l16, r, dinv, yin, a);
-    if (valid && l16 < 3) yout[3 * node + l16] = (l16 == 0 ? a[0] : l16 == 1 ? a[1] : a[2]) * g.inv_deg[node];
+    node_gather<FIRST, false>(g, i, r, dinv, yin, a);
+    const float id = g.inv_deg[i];
+    yout[3 * i] = a[0] * id;
+    yout[3 * i + 1] = a[1] * id;
+    yout[3 * i + 2] = a[2] * id;
   }
 }
 
-// y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of 3n);
-// lane t < 12 of the half warp writes w_{t/3}[t%3]
+// y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of 3n)
 __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restrict__ r,
                                                   const float* __restrict__ dinv, const float* __restrict__ y1,
                                                   const float* __restrict__ y2, PolyCoef pc, float* __restrict__ w,
                                                   const int* done) {
   if (done && *done) return;
-  const int lane = threadIdx.x & 31, l16 = lane & 15;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t n3 = 3 * g.n;
-  for (int64_t k = warp; 2 * k < g.n; k += nwarps) {
-    const int64_t node = 2 * k + (lane >> 4);
-    const bool valid = node < g.n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     float a[3];
-    half_gather<false, false>(g, node, valid, l16, r, dinv, y2, a);
-    if (!valid || l16 >= 12) continue;
-    const int64_t o = 3 * node;
-    const float id = g.inv_deg[node];
+    node_gather<false, false>(g, i, r, dinv, y2, a);
+    const int64_t o = 3 * i;
+    const float id = g.inv_deg[i];
     float y[NL + 1][3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -713,40 +704,68 @@ __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restri
       y[2][c] = y2[o + c];
       y[3][c] = a[c] * id;
     }
-    const int jj = l16 / 3, c = l16 % 3;
-    float acc = 0.f;
 #pragma unroll
-    for (int kk = 0; kk <= NL; kk++)
+    for (int jj = 0; jj <= NL; jj++) {
 #pragma unroll
-      for (int b = 0; b < 3; b++) acc += y[kk][b] * pc.G[kk][jj][3 * b + c];
-    w[jj * n3 + o + c] = acc;
+      for (int c = 0; c < 3; c++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k <= NL; k++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) acc += y[k][b] * pc.G[k][jj][3 * b + c];
+        w[jj * n3 + o + c] = acc;
+      }
+    }
   }
 }
 
-// u_out_i = sum_{j in N(i)} u_in_j / deg_j + wadd_i;  LAST: out = D^-1/2 (c x + that) with x = D^-1/2 r
-template <bool LAST>
+// u_out_i = sum_{j in N(i)} u_in_j / deg_j + wadd_i;  LAST: out = D^-1/2 (c x + that) with x = D^-1/2 r.
+// BETA (with LAST, inside flexible CG): also the Polak-Ribiere sums of the new z = out,
+//   z.(r - rprev), z.r and the same for z_J = D^-1 r, finished by the last block into
+//   s->beta, s->rz and s->jac (Jacobi direction when z.r <= 0), like k_fcg_beta.
+//   partials: 4 gridDim floats.
+template <bool LAST, bool BETA>
 __global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const float* __restrict__ uin,
                                                   const float* __restrict__ wadd, const float* __restrict__ r,
                                                   const float* __restrict__ dinv, float cc, float* __restrict__ out,
-                                                  const int* done) {
+                                                  const int* done, const float* __restrict__ rprev,
+                                                  float* __restrict__ partials, unsigned* counter, CgScalars* s) {
   if (done && *done) return;
-  const int lane = threadIdx.x & 31, l16 = lane & 15;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t k = warp; 2 * k < g.n; k += nwarps) {
-    const int64_t node = 2 * k + (lane >> 4);
-    const bool valid = node < g.n;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     float a[3];
-    half_gather<false, true>(g, node, valid, l16, r, dinv, uin, a);
-    if (!valid || l16 >= 3) continue;
-    const int64_t i = 3 * node + l16;
-    const float v = (l16 == 0 ? a[0] : l16 == 1 ? a[1] : a[2]) + wadd[i];
-    if (LAST) {
-      const float d = dinv[i];
-      out[i] = cc * d * r[i] + sqrtf(d) * v;
-    } else {
-      out[i] = v;
+    node_gather<false, true>(g, i, r, dinv, uin, a);
+    const int64_t o = 3 * i;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float v = a[c] + wadd[o + c];
+      if (LAST) {
+        const float d = dinv[o + c], ri = r[o + c];
+        const float z = cc * d * ri + sqrtf(d) * v;
+        out[o + c] = z;
+        if (BETA) {
+          const float dr = ri - rprev[o + c], zj = d * ri;
+          acc[0] += z * dr;
+          acc[1] += z * ri;
+          acc[2] += zj * dr;
+          acc[3] += zj * ri;
+        }
+      } else {
+        out[o + c] = v;
+      }
     }
+  }
+  if (!BETA) return;
+  double t[4];
+  if (!last_block_sums<4>(acc, partials, counter, t) || threadIdx.x != 0) return;
+  if (t[1] > 0.0 && isfinite(t[1]) && isfinite(t[0])) {
+    s->beta = t[0] / s->rz;
+    s->rz = t[1];
+    s->jac = 0;
+  } else {
+    s->beta = t[2] / s->rz;
+    s->rz = t[3];
+    s->jac = 1;
   }
 }
 

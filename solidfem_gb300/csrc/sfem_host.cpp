@@ -112,6 +112,14 @@ struct sfem_handle {
   double dt = 0.0;  // 0: static
   double *vel = nullptr, *ustart = nullptr;
   double* pm64 = nullptr;  // per patch-node slot mass share / h^2 (implicit dynamics)
+  // neo-Hookean tangent cache of the running Krylov solve (12 E values per precision)
+  double* nhc64 = nullptr;
+  float* nhc32 = nullptr;
+  bool nhc_on = false;
+  // assembled tangent (block CSR over free nodes, built on first use)
+  int64_t bsr_nnzb = -1;
+  int32_t *bsr_rowptr = nullptr, *bsr_col = nullptr, *bsr_slot = nullptr, *bsr_dslot = nullptr;
+  double* bsr_vals = nullptr;
   float* pm32 = nullptr;
   DynView dyn() const { return DynView{vel, ustart, 1.0 / dt, 1.0 / (dt * dt)}; }
   int64_t *csr_ptr = nullptr, *csr_ent = nullptr;
@@ -159,8 +167,10 @@ struct sfem_handle {
   PatchView<T> pv(const T* X, const T* vol, const T* scale, const T* scale_la, T m, T l) const {
     const T* pm = nullptr;
     if (dt > 0) pm = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)pm64 : (const void*)pm32);
+    const T* nhc = nullptr;
+    if (nhc_on) nhc = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)nhc64 : (const void*)nhc32);
     return PatchView<T>{elem_off, node_off, pnode, pdest, lptr, lent, lidx, X, vol, scale, scale_la, E, n_patches,
-                        nbc, m, l, pm};
+                        nbc, m, l, pm, nhc};
   }
   NodeCsr csr() const { return NodeCsr{csr_ptr, csr_ent}; }
   ElemView<double> ev64() const {
@@ -223,17 +233,17 @@ void element_pass(sfem_handle* h, int mode, const T* u, const T* p, T* fe, doubl
 // q = K p over the free DOFs with the fused patch kernel (+ p.q and alpha when s is given)
 template <typename T>
 void hvp(sfem_handle* h, const T* u, const T* p, T* q, CgScalars* s, cudaEvent_t mid = nullptr, const T* r = nullptr,
-         const T* dinv = nullptr, T* p_new = nullptr) {
+         const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr) {
   const ElemView<T> ev = ev_of<T>(h);
   const PatchView<T> pv = h->pv<T>(ev.X, ev.vol, ev.scale, ev.scale_la, ev.mu, ev.lambda);
   T* part = reinterpret_cast<T*>(h->partial);
   const int mat = (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) ? 4 : h->material;
   switch (mat) {
-    case 0: launch_patch_hvp<T, 0>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
-    case 1: launch_patch_hvp<T, 1>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
-    case 2: launch_patch_hvp<T, 2>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
-    case 3: launch_patch_hvp<T, 3>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
-    default: launch_patch_hvp<T, 4>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new); break;
+    case 0: launch_patch_hvp<T, 0>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
+    case 1: launch_patch_hvp<T, 1>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
+    case 2: launch_patch_hvp<T, 2>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
+    case 3: launch_patch_hvp<T, 3>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
+    default: launch_patch_hvp<T, 4>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
   }
 }
 
@@ -284,6 +294,22 @@ int jacobi(sfem_handle* h, T* dinv, T* diag) {
   return 0;
 }
 
+// For a neo-Hookean handle, the tangent factors of the current state are computed once per
+// Krylov solve (k_nh_cache) and the patch product reads them instead of re-forming F, F^-1 and
+// log J per element and iteration; the guard switches the cache off when the solve returns.
+template <typename T>
+struct NhCacheGuard {
+  sfem_handle* h;
+  NhCacheGuard(sfem_handle* hh, const T* u) : h(hh) {
+    if (h->material != SFEM_MMT_NEO_HOOKEAN) return;
+    T** c = reinterpret_cast<T**>(sizeof(T) == 8 ? (void*)&h->nhc64 : (void*)&h->nhc32);
+    if (!*c && dalloc(c, 12 * (size_t)h->E) != 0) return;  // without memory: the uncached product
+    launch_nh_cache<T>(ev_of<T>(h), u, *c, h->stream);
+    h->nhc_on = true;
+  }
+  ~NhCacheGuard() { h->nhc_on = false; }
+};
+
 // Preconditioned CG on K x = b (device vectors of the workspace, full length).
 // The displacement used by the HVP must already be in ws.u (FP32) / h->u (FP64).
 template <typename T>
@@ -298,6 +324,7 @@ int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, doub
   *h->scal_h = s0;
   CU(cudaMemcpyAsync(h->scal, h->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
   if (!dinv) dinv = w.ones;  // unpreconditioned CG: z = r
+  NhCacheGuard<T> cache(h, u);
   launch_cg_init<T>(n, b + o, x + o, w.r + o, w.p + o, dinv + o, h->red(), h->scal, h->stream);
   // directions alternate between two buffers: iteration k reads p_{k-1} from pbuf[k % 2] and
   // the patch kernel writes p_k = dinv r + beta p_{k-1} into pbuf[(k + 1) % 2]
@@ -730,7 +757,8 @@ int sfem_destroy(sfem_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
-                   h->ptf, h->vel, h->ustart, h->pm64, h->pm32};
+                   h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
+                   h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
@@ -816,6 +844,111 @@ int sfem_set_stream(sfem_handle* h, void* stream) {
   h->own_stream = false;
   h->stream = (cudaStream_t)stream;
   return SFEM_OK;
+}
+
+// ---- assembled tangent (ElasticEnergy::AssembleStiffnessMatrix, Source/ElasticEnergy.cpp:573-635) ----
+static int bsr_structure(sfem_handle* h) {
+  if (h->bsr_nnzb >= 0) return 0;
+  const int64_t E = h->E, nbc = h->nbc, nf = h->nf;
+  std::vector<int4> tt((size_t)E);
+  CU(cudaMemcpyAsync(tt.data(), h->tets, tt.size() * sizeof(int4), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  std::vector<uint64_t> keys;
+  keys.reserve((size_t)E * 16 + (size_t)nf);
+  for (int64_t i = 0; i < nf; i++) keys.push_back(((uint64_t)i << 32) | (uint32_t)i);
+  for (const int4& t4 : tt) {
+    const int32_t v[4] = {t4.x, t4.y, t4.z, t4.w};
+    for (int a = 0; a < 4; a++)
+      for (int b = 0; b < 4; b++)
+        if (v[a] >= nbc && v[b] >= nbc) keys.push_back(((uint64_t)(v[a] - nbc) << 32) | (uint32_t)(v[b] - nbc));
+  }
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  if (keys.size() > (size_t)INT32_MAX) return fail(SFEM_ERR_INVALID, "tangent too large for 32-bit block indices");
+  std::vector<int32_t> rowptr((size_t)nf + 1, 0), col(keys.size()), slot((size_t)E * 16, -1), dslot((size_t)nf);
+  for (size_t k = 0; k < keys.size(); k++) {
+    rowptr[(keys[k] >> 32) + 1]++;
+    col[k] = (int32_t)(keys[k] & 0xffffffffu);
+  }
+  for (int64_t i = 0; i < nf; i++) rowptr[i + 1] += rowptr[i];
+  auto find = [&](int64_t r, int32_t c) {
+    const int32_t* b = col.data() + rowptr[r];
+    const int32_t* e = col.data() + rowptr[r + 1];
+    return (int32_t)(std::lower_bound(b, e, c) - col.data());
+  };
+  for (int64_t e = 0; e < E; e++) {
+    const int32_t v[4] = {tt[e].x, tt[e].y, tt[e].z, tt[e].w};
+    for (int a = 0; a < 4; a++)
+      for (int b = 0; b < 4; b++)
+        if (v[a] >= nbc && v[b] >= nbc) slot[16 * e + 4 * a + b] = find(v[a] - nbc, v[b] - nbc);
+  }
+  for (int64_t i = 0; i < nf; i++) dslot[i] = find(i, (int32_t)i);
+  TRY(dalloc(&h->bsr_rowptr, rowptr.size()));
+  TRY(dalloc(&h->bsr_col, std::max<size_t>(col.size(), 1)));
+  TRY(dalloc(&h->bsr_slot, slot.size()));
+  TRY(dalloc(&h->bsr_dslot, std::max<size_t>(dslot.size(), 1)));
+  TRY(dalloc(&h->bsr_vals, std::max<size_t>(9 * col.size(), 1)));
+  CU(cudaMemcpyAsync(h->bsr_rowptr, rowptr.data(), rowptr.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if (!col.empty()) CU(cudaMemcpyAsync(h->bsr_col, col.data(), col.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->bsr_slot, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if (nf > 0) CU(cudaMemcpyAsync(h->bsr_dslot, dslot.data(), dslot.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  TRY(sync(h));
+  h->bsr_nnzb = (int64_t)col.size();
+  return 0;
+}
+
+// assemble the FP64 tangent at the current state into h->bsr_vals
+static int bsr_assemble(sfem_handle* h) {
+  TRY(bsr_structure(h));
+  double* Ke = nullptr;
+  TRY(dalloc(&Ke, (size_t)h->E * 144));
+  const ElemView<double> ev = h->ev64();
+  const int mat = (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) ? 4 : h->material;
+  switch (mat) {
+    case 0: launch_element_stiffness<0>(ev, h->u, Ke, h->stream); break;
+    case 1: launch_element_stiffness<1>(ev, h->u, Ke, h->stream); break;
+    case 2: launch_element_stiffness<2>(ev, h->u, Ke, h->stream); break;
+    case 3: launch_element_stiffness<3>(ev, h->u, Ke, h->stream); break;
+    default: launch_element_stiffness<4>(ev, h->u, Ke, h->stream); break;
+  }
+  CU(cudaMemsetAsync(h->bsr_vals, 0, 9 * (size_t)h->bsr_nnzb * sizeof(double), h->stream));
+  launch_assemble_bsr(h->nbc, h->N, h->csr(), Ke, h->bsr_slot, h->bsr_dslot, h->dt > 0 ? h->mass : nullptr,
+                      h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0, h->bsr_vals, h->stream);
+  const int st = sync(h);
+  cudaFree(Ke);
+  return st;
+}
+
+int sfem_tangent_nnz(sfem_handle* h, int64_t* nnzb) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!nnzb) return fail(SFEM_ERR_INVALID, "null");
+  TRY(bsr_structure(h));
+  *nnzb = h->bsr_nnzb;
+  return SFEM_OK;
+}
+
+int sfem_assemble_tangent(sfem_handle* h, int32_t* rowptr, int32_t* colidx, double* vals) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!rowptr || !colidx || !vals) return fail(SFEM_ERR_INVALID, "null");
+  TRY(bsr_assemble(h));
+  CU(cudaMemcpyAsync(rowptr, h->bsr_rowptr, ((size_t)h->nf + 1) * 4, cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(colidx, h->bsr_col, (size_t)h->bsr_nnzb * 4, cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(vals, h->bsr_vals, 9 * (size_t)h->bsr_nnzb * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int sfem_tangent_matvec(sfem_handle* h, const double* d_free, double* out_free) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!d_free || !out_free) return fail(SFEM_ERR_INVALID, "null");
+  TRY(bsr_assemble(h));
+  const size_t n = 3 * (size_t)h->nf;
+  CU(cudaMemcpyAsync(h->tmp64, d_free, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_bsr_spmv(h->nf, h->bsr_rowptr, h->bsr_col, h->bsr_vals, h->tmp64, h->tmp64b, h->stream);
+  CU(cudaMemcpyAsync(out_free, h->tmp64b, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
 }
 
 // ---- dynamics (FemPhysicsMatrixFree::Step :297-324, SubStep :371-387, Solve :589-597) ----
@@ -1747,6 +1880,7 @@ struct GnnState {
   gnn::PolyCoef pc{};                    // folded coefficients of the current weights
   bool pc_dirty = true;
   float *py1 = nullptr, *py2 = nullptr, *pw = nullptr;  // polynomial-form vectors (3n, 3n, 4 x 3n)
+  float* bpart = nullptr;  // block partials of the fused beta pass (4 per 256 nodes)
   int adam_t = 0;
   bool train_bufs = false;
   gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg}; }
@@ -1755,7 +1889,7 @@ struct GnnState {
 void gnn_free(GnnState* g) {
   void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->params, g->grad, g->m, g->v, g->Wb, g->x, g->xg,
                   g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->losses, g->z, g->rprev, g->tmp,
-                  g->py1, g->py2, g->pw};
+                  g->py1, g->py2, g->pw, g->bpart};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int l = 0; l <= gnn::NL; l++) {
@@ -1919,7 +2053,10 @@ int gnn_loss_grad_dev(sfem_handle* h, const float* r, const float* e, float cinv
   return 0;
 }
 
-// Flexible CG (Polak-Ribiere beta) with the learned preconditioner, FP32; b, x full length
+// Flexible CG (Polak-Ribiere beta) with the learned preconditioner, FP32; b, x full length.
+// Per iteration: the fused patch HVP builds p = z + beta p_old (or D^-1 r + beta p_old after a
+// non-descent z) and K p, p.Kp, alpha; the fused update assembles the shared-node q and does
+// x, r and r.r; the preconditioner's last pass forms z = M(r) and the next beta.
 int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it, sfem_pcg_stats* st) {
   GnnState* g = h->gnn;
   KrylovWs<float>& w = h->k32;
@@ -1931,11 +2068,24 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   *h->scal_h = s0;
   CU(cudaMemcpyAsync(h->scal, h->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
   TRY(gnn_poly_refresh(h));
+  NhCacheGuard<float> cache(h, w.u);
   launch_cg_init<float>(n, b + o, x + o, w.r + o, w.p + o, w.dinv + o, h->red(), h->scal, h->stream);
   const int* done = &h->scal->done;
-  gnn_apply_dev(h, w.r + o, g->z + o, done, false);
-  gnn::launch_fcg_init(n, w.r + o, g->z + o, w.p + o, reinterpret_cast<float*>(h->partials), h->counter, h->scal,
-                       h->stream);
+  float* part = reinterpret_cast<float*>(h->partials);
+  const float* dinv = w.dinv + o;
+  auto precondition = [&](bool with_beta) {
+    if (g->infer_mode == 0) {
+      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->py1, g->py2, g->pw, g->z + o, done, h->stream,
+                             with_beta ? g->rprev + o : nullptr, g->bpart, h->counter, with_beta ? h->scal : nullptr);
+    } else {
+      gnn::launch_apply(g->graph(), w.r + o, dinv, g->params, g->Wb, g->h, g->z + o, done, h->stream);
+      if (with_beta)
+        gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, dinv, part, h->counter, h->scal, h->stream);
+    }
+  };
+  precondition(false);
+  gnn::launch_fcg_init(n, w.r + o, g->z + o, w.p + o, part, h->counter, h->scal, h->stream);  // p_old = 0
+  float* pbuf[2] = {w.p, w.p2};
   const int check_every = 16;
   int it = 0;
   bool pending = false;
@@ -1945,37 +2095,36 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
     TRY(sync(h));
     if (h->scal_h->done || it >= max_it) break;
     if (pending) {
-      float a = 0, b = 0;
+      float a = 0, bms = 0;
       cudaEventElapsedTime(&a, h->pev[0], h->pev[1]);
-      cudaEventElapsedTime(&b, h->pev[1], h->pev[2]);
+      cudaEventElapsedTime(&bms, h->pev[1], h->pev[2]);
       h->prof_elem_ms += a;
-      h->prof_gather_ms += b;
+      h->prof_gather_ms += bms;
       h->prof_samples++;
       pending = false;
     }
     for (int k = 0; k < check_every && it < max_it; k++, it++) {
       const bool sample = h->profiling && k == 0;
+      float* pold = pbuf[it % 2];
+      float* pnew = pbuf[(it + 1) % 2];
       if (sample) CU(cudaEventRecord(h->pev[0], h->stream));
-      hvp<float>(h, w.u, w.p, w.q, h->scal, sample ? h->pev[1] : nullptr);
+      hvp<float>(h, w.u, pold, w.q, h->scal, sample ? h->pev[1] : nullptr, w.r, w.dinv, pnew, g->z);
       if (sample) {
         CU(cudaEventRecord(h->pev[2], h->stream));
         pending = true;
       }
       if (h->profiling) h->prof_launches++;
-      gnn::launch_fcg_update(n, x + o, w.r + o, g->rprev + o, w.p + o, w.q + o,
-                             reinterpret_cast<float*>(h->partials), h->counter, h->scal, h->stream);
-      gnn_apply_dev(h, w.r + o, g->z + o, done, false);
-      gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, w.dinv + o, reinterpret_cast<float*>(h->partials),
-                           h->counter, h->scal, h->stream);
-      gnn::launch_fcg_dir(n, g->z + o, w.r + o, w.dinv + o, w.p + o, h->scal, h->stream);
+      launch_fcg_update_patch<float>(h->nbc, h->N, h->bidx, h->pb(), reinterpret_cast<const float*>(h->partial), x,
+                                     w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream);
+      precondition(true);
     }
   }
   if (pending) {
-    float a = 0, b = 0;
+    float a = 0, bms = 0;
     cudaEventElapsedTime(&a, h->pev[0], h->pev[1]);
-    cudaEventElapsedTime(&b, h->pev[1], h->pev[2]);
+    cudaEventElapsedTime(&bms, h->pev[1], h->pev[2]);
     h->prof_elem_ms += a;
-    h->prof_gather_ms += b;
+    h->prof_gather_ms += bms;
     h->prof_samples++;
   }
   const CgScalars& s = *h->scal_h;
@@ -1986,10 +2135,11 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   }
   if (s.status == -3) return fail(SFEM_ERR_NAN, "non-finite value in the flexible Krylov recurrence");
   if (s.status == 2) {
-    if (s.it == 0) CU(cudaMemcpyAsync(x + o, w.p + o, n * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    // negative curvature at the first iteration: return the first direction (z itself)
+    if (s.it == 0) CU(cudaMemcpyAsync(x + o, pbuf[1] + o, n * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
     return SFEM_NEGATIVE_CURVATURE;
   }
-  return s.status == 1 ? SFEM_NOT_CONVERGED : SFEM_OK;  // status 3: non-descent direction, keep iterate
+  return s.status == 1 ? SFEM_NOT_CONVERGED : SFEM_OK;
 }
 
 }  // namespace
@@ -2075,6 +2225,7 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   TRY(dalloc(&g->py1, 3 * (size_t)n));
   TRY(dalloc(&g->py2, 3 * (size_t)n));
   TRY(dalloc(&g->pw, 12 * (size_t)n));
+  TRY(dalloc(&g->bpart, 4 * (size_t)((n + 255) / 256) + 64));
   TRY(dalloc(&g->spart, 4096));
   TRY(dalloc(&g->scount, 1));
   TRY(dalloc(&g->z, 3 * (size_t)h->N));

@@ -57,6 +57,7 @@ struct CgScalars {
   int32_t max_it;
   int32_t done;
   int32_t status;  // 0 ok, 1 max iters, 2 negative curvature, -3 nan
+  int32_t jac;     // flexible CG: the next direction uses D^-1 r instead of the preconditioner output
 };
 
 // Element patches for the fused Hessian-vector product.  Elements are stored in
@@ -86,7 +87,8 @@ struct PatchView {
   int64_t n_patches;
   int64_t nbc;
   T mu, lambda;
-  const T* pm;  // implicit dynamics: per slot m_g / (h^2 * patches sharing g), else nullptr
+  const T* pm;   // implicit dynamics: per slot m_g / (h^2 * patches sharing g), else nullptr
+  const T* nhc;  // neo-Hookean tangent cache (k_nh_cache, 12 E values) valid for this solve, or nullptr
 };
 
 // Implicit-dynamics terms of the residual (FemPhysicsMatrixFree::ComputeGradients :546-557):
@@ -135,10 +137,13 @@ constexpr int kFeStride = 13;  // odd row stride of the element results in share
 template <typename T, int MAT>
 void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, const T* p, T* q, T* partial,
                       Reduce red, CgScalars* s, cudaStream_t st, cudaEvent_t mid = nullptr, const T* r = nullptr,
-                      const T* dinv = nullptr, T* p_new = nullptr);
+                      const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
 
 // fused Krylov update for the patch product (assembles q at shared nodes, bidx[g] = the
 // node's position in the shared-node list or -1)
+template <typename T>
+void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
+                             T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st);
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
@@ -193,6 +198,18 @@ void launch_dot(int64_t n, const double* a, const double* b, Reduce red, double*
 void launch_potential(int64_t nbc, int64_t N, const double* x0, const double* u, const double* mass,
                       const double* fext, const double* grav, double ff, Reduce red, double* out,
                       cudaStream_t st, const DynView* dv = nullptr);
+// neo-Hookean tangent factors per element (F^-T, mu_e, lambda_e, mu_e - lambda_e log J; 12 E values)
+template <typename T>
+void launch_nh_cache(const ElemView<T>& ev, const T* u, T* cache, cudaStream_t st);
+// assembled tangent: element stiffness (144 doubles per element), block-CSR assembly over free
+// nodes (slot: 16 per element, -1 for a fixed corner; dslot: diagonal block of each free node),
+// block-CSR product
+template <int MAT>
+void launch_element_stiffness(const ElemView<double>& ev, const double* u, double* Ke, cudaStream_t st);
+void launch_assemble_bsr(int64_t nbc, int64_t N, NodeCsr csr, const double* Ke, const int32_t* slot,
+                         const int32_t* dslot, const double* mass, double inv_h2, double* vals, cudaStream_t st);
+void launch_bsr_spmv(int64_t nrows, const int32_t* rowptr, const int32_t* col, const double* vals, const double* x,
+                     double* y, cudaStream_t st);
 // implicit dynamics: per patch-node slot mass share m_g / (h^2 k_g) (k_g patches touch g)
 template <typename T>
 void launch_patch_mass(int64_t n_slots, int64_t nbc, const int32_t* pnode, const int32_t* bidx, PatchBoundary pb,
@@ -222,9 +239,11 @@ namespace gnn {
 // fused into the first and last); Wb holds the 3 packed BF16 weight sets (k_gnn_pack)
 void launch_apply(const Graph& g, const float* r, const float* dinv, const float* params, const __nv_bfloat16* Wb,
                   __nv_bfloat16* const* h, float* out, const int* done, cudaStream_t st);
-// the same M(r) through the folded polynomial (six passes over 3-vectors); y1, y2: 3n, w: 4 x 3n
+// the same M(r) through the folded polynomial (six passes over 3-vectors); y1, y2: 3n, w: 4 x 3n.
+// With s (flexible CG), the last pass also forms the Polak-Ribiere beta from r, rprev (k_fcg_beta).
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
-                       float* w, float* out, const int* done, cudaStream_t st);
+                       float* w, float* out, const int* done, cudaStream_t st, const float* rprev = nullptr,
+                       float* partials = nullptr, unsigned* counter = nullptr, CgScalars* s = nullptr);
 // the same M(r) keeping the activations h0..h3 of S and x = D^-1/2 r (training)
 void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,
                         const __nv_bfloat16* Wb, __nv_bfloat16* const* h, float* x, float* G0, float* G1, float* G2,
@@ -248,14 +267,10 @@ void launch_adam(const float* grad, float* prm, float* m, float* v, float lr, in
                  __nv_bfloat16* Wb, cudaStream_t st);
 void launch_pack(const float* prm, __nv_bfloat16* Wb, cudaStream_t st);
 void launch_sub(int64_t n, const float* a, const float* b, float* d, cudaStream_t st);
-// flexible CG (Polak-Ribiere) vector kernels; partials need >= 2048 floats
+// flexible CG (Polak-Ribiere) vector kernels; partials need >= 4096 floats
 void launch_fcg_init(int64_t n, const float* r, const float* z, float* p, float* partials, unsigned* counter,
                      CgScalars* s, cudaStream_t st);
-void launch_fcg_update(int64_t n, float* x, float* r, float* rprev, const float* p, const float* q, float* partials,
-                       unsigned* counter, CgScalars* s, cudaStream_t st);
 void launch_fcg_beta(int64_t n, const float* r, const float* rprev, const float* z, const float* dinv,
                      float* partials, unsigned* counter, CgScalars* s, cudaStream_t st);
-void launch_fcg_dir(int64_t n, const float* z, const float* r, const float* dinv, float* p, const CgScalars* s,
-                    cudaStream_t st);
 }  // namespace gnn
 }  // namespace sfem

@@ -664,6 +664,141 @@ void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* 
   }
 }
 
+// Element stiffness (12 x 12, row-major, per element) from the tangent:
+//   K_(a,i),(b,c) = vol * (dP^{(b,c)} g_a)_i,  dP^{(b,c)} = tangent(e_c g_b^T),
+// the columns of ElasticEnergy::ComputeLocalStiffnessMatrixFromDifferential
+// (Source/ElasticEnergy.cpp:493-517) in closed form; FP64.
+template <int MAT>
+__global__ void __launch_bounds__(kThreads) k_element_stiffness(ElemView<double> ev, const double* __restrict__ u,
+                                                                double* __restrict__ Ke) {
+  const int64_t E = ev.E;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int4 t = ev.tets[e];
+    M3<double> X;
+#pragma unroll
+    for (int k = 0; k < 9; k++) X.a[k] = ev.X[k * E + e];
+    const double vol = ev.vol[e];
+    double mu = ev.mu, la = ev.lambda;
+    if (ev.scale) {
+      const double sc = ev.scale[e];
+      mu *= sc;
+      la *= ev.scale_la ? ev.scale_la[e] : sc;
+    }
+    M3<double> F = grad_of(u, t, X);
+    F.a[0] += 1.0;
+    F.a[4] += 1.0;
+    F.a[8] += 1.0;
+    Tangent<double, MAT> tg;
+    tg.init(F, mu, la);
+    double g[4][3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      g[0][j] = -(X.a[j] + X.a[3 + j] + X.a[6 + j]);
+      g[1][j] = X.a[j];
+      g[2][j] = X.a[3 + j];
+      g[3][j] = X.a[6 + j];
+    }
+    double* K = Ke + 144 * e;
+#pragma unroll 1
+    for (int b = 0; b < 4; b++) {
+#pragma unroll 1
+      for (int c = 0; c < 3; c++) {
+        M3<double> dF;
+#pragma unroll
+        for (int q = 0; q < 9; q++) dF.a[q] = 0.0;
+        dF.a[3 * c] = g[b][0];
+        dF.a[3 * c + 1] = g[b][1];
+        dF.a[3 * c + 2] = g[b][2];
+        const M3<double> dP = tg.apply(dF);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+            K[(3 * a + i) * 12 + 3 * b + c] =
+                vol * (dP.a[3 * i] * g[a][0] + dP.a[3 * i + 1] * g[a][1] + dP.a[3 * i + 2] * g[a][2]);
+      }
+    }
+  }
+}
+
+template <int MAT>
+void launch_element_stiffness(const ElemView<double>& ev, const double* u, double* Ke, cudaStream_t st) {
+  count_launch();
+  k_element_stiffness<MAT><<<grid_for(ev.E), kThreads, 0, st>>>(ev, u, Ke);
+}
+template void launch_element_stiffness<0>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template void launch_element_stiffness<1>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template void launch_element_stiffness<2>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template void launch_element_stiffness<3>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template void launch_element_stiffness<4>(const ElemView<double>&, const double*, double*, cudaStream_t);
+
+// Block-CSR assembly over free nodes, one thread per row in element order (deterministic):
+// vals[9 s] += K_e block (a, b) for every element entry (e, a) of the row's node and every
+// free corner b (s = slot[16 e + 4 a + b]); plus (m / h^2) I on the diagonal block (dynamics).
+__global__ void __launch_bounds__(kThreads) k_assemble_bsr(int64_t nbc, int64_t N, NodeCsr csr,
+                                                           const double* __restrict__ Ke,
+                                                           const int32_t* __restrict__ slot,
+                                                           const int32_t* __restrict__ dslot,
+                                                           const double* __restrict__ mass, double inv_h2,
+                                                           double* __restrict__ vals) {
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t k = csr.ptr[g]; k < csr.ptr[g + 1]; k++) {
+      const int64_t ent = csr.ent[k];
+      const int64_t e = ent >> 2;
+      const int a = (int)(ent & 3);
+      const double* K = Ke + 144 * e;
+#pragma unroll 1
+      for (int b = 0; b < 4; b++) {
+        const int32_t sl = slot[16 * e + 4 * a + b];
+        if (sl < 0) continue;
+        double* V = vals + 9 * (int64_t)sl;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int c = 0; c < 3; c++) V[3 * i + c] += K[(3 * a + i) * 12 + 3 * b + c];
+      }
+    }
+    if (mass) {
+      double* V = vals + 9 * (int64_t)dslot[g - nbc];
+      const double m = mass[g] * inv_h2;
+      V[0] += m;
+      V[4] += m;
+      V[8] += m;
+    }
+  }
+}
+void launch_assemble_bsr(int64_t nbc, int64_t N, NodeCsr csr, const double* Ke, const int32_t* slot,
+                         const int32_t* dslot, const double* mass, double inv_h2, double* vals, cudaStream_t st) {
+  count_launch();
+  k_assemble_bsr<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, Ke, slot, dslot, mass, inv_h2, vals);
+}
+
+// y = A x for a block-CSR matrix with 3 x 3 blocks (one thread per block row)
+__global__ void __launch_bounds__(kThreads) k_bsr_spmv(int64_t nrows, const int32_t* __restrict__ rowptr,
+                                                       const int32_t* __restrict__ col,
+                                                       const double* __restrict__ vals, const double* __restrict__ x,
+                                                       double* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nrows; i += (int64_t)gridDim.x * blockDim.x) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      const int64_t j = 3 * (int64_t)col[k];
+      const double* V = vals + 9 * (int64_t)k;
+      const double x0 = x[j], x1 = x[j + 1], x2 = x[j + 2];
+      a0 += V[0] * x0 + V[1] * x1 + V[2] * x2;
+      a1 += V[3] * x0 + V[4] * x1 + V[5] * x2;
+      a2 += V[6] * x0 + V[7] * x1 + V[8] * x2;
+    }
+    y[3 * i] = a0;
+    y[3 * i + 1] = a1;
+    y[3 * i + 2] = a2;
+  }
+}
+void launch_bsr_spmv(int64_t nrows, const int32_t* rowptr, const int32_t* col, const double* vals, const double* x,
+                     double* y, cudaStream_t st) {
+  count_launch();
+  k_bsr_spmv<<<grid_for(nrows), kThreads, 0, st>>>(nrows, rowptr, col, vals, x, y);
+}
+
 #define SFEM_INST_ELEM(T, M)                                                                                   \
   template void launch_element<T, M>(int, const ElemView<T>&, const T*, const T*, T*, Reduce, double*, int*, \
                                      const CgScalars*, cudaStream_t);
@@ -908,35 +1043,79 @@ __device__ __forceinline__ void load_elem(const PatchView<T>& pv, int64_t e, Ele
   d.scl = pv.scale_la ? pv.scale_la[e] : d.sc;
 }
 
-template <typename T, int MAT, int NT, bool DIR>
+// Neo-Hookean tangent factors per element for the cached Hessian-vector product: F^-T (9),
+// mu_e, lambda_e and c1 = mu_e - lambda_e log J, SoA cache[k E + e], k = 0..11 (one element pass
+// at the start of every Krylov solve; the product then needs neither u nor F).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_nh_cache(ElemView<T> ev, const T* __restrict__ u, T* __restrict__ c) {
+  const int64_t E = ev.E;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int4 t = ev.tets[e];
+    M3<T> X;
+#pragma unroll
+    for (int k = 0; k < 9; k++) X.a[k] = ev.X[k * E + e];
+    T mu = ev.mu, la = ev.lambda;
+    if (ev.scale) {
+      const T sc = ev.scale[e];
+      mu *= sc;
+      la *= ev.scale_la ? ev.scale_la[e] : sc;
+    }
+    M3<T> F = grad_of(u, t, X);
+    F.a[0] += T(1);
+    F.a[4] += T(1);
+    F.a[8] += T(1);
+    Tangent<T, kNeoHookean> tg;
+    tg.init(F, mu, la);
+#pragma unroll
+    for (int k = 0; k < 9; k++) c[k * E + e] = tg.Fit.a[k];
+    c[9 * E + e] = tg.mu;
+    c[10 * E + e] = tg.la;
+    c[11 * E + e] = tg.c1;
+  }
+}
+template <typename T>
+void launch_nh_cache(const ElemView<T>& ev, const T* u, T* cache, cudaStream_t st) {
+  count_launch();
+  k_nh_cache<T><<<grid_for(ev.E), kThreads, 0, st>>>(ev, u, cache);
+}
+template void launch_nh_cache<double>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template void launch_nh_cache<float>(const ElemView<float>&, const float*, float*, cudaStream_t);
+
+template <typename T, int MAT, int NT, bool DIR, bool CACHED>
 __global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __restrict__ u,
                                                   const T* __restrict__ p, T* __restrict__ q,
                                                   T* __restrict__ partial, Reduce red, CgScalars* s,
                                                   const T* __restrict__ r, const T* __restrict__ dinv,
-                                                  T* __restrict__ p_new) {
+                                                  T* __restrict__ p_new, const T* __restrict__ z) {
   if (s != nullptr && s->done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sfe = reinterpret_cast<T*>(smem_raw);  // kPatchElems * kFeStride
-  T* su = sfe + kPatchElems * kFeStride;    // kPatchNodes * 3
-  T* sp = su + kPatchNodes * 3;             // kPatchNodes * 3
+  T* su = sfe + kPatchElems * kFeStride;           // kPatchNodes * 3 (not with CACHED)
+  T* sp = CACHED ? su : su + kPatchNodes * 3;      // kPatchNodes * 3
   const int c = blockIdx.x;
   const int64_t eb = pv.elem_off[c], ne = pv.elem_off[c + 1] - eb;
   const int64_t nb = pv.node_off[c];
   const int nn = (int)(pv.node_off[c + 1] - nb);
   T beta = T(0);
-  if (DIR) beta = (T)s->beta;
+  bool use_z = false;  // flexible CG: p = z + beta p_old with z the preconditioner output
+  if (DIR) {
+    beta = (T)s->beta;
+    use_z = z != nullptr && s->jac == 0;
+  }
   for (int j = threadIdx.x; j < nn; j += NT) {
     int g = pv.pnode[nb + j];
     if (g < 0) g = ~g;
     const int64_t o = 3 * (int64_t)g;
-    su[3 * j] = u[o];
-    su[3 * j + 1] = u[o + 1];
-    su[3 * j + 2] = u[o + 2];
+    if (!CACHED) {
+      su[3 * j] = u[o];
+      su[3 * j + 1] = u[o + 1];
+      su[3 * j + 2] = u[o + 2];
+    }
     if (DIR) {
-      // zero at fixed nodes: r, dinv and p stay zero there
-      const T p0 = dinv[o] * r[o] + beta * p[o];
-      const T p1 = dinv[o + 1] * r[o + 1] + beta * p[o + 1];
-      const T p2 = dinv[o + 2] * r[o + 2] + beta * p[o + 2];
+      // zero at fixed nodes: r, dinv, z and p stay zero there
+      const T p0 = (use_z ? z[o] : dinv[o] * r[o]) + beta * p[o];
+      const T p1 = (use_z ? z[o + 1] : dinv[o + 1] * r[o + 1]) + beta * p[o + 1];
+      const T p2 = (use_z ? z[o + 2] : dinv[o + 2] * r[o + 2]) + beta * p[o + 2];
       sp[3 * j] = p0;
       sp[3 * j + 1] = p1;
       sp[3 * j + 2] = p2;
@@ -960,25 +1139,42 @@ __global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __re
     M3<T> X;
 #pragma unroll
     for (int q9 = 0; q9 < 9; q9++) X.a[q9] = cur.X[q9];
-    const T mu = pv.mu * cur.sc, la = pv.lambda * cur.scl;
-    M3<T> D, Dp;
+    M3<T> Dp;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const T a0 = su[3 * li.x + i], b0 = sp[3 * li.x + i];
-      D.a[3 * i] = su[3 * li.y + i] - a0;
-      D.a[3 * i + 1] = su[3 * li.z + i] - a0;
-      D.a[3 * i + 2] = su[3 * li.w + i] - a0;
+      const T b0 = sp[3 * li.x + i];
       Dp.a[3 * i] = sp[3 * li.y + i] - b0;
       Dp.a[3 * i + 1] = sp[3 * li.z + i] - b0;
       Dp.a[3 * i + 2] = sp[3 * li.w + i] - b0;
     }
-    M3<T> F = mul(D, X);
-    F.a[0] += T(1);
-    F.a[4] += T(1);
-    F.a[8] += T(1);
-    Tangent<T, MAT> tg;
-    tg.init(F, mu, la);
-    const M3<T> dP = tg.apply(mul(Dp, X));
+    M3<T> dP;
+    if constexpr (CACHED) {
+      Tangent<T, kNeoHookean> tg;
+      const int64_t e = eb + k;
+#pragma unroll
+      for (int q9 = 0; q9 < 9; q9++) tg.Fit.a[q9] = pv.nhc[q9 * pv.E + e];
+      tg.mu = pv.nhc[9 * pv.E + e];
+      tg.la = pv.nhc[10 * pv.E + e];
+      tg.c1 = pv.nhc[11 * pv.E + e];
+      dP = tg.apply(mul(Dp, X));
+    } else {
+      const T mu = pv.mu * cur.sc, la = pv.lambda * cur.scl;
+      M3<T> D;
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const T a0 = su[3 * li.x + i];
+        D.a[3 * i] = su[3 * li.y + i] - a0;
+        D.a[3 * i + 1] = su[3 * li.z + i] - a0;
+        D.a[3 * i + 2] = su[3 * li.w + i] - a0;
+      }
+      M3<T> F = mul(D, X);
+      F.a[0] += T(1);
+      F.a[4] += T(1);
+      F.a[8] += T(1);
+      Tangent<T, MAT> tg;
+      tg.init(F, mu, la);
+      dP = tg.apply(mul(Dp, X));
+    }
     T f[12];
     nodal_forces(dP, X, -cur.vol, f);
 #pragma unroll
@@ -1135,6 +1331,72 @@ __global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64
   }
 }
 
+// Flexible-CG update over nodes: q_g from q (owned) or its patch partials (shared), then
+// x += alpha p, rprev = r, r -= alpha q and r.r with the fixed-order last-block finish.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int64_t N,
+                                                               const int32_t* __restrict__ bidx, PatchBoundary pb,
+                                                               const T* __restrict__ partial, T* __restrict__ x,
+                                                               T* __restrict__ r, T* __restrict__ rprev,
+                                                               const T* __restrict__ p, const T* __restrict__ q,
+                                                               Reduce red, CgScalars* s) {
+  if (s->done) return;
+  const T a = (T)s->alpha;
+  T rr = T(0);
+  for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = 3 * g;
+    T qq[3];
+    const int b = bidx[g];
+    if (b < 0) {
+      qq[0] = q[o];
+      qq[1] = q[o + 1];
+      qq[2] = q[o + 2];
+    } else {
+      qq[0] = qq[1] = qq[2] = T(0);
+      const int t1 = pb.ptr[b + 1];
+      for (int t = pb.ptr[b]; t < t1; t++) {
+        qq[0] += partial[3 * (int64_t)t];
+        qq[1] += partial[3 * (int64_t)t + 1];
+        qq[2] += partial[3 * (int64_t)t + 2];
+      }
+    }
+#pragma unroll
+    for (int c2 = 0; c2 < 3; c2++) {
+      x[o + c2] += a * p[o + c2];
+      const T rp = r[o + c2];
+      rprev[o + c2] = rp;
+      const T rn = rp - a * qq[c2];
+      r[o + c2] = rn;
+      rr += rn * rn;
+    }
+  }
+  T v[1] = {rr}, tot[1];
+  if (reduce_last<T, 1>(v, red, tot) && threadIdx.x == 0) {
+    s->rr = (double)tot[0];
+    s->it += 1;
+    if (!isfinite(s->rr)) {
+      s->done = 1;
+      s->status = -3;
+    } else if (s->rr <= s->tol2) {
+      s->done = 1;
+    } else if (s->it >= s->max_it) {
+      s->done = 1;
+      s->status = 1;
+    }
+  }
+}
+
+template <typename T>
+void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
+                             T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st) {
+  count_launch();
+  k_fcg_update_patch<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, bidx, pb, partial, x, r, rprev, p, q, red,
+                                                                 s);
+}
+template void launch_fcg_update_patch<float>(int64_t, int64_t, const int32_t*, PatchBoundary, const float*, float*,
+                                             float*, float*, const float*, const float*, Reduce, CgScalars*,
+                                             cudaStream_t);
+
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st) {
@@ -1150,25 +1412,42 @@ template void launch_cg_update_patch<float>(int64_t, int64_t, const int32_t*, Pa
 
 template <typename T, int MAT>
 void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, const T* p, T* q, T* partial, Reduce red,
-                      CgScalars* s, cudaStream_t st, cudaEvent_t mid, const T* r, const T* dinv, T* p_new) {
+                      CgScalars* s, cudaStream_t st, cudaEvent_t mid, const T* r, const T* dinv, T* p_new,
+                      const T* z) {
   constexpr int NT = 256;
+  constexpr bool kNH = MAT == kNeoHookean;
+  const bool cached = kNH && pv.nhc != nullptr;
   constexpr size_t smem = sizeof(T) * (kPatchElems * kFeStride + kPatchNodes * 6);
+  constexpr size_t smem_c = sizeof(T) * (kPatchElems * kFeStride + kPatchNodes * 3);
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
-    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (kNH) {
+      cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false, kNH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem_c);
+      cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true, kNH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem_c);
+    }
     attr_set = true;
   }
+  const unsigned grid = (unsigned)pv.n_patches;
   count_launch();
   if (p_new != nullptr) {
     // Krylov iteration: the fused update (k_cg_update_patch) completes the shared nodes
-    k_patch_hvp<T, MAT, NT, true><<<(unsigned)pv.n_patches, NT, smem, st>>>(pv, u, p, q, partial, red, s, r, dinv,
-                                                                           p_new);
+    if (cached)
+      k_patch_hvp<T, MAT, NT, true, kNH><<<grid, NT, smem_c, st>>>(pv, u, p, q, partial, red, s, r, dinv, p_new, z);
+    else
+      k_patch_hvp<T, MAT, NT, true, false><<<grid, NT, smem, st>>>(pv, u, p, q, partial, red, s, r, dinv, p_new, z);
     if (mid) cudaEventRecord(mid, st);
     return;
   }
-  k_patch_hvp<T, MAT, NT, false><<<(unsigned)pv.n_patches, NT, smem, st>>>(pv, u, p, q, partial, red, s, nullptr,
-                                                                          nullptr, nullptr);
+  if (cached)
+    k_patch_hvp<T, MAT, NT, false, kNH><<<grid, NT, smem_c, st>>>(pv, u, p, q, partial, red, s, nullptr, nullptr,
+                                                                  nullptr, nullptr);
+  else
+    k_patch_hvp<T, MAT, NT, false, false><<<grid, NT, smem, st>>>(pv, u, p, q, partial, red, s, nullptr, nullptr,
+                                                                  nullptr, nullptr);
   if (mid) cudaEventRecord(mid, st);
   count_launch();
   k_patch_boundary<T><<<grid_for(pb.n), kThreads, 0, st>>>(pb, partial, q, s);
@@ -1176,7 +1455,7 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
 
 #define SFEM_INST_PATCH(T, M)                                                                                   \
   template void launch_patch_hvp<T, M>(const PatchView<T>&, PatchBoundary, const T*, const T*, T*, T*, Reduce, \
-                                       CgScalars*, cudaStream_t, cudaEvent_t, const T*, const T*, T*);
+                                       CgScalars*, cudaStream_t, cudaEvent_t, const T*, const T*, T*, const T*);
 SFEM_INST_PATCH(double, 0)
 SFEM_INST_PATCH(double, 1)
 SFEM_INST_PATCH(double, 2)

@@ -339,16 +339,27 @@ class FemPhysicsMatrixFree:
         nat.check(nat.load().sfem_kernel_launches(C.byref(n)))
         return n.value
 
-    def get_hessian(self):
-        """Dense tangent K over free DOFs, assembled column by column from GPU
-        matrix-vector products (small problems only)."""
+    def get_hessian_sparse(self):
+        """The assembled FP64 tangent over free DOFs (reshuffled order) as a scipy BSR matrix with
+        3 x 3 blocks (ElasticEnergy::AssembleStiffnessMatrix, assembled on the GPU)."""
+        import scipy.sparse as sp
+
+        nnzb = C.c_int64()
+        nat.check(self._lib.sfem_tangent_nnz(self._h, C.byref(nnzb)))
+        rowptr = np.zeros(self.n_free + 1, dtype=np.int32)
+        col = np.zeros(nnzb.value, dtype=np.int32)
+        vals = np.zeros((nnzb.value, 3, 3))
+        nat.check(self._lib.sfem_assemble_tangent(self._h, rowptr.ctypes.data_as(nat._ip),
+                                                  col.ctypes.data_as(nat._ip), _dp(vals)))
         n = 3 * self.n_free
-        if n > 12000:
-            raise ValueError("get_hessian is meant for small meshes (<= 4000 free nodes)")
-        K = np.zeros((n, n))
-        e = np.zeros(n)
-        for j in range(n):
-            e[j] = 1.0
-            K[:, j] = self.MatrixVectorMultiply(e).ravel()
-            e[j] = 0.0
-        return K
+        return sp.bsr_matrix((vals, col, rowptr), shape=(n, n))
+
+    def get_hessian(self):
+        """Dense tangent over free DOFs (what pysolidfem's get_hessian returns), from the GPU assembly."""
+        return self.get_hessian_sparse().toarray()
+
+    def tangent_matvec(self, d):
+        d = _f64(d).ravel()
+        out = np.zeros_like(d)
+        nat.check(self._lib.sfem_tangent_matvec(self._h, _dp(d), _dp(out)))
+        return out

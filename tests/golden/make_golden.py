@@ -22,7 +22,10 @@ Fixtures (npz):
                      ST_EXPLICIT (dt 0.01, 10 substeps) x 3 and ST_IMPLICIT with SolveNewtonLS
                      (dt 0.01, 1 substep) x 3 -> positions and velocities after each step.
 
-    python tests/golden/make_golden.py [--only dyn]
+  tangent_<mat>.npz  jittered 4x2x2 lattice at perturbed positions, each material: the reference's
+                     assembled tangent ElasticEnergy::AssembleStiffnessMatrix (dense, free DOFs).
+
+    python tests/golden/make_golden.py [--only dyn|tangent]
 """
 from __future__ import annotations
 
@@ -101,9 +104,25 @@ def dynamics():
     print("dyn: implicit tip after 3 steps", xs[-1][m.node_index(8, 2, 2)])
 
 
+def tangents():
+    m = box_lattice(4, 2, 2, extent=(1.0, 0.5, 0.5), jitter=0.15, seed=5)
+    fixed = m.face_nodes(0, 0)
+    for mat, name in MATS.items():
+        ref = RefHarness(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, -9.81, True, mat)
+        rng = np.random.default_rng(20 + mat)
+        x = ref.positions_shuffled() + rng.normal(size=(m.n_nodes, 3)) * 0.01
+        x[:ref.n_bcs] = ref.positions_shuffled()[:ref.n_bcs]
+        ref.set_positions_shuffled(x.ravel())
+        K = ref.assemble_dense()
+        np.savez_compressed(os.path.join(HERE, f"tangent_{name}.npz"), nodes=m.nodes, tets=m.tets, fixed=fixed,
+                            young=1e5, poisson=0.45, density=1070.0, material=mat, pos_shuffled=x,
+                            map=ref.reshuffle_map(), K=K)
+        print(f"tangent {name}: {K.shape}, |K| = {np.abs(K).max():.3e}, asym {np.abs(K - K.T).max():.2e}")
+
+
 def main():
-    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "dyn":
-        dynamics()
+    if "--only" in sys.argv:
+        {"dyn": dynamics, "tangent": tangents}[sys.argv[sys.argv.index("--only") + 1]]()
         return
     if not os.path.isdir(REF):
         sys.exit("reference tree not present; fixtures are generated in the development container")
@@ -169,6 +188,7 @@ def main():
                             eq_positions=ref.positions(), r0=r0, r_eq=rn, newton_iters=its)
         print(f"c2s {MATS[mat]}: its={its} |r0|={r0:.3e} |r|={rn:.3e}")
     dynamics()
+    tangents()
 
 
 if __name__ == "__main__":

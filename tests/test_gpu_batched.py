@@ -23,7 +23,7 @@ def test_batched_bodies_match_separate_solves():
     for k, sp in enumerate(specs):
         m = b.meshes[k]
         x = m.nodes.copy()
-        x[:, 1] += 0.05 * k  # the placement used in the batch (translation does not change the solution)
+        x[:, 1] += b.spacing * k  # the placement used in the batch (translation does not change the solution)
         p = FemPhysicsMatrixFree(m.tets, x, m.face_nodes(0, 0), young=sp.young, poisson=sp.poisson,
                                  density=1070.0, gravity=(0, 0, -9.81), material=3)
         s1 = p.newton_solve(rel_tol=1e-9, max_newton=100)
