@@ -119,6 +119,17 @@ def loads_for(m, seed):
     return random_top_traction(m, seed=seed)
 
 
+def dist_backend():
+    """NCCL between GPU ranks; gloo where no GPU is visible (the host-side tests of the
+    replica logic), or as SFEM_BENCH_BACKEND says."""
+    b = os.environ.get("SFEM_BENCH_BACKEND")
+    if b:
+        return b
+    import torch
+
+    return "nccl" if torch.cuda.is_available() else "gloo"
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -126,7 +137,8 @@ def dist_init():
     if world > 1:
         import torch.distributed as dist
 
-        dist.init_process_group("nccl")
+        if not dist.is_initialized():
+            dist.init_process_group(dist_backend())
     return rank, world, local
 
 
@@ -138,14 +150,22 @@ def barrier(world):
 
 
 def allmax(x, world):
+    """Maximum over ranks (the job's time is the slowest replica's)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_seeds(rank, warmup, steps):
+    """Load seeds of one replica: every rank solves its own loads (10000 + 1000 rank + i), so
+    N replicas do N times the work of one (weak scaling) with no data-path exchange."""
+    return [LOAD_SEED0 + rank * 1000 + i for i in range(warmup + steps)]
 
 
 # ---------------------------------------------------------------------------
@@ -215,7 +235,7 @@ def run_gpu_arm(args):
     if args.dims:
         dims = tuple(int(v) for v in args.dims.split(","))
     m, fixed = make_workload(dims)
-    seeds = [LOAD_SEED0 + rank * 1000 + i for i in range(args.warmup + args.steps)]
+    seeds = replica_seeds(rank, args.warmup, args.steps)
     loads = {s: loads_for(m, s) for s in seeds}
     kw = dict(young=YOUNG, poisson=POISSON, density=DENSITY, gravity=(0.0, 0.0, 0.0), material=3, device=local)
     solve_kw = dict(rel_tol=REL_TOL, max_newton=30, max_cg=200000)

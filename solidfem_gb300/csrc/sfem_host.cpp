@@ -294,14 +294,18 @@ int jacobi(sfem_handle* h, T* dinv, T* diag) {
   return 0;
 }
 
-// For a neo-Hookean handle, the tangent factors of the current state are computed once per
+// For a neo-Hookean FP64 solve, the tangent factors of the current state are computed once per
 // Krylov solve (k_nh_cache) and the patch product reads them instead of re-forming F, F^-1 and
 // log J per element and iteration; the guard switches the cache off when the solve returns.
+// FP64 element arithmetic is bound by the FP64 pipe, so trading it for 96 bytes per element pays
+// (measured: the FP64 Jacobi-PCG solve of the 6.3M-tet workload 35.5 s -> 23.4 s); the FP32
+// product is bound by latency and issue, and the extra bytes made it slower (95 -> 113 us per
+// 3.1M tets), so FP32 solves re-form the factors.
 template <typename T>
 struct NhCacheGuard {
   sfem_handle* h;
   NhCacheGuard(sfem_handle* hh, const T* u) : h(hh) {
-    if (h->material != SFEM_MMT_NEO_HOOKEAN) return;
+    if (h->material != SFEM_MMT_NEO_HOOKEAN || sizeof(T) != sizeof(double)) return;
     T** c = reinterpret_cast<T**>(sizeof(T) == 8 ? (void*)&h->nhc64 : (void*)&h->nhc32);
     if (!*c && dalloc(c, 12 * (size_t)h->E) != 0) return;  // without memory: the uncached product
     launch_nh_cache<T>(ev_of<T>(h), u, *c, h->stream);
