@@ -46,6 +46,17 @@ extern "C" {
 #define SFEM_MMT_STVK 1
 #define SFEM_MMT_COROTATIONAL 2
 #define SFEM_MMT_NEO_HOOKEAN 3
+/* the other MaterialModelType values (FemDataStructures.h:93-107), FP64 handles; their tangent is
+ * the reference's ElasticEnergy::ComputeLocalForceDifferential (ElasticEnergy.cpp:412-479) */
+#define SFEM_MMT_NEO_HOOKEAN_OGDEN 4
+#define SFEM_MMT_DISTORTIONAL_LINEAR 5
+#define SFEM_MMT_DISTORTIONAL_MOONEY 6
+#define SFEM_MMT_DISTORTIONAL_NH2 7
+#define SFEM_MMT_DISTORTIONAL_NH3 8
+#define SFEM_MMT_DISTORTIONAL_BW 9
+#define SFEM_MMT_DISTORTIONAL_OGDEN 10
+#define SFEM_MMT_DISTORTIONAL_NH6 11
+#define SFEM_MMT_DISTORTIONAL_NH7 12
 
 /* ---- precision of the element kernels and the inner Krylov solve ---- */
 #define SFEM_FP64 0

@@ -113,12 +113,17 @@ static void polar_qr(M3 F, M3* R, M3* U) {
 /* ---------------------------------------------------------------------- */
 /* Problem                                                                */
 /* ---------------------------------------------------------------------- */
-enum { MMT_LINEAR = 0, MMT_STVK = 1, MMT_COROTATIONAL = 2, MMT_NEO_HOOKEAN = 3 };
+/* MaterialModelType, Include/FemDataStructures.h:93-107 */
+enum {
+  MMT_LINEAR = 0, MMT_STVK = 1, MMT_COROTATIONAL = 2, MMT_NEO_HOOKEAN = 3, MMT_NEO_HOOKEAN_OGDEN = 4,
+  MMT_DISTORTIONAL_LINEAR = 5, MMT_DISTORTIONAL_MOONEY = 6, MMT_DISTORTIONAL_NH2 = 7, MMT_DISTORTIONAL_NH3 = 8,
+  MMT_DISTORTIONAL_BW = 9, MMT_DISTORTIONAL_OGDEN = 10, MMT_DISTORTIONAL_NH6 = 11, MMT_DISTORTIONAL_NH7 = 12
+};
 
 typedef struct {
   int n_nodes, n_tets, n_bcs, material;
   int tangent;       /* 0: the reference's force differential, 1: exact derivative of the force */
-  double mu, lambda, density, grav[3], force_fraction;
+  double mu, lambda, young, density, grav[3], force_fraction;
   int* map;          /* original -> reshuffled */
   int* tets;         /* reshuffled indices, 4 per element */
   double* X;         /* Dm^-1 per element, 9 (row-major) */
@@ -156,6 +161,7 @@ void* orc_create(const double* nodes, int n_nodes, const int* tets, int n_tets,
   orc_problem* p = (orc_problem*)calloc(1, sizeof(orc_problem));
   p->n_nodes = n_nodes; p->n_tets = n_tets; p->material = material;
   lame(young, poisson, &p->mu, &p->lambda);
+  p->young = young;
   p->density = density;
   for (int i = 0; i < 3; i++) p->grav[i] = gravity[i];
   p->force_fraction = 1.0;
@@ -266,6 +272,13 @@ static void elem_lame(const orc_problem* p, int e, double* mu, double* lambda) {
 
 /* ElasticEnergy::ComputeElementStress, Source/ElasticEnergy.cpp:114-257 (4 materials).
  * Pmu / Plambda are the mu- and lambda-parts for neo-Hookean (zero otherwise). */
+/* the float literals of the reference's formulas as they convert to its real type */
+#define C23 ((double)(2.0f / 3.0f))
+#define C13 ((double)(1.0f / 3.0f))
+
+/* E_e for the NH2 variant (the reference uses GetYoungsModulus(); per-element scales apply) */
+static double elem_young(const orc_problem* p, int e) { return p->escale ? p->young * p->escale[e] : p->young; }
+
 static M3 elem_stress(const orc_problem* p, int e, M3 F, M3* Pmu, M3* Plambda) {
   double mu, lambda;
   elem_lame(p, e, &mu, &lambda);
@@ -274,7 +287,7 @@ static M3 elem_stress(const orc_problem* p, int e, M3 F, M3* Pmu, M3* Plambda) {
   M3 R, U;
   if (p->material == MMT_COROTATIONAL) { polar_qr(F, &R, &U); F = U; }
   M3 strain;
-  if (p->material == MMT_LINEAR || p->material == MMT_COROTATIONAL)
+  if (p->material == MMT_LINEAR || p->material == MMT_COROTATIONAL || p->material == MMT_DISTORTIONAL_LINEAR)
     strain = m3_sub(m3_scale(0.5, m3_add(F, m3_tr(F))), id);
   else
     strain = m3_scale(0.5, m3_sub(m3_mul(m3_tr(F), F), id));
@@ -285,13 +298,42 @@ static M3 elem_stress(const orc_problem* p, int e, M3 F, M3* Pmu, M3* Plambda) {
       return m3_add(m3_scale(2 * mu, strain), m3_scale(lambda * m3_trace(strain), id));
     case MMT_COROTATIONAL:
       return m3_mul(R, m3_add(m3_scale(2 * mu, strain), m3_scale(lambda * m3_trace(strain), id)));
-    default: {
+    case MMT_NEO_HOOKEAN: {
       M3 Finv = m3_inv(F);
       double J = m3_det(F);
       M3 Finvtr = m3_tr(Finv);
       *Pmu = m3_sub(F, Finvtr);
       *Plambda = m3_scale(log(J), Finvtr);
       return m3_add(m3_scale(mu, *Pmu), m3_scale(lambda, *Plambda));
+    }
+    /* the other materials, ElasticEnergy.cpp:188-254 */
+    case MMT_DISTORTIONAL_LINEAR:
+      return m3_sub(m3_scale(2 * mu, strain), m3_scale((2 * mu / 3) * m3_trace(strain), id));
+    case MMT_DISTORTIONAL_MOONEY:
+      return m3_scale(mu, F);
+    case MMT_DISTORTIONAL_NH2:
+      return m3_scale(0.5 * elem_young(p, e), F);
+    case MMT_DISTORTIONAL_NH3:
+      return m3_scale(mu * pow(m3_det(F), -C23), F);
+    default: break;
+  }
+  M3 Finvtr = m3_tr(m3_inv(F));
+  double J = m3_det(F);
+  switch (p->material) {
+    case MMT_NEO_HOOKEAN_OGDEN:
+      return m3_add(m3_scale(mu, m3_sub(F, Finvtr)), m3_scale(lambda * (J - 1) * J, Finvtr));
+    case MMT_DISTORTIONAL_BW: {
+      double I1 = m3_trace(m3_mul(m3_tr(F), F));
+      return m3_scale(mu * pow(J, -C23), m3_sub(F, m3_scale(I1 / 3, Finvtr)));
+    }
+    case MMT_DISTORTIONAL_OGDEN:
+      *Pmu = m3_sub(F, Finvtr);
+      return m3_scale(mu, *Pmu);
+    case MMT_DISTORTIONAL_NH6:
+      return m3_scale(mu, m3_sub(F, m3_scale(J, Finvtr)));
+    default: { /* MMT_DISTORTIONAL_NH7 */
+      double lambda1 = -C23 * mu;
+      return m3_add(m3_scale(mu, m3_sub(F, Finvtr)), m3_scale(lambda1 * log(J), Finvtr));
     }
   }
 }
@@ -437,7 +479,7 @@ static M3 stress_diff(const orc_problem* p, int e, M3 F, M3 dF) {
       return m3_add(m3_mul(dF, m3_add(m3_scale(2 * mu, E), m3_scale(lambda * m3_trace(E), id))),
                     m3_mul(F, m3_add(m3_scale(2 * mu, dE), m3_scale(lambda * m3_trace(dE), id))));
     }
-    default: {
+    case MMT_NEO_HOOKEAN: {
       M3 Finv = m3_inv(F);
       M3 Finvtr = m3_tr(Finv);
       double J = m3_det(F);
@@ -445,6 +487,48 @@ static M3 stress_diff(const orc_problem* p, int e, M3 F, M3 dF) {
       M3 b = m3_mul(m3_mul(m3_scale(mu - lambda * log(J), Finvtr), m3_tr(dF)), Finvtr);
       M3 c = m3_scale(lambda * m3_trace(m3_mul(Finv, dF)), Finvtr);
       return m3_add(m3_add(a, b), c);
+    }
+    /* the other materials: ElasticEnergy::ComputeLocalForceDifferential (ElasticEnergy.cpp:412-479),
+     * the differential of the reference's assembled path (its matrix-free product covers only the
+     * four materials above) */
+    case MMT_DISTORTIONAL_LINEAR:
+      return m3_sub(m3_scale(mu, m3_add(dF, m3_tr(dF))), m3_scale(C23 * mu * m3_trace(dF), id));
+    case MMT_DISTORTIONAL_MOONEY:
+      return m3_scale(mu, dF);
+    case MMT_DISTORTIONAL_NH2:
+      return m3_scale(0.5 * elem_young(p, e), dF);
+    case MMT_DISTORTIONAL_NH3:
+      return m3_scale(mu * pow(m3_det(F), -C23), dF);
+    default: break;
+  }
+  M3 Finv = m3_inv(F);
+  M3 Finvtr = m3_tr(Finv);
+  double J = m3_det(F);
+  double trFd = m3_trace(m3_mul(Finv, dF));
+  switch (p->material) {
+    case MMT_NEO_HOOKEAN_OGDEN: {
+      M3 b = m3_mul(m3_mul(m3_scale(mu - lambda * (J - 1), Finvtr), m3_tr(dF)), Finvtr);
+      return m3_add(m3_add(m3_scale(mu, dF), b), m3_scale(lambda * J * trFd, Finvtr));
+    }
+    case MMT_DISTORTIONAL_BW: {
+      M3 C = m3_mul(m3_tr(F), F);
+      double I1 = m3_trace(C);
+      M3 Q = m3_sub(F, m3_scale(C13 * I1, Finvtr));
+      M3 dC = m3_add(m3_mul(m3_tr(dF), F), m3_mul(m3_tr(F), dF));
+      M3 inner = m3_sub(m3_scale(m3_trace(dC), Finvtr), m3_mul(m3_mul(m3_scale(I1, Finvtr), m3_tr(dF)), Finvtr));
+      M3 dQ = m3_sub(dF, m3_scale(C13, inner));
+      return m3_scale(mu * pow(J, -C23), m3_sub(dQ, m3_scale(C23 * trFd, Q)));
+    }
+    case MMT_DISTORTIONAL_OGDEN:
+      return m3_add(m3_scale(mu, dF), m3_mul(m3_mul(m3_scale(mu, Finvtr), m3_tr(dF)), Finvtr));
+    case MMT_DISTORTIONAL_NH6: {
+      M3 a = m3_add(m3_scale(mu, dF), m3_mul(m3_mul(m3_scale(mu * J, Finvtr), m3_tr(dF)), Finvtr));
+      return m3_sub(a, m3_scale(mu * J * trFd, Finvtr));
+    }
+    default: { /* MMT_DISTORTIONAL_NH7 */
+      double lambda1 = -C23 * mu;
+      M3 b = m3_mul(m3_mul(m3_scale(mu - lambda1 * log(J), Finvtr), m3_tr(dF)), Finvtr);
+      return m3_add(m3_add(m3_scale(mu, dF), b), m3_scale(lambda1 * trFd, Finvtr));
     }
   }
 }
@@ -576,19 +660,23 @@ static double elem_energy(const orc_problem* p, int e) {
   M3 F = def_grad(p, e), R, U;
   if (p->material == MMT_COROTATIONAL) { polar_qr(F, &R, &U); F = U; }
   M3 strain;
-  if (p->material == MMT_LINEAR || p->material == MMT_COROTATIONAL)
+  if (p->material == MMT_LINEAR || p->material == MMT_COROTATIONAL || p->material == MMT_DISTORTIONAL_LINEAR)
     strain = m3_sub(m3_scale(0.5, m3_add(F, m3_tr(F))), id);
   else
     strain = m3_scale(0.5, m3_sub(m3_mul(m3_tr(F), F), id));
-  double en;
-  if (p->material != MMT_NEO_HOOKEAN) {
+  double en = 0;  /* ElasticEnergy.cpp:69-108: the materials without an energy there report 0 */
+  if (p->material == MMT_LINEAR || p->material == MMT_COROTATIONAL || p->material == MMT_STVK) {
     double tr = m3_trace(strain);
     en = mu * m3_ddot(strain, strain) + 0.5 * lambda * tr * tr;
-  } else {
+  } else if (p->material == MMT_NEO_HOOKEAN || p->material == MMT_NEO_HOOKEAN_OGDEN ||
+             p->material == MMT_DISTORTIONAL_MOONEY || p->material == MMT_DISTORTIONAL_OGDEN) {
     double J = m3_det(F);
     double I1 = m3_trace(m3_mul(m3_tr(F), F));
     double lj = log(J);
-    en = 0.5 * mu * (I1 - 3) - mu * lj + 0.5 * lambda * lj * lj;
+    if (p->material == MMT_NEO_HOOKEAN) en = 0.5 * mu * (I1 - 3) - mu * lj + 0.5 * lambda * lj * lj;
+    else if (p->material == MMT_NEO_HOOKEAN_OGDEN) en = 0.5 * mu * (I1 - 3) - mu * lj + 0.5 * lambda * (J - 1) * (J - 1);
+    else if (p->material == MMT_DISTORTIONAL_MOONEY) en = 0.5 * mu * (I1 - 3);
+    else en = 0.5 * mu * (I1 - 3) - mu * lj;
   }
   return p->vol[e] * en;
 }

@@ -23,6 +23,11 @@ SFEM_ERR_BREAKDOWN = -6
 SFEM_ERR_NO_DEVICE = -7
 
 MMT_LINEAR, MMT_STVK, MMT_COROTATIONAL, MMT_NEO_HOOKEAN = 0, 1, 2, 3
+# the other MaterialModelType values (FemDataStructures.h:93-107; FP64 handles)
+(MMT_NEO_HOOKEAN_OGDEN, MMT_DISTORTIONAL_LINEAR, MMT_DISTORTIONAL_MOONEY, MMT_DISTORTIONAL_NH2, MMT_DISTORTIONAL_NH3,
+ MMT_DISTORTIONAL_BW, MMT_DISTORTIONAL_OGDEN, MMT_DISTORTIONAL_NH6, MMT_DISTORTIONAL_NH7) = range(4, 13)
+# materials whose reference energy is defined (ElasticEnergy.cpp:69-108): energy line searches apply
+MATERIALS_WITH_ENERGY = (0, 1, 2, 3, 4, 6, 10)
 FP64, FP32 = 0, 1
 PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
 SIM_EXPLICIT, SIM_IMPLICIT = 2, 3

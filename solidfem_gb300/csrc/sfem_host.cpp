@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <random>
 #include <cstdarg>
@@ -216,18 +217,46 @@ KrylovWs<double>& ws_of<double>(sfem_handle* h) { return h->k64; }
 template <>
 KrylovWs<float>& ws_of<float>(sfem_handle* h) { return h->k32; }
 
+// internal material id of the kernels: MaterialModelType 0..3, 4 = corotational with the exact
+// tangent, m + 1 for the other MaterialModelType values m = 4..12 (FP64 handles only)
+int mat_id(const sfem_handle* h) {
+  if (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) return 4;
+  return h->material <= 3 ? h->material : h->material + 1;
+}
+
+// call f(std::integral_constant<int, M>) for the handle's material id (variants in FP64 only)
+template <typename T, typename Fn>
+void with_mat(int mat, Fn&& f) {
+  switch (mat) {
+    case 0: f(std::integral_constant<int, 0>{}); return;
+    case 1: f(std::integral_constant<int, 1>{}); return;
+    case 2: f(std::integral_constant<int, 2>{}); return;
+    case 3: f(std::integral_constant<int, 3>{}); return;
+    case 4: f(std::integral_constant<int, 4>{}); return;
+    default: break;
+  }
+  if constexpr (sizeof(T) == sizeof(double)) {
+    switch (mat) {
+      case 5: f(std::integral_constant<int, 5>{}); return;
+      case 6: f(std::integral_constant<int, 6>{}); return;
+      case 7: f(std::integral_constant<int, 7>{}); return;
+      case 8: f(std::integral_constant<int, 8>{}); return;
+      case 9: f(std::integral_constant<int, 9>{}); return;
+      case 10: f(std::integral_constant<int, 10>{}); return;
+      case 11: f(std::integral_constant<int, 11>{}); return;
+      case 12: f(std::integral_constant<int, 12>{}); return;
+      default: f(std::integral_constant<int, 13>{}); return;
+    }
+  }
+}
+
 template <typename T>
 void element_pass(sfem_handle* h, int mode, const T* u, const T* p, T* fe, double* result, int* ninv,
                   const CgScalars* s) {
   const ElemView<T> ev = ev_of<T>(h);
-  const int mat = (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) ? 4 : h->material;
-  switch (mat) {
-    case 0: launch_element<T, 0>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
-    case 1: launch_element<T, 1>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
-    case 2: launch_element<T, 2>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
-    case 3: launch_element<T, 3>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
-    default: launch_element<T, 4>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream); break;
-  }
+  with_mat<T>(mat_id(h), [&](auto m) {
+    launch_element<T, decltype(m)::value>(mode, ev, u, p, fe, h->red(), result, ninv, s, h->stream);
+  });
 }
 
 // q = K p over the free DOFs with the fused patch kernel (+ p.q and alpha when s is given)
@@ -237,14 +266,10 @@ void hvp(sfem_handle* h, const T* u, const T* p, T* q, CgScalars* s, cudaEvent_t
   const ElemView<T> ev = ev_of<T>(h);
   const PatchView<T> pv = h->pv<T>(ev.X, ev.vol, ev.scale, ev.scale_la, ev.mu, ev.lambda);
   T* part = reinterpret_cast<T*>(h->partial);
-  const int mat = (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) ? 4 : h->material;
-  switch (mat) {
-    case 0: launch_patch_hvp<T, 0>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
-    case 1: launch_patch_hvp<T, 1>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
-    case 2: launch_patch_hvp<T, 2>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
-    case 3: launch_patch_hvp<T, 3>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
-    default: launch_patch_hvp<T, 4>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new, z); break;
-  }
+  with_mat<T>(mat_id(h), [&](auto m) {
+    launch_patch_hvp<T, decltype(m)::value>(pv, h->pb(), u, p, q, part, h->red(), s, h->stream, mid, r, dinv, p_new,
+                                            z);
+  });
 }
 
 // displacement in precision T for the element passes
@@ -560,7 +585,9 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   if (!nodes || !tets_in || !cfg || n_nodes <= 0 || n_tets <= 0 || (n_fixed > 0 && !fixed))
     return fail(SFEM_ERR_INVALID, "invalid arguments to sfem_create");
   if (n_nodes >= (1ll << 31) || n_tets >= (1ll << 29)) return fail(SFEM_ERR_INVALID, "mesh too large");
-  if (cfg->material < 0 || cfg->material > 3) return fail(SFEM_ERR_INVALID, "unsupported material %d", cfg->material);
+  if (cfg->material < 0 || cfg->material > 12) return fail(SFEM_ERR_INVALID, "unsupported material %d", cfg->material);
+  if (cfg->material > 3 && cfg->precision != SFEM_FP64)
+    return fail(SFEM_ERR_INVALID, "material %d is available in FP64 handles", cfg->material);
   if (cfg->precision != SFEM_FP64 && cfg->precision != SFEM_FP32)
     return fail(SFEM_ERR_INVALID, "unsupported precision %d", cfg->precision);
   for (int64_t i = 0; i < 4 * n_tets; i++)
@@ -907,14 +934,7 @@ static int bsr_assemble(sfem_handle* h) {
   double* Ke = nullptr;
   TRY(dalloc(&Ke, (size_t)h->E * 144));
   const ElemView<double> ev = h->ev64();
-  const int mat = (h->material == SFEM_MMT_COROTATIONAL && h->tangent == SFEM_TANGENT_EXACT) ? 4 : h->material;
-  switch (mat) {
-    case 0: launch_element_stiffness<0>(ev, h->u, Ke, h->stream); break;
-    case 1: launch_element_stiffness<1>(ev, h->u, Ke, h->stream); break;
-    case 2: launch_element_stiffness<2>(ev, h->u, Ke, h->stream); break;
-    case 3: launch_element_stiffness<3>(ev, h->u, Ke, h->stream); break;
-    default: launch_element_stiffness<4>(ev, h->u, Ke, h->stream); break;
-  }
+  with_mat<double>(mat_id(h), [&](auto m) { launch_element_stiffness<decltype(m)::value>(ev, h->u, Ke, h->stream); });
   CU(cudaMemsetAsync(h->bsr_vals, 0, 9 * (size_t)h->bsr_nnzb * sizeof(double), h->stream));
   launch_assemble_bsr(h->nbc, h->N, h->csr(), Ke, h->bsr_slot, h->bsr_dslot, h->dt > 0 ? h->mass : nullptr,
                       h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0, h->bsr_vals, h->stream);
@@ -1794,8 +1814,9 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
 int sfem_adjoint_dev(sfem_handle* h, const double* dLdu_dev, double rel_tol, int32_t max_cg, double* dLdE_dev,
                      double* dLdf_dev) {
   TRY(check_handle(h));
-  if (h->material == SFEM_MMT_COROTATIONAL)
-    return fail(SFEM_ERR_INVALID, "adjoint needs a symmetric tangent (the corotational force has none)");
+  if (h->material == SFEM_MMT_COROTATIONAL || h->material > 3)
+    return fail(SFEM_ERR_INVALID, "adjoint needs the consistent symmetric tangent of the linear, StVK or "
+                                  "neo-Hookean material");
   if (h->has_scale && h->has_scale_la)
     return fail(SFEM_ERR_INVALID, "dL/dE assumes a uniform Poisson ratio (per-element Lame parameters are set)");
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;

@@ -137,6 +137,79 @@ __device__ __forceinline__ void polar_qr(const M3<T>& F, M3<T>& R, M3<T>& U) {
 constexpr int kLinear = 0, kStvk = 1, kCorot = 2, kNeoHookean = 3;
 // corotational force with the exact derivative of that force as its tangent
 constexpr int kCorotExact = 4;
+// the other MaterialModelType values m = 4..12 (FemDataStructures.h:93-107) have the internal id
+// m + 1 (FP64 handles): neo-Hookean (Ogden), distortional linear, Mooney, NH2, NH3, Bonet-Wood,
+// distortional Ogden, NH6, NH7 (ElasticEnergy.cpp:188-254, 412-479)
+constexpr int kNhOgden = 5, kDistLinear = 6, kMooney = 7, kNh2 = 8, kNh3 = 9, kBonetWood = 10, kDistOgden = 11,
+              kNh6 = 12, kNh7 = 13;
+template <int MAT>
+__host__ __device__ constexpr bool is_variant() { return MAT >= kNhOgden; }
+
+// the float literals of the reference's formulas, as they convert to its real type
+template <typename T>
+__device__ __forceinline__ T c_two_thirds() { return T(2.0f / 3.0f); }
+template <typename T>
+__device__ __forceinline__ T c_third() { return T(1.0f / 3.0f); }
+template <typename T>
+__device__ __forceinline__ T dev_pow(T x, T y);
+template <>
+__device__ __forceinline__ double dev_pow<double>(double x, double y) { return pow(x, y); }
+template <>
+__device__ __forceinline__ float dev_pow<float>(float x, float y) { return powf(x, y); }
+
+// PK1 stress of the other materials, ElasticEnergy.cpp:188-254 (the reference's formulas)
+template <typename T, int MAT>
+__device__ __forceinline__ M3<T> variant_stress(const M3<T>& F, T mu, T la) {
+  M3<T> P;
+  if constexpr (MAT == kDistLinear) {  // 2 mu eps - (2 mu / 3) tr(eps) I, Cauchy strain eps
+    T tr = trace(F) - T(3);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        T eps = T(0.5) * (F.a[3 * i + j] + F.a[3 * j + i]) - (i == j ? T(1) : T(0));
+        P.a[3 * i + j] = (T(2) * mu) * eps - (i == j ? (T(2) * mu / T(3)) * tr : T(0));
+      }
+    return P;
+  }
+  if constexpr (MAT == kMooney || MAT == kNh2 || MAT == kNh3) {
+    T c = mu;
+    if (MAT == kNh2) c = T(0.5) * (mu * (T(3) * la + T(2) * mu) / (la + mu));  // 0.5 E
+    if (MAT == kNh3) c = mu * dev_pow<T>(det(F), -c_two_thirds<T>());
+#pragma unroll
+    for (int k = 0; k < 9; k++) P.a[k] = c * F.a[k];
+    return P;
+  }
+  const T J = det(F);
+  const M3<T> Fi = inverse(F);
+  M3<T> Fit;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) Fit.a[3 * i + j] = Fi.a[3 * j + i];
+  if constexpr (MAT == kBonetWood) {  // mu J^-2/3 (F - (I1 / 3) F^-T)
+    T I1 = 0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) I1 += F.a[k] * F.a[k];
+    const T c = mu * dev_pow<T>(J, -c_two_thirds<T>());
+#pragma unroll
+    for (int k = 0; k < 9; k++) P.a[k] = c * (F.a[k] - (I1 / T(3)) * Fit.a[k]);
+    return P;
+  }
+  if constexpr (MAT == kNh6) {  // mu (F - J F^-T)
+#pragma unroll
+    for (int k = 0; k < 9; k++) P.a[k] = mu * (F.a[k] - J * Fit.a[k]);
+    return P;
+  }
+  // mu (F - F^-T) + b F^-T: Ogden-Neo-Hookean b = lambda (J - 1) J, distortional Ogden b = 0,
+  // NH7 b = lambda1 log J with lambda1 = -2/3 mu
+  T b = T(0);
+  if constexpr (MAT == kNhOgden) b = la * (J - T(1)) * J;
+  if constexpr (MAT == kNh7) b = (-c_two_thirds<T>() * mu) * dev_log<T>(J);
+#pragma unroll
+  for (int k = 0; k < 9; k++) P.a[k] = mu * (F.a[k] - Fit.a[k]) + b * Fit.a[k];
+  return P;
+}
 
 // PK1 stress P(F), ElasticEnergy.cpp:132-187
 template <typename T, int MAT>
@@ -170,6 +243,8 @@ __device__ __forceinline__ M3<T> stress(const M3<T>& F, T mu, T la) {
 #pragma unroll
       for (int j = 0; j < 3; j++) S.a[3 * i + j] = mu * (C.a[3 * i + j] - (i == j ? T(1) : T(0))) + (i == j ? la * trE : T(0));
     P = mul(F, S);
+  } else if constexpr (is_variant<MAT>()) {
+    P = variant_stress<T, MAT>(F, mu, la);
   } else {
     T J;
     M3<T> Fi = inverse(F, &J);
@@ -185,6 +260,21 @@ __device__ __forceinline__ M3<T> stress(const M3<T>& F, T mu, T la) {
 // strain energy density, ElasticEnergy.cpp:52-109
 template <typename T, int MAT>
 __device__ __forceinline__ T energy_density(const M3<T>& F, T mu, T la) {
+  if constexpr (is_variant<MAT>()) {
+    // ElasticEnergy.cpp:87-108: only these variants have an energy; the others report 0
+    if constexpr (MAT == kNhOgden || MAT == kMooney || MAT == kDistOgden) {
+      const M3<T> C = mulTN(F, F);
+      const T I1 = trace(C);
+      T e = T(0.5) * mu * (I1 - T(3));
+      if constexpr (MAT != kMooney) {
+        const T J = det(F);
+        e -= mu * dev_log<T>(J);
+        if constexpr (MAT == kNhOgden) e += T(0.5) * la * (J - T(1)) * (J - T(1));
+      }
+      return e;
+    }
+    return T(0);
+  }
   if (MAT == kNeoHookean) {
     T J = det(F);
     T I1 = 0;
@@ -217,8 +307,85 @@ __device__ __forceinline__ T energy_density(const M3<T>& F, T mu, T la) {
 
 // Tangent dP(F; dF), FemPhysicsMatrixFree.cpp:436-470: init() once per element,
 // apply() per direction.
+
+// Tangents of the other materials: the reference's ElasticEnergy::ComputeLocalForceDifferential
+// (ElasticEnergy.cpp:412-479), which its assembled path uses (its matrix-free product covers only
+// the four main materials).  Written as dP = a dF + b dF^T + c tr(dF) I + d F^-T dF^T F^-T
+// + e tr(F^-1 dF) F^-T (+ the Bonet-Wood terms).
 template <typename T, int MAT>
-struct Tangent;
+struct Tangent {
+  static_assert(is_variant<MAT>(), "variant materials only");
+  M3<T> F, Fit;
+  T mu, la, J, I1, cj;
+  __device__ void init(const M3<T>& Fm, T m, T l) {
+    F = Fm;
+    mu = m;
+    la = l;
+    J = det(F);
+    const M3<T> Fi = inverse(F);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) Fit.a[3 * i + j] = Fi.a[3 * j + i];
+    I1 = 0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) I1 += F.a[k] * F.a[k];
+    cj = (MAT == kNh3 || MAT == kBonetWood) ? mu * dev_pow<T>(J, -c_two_thirds<T>()) : T(0);
+  }
+  __device__ M3<T> apply(const M3<T>& dF) const {
+    M3<T> P;
+    if constexpr (MAT == kDistLinear) {
+      const T tr = trace(dF);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+          P.a[3 * i + j] = mu * (dF.a[3 * i + j] + dF.a[3 * j + i]) - (i == j ? c_two_thirds<T>() * mu * tr : T(0));
+      return P;
+    }
+    if constexpr (MAT == kMooney || MAT == kNh2 || MAT == kNh3) {
+      T c = mu;
+      if (MAT == kNh2) c = T(0.5) * (mu * (T(3) * la + T(2) * mu) / (la + mu));
+      if (MAT == kNh3) c = cj;
+#pragma unroll
+      for (int k = 0; k < 9; k++) P.a[k] = c * dF.a[k];
+      return P;
+    }
+    const M3<T> B = mul(mulNT(Fit, dF), Fit);  // F^-T dF^T F^-T
+    T trFi = 0;                                // tr(F^-1 dF)
+#pragma unroll
+    for (int k = 0; k < 9; k++) trFi += Fit.a[k] * dF.a[k];
+    if constexpr (MAT == kBonetWood) {
+      T trdC = 0;  // tr(dF^T F + F^T dF)
+#pragma unroll
+      for (int k = 0; k < 9; k++) trdC += T(2) * dF.a[k] * F.a[k];
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        const T Q = F.a[k] - c_third<T>() * I1 * Fit.a[k];
+        const T dQ = dF.a[k] - c_third<T>() * (trdC * Fit.a[k] - I1 * B.a[k]);
+        P.a[k] = cj * (dQ - c_two_thirds<T>() * trFi * Q);
+      }
+      return P;
+    }
+    T cb = 0, ce = 0;
+    if constexpr (MAT == kNhOgden) {
+      cb = mu - la * (J - T(1));
+      ce = la * J;
+    } else if constexpr (MAT == kDistOgden) {
+      cb = mu;
+    } else if constexpr (MAT == kNh6) {
+      cb = mu * J;
+      ce = -mu * J;
+    } else if constexpr (MAT == kNh7) {
+      const T l1 = -c_two_thirds<T>() * mu;
+      cb = mu - l1 * dev_log<T>(J);
+      ce = l1;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) P.a[k] = mu * dF.a[k] + cb * B.a[k] + ce * trFi * Fit.a[k];
+    return P;
+  }
+};
 
 template <typename T>
 struct Tangent<T, kLinear> {
@@ -580,6 +747,12 @@ __global__ void __launch_bounds__(kThreads) k_element(ElemView<T> ev, const T* _
 #pragma unroll
           for (int j = 0; j < 3; j++)
             Pp.a[3 * i + j] = MODE == MODE_PMU ? F.a[3 * i + j] - Fi.a[3 * j + i] : lj * Fi.a[3 * j + i];
+      } else if (MAT == kDistOgden && MODE == MODE_PMU) {  // Pmu = F - F^-T (ElasticEnergy.cpp:239-245)
+        const M3<T> Fi = inverse(F);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) Pp.a[3 * i + j] = F.a[3 * i + j] - Fi.a[3 * j + i];
       }
       nodal_forces(Pp, X, -vol, f);
       store12(fe, e, f);
@@ -731,6 +904,16 @@ template void launch_element_stiffness<1>(const ElemView<double>&, const double*
 template void launch_element_stiffness<2>(const ElemView<double>&, const double*, double*, cudaStream_t);
 template void launch_element_stiffness<3>(const ElemView<double>&, const double*, double*, cudaStream_t);
 template void launch_element_stiffness<4>(const ElemView<double>&, const double*, double*, cudaStream_t);
+#define SFEM_INST_STIFF(M) template void launch_element_stiffness<M>(const ElemView<double>&, const double*, double*, cudaStream_t);
+SFEM_INST_STIFF(5)
+SFEM_INST_STIFF(6)
+SFEM_INST_STIFF(7)
+SFEM_INST_STIFF(8)
+SFEM_INST_STIFF(9)
+SFEM_INST_STIFF(10)
+SFEM_INST_STIFF(11)
+SFEM_INST_STIFF(12)
+SFEM_INST_STIFF(13)
 
 // Block-CSR assembly over free nodes, one thread per row in element order (deterministic):
 // vals[9 s] += K_e block (a, b) for every element entry (e, a) of the row's node and every
@@ -806,6 +989,15 @@ SFEM_INST_ELEM(double, 0)
 SFEM_INST_ELEM(double, 1)
 SFEM_INST_ELEM(double, 2)
 SFEM_INST_ELEM(double, 3)
+SFEM_INST_ELEM(double, 5)
+SFEM_INST_ELEM(double, 6)
+SFEM_INST_ELEM(double, 7)
+SFEM_INST_ELEM(double, 8)
+SFEM_INST_ELEM(double, 9)
+SFEM_INST_ELEM(double, 10)
+SFEM_INST_ELEM(double, 11)
+SFEM_INST_ELEM(double, 12)
+SFEM_INST_ELEM(double, 13)
 SFEM_INST_ELEM(float, 0)
 SFEM_INST_ELEM(float, 1)
 SFEM_INST_ELEM(float, 2)
@@ -1461,6 +1653,15 @@ SFEM_INST_PATCH(double, 1)
 SFEM_INST_PATCH(double, 2)
 SFEM_INST_PATCH(double, 3)
 SFEM_INST_PATCH(double, 4)
+SFEM_INST_PATCH(double, 5)
+SFEM_INST_PATCH(double, 6)
+SFEM_INST_PATCH(double, 7)
+SFEM_INST_PATCH(double, 8)
+SFEM_INST_PATCH(double, 9)
+SFEM_INST_PATCH(double, 10)
+SFEM_INST_PATCH(double, 11)
+SFEM_INST_PATCH(double, 12)
+SFEM_INST_PATCH(double, 13)
 SFEM_INST_PATCH(float, 0)
 SFEM_INST_PATCH(float, 1)
 SFEM_INST_PATCH(float, 2)

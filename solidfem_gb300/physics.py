@@ -265,7 +265,8 @@ class FemPhysicsMatrixFree:
         hyperelastic materials and residual-norm backtracking for corotational (whose force
         is not the gradient of an energy)."""
         if ls_condition is None:
-            nonconservative = self.material == nat.MMT_COROTATIONAL or getattr(self, "_has_pressure", False)
+            nonconservative = (self.material == nat.MMT_COROTATIONAL or getattr(self, "_has_pressure", False)
+                               or self.material not in nat.MATERIALS_WITH_ENERGY)
             ls_condition = nat.LSC_RESIDUAL if nonconservative else nat.LSC_ARMIJO
         o = nat.NewtonOpts(rel_tol=rel_tol, abs_tol=abs_tol, max_newton=max_newton, max_cg=max_cg, eta_max=eta_max,
                            eta_min=eta_min, precond=precond, ls_condition=ls_condition,
@@ -285,7 +286,8 @@ class FemPhysicsMatrixFree:
             nat.check(self._lib.sfem_step(self._h, float(dt), nat.SIM_EXPLICIT, int(substeps), None, None))
             return dict(status=0)
         kw = dict(rel_tol=1e-8, abs_tol=0.0, max_newton=50, max_cg=100000, precond=nat.PC_JACOBI,
-                  ls_condition=nat.LSC_RESIDUAL if self.material == nat.MMT_COROTATIONAL else nat.LSC_ARMIJO,
+                  ls_condition=nat.LSC_ARMIJO if (self.material in nat.MATERIALS_WITH_ENERGY
+                                                  and self.material != nat.MMT_COROTATIONAL) else nat.LSC_RESIDUAL,
                   eta_max=0.5, eta_min=0.0, load_steps=1, verbose=0, max_bisection=0)
         kw.update(newton_kw)
         o = nat.NewtonOpts(**kw)

@@ -21,7 +21,12 @@ ST_STATIC, ST_QUASI_STATIC, ST_EXPLICIT, ST_IMPLICIT = 0, 1, 2, 3
 NST_NEWTON, NST_NEWTON_LS, NST_NEWTON_CG, NST_NONLINEAR_CG = 0, 1, 2, 3
 
 _MATERIALS = {"linear": nat.MMT_LINEAR, "stvk": nat.MMT_STVK, "corotational": nat.MMT_COROTATIONAL,
-              "neo-hookean": nat.MMT_NEO_HOOKEAN, "neohookean": nat.MMT_NEO_HOOKEAN}
+              "neo-hookean": nat.MMT_NEO_HOOKEAN, "neohookean": nat.MMT_NEO_HOOKEAN,
+              "neo-hookean-ogden": nat.MMT_NEO_HOOKEAN_OGDEN, "distortional-linear": nat.MMT_DISTORTIONAL_LINEAR,
+              "distortional-mooney": nat.MMT_DISTORTIONAL_MOONEY, "distortional-nh2": nat.MMT_DISTORTIONAL_NH2,
+              "distortional-nh3": nat.MMT_DISTORTIONAL_NH3, "distortional-bw": nat.MMT_DISTORTIONAL_BW,
+              "distortional-ogden": nat.MMT_DISTORTIONAL_OGDEN, "distortional-nh6": nat.MMT_DISTORTIONAL_NH6,
+              "distortional-nh7": nat.MMT_DISTORTIONAL_NH7}
 
 
 class NonlinearFEM:

@@ -24,8 +24,10 @@ Fixtures (npz):
 
   tangent_<mat>.npz  jittered 4x2x2 lattice at perturbed positions, each material: the reference's
                      assembled tangent ElasticEnergy::AssembleStiffnessMatrix (dense, free DOFs).
+  variant_<m>.npz    the same lattice for the other MaterialModelType values m = 4..12: stress,
+                     gradients, energy, tangent diagonal and assembled tangent from the reference.
 
-    python tests/golden/make_golden.py [--only dyn|tangent]
+    python tests/golden/make_golden.py [--only dyn|tangent|variant]
 """
 from __future__ import annotations
 
@@ -120,9 +122,27 @@ def tangents():
         print(f"tangent {name}: {K.shape}, |K| = {np.abs(K).max():.3e}, asym {np.abs(K - K.T).max():.2e}")
 
 
+def variants():
+    m = box_lattice(4, 2, 2, extent=(1.0, 0.5, 0.5), jitter=0.15, seed=5)
+    fixed = m.face_nodes(0, 0)
+    for mat in range(4, 13):
+        ref = RefHarness(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, -9.81, True, mat)
+        ref.set_force_fraction(1.0)
+        rng = np.random.default_rng(40 + mat)
+        x = ref.positions_shuffled() + rng.normal(size=(m.n_nodes, 3)) * 0.01
+        x[:ref.n_bcs] = ref.positions_shuffled()[:ref.n_bcs]
+        ref.set_positions_shuffled(x.ravel())
+        np.savez_compressed(os.path.join(HERE, f"variant_{mat}.npz"), nodes=m.nodes, tets=m.tets, fixed=fixed,
+                            young=1e5, poisson=0.45, density=1070.0, gravity=np.array([0.0, 0.0, -9.81]),
+                            material=mat, pos_shuffled=x, map=ref.reshuffle_map(), stress=ref.element_stress(),
+                            grad=ref.gradients(), energy=ref.elastic_energy(), diag=ref.jacobi_diagonal(),
+                            K=ref.assemble_dense())
+        print(f"variant {mat}: |grad| {np.linalg.norm(ref.gradients()):.3e} energy {ref.elastic_energy():.3e}")
+
+
 def main():
     if "--only" in sys.argv:
-        {"dyn": dynamics, "tangent": tangents}[sys.argv[sys.argv.index("--only") + 1]]()
+        {"dyn": dynamics, "tangent": tangents, "variant": variants}[sys.argv[sys.argv.index("--only") + 1]]()
         return
     if not os.path.isdir(REF):
         sys.exit("reference tree not present; fixtures are generated in the development container")
@@ -189,6 +209,7 @@ def main():
         print(f"c2s {MATS[mat]}: its={its} |r0|={r0:.3e} |r|={rn:.3e}")
     dynamics()
     tangents()
+    variants()
 
 
 if __name__ == "__main__":

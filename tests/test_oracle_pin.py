@@ -129,3 +129,25 @@ def test_dynamics_golden_is_consistent_with_the_oracle():
         for _ in range(int(g["explicit_substeps"])):
             o2.explicit_substep(dt / int(g["explicit_substeps"]))
         np.testing.assert_allclose(o2.positions(), g["explicit_positions"][k], rtol=0, atol=1e-14)
+
+
+# ---- the other MaterialModelType values (ElasticEnergy.cpp:40-112, 188-254, 412-479) ----
+@pytest.mark.skipif(not RefHarness.available(), reason="reference not built here")
+@pytest.mark.parametrize("mat", list(range(4, 13)))
+def test_variant_materials_bit_identical_to_reference(mat):
+    m = box_lattice(4, 2, 2, extent=(1.0, 0.5, 0.5), jitter=0.15, seed=5)
+    fixed = m.face_nodes(0, 0)
+    ref = RefHarness(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, -9.81, True, mat)
+    orc = Oracle(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, (0, 0, -9.81), mat)
+    ref.set_force_fraction(1.0)
+    rng = np.random.default_rng(mat)
+    x = ref.positions_shuffled() + rng.normal(size=(m.n_nodes, 3)) * 0.01
+    x[:ref.n_bcs] = ref.positions_shuffled()[:ref.n_bcs]
+    ref.set_positions_shuffled(x.ravel())
+    orc.set_positions_shuffled(x)
+    np.testing.assert_array_equal(orc.element_stress().ravel(), ref.element_stress().ravel())
+    np.testing.assert_array_equal(orc.gradients(), ref.gradients())
+    assert orc.elastic_energy() == ref.elastic_energy()
+    np.testing.assert_array_equal(orc.jacobi_diagonal(), ref.jacobi_diagonal())
+    for a, b in zip(orc.force_param_grads(), ref.force_param_grads()):
+        np.testing.assert_array_equal(a, b)
