@@ -35,6 +35,7 @@ struct Graph {
   const int32_t* ptr;     // n + 1
   const int32_t* idx;     // neighbours (free-node indices)
   const float* inv_deg;   // 1 / max(deg, 1)
+  const int16_t* d16;     // the same neighbours as j - i when every |j - i| < 2^15 (else null)
 };
 
 

@@ -645,10 +645,11 @@ __device__ __forceinline__ void node_gather(const Graph& g, int64_t i, const flo
     const int64_t j = 3 * (int64_t)jn + c;
     return FIRST ? r[j] * sqrtf(dinv[j]) : v[j];
   };
+  const int ii = (int)i;
   for (; e + 4 <= p1; e += 4) {
     int jn[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) jn[u] = g.idx[e + u];
+    for (int u = 0; u < 4; u++) jn[u] = g.d16 ? ii + (int)g.d16[e + u] : g.idx[e + u];
     float x[4][3], wg[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
@@ -662,7 +663,7 @@ __device__ __forceinline__ void node_gather(const Graph& g, int64_t i, const flo
       for (int c = 0; c < 3; c++) a[c] += wg[u] * x[u][c];
   }
   for (; e < p1; e++) {
-    const int jn = g.idx[e];
+    const int jn = g.d16 ? ii + (int)g.d16[e] : g.idx[e];
     const float wg = TRANS ? g.inv_deg[jn] : 1.f;
 #pragma unroll
     for (int c = 0; c < 3; c++) a[c] += wg * val(jn, c);

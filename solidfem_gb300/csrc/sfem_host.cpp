@@ -128,6 +128,7 @@ struct sfem_handle {
   std::vector<int32_t> perm_h;
   int32_t* perm = nullptr;
   int64_t n_patches = 0, n_slots = 0, n_shared = 0;
+  int max_pnodes = 0;  // largest node count of a patch
   int64_t *elem_off = nullptr, *node_off = nullptr;
   int32_t *pnode = nullptr, *pdest = nullptr, *bnode = nullptr, *bptr = nullptr, *bidx = nullptr;
   uint16_t *lptr = nullptr, *lent = nullptr;
@@ -171,7 +172,7 @@ struct sfem_handle {
     const T* nhc = nullptr;
     if (nhc_on) nhc = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)nhc64 : (const void*)nhc32);
     return PatchView<T>{elem_off, node_off, pnode, pdest, lptr, lent, lidx, X, vol, scale, scale_la, E, n_patches,
-                        nbc, m, l, pm, nhc};
+                        nbc, m, l, pm, nhc, max_pnodes};
   }
   NodeCsr csr() const { return NodeCsr{csr_ptr, csr_ent}; }
   ElemView<double> ev64() const {
@@ -423,6 +424,7 @@ struct PatchBuild {
   std::vector<int32_t> pnode, pdest, bnode, bptr;
   std::vector<uint16_t> lptr, lent;
   std::vector<ushort4> lidx;
+  int max_nodes = 0;
 };
 
 uint32_t spread3(uint32_t v) {  // 10 bits -> every third bit
@@ -516,6 +518,7 @@ void build_patches(const std::vector<int4>& tt, const std::vector<double>& x0, i
       const unsigned short li[4] = {l.x, l.y, l.z, l.w};
       for (int j = 0; j < 4; j++) pb.lent[4 * e0 + fill[li[j]]++] = (uint16_t)(kFeStride * i + 3 * j);
     }
+    pb.max_nodes = std::max<int>(pb.max_nodes, (int)nn);
     for (size_t j = 0; j <= nn; j++) pb.lptr.push_back(deg[j]);
     for (size_t j = 0; j < nn; j++) pb.pnode.push_back(nodes[j]);
     pb.elem_off.push_back((int64_t)k);
@@ -699,6 +702,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   h->perm_h = pbld.perm;
   h->n_patches = (int64_t)pbld.elem_off.size() - 1;
   h->n_slots = (int64_t)pbld.pnode.size();
+  h->max_pnodes = std::max(pbld.max_nodes, 1);
   h->n_shared = (int64_t)pbld.bnode.size();
 
   // ---- node -> element CSR (entries in element order) ----
@@ -1908,13 +1912,14 @@ struct GnnState {
   float* bpart = nullptr;  // block partials of the fused beta pass (4 per 256 nodes)
   int adam_t = 0;
   bool train_bufs = false;
-  gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg}; }
+  int16_t* d16 = nullptr;  // neighbour deltas (polynomial passes), when they fit
+  gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg, d16}; }
 };
 
 void gnn_free(GnnState* g) {
   void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->params, g->grad, g->m, g->v, g->Wb, g->x, g->xg,
                   g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->losses, g->z, g->rprev, g->tmp,
-                  g->py1, g->py2, g->pw, g->bpart};
+                  g->py1, g->py2, g->pw, g->bpart, g->d16};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int l = 0; l <= gnn::NL; l++) {
@@ -2229,6 +2234,18 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   for (int64_t i = 0; i < n; i++) ptr[i + 1] += ptr[i];
   std::vector<float> invdeg((size_t)n);
   for (int64_t i = 0; i < n; i++) invdeg[i] = 1.f / (float)std::max(1, ptr[i + 1] - ptr[i]);
+  // 16-bit neighbour deltas halve the index traffic of the polynomial passes when they fit
+  std::vector<int16_t> d16(idx.size());
+  bool fits16 = true;
+  for (int64_t i = 0; i < n && fits16; i++)
+    for (int32_t k = ptr[i]; k < ptr[i + 1]; k++) {
+      const int64_t dlt = (int64_t)idx[k] - i;
+      if (dlt < -32768 || dlt > 32767) {
+        fits16 = false;
+        break;
+      }
+      d16[k] = (int16_t)dlt;
+    }
   // seeded normal weights; log c = 0
   std::vector<float> prm(gnn::NPARAM, 0.f);
   std::mt19937_64 rng(seed);
@@ -2260,6 +2277,10 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   if (!idx.empty())
     CU(cudaMemcpyAsync(g->idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemcpyAsync(g->inv_deg, invdeg.data(), invdeg.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  if (fits16 && !d16.empty()) {
+    TRY(dalloc(&g->d16, d16.size()));
+    CU(cudaMemcpyAsync(g->d16, d16.data(), d16.size() * sizeof(int16_t), cudaMemcpyHostToDevice, h->stream));
+  }
   CU(cudaMemcpyAsync(g->params, prm.data(), prm.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(g->m, 0, gnn::NPARAM * sizeof(float), h->stream));
   CU(cudaMemsetAsync(g->v, 0, gnn::NPARAM * sizeof(float), h->stream));

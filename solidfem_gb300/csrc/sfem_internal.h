@@ -89,6 +89,7 @@ struct PatchView {
   T mu, lambda;
   const T* pm;   // implicit dynamics: per slot m_g / (h^2 * patches sharing g), else nullptr
   const T* nhc;  // neo-Hookean tangent cache (k_nh_cache, 12 E values) valid for this solve, or nullptr
+  int max_nodes;  // the largest node count of a patch (sizes the shared-memory node arrays)
 };
 
 // Implicit-dynamics terms of the residual (FemPhysicsMatrixFree::ComputeGradients :546-557):

@@ -1281,9 +1281,9 @@ __global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __re
                                                   T* __restrict__ p_new, const T* __restrict__ z) {
   if (s != nullptr && s->done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sfe = reinterpret_cast<T*>(smem_raw);  // kPatchElems * kFeStride
-  T* su = sfe + kPatchElems * kFeStride;           // kPatchNodes * 3 (not with CACHED)
-  T* sp = CACHED ? su : su + kPatchNodes * 3;      // kPatchNodes * 3
+  T* sfe = reinterpret_cast<T*>(smem_raw);         // kPatchElems * kFeStride
+  T* su = sfe + kPatchElems * kFeStride;           // max_nodes * 3 (not with CACHED)
+  T* sp = CACHED ? su : su + pv.max_nodes * 3;     // max_nodes * 3
   const int c = blockIdx.x;
   const int64_t eb = pv.elem_off[c], ne = pv.elem_off[c + 1] - eb;
   const int64_t nb = pv.node_off[c];
@@ -1609,17 +1609,17 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
   constexpr int NT = 256;
   constexpr bool kNH = MAT == kNeoHookean;
   const bool cached = kNH && pv.nhc != nullptr;
-  constexpr size_t smem = sizeof(T) * (kPatchElems * kFeStride + kPatchNodes * 6);
-  constexpr size_t smem_c = sizeof(T) * (kPatchElems * kFeStride + kPatchNodes * 3);
+  constexpr size_t smem_max = sizeof(T) * (kPatchElems * kFeStride + kPatchNodes * 6);
+  const size_t smem = sizeof(T) * (kPatchElems * kFeStride + (size_t)pv.max_nodes * 6);
+  const size_t smem_c = sizeof(T) * (kPatchElems * kFeStride + (size_t)pv.max_nodes * 3);
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
-    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int mx = (int)smem_max;
+    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     if (kNH) {
-      cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false, kNH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem_c);
-      cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true, kNH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem_c);
+      cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, false, kNH>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+      cudaFuncSetAttribute(k_patch_hvp<T, MAT, NT, true, kNH>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     }
     attr_set = true;
   }
