@@ -28,8 +28,8 @@ def slab_mesh(nx, ny, nz, jitter=0.2, seed=0):
     return box_lattice(nx, ny, nz, extent=(nx / 64.0, ny / 64.0, nz / 64.0), jitter=jitter, seed=seed)
 
 
-def train(dims=(64, 16, 16), seeds=64, every=25, max_snaps=40, steps=2000, lr=1e-3, init_seed=0, verbose=True,
-          loss="energy", batch=8):
+def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1e-3, init_seed=0, verbose=True,
+          loss="energy", batch=16):
     m = slab_mesh(*dims)
     fixed = m.face_nodes(2, 0)
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
@@ -58,11 +58,11 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--dims", default="64,16,16")
-    ap.add_argument("--seeds", type=int, default=64)
+    ap.add_argument("--seeds", type=int, default=128)
     ap.add_argument("--every", type=int, default=25)
     ap.add_argument("--max-snaps", type=int, default=40)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=6000)
+    ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--loss", default="energy", choices=["energy", "residual"])
     a = ap.parse_args()
