@@ -52,6 +52,9 @@ WORKLOAD = ("256x64x64 hexes x 6 tets (1,085,825 nodes / 6,291,456 tets), jitter
 FP64_JACOBI_COUNTS = {"newton_iters": 5, "cg_iters": 10166, "residual_evals": 6}
 
 
+HVP_DRAM_BYTES_PER_TET = 220.1e6 / 3145728  # k_patch_hvp<float, NH, DIR> (ncu, see the traffic note below)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -335,7 +338,10 @@ def run_gpu_arm(args):
     pk, pk_kind = peaks()
     ms = prof["hvp_elem_ms"] / max(prof["samples"], 1)
     achieved = prof["algo_bytes_hvp"] / (ms * 1e-3) / 1e9 if prof["samples"] else None
-    traffic = args.traffic if args.traffic else None
+    # DRAM bytes of one patch-product launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum on a
+    # 3,145,728-tet case of the same kernel (220.1 MB per launch, profiles/patch_hvp_fp32_c3.md), scaled
+    # by the tet count (the element data streams once per launch, far above L2 in both cases)
+    traffic = args.traffic if args.traffic else HVP_DRAM_BYTES_PER_TET * m.n_tets
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -359,7 +365,9 @@ def run_gpu_arm(args):
                          "frac": achieved / pk if achieved else None, "traffic": traffic,
                          "kernel": "k_patch_hvp<float, neo-Hookean> (fused element Hessian-vector product)",
                          "algo_bytes_per_launch": prof["algo_bytes_hvp"], "ms_per_launch": ms,
-                         "peak_source": pk_kind},
+                         "peak_source": pk_kind,
+                         "traffic_source": "ncu capture at 3,145,728 tets scaled by the tet count"
+                         if not args.traffic else "--traffic"},
             "e2e": {"value": e2e_t, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(),
             "gpu_launches": launches,

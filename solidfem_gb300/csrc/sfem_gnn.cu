@@ -78,17 +78,20 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
                        float* w, float* out, const int* done, cudaStream_t st, const float* rprev, float* partials,
-                       unsigned* counter, CgScalars* s) {
+                       unsigned* counter, CgScalars* s, const float* xs) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
   const int64_t n3 = 3 * g.n;
   // one node per thread; the partials of the BETA pass hold 4 values per block
   const int grid = blocks_for(g.n, 256);
   count_launch();
-  k_poly_fwd<true><<<grid, 256, 0, st>>>(g, r, dinv, nullptr, y1, done);
+  if (xs)  // x = D^-1/2 r already formed (by the flexible-CG update)
+    k_poly_fwd<false><<<grid, 256, 0, st>>>(g, r, dinv, xs, y1, done);
+  else
+    k_poly_fwd<true><<<grid, 256, 0, st>>>(g, r, dinv, nullptr, y1, done);
   count_launch();
   k_poly_fwd<false><<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, done);
   count_launch();
-  k_poly_mid<<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, pc, w, done);
+  k_poly_mid<<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, pc, w, done, xs);
   // Horner in A^T: u = w3 -> A^T u + w2 (into y1) -> A^T u + w1 (into y2) -> out
   count_launch();
   k_poly_bwd<false, false><<<grid, 256, 0, st>>>(g, w + 3 * n3, w + 2 * n3, r, dinv, 0.f, y1, done, nullptr, nullptr,
@@ -189,6 +192,18 @@ void launch_pack(const float* prm, __nv_bfloat16* Wb, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 namespace sfem {
 namespace gnn {
+
+// xs = r D^-1/2 (the input of the polynomial passes), elementwise
+__global__ void k_scale_sqrt(int64_t n, const float* __restrict__ r, const float* __restrict__ dinv,
+                             float* __restrict__ xs) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    xs[i] = r[i] * sqrtf(dinv[i]);
+}
+void launch_scale_sqrt(int64_t n, const float* r, const float* dinv, float* xs, cudaStream_t st) {
+  int grid = (int)std::min<int64_t>((n + 255) / 256, 2048);
+  count_launch();
+  k_scale_sqrt<<<grid < 1 ? 1 : grid, 256, 0, st>>>(n, r, dinv, xs);
+}
 
 // d = a - b
 __global__ void k_sub(int64_t n, const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ d) {

@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float* __restri
 __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restrict__ r,
                                                   const float* __restrict__ dinv, const float* __restrict__ y1,
                                                   const float* __restrict__ y2, PolyCoef pc, float* __restrict__ w,
-                                                  const int* done) {
+                                                  const int* done, const float* __restrict__ xs) {
   if (done && *done) return;
   const int64_t n3 = 3 * g.n;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restri
     float y[NL + 1][3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      y[0][c] = r[o + c] * sqrtf(dinv[o + c]);
+      y[0][c] = xs ? xs[o + c] : r[o + c] * sqrtf(dinv[o + c]);
       y[1][c] = y1[o + c];
       y[2][c] = y2[o + c];
       y[3][c] = a[c] * id;

@@ -2103,16 +2103,19 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   const int* done = &h->scal->done;
   float* part = reinterpret_cast<float*>(h->partials);
   const float* dinv = w.dinv + o;
+  float* xs = g->infer_mode == 0 ? g->tmp : nullptr;  // D^-1/2 r, formed by the update kernel (3N)
   auto precondition = [&](bool with_beta) {
     if (g->infer_mode == 0) {
       gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->py1, g->py2, g->pw, g->z + o, done, h->stream,
-                             with_beta ? g->rprev + o : nullptr, g->bpart, h->counter, with_beta ? h->scal : nullptr);
+                             with_beta ? g->rprev + o : nullptr, g->bpart, h->counter, with_beta ? h->scal : nullptr,
+                             xs + o);
     } else {
       gnn::launch_apply(g->graph(), w.r + o, dinv, g->params, g->Wb, g->h, g->z + o, done, h->stream);
       if (with_beta)
         gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, dinv, part, h->counter, h->scal, h->stream);
     }
   };
+  if (xs) gnn::launch_scale_sqrt(n, w.r + o, dinv, xs + o, h->stream);
   precondition(false);
   gnn::launch_fcg_init(n, w.r + o, g->z + o, w.p + o, part, h->counter, h->scal, h->stream);  // p_old = 0
   float* pbuf[2] = {w.p, w.p2};
@@ -2145,7 +2148,7 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
       }
       if (h->profiling) h->prof_launches++;
       launch_fcg_update_patch<float>(h->nbc, h->N, h->bidx, h->pb(), reinterpret_cast<const float*>(h->partial), x,
-                                     w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream);
+                                     w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream, xs ? w.dinv : nullptr, xs);
       precondition(true);
     }
   }

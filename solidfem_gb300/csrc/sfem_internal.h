@@ -144,7 +144,8 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
 // node's position in the shared-node list or -1)
 template <typename T>
 void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
-                             T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st);
+                             T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
+                             const T* dinv = nullptr, T* xs = nullptr);
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
@@ -244,7 +245,10 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 // With s (flexible CG), the last pass also forms the Polak-Ribiere beta from r, rprev (k_fcg_beta).
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
                        float* w, float* out, const int* done, cudaStream_t st, const float* rprev = nullptr,
-                       float* partials = nullptr, unsigned* counter = nullptr, CgScalars* s = nullptr);
+                       float* partials = nullptr, unsigned* counter = nullptr, CgScalars* s = nullptr,
+                       const float* xs = nullptr);
+// xs = r D^-1/2 elementwise
+void launch_scale_sqrt(int64_t n, const float* r, const float* dinv, float* xs, cudaStream_t st);
 // the same M(r) keeping the activations h0..h3 of S and x = D^-1/2 r (training)
 void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,
                         const __nv_bfloat16* Wb, __nv_bfloat16* const* h, float* x, float* G0, float* G1, float* G2,

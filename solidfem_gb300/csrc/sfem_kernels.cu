@@ -1531,7 +1531,8 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
                                                                const T* __restrict__ partial, T* __restrict__ x,
                                                                T* __restrict__ r, T* __restrict__ rprev,
                                                                const T* __restrict__ p, const T* __restrict__ q,
-                                                               Reduce red, CgScalars* s) {
+                                                               Reduce red, CgScalars* s, const T* __restrict__ dinv,
+                                                               T* __restrict__ xs) {
   if (s->done) return;
   const T a = (T)s->alpha;
   T rr = T(0);
@@ -1559,6 +1560,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
       rprev[o + c2] = rp;
       const T rn = rp - a * qq[c2];
       r[o + c2] = rn;
+      if (xs) xs[o + c2] = rn * sqrt(dinv[o + c2]);  // the preconditioner's input D^-1/2 r
       rr += rn * rn;
     }
   }
@@ -1580,14 +1582,15 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
 
 template <typename T>
 void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
-                             T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st) {
+                             T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
+                             const T* dinv, T* xs) {
   count_launch();
   k_fcg_update_patch<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, bidx, pb, partial, x, r, rprev, p, q, red,
-                                                                 s);
+                                                                 s, dinv, xs);
 }
 template void launch_fcg_update_patch<float>(int64_t, int64_t, const int32_t*, PatchBoundary, const float*, float*,
                                              float*, float*, const float*, const float*, Reduce, CgScalars*,
-                                             cudaStream_t);
+                                             cudaStream_t, const float*, float*);
 
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
