@@ -129,6 +129,8 @@ struct sfem_handle {
   int32_t* perm = nullptr;
   int64_t n_patches = 0, n_slots = 0, n_shared = 0;
   int max_pnodes = 0;  // largest node count of a patch
+  double* rec64 = nullptr;  // patch-product element records (12 values per element, see PatchView::rec)
+  float* rec32 = nullptr;
   int64_t *elem_off = nullptr, *node_off = nullptr;
   int32_t *pnode = nullptr, *pdest = nullptr, *bnode = nullptr, *bptr = nullptr, *bidx = nullptr;
   uint16_t *lptr = nullptr, *lent = nullptr;
@@ -171,8 +173,9 @@ struct sfem_handle {
     if (dt > 0) pm = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)pm64 : (const void*)pm32);
     const T* nhc = nullptr;
     if (nhc_on) nhc = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)nhc64 : (const void*)nhc32);
+    const T* rec = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)rec64 : (const void*)rec32);
     return PatchView<T>{elem_off, node_off, pnode, pdest, lptr, lent, lidx, X, vol, scale, scale_la, E, n_patches,
-                        nbc, m, l, pm, nhc, max_pnodes};
+                        nbc, m, l, pm, nhc, max_pnodes, rec};
   }
   NodeCsr csr() const { return NodeCsr{csr_ptr, csr_ent}; }
   ElemView<double> ev64() const {
@@ -738,7 +741,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
       (st = dalloc(&h->bidx, (size_t)n_nodes)) ||
       (st = dalloc(&h->scal, 1)) || (st = dalloc(&h->dres, 8)) || (st = dalloc(&h->ninv, 1)) ||
       (st = dalloc(&h->r64, N3)) || (st = dalloc(&h->ubase, N3)) || (st = dalloc(&h->tmp64, N3)) ||
-      (st = dalloc(&h->tmp64b, N3)))
+      (st = dalloc(&h->tmp64b, N3)) || (st = dalloc(&h->rec64, 12 * E)) || (st = dalloc(&h->rec32, 12 * E)))
     return bail(st);
   if (cudaMallocHost((void**)&h->scal_h, sizeof(CgScalars)) != cudaSuccess ||
       cudaMallocHost((void**)&h->dres_h, 8 * sizeof(double)) != cudaSuccess)
@@ -755,6 +758,22 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   UP(h->vol64, vol.data(), E * sizeof(double));
   UP(h->X32, X32.data(), 9 * E * sizeof(float));
   UP(h->vol32, vol32.data(), E * sizeof(float));
+  {  // element records of the patch product: one 16-byte-aligned row per element
+    std::vector<double> r64(12 * E, 0.0);
+    std::vector<float> r32(12 * E, 0.f);
+    for (size_t e = 0; e < E; e++) {
+      for (int q9 = 0; q9 < 9; q9++) {
+        r64[12 * e + q9] = X[q9 * E + e];
+        r32[12 * e + q9] = X32[q9 * E + e];
+      }
+      r64[12 * e + 9] = vol[e];
+      r32[12 * e + 9] = vol32[e];
+      memcpy(&r64[12 * e + 10], &pbld.lidx[e], sizeof(ushort4));
+      memcpy(&r32[12 * e + 10], &pbld.lidx[e], sizeof(ushort4));
+    }
+    UP(h->rec64, r64.data(), 12 * E * sizeof(double));
+    UP(h->rec32, r32.data(), 12 * E * sizeof(float));
+  }
   UP(h->x0, x0.data(), N3 * sizeof(double));
   UP(h->mass, mass.data(), (size_t)n_nodes * sizeof(double));
   UP(h->grav_d, h->grav, 3 * sizeof(double));
@@ -793,7 +812,7 @@ int sfem_destroy(sfem_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
-                   h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32};
+                   h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,

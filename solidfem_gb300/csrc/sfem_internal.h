@@ -90,6 +90,7 @@ struct PatchView {
   const T* pm;   // implicit dynamics: per slot m_g / (h^2 * patches sharing g), else nullptr
   const T* nhc;  // neo-Hookean tangent cache (k_nh_cache, 12 E values) valid for this solve, or nullptr
   int max_nodes;  // the largest node count of a patch (sizes the shared-memory node arrays)
+  const T* rec;   // per element 12 values: X (9), vol, the local corners' 8 bytes, padding (16-byte rows)
 };
 
 // Implicit-dynamics terms of the residual (FemPhysicsMatrixFree::ComputeGradients :546-557):

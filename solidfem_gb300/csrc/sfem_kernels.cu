@@ -1225,12 +1225,32 @@ struct ElemLoad {  // one element's data, loaded ahead of its use
   T vol, sc, scl;
 };
 
+// one element's row of the patch-product records: 16-byte loads (3 in FP32, 6 in FP64)
+__device__ __forceinline__ void load_rec(const float* rec, int64_t e, float (&x)[9], float& vol, ushort4& li) {
+  const float4* r4 = reinterpret_cast<const float4*>(rec + 12 * e);
+  const float4 a = __ldg(r4), b = __ldg(r4 + 1), c = __ldg(r4 + 2);
+  x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+  x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+  x[8] = c.x;
+  vol = c.y;
+  const uint32_t w0 = __float_as_uint(c.z), w1 = __float_as_uint(c.w);
+  li = make_ushort4((unsigned short)(w0 & 0xffffu), (unsigned short)(w0 >> 16), (unsigned short)(w1 & 0xffffu),
+                    (unsigned short)(w1 >> 16));
+}
+__device__ __forceinline__ void load_rec(const double* rec, int64_t e, double (&x)[9], double& vol, ushort4& li) {
+  const double2* r2 = reinterpret_cast<const double2*>(rec + 12 * e);
+  const double2 a = __ldg(r2), b = __ldg(r2 + 1), c = __ldg(r2 + 2), d = __ldg(r2 + 3), f = __ldg(r2 + 4),
+                g = __ldg(r2 + 5);
+  x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y; x[4] = c.x; x[5] = c.y; x[6] = d.x; x[7] = d.y; x[8] = f.x;
+  vol = f.y;
+  const unsigned long long w = (unsigned long long)__double_as_longlong(g.x);
+  li = make_ushort4((unsigned short)(w & 0xffffu), (unsigned short)((w >> 16) & 0xffffu),
+                    (unsigned short)((w >> 32) & 0xffffu), (unsigned short)(w >> 48));
+}
+
 template <typename T>
 __device__ __forceinline__ void load_elem(const PatchView<T>& pv, int64_t e, ElemLoad<T>& d) {
-  d.li = pv.lidx[e];
-#pragma unroll
-  for (int q9 = 0; q9 < 9; q9++) d.X[q9] = pv.X[q9 * pv.E + e];
-  d.vol = pv.vol[e];
+  load_rec(pv.rec, e, d.X, d.vol, d.li);
   d.sc = pv.scale ? pv.scale[e] : T(1);
   d.scl = pv.scale_la ? pv.scale_la[e] : d.sc;
 }
