@@ -1,4 +1,4 @@
-"""Batched solves of independent bodies in one handle (BASELINE configuration 4).
+"""Batched solves of independent bodies in one handle (the 64-body batched workload).
 
 The bodies are concatenated into one mesh (disjoint components) with per-element Lame
 parameters; every kernel launch of the Newton-Krylov solve covers all of them, and the

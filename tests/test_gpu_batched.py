@@ -1,4 +1,4 @@
-"""Batched uneven solves (BASELINE configuration 4): independent bodies in one handle,
+"""Batched uneven solves (the 64-body workload): independent bodies in one handle,
 per-body convergence masks; every body must match its own separate solve."""
 import time
 

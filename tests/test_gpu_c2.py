@@ -1,4 +1,4 @@
-"""BASELINE configuration 2 at full size: box [0,8]x[0,2]x[0,2], 128x32x32 hexes x 6 tets
+"""The large plain-vs-mixed-precision workload at full size: box [0,8]x[0,2]x[0,2], 128x32x32 hexes x 6 tets
 (140,481 nodes / 786,432 tets), corotational and neo-Hookean, E = 1e6 Pa, nu = 0.4, 500 Pa
 traction in -z on the x = 8 face, x = 0 clamped.  FP64 element kernels + CG against FP32
 element kernels + CG with the FP64 Newton residual; the FP64 equilibrium is certified by the

@@ -1,6 +1,6 @@
 """Learned preconditioner on the GPU: forward and gradients of the hand-written BF16
 tensor-core kernels against the FP64 oracle (oracle/gnn_oracle.py), and what the trained
-network gains over Jacobi inside the Newton-Krylov solve, judged by the same FP64
+network gains over Jacobi inside the Newton-Krylov solve, held to the same FP64
 residual tolerance."""
 import numpy as np
 import pytest

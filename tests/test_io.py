@@ -5,11 +5,12 @@ import os
 import numpy as np
 import pytest
 
+from oracle.oracle import REF_TREE
 from solidfem_gb300 import io
 from solidfem_gb300.mesh import box_lattice
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_MODELS = "/root/reference/Models"
+REF_MODELS = os.path.join(REF_TREE, "Models")
 
 
 def test_tet1_roundtrip_swaps_y_and_z(tmp_path):
