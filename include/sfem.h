@@ -297,6 +297,10 @@ int sfem_gnn_clear_dataset(sfem_handle* h);
  * G_kj (exact, since S is linear; six passes over 3-vectors), 1 = the six BF16 tensor-core
  * layer kernels.  Training always runs the layer kernels. */
 int sfem_gnn_set_inference(sfem_handle* h, int32_t mode);
+/* how the polynomial passes find a node's neighbours: *form = 2 (a pattern table shared by
+ * nodes with equal neighbour-delta lists, *patterns entries), 1 (16-bit deltas per node) or
+ * 0 (32-bit indices); the three give the same neighbours in the same order */
+int sfem_gnn_graph_form(sfem_handle* h, int32_t* form, int32_t* patterns);
 /* pairs per Adam step (gradient averaged over them); default 1 */
 int sfem_gnn_set_batch(sfem_handle* h, int32_t batch);
 /* Adam on the collected pairs, `batch` seeded random pairs per step; losses: steps floats

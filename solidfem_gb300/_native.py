@@ -127,6 +127,7 @@ SIGNATURES = {
     "sfem_gnn_set_loss": [_vp, C.c_int32],
     "sfem_gnn_set_batch": [_vp, C.c_int32],
     "sfem_gnn_set_inference": [_vp, C.c_int32],
+    "sfem_gnn_graph_form": [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "sfem_gnn_get_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_set_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_apply": [_vp, _dp, _dp],

@@ -76,35 +76,29 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
   k_gnn_layer_inf<false, true, true><<<grid, LT, 0, st>>>(g, h[2], r, dinv, params, Wsb, nullptr, out, done);
 }
 
-void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
-                       float* w, float* out, const int* done, cudaStream_t st, const float* rprev, float* partials,
-                       unsigned* counter, CgScalars* s, const float* xs) {
+void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float4* x4, float4* y1,
+                       float4* y2, float4* w, float* out, const int* done, cudaStream_t st, const float* rprev,
+                       float* partials, unsigned* counter, CgScalars* s, bool x_ready) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
-  const int64_t n3 = 3 * g.n;
   // one node per thread; the partials of the BETA pass hold 4 values per block
   const int grid = blocks_for(g.n, 256);
+  if (!x_ready) launch_scale_sqrt4(g.n, r, dinv, x4, st);
   count_launch();
-  if (xs)  // x = D^-1/2 r already formed (by the flexible-CG update)
-    k_poly_fwd<false><<<grid, 256, 0, st>>>(g, r, dinv, xs, y1, done);
-  else
-    k_poly_fwd<true><<<grid, 256, 0, st>>>(g, r, dinv, nullptr, y1, done);
+  k_poly_fwd<<<grid, 256, 0, st>>>(g, x4, y1, done);
   count_launch();
-  k_poly_fwd<false><<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, done);
+  k_poly_fwd<<<grid, 256, 0, st>>>(g, y1, y2, done);
   count_launch();
-  k_poly_mid<<<grid, 256, 0, st>>>(g, r, dinv, y1, y2, pc, w, done, xs);
-  // Horner in A^T: u = w3 -> A^T u + w2 (into y1) -> A^T u + w1 (into y2) -> out
+  k_poly_mid<<<grid, 256, 0, st>>>(g, x4, y1, y2, pc, w, done);
+  // Horner in A^T: w3 -> A^T u + w2 (into y1) -> A^T u + w1 (into y2) -> out
   count_launch();
-  k_poly_bwd<false, false><<<grid, 256, 0, st>>>(g, w + 3 * n3, w + 2 * n3, r, dinv, 0.f, y1, done, nullptr, nullptr,
-                                                 nullptr, nullptr);
+  k_poly_bwd<<<grid, 256, 0, st>>>(g, w + 3 * g.n, w + 2 * g.n, y1, done);
   count_launch();
-  k_poly_bwd<false, false><<<grid, 256, 0, st>>>(g, y1, w + n3, r, dinv, 0.f, y2, done, nullptr, nullptr, nullptr,
-                                                 nullptr);
+  k_poly_bwd<<<grid, 256, 0, st>>>(g, y1, w + g.n, y2, done);
   count_launch();
   if (s)
-    k_poly_bwd<true, true><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, rprev, partials, counter, s);
+    k_poly_last<true><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, rprev, partials, counter, s);
   else
-    k_poly_bwd<true, false><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, nullptr, nullptr, nullptr,
-                                                  nullptr);
+    k_poly_last<false><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, nullptr, nullptr, nullptr, nullptr);
 }
 
 // the training forward: activations h0..h3 of S at x (kept, with x), then S^T through the
@@ -194,15 +188,10 @@ namespace sfem {
 namespace gnn {
 
 // xs = r D^-1/2 (the input of the polynomial passes), elementwise
-__global__ void k_scale_sqrt(int64_t n, const float* __restrict__ r, const float* __restrict__ dinv,
-                             float* __restrict__ xs) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    xs[i] = r[i] * sqrtf(dinv[i]);
-}
-void launch_scale_sqrt(int64_t n, const float* r, const float* dinv, float* xs, cudaStream_t st) {
+void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float4* x4, cudaStream_t st) {
   int grid = (int)std::min<int64_t>((n + 255) / 256, 2048);
   count_launch();
-  k_scale_sqrt<<<grid < 1 ? 1 : grid, 256, 0, st>>>(n, r, dinv, xs);
+  k_scale_sqrt4<<<grid < 1 ? 1 : grid, 256, 0, st>>>(n, r, dinv, x4);
 }
 
 // d = a - b

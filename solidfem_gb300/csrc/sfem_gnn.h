@@ -36,6 +36,10 @@ struct Graph {
   const int32_t* idx;     // neighbours (free-node indices)
   const float* inv_deg;   // 1 / max(deg, 1)
   const int16_t* d16;     // the same neighbours as j - i when every |j - i| < 2^15 (else null)
+  // neighbour patterns (else null): node i's deltas j - i are ptab[pptr[pid[i]] .. pptr[pid[i] + 1])
+  const uint16_t* pid;
+  const int32_t* pptr;
+  const int16_t* ptab;
 };
 
 

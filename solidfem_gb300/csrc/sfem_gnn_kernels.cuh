@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include "sfem_gnn.h"
+#include "sfem_reduce.cuh"
 
 namespace sfem {
 namespace gnn {
@@ -88,12 +89,14 @@ __device__ __forceinline__ bool last_block_sums(float (&v)[K], float* partials, 
   __syncthreads();
   if (!last) return false;
   __threadfence();
+  double a[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) a[k] = 0.0;
+  strided_sums<double, float, K>(partials, gridDim.x, gridDim.x, a);
 #pragma unroll
   for (int k = 0; k < K; k++) {
-    double a = 0.0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) a += (double)__ldcg(&partials[k * gridDim.x + b]);
-    a = warp_sumd(a);
-    if (lane == 0) sd[k][w] = a;
+    const double b = warp_sumd(a[k]);
+    if (lane == 0) sd[k][w] = b;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -629,84 +632,86 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_inf(Graph g, const __nv_bfloat
 // ======================= inference through the folded polynomial =======================
 // y_{k+1} = A y_k (mean over neighbours), y_0 = x = D^-1/2 r; then w_j = sum_k y_k G[k][j]
 // and M(r) = D^-1/2 (c x + w_0 + A^T (w_1 + A^T (w_2 + A^T w_3)))   (Horner in A^T).
-// Six passes over 3-vectors, one thread per node; the neighbour loop is unrolled by four so
-// that four neighbour loads are in flight, and adds in neighbour order (deterministic).
+// Six passes, one thread per node, over node rows of 16 bytes (x, y, z, 0) so that one
+// neighbour costs one vector load.  A^T u = sum_j u_j / deg_j: the pass that writes a Horner
+// operand stores u_i / deg_i, so every gather is a plain neighbour sum.  The neighbour loop
+// is unrolled by four (four loads in flight) and adds in neighbour order (deterministic).
 
-// sum over the neighbours j of node i of wgt_j * v_j (3-vectors).
-// FIRST: v_j = r_j D_j^-1/2; TRANS: wgt_j = 1 / deg_j, else 1.
-template <bool FIRST, bool TRANS>
-__device__ __forceinline__ void node_gather(const Graph& g, int64_t i, const float* __restrict__ r,
-                                            const float* __restrict__ dinv, const float* __restrict__ v,
-                                            float (&a)[3]) {
-  a[0] = a[1] = a[2] = 0.f;
-  const int p1 = g.ptr[i + 1];
-  int e = g.ptr[i];
-  auto val = [&](int jn, int c) -> float {
-    const int64_t j = 3 * (int64_t)jn + c;
-    return FIRST ? r[j] * sqrtf(dinv[j]) : v[j];
-  };
+// sum over the neighbours j of node i of v_j.  The neighbours come from the pattern table when
+// there is one (a 2-byte id per node; the table's few hundred deltas stay in L1 and a warp of
+// interior nodes reads one address), else from the 16-bit deltas or the 32-bit CSR; the three
+// list the same neighbours in the same order.
+__device__ __forceinline__ float3 node_gather4(const Graph& g, int64_t i, const float4* __restrict__ v) {
+  float3 a = make_float3(0.f, 0.f, 0.f);
+  int e, p1;
+  const int16_t* dl = g.d16;
+  if (g.pid) {
+    const int pat = g.pid[i];
+    e = __ldg(&g.pptr[pat]);
+    p1 = __ldg(&g.pptr[pat + 1]);
+    dl = g.ptab;
+  } else {
+    e = g.ptr[i];
+    p1 = g.ptr[i + 1];
+  }
   const int ii = (int)i;
   for (; e + 4 <= p1; e += 4) {
     int jn[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) jn[u] = g.d16 ? ii + (int)g.d16[e + u] : g.idx[e + u];
-    float x[4][3], wg[4];
+    for (int u = 0; u < 4; u++) jn[u] = dl ? ii + (int)__ldg(&dl[e + u]) : g.idx[e + u];
+    float4 x[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) x[u] = v[jn[u]];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      wg[u] = TRANS ? g.inv_deg[jn[u]] : 1.f;
-#pragma unroll
-      for (int c = 0; c < 3; c++) x[u][c] = val(jn[u], c);
+      a.x += x[u].x;
+      a.y += x[u].y;
+      a.z += x[u].z;
     }
-#pragma unroll
-    for (int u = 0; u < 4; u++)
-#pragma unroll
-      for (int c = 0; c < 3; c++) a[c] += wg[u] * x[u][c];
   }
   for (; e < p1; e++) {
-    const int jn = g.d16 ? ii + (int)g.d16[e] : g.idx[e];
-    const float wg = TRANS ? g.inv_deg[jn] : 1.f;
-#pragma unroll
-    for (int c = 0; c < 3; c++) a[c] += wg * val(jn, c);
+    const float4 x = v[dl ? ii + (int)__ldg(&dl[e]) : g.idx[e]];
+    a.x += x.x;
+    a.y += x.y;
+    a.z += x.z;
   }
+  return a;
 }
 
-template <bool FIRST>
-__global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float* __restrict__ r,
-                                                  const float* __restrict__ dinv, const float* __restrict__ yin,
-                                                  float* __restrict__ yout, const int* done) {
-  if (done && *done) return;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    float a[3];
-    node_gather<FIRST, false>(g, i, r, dinv, yin, a);
-    const float id = g.inv_deg[i];
-    yout[3 * i] = a[0] * id;
-    yout[3 * i + 1] = a[1] * id;
-    yout[3 * i + 2] = a[2] * id;
-  }
-}
+__device__ __forceinline__ float4 row4(float3 a, float s) { return make_float4(a.x * s, a.y * s, a.z * s, 0.f); }
 
-// y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of 3n)
-__global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restrict__ r,
-                                                  const float* __restrict__ dinv, const float* __restrict__ y1,
-                                                  const float* __restrict__ y2, PolyCoef pc, float* __restrict__ w,
-                                                  const int* done, const float* __restrict__ xs) {
-  if (done && *done) return;
-  const int64_t n3 = 3 * g.n;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    float a[3];
-    node_gather<false, false>(g, i, r, dinv, y2, a);
+// x rows = D^-1/2 r
+__global__ void __launch_bounds__(256) k_scale_sqrt4(int64_t n, const float* __restrict__ r,
+                                                     const float* __restrict__ dinv, float4* __restrict__ x4) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * i;
+    x4[i] = make_float4(r[o] * sqrtf(dinv[o]), r[o + 1] * sqrtf(dinv[o + 1]), r[o + 2] * sqrtf(dinv[o + 2]), 0.f);
+  }
+}
+
+// yout = A yin
+__global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float4* __restrict__ yin,
+                                                  float4* __restrict__ yout, const int* done) {
+  if (done && *done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
+    yout[i] = row4(node_gather4(g, i, yin), g.inv_deg[i]);
+}
+
+// y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of n rows;
+// w_3, the first Horner operand, stored divided by the node's degree)
+__global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float4* __restrict__ x4,
+                                                  const float4* __restrict__ y1, const float4* __restrict__ y2,
+                                                  PolyCoef pc, float4* __restrict__ w, const int* done) {
+  if (done && *done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float3 a = node_gather4(g, i, y2);
     const float id = g.inv_deg[i];
-    float y[NL + 1][3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      y[0][c] = xs ? xs[o + c] : r[o + c] * sqrtf(dinv[o + c]);
-      y[1][c] = y1[o + c];
-      y[2][c] = y2[o + c];
-      y[3][c] = a[c] * id;
-    }
+    const float4 v0 = x4[i], v1 = y1[i], v2 = y2[i];
+    const float y[NL + 1][3] = {{v0.x, v0.y, v0.z}, {v1.x, v1.y, v1.z}, {v2.x, v2.y, v2.z},
+                                {a.x * id, a.y * id, a.z * id}};
 #pragma unroll
     for (int jj = 0; jj <= NL; jj++) {
+      float o[3];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         float acc = 0.f;
@@ -714,45 +719,54 @@ __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float* __restri
         for (int k = 0; k <= NL; k++)
 #pragma unroll
           for (int b = 0; b < 3; b++) acc += y[k][b] * pc.G[k][jj][3 * b + c];
-        w[jj * n3 + o + c] = acc;
+        o[c] = acc;
       }
+      w[jj * g.n + i] = row4(make_float3(o[0], o[1], o[2]), jj == NL ? id : 1.f);
     }
   }
 }
 
-// u_out_i = sum_{j in N(i)} u_in_j / deg_j + wadd_i;  LAST: out = D^-1/2 (c x + that) with x = D^-1/2 r.
-// BETA (with LAST, inside flexible CG): also the Polak-Ribiere sums of the new z = out,
+// u_i = sum_{j in N(i)} ud_j + wadd_i, stored as u_i / deg_i (ud_j = u_j / deg_j on input)
+__global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const float4* __restrict__ ud,
+                                                  const float4* __restrict__ wadd, float4* __restrict__ out,
+                                                  const int* done) {
+  if (done && *done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float3 a = node_gather4(g, i, ud);
+    const float4 wa = wadd[i];
+    out[i] = row4(make_float3(a.x + wa.x, a.y + wa.y, a.z + wa.z), g.inv_deg[i]);
+  }
+}
+
+// the last Horner pass: z = D^-1/2 (c x + w_0 + A^T u) = c D^-1 r + D^-1/2 (w_0 + A^T u), 3n.
+// BETA (inside flexible CG): also the Polak-Ribiere sums of the new z,
 //   z.(r - rprev), z.r and the same for z_J = D^-1 r, finished by the last block into
 //   s->beta, s->rz and s->jac (Jacobi direction when z.r <= 0), like k_fcg_beta.
 //   partials: 4 gridDim floats.
-template <bool LAST, bool BETA>
-__global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const float* __restrict__ uin,
-                                                  const float* __restrict__ wadd, const float* __restrict__ r,
-                                                  const float* __restrict__ dinv, float cc, float* __restrict__ out,
-                                                  const int* done, const float* __restrict__ rprev,
-                                                  float* __restrict__ partials, unsigned* counter, CgScalars* s) {
+template <bool BETA>
+__global__ void __launch_bounds__(256) k_poly_last(Graph g, const float4* __restrict__ ud,
+                                                   const float4* __restrict__ w0, const float* __restrict__ r,
+                                                   const float* __restrict__ dinv, float cc, float* __restrict__ out,
+                                                   const int* done, const float* __restrict__ rprev,
+                                                   float* __restrict__ partials, unsigned* counter, CgScalars* s) {
   if (done && *done) return;
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    float a[3];
-    node_gather<false, true>(g, i, r, dinv, uin, a);
+    const float3 a = node_gather4(g, i, ud);
+    const float4 wa = w0[i];
+    const float v[3] = {a.x + wa.x, a.y + wa.y, a.z + wa.z};
     const int64_t o = 3 * i;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      const float v = a[c] + wadd[o + c];
-      if (LAST) {
-        const float d = dinv[o + c], ri = r[o + c];
-        const float z = cc * d * ri + sqrtf(d) * v;
-        out[o + c] = z;
-        if (BETA) {
-          const float dr = ri - rprev[o + c], zj = d * ri;
-          acc[0] += z * dr;
-          acc[1] += z * ri;
-          acc[2] += zj * dr;
-          acc[3] += zj * ri;
-        }
-      } else {
-        out[o + c] = v;
+      const float d = dinv[o + c], ri = r[o + c];
+      const float z = cc * d * ri + sqrtf(d) * v[c];
+      out[o + c] = z;
+      if (BETA) {
+        const float dr = ri - rprev[o + c], zj = d * ri;
+        acc[0] += z * dr;
+        acc[1] += z * ri;
+        acc[2] += zj * dr;
+        acc[3] += zj * ri;
       }
     }
   }

@@ -16,6 +16,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -1927,18 +1928,23 @@ struct GnnState {
   int infer_mode = 0;                    // 0: folded polynomial, 1: tensor-core layers
   gnn::PolyCoef pc{};                    // folded coefficients of the current weights
   bool pc_dirty = true;
-  float *py1 = nullptr, *py2 = nullptr, *pw = nullptr;  // polynomial-form vectors (3n, 3n, 4 x 3n)
+  // polynomial-form node rows (x, y, z, 0): the input D^-1/2 r, y1, y2 (n each) and w (4 x n)
+  float4 *px = nullptr, *py1 = nullptr, *py2 = nullptr, *pw = nullptr;
   float* bpart = nullptr;  // block partials of the fused beta pass (4 per 256 nodes)
   int adam_t = 0;
   bool train_bufs = false;
   int16_t* d16 = nullptr;  // neighbour deltas (polynomial passes), when they fit
-  gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg, d16}; }
+  uint16_t* pid = nullptr;  // neighbour patterns (polynomial passes), when the table is small
+  int32_t* pptr = nullptr;
+  int16_t* ptab = nullptr;
+  int32_t npat = 0;
+  gnn::Graph graph() const { return gnn::Graph{n, ptr, idx, inv_deg, d16, pid, pptr, ptab}; }
 };
 
 void gnn_free(GnnState* g) {
   void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->params, g->grad, g->m, g->v, g->Wb, g->x, g->xg,
                   g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->losses, g->z, g->rprev, g->tmp,
-                  g->py1, g->py2, g->pw, g->bpart, g->d16};
+                  g->px, g->py1, g->py2, g->pw, g->bpart, g->d16, g->pid, g->pptr, g->ptab};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int l = 0; l <= gnn::NL; l++) {
@@ -2056,7 +2062,7 @@ void gnn_apply_dev(sfem_handle* h, const float* r, float* out, const int* done, 
   if (train)
     gnn::launch_apply_train(g->graph(), r, dinv, g->params, g->Wb, g->h, g->x, g->G0, g->G1, g->G2, out, h->stream);
   else if (g->infer_mode == 0)
-    gnn::launch_apply_poly(g->graph(), r, dinv, g->pc, g->py1, g->py2, g->pw, out, done, h->stream);
+    gnn::launch_apply_poly(g->graph(), r, dinv, g->pc, g->px, g->py1, g->py2, g->pw, out, done, h->stream);
   else
     gnn::launch_apply(g->graph(), r, dinv, g->params, g->Wb, g->h, out, done, h->stream);
 }
@@ -2122,19 +2128,19 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   const int* done = &h->scal->done;
   float* part = reinterpret_cast<float*>(h->partials);
   const float* dinv = w.dinv + o;
-  float* xs = g->infer_mode == 0 ? g->tmp : nullptr;  // D^-1/2 r, formed by the update kernel (3N)
+  // the polynomial's input rows D^-1/2 r, formed by the update kernel from the second pass on
+  float4* xs = g->infer_mode == 0 ? g->px : nullptr;
   auto precondition = [&](bool with_beta) {
     if (g->infer_mode == 0) {
-      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->py1, g->py2, g->pw, g->z + o, done, h->stream,
-                             with_beta ? g->rprev + o : nullptr, g->bpart, h->counter, with_beta ? h->scal : nullptr,
-                             xs + o);
+      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->z + o, done,
+                             h->stream, with_beta ? g->rprev + o : nullptr, g->bpart, h->counter,
+                             with_beta ? h->scal : nullptr, with_beta);
     } else {
       gnn::launch_apply(g->graph(), w.r + o, dinv, g->params, g->Wb, g->h, g->z + o, done, h->stream);
       if (with_beta)
         gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, dinv, part, h->counter, h->scal, h->stream);
     }
   };
-  if (xs) gnn::launch_scale_sqrt(n, w.r + o, dinv, xs + o, h->stream);
   precondition(false);
   gnn::launch_fcg_init(n, w.r + o, g->z + o, w.p + o, part, h->counter, h->scal, h->stream);  // p_old = 0
   float* pbuf[2] = {w.p, w.p2};
@@ -2268,6 +2274,33 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
       }
       d16[k] = (int16_t)dlt;
     }
+  // Nodes with equal delta lists (the interior of a structured lattice, each face, edge and
+  // corner class) share one entry of a pattern table; a polynomial pass then reads a 2-byte id
+  // per node instead of the node's list.  Kept when the table is at most a quarter of the
+  // deltas and 32768 entries, i.e. when most nodes repeat a pattern.
+  std::vector<uint16_t> pid;
+  std::vector<int32_t> pptr(1, 0);
+  std::vector<int16_t> ptab;
+  if (fits16 && n > 0) {
+    const size_t cap = std::min<size_t>(32768, d16.size() / 4);
+    std::map<std::vector<int16_t>, uint16_t> seen;
+    pid.resize((size_t)n);
+    std::vector<int16_t> key;
+    for (int64_t i = 0; i < n; i++) {
+      key.assign(d16.begin() + ptr[i], d16.begin() + ptr[i + 1]);
+      auto it = seen.find(key);
+      if (it == seen.end()) {
+        if (seen.size() >= 65535 || ptab.size() + key.size() > cap) {
+          pid.clear();
+          break;
+        }
+        it = seen.emplace(key, (uint16_t)seen.size()).first;
+        ptab.insert(ptab.end(), key.begin(), key.end());
+        pptr.push_back((int32_t)ptab.size());
+      }
+      pid[(size_t)i] = it->second;
+    }
+  }
   // seeded normal weights; log c = 0
   std::vector<float> prm(gnn::NPARAM, 0.f);
   std::mt19937_64 rng(seed);
@@ -2286,9 +2319,10 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   TRY(dalloc(&g->v, gnn::NPARAM));
   TRY(dalloc(&g->Wb, (size_t)3 * gnn::NL * gnn::H * gnn::AIN));
   for (int l = 0; l <= gnn::NL; l++) TRY(dalloc(&g->h[l], nh));
-  TRY(dalloc(&g->py1, 3 * (size_t)n));
-  TRY(dalloc(&g->py2, 3 * (size_t)n));
-  TRY(dalloc(&g->pw, 12 * (size_t)n));
+  TRY(dalloc(&g->px, (size_t)n));
+  TRY(dalloc(&g->py1, (size_t)n));
+  TRY(dalloc(&g->py2, (size_t)n));
+  TRY(dalloc(&g->pw, 4 * (size_t)n));
   TRY(dalloc(&g->bpart, 4 * (size_t)((n + 255) / 256) + 64));
   TRY(dalloc(&g->spart, 4096));
   TRY(dalloc(&g->scount, 1));
@@ -2302,6 +2336,15 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   if (fits16 && !d16.empty()) {
     TRY(dalloc(&g->d16, d16.size()));
     CU(cudaMemcpyAsync(g->d16, d16.data(), d16.size() * sizeof(int16_t), cudaMemcpyHostToDevice, h->stream));
+  }
+  if (!pid.empty() && !ptab.empty()) {
+    g->npat = (int32_t)pptr.size() - 1;
+    TRY(dalloc(&g->pid, pid.size()));
+    TRY(dalloc(&g->pptr, pptr.size()));
+    TRY(dalloc(&g->ptab, ptab.size()));
+    CU(cudaMemcpyAsync(g->pid, pid.data(), pid.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(g->pptr, pptr.data(), pptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(g->ptab, ptab.data(), ptab.size() * sizeof(int16_t), cudaMemcpyHostToDevice, h->stream));
   }
   CU(cudaMemcpyAsync(g->params, prm.data(), prm.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(g->m, 0, gnn::NPARAM * sizeof(float), h->stream));
@@ -2326,6 +2369,15 @@ int sfem_gnn_set_inference(sfem_handle* h, int32_t mode) {
   TRY(gnn_need(h));
   if (mode != 0 && mode != 1) return fail(SFEM_ERR_INVALID, "inference mode is 0 (folded polynomial) or 1 (layers)");
   h->gnn->infer_mode = mode;
+  return SFEM_OK;
+}
+
+int sfem_gnn_graph_form(sfem_handle* h, int32_t* form, int32_t* patterns) {
+  TRY(check_handle(h));
+  TRY(gnn_need(h));
+  const GnnState* g = h->gnn;
+  if (form) *form = g->pid ? 2 : g->d16 ? 1 : 0;
+  if (patterns) *patterns = g->npat;
   return SFEM_OK;
 }
 

@@ -142,11 +142,12 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
                       const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
 
 // fused Krylov update for the patch product (assembles q at shared nodes, bidx[g] = the
-// node's position in the shared-node list or -1)
+// node's position in the shared-node list or -1); with xs, also the preconditioner's input
+// rows D^-1/2 r (x, y, z, 0) of the free nodes
 template <typename T>
 void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
-                             const T* dinv = nullptr, T* xs = nullptr);
+                             const T* dinv = nullptr, float4* xs = nullptr);
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
@@ -242,14 +243,16 @@ namespace gnn {
 // fused into the first and last); Wb holds the 3 packed BF16 weight sets (k_gnn_pack)
 void launch_apply(const Graph& g, const float* r, const float* dinv, const float* params, const __nv_bfloat16* Wb,
                   __nv_bfloat16* const* h, float* out, const int* done, cudaStream_t st);
-// the same M(r) through the folded polynomial (six passes over 3-vectors); y1, y2: 3n, w: 4 x 3n.
-// With s (flexible CG), the last pass also forms the Polak-Ribiere beta from r, rprev (k_fcg_beta).
-void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float* y1, float* y2,
-                       float* w, float* out, const int* done, cudaStream_t st, const float* rprev = nullptr,
-                       float* partials = nullptr, unsigned* counter = nullptr, CgScalars* s = nullptr,
-                       const float* xs = nullptr);
-// xs = r D^-1/2 elementwise
-void launch_scale_sqrt(int64_t n, const float* r, const float* dinv, float* xs, cudaStream_t st);
+// the same M(r) through the folded polynomial: six gather passes over node rows of 16 bytes
+// (x, y, z, 0); x4, y1, y2: n rows, w: 4 x n rows.  x4 = D^-1/2 r is formed first unless
+// x_ready (the flexible-CG update wrote it).  With s (flexible CG), the last pass also forms
+// the Polak-Ribiere beta from r, rprev (like k_fcg_beta).
+void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float4* x4, float4* y1,
+                       float4* y2, float4* w, float* out, const int* done, cudaStream_t st,
+                       const float* rprev = nullptr, float* partials = nullptr, unsigned* counter = nullptr,
+                       CgScalars* s = nullptr, bool x_ready = false);
+// x4 rows = D^-1/2 r (r, dinv: 3n)
+void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float4* x4, cudaStream_t st);
 // the same M(r) keeping the activations h0..h3 of S and x = D^-1/2 r (training)
 void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,
                         const __nv_bfloat16* Wb, __nv_bfloat16* const* h, float* x, float* G0, float* G1, float* G2,

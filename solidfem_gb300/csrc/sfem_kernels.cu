@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "sfem_internal.h"
+#include "sfem_reduce.cuh"
 
 namespace sfem {
 
@@ -609,10 +610,8 @@ __device__ __forceinline__ bool reduce_last(A (&v)[K], Reduce red, A (&tot)[K]) 
   __threadfence();
   A s[K];
 #pragma unroll
-  for (int k = 0; k < K; k++) {
-    s[k] = A(0);
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s[k] += __ldcg(&P[k * gridDim.x + i]);
-  }
+  for (int k = 0; k < K; k++) s[k] = A(0);
+  strided_sums<A, A, K>(P, gridDim.x, gridDim.x, s);
   block_sum<A, K>(s);
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -1445,7 +1444,7 @@ __global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __re
   if (!is_last) return;
   __threadfence();
   T sum[1] = {T(0)};
-  for (int64_t i = threadIdx.x; i < (int64_t)gridDim.x; i += NT) sum[0] += __ldcg(&P[i]);
+  strided_sums<T, T, 1>(P, gridDim.x, gridDim.x, sum);
   block_sum<T, 1>(sum);
   if (threadIdx.x == 0) {
     *red.counter = 0u;
@@ -1552,7 +1551,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
                                                                T* __restrict__ r, T* __restrict__ rprev,
                                                                const T* __restrict__ p, const T* __restrict__ q,
                                                                Reduce red, CgScalars* s, const T* __restrict__ dinv,
-                                                               T* __restrict__ xs) {
+                                                               float4* __restrict__ xs) {
   if (s->done) return;
   const T a = (T)s->alpha;
   T rr = T(0);
@@ -1573,16 +1572,19 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
         qq[2] += partial[3 * (int64_t)t + 2];
       }
     }
+    T rn[3];
 #pragma unroll
     for (int c2 = 0; c2 < 3; c2++) {
       x[o + c2] += a * p[o + c2];
       const T rp = r[o + c2];
       rprev[o + c2] = rp;
-      const T rn = rp - a * qq[c2];
-      r[o + c2] = rn;
-      if (xs) xs[o + c2] = rn * sqrt(dinv[o + c2]);  // the preconditioner's input D^-1/2 r
-      rr += rn * rn;
+      rn[c2] = rp - a * qq[c2];
+      r[o + c2] = rn[c2];
+      rr += rn[c2] * rn[c2];
     }
+    if (xs)  // the preconditioner's input D^-1/2 r
+      xs[g - nbc] = make_float4((float)(rn[0] * sqrt(dinv[o])), (float)(rn[1] * sqrt(dinv[o + 1])),
+                                (float)(rn[2] * sqrt(dinv[o + 2])), 0.f);
   }
   T v[1] = {rr}, tot[1];
   if (reduce_last<T, 1>(v, red, tot) && threadIdx.x == 0) {
@@ -1603,14 +1605,14 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
 template <typename T>
 void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
-                             const T* dinv, T* xs) {
+                             const T* dinv, float4* xs) {
   count_launch();
   k_fcg_update_patch<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, bidx, pb, partial, x, r, rprev, p, q, red,
                                                                  s, dinv, xs);
 }
 template void launch_fcg_update_patch<float>(int64_t, int64_t, const int32_t*, PatchBoundary, const float*, float*,
                                              float*, float*, const float*, const float*, Reduce, CgScalars*,
-                                             cudaStream_t, const float*, float*);
+                                             cudaStream_t, const float*, float4*);
 
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,

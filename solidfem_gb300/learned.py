@@ -70,6 +70,13 @@ class LearnedPreconditioner:
         is linear); 'layers': the BF16 tensor-core layer kernels."""
         nat.check(self._lib.sfem_gnn_set_inference(self.phys.handle, {"poly": 0, "layers": 1}[mode]))
 
+    def graph_form(self) -> tuple[str, int]:
+        """How the polynomial passes read the neighbours: ('patterns', table entries) when nodes
+        share neighbour-delta lists, else ('delta16', 0) or ('index32', 0)."""
+        form, pat = C.c_int32(), C.c_int32()
+        nat.check(self._lib.sfem_gnn_graph_form(self.phys.handle, C.byref(form), C.byref(pat)))
+        return ("index32", "delta16", "patterns")[form.value], pat.value
+
     def set_batch(self, batch: int) -> None:
         """Pairs per Adam step (the gradient is averaged over them)."""
         nat.check(self._lib.sfem_gnn_set_batch(self.phys.handle, int(batch)))

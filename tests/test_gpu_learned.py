@@ -51,15 +51,40 @@ def test_forward_matches_fp64_oracle(mode):
     c = np.exp(prm[go.OFF_C])
     ss_g, ss_o = out_g - c * dinv * r, out_o - c * dinv * r
     err_ss = rel(ss_g, ss_o)
-    print(f"M(r) GPU ({mode}) vs FP64 oracle: rel err {err:.2e}; S^T S part {err_ss:.2e}")
+    print(f"M(r) GPU ({mode}) vs FP64 oracle: rel err {err:.2e}; S^T S part {err_ss:.2e}; {net.graph_form()}")
     assert err < 2e-2 and err_ss < 3e-2
     if mode == "poly":  # FP32 arithmetic on the folded coefficients: no BF16 activations
         assert err_ss < 1e-4
+        # a lattice's free nodes fall in 3 x 3 x 3 neighbour patterns (interior, faces, edges,
+        # corners; the layer above the clamped face is a class of its own)
+        assert net.graph_form()[0] == "patterns"
+        assert net.graph_form()[1] == 27
     # linear and symmetric on the device too (up to BF16 rounding of the activations)
     u, v = rng.normal(size=(2, 3 * o.n_free))
     Mu, Mv = net.apply(u), net.apply(v)
     assert abs(u @ Mv - v @ Mu) <= 2e-2 * abs(u @ Mv)
     assert rel(net.apply(2.0 * u + v), 2.0 * Mu + Mv) < 2e-2
+
+
+def test_forward_without_shared_patterns():
+    """The polynomial passes on a randomly numbered mesh, where no two nodes share a neighbour
+    list: the per-node 16-bit deltas are read instead of the pattern table."""
+    m, fixed, _ = slab(24, 8, 8)
+    perm = np.random.default_rng(5).permutation(len(m.nodes))
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(len(perm))
+    m.nodes = m.nodes[perm]
+    m.tets = inv[m.tets].astype(np.int32)
+    fixed = inv[fixed]
+    p, net, o, Am, dinv = gpu_and_oracle(m, fixed, seed=3)
+    assert net.graph_form()[0] == "delta16"
+    r = np.random.default_rng(1).normal(size=3 * o.n_free)
+    out_g = net.apply(r)
+    out_o = go.forward(net.get_params(), Am, r, dinv)
+    c = np.exp(net.get_params().astype(np.float64)[go.OFF_C])
+    err_ss = rel(out_g - c * dinv * r, out_o - c * dinv * r)
+    print(f"M(r) GPU (poly, per-node deltas) vs FP64 oracle: S^T S part {err_ss:.2e}")
+    assert err_ss < 1e-4
 
 
 @pytest.mark.parametrize("mode", ["energy", "residual"])
