@@ -80,25 +80,33 @@ void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const 
                        float4* y2, float4* w, float* out, const int* done, cudaStream_t st, const float* rprev,
                        float* partials, unsigned* counter, CgScalars* s, bool x_ready) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
-  // one node per thread; the partials of the BETA pass hold 4 values per block
-  const int grid = blocks_for(g.n, 256);
+  // grid-stride passes sized to one resident wave (no partly filled last wave; the BETA pass
+  // then finishes with one block partial per resident CTA, 4 values each)
+  static const int wave_fwd = resident_ctas(k_poly_fwd, 256, 0), wave_mid = resident_ctas(k_poly_mid, 256, 0),
+                   wave_bwd = resident_ctas(k_poly_bwd, 256, 0),
+                   wave_last = std::min(resident_ctas(k_poly_last<true>, 256, 0),
+                                        resident_ctas(k_poly_last<false>, 256, 0));
+  const int blocks = blocks_for(g.n, 256);
   if (!x_ready) launch_scale_sqrt4(g.n, r, dinv, x4, st);
   count_launch();
-  k_poly_fwd<<<grid, 256, 0, st>>>(g, x4, y1, done);
+  launch_pdl(k_poly_fwd, std::min(blocks, wave_fwd), 256, 0, st, g, x4, y1, done);
   count_launch();
-  k_poly_fwd<<<grid, 256, 0, st>>>(g, y1, y2, done);
+  launch_pdl(k_poly_fwd, std::min(blocks, wave_fwd), 256, 0, st, g, y1, y2, done);
   count_launch();
-  k_poly_mid<<<grid, 256, 0, st>>>(g, x4, y1, y2, pc, w, done);
+  launch_pdl(k_poly_mid, std::min(blocks, wave_mid), 256, 0, st, g, x4, y1, y2, pc, w, done);
   // Horner in A^T: w3 -> A^T u + w2 (into y1) -> A^T u + w1 (into y2) -> out
   count_launch();
-  k_poly_bwd<<<grid, 256, 0, st>>>(g, w + 3 * g.n, w + 2 * g.n, y1, done);
+  launch_pdl(k_poly_bwd, std::min(blocks, wave_bwd), 256, 0, st, g, w + 3 * g.n, w + 2 * g.n, y1, done);
   count_launch();
-  k_poly_bwd<<<grid, 256, 0, st>>>(g, y1, w + g.n, y2, done);
+  launch_pdl(k_poly_bwd, std::min(blocks, wave_bwd), 256, 0, st, g, y1, w + g.n, y2, done);
   count_launch();
+  const int grid_last = std::min(blocks, wave_last);
   if (s)
-    k_poly_last<true><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, rprev, partials, counter, s);
+    launch_pdl(k_poly_last<true>, grid_last, 256, 0, st, g, y2, w, r, dinv, pc.c, out, done, rprev, partials, counter,
+               s);
   else
-    k_poly_last<false><<<grid, 256, 0, st>>>(g, y2, w, r, dinv, pc.c, out, done, nullptr, nullptr, nullptr, nullptr);
+    launch_pdl(k_poly_last<false>, grid_last, 256, 0, st, g, y2, w, r, dinv, pc.c, out, done, nullptr, nullptr,
+               nullptr, nullptr);
 }
 
 // the training forward: activations h0..h3 of S at x (kept, with x), then S^T through the
@@ -191,7 +199,7 @@ namespace gnn {
 void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float4* x4, cudaStream_t st) {
   int grid = (int)std::min<int64_t>((n + 255) / 256, 2048);
   count_launch();
-  k_scale_sqrt4<<<grid < 1 ? 1 : grid, 256, 0, st>>>(n, r, dinv, x4);
+  launch_pdl(k_scale_sqrt4, grid < 1 ? 1 : grid, 256, 0, st, n, r, dinv, x4);
 }
 
 // d = a - b

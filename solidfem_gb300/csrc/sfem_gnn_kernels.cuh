@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include "sfem_gnn.h"
+#include "sfem_pdl.cuh"
 #include "sfem_reduce.cuh"
 
 namespace sfem {
@@ -683,6 +684,8 @@ __device__ __forceinline__ float4 row4(float3 a, float s) { return make_float4(a
 // x rows = D^-1/2 r
 __global__ void __launch_bounds__(256) k_scale_sqrt4(int64_t n, const float* __restrict__ r,
                                                      const float* __restrict__ dinv, float4* __restrict__ x4) {
+  pdl_wait();
+  pdl_launch_dependents();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * i;
     x4[i] = make_float4(r[o] * sqrtf(dinv[o]), r[o + 1] * sqrtf(dinv[o + 1]), r[o + 2] * sqrtf(dinv[o + 2]), 0.f);
@@ -692,6 +695,8 @@ __global__ void __launch_bounds__(256) k_scale_sqrt4(int64_t n, const float* __r
 // yout = A yin
 __global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float4* __restrict__ yin,
                                                   float4* __restrict__ yout, const int* done) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (done && *done) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
     yout[i] = row4(node_gather4(g, i, yin), g.inv_deg[i]);
@@ -702,6 +707,8 @@ __global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float4* __restr
 __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float4* __restrict__ x4,
                                                   const float4* __restrict__ y1, const float4* __restrict__ y2,
                                                   PolyCoef pc, float4* __restrict__ w, const int* done) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (done && *done) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     const float3 a = node_gather4(g, i, y2);
@@ -730,6 +737,8 @@ __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float4* __restr
 __global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const float4* __restrict__ ud,
                                                   const float4* __restrict__ wadd, float4* __restrict__ out,
                                                   const int* done) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (done && *done) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
     const float3 a = node_gather4(g, i, ud);
@@ -749,6 +758,8 @@ __global__ void __launch_bounds__(256) k_poly_last(Graph g, const float4* __rest
                                                    const float* __restrict__ dinv, float cc, float* __restrict__ out,
                                                    const int* done, const float* __restrict__ rprev,
                                                    float* __restrict__ partials, unsigned* counter, CgScalars* s) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (done && *done) return;
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {

@@ -18,9 +18,12 @@
 // the last block to finish, so results are run-to-run identical.
 #include <cuda_runtime.h>
 #include <math.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include "sfem_internal.h"
+#include "sfem_pdl.cuh"
 #include "sfem_reduce.cuh"
 
 namespace sfem {
@@ -1298,6 +1301,8 @@ __global__ void __launch_bounds__(NT) k_patch_hvp(PatchView<T> pv, const T* __re
                                                   T* __restrict__ partial, Reduce red, CgScalars* s,
                                                   const T* __restrict__ r, const T* __restrict__ dinv,
                                                   T* __restrict__ p_new, const T* __restrict__ z) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (s != nullptr && s->done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sfe = reinterpret_cast<T*>(smem_raw);         // kPatchElems * kFeStride
@@ -1494,6 +1499,8 @@ __global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64
                                                               T* __restrict__ x, T* __restrict__ r,
                                                               const T* __restrict__ p, const T* __restrict__ q,
                                                               const T* __restrict__ dinv, Reduce red, CgScalars* s) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (s->done) return;
   const T a = (T)s->alpha;
   T rz = T(0), rr = T(0);
@@ -1552,6 +1559,8 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
                                                                const T* __restrict__ p, const T* __restrict__ q,
                                                                Reduce red, CgScalars* s, const T* __restrict__ dinv,
                                                                float4* __restrict__ xs) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (s->done) return;
   const T a = (T)s->alpha;
   T rr = T(0);
@@ -1607,8 +1616,9 @@ void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchB
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
                              const T* dinv, float4* xs) {
   count_launch();
-  k_fcg_update_patch<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, bidx, pb, partial, x, r, rprev, p, q, red,
-                                                                 s, dinv, xs);
+  static const int wave = resident_ctas(k_fcg_update_patch<T>, kThreads, 0);
+  launch_pdl(k_fcg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bidx, pb, partial, x,
+             r, rprev, p, q, red, s, dinv, xs);
 }
 template void launch_fcg_update_patch<float>(int64_t, int64_t, const int32_t*, PatchBoundary, const float*, float*,
                                              float*, float*, const float*, const float*, Reduce, CgScalars*,
@@ -1618,7 +1628,9 @@ template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st) {
   count_launch();
-  k_cg_update_patch<T><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, bidx, pb, partial, x, r, p, q, dinv, red, s);
+  static const int wave = resident_ctas(k_cg_update_patch<T>, kThreads, 0);
+  launch_pdl(k_cg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bidx, pb, partial, x, r,
+             p, q, dinv, red, s);
 }
 template void launch_cg_update_patch<double>(int64_t, int64_t, const int32_t*, PatchBoundary, const double*, double*,
                                              double*, const double*, const double*, const double*, Reduce,
@@ -1653,9 +1665,11 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
   if (p_new != nullptr) {
     // Krylov iteration: the fused update (k_cg_update_patch) completes the shared nodes
     if (cached)
-      k_patch_hvp<T, MAT, NT, true, kNH><<<grid, NT, smem_c, st>>>(pv, u, p, q, partial, red, s, r, dinv, p_new, z);
+      launch_pdl(k_patch_hvp<T, MAT, NT, true, kNH>, grid, NT, smem_c, st, pv, u, p, q, partial, red, s, r, dinv, p_new,
+                 z);
     else
-      k_patch_hvp<T, MAT, NT, true, false><<<grid, NT, smem, st>>>(pv, u, p, q, partial, red, s, r, dinv, p_new, z);
+      launch_pdl(k_patch_hvp<T, MAT, NT, true, false>, grid, NT, smem, st, pv, u, p, q, partial, red, s, r, dinv, p_new,
+                 z);
     if (mid) cudaEventRecord(mid, st);
     return;
   }
