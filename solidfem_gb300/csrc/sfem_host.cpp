@@ -94,6 +94,7 @@ struct sfem_handle {
   int tangent = SFEM_TANGENT_REFERENCE;
   double young = 0, poisson = 0, mu = 0, lambda = 0, density = 0, grav[3] = {0, 0, 0}, ff = 1.0;
   std::vector<int32_t> map;  // original -> reshuffled
+  int32_t* dmap = nullptr;   // the same on the device
   bool has_scale = false;
 
   // element data
@@ -568,11 +569,10 @@ int set_device(const sfem_handle* h) {
 }
 
 // host original-order N x 3 -> device reshuffled 3N
+// one contiguous copy of a node array in the caller's order, permuted on the device
 int upload_nodes(sfem_handle* h, const double* src, double* dst) {
-  std::vector<double> tmp(3 * (size_t)h->N);
-  for (int64_t i = 0; i < h->N; i++)
-    for (int c = 0; c < 3; c++) tmp[3 * (size_t)h->map[i] + c] = src[3 * (size_t)i + c];
-  CU(cudaMemcpyAsync(dst, tmp.data(), tmp.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->tmp64b, src, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_nodes_in(h->N, h->dmap, h->tmp64b, nullptr, 0, dst, h->stream);
   return sync(h);
 }
 
@@ -739,7 +739,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
       (st = dalloc(&h->lptr, (size_t)(h->n_slots + h->n_patches))) ||
       (st = dalloc(&h->lent, 4 * E)) || (st = dalloc(&h->lidx, E)) || (st = dalloc(&h->partial, 3 * (size_t)h->n_slots)) ||
       (st = dalloc(&h->bnode, (size_t)h->n_shared)) || (st = dalloc(&h->bptr, (size_t)h->n_shared + 1)) ||
-      (st = dalloc(&h->bidx, (size_t)n_nodes)) ||
+      (st = dalloc(&h->bidx, (size_t)n_nodes)) || (st = dalloc(&h->dmap, (size_t)n_nodes)) ||
       (st = dalloc(&h->scal, 1)) || (st = dalloc(&h->dres, 8)) || (st = dalloc(&h->ninv, 1)) ||
       (st = dalloc(&h->r64, N3)) || (st = dalloc(&h->ubase, N3)) || (st = dalloc(&h->tmp64, N3)) ||
       (st = dalloc(&h->tmp64b, N3)) || (st = dalloc(&h->rec64, 12 * E)) || (st = dalloc(&h->rec32, 12 * E)))
@@ -755,6 +755,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)          \
     return bail(fail(SFEM_ERR_CUDA, "upload failed: %s", cudaGetErrorString(cudaGetLastError())));
   UP(h->tets, tt.data(), E * sizeof(int4));
+  UP(h->dmap, h->map.data(), (size_t)n_nodes * sizeof(int32_t));
   UP(h->X64, X.data(), 9 * E * sizeof(double));
   UP(h->vol64, vol.data(), E * sizeof(double));
   UP(h->X32, X32.data(), 9 * E * sizeof(float));
@@ -817,7 +818,7 @@ int sfem_destroy(sfem_handle* h) {
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
-                   h->partial, h->bnode, h->bptr, h->bidx};
+                   h->partial, h->bnode, h->bptr, h->bidx, h->dmap};
   for (void* b : pbufs)
     if (b) cudaFree(b);
   void* bufs[] = {h->tets, h->X64, h->vol64, h->scale64, h->young_e, h->X32, h->vol32, h->scale32, h->x0, h->u,
@@ -1024,19 +1025,14 @@ int sfem_get_time_step(sfem_handle* h, double* dt) {
 
 static int node_vec_io(sfem_handle* h, double* dev, const double* in, double* out) {
   const size_t N3 = 3 * (size_t)h->N;
-  std::vector<double> t(N3, 0.0);
   if (in) {
-    for (int64_t i = 0; i < h->N; i++)
-      for (int c = 0; c < 3; c++) t[3 * (size_t)h->map[i] + c] = in[3 * (size_t)i + c];
-    for (size_t k = 0; k < 3 * (size_t)h->nbc; k++) t[k] = 0.0;  // fixed nodes do not move
-    CU(cudaMemcpyAsync(dev, t.data(), N3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->tmp64b, in, N3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_nodes_in(h->N, h->dmap, h->tmp64b, nullptr, h->nbc, dev, h->stream);  // fixed nodes do not move
     return sync(h);
   }
-  CU(cudaMemcpyAsync(t.data(), dev, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  TRY(sync(h));
-  for (int64_t i = 0; i < h->N; i++)
-    for (int c = 0; c < 3; c++) out[3 * (size_t)i + c] = t[3 * (size_t)h->map[i] + c];
-  return SFEM_OK;
+  launch_nodes_out(h->N, h->dmap, dev, nullptr, h->tmp64, h->stream);
+  CU(cudaMemcpyAsync(out, h->tmp64, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
 }
 
 int sfem_set_velocities(sfem_handle* h, const double* vel) {
@@ -1115,32 +1111,16 @@ int sfem_step(sfem_handle* h, double dt, int32_t sim_type, int32_t substeps, con
 int sfem_get_positions(sfem_handle* h, double* pos) {
   TRY(check_handle(h));
   TRY(set_device(h));
-  const size_t N3 = 3 * (size_t)h->N;
-  std::vector<double> x0(N3), u(N3);
-  CU(cudaMemcpyAsync(x0.data(), h->x0, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CU(cudaMemcpyAsync(u.data(), h->u, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  TRY(sync(h));
-  for (int64_t i = 0; i < h->N; i++)
-    for (int c = 0; c < 3; c++) {
-      size_t g = 3 * (size_t)h->map[i] + c;
-      pos[3 * (size_t)i + c] = x0[g] + u[g];
-    }
-  return SFEM_OK;
+  launch_nodes_out(h->N, h->dmap, h->x0, h->u, h->tmp64, h->stream);
+  CU(cudaMemcpyAsync(pos, h->tmp64, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
 }
 
 int sfem_set_positions(sfem_handle* h, const double* pos) {
   TRY(check_handle(h));
   TRY(set_device(h));
-  const size_t N3 = 3 * (size_t)h->N;
-  std::vector<double> x0(N3), u(N3);
-  CU(cudaMemcpyAsync(x0.data(), h->x0, N3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  TRY(sync(h));
-  for (int64_t i = 0; i < h->N; i++)
-    for (int c = 0; c < 3; c++) {
-      size_t g = 3 * (size_t)h->map[i] + c;
-      u[g] = pos[3 * (size_t)i + c] - x0[g];
-    }
-  CU(cudaMemcpyAsync(h->u, u.data(), N3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->tmp64b, pos, 3 * (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_nodes_in(h->N, h->dmap, h->tmp64b, h->x0, 0, h->u, h->stream);
   return sync(h);
 }
 

@@ -224,6 +224,12 @@ void launch_explicit_substep(int64_t nbc, int64_t N, const double* f, const doub
 // implicit step end (FemPhysicsMatrixFree::Solve :589-597): v = (u - u_start) / h
 void launch_velocity_update(int64_t nbc, int64_t N, const double* u, const double* u_start, double inv_h,
                             double* vel, cudaStream_t st);
+// node vectors between the caller's order and the reshuffled order (map: original -> reshuffled)
+// in: dst[3 map[i] + c] = src[3 i + c] - sub[...] (sub optional; zero where map[i] < nzero)
+void launch_nodes_in(int64_t N, const int32_t* map, const double* src, const double* sub, int64_t nzero, double* dst,
+                     cudaStream_t st);
+// out: dst[3 i + c] = a[3 map[i] + c] + b[...] (b optional)
+void launch_nodes_out(int64_t N, const int32_t* map, const double* a, const double* b, double* dst, cudaStream_t st);
 template <typename Tin, typename Tout>
 void launch_convert(int64_t n, const Tin* a, Tout* b, cudaStream_t st);
 // x = x + a * d   (FP64 state += precision-T direction)

@@ -1950,6 +1950,36 @@ void launch_velocity_update(int64_t nbc, int64_t N, const double* u, const doubl
   k_velocity_update<<<grid_for(3 * (N - nbc)), kThreads, 0, st>>>(nbc, N, u, u_start, inv_h, vel);
 }
 
+// Node vectors between the caller's node order and the reshuffled device order (map: original ->
+// reshuffled), so host arrays travel as one contiguous copy and the permutation runs here.
+// in:  dst[3 map[i] + c] = src[3 i + c] - sub[3 map[i] + c] (sub optional), zero where map[i] < nzero
+// out: dst[3 i + c] = a[3 map[i] + c] + b[3 map[i] + c] (b optional)
+__global__ void k_nodes_in(int64_t N, const int32_t* __restrict__ map, const double* __restrict__ src,
+                           const double* __restrict__ sub, int64_t nzero, double* __restrict__ dst) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < 3 * N; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = k / 3, c = k - 3 * i, g = map[i];
+    const int64_t o = 3 * g + c;
+    dst[o] = g < nzero ? 0.0 : src[k] - (sub ? sub[o] : 0.0);
+  }
+}
+__global__ void k_nodes_out(int64_t N, const int32_t* __restrict__ map, const double* __restrict__ a,
+                            const double* __restrict__ b, double* __restrict__ dst) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < 3 * N; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = k / 3, c = k - 3 * i;
+    const int64_t o = 3 * (int64_t)map[i] + c;
+    dst[k] = a[o] + (b ? b[o] : 0.0);
+  }
+}
+void launch_nodes_in(int64_t N, const int32_t* map, const double* src, const double* sub, int64_t nzero, double* dst,
+                     cudaStream_t st) {
+  count_launch();
+  k_nodes_in<<<grid_for(3 * N), kThreads, 0, st>>>(N, map, src, sub, nzero, dst);
+}
+void launch_nodes_out(int64_t N, const int32_t* map, const double* a, const double* b, double* dst, cudaStream_t st) {
+  count_launch();
+  k_nodes_out<<<grid_for(3 * N), kThreads, 0, st>>>(N, map, a, b, dst);
+}
+
 template <typename Tin, typename Tout>
 __global__ void k_convert(int64_t n, const Tin* __restrict__ a, Tout* __restrict__ b) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)

@@ -97,11 +97,15 @@ class FemPhysicsMatrixFree:
         return m
 
     # ---- state ----
-    def get_positions(self):
-        """All node positions, original order (N, 3)."""
-        x = np.zeros((self.n_nodes, 3))
-        nat.check(self._lib.sfem_get_positions(self._h, _dp(x)))
-        return x
+    def get_positions(self, out=None):
+        """All node positions, original order (N, 3); into ``out`` (float64, C-contiguous (N, 3),
+        e.g. a pinned buffer) when given."""
+        if out is None:
+            out = np.zeros((self.n_nodes, 3))
+        elif out.dtype != np.float64 or out.shape != (self.n_nodes, 3) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape (n_nodes, 3)")
+        nat.check(self._lib.sfem_get_positions(self._h, _dp(out)))
+        return out
 
     def set_positions(self, pos):
         pos = _f64(pos).reshape(-1, 3)
