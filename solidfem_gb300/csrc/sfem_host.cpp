@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <type_traits>
 #include <cmath>
 #include <random>
@@ -296,20 +297,30 @@ int sync(sfem_handle* h) {
 }
 
 // FP64 residual r64 = f_int + m g ff + f_ext ff; returns |r| and the number of inverted elements.
-int residual(sfem_handle* h, double* rnorm, int* n_inverted) {
+// With energy (elastic, total), the element pass also sums the elastic energy and a node pass
+// the potential of the loads (the values sfem_energy returns, from the same kernels' arithmetic).
+int residual(sfem_handle* h, double* rnorm, int* n_inverted, double* energy = nullptr) {
   CU(cudaMemsetAsync(h->ninv, 0, sizeof(int), h->stream));
-  element_pass<double>(h, MODE_FORCE, h->u, nullptr, h->fe, nullptr, h->ninv, nullptr);
+  element_pass<double>(h, energy ? MODE_FORCE_ENERGY : MODE_FORCE, h->u, nullptr, h->fe, energy ? h->dres + 3 : nullptr,
+                       h->ninv, nullptr);
   const PressureView pv = h->pres();
   if (h->n_tris > 0) launch_pressure_tris(pv, h->x0, h->u, h->ff, h->stream);
   const DynView dv = h->dyn();
   launch_gather_force(h->nbc, h->N, h->csr(), h->fe, h->mass, h->fext, h->grav, h->ff, h->r64, h->red(),
                       h->dres, h->stream, h->n_tris > 0 ? &pv : nullptr, h->dt > 0 ? &dv : nullptr, h->u);
-  CU(cudaMemcpyAsync(h->dres_h, h->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (energy)
+    launch_potential(h->nbc, h->N, h->x0, h->u, h->mass, h->fext, h->grav, h->ff, h->red(), h->dres + 4, h->stream,
+                     h->dt > 0 ? &dv : nullptr);
+  CU(cudaMemcpyAsync(h->dres_h, h->dres, (energy ? 5 : 1) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   int ninv_h = 0;
   CU(cudaMemcpyAsync(&ninv_h, h->ninv, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
   if (rnorm) *rnorm = std::sqrt(h->dres_h[0]);
   if (n_inverted) *n_inverted = ninv_h;
+  if (energy) {
+    energy[0] = h->dres_h[3];
+    energy[1] = h->dres_h[3] + h->dres_h[4];
+  }
   return 0;
 }
 
@@ -1574,6 +1585,8 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
                  int* cuts, int max_newton) {
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
   double rn = *rn_io, rprev = rn, eta = op.eta_max;
+  bool have_e = false;  // e_acc holds the total energy at the current state
+  double e_acc = 0.0;
   const int max_bis = op.max_bisection > 0 ? op.max_bisection : 30;
   const bool inst = h->n_inst > 0;
   if (inst) h->inst_rel.assign(h->n_inst, 1.0);
@@ -1600,14 +1613,29 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
     eta = std::max(eta, op.eta_min);
     eta = std::min(eta, op.eta_max);
     int its = 0;
+    using clk = std::chrono::steady_clock;
+    clk::time_point t0, t1;
+    if (op.verbose) {
+      TRY(sync(h));
+      t0 = clk::now();
+    }
     TRY(inner_solve(h, eta, op.max_cg, op.precond, &its));
+    if (op.verbose) {
+      TRY(sync(h));
+      t1 = clk::now();
+    }
     *cgit += its;
     (*nit)++;
     // backtracking line search on the FP64 residual
     CU(cudaMemcpyAsync(h->ubase, h->u, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     double e_old = 0, slope = 0;
     if (op.ls_condition == SFEM_LSC_ARMIJO) {
-      TRY(sfem_energy(h, nullptr, &e_old));
+      // the energy at this state was computed when the previous step accepted it (same kernel,
+      // same state: the same value)
+      if (have_e)
+        e_old = e_acc;
+      else
+        TRY(sfem_energy(h, nullptr, &e_old));
       // slope = grad E . d = -r . d
       launch_dot((int64_t)n, h->r64 + o, h->tmp64 + o, h->red(), h->dres + 2, h->stream);
       CU(cudaMemcpyAsync(h->dres_h + 2, h->dres + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1623,7 +1651,7 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
     }
     double a = 1.0;
     bool ok = false;
-    double rnew = rn;
+    double rnew = rn, e_try = 0.0;
     if (op.ls_condition == SFEM_LSC_RESIDUAL) {
       // residual-norm backtracking: halve until |r| decreases sufficiently and no element inverts
       for (int ls = 0; ls <= max_bis; ls++) {
@@ -1644,12 +1672,13 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
       for (;;) {
         launch_axpy_state<double>((int64_t)n, a, h->tmp64 + o, h->ubase + o, h->u + o, h->stream);
         int ninv = 0;
-        TRY(residual(h, &rnew, &ninv));
+        double en[2] = {0.0, 0.0};  // elastic and total energy, with the residual (Armijo)
+        TRY(residual(h, &rnew, &ninv, op.ls_condition == SFEM_LSC_ARMIJO ? en : nullptr));
         bool cond = false;
         if (ninv == 0 && std::isfinite(rnew)) {
           if (op.ls_condition == SFEM_LSC_ARMIJO) {
-            double e_el = 0, e_new = 0;
-            TRY(sfem_energy(h, &e_el, &e_new));
+            const double e_el = en[0], e_new = en[1];
+            e_try = e_new;
             cond = e_new < e_old + 1e-4 * a * slope;  // Armijo, mAlpha = 1e-4
             // near convergence the energy decrease falls below FP64 resolution of the energy:
             // then a decrease of the residual norm decides
@@ -1677,8 +1706,13 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
         if (a < 1e-10) break;
       }
     }
-    if (op.verbose)
-      fprintf(stderr, "[sfem] newton %d: |r| %.6e -> %.6e  cg %d  eta %.2e  step %.3g\n", *nit, rn, rnew, its, eta, a);
+    if (op.verbose) {
+      TRY(sync(h));
+      const double ms_cg = std::chrono::duration<double, std::milli>(t1 - t0).count();
+      const double ms_ls = std::chrono::duration<double, std::milli>(clk::now() - t1).count();
+      fprintf(stderr, "[sfem] newton %d: |r| %.6e -> %.6e  cg %d  eta %.2e  step %.3g  (%.2f ms solve, %.2f ms line search)\n",
+              *nit, rn, rnew, its, eta, a, ms_cg, ms_ls);
+    }
     if (!ok) {
       CU(cudaMemcpyAsync(h->u, h->ubase, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
       TRY(residual(h, &rn, nullptr));
@@ -1687,6 +1721,8 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
     }
     rprev = rn;
     rn = rnew;
+    have_e = op.ls_condition == SFEM_LSC_ARMIJO && !inst;
+    e_acc = e_try;
     if (inst) {
       std::vector<int32_t> act(h->n_inst);
       CU(cudaMemcpyAsync(act.data(), h->inst_active, h->n_inst * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));

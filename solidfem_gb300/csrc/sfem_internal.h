@@ -14,7 +14,8 @@ enum Mode {
   MODE_STRESS = 4,   // PK1 stress (9 per element, 12-stride)
   MODE_PMU = 5,      // forces of the mu-part of the neo-Hookean stress
   MODE_PLAMBDA = 6,  // forces of the lambda-part
-  MODE_NODALVOL = 7  // V/4 per element corner
+  MODE_NODALVOL = 7,      // V/4 per element corner
+  MODE_FORCE_ENERGY = 8   // MODE_FORCE and the MODE_ENERGY sum in one pass
 };
 
 // Element arrays on the device, structure-of-arrays.

@@ -713,11 +713,12 @@ __global__ void __launch_bounds__(kThreads) k_element(ElemView<T> ev, const T* _
     F.a[4] += T(1);
     F.a[8] += T(1);
     T f[12];
-    if (MODE == MODE_FORCE) {
+    if (MODE == MODE_FORCE || MODE == MODE_FORCE_ENERGY) {
       if (det(F) <= T(0)) ninv++;
       M3<T> P = stress<T, MAT>(F, mu, la);
       nodal_forces(P, X, -vol, f);
       store12(fe, e, f);
+      if (MODE == MODE_FORCE_ENERGY) eacc += (double)(vol * energy_density<T, MAT>(F, mu, la));
     } else if (MODE == MODE_ENERGY) {
       if (det(F) <= T(0)) ninv++;
       eacc += (double)(vol * energy_density<T, MAT>(F, mu, la));
@@ -795,11 +796,11 @@ __global__ void __launch_bounds__(kThreads) k_element(ElemView<T> ev, const T* _
       store12(fe, e, f);
     }
   }
-  if (MODE == MODE_ENERGY) {
+  if (MODE == MODE_ENERGY || MODE == MODE_FORCE_ENERGY) {
     double v[1] = {eacc}, tot[1];
     if (reduce_last<double, 1>(v, red, tot) && threadIdx.x == 0) *result = tot[0];
   }
-  if ((MODE == MODE_FORCE || MODE == MODE_ENERGY) && n_inv != nullptr) {
+  if ((MODE == MODE_FORCE || MODE == MODE_ENERGY || MODE == MODE_FORCE_ENERGY) && n_inv != nullptr) {
     int v[1] = {ninv};
     block_sum<int, 1>(v);
     if (threadIdx.x == 0 && v[0] != 0) atomicAdd(n_inv, v[0]);
@@ -823,6 +824,9 @@ void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* 
       break;
     case MODE_ENERGY:
       k_element<T, MAT, MODE_ENERGY><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
+      break;
+    case MODE_FORCE_ENERGY:
+      k_element<T, MAT, MODE_FORCE_ENERGY><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
       break;
     case MODE_STRESS:
       k_element<T, MAT, MODE_STRESS><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
