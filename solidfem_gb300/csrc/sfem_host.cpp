@@ -136,6 +136,7 @@ struct sfem_handle {
   float* rec32 = nullptr;
   int64_t *elem_off = nullptr, *node_off = nullptr;
   int32_t *pnode = nullptr, *pdest = nullptr, *bnode = nullptr, *bptr = nullptr, *bidx = nullptr;
+  int2* bslot = nullptr;  // per node: (first partial slot, count) of a shared node, (0, 0) otherwise
   uint16_t *lptr = nullptr, *lent = nullptr;
   ushort4* lidx = nullptr;
   double* partial = nullptr;  // 3 * n_slots values (float passes use it as floats)
@@ -403,7 +404,7 @@ int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, doub
         pending = true;
       }
       if (h->profiling) h->prof_launches++;
-      launch_cg_update_patch<T>(h->nbc, h->N, h->bidx, h->pb(), reinterpret_cast<const T*>(h->partial), x, w.r,
+      launch_cg_update_patch<T>(h->nbc, h->N, h->bslot, reinterpret_cast<const T*>(h->partial), x, w.r,
                                 pnew, w.q, dinv, h->red(), h->scal, h->stream);
     }
   }
@@ -751,6 +752,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
       (st = dalloc(&h->lent, 4 * E)) || (st = dalloc(&h->lidx, E)) || (st = dalloc(&h->partial, 3 * (size_t)h->n_slots)) ||
       (st = dalloc(&h->bnode, (size_t)h->n_shared)) || (st = dalloc(&h->bptr, (size_t)h->n_shared + 1)) ||
       (st = dalloc(&h->bidx, (size_t)n_nodes)) || (st = dalloc(&h->dmap, (size_t)n_nodes)) ||
+      (st = dalloc(&h->bslot, (size_t)n_nodes)) ||
       (st = dalloc(&h->scal, 1)) || (st = dalloc(&h->dres, 8)) || (st = dalloc(&h->ninv, 1)) ||
       (st = dalloc(&h->r64, N3)) || (st = dalloc(&h->ubase, N3)) || (st = dalloc(&h->tmp64, N3)) ||
       (st = dalloc(&h->tmp64b, N3)) || (st = dalloc(&h->rec64, 12 * E)) || (st = dalloc(&h->rec32, 12 * E)))
@@ -803,8 +805,13 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   if (h->n_shared > 0) UP(h->bnode, pbld.bnode.data(), pbld.bnode.size() * sizeof(int32_t));
   UP(h->bptr, pbld.bptr.data(), pbld.bptr.size() * sizeof(int32_t));
   std::vector<int32_t> bidx_h((size_t)n_nodes, -1);
-  for (size_t i = 0; i < pbld.bnode.size(); i++) bidx_h[pbld.bnode[i]] = (int32_t)i;
+  std::vector<int2> bslot_h((size_t)n_nodes, make_int2(0, 0));
+  for (size_t i = 0; i < pbld.bnode.size(); i++) {
+    bidx_h[pbld.bnode[i]] = (int32_t)i;
+    bslot_h[pbld.bnode[i]] = make_int2(pbld.bptr[i], pbld.bptr[i + 1] - pbld.bptr[i]);
+  }
   UP(h->bidx, bidx_h.data(), bidx_h.size() * sizeof(int32_t));
+  UP(h->bslot, bslot_h.data(), bslot_h.size() * sizeof(int2));
 #undef UP
   double* zero_bufs[] = {h->u, h->fext, h->r64, h->ubase, h->tmp64, h->tmp64b, h->vel, h->ustart};
   for (double* z : zero_bufs)
@@ -829,7 +836,7 @@ int sfem_destroy(sfem_handle* h) {
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
-                   h->partial, h->bnode, h->bptr, h->bidx, h->dmap};
+                   h->partial, h->bnode, h->bptr, h->bidx, h->dmap, h->bslot};
   for (void* b : pbufs)
     if (b) cudaFree(b);
   void* bufs[] = {h->tets, h->X64, h->vol64, h->scale64, h->young_e, h->X32, h->vol32, h->scale32, h->x0, h->u,
@@ -2188,7 +2195,7 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
         pending = true;
       }
       if (h->profiling) h->prof_launches++;
-      launch_fcg_update_patch<float>(h->nbc, h->N, h->bidx, h->pb(), reinterpret_cast<const float*>(h->partial), x,
+      launch_fcg_update_patch<float>(h->nbc, h->N, h->bslot, reinterpret_cast<const float*>(h->partial), x,
                                      w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream, xs ? w.dinv : nullptr, xs);
       precondition(true);
     }
@@ -2533,7 +2540,7 @@ int sfem_gnn_collect(sfem_handle* h, const double* b_free, int32_t every, int32_
       float* pold = pbuf[it % 2];
       float* pnew = pbuf[(it + 1) % 2];
       hvp<float>(h, w.u, pold, w.q, h->scal, nullptr, w.r, w.dinv, pnew);
-      launch_cg_update_patch<float>(h->nbc, h->N, h->bidx, h->pb(), reinterpret_cast<const float*>(h->partial), w.x,
+      launch_cg_update_patch<float>(h->nbc, h->N, h->bslot, reinterpret_cast<const float*>(h->partial), w.x,
                                     w.r, pnew, w.q, w.dinv, h->red(), h->scal, h->stream);
     }
   }

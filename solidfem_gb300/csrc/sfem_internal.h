@@ -142,16 +142,16 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
                       Reduce red, CgScalars* s, cudaStream_t st, cudaEvent_t mid = nullptr, const T* r = nullptr,
                       const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
 
-// fused Krylov update for the patch product (assembles q at shared nodes, bidx[g] = the
-// node's position in the shared-node list or -1); with xs, also the preconditioner's input
-// rows D^-1/2 r (x, y, z, 0) of the free nodes
+// fused Krylov update for the patch product (assembles q at shared nodes: bslot[g] = (first
+// partial slot, count), count 0 for nodes of one patch); with xs, also the preconditioner's
+// input rows D^-1/2 r (x, y, z, 0) of the free nodes
 template <typename T>
-void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
-                             T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
+void launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x, T* r, T* rprev,
+                             const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
                              const T* dinv = nullptr, float4* xs = nullptr);
 template <typename T>
-void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
-                            T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
+void launch_cg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x, T* r, const T* p,
+                            const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
 
 // ---- node gathers (FP64 residual / T HVP / T diagonal) ----
 // follower pressure (FemPhysicsMatrixFree::ComputePressureForces): per triangle the force

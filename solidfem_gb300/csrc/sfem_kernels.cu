@@ -1494,12 +1494,32 @@ __global__ void __launch_bounds__(kThreads) k_patch_boundary(PatchBoundary pb, c
   }
 }
 
-// Fused Krylov update over nodes: q_g from q (owned nodes) or the sum of its patch
-// partials (shared nodes, bidx[g] >= 0), then x += alpha p, r -= alpha q, z = dinv r,
-// r.z and r.r with the fixed-order last-block finish (beta, convergence test).
+// q at node g: from q (nodes of one patch, slot.y == 0) or the sum of its patch partials
+// partial[slot.x .. slot.x + slot.y) in patch order (shared nodes)
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64_t N, const int32_t* __restrict__ bidx,
-                                                              PatchBoundary pb, const T* __restrict__ partial,
+__device__ __forceinline__ void node_q(const T* __restrict__ q, const T* __restrict__ partial, int2 slot, int64_t o,
+                                       T (&qq)[3]) {
+  if (slot.y == 0) {
+    qq[0] = q[o];
+    qq[1] = q[o + 1];
+    qq[2] = q[o + 2];
+  } else {
+    qq[0] = qq[1] = qq[2] = T(0);
+    const int t1 = slot.x + slot.y;
+    for (int t = slot.x; t < t1; t++) {
+      qq[0] += partial[3 * (int64_t)t];
+      qq[1] += partial[3 * (int64_t)t + 1];
+      qq[2] += partial[3 * (int64_t)t + 2];
+    }
+  }
+}
+
+// Fused Krylov update over nodes: q_g from q or the node's patch partials (node_q), then
+// x += alpha p, r -= alpha q, z = dinv r, r.z and r.r with the fixed-order last-block finish
+// (beta, convergence test).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64_t N, const int2* __restrict__ bslot,
+                                                              const T* __restrict__ partial,
                                                               T* __restrict__ x, T* __restrict__ r,
                                                               const T* __restrict__ p, const T* __restrict__ q,
                                                               const T* __restrict__ dinv, Reduce red, CgScalars* s) {
@@ -1511,20 +1531,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * g;
     T qq[3];
-    const int b = bidx[g];
-    if (b < 0) {
-      qq[0] = q[o];
-      qq[1] = q[o + 1];
-      qq[2] = q[o + 2];
-    } else {
-      qq[0] = qq[1] = qq[2] = T(0);
-      const int t1 = pb.ptr[b + 1];
-      for (int t = pb.ptr[b]; t < t1; t++) {
-        qq[0] += partial[3 * (int64_t)t];
-        qq[1] += partial[3 * (int64_t)t + 1];
-        qq[2] += partial[3 * (int64_t)t + 2];
-      }
-    }
+    node_q(q, partial, bslot[g], o, qq);
 #pragma unroll
     for (int c2 = 0; c2 < 3; c2++) {
       x[o + c2] += a * p[o + c2];
@@ -1557,7 +1564,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64
 // x += alpha p, rprev = r, r -= alpha q and r.r with the fixed-order last-block finish.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int64_t N,
-                                                               const int32_t* __restrict__ bidx, PatchBoundary pb,
+                                                               const int2* __restrict__ bslot,
                                                                const T* __restrict__ partial, T* __restrict__ x,
                                                                T* __restrict__ r, T* __restrict__ rprev,
                                                                const T* __restrict__ p, const T* __restrict__ q,
@@ -1571,20 +1578,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * g;
     T qq[3];
-    const int b = bidx[g];
-    if (b < 0) {
-      qq[0] = q[o];
-      qq[1] = q[o + 1];
-      qq[2] = q[o + 2];
-    } else {
-      qq[0] = qq[1] = qq[2] = T(0);
-      const int t1 = pb.ptr[b + 1];
-      for (int t = pb.ptr[b]; t < t1; t++) {
-        qq[0] += partial[3 * (int64_t)t];
-        qq[1] += partial[3 * (int64_t)t + 1];
-        qq[2] += partial[3 * (int64_t)t + 2];
-      }
-    }
+    node_q(q, partial, bslot[g], o, qq);
     T rn[3];
 #pragma unroll
     for (int c2 = 0; c2 < 3; c2++) {
@@ -1616,30 +1610,30 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
 }
 
 template <typename T>
-void launch_fcg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
+void launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x,
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
                              const T* dinv, float4* xs) {
   count_launch();
   static const int wave = resident_ctas(k_fcg_update_patch<T>, kThreads, 0);
-  launch_pdl(k_fcg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bidx, pb, partial, x,
-             r, rprev, p, q, red, s, dinv, xs);
+  launch_pdl(k_fcg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bslot, partial, x, r,
+             rprev, p, q, red, s, dinv, xs);
 }
-template void launch_fcg_update_patch<float>(int64_t, int64_t, const int32_t*, PatchBoundary, const float*, float*,
+template void launch_fcg_update_patch<float>(int64_t, int64_t, const int2*, const float*, float*,
                                              float*, float*, const float*, const float*, Reduce, CgScalars*,
                                              cudaStream_t, const float*, float4*);
 
 template <typename T>
-void launch_cg_update_patch(int64_t nbc, int64_t N, const int32_t* bidx, PatchBoundary pb, const T* partial, T* x,
+void launch_cg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x,
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st) {
   count_launch();
   static const int wave = resident_ctas(k_cg_update_patch<T>, kThreads, 0);
-  launch_pdl(k_cg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bidx, pb, partial, x, r,
-             p, q, dinv, red, s);
+  launch_pdl(k_cg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bslot, partial, x, r, p,
+             q, dinv, red, s);
 }
-template void launch_cg_update_patch<double>(int64_t, int64_t, const int32_t*, PatchBoundary, const double*, double*,
+template void launch_cg_update_patch<double>(int64_t, int64_t, const int2*, const double*, double*,
                                              double*, const double*, const double*, const double*, Reduce,
                                              CgScalars*, cudaStream_t);
-template void launch_cg_update_patch<float>(int64_t, int64_t, const int32_t*, PatchBoundary, const float*, float*,
+template void launch_cg_update_patch<float>(int64_t, int64_t, const int2*, const float*, float*,
                                             float*, const float*, const float*, const float*, Reduce, CgScalars*,
                                             cudaStream_t);
 
