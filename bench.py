@@ -244,6 +244,7 @@ def run_gpu_arm(args):
     solve_kw = dict(rel_tol=REL_TOL, max_newton=30, max_cg=200000)
 
     p32 = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision="fp32", **kw)
+    p32.set_operator(args.operator)
     method = "jacobi"
     weights = args.weights if args.weights else os.path.join(ROOT, "solidfem_gb300", "data", "gnn_slab.bin")
     if args.precond in ("learned", "auto") and os.path.exists(weights):
@@ -343,7 +344,15 @@ def run_gpu_arm(args):
     # DRAM bytes of one patch-product launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum on a
     # 3,145,728-tet case of the same kernel (220.1 MB per launch, profiles/patch_hvp_fp32_c3.md), scaled
     # by the tet count (the element data streams once per launch, far above L2 in both cases)
-    traffic = args.traffic if args.traffic else HVP_DRAM_BYTES_PER_TET * m.n_tets
+    if args.operator == "assembled":
+        kernel = "k_sell_hvp<float> (tangent assembled per Newton step, sliced-ELL sparse product)"
+        traffic = args.traffic
+        traffic_source = "--traffic" if args.traffic else None
+    else:
+        kernel = "k_patch_hvp<float, neo-Hookean> (fused element Hessian-vector product)"
+        traffic = args.traffic if args.traffic else HVP_DRAM_BYTES_PER_TET * m.n_tets
+        traffic_source = ("ncu capture at 3,145,728 tets scaled by the tet count" if not args.traffic
+                          else "--traffic")
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -354,6 +363,7 @@ def run_gpu_arm(args):
                 "method": ("inexact Newton (Eisenstat-Walker), " +
                            ("learned-preconditioner flexible PCG" if method == "learned" else "Jacobi-PCG") +
                            " inner solves in FP32, FP64 residual and convergence test"),
+                "operator": args.operator,
                 "preconditioner": method, "l2": "inputs larger than L2 (element data 0.35 GB FP32)",
                 "jacobi_fp32_stats": st_j32,
                 "converged": ok, "newton_iters": [s_["newton_iters"] for s_ in stats],
@@ -365,11 +375,9 @@ def run_gpu_arm(args):
             },
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk, "unit": "GB/s",
                          "frac": achieved / pk if achieved else None, "traffic": traffic,
-                         "kernel": "k_patch_hvp<float, neo-Hookean> (fused element Hessian-vector product)",
+                         "kernel": kernel,
                          "algo_bytes_per_launch": prof["algo_bytes_hvp"], "ms_per_launch": ms,
-                         "peak_source": pk_kind,
-                         "traffic_source": "ncu capture at 3,145,728 tets scaled by the tet count"
-                         if not args.traffic else "--traffic"},
+                         "peak_source": pk_kind, "traffic_source": traffic_source},
             "e2e": {"value": e2e_t, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(),
             "gpu_launches": launches,
@@ -407,6 +415,8 @@ def main():
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")
+    ap.add_argument("--operator", default="matrix-free", choices=["matrix-free", "assembled"],
+                    help="operator of the FP32 Krylov solves (the FP64 baseline stays matrix-free)")
     args = ap.parse_args()
     if args.warmup < 3 and not args.small:
         args.warmup = 3

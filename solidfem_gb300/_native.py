@@ -31,6 +31,7 @@ MATERIALS_WITH_ENERGY = (0, 1, 2, 3, 4, 6, 10)
 FP64, FP32 = 0, 1
 PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
 SIM_EXPLICIT, SIM_IMPLICIT = 2, 3
+OP_MATRIX_FREE, OP_ASSEMBLED = 0, 1
 LSC_ARMIJO, LSC_ENGINEERING, LSC_RESIDUAL = 0, 1, 2
 TANGENT_REFERENCE, TANGENT_EXACT = 0, 1
 
@@ -127,6 +128,7 @@ SIGNATURES = {
     "sfem_gnn_set_loss": [_vp, C.c_int32],
     "sfem_gnn_set_batch": [_vp, C.c_int32],
     "sfem_gnn_set_inference": [_vp, C.c_int32],
+    "sfem_set_operator": [_vp, C.c_int32],
     "sfem_gnn_graph_form": [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "sfem_gnn_get_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_set_params": [_vp, C.POINTER(C.c_float)],

@@ -19,6 +19,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sfem.h"
@@ -124,6 +125,16 @@ struct sfem_handle {
   int64_t bsr_nnzb = -1;
   int32_t *bsr_rowptr = nullptr, *bsr_col = nullptr, *bsr_slot = nullptr, *bsr_dslot = nullptr;
   double* bsr_vals = nullptr;
+  // FP32 Krylov operator: 0 = matrix-free patch product, 1 = the tangent assembled in sliced ELL
+  // at the start of every FP32 Krylov solve (sell_on while its values match the current state)
+  int32_t op_mode = 0;
+  bool sell_on = false;
+  int64_t sell_T = -1, sell_nnzb = 0;  // block-slots (with padding), blocks
+  int64_t *sell_base = nullptr, *sell_cptr = nullptr;
+  int32_t *sell_col = nullptr, *sell_dslot = nullptr;
+  uint32_t* sell_code = nullptr;
+  float *sell_vals32 = nullptr, *sell_ke32 = nullptr;
+  int32_t prof_op = 0;  // operator of the sampled Krylov launches
   float* pm32 = nullptr;
   DynView dyn() const { return DynView{vel, ustart, 1.0 / dt, 1.0 / (dt * dt)}; }
   int64_t *csr_ptr = nullptr, *csr_ent = nullptr;
@@ -280,6 +291,27 @@ void hvp(sfem_handle* h, const T* u, const T* p, T* q, CgScalars* s, cudaEvent_t
   });
 }
 
+// the Krylov loops' product: the assembled FP32 tangent while it is current (sell_on), else the
+// patch product; both form the direction on the fly (p_new) and finish p.q and alpha
+template <typename T>
+void krylov_hvp(sfem_handle* h, const T* u, const T* p, T* q, cudaEvent_t mid, const T* r, const T* dinv, T* p_new,
+                const T* z = nullptr) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (h->sell_on) {
+      launch_sell_hvp<float>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_vals32, p, q, h->red(), h->scal,
+                             h->stream, r, dinv, p_new, z);
+      if (mid) cudaEventRecord(mid, h->stream);
+      return;
+    }
+  }
+  hvp<T>(h, u, p, q, h->scal, mid, r, dinv, p_new, z);
+}
+// shared-node partial slots of the patch product (none with the assembled tangent: q is complete)
+template <typename T>
+const int2* krylov_bslot(const sfem_handle* h) {
+  return (std::is_same<T, float>::value && h->sell_on) ? nullptr : h->bslot;
+}
+
 // displacement in precision T for the element passes
 template <typename T>
 const T* disp(sfem_handle* h);
@@ -379,7 +411,10 @@ int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, doub
   if (check_every <= 0) check_every = 32;
   int it = 0;
   bool pending = false;
-  if (h->profiling) h->prof_precision = sizeof(T) == 4 ? SFEM_FP32 : SFEM_FP64;
+  if (h->profiling) {
+    h->prof_precision = sizeof(T) == 4 ? SFEM_FP32 : SFEM_FP64;
+    h->prof_op = krylov_bslot<T>(h) == nullptr ? 1 : 0;
+  }
   for (;;) {
     CU(cudaMemcpyAsync(h->scal_h, h->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
     TRY(sync(h));
@@ -398,13 +433,13 @@ int pcg_device(sfem_handle* h, const T* u, const T* b, T* x, const T* dinv, doub
       if (sample) CU(cudaEventRecord(h->pev[0], h->stream));
       T* pold = pbuf[it % 2];
       T* pnew = pbuf[(it + 1) % 2];
-      hvp<T>(h, u, pold, w.q, h->scal, sample ? h->pev[1] : nullptr, w.r, dinv, pnew);
+      krylov_hvp<T>(h, u, pold, w.q, sample ? h->pev[1] : nullptr, w.r, dinv, pnew);
       if (sample) {
         CU(cudaEventRecord(h->pev[2], h->stream));
         pending = true;
       }
       if (h->profiling) h->prof_launches++;
-      launch_cg_update_patch<T>(h->nbc, h->N, h->bslot, reinterpret_cast<const T*>(h->partial), x, w.r,
+      launch_cg_update_patch<T>(h->nbc, h->N, krylov_bslot<T>(h), reinterpret_cast<const T*>(h->partial), x, w.r,
                                 pnew, w.q, dinv, h->red(), h->scal, h->stream);
     }
   }
@@ -832,7 +867,8 @@ int sfem_destroy(sfem_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
-                   h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32};
+                   h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
+                   h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32, h->sell_ke32};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
@@ -877,7 +913,11 @@ int sfem_get_profile(const sfem_handle* h, sfem_profile* out) {
   out->samples = h->prof_samples;
   out->hvp_launches = h->prof_launches;
   const double sz = h->prof_precision == SFEM_FP32 ? 4.0 : 8.0;
-  out->algo_bytes_hvp = (double)h->E * (16.0 + 10.0 * sz) + (double)h->N * 9.0 * sz;
+  if (h->prof_op == 1)  // assembled tangent: blocks and their column indices, and per free node the
+                        // direction inputs (z or r, p_old) and outputs (p, q)
+    out->algo_bytes_hvp = (double)h->sell_nnzb * (9.0 * sz + 4.0) + (double)h->nf * 12.0 * sz;
+  else
+    out->algo_bytes_hvp = (double)h->E * (16.0 + 10.0 * sz) + (double)h->N * 9.0 * sz;
   out->precision = h->prof_precision;
   out->reserved = 0;
   return SFEM_OK;
@@ -921,8 +961,10 @@ int sfem_set_stream(sfem_handle* h, void* stream) {
 }
 
 // ---- assembled tangent (ElasticEnergy::AssembleStiffnessMatrix, Source/ElasticEnergy.cpp:573-635) ----
-static int bsr_structure(sfem_handle* h) {
-  if (h->bsr_nnzb >= 0) return 0;
+// block-CSR pattern of the tangent over the free nodes (sorted columns per row), the block of
+// every (element, corner a, corner b) with both corners free (-1 otherwise) and each row's diagonal
+static int tangent_pattern(sfem_handle* h, std::vector<int32_t>& rowptr, std::vector<int32_t>& col,
+                           std::vector<int32_t>& slot, std::vector<int32_t>& dslot) {
   const int64_t E = h->E, nbc = h->nbc, nf = h->nf;
   std::vector<int4> tt((size_t)E);
   CU(cudaMemcpyAsync(tt.data(), h->tets, tt.size() * sizeof(int4), cudaMemcpyDeviceToHost, h->stream));
@@ -939,7 +981,10 @@ static int bsr_structure(sfem_handle* h) {
   std::sort(keys.begin(), keys.end());
   keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
   if (keys.size() > (size_t)INT32_MAX) return fail(SFEM_ERR_INVALID, "tangent too large for 32-bit block indices");
-  std::vector<int32_t> rowptr((size_t)nf + 1, 0), col(keys.size()), slot((size_t)E * 16, -1), dslot((size_t)nf);
+  rowptr.assign((size_t)nf + 1, 0);
+  col.resize(keys.size());
+  slot.assign((size_t)E * 16, -1);
+  dslot.resize((size_t)nf);
   for (size_t k = 0; k < keys.size(); k++) {
     rowptr[(keys[k] >> 32) + 1]++;
     col[k] = (int32_t)(keys[k] & 0xffffffffu);
@@ -957,6 +1002,14 @@ static int bsr_structure(sfem_handle* h) {
         if (v[a] >= nbc && v[b] >= nbc) slot[16 * e + 4 * a + b] = find(v[a] - nbc, v[b] - nbc);
   }
   for (int64_t i = 0; i < nf; i++) dslot[i] = find(i, (int32_t)i);
+  return 0;
+}
+
+static int bsr_structure(sfem_handle* h) {
+  if (h->bsr_nnzb >= 0) return 0;
+  const int64_t nf = h->nf;
+  std::vector<int32_t> rowptr, col, slot, dslot;
+  TRY(tangent_pattern(h, rowptr, col, slot, dslot));
   TRY(dalloc(&h->bsr_rowptr, rowptr.size()));
   TRY(dalloc(&h->bsr_col, std::max<size_t>(col.size(), 1)));
   TRY(dalloc(&h->bsr_slot, slot.size()));
@@ -971,19 +1024,191 @@ static int bsr_structure(sfem_handle* h) {
   return 0;
 }
 
+extern "C++" {
+// rows [0, n) split over the host's threads
+template <typename F>
+static void parallel_rows(int64_t n, F&& f) {
+  const int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  if (nt == 1 || n < 4096) {
+    f((int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const int64_t chunk = (n + nt - 1) / nt;
+  for (int k = 0; k < nt; k++) {
+    const int64_t a = k * chunk, b = std::min(n, a + chunk);
+    if (a < b) pool.emplace_back([&f, a, b] { f(a, b); });
+  }
+  for (auto& th : pool) th.join();
+}
+}
+
+// The tangent's pattern in sliced ELL, built row by row from the node->element CSR: a free row's
+// columns are the free nodes of its elements (sorted; the diagonal always present); slices of 32
+// rows are padded to their longest row (padding blocks point at the row itself and stay zero);
+// block (row r, position k) is block-slot base[r / 32] + 32 k + r % 32.  Each block-slot lists
+// its contributions 16 e + 4 a + b (block (a, b) of element e, a the row's corner) in the order of
+// the row's element entries, so the assembly is a deterministic gather.
+static int sell_structure(sfem_handle* h) {
+  if (h->sell_T >= 0) return 0;
+  const int64_t E = h->E, N = h->N, nbc = h->nbc, nf = h->nf, ns = (nf + 31) / 32;
+  if (E >= (int64_t(1) << 28)) return fail(SFEM_ERR_INVALID, "too many elements for the assembled operator");
+  std::vector<int4> tt((size_t)E);
+  std::vector<int64_t> cp((size_t)N + 1), ce((size_t)4 * E);
+  CU(cudaMemcpyAsync(tt.data(), h->tets, tt.size() * sizeof(int4), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(cp.data(), h->csr_ptr, cp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(ce.data(), h->csr_ent, ce.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  auto columns = [&](int64_t r, std::vector<int32_t>& cols) {
+    cols.clear();
+    cols.push_back((int32_t)r);
+    for (int64_t k = cp[nbc + r]; k < cp[nbc + r + 1]; k++) {
+      const int4 t4 = tt[ce[k] >> 2];
+      const int32_t v[4] = {t4.x, t4.y, t4.z, t4.w};
+      for (int b = 0; b < 4; b++)
+        if (v[b] >= nbc) cols.push_back((int32_t)(v[b] - nbc));
+    }
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+  };
+  std::vector<int32_t> len((size_t)nf);
+  parallel_rows(nf, [&](int64_t a, int64_t b) {
+    std::vector<int32_t> cols;
+    for (int64_t r = a; r < b; r++) {
+      columns(r, cols);
+      len[r] = (int32_t)cols.size();
+    }
+  });
+  std::vector<int64_t> base((size_t)ns + 1, 0);
+  int64_t nnzb = 0;
+  for (int64_t sl = 0; sl < ns; sl++) {
+    int64_t w = 0;
+    for (int64_t r = 32 * sl; r < std::min(nf, 32 * sl + 32); r++) {
+      w = std::max<int64_t>(w, len[r]);
+      nnzb += len[r];
+    }
+    base[sl + 1] = base[sl] + 32 * w;
+  }
+  const int64_t T = base[ns];
+  if (T > (int64_t)INT32_MAX) return fail(SFEM_ERR_INVALID, "tangent too large for 32-bit block-slots");
+  std::vector<int32_t> scol((size_t)T, 0), dslot((size_t)nf);
+  std::vector<int64_t> cnt((size_t)T + 1, 0);
+  // contributions per block-slot (each slot belongs to one row: rows fill theirs independently)
+  auto for_contrib = [&](int64_t r, const std::vector<int32_t>& cols, auto&& emit) {
+    const int64_t sl = r / 32, l = r % 32;
+    for (int64_t k = cp[nbc + r]; k < cp[nbc + r + 1]; k++) {
+      const int64_t ent = ce[k], e = ent >> 2;
+      const int a = (int)(ent & 3);
+      const int32_t v[4] = {tt[e].x, tt[e].y, tt[e].z, tt[e].w};
+      for (int b = 0; b < 4; b++) {
+        if (v[b] < nbc) continue;
+        const int64_t pos = std::lower_bound(cols.begin(), cols.end(), v[b] - (int32_t)nbc) - cols.begin();
+        emit(base[sl] + 32 * pos + l, (uint32_t)(16 * e + 4 * a + b));
+      }
+    }
+  };
+  parallel_rows(nf, [&](int64_t a, int64_t b) {
+    std::vector<int32_t> cols;
+    for (int64_t r = a; r < b; r++) {
+      columns(r, cols);
+      const int64_t sl = r / 32, l = r % 32, w = (base[sl + 1] - base[sl]) / 32;
+      for (int64_t k = 0; k < w; k++) {
+        const int64_t t = base[sl] + 32 * k + l;
+        scol[t] = k < (int64_t)cols.size() ? cols[k] : (int32_t)r;
+        if (k < (int64_t)cols.size() && cols[k] == (int32_t)r) dslot[r] = (int32_t)t;
+      }
+      for_contrib(r, cols, [&](int64_t t, uint32_t) { cnt[t + 1]++; });
+    }
+  });
+  for (int64_t t = 0; t < T; t++) cnt[t + 1] += cnt[t];
+  std::vector<uint32_t> code((size_t)cnt[T]);
+  parallel_rows(nf, [&](int64_t a, int64_t b) {
+    std::vector<int32_t> cols;
+    std::vector<int64_t> fill;
+    for (int64_t r = a; r < b; r++) {
+      columns(r, cols);
+      for_contrib(r, cols, [&](int64_t t, uint32_t c) {
+        // slots of one row are visited only by this thread: cnt[t] advances as the slot's cursor
+        code[cnt[t]++] = c;
+      });
+    }
+  });
+  // the fill advanced cnt[t] to the end of slot t's list: shift back to start offsets
+  for (int64_t t = T; t > 0; t--) cnt[t] = cnt[t - 1];
+  cnt[0] = 0;
+  TRY(dalloc(&h->sell_base, base.size()));
+  TRY(dalloc(&h->sell_col, std::max<size_t>(scol.size(), 1)));
+  TRY(dalloc(&h->sell_cptr, cnt.size()));
+  TRY(dalloc(&h->sell_code, std::max<size_t>(code.size(), 1)));
+  TRY(dalloc(&h->sell_dslot, std::max<size_t>(dslot.size(), 1)));
+  TRY(dalloc(&h->sell_vals32, std::max<size_t>(9 * (size_t)T, 1)));
+  CU(cudaMemcpyAsync(h->sell_base, base.data(), base.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  if (T > 0) CU(cudaMemcpyAsync(h->sell_col, scol.data(), scol.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->sell_cptr, cnt.data(), cnt.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  if (!code.empty())
+    CU(cudaMemcpyAsync(h->sell_code, code.data(), code.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if (nf > 0) CU(cudaMemcpyAsync(h->sell_dslot, dslot.data(), dslot.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemsetAsync(h->sell_vals32, 0, 9 * (size_t)T * sizeof(float), h->stream));
+  TRY(sync(h));
+  h->sell_T = T;
+  h->sell_nnzb = nnzb;
+  return 0;
+}
+
+// assemble the FP32 tangent at the current state into the sliced-ELL values
+static int sell_assemble32(sfem_handle* h) {
+  TRY(sell_structure(h));
+  // 12-slot blocks per element: 16 for the corotational tangents (not symmetric), 10 otherwise
+  const int nb_alloc = (h->material == SFEM_MMT_COROTATIONAL) ? 16 : 10;
+  if (!h->sell_ke32) TRY(dalloc(&h->sell_ke32, (size_t)h->E * 12 * nb_alloc));
+  const float* u32 = disp<float>(h);
+  const ElemView<float> ev = ev_of<float>(h);
+  int nb = 10;
+  with_mat<float>(mat_id(h), [&](auto m) {
+    nb = launch_element_stiffness_sym<float, decltype(m)::value>(ev, u32, h->sell_ke32, h->stream);
+  });
+  launch_assemble_sell<float>(h->sell_T, h->sell_cptr, h->sell_code, h->sell_ke32, nb, h->nbc, h->nf, h->sell_dslot,
+                              h->dt > 0 ? h->mass : nullptr, h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0,
+                              h->sell_vals32, h->stream);
+  CU(cudaGetLastError());
+  return 0;
+}
+
+// The FP32 Krylov solves' operator for their duration: with op_mode 1 the tangent is assembled
+// at the current state and the loops use it; the patch product otherwise.
+struct OperatorScope {
+  sfem_handle* h;
+  int st = 0;
+  explicit OperatorScope(sfem_handle* hh) : h(hh) {
+    if (h->op_mode == 1 && h->n_inst == 0) {
+      st = sell_assemble32(h);
+      h->sell_on = st == 0;
+    }
+  }
+  ~OperatorScope() { h->sell_on = false; }
+};
+
 // assemble the FP64 tangent at the current state into h->bsr_vals
 static int bsr_assemble(sfem_handle* h) {
   TRY(bsr_structure(h));
   double* Ke = nullptr;
   TRY(dalloc(&Ke, (size_t)h->E * 144));
   const ElemView<double> ev = h->ev64();
-  with_mat<double>(mat_id(h), [&](auto m) { launch_element_stiffness<decltype(m)::value>(ev, h->u, Ke, h->stream); });
+  with_mat<double>(mat_id(h), [&](auto m) { launch_element_stiffness<double, decltype(m)::value>(ev, h->u, Ke, h->stream); });
   CU(cudaMemsetAsync(h->bsr_vals, 0, 9 * (size_t)h->bsr_nnzb * sizeof(double), h->stream));
   launch_assemble_bsr(h->nbc, h->N, h->csr(), Ke, h->bsr_slot, h->bsr_dslot, h->dt > 0 ? h->mass : nullptr,
                       h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0, h->bsr_vals, h->stream);
   const int st = sync(h);
   cudaFree(Ke);
   return st;
+}
+
+int sfem_set_operator(sfem_handle* h, int32_t op) {
+  TRY(check_handle(h));
+  if (op != SFEM_OP_MATRIX_FREE && op != SFEM_OP_ASSEMBLED)
+    return fail(SFEM_ERR_INVALID, "operator is SFEM_OP_MATRIX_FREE (0) or SFEM_OP_ASSEMBLED (1)");
+  h->op_mode = op;
+  return SFEM_OK;
 }
 
 int sfem_tangent_nnz(sfem_handle* h, int64_t* nnzb) {
@@ -1497,6 +1722,8 @@ int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* op
     CU(cudaMemcpyAsync(x, w.x + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   } else {
     KrylovWs<float>& w = h->k32;
+    OperatorScope ops(h);
+    TRY(ops.st);
     CU(cudaMemcpyAsync(h->tmp64 + o, b, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     launch_convert<double, float>((int64_t)n, h->tmp64 + o, w.b + o, h->stream);
     const float* u32 = disp<float>(h);
@@ -1544,6 +1771,8 @@ int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
     CU(cudaMemcpyAsync(h->tmp64 + o, w.x + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
   } else {
     KrylovWs<float>& w = h->k32;
+    OperatorScope ops(h);
+    TRY(ops.st);
     const float* u32 = disp<float>(h);
     launch_convert<double, float>((int64_t)n, h->r64 + o, w.b + o, h->stream);
     if (pc) TRY(jacobi<float>(h, w.dinv, nullptr));
@@ -2170,7 +2399,10 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   const int check_every = 16;
   int it = 0;
   bool pending = false;
-  if (h->profiling) h->prof_precision = SFEM_FP32;
+  if (h->profiling) {
+    h->prof_precision = SFEM_FP32;
+    h->prof_op = h->sell_on ? 1 : 0;
+  }
   for (;;) {
     CU(cudaMemcpyAsync(h->scal_h, h->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
     TRY(sync(h));
@@ -2189,13 +2421,13 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
       float* pold = pbuf[it % 2];
       float* pnew = pbuf[(it + 1) % 2];
       if (sample) CU(cudaEventRecord(h->pev[0], h->stream));
-      hvp<float>(h, w.u, pold, w.q, h->scal, sample ? h->pev[1] : nullptr, w.r, w.dinv, pnew, g->z);
+      krylov_hvp<float>(h, w.u, pold, w.q, sample ? h->pev[1] : nullptr, w.r, w.dinv, pnew, g->z);
       if (sample) {
         CU(cudaEventRecord(h->pev[2], h->stream));
         pending = true;
       }
       if (h->profiling) h->prof_launches++;
-      launch_fcg_update_patch<float>(h->nbc, h->N, h->bslot, reinterpret_cast<const float*>(h->partial), x,
+      launch_fcg_update_patch<float>(h->nbc, h->N, krylov_bslot<float>(h), reinterpret_cast<const float*>(h->partial), x,
                                      w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream, xs ? w.dinv : nullptr, xs);
       precondition(true);
     }
@@ -2230,6 +2462,8 @@ int sfem_gnn_inner_solve(sfem_handle* h, double eta, int max_cg, int* its) {
   TRY(gnn_need(h));
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
   KrylovWs<float>& w = h->k32;
+  OperatorScope ops(h);
+  TRY(ops.st);
   launch_convert<double, float>(3 * h->N, h->u, w.u, h->stream);
   launch_convert<double, float>((int64_t)n, h->r64 + o, w.b + o, h->stream);
   TRY(gnn_refresh_diag(h));

@@ -209,12 +209,31 @@ void launch_nh_cache(const ElemView<T>& ev, const T* u, T* cache, cudaStream_t s
 // assembled tangent: element stiffness (144 doubles per element), block-CSR assembly over free
 // nodes (slot: 16 per element, -1 for a fixed corner; dslot: diagonal block of each free node),
 // block-CSR product
-template <int MAT>
-void launch_element_stiffness(const ElemView<double>& ev, const double* u, double* Ke, cudaStream_t st);
+template <typename T, int MAT>
+void launch_element_stiffness(const ElemView<T>& ev, const T* u, T* Ke, cudaStream_t st);
 void launch_assemble_bsr(int64_t nbc, int64_t N, NodeCsr csr, const double* Ke, const int32_t* slot,
                          const int32_t* dslot, const double* mass, double inv_h2, double* vals, cudaStream_t st);
 void launch_bsr_spmv(int64_t nrows, const int32_t* rowptr, const int32_t* col, const double* vals, const double* x,
                      double* y, cudaStream_t st);
+// the same tangent in sliced ELL for the Krylov loops (32 rows per slice; block-slot t of row r is
+// base[r / 32] + 32 k + r % 32, values at 9 (t - t % 32) + 32 q + t % 32, q = 3 i + c)
+// element stiffness as 3 x 3 blocks of 12 slots: the ten blocks a <= b of a symmetric tangent, all
+// sixteen of a corotational one (returns the block count, 10 or 16); neo-Hookean in closed form
+template <typename T, int MAT>
+int launch_element_stiffness_sym(const ElemView<T>& ev, const T* u, T* Ke, cudaStream_t st);
+// assembly: block-slot t sums its contributions code[cptr[t] .. cptr[t+1]) (code = 16 e + 4 a + b:
+// block (a, b) of element e, from Ke in the ten-block layout); with mass, (m / h^2) I on each
+// diagonal block
+template <typename T>
+void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* code, const T* Ke, int nb,
+                          int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass, double inv_h2, T* vals,
+                          cudaStream_t st);
+// q = K p over the free rows (+ p.q, alpha with s); with p_new the direction is formed on the fly,
+// p = (z or D^-1 r) + beta p_old, as the patch product does
+template <typename T>
+void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const T* vals, const T* p,
+                     T* q, Reduce red, CgScalars* s, cudaStream_t st, const T* r = nullptr, const T* dinv = nullptr,
+                     T* p_new = nullptr, const T* z = nullptr);
 // implicit dynamics: per patch-node slot mass share m_g / (h^2 k_g) (k_g patches touch g)
 template <typename T>
 void launch_patch_mass(int64_t n_slots, int64_t nbc, const int32_t* pnode, const int32_t* bidx, PatchBoundary pb,

@@ -847,29 +847,29 @@ void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* 
 //   K_(a,i),(b,c) = vol * (dP^{(b,c)} g_a)_i,  dP^{(b,c)} = tangent(e_c g_b^T),
 // the columns of ElasticEnergy::ComputeLocalStiffnessMatrixFromDifferential
 // (Source/ElasticEnergy.cpp:493-517) in closed form; FP64.
-template <int MAT>
-__global__ void __launch_bounds__(kThreads) k_element_stiffness(ElemView<double> ev, const double* __restrict__ u,
-                                                                double* __restrict__ Ke) {
+template <typename T, int MAT>
+__global__ void __launch_bounds__(kThreads) k_element_stiffness(ElemView<T> ev, const T* __restrict__ u,
+                                                                T* __restrict__ Ke) {
   const int64_t E = ev.E;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
     const int4 t = ev.tets[e];
-    M3<double> X;
+    M3<T> X;
 #pragma unroll
     for (int k = 0; k < 9; k++) X.a[k] = ev.X[k * E + e];
-    const double vol = ev.vol[e];
-    double mu = ev.mu, la = ev.lambda;
+    const T vol = ev.vol[e];
+    T mu = ev.mu, la = ev.lambda;
     if (ev.scale) {
-      const double sc = ev.scale[e];
+      const T sc = ev.scale[e];
       mu *= sc;
       la *= ev.scale_la ? ev.scale_la[e] : sc;
     }
-    M3<double> F = grad_of(u, t, X);
-    F.a[0] += 1.0;
-    F.a[4] += 1.0;
-    F.a[8] += 1.0;
-    Tangent<double, MAT> tg;
+    M3<T> F = grad_of(u, t, X);
+    F.a[0] += T(1);
+    F.a[4] += T(1);
+    F.a[8] += T(1);
+    Tangent<T, MAT> tg;
     tg.init(F, mu, la);
-    double g[4][3];
+    T g[4][3];
 #pragma unroll
     for (int j = 0; j < 3; j++) {
       g[0][j] = -(X.a[j] + X.a[3 + j] + X.a[6 + j]);
@@ -877,18 +877,18 @@ __global__ void __launch_bounds__(kThreads) k_element_stiffness(ElemView<double>
       g[2][j] = X.a[3 + j];
       g[3][j] = X.a[6 + j];
     }
-    double* K = Ke + 144 * e;
+    T* K = Ke + 144 * e;
 #pragma unroll 1
     for (int b = 0; b < 4; b++) {
 #pragma unroll 1
       for (int c = 0; c < 3; c++) {
-        M3<double> dF;
+        M3<T> dF;
 #pragma unroll
-        for (int q = 0; q < 9; q++) dF.a[q] = 0.0;
+        for (int q = 0; q < 9; q++) dF.a[q] = T(0);
         dF.a[3 * c] = g[b][0];
         dF.a[3 * c + 1] = g[b][1];
         dF.a[3 * c + 2] = g[b][2];
-        const M3<double> dP = tg.apply(dF);
+        const M3<T> dP = tg.apply(dF);
 #pragma unroll
         for (int a = 0; a < 4; a++)
 #pragma unroll
@@ -900,17 +900,25 @@ __global__ void __launch_bounds__(kThreads) k_element_stiffness(ElemView<double>
   }
 }
 
-template <int MAT>
-void launch_element_stiffness(const ElemView<double>& ev, const double* u, double* Ke, cudaStream_t st) {
+template <typename T, int MAT>
+void launch_element_stiffness(const ElemView<T>& ev, const T* u, T* Ke, cudaStream_t st) {
   count_launch();
-  k_element_stiffness<MAT><<<grid_for(ev.E), kThreads, 0, st>>>(ev, u, Ke);
+  k_element_stiffness<T, MAT><<<grid_for(ev.E), kThreads, 0, st>>>(ev, u, Ke);
 }
-template void launch_element_stiffness<0>(const ElemView<double>&, const double*, double*, cudaStream_t);
-template void launch_element_stiffness<1>(const ElemView<double>&, const double*, double*, cudaStream_t);
-template void launch_element_stiffness<2>(const ElemView<double>&, const double*, double*, cudaStream_t);
-template void launch_element_stiffness<3>(const ElemView<double>&, const double*, double*, cudaStream_t);
-template void launch_element_stiffness<4>(const ElemView<double>&, const double*, double*, cudaStream_t);
-#define SFEM_INST_STIFF(M) template void launch_element_stiffness<M>(const ElemView<double>&, const double*, double*, cudaStream_t);
+#define SFEM_INST_STIFF(M)                                                                                     \
+  template void launch_element_stiffness<double, M>(const ElemView<double>&, const double*, double*, cudaStream_t);
+#define SFEM_INST_STIFF32(M)                                                                                   \
+  template void launch_element_stiffness<float, M>(const ElemView<float>&, const float*, float*, cudaStream_t);
+SFEM_INST_STIFF(0)
+SFEM_INST_STIFF(1)
+SFEM_INST_STIFF(2)
+SFEM_INST_STIFF(3)
+SFEM_INST_STIFF(4)
+SFEM_INST_STIFF32(0)
+SFEM_INST_STIFF32(1)
+SFEM_INST_STIFF32(2)
+SFEM_INST_STIFF32(3)
+SFEM_INST_STIFF32(4)
 SFEM_INST_STIFF(5)
 SFEM_INST_STIFF(6)
 SFEM_INST_STIFF(7)
@@ -961,6 +969,294 @@ void launch_assemble_bsr(int64_t nbc, int64_t N, NodeCsr csr, const double* Ke, 
   count_launch();
   k_assemble_bsr<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, Ke, slot, dslot, mass, inv_h2, vals);
 }
+
+// Element stiffness for the sliced-ELL assembly, block (a, b) row-major [i][c] in 12 slots (9 used),
+// written as 16-byte stores.  Symmetric tangents (linear, StVK, neo-Hookean) store the ten blocks
+// a <= b in the order (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3) (120 values per
+// element); the corotational tangents, which are not symmetric, all sixteen in the order 4 a + b
+// (192 values).  Neo-Hookean in closed form, with g_a the corner gradients and h_a = F^-T g_a:
+//   K_ab[i][c] = vol (mu (g_a . g_b) d_ic + (mu - lambda log J) (h_b)_i (h_a)_c + lambda (h_a)_i (h_b)_c),
+// the other materials from their tangent's columns as k_element_stiffness.
+template <int MAT>
+__host__ __device__ constexpr int stiffness_blocks() { return (MAT == kCorot || MAT == kCorotExact) ? 16 : 10; }
+
+template <typename T, int MAT>
+__global__ void __launch_bounds__(kThreads) k_element_stiffness_sym(ElemView<T> ev, const T* __restrict__ u,
+                                                                    T* __restrict__ Ke) {
+  constexpr int NB = stiffness_blocks<MAT>();
+  const int64_t E = ev.E;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int4 t = ev.tets[e];
+    M3<T> X;
+#pragma unroll
+    for (int k = 0; k < 9; k++) X.a[k] = ev.X[k * E + e];
+    const T vol = ev.vol[e];
+    T mu = ev.mu, la = ev.lambda;
+    if (ev.scale) {
+      const T sc = ev.scale[e];
+      mu *= sc;
+      la *= ev.scale_la ? ev.scale_la[e] : sc;
+    }
+    M3<T> F = grad_of(u, t, X);
+    F.a[0] += T(1);
+    F.a[4] += T(1);
+    F.a[8] += T(1);
+    T g[4][3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      g[0][j] = -(X.a[j] + X.a[3 + j] + X.a[6 + j]);
+      g[1][j] = X.a[j];
+      g[2][j] = X.a[3 + j];
+      g[3][j] = X.a[6 + j];
+    }
+    T* K = Ke + 12 * NB * e;
+    if constexpr (MAT == kNeoHookean) {
+      T J;
+      const M3<T> Fi = inverse(F, &J);
+      const T c1 = mu - la * dev_log<T>(J);
+      T hh[4][3];  // h_a = F^-T g_a: (h_a)_i = sum_k Fi[k][i] g_a[k]
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) hh[a][i] = Fi.a[i] * g[a][0] + Fi.a[3 + i] * g[a][1] + Fi.a[6 + i] * g[a][2];
+      int blk = 0;
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+#pragma unroll
+        for (int b = a; b < 4; b++, blk++) {
+          const T gg = mu * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]);
+          T v[12];
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+              v[3 * i + c] = vol * ((i == c ? gg : T(0)) + c1 * hh[b][i] * hh[a][c] + la * hh[a][i] * hh[b][c]);
+          v[9] = v[10] = v[11] = T(0);
+          store12(K + 12 * blk, 0, v);
+        }
+      }
+    } else {
+      Tangent<T, MAT> tg;
+      tg.init(F, mu, la);
+      // column (b, c) of the element matrix gives rows a <= b of block (a, b)
+      T cols[3][12];
+#pragma unroll 1
+      for (int b = 0; b < 4; b++) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          M3<T> dF;
+#pragma unroll
+          for (int q = 0; q < 9; q++) dF.a[q] = T(0);
+          dF.a[3 * c] = g[b][0];
+          dF.a[3 * c + 1] = g[b][1];
+          dF.a[3 * c + 2] = g[b][2];
+          const M3<T> dP = tg.apply(dF);
+#pragma unroll
+          for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+              cols[c][3 * a + i] = vol * (dP.a[3 * i] * g[a][0] + dP.a[3 * i + 1] * g[a][1] + dP.a[3 * i + 2] * g[a][2]);
+        }
+#pragma unroll 1
+        for (int a = 0; a < (NB == 16 ? 4 : b + 1); a++) {
+          const int blk = NB == 16 ? 4 * a + b : a == 0 ? b : a == 1 ? 3 + b : a == 2 ? 5 + b : 9;
+          T v[12];
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) v[3 * i + c] = cols[c][3 * a + i];
+          v[9] = v[10] = v[11] = T(0);
+          store12(K + 12 * blk, 0, v);
+        }
+      }
+    }
+  }
+}
+template <typename T, int MAT>
+int launch_element_stiffness_sym(const ElemView<T>& ev, const T* u, T* Ke, cudaStream_t st) {
+  count_launch();
+  k_element_stiffness_sym<T, MAT><<<grid_for(ev.E), kThreads, 0, st>>>(ev, u, Ke);
+  return stiffness_blocks<MAT>();
+}
+template int launch_element_stiffness_sym<float, 0>(const ElemView<float>&, const float*, float*, cudaStream_t);
+template int launch_element_stiffness_sym<float, 1>(const ElemView<float>&, const float*, float*, cudaStream_t);
+template int launch_element_stiffness_sym<float, 2>(const ElemView<float>&, const float*, float*, cudaStream_t);
+template int launch_element_stiffness_sym<float, 3>(const ElemView<float>&, const float*, float*, cudaStream_t);
+template int launch_element_stiffness_sym<float, 4>(const ElemView<float>&, const float*, float*, cudaStream_t);
+
+// ---- assembled tangent in sliced ELL (32 rows per slice) for the Krylov loops ----
+// Block-slot t of free row r (slice r / 32, lane l = r % 32, position k in the row) is
+// t = base[slice] + 32 k + l; its nine values sit at vals[9 (t - l) + 32 q + l] (q = 3 i + c), so a
+// warp (one slice) reads each value of a row position with one coalesced 128-byte load.
+
+// the nine used values of a 12-slot, 16-byte aligned block
+__device__ __forceinline__ void load9(const float* K, float (&kb)[9]) {
+  const float4* K4 = reinterpret_cast<const float4*>(K);
+  const float4 a = K4[0], b = K4[1], c = K4[2];
+  kb[0] = a.x; kb[1] = a.y; kb[2] = a.z; kb[3] = a.w;
+  kb[4] = b.x; kb[5] = b.y; kb[6] = b.z; kb[7] = b.w;
+  kb[8] = c.x;
+}
+
+// assembly, one thread per block-slot: the slot's contributions K_e(a, b) (code = 16 e + 4 a + b;
+// Ke in the ten-block symmetric layout of k_element_stiffness_sym) in the order of its row's element entries (the node->element CSR order, deterministic), summed
+// in registers and stored once (consecutive slots of a slice store coalesced)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_assemble_sell(int64_t nslots, const int64_t* __restrict__ cptr,
+                                                            const uint32_t* __restrict__ code, const T* __restrict__ Ke,
+                                                            int nb, T* __restrict__ vals) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nslots; t += (int64_t)gridDim.x * blockDim.x) {
+    T acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) acc[q] = T(0);
+    for (int64_t c = cptr[t]; c < cptr[t + 1]; c++) {
+      const uint32_t v = code[c];
+      const int a = (int)((v >> 2) & 3), b = (int)(v & 3);
+      const int lo = a < b ? a : b, hi = a < b ? b : a;
+      const int blk = nb == 16 ? 4 * a + b : lo == 0 ? hi : lo == 1 ? 3 + hi : lo == 2 ? 5 + hi : 9;
+      T kb[9];
+      load9(Ke + 12 * nb * (int64_t)(v >> 4) + 12 * blk, kb);
+      if (nb == 16 || a <= b) {
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[q] += kb[q];
+      } else {  // block (a, b) is the transpose of the stored block (b, a)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int cc = 0; cc < 3; cc++) acc[3 * i + cc] += kb[3 * cc + i];
+      }
+    }
+    T* V = vals + 9 * (t & ~(int64_t)31) + (t & 31);
+#pragma unroll
+    for (int q = 0; q < 9; q++) V[32 * q] = acc[q];
+  }
+}
+// implicit dynamics: (m / h^2) I added to each free row's diagonal block
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_sell_mass(int64_t nbc, int64_t nf, const int32_t* __restrict__ dslot,
+                                                        const double* __restrict__ mass, double inv_h2,
+                                                        T* __restrict__ vals) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nf; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = dslot[r];
+    T* V = vals + 9 * (t & ~(int64_t)31) + (t & 31);
+    const T m = (T)(mass[nbc + r] * inv_h2);
+    V[0] += m;
+    V[32 * 4] += m;
+    V[32 * 8] += m;
+  }
+}
+template <typename T>
+void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* code, const T* Ke, int nb,
+                          int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass, double inv_h2, T* vals,
+                          cudaStream_t st) {
+  count_launch();
+  k_assemble_sell<T><<<grid_for(nslots), kThreads, 0, st>>>(nslots, cptr, code, Ke, nb, vals);
+  if (mass) {
+    count_launch();
+    k_sell_mass<T><<<grid_for(nf), kThreads, 0, st>>>(nbc, nf, dslot, mass, inv_h2, vals);
+  }
+}
+template void launch_assemble_sell<float>(int64_t, const int64_t*, const uint32_t*, const float*, int, int64_t,
+                                          int64_t, const int32_t*, const double*, double, float*, cudaStream_t);
+
+// q = K p over the free rows from the sliced-ELL tangent, one thread per row (a warp per slice).
+// DIR (Krylov iteration): the direction is formed where it is read, as in the patch product,
+// p = (z or D^-1 r) + beta p_old, and written to p_new for the row's node.  With s: p.q and
+// alpha = r.z / p.q by the last block (non-finite or non-positive p.q ends the solve).
+template <typename T, bool DIR>
+__global__ void __launch_bounds__(kThreads) k_sell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
+                                                       const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                                       const T* __restrict__ p, T* __restrict__ q, Reduce red,
+                                                       CgScalars* s, const T* __restrict__ r,
+                                                       const T* __restrict__ dinv, T* __restrict__ p_new,
+                                                       const T* __restrict__ z) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (s != nullptr && s->done) return;
+  T beta = T(0);
+  bool use_z = false;
+  if (DIR) {
+    beta = (T)s->beta;
+    use_z = z != nullptr && s->jac == 0;
+  }
+  T acc = T(0);
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nf; row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sl = row >> 5;
+    const int lane = (int)(row & 31);
+    const int64_t b0 = base[sl], w = (base[sl + 1] - b0) >> 5;
+    T y0 = T(0), y1 = T(0), y2 = T(0);
+    for (int64_t k = 0; k < w; k++) {
+      const int64_t j = 3 * (nbc + (int64_t)col[b0 + 32 * k + lane]);
+      const T* V = vals + 9 * (b0 + 32 * k) + lane;
+      T x0, x1, x2;
+      if (DIR) {
+        x0 = (use_z ? z[j] : dinv[j] * r[j]) + beta * p[j];
+        x1 = (use_z ? z[j + 1] : dinv[j + 1] * r[j + 1]) + beta * p[j + 1];
+        x2 = (use_z ? z[j + 2] : dinv[j + 2] * r[j + 2]) + beta * p[j + 2];
+      } else {
+        x0 = p[j];
+        x1 = p[j + 1];
+        x2 = p[j + 2];
+      }
+      y0 += V[0] * x0 + V[32] * x1 + V[64] * x2;
+      y1 += V[96] * x0 + V[128] * x1 + V[160] * x2;
+      y2 += V[192] * x0 + V[224] * x1 + V[256] * x2;
+    }
+    const int64_t o = 3 * (nbc + row);
+    T p0, p1, p2;
+    if (DIR) {
+      p0 = (use_z ? z[o] : dinv[o] * r[o]) + beta * p[o];
+      p1 = (use_z ? z[o + 1] : dinv[o + 1] * r[o + 1]) + beta * p[o + 1];
+      p2 = (use_z ? z[o + 2] : dinv[o + 2] * r[o + 2]) + beta * p[o + 2];
+      p_new[o] = p0;
+      p_new[o + 1] = p1;
+      p_new[o + 2] = p2;
+    } else {
+      p0 = p[o];
+      p1 = p[o + 1];
+      p2 = p[o + 2];
+    }
+    q[o] = y0;
+    q[o + 1] = y1;
+    q[o + 2] = y2;
+    acc += p0 * y0 + p1 * y1 + p2 * y2;
+  }
+  if (s == nullptr) return;
+  T v[1] = {acc}, tot[1];
+  if (reduce_last<T, 1>(v, red, tot) && threadIdx.x == 0) {
+    const double pq = (double)tot[0];
+    s->pq = pq;
+    if (!isfinite(pq)) {
+      s->done = 1;
+      s->status = -3;
+      s->alpha = 0.0;
+    } else if (!(pq > 0.0)) {
+      s->done = 1;
+      s->status = 2;
+      s->alpha = 0.0;
+    } else {
+      s->alpha = s->rz / pq;
+    }
+  }
+}
+template <typename T>
+void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const T* vals, const T* p,
+                     T* q, Reduce red, CgScalars* s, cudaStream_t st, const T* r, const T* dinv, T* p_new,
+                     const T* z) {
+  static const int wave = std::min(resident_ctas(k_sell_hvp<T, true>, kThreads, 0),
+                                   resident_ctas(k_sell_hvp<T, false>, kThreads, 0));
+  const int grid = std::max(1, std::min(wave, (int)((nf + kThreads - 1) / kThreads)));
+  count_launch();
+  if (p_new != nullptr)
+    launch_pdl(k_sell_hvp<T, true>, grid, kThreads, 0, st, nbc, nf, base, col, vals, p, q, red, s, r, dinv, p_new,
+               z);
+  else
+    launch_pdl(k_sell_hvp<T, false>, grid, kThreads, 0, st, nbc, nf, base, col, vals, p, q, red, s, nullptr, nullptr,
+               nullptr, nullptr);
+}
+template void launch_sell_hvp<float>(int64_t, int64_t, const int64_t*, const int32_t*, const float*, const float*,
+                                     float*, Reduce, CgScalars*, cudaStream_t, const float*, const float*, float*,
+                                     const float*);
 
 // y = A x for a block-CSR matrix with 3 x 3 blocks (one thread per block row)
 __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int64_t nrows, const int32_t* __restrict__ rowptr,
@@ -1531,7 +1827,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update_patch(int64_t nbc, int64
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * g;
     T qq[3];
-    node_q(q, partial, bslot[g], o, qq);
+    node_q(q, partial, bslot ? bslot[g] : make_int2(0, 0), o, qq);
 #pragma unroll
     for (int c2 = 0; c2 < 3; c2++) {
       x[o + c2] += a * p[o + c2];
@@ -1578,7 +1874,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * g;
     T qq[3];
-    node_q(q, partial, bslot[g], o, qq);
+    node_q(q, partial, bslot ? bslot[g] : make_int2(0, 0), o, qq);
     T rn[3];
 #pragma unroll
     for (int c2 = 0; c2 < 3; c2++) {

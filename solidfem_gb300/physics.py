@@ -331,6 +331,13 @@ class FemPhysicsMatrixFree:
         nat.check(self._lib.sfem_adjoint(self._h, _dp(g), rel_tol, max_cg, _dp(dE), _dp(df)))
         return dE, df
 
+    def set_operator(self, op: str) -> None:
+        """Operator of the FP32 Krylov solves: 'matrix-free' (the patch product, default) or
+        'assembled' (the tangent assembled in FP32 at every Newton step, one sparse product per
+        iteration)."""
+        nat.check(self._lib.sfem_set_operator(self._h, {"matrix-free": nat.OP_MATRIX_FREE,
+                                                         "assembled": nat.OP_ASSEMBLED}[op]))
+
     def set_profiling(self, enable=True):
         nat.check(self._lib.sfem_set_profiling(self._h, int(enable)))
 
