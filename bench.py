@@ -53,6 +53,9 @@ FP64_JACOBI_COUNTS = {"newton_iters": 5, "cg_iters": 10166, "residual_evals": 6}
 
 
 HVP_DRAM_BYTES_PER_TET = 220.1e6 / 3145728  # k_patch_hvp<float, NH, DIR> (ncu, see the traffic note below)
+# k_sell_hvp<float, DIR>: ncu dram__bytes_read.sum + dram__bytes_write.sum on the 128x64x64 case, 331.0 + 10.9 MB
+# per launch, against its 341.1 MB of algorithmic bytes (7,884,222 blocks x 40 B + 536,640 free nodes x 48 B)
+SELL_DRAM_PER_ALGO_BYTE = (331.0e6 + 10.9e6) / 341.1276e6
 
 
 def peaks():
@@ -346,8 +349,9 @@ def run_gpu_arm(args):
     # by the tet count (the element data streams once per launch, far above L2 in both cases)
     if args.operator == "assembled":
         kernel = "k_sell_hvp<float> (tangent assembled per Newton step, sliced-ELL sparse product)"
-        traffic = args.traffic
-        traffic_source = "--traffic" if args.traffic else None
+        traffic = args.traffic if args.traffic else SELL_DRAM_PER_ALGO_BYTE * prof["algo_bytes_hvp"]
+        traffic_source = ("ncu capture at 3,145,728 tets scaled by the algorithmic bytes" if not args.traffic
+                          else "--traffic")
     else:
         kernel = "k_patch_hvp<float, neo-Hookean> (fused element Hessian-vector product)"
         traffic = args.traffic if args.traffic else HVP_DRAM_BYTES_PER_TET * m.n_tets
@@ -415,8 +419,10 @@ def main():
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")
-    ap.add_argument("--operator", default="matrix-free", choices=["matrix-free", "assembled"],
-                    help="operator of the FP32 Krylov solves (the FP64 baseline stays matrix-free)")
+    ap.add_argument("--operator", default="assembled", choices=["matrix-free", "assembled"],
+                    help="operator of the FP32 Krylov solves: the tangent assembled per Newton step "
+                         "(default, faster) or the matrix-free patch product; the FP64 baseline stays "
+                         "matrix-free")
     args = ap.parse_args()
     if args.warmup < 3 and not args.small:
         args.warmup = 3
