@@ -132,6 +132,7 @@ struct sfem_handle {
   int64_t sell_T = -1, sell_nnzb = 0;  // block-slots (with padding), blocks
   int64_t *sell_base = nullptr, *sell_cptr = nullptr;
   int32_t *sell_col = nullptr, *sell_dslot = nullptr;
+  int16_t* sell_col16 = nullptr;  // the columns as differences to the row, when all fit (else sell_col)
   uint32_t* sell_code = nullptr;
   float *sell_vals32 = nullptr, *sell_ke32 = nullptr;
   int32_t prof_op = 0;  // operator of the sampled Krylov launches
@@ -298,7 +299,8 @@ void krylov_hvp(sfem_handle* h, const T* u, const T* p, T* q, cudaEvent_t mid, c
                 const T* z = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
     if (h->sell_on) {
-      launch_sell_hvp<float>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_vals32, p, q, h->red(), h->scal,
+      launch_sell_hvp<float>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, h->sell_vals32, p, q, h->red(),
+                             h->scal,
                              h->stream, r, dinv, p_new, z);
       if (mid) cudaEventRecord(mid, h->stream);
       return;
@@ -868,7 +870,8 @@ int sfem_destroy(sfem_handle* h) {
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
-                   h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32, h->sell_ke32};
+                   h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32, h->sell_ke32,
+                   h->sell_col16};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
@@ -915,7 +918,7 @@ int sfem_get_profile(const sfem_handle* h, sfem_profile* out) {
   const double sz = h->prof_precision == SFEM_FP32 ? 4.0 : 8.0;
   if (h->prof_op == 1)  // assembled tangent: blocks and their column indices, and per free node the
                         // direction inputs (z or r, p_old) and outputs (p, q)
-    out->algo_bytes_hvp = (double)h->sell_nnzb * (9.0 * sz + 4.0) + (double)h->nf * 12.0 * sz;
+    out->algo_bytes_hvp = (double)h->sell_nnzb * (9.0 * sz + (h->sell_col16 ? 2.0 : 4.0)) + (double)h->nf * 12.0 * sz;
   else
     out->algo_bytes_hvp = (double)h->E * (16.0 + 10.0 * sz) + (double)h->N * 9.0 * sz;
   out->precision = h->prof_precision;
@@ -1136,14 +1139,40 @@ static int sell_structure(sfem_handle* h) {
   // the fill advanced cnt[t] to the end of slot t's list: shift back to start offsets
   for (int64_t t = T; t > 0; t--) cnt[t] = cnt[t - 1];
   cnt[0] = 0;
+  // 16-bit column differences (2 instead of 4 bytes per block) when every |column - row| fits
+  bool fits16 = true;
+  for (int64_t r = 0; r < nf && fits16; r++) {
+    const int64_t sl = r / 32, l = r % 32, w = (base[sl + 1] - base[sl]) / 32;
+    for (int64_t k = 0; k < w; k++) {
+      const int64_t d = (int64_t)scol[base[sl] + 32 * k + l] - r;
+      if (d < -32768 || d > 32767) {
+        fits16 = false;
+        break;
+      }
+    }
+  }
   TRY(dalloc(&h->sell_base, base.size()));
-  TRY(dalloc(&h->sell_col, std::max<size_t>(scol.size(), 1)));
+  if (fits16) {
+    std::vector<int16_t> d16((size_t)T, 0);
+    for (int64_t r = 0; r < nf; r++) {
+      const int64_t sl = r / 32, l = r % 32, w = (base[sl + 1] - base[sl]) / 32;
+      for (int64_t k = 0; k < w; k++) {
+        const int64_t t = base[sl] + 32 * k + l;
+        d16[t] = (int16_t)((int64_t)scol[t] - r);
+      }
+    }
+    TRY(dalloc(&h->sell_col16, std::max<size_t>(d16.size(), 1)));
+    if (T > 0) CU(cudaMemcpyAsync(h->sell_col16, d16.data(), d16.size() * 2, cudaMemcpyHostToDevice, h->stream));
+    TRY(sync(h));
+  }
+  if (!fits16) TRY(dalloc(&h->sell_col, std::max<size_t>(scol.size(), 1)));
   TRY(dalloc(&h->sell_cptr, cnt.size()));
   TRY(dalloc(&h->sell_code, std::max<size_t>(code.size(), 1)));
   TRY(dalloc(&h->sell_dslot, std::max<size_t>(dslot.size(), 1)));
   TRY(dalloc(&h->sell_vals32, std::max<size_t>(9 * (size_t)T, 1)));
   CU(cudaMemcpyAsync(h->sell_base, base.data(), base.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
-  if (T > 0) CU(cudaMemcpyAsync(h->sell_col, scol.data(), scol.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if (!fits16 && T > 0)
+    CU(cudaMemcpyAsync(h->sell_col, scol.data(), scol.size() * 4, cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemcpyAsync(h->sell_cptr, cnt.data(), cnt.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
   if (!code.empty())
     CU(cudaMemcpyAsync(h->sell_code, code.data(), code.size() * 4, cudaMemcpyHostToDevice, h->stream));

@@ -230,10 +230,11 @@ void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* c
                           cudaStream_t st);
 // q = K p over the free rows (+ p.q, alpha with s); with p_new the direction is formed on the fly,
 // p = (z or D^-1 r) + beta p_old, as the patch product does
+// (columns: col, free-node indices, or col16, differences to the row when every one fits 16 bits)
 template <typename T>
-void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const T* vals, const T* p,
-                     T* q, Reduce red, CgScalars* s, cudaStream_t st, const T* r = nullptr, const T* dinv = nullptr,
-                     T* p_new = nullptr, const T* z = nullptr);
+void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const int16_t* col16,
+                     const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st,
+                     const T* r = nullptr, const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
 // implicit dynamics: per patch-node slot mass share m_g / (h^2 k_g) (k_g patches touch g)
 template <typename T>
 void launch_patch_mass(int64_t n_slots, int64_t nbc, const int32_t* pnode, const int32_t* bidx, PatchBoundary pb,

@@ -1163,9 +1163,9 @@ template void launch_assemble_sell<float>(int64_t, const int64_t*, const uint32_
 // DIR (Krylov iteration): the direction is formed where it is read, as in the patch product,
 // p = (z or D^-1 r) + beta p_old, and written to p_new for the row's node.  With s: p.q and
 // alpha = r.z / p.q by the last block (non-finite or non-positive p.q ends the solve).
-template <typename T, bool DIR>
+template <typename T, bool DIR, typename CI>
 __global__ void __launch_bounds__(kThreads) k_sell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
-                                                       const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                                       const CI* __restrict__ col, const T* __restrict__ vals,
                                                        const T* __restrict__ p, T* __restrict__ q, Reduce red,
                                                        CgScalars* s, const T* __restrict__ r,
                                                        const T* __restrict__ dinv, T* __restrict__ p_new,
@@ -1183,12 +1183,15 @@ __global__ void __launch_bounds__(kThreads) k_sell_hvp(int64_t nbc, int64_t nf, 
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nf; row += (int64_t)gridDim.x * blockDim.x) {
     const int64_t sl = row >> 5;
     const int lane = (int)(row & 31);
-    const int64_t b0 = base[sl], w = (base[sl + 1] - b0) >> 5;
-    T y0 = T(0), y1 = T(0), y2 = T(0);
-    for (int64_t k = 0; k < w; k++) {
-      const int64_t j = 3 * (nbc + (int64_t)col[b0 + 32 * k + lane]);
-      const T* V = vals + 9 * (b0 + 32 * k) + lane;
-      T x0, x1, x2;
+    const int64_t b0 = base[sl];
+    const int w = (int)((base[sl + 1] - b0) >> 5);
+    const CI* cl = col + b0 + lane;
+    // a column is the free-node index (32-bit) or its difference to the row (16-bit)
+    const int64_t cbase = sizeof(CI) == 2 ? row : 0;
+    const T* Vb = vals + 9 * b0 + lane;
+    // the direction at free node jf (3 components)
+    auto xdir = [&](int64_t jf, T& x0, T& x1, T& x2) {
+      const int64_t j = 3 * (nbc + jf);
       if (DIR) {
         x0 = (use_z ? z[j] : dinv[j] * r[j]) + beta * p[j];
         x1 = (use_z ? z[j + 1] : dinv[j + 1] * r[j + 1]) + beta * p[j + 1];
@@ -1198,9 +1201,37 @@ __global__ void __launch_bounds__(kThreads) k_sell_hvp(int64_t nbc, int64_t nf, 
         x1 = p[j + 1];
         x2 = p[j + 2];
       }
-      y0 += V[0] * x0 + V[32] * x1 + V[64] * x2;
-      y1 += V[96] * x0 + V[128] * x1 + V[160] * x2;
-      y2 += V[192] * x0 + V[224] * x1 + V[256] * x2;
+    };
+    T y0 = T(0), y1 = T(0), y2 = T(0);
+    int k = 0;
+    // two block positions per step: their column, value and direction loads are all in flight
+    for (; k + 2 <= w; k += 2) {
+      const int64_t ja = cbase + cl[32 * k], jb = cbase + cl[32 * k + 32];
+      const T* Va = Vb + 288 * k;
+      const T* Wb = Va + 288;
+      T va[9], vb[9];
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        va[q] = Va[32 * q];
+        vb[q] = Wb[32 * q];
+      }
+      T xa0, xa1, xa2, xb0, xb1, xb2;
+      xdir(ja, xa0, xa1, xa2);
+      xdir(jb, xb0, xb1, xb2);
+      y0 += va[0] * xa0 + va[1] * xa1 + va[2] * xa2;
+      y1 += va[3] * xa0 + va[4] * xa1 + va[5] * xa2;
+      y2 += va[6] * xa0 + va[7] * xa1 + va[8] * xa2;
+      y0 += vb[0] * xb0 + vb[1] * xb1 + vb[2] * xb2;
+      y1 += vb[3] * xb0 + vb[4] * xb1 + vb[5] * xb2;
+      y2 += vb[6] * xb0 + vb[7] * xb1 + vb[8] * xb2;
+    }
+    if (k < w) {
+      const T* Va = Vb + 288 * k;
+      T x0, x1, x2;
+      xdir(cbase + cl[32 * k], x0, x1, x2);
+      y0 += Va[0] * x0 + Va[32] * x1 + Va[64] * x2;
+      y1 += Va[96] * x0 + Va[128] * x1 + Va[160] * x2;
+      y2 += Va[192] * x0 + Va[224] * x1 + Va[256] * x2;
     }
     const int64_t o = 3 * (nbc + row);
     T p0, p1, p2;
@@ -1240,23 +1271,31 @@ __global__ void __launch_bounds__(kThreads) k_sell_hvp(int64_t nbc, int64_t nf, 
   }
 }
 template <typename T>
-void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const T* vals, const T* p,
-                     T* q, Reduce red, CgScalars* s, cudaStream_t st, const T* r, const T* dinv, T* p_new,
-                     const T* z) {
-  static const int wave = std::min(resident_ctas(k_sell_hvp<T, true>, kThreads, 0),
-                                   resident_ctas(k_sell_hvp<T, false>, kThreads, 0));
+void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const int16_t* col16,
+                     const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st, const T* r,
+                     const T* dinv, T* p_new, const T* z) {
+  static const int wave = std::min(std::min(resident_ctas(k_sell_hvp<T, true, int32_t>, kThreads, 0),
+                                            resident_ctas(k_sell_hvp<T, false, int32_t>, kThreads, 0)),
+                                   std::min(resident_ctas(k_sell_hvp<T, true, int16_t>, kThreads, 0),
+                                            resident_ctas(k_sell_hvp<T, false, int16_t>, kThreads, 0)));
   const int grid = std::max(1, std::min(wave, (int)((nf + kThreads - 1) / kThreads)));
   count_launch();
-  if (p_new != nullptr)
-    launch_pdl(k_sell_hvp<T, true>, grid, kThreads, 0, st, nbc, nf, base, col, vals, p, q, red, s, r, dinv, p_new,
-               z);
+  if (col16 && p_new != nullptr)
+    launch_pdl(k_sell_hvp<T, true, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, vals, p, q, red, s, r, dinv,
+               p_new, z);
+  else if (col16)
+    launch_pdl(k_sell_hvp<T, false, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, vals, p, q, red, s,
+               nullptr, nullptr, nullptr, nullptr);
+  else if (p_new != nullptr)
+    launch_pdl(k_sell_hvp<T, true, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, vals, p, q, red, s, r, dinv,
+               p_new, z);
   else
-    launch_pdl(k_sell_hvp<T, false>, grid, kThreads, 0, st, nbc, nf, base, col, vals, p, q, red, s, nullptr, nullptr,
-               nullptr, nullptr);
+    launch_pdl(k_sell_hvp<T, false, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, vals, p, q, red, s,
+               nullptr, nullptr, nullptr, nullptr);
 }
-template void launch_sell_hvp<float>(int64_t, int64_t, const int64_t*, const int32_t*, const float*, const float*,
-                                     float*, Reduce, CgScalars*, cudaStream_t, const float*, const float*, float*,
-                                     const float*);
+template void launch_sell_hvp<float>(int64_t, int64_t, const int64_t*, const int32_t*, const int16_t*, const float*,
+                                     const float*, float*, Reduce, CgScalars*, cudaStream_t, const float*,
+                                     const float*, float*, const float*);
 
 // y = A x for a block-CSR matrix with 3 x 3 blocks (one thread per block row)
 __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int64_t nrows, const int32_t* __restrict__ rowptr,
