@@ -135,6 +135,7 @@ struct sfem_handle {
   int16_t* sell_col16 = nullptr;  // the columns as differences to the row, when all fit (else sell_col)
   uint32_t* sell_code = nullptr;
   float *sell_vals32 = nullptr, *sell_ke32 = nullptr;
+  double *sell_vals64 = nullptr, *sell_ke64 = nullptr;
   int32_t prof_op = 0;  // operator of the sampled Krylov launches
   float* pm32 = nullptr;
   DynView dyn() const { return DynView{vel, ustart, 1.0 / dt, 1.0 / (dt * dt)}; }
@@ -297,21 +298,23 @@ void hvp(sfem_handle* h, const T* u, const T* p, T* q, CgScalars* s, cudaEvent_t
 template <typename T>
 void krylov_hvp(sfem_handle* h, const T* u, const T* p, T* q, cudaEvent_t mid, const T* r, const T* dinv, T* p_new,
                 const T* z = nullptr) {
-  if constexpr (std::is_same<T, float>::value) {
-    if (h->sell_on) {
-      launch_sell_hvp<float>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, h->sell_vals32, p, q, h->red(),
-                             h->scal,
-                             h->stream, r, dinv, p_new, z);
-      if (mid) cudaEventRecord(mid, h->stream);
-      return;
-    }
+  if (h->sell_on) {
+    const T* vals;
+    if constexpr (std::is_same<T, float>::value)
+      vals = h->sell_vals32;
+    else
+      vals = h->sell_vals64;
+    launch_sell_hvp<T>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, vals, p, q, h->red(), h->scal,
+                       h->stream, r, dinv, p_new, z);
+    if (mid) cudaEventRecord(mid, h->stream);
+    return;
   }
   hvp<T>(h, u, p, q, h->scal, mid, r, dinv, p_new, z);
 }
 // shared-node partial slots of the patch product (none with the assembled tangent: q is complete)
 template <typename T>
 const int2* krylov_bslot(const sfem_handle* h) {
-  return (std::is_same<T, float>::value && h->sell_on) ? nullptr : h->bslot;
+  return h->sell_on ? nullptr : h->bslot;
 }
 
 // displacement in precision T for the element passes
@@ -382,7 +385,8 @@ template <typename T>
 struct NhCacheGuard {
   sfem_handle* h;
   NhCacheGuard(sfem_handle* hh, const T* u) : h(hh) {
-    if (h->material != SFEM_MMT_NEO_HOOKEAN || sizeof(T) != sizeof(double)) return;
+    // not with the assembled operator, whose blocks already hold the tangent
+    if (h->material != SFEM_MMT_NEO_HOOKEAN || sizeof(T) != sizeof(double) || h->sell_on) return;
     T** c = reinterpret_cast<T**>(sizeof(T) == 8 ? (void*)&h->nhc64 : (void*)&h->nhc32);
     if (!*c && dalloc(c, 12 * (size_t)h->E) != 0) return;  // without memory: the uncached product
     launch_nh_cache<T>(ev_of<T>(h), u, *c, h->stream);
@@ -871,7 +875,7 @@ int sfem_destroy(sfem_handle* h) {
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
                    h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32, h->sell_ke32,
-                   h->sell_col16};
+                   h->sell_col16, h->sell_vals64, h->sell_ke64};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
@@ -1169,7 +1173,7 @@ static int sell_structure(sfem_handle* h) {
   TRY(dalloc(&h->sell_cptr, cnt.size()));
   TRY(dalloc(&h->sell_code, std::max<size_t>(code.size(), 1)));
   TRY(dalloc(&h->sell_dslot, std::max<size_t>(dslot.size(), 1)));
-  TRY(dalloc(&h->sell_vals32, std::max<size_t>(9 * (size_t)T, 1)));
+
   CU(cudaMemcpyAsync(h->sell_base, base.data(), base.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
   if (!fits16 && T > 0)
     CU(cudaMemcpyAsync(h->sell_col, scol.data(), scol.size() * 4, cudaMemcpyHostToDevice, h->stream));
@@ -1177,40 +1181,48 @@ static int sell_structure(sfem_handle* h) {
   if (!code.empty())
     CU(cudaMemcpyAsync(h->sell_code, code.data(), code.size() * 4, cudaMemcpyHostToDevice, h->stream));
   if (nf > 0) CU(cudaMemcpyAsync(h->sell_dslot, dslot.data(), dslot.size() * 4, cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemsetAsync(h->sell_vals32, 0, 9 * (size_t)T * sizeof(float), h->stream));
+
   TRY(sync(h));
   h->sell_T = T;
   h->sell_nnzb = nnzb;
   return 0;
 }
 
-// assemble the FP32 tangent at the current state into the sliced-ELL values
-static int sell_assemble32(sfem_handle* h) {
+extern "C++" {
+// assemble the tangent at the current state into the sliced-ELL values of precision T
+template <typename T>
+static int sell_assemble(sfem_handle* h) {
   TRY(sell_structure(h));
+  T** vals = reinterpret_cast<T**>(sizeof(T) == 4 ? (void*)&h->sell_vals32 : (void*)&h->sell_vals64);
+  T** ke = reinterpret_cast<T**>(sizeof(T) == 4 ? (void*)&h->sell_ke32 : (void*)&h->sell_ke64);
+  if (!*vals) TRY(dalloc(vals, std::max<size_t>(9 * (size_t)h->sell_T, 1)));
   // 12-slot blocks per element: 16 for the corotational tangents (not symmetric), 10 otherwise
   const int nb_alloc = (h->material == SFEM_MMT_COROTATIONAL) ? 16 : 10;
-  if (!h->sell_ke32) TRY(dalloc(&h->sell_ke32, (size_t)h->E * 12 * nb_alloc));
-  const float* u32 = disp<float>(h);
-  const ElemView<float> ev = ev_of<float>(h);
+  if (!*ke) TRY(dalloc(ke, (size_t)h->E * 12 * nb_alloc));
+  const T* uT = disp<T>(h);
+  const ElemView<T> ev = ev_of<T>(h);
   int nb = 10;
-  with_mat<float>(mat_id(h), [&](auto m) {
-    nb = launch_element_stiffness_sym<float, decltype(m)::value>(ev, u32, h->sell_ke32, h->stream);
+  const int mat = mat_id(h);
+  if (mat > 4) return fail(SFEM_ERR_INVALID, "the assembled operator covers materials 0-3");
+  with_mat<float>(mat, [&](auto m) {  // the materials 0-4 (dispatch list shared by both precisions)
+    nb = launch_element_stiffness_sym<T, decltype(m)::value>(ev, uT, *ke, h->stream);
   });
-  launch_assemble_sell<float>(h->sell_T, h->sell_cptr, h->sell_code, h->sell_ke32, nb, h->nbc, h->nf, h->sell_dslot,
-                              h->dt > 0 ? h->mass : nullptr, h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0,
-                              h->sell_vals32, h->stream);
+  launch_assemble_sell<T>(h->sell_T, h->sell_cptr, h->sell_code, *ke, nb, h->nbc, h->nf, h->sell_dslot,
+                          h->dt > 0 ? h->mass : nullptr, h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0, *vals, h->stream);
   CU(cudaGetLastError());
   return 0;
 }
+}
 
-// The FP32 Krylov solves' operator for their duration: with op_mode 1 the tangent is assembled
-// at the current state and the loops use it; the patch product otherwise.
+// The Krylov solves' operator for their duration: with op_mode 1 (materials 0-3, no batched
+// instances) the tangent is assembled at the current state in the handle's precision and the
+// loops use it; the patch product otherwise.
 struct OperatorScope {
   sfem_handle* h;
   int st = 0;
   explicit OperatorScope(sfem_handle* hh) : h(hh) {
-    if (h->op_mode == 1 && h->n_inst == 0) {
-      st = sell_assemble32(h);
+    if (h->op_mode == 1 && h->n_inst == 0 && mat_id(h) <= 4) {
+      st = h->precision == SFEM_FP32 ? sell_assemble<float>(h) : sell_assemble<double>(h);
       h->sell_on = st == 0;
     }
   }
@@ -1742,6 +1754,8 @@ int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* op
   int st = 0;
   if (h->precision == SFEM_FP64) {
     KrylovWs<double>& w = h->k64;
+    OperatorScope ops(h);
+    TRY(ops.st);
     CU(cudaMemcpyAsync(w.b + o, b, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (pc) TRY(jacobi<double>(h, w.dinv, nullptr));
     st = pcg_device<double>(h, h->u, w.b, w.x, pc ? w.dinv : nullptr, opts->rel_tol, opts->max_iters,
@@ -1789,6 +1803,8 @@ int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
   if (masked) launch_segment_mask<double>(h->n_inst, h->inst_seg, h->inst_active, h->r64 + o, h->stream);
   if (h->precision == SFEM_FP64) {
     KrylovWs<double>& w = h->k64;
+    OperatorScope ops(h);
+    TRY(ops.st);
     if (pc) TRY(jacobi<double>(h, w.dinv, nullptr));
     if (masked) {
       // the unpreconditioned case masks a copy of the identity

@@ -1083,6 +1083,11 @@ template int launch_element_stiffness_sym<float, 1>(const ElemView<float>&, cons
 template int launch_element_stiffness_sym<float, 2>(const ElemView<float>&, const float*, float*, cudaStream_t);
 template int launch_element_stiffness_sym<float, 3>(const ElemView<float>&, const float*, float*, cudaStream_t);
 template int launch_element_stiffness_sym<float, 4>(const ElemView<float>&, const float*, float*, cudaStream_t);
+template int launch_element_stiffness_sym<double, 0>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template int launch_element_stiffness_sym<double, 1>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template int launch_element_stiffness_sym<double, 2>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template int launch_element_stiffness_sym<double, 3>(const ElemView<double>&, const double*, double*, cudaStream_t);
+template int launch_element_stiffness_sym<double, 4>(const ElemView<double>&, const double*, double*, cudaStream_t);
 
 // ---- assembled tangent in sliced ELL (32 rows per slice) for the Krylov loops ----
 // Block-slot t of free row r (slice r / 32, lane l = r % 32, position k in the row) is
@@ -1090,6 +1095,12 @@ template int launch_element_stiffness_sym<float, 4>(const ElemView<float>&, cons
 // warp (one slice) reads each value of a row position with one coalesced 128-byte load.
 
 // the nine used values of a 12-slot, 16-byte aligned block
+__device__ __forceinline__ void load9(const double* K, double (&kb)[9]) {
+  const double2* K2 = reinterpret_cast<const double2*>(K);
+  const double2 a = K2[0], b = K2[1], c = K2[2], d = K2[3], e = K2[4];
+  kb[0] = a.x; kb[1] = a.y; kb[2] = b.x; kb[3] = b.y; kb[4] = c.x; kb[5] = c.y; kb[6] = d.x; kb[7] = d.y;
+  kb[8] = e.x;
+}
 __device__ __forceinline__ void load9(const float* K, float (&kb)[9]) {
   const float4* K4 = reinterpret_cast<const float4*>(K);
   const float4 a = K4[0], b = K4[1], c = K4[2];
@@ -1158,6 +1169,8 @@ void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* c
 }
 template void launch_assemble_sell<float>(int64_t, const int64_t*, const uint32_t*, const float*, int, int64_t,
                                           int64_t, const int32_t*, const double*, double, float*, cudaStream_t);
+template void launch_assemble_sell<double>(int64_t, const int64_t*, const uint32_t*, const double*, int, int64_t,
+                                           int64_t, const int32_t*, const double*, double, double*, cudaStream_t);
 
 // q = K p over the free rows from the sliced-ELL tangent, one thread per row (a warp per slice).
 // DIR (Krylov iteration): the direction is formed where it is read, as in the patch product,
@@ -1296,6 +1309,9 @@ void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t
 template void launch_sell_hvp<float>(int64_t, int64_t, const int64_t*, const int32_t*, const int16_t*, const float*,
                                      const float*, float*, Reduce, CgScalars*, cudaStream_t, const float*,
                                      const float*, float*, const float*);
+template void launch_sell_hvp<double>(int64_t, int64_t, const int64_t*, const int32_t*, const int16_t*, const double*,
+                                      const double*, double*, Reduce, CgScalars*, cudaStream_t, const double*,
+                                      const double*, double*, const double*);
 
 // y = A x for a block-CSR matrix with 3 x 3 blocks (one thread per block row)
 __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int64_t nrows, const int32_t* __restrict__ rowptr,

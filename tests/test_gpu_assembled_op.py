@@ -87,3 +87,34 @@ def test_implicit_step_matches_matrix_free():
     (u_mf, st_mf), (u_as, st_as) = res
     print(st_mf, st_as, rel(u_as, u_mf))
     assert rel(u_as, u_mf) < 1e-6
+
+
+@pytest.mark.parametrize("material", [1, 3])
+def test_fp64_assembled_matches_matrix_free(material):
+    """The FP64 assembled operator: a PCG solve to 1e-10 and the Newton equilibrium agree with the
+    matrix-free FP64 product to rounding."""
+    from solidfem_gb300 import FemPhysicsMatrixFree
+    from solidfem_gb300.mesh import box_lattice, random_top_traction
+
+    m = box_lattice(24, 8, 8, extent=(24 / 64, 8 / 64, 8 / 64), jitter=0.2, seed=0)
+    fixed = m.face_nodes(2, 0)
+    p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.45, density=1070.0,
+                             gravity=(0, 0, 0), material=material, precision="fp64")
+    p.set_nodal_loads(random_top_traction(m, seed=3))
+    rng = np.random.default_rng(5)
+    p.set_positions(m.nodes + 2e-5 * rng.normal(size=m.nodes.shape))
+    b = rng.normal(size=(p.n_free, 3))
+    x_mf, st_mf = p.pcg(b, rel_tol=1e-10, max_iters=50000)
+    p.set_operator("assembled")
+    x_as, st_as = p.pcg(b, rel_tol=1e-10, max_iters=50000)
+    print(f"FP64 material {material}: PCG {st_mf['iters']} / {st_as['iters']}, rel diff {rel(x_as, x_mf):.2e}")
+    assert st_mf["status"] == 0 and st_as["status"] == 0 and rel(x_as, x_mf) < 1e-7
+    sols = []
+    for op in ("matrix-free", "assembled"):
+        p.set_operator(op)
+        p.set_positions(m.nodes)
+        st = p.newton_solve(rel_tol=1e-9)
+        assert st["status"] == 0, (op, st)
+        sols.append(p.get_positions() - m.nodes)
+    print(f"  Newton displacement rel diff {rel(sols[1], sols[0]):.2e}")
+    assert rel(sols[1], sols[0]) < 1e-8
