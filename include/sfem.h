@@ -237,12 +237,13 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
 int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max_cg,
                  double* dLdE, double* dLdf);
 
-/* ---- operator of the FP32 Krylov solves (MatrixVectorMultiply, Source/FemPhysicsMatrixFree.cpp:523-534) ----
+/* ---- operator of the Krylov solves (MatrixVectorMultiply, Source/FemPhysicsMatrixFree.cpp:523-534) ----
  * SFEM_OP_MATRIX_FREE (default): the fused patch Hessian-vector product, re-forming each element's
- * tangent every iteration.  SFEM_OP_ASSEMBLED: the same tangent assembled in FP32 (sliced ELL, 32
- * rows per slice) at the start of every FP32 Krylov solve (Newton step), then one streamed sparse
- * product per iteration; uses about 600 B per free node plus 576 B per element of device memory.
- * FP64 solves and batched instances always use the matrix-free product. */
+ * tangent every iteration.  SFEM_OP_ASSEMBLED: the same tangent assembled in the handle's precision
+ * (sliced ELL, 32 rows per slice) at the start of every Krylov solve (Newton step), then one streamed sparse
+ * product per iteration; uses about 600 B per free node plus 480 B per element of device memory
+ * (FP32; twice that in FP64).  Materials 0-3 in either precision; batched instances and the other
+ * materials use the matrix-free product. */
 #define SFEM_OP_MATRIX_FREE 0
 #define SFEM_OP_ASSEMBLED 1
 int sfem_set_operator(sfem_handle* h, int32_t op);

@@ -332,9 +332,9 @@ class FemPhysicsMatrixFree:
         return dE, df
 
     def set_operator(self, op: str) -> None:
-        """Operator of the FP32 Krylov solves: 'matrix-free' (the patch product, default) or
-        'assembled' (the tangent assembled in FP32 at every Newton step, one sparse product per
-        iteration)."""
+        """Operator of the Krylov solves: 'matrix-free' (the patch product, default) or 'assembled'
+        (the tangent assembled in the handle's precision at every Newton step, one sparse product
+        per iteration; materials 0-3, single bodies)."""
         nat.check(self._lib.sfem_set_operator(self._h, {"matrix-free": nat.OP_MATRIX_FREE,
                                                          "assembled": nat.OP_ASSEMBLED}[op]))
 
