@@ -20,6 +20,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <stdint.h>
 
 #include "sfem_internal.h"
@@ -1960,10 +1961,115 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
   }
 }
 
+// The flexible-CG update when q is complete (the assembled operator: no shared-node partials), over
+// groups of four nodes: twelve consecutive values, three 16-byte loads or stores per array.  Groups
+// start at the first node g0 >= nbc with g0 % 4 == 0 (12 g0 bytes then 16-byte aligned); the nodes
+// before g0 and after the last whole group are updated one by one.
+__device__ __forceinline__ void fcg_node(int64_t g, float a, float* __restrict__ x, float* __restrict__ r,
+                                         float* __restrict__ rprev, const float* __restrict__ p,
+                                         const float* __restrict__ q, const float* __restrict__ dinv,
+                                         float4* __restrict__ xs, int64_t nbc, float& rr) {
+  const int64_t o = 3 * g;
+  float rn[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    x[o + c] += a * p[o + c];
+    const float rp = r[o + c];
+    rprev[o + c] = rp;
+    rn[c] = rp - a * q[o + c];
+    r[o + c] = rn[c];
+    rr += rn[c] * rn[c];
+  }
+  if (xs) xs[g - nbc] = make_float4(rn[0] * sqrtf(dinv[o]), rn[1] * sqrtf(dinv[o + 1]), rn[2] * sqrtf(dinv[o + 2]), 0.f);
+}
+__device__ __forceinline__ void ld12(const float* __restrict__ a, float (&v)[12]) {
+  const float4* a4 = reinterpret_cast<const float4*>(a);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float4 t = a4[k];
+    v[4 * k] = t.x;
+    v[4 * k + 1] = t.y;
+    v[4 * k + 2] = t.z;
+    v[4 * k + 3] = t.w;
+  }
+}
+__device__ __forceinline__ void st12(float* __restrict__ a, const float (&v)[12]) {
+  float4* a4 = reinterpret_cast<float4*>(a);
+#pragma unroll
+  for (int k = 0; k < 3; k++) a4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+}
+__global__ void __launch_bounds__(kThreads) k_fcg_update_vec(int64_t nbc, int64_t N, float* __restrict__ x,
+                                                             float* __restrict__ r, float* __restrict__ rprev,
+                                                             const float* __restrict__ p, const float* __restrict__ q,
+                                                             Reduce red, CgScalars* s, const float* __restrict__ dinv,
+                                                             float4* __restrict__ xs) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (s->done) return;
+  const float a = (float)s->alpha;
+  float rr = 0.f;
+  const int64_t g0a = (nbc + 3) & ~(int64_t)3, g0 = g0a < N ? g0a : N;
+  const int64_t ng = (N - g0) / 4, gend = g0 + 4 * ng;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = tid; k < ng; k += stride) {
+    const int64_t g = g0 + 4 * k, o = 3 * g;
+    float xv[12], rv[12], pv[12], qv[12], dv[12];
+    ld12(x + o, xv);
+    ld12(r + o, rv);
+    ld12(p + o, pv);
+    ld12(q + o, qv);
+    if (xs) ld12(dinv + o, dv);
+    st12(rprev + o, rv);
+    float rn[12];
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      xv[i] += a * pv[i];
+      rn[i] = rv[i] - a * qv[i];
+      rr += rn[i] * rn[i];
+    }
+    st12(x + o, xv);
+    st12(r + o, rn);
+    if (xs) {
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+        xs[g + m - nbc] = make_float4(rn[3 * m] * sqrtf(dv[3 * m]), rn[3 * m + 1] * sqrtf(dv[3 * m + 1]),
+                                      rn[3 * m + 2] * sqrtf(dv[3 * m + 2]), 0.f);
+    }
+  }
+  // the nodes before the first group and after the last
+  const int64_t nhead = g0 - nbc, ntail = N - gend;
+  if (tid < nhead) fcg_node(nbc + tid, a, x, r, rprev, p, q, dinv, xs, nbc, rr);
+  else if (tid < nhead + ntail) fcg_node(gend + (tid - nhead), a, x, r, rprev, p, q, dinv, xs, nbc, rr);
+  float v[1] = {rr}, tot[1];
+  if (reduce_last<float, 1>(v, red, tot) && threadIdx.x == 0) {
+    s->rr = (double)tot[0];
+    s->it += 1;
+    if (!isfinite(s->rr)) {
+      s->done = 1;
+      s->status = -3;
+    } else if (s->rr <= s->tol2) {
+      s->done = 1;
+    } else if (s->it >= s->max_it) {
+      s->done = 1;
+      s->status = 1;
+    }
+  }
+}
+
 template <typename T>
 void launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x,
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
                              const T* dinv, float4* xs) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (bslot == nullptr) {  // q complete: the grouped update
+      static const int wave_v = resident_ctas(k_fcg_update_vec, kThreads, 0);
+      const int64_t groups = (N - nbc) / 4 + 1;
+      count_launch();
+      launch_pdl(k_fcg_update_vec, std::max(1, (int)std::min<int64_t>(wave_v, (groups + kThreads - 1) / kThreads)),
+                 kThreads, 0, st, nbc, N, x, r, rprev, p, q, red, s, dinv, xs);
+      return;
+    }
+  }
   count_launch();
   static const int wave = resident_ctas(k_fcg_update_patch<T>, kThreads, 0);
   launch_pdl(k_fcg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bslot, partial, x, r,
@@ -1973,9 +2079,101 @@ template void launch_fcg_update_patch<float>(int64_t, int64_t, const int2*, cons
                                              float*, float*, const float*, const float*, Reduce, CgScalars*,
                                              cudaStream_t, const float*, float4*);
 
+// 12 consecutive values (4 nodes) with 16-byte loads and stores, FP64
+__device__ __forceinline__ void ld12(const double* __restrict__ a, double (&v)[12]) {
+  const double2* a2 = reinterpret_cast<const double2*>(a);
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const double2 t = a2[k];
+    v[2 * k] = t.x;
+    v[2 * k + 1] = t.y;
+  }
+}
+__device__ __forceinline__ void st12(double* __restrict__ a, const double (&v)[12]) {
+  double2* a2 = reinterpret_cast<double2*>(a);
+#pragma unroll
+  for (int k = 0; k < 6; k++) a2[k] = make_double2(v[2 * k], v[2 * k + 1]);
+}
+
+// The preconditioned-CG update when q is complete (the assembled operator), over groups of four
+// nodes as k_fcg_update_vec: x += alpha p, r -= alpha q, r.(D^-1 r) and r.r, then beta and the
+// convergence test in the last block.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_cg_update_vec(int64_t nbc, int64_t N, T* __restrict__ x,
+                                                            T* __restrict__ r, const T* __restrict__ p,
+                                                            const T* __restrict__ q, const T* __restrict__ dinv,
+                                                            Reduce red, CgScalars* s) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (s->done) return;
+  const T a = (T)s->alpha;
+  T rz = T(0), rr = T(0);
+  const int64_t g0a = (nbc + 3) & ~(int64_t)3, g0 = g0a < N ? g0a : N;
+  const int64_t ng = (N - g0) / 4, gend = g0 + 4 * ng;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = tid; k < ng; k += stride) {
+    const int64_t o = 3 * (g0 + 4 * k);
+    T xv[12], rv[12], pv[12], qv[12], dv[12];
+    ld12(x + o, xv);
+    ld12(r + o, rv);
+    ld12(p + o, pv);
+    ld12(q + o, qv);
+    ld12(dinv + o, dv);
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      xv[i] += a * pv[i];
+      rv[i] -= a * qv[i];
+      rz += rv[i] * (dv[i] * rv[i]);
+      rr += rv[i] * rv[i];
+    }
+    st12(x + o, xv);
+    st12(r + o, rv);
+  }
+  const int64_t nhead = g0 - nbc, ntail = N - gend;
+  int64_t g = -1;
+  if (tid < nhead) g = nbc + tid;
+  else if (tid < nhead + ntail) g = gend + (tid - nhead);
+  if (g >= 0) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const int64_t o = 3 * g + c;
+      x[o] += a * p[o];
+      const T ri = r[o] - a * q[o];
+      r[o] = ri;
+      rz += ri * (dinv[o] * ri);
+      rr += ri * ri;
+    }
+  }
+  T v[2] = {rz, rr}, tot[2];
+  if (reduce_last<T, 2>(v, red, tot) && threadIdx.x == 0) {
+    const double rzn = (double)tot[0];
+    s->beta = rzn / s->rz;
+    s->rz = rzn;
+    s->rr = (double)tot[1];
+    s->it += 1;
+    if (!isfinite(s->rr)) {
+      s->done = 1;
+      s->status = -3;
+    } else if (s->rr <= s->tol2) {
+      s->done = 1;
+    } else if (s->it >= s->max_it) {
+      s->done = 1;
+      s->status = 1;
+    }
+  }
+}
+
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x,
                             T* r, const T* p, const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st) {
+  if (bslot == nullptr) {  // q complete: the grouped update
+    static const int wave_v = resident_ctas(k_cg_update_vec<T>, kThreads, 0);
+    const int64_t groups = (N - nbc) / 4 + 1;
+    count_launch();
+    launch_pdl(k_cg_update_vec<T>, std::max(1, (int)std::min<int64_t>(wave_v, (groups + kThreads - 1) / kThreads)),
+               kThreads, 0, st, nbc, N, x, r, p, q, dinv, red, s);
+    return;
+  }
   count_launch();
   static const int wave = resident_ctas(k_cg_update_patch<T>, kThreads, 0);
   launch_pdl(k_cg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bslot, partial, x, r, p,
