@@ -242,8 +242,8 @@ int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max
  * tangent every iteration.  SFEM_OP_ASSEMBLED: the same tangent assembled in the handle's precision
  * (sliced ELL, 32 rows per slice) at the start of every Krylov solve (Newton step), then one streamed sparse
  * product per iteration; uses about 600 B per free node plus 480 B per element of device memory
- * (FP32; twice that in FP64).  Materials 0-3 in either precision; batched instances and the other
- * materials use the matrix-free product. */
+ * (FP32; twice that in FP64), released again by sfem_set_operator(h, SFEM_OP_MATRIX_FREE).  Materials
+ * 0-3 in either precision; batched instances and the other materials use the matrix-free product. */
 #define SFEM_OP_MATRIX_FREE 0
 #define SFEM_OP_ASSEMBLED 1
 int sfem_set_operator(sfem_handle* h, int32_t op);

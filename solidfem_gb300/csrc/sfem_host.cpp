@@ -1249,6 +1249,22 @@ int sfem_set_operator(sfem_handle* h, int32_t op) {
   if (op != SFEM_OP_MATRIX_FREE && op != SFEM_OP_ASSEMBLED)
     return fail(SFEM_ERR_INVALID, "operator is SFEM_OP_MATRIX_FREE (0) or SFEM_OP_ASSEMBLED (1)");
   h->op_mode = op;
+  if (op == SFEM_OP_MATRIX_FREE && h->sell_T >= 0) {  // release the assembled operator's memory
+    TRY(set_device(h));
+    TRY(sync(h));
+    void* bufs[] = {h->sell_base, h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32,
+                    h->sell_ke32, h->sell_col16, h->sell_vals64, h->sell_ke64};
+    for (void* b : bufs)
+      if (b) cudaFree(b);
+    h->sell_base = h->sell_cptr = nullptr;
+    h->sell_col = h->sell_dslot = nullptr;
+    h->sell_code = nullptr;
+    h->sell_vals32 = h->sell_ke32 = nullptr;
+    h->sell_col16 = nullptr;
+    h->sell_vals64 = h->sell_ke64 = nullptr;
+    h->sell_T = -1;
+    h->sell_nnzb = 0;
+  }
   return SFEM_OK;
 }
 
