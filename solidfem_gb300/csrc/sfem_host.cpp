@@ -1224,6 +1224,10 @@ struct OperatorScope {
     if (h->op_mode == 1 && h->n_inst == 0 && mat_id(h) <= 4) {
       st = h->precision == SFEM_FP32 ? sell_assemble<float>(h) : sell_assemble<double>(h);
       h->sell_on = st == 0;
+      if (st == SFEM_ERR_OOM) {  // without the memory: the matrix-free product
+        cudaGetLastError();
+        st = 0;
+      }
     }
   }
   ~OperatorScope() { h->sell_on = false; }
