@@ -1,6 +1,8 @@
 """Train the learned preconditioner on residual/correction pairs from plain solves.
 
-    python -m solidfem_gb300.train_preconditioner --out solidfem_gb300/data/gnn_slab.bin
+    python -m solidfem_gb300.train_preconditioner --out base.bin
+    python -m solidfem_gb300.train_preconditioner --init base.bin --first-seed 128 --every 15 \
+        --max-snaps 60 --lr 3e-4 --init-seed 1 --out solidfem_gb300/data/gnn_slab.bin
 
 Training meshes are slabs with the benchmark's element size (h = 1/64), jitter,
 material (neo-Hookean E = 1e5 Pa, nu = 0.49) and boundary conditions (bottom face
@@ -29,23 +31,28 @@ def slab_mesh(nx, ny, nz, jitter=0.2, seed=0):
 
 
 def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1e-3, init_seed=0, verbose=True,
-          loss="energy", batch=16):
+          loss="energy", batch=16, init=None, first_seed=0):
+    """Collect pairs from load seeds first_seed .. first_seed + seeds - 1 and train; init: weights
+    to start from (a previous run's output) instead of the seeded random initialisation."""
     m = slab_mesh(*dims)
     fixed = m.face_nodes(2, 0)
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
                              material=3, precision="fp32")
     net = LearnedPreconditioner(p, seed=init_seed)
+    if init:
+        net.load(init)
     net.set_loss(loss)
     net.set_batch(batch)
     t0 = time.time()
-    for s in range(seeds):
+    for s in range(first_seed, first_seed + seeds):
         p.set_nodal_loads(random_top_traction(m, seed=s))
         net.collect(None, every=every, max_snaps=max_snaps, rel_tol=1e-6)
     t_collect = time.time() - t0
     t0 = time.time()
     losses = net.train(steps=steps, lr=lr, seed=init_seed)
     t_train = time.time() - t0
-    info = {"dims": list(dims), "load_seeds": [0, seeds - 1], "pairs": net.dataset_size(), "every": every, "loss": loss, "batch": batch,
+    info = {"dims": list(dims), "load_seeds": [first_seed, first_seed + seeds - 1], "pairs": net.dataset_size(),
+            "every": every, "max_snaps": max_snaps, "loss": loss, "batch": batch, "init": init, "init_seed": init_seed,
             "steps": steps, "lr": lr, "loss_first50": float(np.mean(losses[:50])),
             "loss_last50": float(np.mean(losses[-50:])), "collect_s": t_collect, "train_s": t_train,
             "material": "neo-Hookean E=1e5 nu=0.49, h=1/64, jitter 0.2h, bottom clamped, random top traction"}
@@ -65,9 +72,13 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--loss", default="energy", choices=["energy", "residual"])
+    ap.add_argument("--init", default=None, help="start from these weights (fine-tuning)")
+    ap.add_argument("--first-seed", type=int, default=0, help="first load seed of the collected pairs")
+    ap.add_argument("--init-seed", type=int, default=0, help="seed of the initialisation and of the minibatches")
     a = ap.parse_args()
     dims = tuple(int(v) for v in a.dims.split(","))
-    net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr, loss=a.loss, batch=a.batch)
+    net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr, init_seed=a.init_seed, loss=a.loss,
+                              batch=a.batch, init=a.init, first_seed=a.first_seed)
     net.save(a.out, meta=info)
     np.save(a.out.rsplit(".", 1)[0] + "_losses.npy", losses)
 
