@@ -2,7 +2,9 @@
 
     python -m solidfem_gb300.train_preconditioner --out base.bin
     python -m solidfem_gb300.train_preconditioner --init base.bin --first-seed 128 --every 15 \
-        --max-snaps 60 --lr 3e-4 --init-seed 1 --out solidfem_gb300/data/gnn_slab.bin
+        --max-snaps 60 --lr 3e-4 --init-seed 1 --out tuned1.bin
+    python -m solidfem_gb300.train_preconditioner --init tuned1.bin --first-seed 256 --every 15 \
+        --max-snaps 60 --lr 1e-4 --init-seed 2 --out solidfem_gb300/data/gnn_slab.bin
 
 Training meshes are slabs with the benchmark's element size (h = 1/64), jitter,
 material (neo-Hookean E = 1e5 Pa, nu = 0.49) and boundary conditions (bottom face
