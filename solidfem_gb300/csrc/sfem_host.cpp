@@ -2119,17 +2119,17 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
   TRY(residual(h, &rn, nullptr));
   CU(cudaMemsetAsync(d, 0, 3 * (size_t)h->N * sizeof(double), h->stream));
   CU(cudaMemcpyAsync(d + o, h->r64 + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-  double delta;
+  double delta = 0.0;
   TRY(dot(h->r64, h->r64, &delta));
   const double delta0 = delta;
   int iter = 0;
   if (delta != 0) {
     for (; iter < outer_iters; iter++) {
-      double deltaD;
+      double deltaD = 0.0;
       TRY(dot(d, d, &deltaD));
       for (int inner = 0; inner < inner_iters; inner++) {
         hvp<double>(h, h->u, d, df, nullptr);
-        double rd, ddf;
+        double rd = 0.0, ddf = 0.0;
         TRY(dot(h->r64, d, &rd));
         TRY(dot(d, df, &ddf));
         const double alpha = rd / ddf;
@@ -2137,7 +2137,7 @@ int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, 
         TRY(residual(h, &rn, nullptr));
         if (alpha * alpha * deltaD < tol2) break;
       }
-      double delta1;
+      double delta1 = 0.0;
       TRY(dot(h->r64, h->r64, &delta1));
       const double beta = delta1 / delta;
       delta = delta1;
