@@ -131,6 +131,21 @@ def free_block_pattern(tets, rmap, nbc):
     return key // (int(t.max()) + 1), key % (int(t.max()) + 1)
 
 
+def randomly_numbered_lattice():
+    """The 64x24x24-hex lattice (40,625 nodes) and the same mesh under a random node numbering:
+    (lattice mesh, fixed nodes, loads), (nodes, tets, fixed nodes, loads) renumbered, perm
+    (node k of the renumbered mesh is node perm[k] of the lattice)."""
+    from solidfem_gb300.mesh import box_lattice, random_top_traction
+
+    m = box_lattice(64, 24, 24, extent=(1.0, 24 / 64, 24 / 64), jitter=0.2, seed=0)
+    fixed = m.face_nodes(2, 0)
+    loads = random_top_traction(m, seed=7)
+    perm = np.random.default_rng(11).permutation(len(m.nodes))
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(len(perm))
+    return (m, fixed, loads), (m.nodes[perm], inv[m.tets].astype(np.int32), inv[fixed], loads[perm]), perm
+
+
 def test_randomly_numbered_mesh_32bit_indices():
     """A randomly numbered lattice of 40,625 nodes, where column differences and neighbour deltas no
     longer fit 16 bits: the sliced-ELL product keeps 32-bit columns (read back from the profile's
@@ -141,15 +156,8 @@ def test_randomly_numbered_mesh_32bit_indices():
 
     from solidfem_gb300 import PC_LEARNED, FemPhysicsMatrixFree
     from solidfem_gb300.learned import LearnedPreconditioner
-    from solidfem_gb300.mesh import box_lattice, random_top_traction
 
-    m = box_lattice(64, 24, 24, extent=(1.0, 24 / 64, 24 / 64), jitter=0.2, seed=0)
-    fixed = m.face_nodes(2, 0)
-    loads = random_top_traction(m, seed=7)
-    perm = np.random.default_rng(11).permutation(len(m.nodes))
-    inv = np.empty_like(perm)
-    inv[perm] = np.arange(len(perm))
-    nodes_p, tets_p, fixed_p, loads_p = m.nodes[perm], inv[m.tets].astype(np.int32), inv[fixed], loads[perm]
+    (m, fixed, loads), (nodes_p, tets_p, fixed_p, loads_p), perm = randomly_numbered_lattice()
     weights = os.path.join(os.path.dirname(__file__), "..", "solidfem_gb300", "data", "gnn_slab.bin")
 
     def physics(nodes, tets, fx, f):
@@ -202,3 +210,28 @@ def test_randomly_numbered_mesh_32bit_indices():
     u_lattice = (q.get_positions() - m.nodes)[perm]
     print(f"displacement rel diffs: operators {rel(sols[1], sols[0]):.2e}, numberings {rel(sols[1], u_lattice):.2e}")
     assert rel(sols[1], sols[0]) < 1e-6 and rel(sols[1], u_lattice) < 1e-6
+
+
+def test_randomly_numbered_mesh_fp64_assembled():
+    """The FP64 assembled operator with 32-bit columns (the randomly numbered lattice): a Jacobi-PCG
+    solve to 1e-10 agrees with the matrix-free FP64 product to rounding."""
+    from solidfem_gb300 import FemPhysicsMatrixFree
+
+    _, (nodes_p, tets_p, fixed_p, _), _ = randomly_numbered_lattice()
+    p = FemPhysicsMatrixFree(tets_p, nodes_p, fixed_p, young=1e5, poisson=0.45, density=1070.0,
+                             gravity=(0, 0, 0), material=3, precision="fp64")
+    rows, cols = free_block_pattern(tets_p, p.reshuffle_map(), p.n_bcs)
+    rng = np.random.default_rng(5)
+    p.set_positions(nodes_p + 2e-5 * rng.normal(size=nodes_p.shape))
+    b = rng.normal(size=(p.n_free, 3))
+    x_mf, st_mf = p.pcg(b, rel_tol=1e-10, max_iters=50000)
+    p.set_operator("assembled")
+    p.set_profiling(True)
+    x_as, st_as = p.pcg(b, rel_tol=1e-10, max_iters=50000)
+    prof = p.get_profile()
+    p.set_profiling(False)
+    col_bytes = (prof["algo_bytes_hvp"] - 96.0 * p.n_free) / len(rows) - 72.0
+    print(f"FP64 PCG {st_mf['iters']} / {st_as['iters']}, column bytes {col_bytes:.3f}, "
+          f"rel diff {rel(x_as, x_mf):.2e}")
+    assert abs(col_bytes - 4.0) < 1e-6
+    assert st_mf["status"] == 0 and st_as["status"] == 0 and rel(x_as, x_mf) < 1e-7
