@@ -8,7 +8,9 @@ Definition (free DOFs in the reshuffled order, 3 per node):
               their rest position
   P:          per aggregate, the six rigid-body modes of its nodes (three translations and three
               rotations about the aggregate's centroid), orthonormalised; modes that degenerate
-              (an aggregate of one node or of collinear nodes) are dropped.  P^T P = I.
+              (an aggregate of one node or of collinear nodes) are dropped.  P^T P = I.  Compact
+              form: node i's 3 x 6 block is B(d_i) R_a, d_i its offset from the centroid and R_a a
+              6 x 6 matrix per aggregate (rigid_body_factors).
   Kc:         P^T K P (dense; symmetric positive definite when K is)
   M2(r):      M(r) + P Kc^-1 P^T r, M the one-level preconditioner (Jacobi or learned)
 The tangent K is probed from the FP64 oracle's Hessian-vector product with one product per
@@ -77,32 +79,52 @@ def aggregate_cells(X: np.ndarray, cell: float) -> np.ndarray:
 
 
 def rigid_body_basis(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8) -> sp.csr_matrix:
-    """P: orthonormal rigid-body modes of every aggregate (columns grouped by aggregate)."""
-    n = X.shape[0]
+    """P: orthonormal rigid-body modes of every aggregate (columns grouped by aggregate), assembled
+    from the compact form B(d_i) R_a of rigid_body_factors."""
+    d, R = rigid_body_factors(X, aid, rtol)
+    kept = (np.abs(R).sum(axis=1) > 0).sum(axis=1)  # columns per aggregate
+    first = np.concatenate([[0], np.cumsum(kept)])
+    rows, cols, vals = [], [], []
+    for i in range(X.shape[0]):
+        a = aid[i]
+        blk = modes(d[i:i + 1]) @ R[a][:, :kept[a]]
+        for c in range(3):
+            rows.append(np.full(kept[a], 3 * i + c))
+            cols.append(first[a] + np.arange(kept[a]))
+            vals.append(blk[c])
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                         shape=(3 * X.shape[0], int(first[-1])))
+
+
+def modes(d: np.ndarray) -> np.ndarray:
+    """B for nodes at offsets d from their centroid: (3 n x 6), translations then rotations."""
+    B = np.zeros((3 * d.shape[0], 6))
+    for c in range(3):
+        B[c::3, c] = 1.0
+    for r, (i, j) in enumerate(((1, 2), (2, 0), (0, 1))):
+        B[i::3, 3 + r] = -d[:, j]
+        B[j::3, 3 + r] = d[:, i]
+    return B
+
+
+def rigid_body_factors(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8):
+    """The compact form of P: per node its offset d_i from the aggregate's centroid, per aggregate a
+    6 x 6 matrix R_a (zero columns for dropped modes) with P's block of node i = B(d_i) R_a."""
     na = int(aid.max()) + 1
+    cnt = np.bincount(aid, minlength=na)
+    cen = np.zeros((na, 3))
+    np.add.at(cen, aid, X)
+    cen /= cnt[:, None]
+    d = X - cen[aid]
+    R = np.zeros((na, 6, 6))
     order = np.argsort(aid, kind="stable")
     starts = np.searchsorted(aid[order], np.arange(na + 1))
-    rows, cols, vals = [], [], []
-    ncol = 0
     for a in range(na):
-        nodes = order[starts[a]:starts[a + 1]]
-        d = X[nodes] - X[nodes].mean(axis=0)
-        B = np.zeros((3 * nodes.size, 6))
-        for c in range(3):
-            B[c::3, c] = 1.0
-        # rotation about axis e_r: e_r x d
-        for r, (i, j) in enumerate(((1, 2), (2, 0), (0, 1))):
-            B[i::3, 3 + r] = -d[:, j]
-            B[j::3, 3 + r] = d[:, i]
-        U, s, _ = np.linalg.svd(B, full_matrices=False)
-        U = U[:, s > rtol * s[0]]
-        dofs = (3 * nodes[:, None] + np.arange(3)).ravel()
-        for c in range(U.shape[1]):
-            rows.append(dofs)
-            cols.append(np.full(dofs.size, ncol + c))
-            vals.append(U[:, c])
-        ncol += U.shape[1]
-    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(3 * n, ncol))
+        B = modes(d[order[starts[a]:starts[a + 1]]])
+        _, s, Vt = np.linalg.svd(B, full_matrices=False)
+        keep = s > rtol * s[0]
+        R[a][:, :keep.sum()] = Vt[keep].T / s[keep]
+    return d, R
 
 
 def coarse_matrix(K: sp.spmatrix, P: sp.spmatrix) -> np.ndarray:

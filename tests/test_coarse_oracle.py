@@ -51,6 +51,24 @@ def test_rigid_body_basis_is_orthonormal_and_spans_rigid_motions():
     for e in np.eye(3):
         for v in (np.tile(e, X.shape[0]), np.cross(e, X).ravel()):
             assert np.linalg.norm(v - P @ (P.T @ v)) <= 1e-10 * np.linalg.norm(v)
+    # the compact form (offsets and one 6 x 6 matrix per aggregate) gives the same columns
+    d, R = co.rigid_body_factors(X, aid)
+    rng = np.random.default_rng(1)
+    r = rng.normal(size=3 * X.shape[0])
+    rc = np.zeros((R.shape[0], 6))  # restriction: R_a^T (sum r_i, sum d_i x r_i)
+    ri = r.reshape(-1, 3)
+    np.add.at(rc, aid, np.hstack([ri, np.cross(d, ri)]))
+    rc = np.einsum("aij,ai->aj", R, rc)
+    cols = np.cumsum([0] + [int((abs(R[a]).sum(axis=0) > 0).sum()) for a in range(R.shape[0])])
+    packed = np.concatenate([rc[a, :cols[a + 1] - cols[a]] for a in range(R.shape[0])])
+    np.testing.assert_allclose(packed, P.T @ r, rtol=1e-10, atol=1e-12 * np.abs(P.T @ r).max())
+    y = rng.normal(size=P.shape[1])  # prolongation: u_a + omega_a x d_i, (u_a, omega_a) = R_a y_a
+    ya = np.zeros((R.shape[0], 6))
+    for a in range(R.shape[0]):
+        ya[a, :cols[a + 1] - cols[a]] = y[cols[a]:cols[a + 1]]
+    uw = np.einsum("aij,aj->ai", R, ya)
+    z = uw[aid, :3] + np.cross(uw[aid, 3:], d)
+    np.testing.assert_allclose(z.ravel(), P @ y, rtol=1e-10, atol=1e-12 * np.abs(P @ y).max())
 
 
 def test_two_level_preconditioners_cut_iterations():
