@@ -9,8 +9,9 @@ Definition (free DOFs in the reshuffled order, 3 per node):
   P:          per aggregate, the six rigid-body modes of its nodes (three translations and three
               rotations about the aggregate's centroid), orthonormalised; modes that degenerate
               (an aggregate of one node or of collinear nodes) are dropped.  P^T P = I.  Compact
-              form: node i's 3 x 6 block is B(d_i) R_a, d_i its offset from the centroid and R_a a
-              6 x 6 matrix per aggregate (rigid_body_factors).
+              form: node i's 3 x 6 block is B(d_i) R_a, d_i its offset from the centroid and
+              R_a = diag(I / sqrt(n_a), W_a), W_a from the eigenpairs of the aggregate's inertia
+              tensor (rigid_body_factors).
   Kc:         P^T K P (dense; symmetric positive definite when K is)
   M2(r):      M(r) + P Kc^-1 P^T r, M the one-level preconditioner (Jacobi or learned)
 The tangent K is probed from the FP64 oracle's Hessian-vector product with one product per
@@ -109,21 +110,27 @@ def modes(d: np.ndarray) -> np.ndarray:
 
 def rigid_body_factors(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8):
     """The compact form of P: per node its offset d_i from the aggregate's centroid, per aggregate a
-    6 x 6 matrix R_a (zero columns for dropped modes) with P's block of node i = B(d_i) R_a."""
+    6 x 6 matrix R_a (zero columns for dropped modes) with P's block of node i = B(d_i) R_a.
+
+    With the offsets summing to zero, B^T B = diag(n I, J), J = sum(|d|^2 I - d d^T) the
+    aggregate's inertia tensor, so R_a = diag(I / sqrt(n), V L^-1/2) from the eigenpairs (L, V) of
+    J; rotations whose eigenvalue is below rtol times the largest are dropped (one node: all three;
+    collinear nodes: the one about their line)."""
     na = int(aid.max()) + 1
-    cnt = np.bincount(aid, minlength=na)
+    cnt = np.bincount(aid, minlength=na).astype(np.float64)
     cen = np.zeros((na, 3))
     np.add.at(cen, aid, X)
     cen /= cnt[:, None]
     d = X - cen[aid]
+    J = np.zeros((na, 3, 3))
+    np.add.at(J, aid, (d * d).sum(axis=1)[:, None, None] * np.eye(3) - d[:, :, None] * d[:, None, :])
     R = np.zeros((na, 6, 6))
-    order = np.argsort(aid, kind="stable")
-    starts = np.searchsorted(aid[order], np.arange(na + 1))
+    R[:, :3, :3] = np.eye(3) / np.sqrt(cnt)[:, None, None]
+    lam, V = np.linalg.eigh(J)  # ascending
     for a in range(na):
-        B = modes(d[order[starts[a]:starts[a + 1]]])
-        _, s, Vt = np.linalg.svd(B, full_matrices=False)
-        keep = s > rtol * s[0]
-        R[a][:, :keep.sum()] = Vt[keep].T / s[keep]
+        keep = lam[a] > rtol * max(lam[a, -1], 0.0)
+        k = int(keep.sum())
+        R[a, 3:, 3:3 + k] = V[a][:, keep] / np.sqrt(lam[a][keep])
     return d, R
 
 
