@@ -349,6 +349,18 @@ int sfem_kernel_launches(int64_t* count);
  * address up (cudaGetSymbolAddress) and should come before any stream capture. */
 int sfem_dot_noalloc_dev(const double* a_dev, const double* b_dev, int64_t n, double* out_dev, void* stream);
 
+/* ---- coarse space (extension; the reference's SolveConjugateGradientMF,
+ * Math/IterativeSolvers.h:115-195, has none): host-side groundwork of a two-level preconditioner.
+ * X: n points (3n doubles, e.g. free-node rest positions); aggregates are the cells of a uniform
+ * grid of spacing `cell` anchored at the points' minimum corner, numbered in increasing cell order
+ * (aid: n).  d: 3n, each point's offset from its aggregate's centroid.  R (optional, 36 * n_agg
+ * doubles, row-major 6 x 6 per aggregate): the aggregate's rigid-body modes B_i = [I, -[d_i]x]
+ * orthonormalised, P_i = B_i R_a, R_a = diag(I / sqrt(n_a), V L^-1/2) from the eigenpairs of the
+ * aggregate's inertia tensor; rotations with eigenvalue <= rtol * the largest are dropped (zero
+ * columns).  Call with R = NULL to learn n_agg.  No device work. */
+int sfem_coarse_factors(const double* X, int64_t n, double cell, double rtol, int32_t* aid, double* d,
+                        double* R, int64_t* n_agg);
+
 /* ---- device-pointer variants (stream-ordered on the handle's stream) ---- */
 int sfem_compute_gradients_dev(sfem_handle* h, double* r_dev);
 int sfem_matvec_dev(sfem_handle* h, const double* d_dev, double* Kd_dev);

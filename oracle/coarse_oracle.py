@@ -83,10 +83,15 @@ def rigid_body_basis(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8) -> sp.c
     """P: orthonormal rigid-body modes of every aggregate (columns grouped by aggregate), assembled
     from the compact form B(d_i) R_a of rigid_body_factors."""
     d, R = rigid_body_factors(X, aid, rtol)
+    return basis_from_factors(aid, d, R)
+
+
+def basis_from_factors(aid: np.ndarray, d: np.ndarray, R: np.ndarray) -> sp.csr_matrix:
+    """P from a compact form: node i's block B(d_i) R_a, the nonzero columns of R_a kept in order."""
     kept = (np.abs(R).sum(axis=1) > 0).sum(axis=1)  # columns per aggregate
     first = np.concatenate([[0], np.cumsum(kept)])
     rows, cols, vals = [], [], []
-    for i in range(X.shape[0]):
+    for i in range(d.shape[0]):
         a = aid[i]
         blk = modes(d[i:i + 1]) @ R[a][:, :kept[a]]
         for c in range(3):
@@ -94,7 +99,7 @@ def rigid_body_basis(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8) -> sp.c
             cols.append(first[a] + np.arange(kept[a]))
             vals.append(blk[c])
     return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
-                         shape=(3 * X.shape[0], int(first[-1])))
+                         shape=(3 * d.shape[0], int(first[-1])))
 
 
 def modes(d: np.ndarray) -> np.ndarray:

@@ -130,6 +130,7 @@ SIGNATURES = {
     "sfem_gnn_set_inference": [_vp, C.c_int32],
     "sfem_set_operator": [_vp, C.c_int32],
     "sfem_gnn_graph_form": [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
+    "sfem_coarse_factors": [_dp, C.c_int64, C.c_double, C.c_double, _ip, _dp, _dp, _i64p],
     "sfem_gnn_get_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_set_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_apply": [_vp, _dp, _dp],
