@@ -143,6 +143,29 @@ def coarse_matrix(K: sp.spmatrix, P: sp.spmatrix) -> np.ndarray:
     return np.asarray((P.T @ (K @ P)).todense())
 
 
+def coarse_matrix_blocks(K: sp.spmatrix, aid: np.ndarray, d: np.ndarray, R: np.ndarray) -> np.ndarray:
+    """Kc from the 3 x 3 blocks of K, the form a device assembly uses: every block K_ij adds
+    B_i^T K_ij B_j (6 x 6) to the aggregate pair (a(i), a(j)); Kc_ab = R_a^T G_ab R_b over the kept
+    columns (ordered as in basis_from_factors).  Dense in the aggregate pairs: for small cases."""
+    Kb = K.tobsr(blocksize=(3, 3))
+    na = R.shape[0]
+    rows = np.repeat(np.arange(Kb.shape[0] // 3), np.diff(Kb.indptr))
+    cols = Kb.indices
+    B = np.stack([modes(d[k:k + 1]) for k in range(d.shape[0])])  # (n, 3, 6)
+    contrib = np.einsum("kxi,kxy,kyj->kij", B[rows], Kb.data, B[cols])
+    G = np.zeros((na, na, 6, 6))
+    np.add.at(G, (aid[rows], aid[cols]), contrib)
+    kept = (np.abs(R).sum(axis=1) > 0).sum(axis=1)
+    first = np.concatenate([[0], np.cumsum(kept)])
+    Kc = np.zeros((first[-1], first[-1]))
+    for a in range(na):
+        for b in range(na):
+            if np.any(G[a, b]):
+                Kc[first[a]:first[a + 1], first[b]:first[b + 1]] = (R[a][:, :kept[a]].T @ G[a, b]
+                                                                     @ R[b][:, :kept[b]])
+    return Kc
+
+
 def two_level(M, P: sp.spmatrix, Kc: np.ndarray):
     """r -> M(r) + P Kc^-1 P^T r (Kc factorised once)."""
     fac = sla.cho_factor(Kc)

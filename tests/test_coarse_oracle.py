@@ -81,6 +81,10 @@ def test_two_level_preconditioners_cut_iterations():
     Kc = co.coarse_matrix(K, P)
     assert abs(Kc - Kc.T).max() <= 1e-10 * abs(Kc).max()
     assert np.linalg.eigvalsh(Kc).min() > 0
+    # the block form a device assembly uses gives the same matrix
+    aid = co.aggregate_cells(X, 4 / 64)
+    d, R = co.rigid_body_factors(X, aid)
+    np.testing.assert_allclose(co.coarse_matrix_blocks(K, aid, d, R), Kc, rtol=0, atol=1e-10 * abs(Kc).max())
 
     params = np.fromfile(WEIGHTS, dtype=np.float32)
     Am = go.free_graph(o.tets(), o.n_bcs, o.n_nodes)
