@@ -178,27 +178,72 @@ def replica_seeds(rank, warmup, steps):
 # ---------------------------------------------------------------------------
 # CPU arm (oracle port)
 # ---------------------------------------------------------------------------
-def cpu_sample(m, fixed, counts, budget_s=25.0):
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:  # noqa: BLE001
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:  # noqa: BLE001
+        pass
+    import platform
+
+    return platform.machine()
+
+
+def make_oracle(m, fixed):
+    from oracle.oracle import Oracle
+
+    return Oracle(m.nodes, m.tets, fixed, YOUNG, POISSON, DENSITY, (0.0, 0.0, 0.0), 3)
+
+
+def shuffled(o, x):
+    """Node array in the caller's order -> the oracle's reshuffled order."""
+    out = np.zeros_like(x)
+    out[o.reshuffle_map()] = x
+    return out
+
+
+def oracle_rel_res(o, m, f, positions):
+    """|r(x)| / |r(x0)| of the oracle's FP64 residual (ComputeGradients semantics) at the given
+    positions (caller's node order) under the nodal loads f."""
+    o.set_nodal_loads(f)
+    o.set_positions_shuffled(shuffled(o, m.nodes))
+    r0 = float(np.linalg.norm(o.gradients()))
+    o.set_positions_shuffled(shuffled(o, positions))
+    return float(np.linalg.norm(o.gradients())) / r0
+
+
+def cpu_sample(m, fixed, counts, its=20, o=None):
     """Time the oracle's FP64 operations on the full workload mesh on the host cores and
     extrapolate a Jacobi-PCG Newton solve with the given iteration counts."""
     from oracle.oracle import Oracle
 
-    o = Oracle(m.nodes, m.tets, fixed, YOUNG, POISSON, DENSITY, (0.0, 0.0, 0.0), 3)
+    if o is None:
+        o = make_oracle(m, fixed)
     o.set_nodal_loads(loads_for(m, LOAD_SEED0))
+    o.set_positions_shuffled(shuffled(o, m.nodes))
     t = time.perf_counter()
     r = o.gradients()
     t_grad = time.perf_counter() - t
     t = time.perf_counter()
     diag = o.jacobi_diagonal()
     t_diag = time.perf_counter() - t
-    its = 2
     t = time.perf_counter()
     o.pcg(r, diag=diag, tol=1e-30, max_iters=its)
     t_iter = (time.perf_counter() - t) / its
     est = (counts["cg_iters"] * t_iter + counts["newton_iters"] * t_diag + counts["residual_evals"] * t_grad)
     sample = (f"oracle port on {m.n_tets} tets: 1 residual ({t_grad:.2f} s, serial as the reference), "
-              f"1 Jacobi diagonal ({t_diag:.2f} s), {its} PCG iterations ({t_iter:.2f} s/it, OpenMP element loop); "
-              f"extrapolated x {counts['cg_iters']} CG its, {counts['newton_iters']} Newton its, "
+              f"1 Jacobi diagonal ({t_diag:.2f} s), {its} PCG iterations measured ({t_iter:.3f} s/it, OpenMP "
+              f"element loop); extrapolated x {counts['cg_iters']} CG its, {counts['newton_iters']} Newton its, "
               f"{counts['residual_evals']} residuals")
     return est, sample, Oracle.num_threads()
 
@@ -223,7 +268,8 @@ def run_reference_arm(args):
             "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD if not args.small else "reduced (64, 16, 16) variant of: " + WORKLOAD,
                        "method": "FP64 Jacobi-PCG Newton, oracle CPU port (extrapolated)"},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample,
+                             "cpu_model": cpu_model()},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -326,44 +372,87 @@ def run_gpu_arm(args):
     assert out is not None and np.isfinite(out).all()
     h2d += 8 * 3 * m.n_nodes  # rest positions sent each step
 
-    # Jacobi-PCG FP32 of the first timed load (what the learned preconditioner replaces)
-    st_j32 = None
-    if method == "learned":
-        st_j32 = solve(p32, seeds[args.warmup], PC_JACOBI)
-    # plain FP64 Jacobi-PCG of the first timed load (the comparison the metric names)
-    t64 = None
-    st64 = None
-    st64a = None
-    if not args.skip_fp64:
-        p32.close()
-        p64 = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision="fp64", **kw)
-        s = seeds[args.warmup]
-        torch.cuda.synchronize()
-        st64 = solve(p64, s, PC_JACOBI)
-        t64 = st64["seconds"]
-        # the same FP64 solve through the assembled FP64 operator (context; the metric's FP64 baseline
-        # is the matrix-free solve above, the reference's method)
-        p64.set_operator("assembled")
-        solve(p64, s, PC_JACOBI)  # builds the sliced-ELL structure once
-        st64a = solve(p64, s, PC_JACOBI)
-        p64.close()
-
     pk, pk_kind = peaks()
     ms = prof["hvp_elem_ms"] / max(prof["samples"], 1)
-    achieved = prof["algo_bytes_hvp"] / (ms * 1e-3) / 1e9 if prof["samples"] else None
-    # DRAM bytes of one patch-product launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum on a
-    # 3,145,728-tet case of the same kernel (220.1 MB per launch, profiles/patch_hvp_fp32_c3.md), scaled
-    # by the tet count (the element data streams once per launch, far above L2 in both cases)
+    # algorithmic bytes of one FP32 Hessian-vector product: 56 B per tet (4 int32 corner indices,
+    # Dm^-1 and the volume, as the reference stores them) + 36 B per node (x and p read, Kp written)
+    algo_bytes = 56.0 * m.n_tets + 36.0 * m.n_nodes
+    achieved = algo_bytes / (ms * 1e-3) / 1e9 if prof["samples"] else None
+    # the bytes the launch itself must stream (for the assembled operator: the blocks, their columns
+    # and per free node z, p_old in and p, q out), reported beside the unit above
+    achieved_own = prof["algo_bytes_hvp"] / (ms * 1e-3) / 1e9 if prof["samples"] else None
     if args.operator == "assembled":
         kernel = "k_sell_hvp<float> (tangent assembled per Newton step, sliced-ELL sparse product)"
+        # DRAM bytes per launch: an ncu capture of the 3,145,728-tet case, scaled by the streamed bytes
         traffic = args.traffic if args.traffic else SELL_DRAM_PER_ALGO_BYTE * prof["algo_bytes_hvp"]
-        traffic_source = ("ncu capture at 3,145,728 tets scaled by the algorithmic bytes" if not args.traffic
+        traffic_source = ("ncu capture at 3,145,728 tets scaled by the streamed bytes" if not args.traffic
                           else "--traffic")
     else:
         kernel = "k_patch_hvp<float, neo-Hookean> (fused element Hessian-vector product)"
         traffic = args.traffic if args.traffic else HVP_DRAM_BYTES_PER_TET * m.n_tets
         traffic_source = ("ncu capture at 3,145,728 tets scaled by the tet count" if not args.traffic
                           else "--traffic")
+
+    # Jacobi-PCG FP32 of the first timed load (what the learned preconditioner replaces)
+    s_ref = seeds[args.warmup]
+    st_j32 = None
+    if method == "learned":
+        st_j32 = solve(p32, s_ref, PC_JACOBI)
+    # the main method on the first timed load again: its equilibrium for the oracle and FP64 checks
+    st_main = solve(p32, s_ref)
+    x32 = p32.get_positions()
+    # the same method through the matrix-free patch product (second record; the SURVEY's operator)
+    mf = None
+    if args.operator == "assembled" and not args.skip_matrix_free:
+        p32.set_operator("matrix-free")
+        solve(p32, s_ref)
+        torch.cuda.synchronize()
+        p32.set_profiling(True)
+        mf_stats = [solve(p32, s_) for s_ in seeds[args.warmup:args.warmup + 2]]
+        mprof = p32.get_profile()
+        p32.set_profiling(False)
+        mf_ms = mprof["hvp_elem_ms"] / max(mprof["samples"], 1)
+        mf_ach = algo_bytes / (mf_ms * 1e-3) / 1e9 if mprof["samples"] else None
+        mf = {"s_per_solve": [st_["seconds"] for st_ in mf_stats],
+              "newton_iters": [st_["newton_iters"] for st_ in mf_stats],
+              "cg_iters": [st_["cg_iters"] for st_ in mf_stats],
+              "converged": all(st_["status"] == 0 and st_["rel_res"] <= REL_TOL for st_ in mf_stats),
+              "kernel": "k_patch_hvp<float, neo-Hookean>", "ms_per_launch": mf_ms,
+              "achieved_gbs": mf_ach, "frac": mf_ach / pk if mf_ach else None, "peak_source": pk_kind}
+        p32.set_operator(args.operator)
+    # plain FP64 Jacobi-PCG of the first timed load (the comparison the metric names)
+    t64 = None
+    st64 = None
+    st64a = None
+    x64 = None
+    if not args.skip_fp64:
+        p32.close()
+        p64 = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision="fp64", **kw)
+        torch.cuda.synchronize()
+        st64 = solve(p64, s_ref, PC_JACOBI)
+        t64 = st64["seconds"]
+        x64 = p64.get_positions()
+        # the same FP64 solve through the assembled FP64 operator (context; the metric's FP64 baseline
+        # is the matrix-free solve above, the reference's method)
+        p64.set_operator("assembled")
+        solve(p64, s_ref, PC_JACOBI)  # builds the sliced-ELL structure once
+        st64a = solve(p64, s_ref, PC_JACOBI)
+        p64.close()
+
+    # parity of the timed result: the oracle's FP64 residual (ComputeGradients semantics) at the
+    # GPU's equilibria, and the FP32 solution's displacement error against the FP64 solve
+    oracle = None
+    parity = None
+    if rank == 0 and not args.skip_oracle:
+        oracle = make_oracle(m, fixed)
+        parity = {"load_seed": s_ref,
+                  "oracle_rel_res": oracle_rel_res(oracle, m, loads[s_ref], x32),
+                  "oracle_rel_res_fp64_solve": (oracle_rel_res(oracle, m, loads[s_ref], x64)
+                                                if x64 is not None else None)}
+        if x64 is not None:
+            parity["fp32_vs_fp64_displacement_rel_err"] = float(
+                np.linalg.norm(x32 - x64) / np.linalg.norm(x64 - m.nodes))
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -376,9 +465,12 @@ def run_gpu_arm(args):
                            " inner solves in FP32, FP64 residual and convergence test"),
                 "operator": args.operator,
                 "preconditioner": method, "l2": "inputs larger than L2 (element data 0.35 GB FP32)",
-                "jacobi_fp32_stats": st_j32,
                 "converged": ok, "newton_iters": [s_["newton_iters"] for s_ in stats],
                 "cg_iters": [s_["cg_iters"] for s_ in stats],
+                "parity": parity,
+                "main_method_stats": st_main,
+                "jacobi_fp32_stats": st_j32,
+                "matrix_free": mf,
                 "fp64_jacobi_pcg_s": t64,
                 "fp64_jacobi_pcg_stats": st64,
                 "fp64_jacobi_pcg_assembled_stats": st64a,
@@ -387,8 +479,12 @@ def run_gpu_arm(args):
             },
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk, "unit": "GB/s",
                          "frac": achieved / pk if achieved else None, "traffic": traffic,
-                         "kernel": kernel,
-                         "algo_bytes_per_launch": prof["algo_bytes_hvp"], "ms_per_launch": ms,
+                         "kernel": kernel, "algo_bytes_per_launch": algo_bytes,
+                         "algo_bytes_unit": "56 B per tet + 36 B per node (FP32 Hessian-vector product)",
+                         "ms_per_launch": ms,
+                         "streamed_bytes_per_launch": prof["algo_bytes_hvp"],
+                         "achieved_on_streamed_bytes": achieved_own,
+                         "frac_on_streamed_bytes": achieved_own / pk if achieved_own else None,
                          "peak_source": pk_kind, "traffic_source": traffic_source},
             "e2e": {"value": e2e_t, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(),
@@ -400,8 +496,9 @@ def run_gpu_arm(args):
                 counts = {"newton_iters": st64["newton_iters"], "cg_iters": st64["cg_iters"],
                           "residual_evals": st64["newton_iters"] + st64["line_search_cuts"] + 1}
             if counts["cg_iters"] is not None:
-                est, sample, cores = cpu_sample(m, fixed, counts)
-                line["cpu_baseline"] = {"value": est, "unit": "s", "cores": cores, "kind": "port", "sample": sample}
+                est, sample, cores = cpu_sample(m, fixed, counts, o=oracle)
+                line["cpu_baseline"] = {"value": est, "unit": "s", "cores": cores, "kind": "port",
+                                        "sample": sample, "cpu_model": cpu_model()}
         print(json.dumps(line), flush=True)
 
 
@@ -423,6 +520,8 @@ def main():
     ap.add_argument("--dims", default=None, help="override the lattice, e.g. 128,64,64 (profiling; not a bench line)")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-oracle", action="store_true", help="no oracle residual at the GPU equilibria")
+    ap.add_argument("--skip-matrix-free", action="store_true", help="no matrix-free record")
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per HVP launch, if captured")
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")

@@ -247,6 +247,14 @@ int sfem_adjoint(sfem_handle* h, const double* dLdu, double rel_tol, int32_t max
 #define SFEM_OP_MATRIX_FREE 0
 #define SFEM_OP_ASSEMBLED 1
 int sfem_set_operator(sfem_handle* h, int32_t op);
+/* Cap on the device bytes the assembled operator may hold (0: no cap; default).  When the assembly
+ * cannot get its memory (the cap, or cudaMalloc out of memory) the buffers it took are freed, the
+ * Krylov solves use the matrix-free product, the call reports success and the handle does not retry
+ * until sfem_set_operator or this function is called again.  No reference counterpart (the reference
+ * allocates its sparse matrix on the host, ElasticEnergy.cpp:573-635). */
+int sfem_set_operator_memory_limit(sfem_handle* h, int64_t bytes);
+/* Device bytes the assembled operator holds, and 1 in *fallback after an assembly ran out of memory. */
+int sfem_operator_info(sfem_handle* h, int64_t* bytes, int32_t* fallback);
 
 /* ---- assembled tangent (ElasticEnergy::AssembleStiffnessMatrix, Source/ElasticEnergy.cpp:573-635;
  * FemPhysicsMatrixFree::ComputeSystemMatrix :700-722 adds M/h^2 for implicit dynamics) ----
@@ -341,12 +349,16 @@ int sfem_kernel_launches(int64_t* count);
  * CUDA stream capture (allocation is not capturable and synchronises the device), control
  * loops that forbid allocation after start-up, and host applications that plan all device
  * memory themselves.  Computes out_dev[0] = sum_i a_dev[i] * b_dev[i] (device pointers),
- * ordered on `stream`, with the same fixed-order reduction as sfem_dot.  Its scratch is a
+ * ordered on `stream`.  The sum is deterministic (the same bits on every run: fixed 2048-entry
+ * tiles, the tile partials added in index order by the last block) but its order differs from
+ * sfem_dot's, so the two can differ in the last bits.  Its scratch is a
  * fixed static device array (one partial per 2048 entries + a counter, 512 KiB), held by every
  * device that loads this library until the process exits; n above 134,217,728 is rejected
  * with SFEM_ERR_INVALID.  Every call shares the array and clears its counter first, so calls
  * that overlap on the GPU race: serialise them.  The first call on a device looks the array's
- * address up (cudaGetSymbolAddress) and should come before any stream capture. */
+ * address up (cudaGetSymbolAddress) and should come before any stream capture.  That address is
+ * kept for the life of the process: after cudaDeviceReset (or any release of the device's primary
+ * context) it is stale, so do not call this entry point on that device again in the process. */
 int sfem_dot_noalloc_dev(const double* a_dev, const double* b_dev, int64_t n, double* out_dev, void* stream);
 
 /* ---- coarse space (extension; the reference's SolveConjugateGradientMF,

@@ -14,7 +14,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsfem_ref.so")
-REF_TREE = "/root/reference"
+# the reference source tree (present in the development container only); SFEM_REF_TREE overrides it
+REF_TREE = os.environ.get("SFEM_REF_TREE", "/root/reference")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

@@ -129,6 +129,8 @@ SIGNATURES = {
     "sfem_gnn_set_batch": [_vp, C.c_int32],
     "sfem_gnn_set_inference": [_vp, C.c_int32],
     "sfem_set_operator": [_vp, C.c_int32],
+    "sfem_set_operator_memory_limit": [_vp, C.c_int64],
+    "sfem_operator_info": [_vp, _i64p, _ip],
     "sfem_gnn_graph_form": [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "sfem_coarse_factors": [_dp, C.c_int64, C.c_double, C.c_double, _ip, _dp, _dp, _i64p],
     "sfem_gnn_get_params": [_vp, C.POINTER(C.c_float)],

@@ -136,6 +136,10 @@ struct sfem_handle {
   uint32_t* sell_code = nullptr;
   float *sell_vals32 = nullptr, *sell_ke32 = nullptr;
   double *sell_vals64 = nullptr, *sell_ke64 = nullptr;
+  // device bytes the assembled operator holds, the caller's cap on them (0: none), and whether an
+  // allocation failed (then the Krylov solves keep the matrix-free product until the operator is set again)
+  int64_t sell_bytes = 0, sell_limit = 0;
+  bool sell_oom = false;
   int32_t prof_op = 0;  // operator of the sampled Krylov launches
   float* pm32 = nullptr;
   DynView dyn() const { return DynView{vel, ustart, 1.0 / dt, 1.0 / (dt * dt)}; }
@@ -1056,6 +1060,38 @@ static void parallel_rows(int64_t n, F&& f) {
 // block (row r, position k) is block-slot base[r / 32] + 32 k + r % 32.  Each block-slot lists
 // its contributions 16 e + 4 a + b (block (a, b) of element e, a the row's corner) in the order of
 // the row's element entries, so the assembly is a deterministic gather.
+// device allocation for the assembled operator, counted against the handle's cap (sell_limit)
+extern "C++" {
+template <typename T>
+static int sell_alloc(sfem_handle* h, T** p, size_t count) {
+  *p = nullptr;
+  const int64_t bytes = (int64_t)(std::max<size_t>(count, 1) * sizeof(T));
+  if (h->sell_limit > 0 && h->sell_bytes + bytes > h->sell_limit)
+    return fail(SFEM_ERR_OOM, "assembled operator: %lld more bytes exceed the limit of %lld", (long long)bytes,
+                (long long)h->sell_limit);
+  TRY(dalloc(p, count));
+  h->sell_bytes += bytes;
+  return 0;
+}
+}
+
+// free every buffer of the assembled operator (also the ones a failed build left behind)
+static void sell_release(sfem_handle* h) {
+  void* bufs[] = {h->sell_base, h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32,
+                  h->sell_ke32, h->sell_col16, h->sell_vals64, h->sell_ke64};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  h->sell_base = h->sell_cptr = nullptr;
+  h->sell_col = h->sell_dslot = nullptr;
+  h->sell_code = nullptr;
+  h->sell_vals32 = h->sell_ke32 = nullptr;
+  h->sell_col16 = nullptr;
+  h->sell_vals64 = h->sell_ke64 = nullptr;
+  h->sell_T = -1;
+  h->sell_nnzb = 0;
+  h->sell_bytes = 0;
+}
+
 static int sell_structure(sfem_handle* h) {
   if (h->sell_T >= 0) return 0;
   const int64_t E = h->E, N = h->N, nbc = h->nbc, nf = h->nf, ns = (nf + 31) / 32;
@@ -1155,7 +1191,7 @@ static int sell_structure(sfem_handle* h) {
       }
     }
   }
-  TRY(dalloc(&h->sell_base, base.size()));
+  TRY(sell_alloc(h, &h->sell_base, base.size()));
   if (fits16) {
     std::vector<int16_t> d16((size_t)T, 0);
     for (int64_t r = 0; r < nf; r++) {
@@ -1165,14 +1201,14 @@ static int sell_structure(sfem_handle* h) {
         d16[t] = (int16_t)((int64_t)scol[t] - r);
       }
     }
-    TRY(dalloc(&h->sell_col16, std::max<size_t>(d16.size(), 1)));
+    TRY(sell_alloc(h, &h->sell_col16, std::max<size_t>(d16.size(), 1)));
     if (T > 0) CU(cudaMemcpyAsync(h->sell_col16, d16.data(), d16.size() * 2, cudaMemcpyHostToDevice, h->stream));
     TRY(sync(h));
   }
-  if (!fits16) TRY(dalloc(&h->sell_col, std::max<size_t>(scol.size(), 1)));
-  TRY(dalloc(&h->sell_cptr, cnt.size()));
-  TRY(dalloc(&h->sell_code, std::max<size_t>(code.size(), 1)));
-  TRY(dalloc(&h->sell_dslot, std::max<size_t>(dslot.size(), 1)));
+  if (!fits16) TRY(sell_alloc(h, &h->sell_col, std::max<size_t>(scol.size(), 1)));
+  TRY(sell_alloc(h, &h->sell_cptr, cnt.size()));
+  TRY(sell_alloc(h, &h->sell_code, std::max<size_t>(code.size(), 1)));
+  TRY(sell_alloc(h, &h->sell_dslot, std::max<size_t>(dslot.size(), 1)));
 
   CU(cudaMemcpyAsync(h->sell_base, base.data(), base.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
   if (!fits16 && T > 0)
@@ -1195,10 +1231,10 @@ static int sell_assemble(sfem_handle* h) {
   TRY(sell_structure(h));
   T** vals = reinterpret_cast<T**>(sizeof(T) == 4 ? (void*)&h->sell_vals32 : (void*)&h->sell_vals64);
   T** ke = reinterpret_cast<T**>(sizeof(T) == 4 ? (void*)&h->sell_ke32 : (void*)&h->sell_ke64);
-  if (!*vals) TRY(dalloc(vals, std::max<size_t>(9 * (size_t)h->sell_T, 1)));
+  if (!*vals) TRY(sell_alloc(h, vals, std::max<size_t>(9 * (size_t)h->sell_T, 1)));
   // 12-slot blocks per element: 16 for the corotational tangents (not symmetric), 10 otherwise
   const int nb_alloc = (h->material == SFEM_MMT_COROTATIONAL) ? 16 : 10;
-  if (!*ke) TRY(dalloc(ke, (size_t)h->E * 12 * nb_alloc));
+  if (!*ke) TRY(sell_alloc(h, ke, (size_t)h->E * 12 * nb_alloc));
   const T* uT = disp<T>(h);
   const ElemView<T> ev = ev_of<T>(h);
   int nb = 10;
@@ -1221,11 +1257,16 @@ struct OperatorScope {
   sfem_handle* h;
   int st = 0;
   explicit OperatorScope(sfem_handle* hh) : h(hh) {
-    if (h->op_mode == 1 && h->n_inst == 0 && mat_id(h) <= 4) {
+    if (h->op_mode == 1 && h->n_inst == 0 && mat_id(h) <= 4 && !h->sell_oom) {
       st = h->precision == SFEM_FP32 ? sell_assemble<float>(h) : sell_assemble<double>(h);
       h->sell_on = st == 0;
-      if (st == SFEM_ERR_OOM) {  // without the memory: the matrix-free product
+      if (st == SFEM_ERR_OOM) {
+        // without the memory: free what the failed build holds, remember the failure so that later
+        // Newton steps go straight to the matrix-free product, and report success
         cudaGetLastError();
+        sell_release(h);
+        h->sell_oom = true;
+        g_err.clear();
         st = 0;
       }
     }
@@ -1253,22 +1294,27 @@ int sfem_set_operator(sfem_handle* h, int32_t op) {
   if (op != SFEM_OP_MATRIX_FREE && op != SFEM_OP_ASSEMBLED)
     return fail(SFEM_ERR_INVALID, "operator is SFEM_OP_MATRIX_FREE (0) or SFEM_OP_ASSEMBLED (1)");
   h->op_mode = op;
+  h->sell_oom = false;  // setting the operator again retries the assembly
   if (op == SFEM_OP_MATRIX_FREE && h->sell_T >= 0) {  // release the assembled operator's memory
     TRY(set_device(h));
     TRY(sync(h));
-    void* bufs[] = {h->sell_base, h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32,
-                    h->sell_ke32, h->sell_col16, h->sell_vals64, h->sell_ke64};
-    for (void* b : bufs)
-      if (b) cudaFree(b);
-    h->sell_base = h->sell_cptr = nullptr;
-    h->sell_col = h->sell_dslot = nullptr;
-    h->sell_code = nullptr;
-    h->sell_vals32 = h->sell_ke32 = nullptr;
-    h->sell_col16 = nullptr;
-    h->sell_vals64 = h->sell_ke64 = nullptr;
-    h->sell_T = -1;
-    h->sell_nnzb = 0;
+    sell_release(h);
   }
+  return SFEM_OK;
+}
+
+int sfem_set_operator_memory_limit(sfem_handle* h, int64_t bytes) {
+  TRY(check_handle(h));
+  if (bytes < 0) return fail(SFEM_ERR_INVALID, "the limit is a byte count (0: no limit)");
+  h->sell_limit = bytes;
+  h->sell_oom = false;
+  return SFEM_OK;
+}
+
+int sfem_operator_info(sfem_handle* h, int64_t* bytes, int32_t* fallback) {
+  TRY(check_handle(h));
+  if (bytes) *bytes = h->sell_bytes;
+  if (fallback) *fallback = h->sell_oom ? 1 : 0;
   return SFEM_OK;
 }
 

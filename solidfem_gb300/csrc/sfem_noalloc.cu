@@ -17,7 +17,11 @@
 //    (concurrent streams) race and must be serialised by the caller;
 //  * the first call on each device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current); make that first call before
-//    any stream capture begins.
+//    any stream capture begins.  The address is cached for the life of the process:
+//    after cudaDeviceReset, or after the device's primary context is released, the
+//    cached address is stale and the entry point must not be called on that device;
+//  * the summation order (fixed tiles, partials in index order) is deterministic but
+//    not sfem_dot's, so the two results can differ in the last bits.
 #include <cuda_runtime.h>
 #include <stdint.h>
 

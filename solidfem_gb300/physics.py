@@ -338,6 +338,18 @@ class FemPhysicsMatrixFree:
         nat.check(self._lib.sfem_set_operator(self._h, {"matrix-free": nat.OP_MATRIX_FREE,
                                                          "assembled": nat.OP_ASSEMBLED}[op]))
 
+    def set_operator_memory_limit(self, nbytes: int) -> None:
+        """Cap on the device memory of the assembled operator (0: none); beyond it the Krylov solves
+        keep the matrix-free product."""
+        nat.check(self._lib.sfem_set_operator_memory_limit(self._h, int(nbytes)))
+
+    def operator_info(self):
+        """(bytes held by the assembled operator, True when its assembly ran out of memory)."""
+        b = C.c_int64()
+        f = C.c_int32()
+        nat.check(self._lib.sfem_operator_info(self._h, C.byref(b), C.byref(f)))
+        return b.value, bool(f.value)
+
     def set_profiling(self, enable=True):
         nat.check(self._lib.sfem_set_profiling(self._h, int(enable)))
 

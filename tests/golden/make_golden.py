@@ -3,7 +3,7 @@
 The reference's hot-path sources are compiled unmodified into
 oracle/_ref/libsfem_ref.so (oracle/Makefile.ref) and driven through
 oracle/ref_harness.cpp.  This script needs the reference tree
-(/root/reference) and is run in the development container only:
+(SFEM_REF_TREE, default /root/reference) and is run in the development container only:
 
     python tests/golden/make_golden.py
 
@@ -40,10 +40,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle.oracle import RefHarness  # noqa: E402
+from oracle.oracle import REF_TREE, RefHarness  # noqa: E402
 from solidfem_gb300.mesh import box_lattice, lumped_face_load  # noqa: E402
 
-REF = "/root/reference"
+REF = REF_TREE
 MATS = {0: "linear", 1: "stvk", 2: "corot", 3: "nh"}
 
 

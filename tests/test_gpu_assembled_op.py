@@ -235,3 +235,38 @@ def test_randomly_numbered_mesh_fp64_assembled():
           f"rel diff {rel(x_as, x_mf):.2e}")
     assert abs(col_bytes - 4.0) < 1e-6
     assert st_mf["status"] == 0 and st_as["status"] == 0 and rel(x_as, x_mf) < 1e-7
+
+
+def test_memory_limit_falls_back_without_leaking():
+    """An assembly that cannot get its memory frees what it took, solves matrix-free, reports success
+    with no error message, and does not retry every Newton step; lifting the cap assembles again."""
+    from solidfem_gb300 import _native as nat
+
+    m, p = slab(16, 8, 8)
+    p.set_operator("assembled")
+    st_ok = p.newton_solve(rel_tol=1e-8, max_newton=30)
+    full, fb = p.operator_info()
+    assert st_ok["status"] == 0 and full > 0 and not fb
+    x_as = p.get_free_positions()
+    p.set_operator("matrix-free")
+    assert p.operator_info() == (0, False)
+    p.set_positions(m.nodes)
+    st_mf = p.newton_solve(rel_tol=1e-8, max_newton=30)
+    x_mf = p.get_free_positions()
+    # caps that fail at the first and at the last allocation of the assembly
+    for cap in (1024, full - 1):
+        p.set_operator("assembled")
+        p.set_operator_memory_limit(cap)
+        p.set_positions(m.nodes)
+        st = p.newton_solve(rel_tol=1e-8, max_newton=30)
+        assert st["status"] == 0 and st["newton_iters"] >= 2
+        assert p.operator_info() == (0, True), p.operator_info()
+        assert nat.load().sfem_last_error() in (b"", None)
+        # the same iterates as the matrix-free solve: the fallback is that solve
+        assert st["cg_iters"] == st_mf["cg_iters"]
+        assert rel(p.get_free_positions(), x_mf) < 1e-12
+    p.set_operator_memory_limit(0)
+    p.set_positions(m.nodes)
+    st = p.newton_solve(rel_tol=1e-8, max_newton=30)
+    assert st["status"] == 0 and p.operator_info() == (full, False)
+    assert rel(p.get_free_positions(), x_as) < 1e-6

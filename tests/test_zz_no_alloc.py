@@ -46,6 +46,8 @@ def test_noalloc_dot_matches_sfem_dot_on_two_calls_in_a_row():
         got = out.item()
         scale = float(np.abs(a) @ np.abs(b))
         assert abs(got - expected) <= TOL * scale, (call, got, expected)
+        # and against the FP64 dot product on the host
+        assert abs(got - float(a @ b)) <= TOL * scale, (call, got, float(a @ b))
 
 
 def test_noalloc_dot_rejects_sizes_beyond_its_maximum():
