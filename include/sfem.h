@@ -225,6 +225,12 @@ int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* op
  * SolveNewtonLS, Source/FemPhysicsMatrixFree.cpp:325-331, 604-628, 733-781): globalized inexact
  * Newton with matrix-free PCG inner solves.  Updates the handle's positions. */
 int sfem_newton_solve(sfem_handle* h, const sfem_newton_opts* opts, sfem_newton_stats* stats);
+/* Record every line-search trial of the following Newton solves into caller-owned host memory:
+ * trace[3k .. 3k+2] = (Newton iteration from 0, step length, FP64 residual norm at the trial) for
+ * k < *count <= cap; *count is reset to 0 here and advanced by the solves.  trace = NULL stops it.
+ * The trials are the ones NewtonSolverBackTrack::Solve (Include/NewtonSolver.h:179-348) evaluates,
+ * so its bisection can be compared step by step. */
+int sfem_set_newton_trace(sfem_handle* h, double* trace, int32_t cap, int32_t* count);
 /* NonlinearConjugateGradientMinimizer::Solve (Include/NonlinearCG.h:51-114) with the
  * reference's constants; outer/inner iteration caps and absolute threshold as its fields. */
 int sfem_nonlinear_cg(sfem_handle* h, int32_t outer_iters, int32_t inner_iters, double abs_tol,

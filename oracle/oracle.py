@@ -314,6 +314,8 @@ class RefHarness:
             lib.ref_newton_direct.restype = C.c_int
             lib.ref_newton_fd.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp]
             lib.ref_newton_fd.restype = C.c_int
+            lib.ref_newton_ls_trace.argtypes = [C.c_void_p, C.c_int, C.c_double, _ip, _dp, _dp, C.c_int, _dp, _ip]
+            lib.ref_newton_ls_trace.restype = C.c_int
             cls._lib = lib
         return cls._lib
 
@@ -444,3 +446,16 @@ class RefHarness:
         r = np.zeros(1)
         it = self.lib().ref_newton_direct(self.h, max_iters, rel_tol, _p(r))
         return it, r[0]
+
+    def newton_ls_trace(self, max_iters=400, abs_tol=1e-9, cap=100000):
+        """The reference's NewtonSolverBackTrack with its Bonet-Wood condition (SolveNewtonLS's set-up):
+        per line-search trial the Newton iteration, the step length and the residual norm."""
+        it = np.zeros(cap, dtype=np.int32)
+        step = np.zeros(cap)
+        res = np.zeros(cap)
+        r0 = np.zeros(1)
+        conv = np.zeros(1, dtype=np.int32)
+        n = self.lib().ref_newton_ls_trace(self.h, max_iters, abs_tol, _p(it, _ip), _p(step), _p(res), cap,
+                                           _p(r0), _p(conv, _ip))
+        return dict(it=it[:n].copy(), step=step[:n].copy(), res=res[:n].copy(), r0=float(r0[0]),
+                    converged=bool(conv[0]))

@@ -25,6 +25,7 @@ FILE* out = NULL;  // the reference's Printf sink (FEMLibrary.cpp:35)
 #include "FemPhysicsMatrixFree.h"
 #include "ElasticEnergy.h"
 #include "LinearSolver.h"
+#include "NewtonSolver.h"
 #include <Eigen/SparseLU>
 #include <Eigen/LU>
 
@@ -363,6 +364,79 @@ int ref_newton_fd(void* hp, int max_iters, double rel_tol, double* res_out) {
   }
   *res_out = rn;
   return it;
+}
+
+// The reference's own NewtonSolverBackTrack (Include/NewtonSolver.h:179-348) with the default
+// Bonet-Wood condition, exactly as FemPhysicsMatrixFree::SolveNewtonLS sets it up
+// (Source/FemPhysicsMatrixFree.cpp:733-781, static case), over a problem that forwards every
+// callback to the reference class and records each line-search trial: the Newton iteration it
+// belongs to, its step length relative to the Newton direction, and the norm of its residual.
+namespace {
+struct TraceProblem {
+  RefProblem* p;
+  std::vector<int> it;
+  std::vector<double> step, res;
+  EigenVector base, delta, last;
+  int iter = -1;
+  double res0 = 0;
+  EigenVector ComputeRhs(const EigenVector& sol) {
+    EigenVector r = p->ComputeRhs(sol);
+    if (iter < 0) {
+      res0 = r.norm();
+    } else {
+      it.push_back(iter);
+      step.push_back((sol - base).dot(delta) / delta.squaredNorm());
+      res.push_back(r.norm());
+    }
+    last = sol;
+    return r;
+  }
+  // FemPhysicsMatrixFree::ComputeSystemMatrix (:696-715) for a static problem without Dirichlet
+  // penalties or cables: the assembled tangent at the state of the last ComputeRhs
+  void ComputeSystemMatrix(const EigenVector&, const EigenVector&, SparseMatrix& K) {
+    ElasticEnergy::AssembleStiffnessMatrix(p, K);
+  }
+  EigenVector SolveLinearSystem(SparseMatrix& K, const EigenVector& rhs, const EigenVector& s, const EigenVector& y) {
+    EigenVector d = p->SolveLinearSystem(K, rhs, s, y);
+    iter++;
+    base = last;
+    delta = d;
+    return d;
+  }
+  real MeritResidual(const EigenVector& rhs) { return p->MeritResidual(rhs); }
+};
+}  // namespace
+
+// Returns the number of recorded trials (at most cap); it/step/res per trial, *res0 the initial
+// residual norm, *converged the solver's result.  Positions are left at the solver's solution.
+int ref_newton_ls_trace(void* hp, int max_iters, double abs_tol, int* it, double* step, double* res, int cap,
+                        double* res0, int* converged) {
+  RefProblem* p = ((Handle*)hp)->phys;
+  p->SetForceFraction(1);
+  TraceProblem tp;
+  tp.p = p;
+  NewtonSolverBackTrack<TraceProblem, SparseMatrix> solver;
+  solver.mNumIterations = max_iters;
+  solver.mVerbose = VL_NONE;
+  solver.mResidualThreshold = abs_tol;
+  solver.mUseProblemSolver = true;
+  const uint32 nf = p->GetNumFreeNodes(), nbc = p->NumBCs();
+  EigenVector solution(3 * nf);
+  for (uint32 i = 0; i < nf; i++) {
+    const Vector3R& x = p->Nodes()[i + nbc].pos;
+    solution(3 * i) = x.x; solution(3 * i + 1) = x.y; solution(3 * i + 2) = x.z;
+  }
+  *converged = solver.Solve(tp, 3 * nf, solution) ? 1 : 0;
+  for (uint32 i = 0; i < nf; i++)
+    p->Nodes()[i + nbc].pos = Vector3R(solution(3 * i), solution(3 * i + 1), solution(3 * i + 2));
+  *res0 = tp.res0;
+  const int n = std::min<int>(cap, (int)tp.it.size());
+  for (int k = 0; k < n; k++) {
+    it[k] = tp.it[k];
+    step[k] = tp.step[k];
+    res[k] = tp.res[k];
+  }
+  return n;
 }
 
 }  // extern "C"

@@ -130,6 +130,7 @@ SIGNATURES = {
     "sfem_gnn_set_inference": [_vp, C.c_int32],
     "sfem_set_operator": [_vp, C.c_int32],
     "sfem_set_operator_memory_limit": [_vp, C.c_int64],
+    "sfem_set_newton_trace": [_vp, _dp, C.c_int32, _ip],
     "sfem_operator_info": [_vp, _i64p, _ip],
     "sfem_gnn_graph_form": [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "sfem_coarse_factors": [_dp, C.c_int64, C.c_double, C.c_double, _ip, _dp, _dp, _i64p],

@@ -140,6 +140,10 @@ struct sfem_handle {
   // allocation failed (then the Krylov solves keep the matrix-free product until the operator is set again)
   int64_t sell_bytes = 0, sell_limit = 0;
   bool sell_oom = false;
+  // optional record of every line-search trial of the Newton solves (caller-owned host memory)
+  double* ls_trace = nullptr;
+  int32_t ls_trace_cap = 0;
+  int32_t* ls_trace_count = nullptr;
   int32_t prof_op = 0;  // operator of the sampled Krylov launches
   float* pm32 = nullptr;
   DynView dyn() const { return DynView{vel, ustart, 1.0 / dt, 1.0 / (dt * dt)}; }
@@ -1303,6 +1307,16 @@ int sfem_set_operator(sfem_handle* h, int32_t op) {
   return SFEM_OK;
 }
 
+int sfem_set_newton_trace(sfem_handle* h, double* trace, int32_t cap, int32_t* count) {
+  TRY(check_handle(h));
+  if (trace && (cap < 0 || !count)) return fail(SFEM_ERR_INVALID, "trace needs a capacity and a count");
+  h->ls_trace = trace;
+  h->ls_trace_cap = trace ? cap : 0;
+  h->ls_trace_count = trace ? count : nullptr;
+  if (count) *count = 0;
+  return SFEM_OK;
+}
+
 int sfem_set_operator_memory_limit(sfem_handle* h, int64_t bytes) {
   TRY(check_handle(h));
   if (bytes < 0) return fail(SFEM_ERR_INVALID, "the limit is a byte count (0: no limit)");
@@ -1928,6 +1942,16 @@ int instances_update(sfem_handle* h, const sfem_newton_opts& op, bool first, boo
   return 0;
 }
 
+// one line-search trial into the caller's trace buffer (Newton iteration, step length, |r|)
+void trace_trial(sfem_handle* h, int iter, double step, double rnorm) {
+  if (!h->ls_trace || !h->ls_trace_count || *h->ls_trace_count >= h->ls_trace_cap) return;
+  double* t = h->ls_trace + 3 * (size_t)*h->ls_trace_count;
+  t[0] = iter;
+  t[1] = step;
+  t[2] = rnorm;
+  (*h->ls_trace_count)++;
+}
+
 int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, double* rn_io, int* nit, int* cgit,
                  int* cuts, int max_newton) {
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
@@ -2005,6 +2029,7 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
         launch_axpy_state<double>((int64_t)n, a, h->tmp64 + o, h->ubase + o, h->u + o, h->stream);
         int ninv = 0;
         TRY(residual(h, &rnew, &ninv));
+        trace_trial(h, *nit - 1, a, rnew);
         if (ninv == 0 && std::isfinite(rnew) && rnew <= (1 - 1e-4 * a) * rn) {
           ok = true;
           break;
@@ -2021,6 +2046,7 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
         int ninv = 0;
         double en[2] = {0.0, 0.0};  // elastic and total energy, with the residual (Armijo)
         TRY(residual(h, &rnew, &ninv, op.ls_condition == SFEM_LSC_ARMIJO ? en : nullptr));
+        trace_trial(h, *nit - 1, a, rnew);
         bool cond = false;
         if (ninv == 0 && std::isfinite(rnew)) {
           if (op.ls_condition == SFEM_LSC_ARMIJO) {

@@ -318,6 +318,22 @@ class FemPhysicsMatrixFree:
         """x_start = x (the reference's pos0 = pos at the start of an implicit Step)."""
         nat.check(self._lib.sfem_begin_step(self._h))
 
+    def set_newton_trace(self, cap=100000):
+        """Record every line-search trial of the following Newton solves (cap trials; 0 stops it):
+        newton_trace() then returns rows (Newton iteration, step length, |r| at the trial)."""
+        if cap <= 0:
+            nat.check(self._lib.sfem_set_newton_trace(self._h, None, 0, None))
+            self._trace = None
+            return
+        buf = np.zeros((cap, 3))
+        cnt = C.c_int32(0)
+        nat.check(self._lib.sfem_set_newton_trace(self._h, _dp(buf), cap, C.byref(cnt)))
+        self._trace = (buf, cnt)  # kept alive while the library writes into them
+
+    def newton_trace(self):
+        buf, cnt = self._trace
+        return buf[:cnt.value].copy()
+
     def nonlinear_cg(self, outer_iters=200, inner_iters=10, abs_tol=1e-4):
         it = C.c_int32()
         nat.check(self._lib.sfem_nonlinear_cg(self._h, outer_iters, inner_iters, abs_tol, C.byref(it)))

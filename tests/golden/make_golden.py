@@ -27,7 +27,12 @@ Fixtures (npz):
   variant_<m>.npz    the same lattice for the other MaterialModelType values m = 4..12: stress,
                      gradients, energy, tangent diagonal and assembled tangent from the reference.
 
-    python tests/golden/make_golden.py [--only dyn|tangent|variant]
+  nlcg_c1.npz        the C1 cantilever: the reference's NonlinearConjugateGradientMinimizer iterate after
+                     k outer iterations (10 inner), for E = 1e7 (k = 1, 3, 10) and E = 1e5 (k = 1, 3).
+  bw_c1.npz          the C1 cantilever: the reference's NewtonSolverBackTrack with the Bonet-Wood condition,
+                     every line-search trial (Newton iteration, step length, residual norm) and the solution.
+
+    python tests/golden/make_golden.py [--only dyn|tangent|variant|solvers]
 """
 from __future__ import annotations
 
@@ -140,9 +145,42 @@ def variants():
         print(f"variant {mat}: |grad| {np.linalg.norm(ref.gradients()):.3e} energy {ref.elastic_energy():.3e}")
 
 
+def reference_solvers():
+    """The reference's own nonlinear solvers on the C1 cantilever (16x4x4, gravity, x=0 clamped):
+    NonlinearConjugateGradientMinimizer (Include/NonlinearCG.h:51-114, through Step(0) with
+    NST_NONLINEAR_CG) after k outer iterations, and NewtonSolverBackTrack with its Bonet-Wood
+    condition (SolveNewtonLS's set-up) with every line-search trial recorded."""
+    m = box_lattice(16, 4, 4, extent=(4.0, 1.0, 1.0))
+    fixed = m.face_nodes(0, 0)
+    out = dict(nodes=m.nodes, tets=m.tets, fixed=fixed, poisson=0.45, density=1070.0,
+               gravity=np.array([0.0, 0.0, -9.81]), material=3, inner_iters=10, abs_tol=1e-12)
+    cases = [(1e7, 1), (1e7, 3), (1e7, 10), (1e5, 1), (1e5, 3)]
+    pos = []
+    for young, k in cases:
+        ref = RefHarness(m.nodes, m.tets, fixed, young, 0.45, 1070.0, -9.81, True, 3, solver=3, outer_iters=k,
+                         inner_iters=10, abs_tol=1e-12)
+        ref.set_force_fraction(0.0)  # Step(0) of ST_STATIC solves only while mForceFraction == 0
+        ref.step()
+        pos.append(ref.positions())
+        print(f"nlcg E={young:g} k={k}: max |u| {np.abs(pos[-1] - m.nodes).max():.4e}")
+    out.update(young=np.array([c[0] for c in cases]), outer_iters=np.array([c[1] for c in cases]),
+               positions=np.array(pos))
+    np.savez_compressed(os.path.join(HERE, "nlcg_c1.npz"), **out)
+
+    ref = RefHarness(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, -9.81, True, 3, solver=1, outer_iters=400,
+                     abs_tol=1e-9)
+    tr = ref.newton_ls_trace(400, 1e-9)
+    np.savez_compressed(os.path.join(HERE, "bw_c1.npz"), nodes=m.nodes, tets=m.tets, fixed=fixed, young=1e5,
+                        poisson=0.45, density=1070.0, gravity=np.array([0.0, 0.0, -9.81]), material=3,
+                        abs_tol=1e-9, trial_iter=tr["it"], trial_step=tr["step"], trial_res=tr["res"], r0=tr["r0"],
+                        converged=tr["converged"], eq_positions=ref.positions())
+    print(f"bonet-wood: {tr['it'].max() + 1} Newton iterations, {tr['it'].size} trials, converged {tr['converged']}")
+
+
 def main():
     if "--only" in sys.argv:
-        {"dyn": dynamics, "tangent": tangents, "variant": variants}[sys.argv[sys.argv.index("--only") + 1]]()
+        {"dyn": dynamics, "tangent": tangents, "variant": variants,
+         "solvers": reference_solvers}[sys.argv[sys.argv.index("--only") + 1]]()
         return
     if not os.path.isdir(REF):
         sys.exit("reference tree not present; fixtures are generated in the development container")
@@ -210,6 +248,7 @@ def main():
     dynamics()
     tangents()
     variants()
+    reference_solvers()
 
 
 if __name__ == "__main__":

@@ -86,14 +86,25 @@ def test_adjoint_vs_finite_differences_and_oracle(dims, n_fd):
         fdv = (L(young, fp) - L(young, fm)) / (2 * h)
         assert abs(gF[i, c] - fdv) <= 1e-4 * np.abs(gF).max() + 1e-6 * abs(fdv)
 
-    # FP64 oracle adjoint at the oracle's own equilibrium
+    # the FP64 oracle's adjoint (the reference gradient): at the oracle's own equilibrium on the small
+    # mesh; at the full 98,304-tet size at the GPU's equilibrium, after the oracle's own FP64 residual
+    # has certified it (one CPU PCG solve of K lam = dL/du instead of a CPU Newton solve)
+    o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, (0.0, 0.0, 0.0), 3)
+    o.set_element_scale(young / 1e5)
+    o.set_nodal_loads(f)
     if m.n_tets <= 2000:
-        o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, (0.0, 0.0, 0.0), 3)
-        o.set_element_scale(young / 1e5)
-        o.set_nodal_loads(f)
         status, st_o = o.newton_pcg(rtol=1e-11, max_newton=100)
         assert status == 0, st_o
         uo = o.free_positions().reshape(-1, 3) - rest
-        dE_o, dF_o, _ = o.adjoint((2 * (uo - u_t)).ravel(), young, tol=1e-12)
-        assert np.linalg.norm(gE - dE_o) <= 1e-6 * np.linalg.norm(dE_o)
-        assert np.linalg.norm(gF.ravel() - dF_o) <= 1e-6 * np.linalg.norm(dF_o)
+    else:
+        r0 = np.linalg.norm(o.gradients())
+        uo = solve_u(phys, young, f_free, rest)
+        o.set_free_positions((rest + uo).ravel())
+        r_eq = np.linalg.norm(o.gradients()) / r0
+        print(f"{dims}: oracle |r|/|r0| at the GPU equilibrium {r_eq:.2e}")
+        assert r_eq <= 1e-9
+    dE_o, dF_o, its = o.adjoint((2 * (uo - u_t)).ravel(), young, tol=1e-12, max_cg=200000)
+    eE = np.linalg.norm(gE - dE_o) / np.linalg.norm(dE_o)
+    eF = np.linalg.norm(gF.ravel() - dF_o) / np.linalg.norm(dF_o)
+    print(f"{dims}: adjoint vs the FP64 oracle's ({its} CPU PCG iterations): dL/dE {eE:.2e}, dL/df {eF:.2e}")
+    assert eE <= 1e-6 and eF <= 1e-6

@@ -59,15 +59,24 @@ def test_c3_slab_fp32_learned_vs_oracle_and_fp64():
     r0 = np.linalg.norm(o.gradients())
     o.set_positions_shuffled(_shuffled(o, m.nodes + u32))
     r32 = np.linalg.norm(o.gradients()) / r0
-    o.set_positions_shuffled(_shuffled(o, m.nodes + u64))
+    x64 = _shuffled(o, m.nodes + u64)
+    o.set_positions_shuffled(x64)
     r64 = np.linalg.norm(o.gradients()) / r0
+    # the oracle evaluates positions, not displacements: rounding a position to FP64 alone moves the
+    # residual by about this much (the same positions moved by one ulp at random)
+    rng = np.random.default_rng(1)
+    xp = x64.copy()
+    xp[o.n_bcs:] = np.nextafter(xp[o.n_bcs:], np.where(rng.random(xp[o.n_bcs:].shape) < 0.5, -np.inf, np.inf))
+    o.set_positions_shuffled(xp)
+    floor = np.linalg.norm(o.gradients()) / r0
     err = np.linalg.norm(u32 - u64) / np.linalg.norm(u64)
     print(f"C3 slab 3.1M tets: FP32 learned {st32['seconds']:.3f} s ({st32['newton_iters']} Newton, "
           f"{st32['cg_iters']} CG), oracle |r|/|r0| {r32:.2e}; FP64 Jacobi {st64['seconds']:.2f} s "
-          f"({st64['newton_iters']} Newton, {st64['cg_iters']} CG), oracle |r|/|r0| {r64:.2e}; "
-          f"displacement error FP32 vs FP64 {err:.2e}")
+          f"({st64['newton_iters']} Newton, {st64['cg_iters']} CG), oracle |r|/|r0| {r64:.2e} (1-ulp "
+          f"position floor {floor:.2e}); displacement error FP32 vs FP64 {err:.2e}")
     # the oracle's residual agrees with the GPU's FP64 residual up to summation order
     assert r32 <= 1.5e-8
-    assert r64 <= 1.5e-10
+    # below 1e-9 the oracle's measure reaches the floor set by FP64 positions
+    assert r64 <= max(1.5e-10, 2.0 * floor)
     # the FP32-refined solution's error against the FP64 solution (stated; bounded here)
     assert err <= 1e-5
