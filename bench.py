@@ -510,12 +510,159 @@ def _stream_of(p):
     return s.value
 
 
+# ---------------------------------------------------------------------------
+# The other configurations: GPU time beside the oracle port's CPU time (one JSON line each)
+# ---------------------------------------------------------------------------
+def _cpu_window(o, counts, its=20):
+    """Per-operation CPU costs of the oracle port (one residual, one Jacobi diagonal, `its` PCG
+    iterations, OpenMP over the host cores) extrapolated by a solve's operation counts."""
+    t = time.perf_counter()
+    r = o.gradients()
+    t_grad = time.perf_counter() - t
+    t = time.perf_counter()
+    diag = o.jacobi_diagonal()
+    t_diag = time.perf_counter() - t
+    t = time.perf_counter()
+    o.pcg(r, diag=diag, tol=1e-30, max_iters=its)
+    t_iter = (time.perf_counter() - t) / its
+    est = counts["cg_iters"] * t_iter + counts["newton_iters"] * t_diag + counts["residual_evals"] * t_grad
+    return est, (f"measured: 1 residual {t_grad:.3f} s, 1 Jacobi diagonal {t_diag:.3f} s, {its} PCG iterations "
+                 f"{t_iter * 1e3:.2f} ms/it; extrapolated x {counts['cg_iters']} CG its, {counts['newton_iters']} "
+                 f"Newton its, {counts['residual_evals']} residuals")
+
+
+def _gpu_newton(p, x0, reps=3, **kw):
+    times, st = [], None
+    for _ in range(reps + 1):
+        p.set_positions(x0)
+        st = p.newton_solve(**kw)
+        times.append(st["seconds"])
+    return float(np.median(times[1:])), st
+
+
+def run_config(args):
+    """C1 (16x4x4 cantilever, FP64 Newton to 1e-10), C2 (128x32x32, corotational and neo-Hookean,
+    FP64 and FP32-refined to 1e-10), C4 (64 bodies, FP32-refined to 1e-8), C5 (64x16x16, per-element E:
+    FP64 Newton to 1e-11 and the adjoint) on the GPU, next to the oracle port on the host cores."""
+    import torch
+
+    from oracle.oracle import Oracle
+    from solidfem_gb300 import FemPhysicsMatrixFree
+    from solidfem_gb300.mesh import box_lattice, lumped_face_load
+
+    torch.cuda.init()
+    cfg = args.config
+    rec = {"metric": f"{cfg}: solve time, GPU beside the oracle CPU port", "config": cfg, "unit": "s"}
+    cores = Oracle.num_threads()
+    if cfg == "c1":
+        m = box_lattice(16, 4, 4, extent=(4.0, 1.0, 1.0))
+        fixed = m.face_nodes(0, 0)
+        p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.45, density=1070.0,
+                                 gravity=(0.0, 0.0, -9.81), material=3)
+        t_gpu, st = _gpu_newton(p, m.nodes, rel_tol=1e-10, max_newton=200)
+        o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, (0.0, 0.0, -9.81), 3)
+        t = time.perf_counter()
+        status, so = o.newton_pcg(rtol=1e-10, max_newton=200)
+        t_cpu = time.perf_counter() - t
+        rec.update(workload="16x4x4 x 6 tets (425 nodes / 1,536 tets), neo-Hookean E=1e5 nu=0.45, gravity, "
+                            "FP64 Jacobi-PCG Newton to 1e-10",
+                   gpu={"s": t_gpu, "newton_iters": st["newton_iters"], "cg_iters": st["cg_iters"],
+                        "status": st["status"]},
+                   cpu_baseline={"value": t_cpu, "kind": "port", "cores": cores, "cpu_model": cpu_model(),
+                                 "sample": f"full solve measured (status {status}, {so['newton_iters']} Newton, "
+                                           f"{so['cg_iters']} CG)"})
+    elif cfg == "c2":
+        m = box_lattice(128, 32, 32, extent=(8.0, 2.0, 2.0))
+        fixed = m.face_nodes(0, 0)
+        f = lumped_face_load(m, 0, 1, (0.0, 0.0, -500.0))
+        rec["workload"] = ("128x32x32 x 6 tets (140,481 nodes / 786,432 tets), E=1e6 nu=0.4, 500 Pa -z traction "
+                           "on x=8, Newton to 1e-10")
+        for mat, name in ((2, "corotational"), (3, "neo-Hookean")):
+            kw = dict(young=1e6, poisson=0.4, density=1070.0, gravity=(0, 0, 0), material=mat, tangent="exact")
+            out = {}
+            for prec in ("fp64", "fp32"):
+                p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision=prec, **kw)
+                p.set_nodal_loads(f)
+                t_gpu, st = _gpu_newton(p, m.nodes, reps=1, rel_tol=1e-10, max_newton=60)
+                out[prec] = {"s": t_gpu, "newton_iters": st["newton_iters"], "cg_iters": st["cg_iters"],
+                             "status": st["status"]}
+                if prec == "fp64":
+                    counts = {"newton_iters": st["newton_iters"], "cg_iters": st["cg_iters"],
+                              "residual_evals": st["newton_iters"] + st["line_search_cuts"] + 1}
+                p.close()
+            o = Oracle(m.nodes, m.tets, fixed, 1e6, 0.4, 1070.0, (0, 0, 0), mat)
+            o.set_tangent(1)
+            o.set_nodal_loads(f)
+            est, sample = _cpu_window(o, counts)
+            out["cpu_baseline"] = {"value": est, "kind": "port", "cores": cores, "cpu_model": cpu_model(),
+                                   "sample": sample + " (the GPU FP64 solve's counts)"}
+            rec[name] = out
+    elif cfg == "c4":
+        from solidfem_gb300.batch import BatchedBodies, c4_specs
+
+        b = BatchedBodies(c4_specs(64, seed=0), precision="fp32")
+        times = []
+        for _ in range(3):
+            b.phys.set_positions(b.nodes)
+            st = b.solve(rel_tol=1e-8, max_newton=200)
+            times.append(st["seconds"])
+        rec.update(workload=f"64 bodies n x n/4 x n/4, n log-uniform [8,64] (seed 0), {b.phys.n_tets} tets, "
+                            "FP32-refined Newton, every body to 1e-8",
+                   gpu={"s": float(np.median(times[1:])), "newton_iters": st["newton_iters"],
+                        "cg_iters": st["cg_iters"], "status": st["status"],
+                        "max_body_rel_res": float(st["instance_rel_res"].max())})
+        o = Oracle(b.nodes, b.tets, b.fixed, 1e5, 0.4, 1070.0, (0.0, 0.0, -9.81), 3)
+        counts = {"newton_iters": st["newton_iters"], "cg_iters": st["cg_iters"],
+                  "residual_evals": st["newton_iters"] + st["line_search_cuts"] + 1}
+        est, sample = _cpu_window(o, counts)
+        rec["cpu_baseline"] = {"value": est, "kind": "port", "cores": cores, "cpu_model": cpu_model(),
+                               "sample": sample + " (FP64 per-operation cost on the union mesh, the GPU solve's "
+                                                  "counts)"}
+    elif cfg == "c5":
+        m = box_lattice(64, 16, 16, extent=(4.0, 1.0, 1.0))
+        fixed = m.face_nodes(0, 0)
+        young = 1e5 * np.exp(0.5 * np.random.default_rng(1).normal(size=m.n_tets))
+        f = lumped_face_load(m, 0, 1, (0.0, 0.0, -1000.0))
+        p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.45, density=1070.0,
+                                 gravity=(0.0, 0.0, 0.0), material=3)
+        p.set_element_youngs(young)
+        p.set_nodal_loads(f)
+        t_gpu, st = _gpu_newton(p, m.nodes, rel_tol=1e-11, max_newton=100)
+        dLdu = np.ones((p.n_free, 3))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(3):
+            p.adjoint(dLdu, rel_tol=1e-12)
+        t_adj = (time.perf_counter() - t) / 3
+        o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.45, 1070.0, (0.0, 0.0, 0.0), 3)
+        o.set_element_scale(young / 1e5)
+        o.set_nodal_loads(f)
+        counts = {"newton_iters": st["newton_iters"], "cg_iters": st["cg_iters"],
+                  "residual_evals": st["newton_iters"] + st["line_search_cuts"] + 1}
+        est, sample = _cpu_window(o, counts)
+        o.set_free_positions(p.get_free_positions().ravel())
+        t = time.perf_counter()
+        _, _, its = o.adjoint(dLdu.ravel(), young, tol=1e-12, max_cg=200000)
+        t_adj_cpu = time.perf_counter() - t
+        rec.update(workload="64x16x16 x 6 tets (18,785 nodes / 98,304 tets), neo-Hookean nu=0.45, per-element E "
+                            "log-normal (median 1e5, sigma 0.5), 1 kPa tip traction; FP64 Newton to 1e-11, adjoint "
+                            "to 1e-12",
+                   gpu={"newton_s": t_gpu, "newton_iters": st["newton_iters"], "cg_iters": st["cg_iters"],
+                        "adjoint_s": t_adj},
+                   cpu_baseline={"value": est + t_adj_cpu, "kind": "port", "cores": cores, "cpu_model": cpu_model(),
+                                 "newton_s": est, "adjoint_s": t_adj_cpu,
+                                 "sample": sample + f"; the adjoint solve measured in full ({its} PCG iterations)"})
+    print(json.dumps(rec), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default=None, choices=["c1", "c2", "c4", "c5"],
+                    help="time one of the other configurations (GPU beside the oracle CPU port) instead")
     ap.add_argument("--small", action="store_true", help="64x16x16 variant (quick check; not a bench line)")
     ap.add_argument("--dims", default=None, help="override the lattice, e.g. 128,64,64 (profiling; not a bench line)")
     ap.add_argument("--skip-fp64", action="store_true")
@@ -533,7 +680,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and not args.small:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.config:
+        run_config(args)
+    elif args.impl == "reference":
         run_reference_arm(args)
     else:
         run_gpu_arm(args)

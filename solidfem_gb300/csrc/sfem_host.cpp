@@ -158,7 +158,7 @@ struct sfem_handle {
   int64_t *elem_off = nullptr, *node_off = nullptr;
   int32_t *pnode = nullptr, *pdest = nullptr, *bnode = nullptr, *bptr = nullptr, *bidx = nullptr;
   int2* bslot = nullptr;  // per node: (first partial slot, count) of a shared node, (0, 0) otherwise
-  uint16_t *lptr = nullptr, *lent = nullptr;
+  uint16_t *lptr = nullptr, *lent = nullptr, *lent12 = nullptr;
   ushort4* lidx = nullptr;
   double* partial = nullptr;  // 3 * n_slots values (float passes use it as floats)
   double* etmp = nullptr;     // E scratch doubles
@@ -200,7 +200,7 @@ struct sfem_handle {
     if (nhc_on) nhc = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)nhc64 : (const void*)nhc32);
     const T* rec = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)rec64 : (const void*)rec32);
     return PatchView<T>{elem_off, node_off, pnode, pdest, lptr, lent, lidx, X, vol, scale, scale_la, E, n_patches,
-                        nbc, m, l, pm, nhc, max_pnodes, rec};
+                        nbc, m, l, pm, nhc, max_pnodes, rec, sizeof(T) == 4 ? lent12 : nullptr};
   }
   NodeCsr csr() const { return NodeCsr{csr_ptr, csr_ent}; }
   ElemView<double> ev64() const {
@@ -798,7 +798,7 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
       (st = dalloc(&h->elem_off, (size_t)h->n_patches + 1)) || (st = dalloc(&h->node_off, (size_t)h->n_patches + 1)) ||
       (st = dalloc(&h->pnode, (size_t)h->n_slots)) || (st = dalloc(&h->pdest, (size_t)h->n_slots)) ||
       (st = dalloc(&h->lptr, (size_t)(h->n_slots + h->n_patches))) ||
-      (st = dalloc(&h->lent, 4 * E)) || (st = dalloc(&h->lidx, E)) || (st = dalloc(&h->partial, 3 * (size_t)h->n_slots)) ||
+      (st = dalloc(&h->lent, 4 * E)) || (st = dalloc(&h->lent12, 4 * E)) || (st = dalloc(&h->lidx, E)) || (st = dalloc(&h->partial, 3 * (size_t)h->n_slots)) ||
       (st = dalloc(&h->bnode, (size_t)h->n_shared)) || (st = dalloc(&h->bptr, (size_t)h->n_shared + 1)) ||
       (st = dalloc(&h->bidx, (size_t)n_nodes)) || (st = dalloc(&h->dmap, (size_t)n_nodes)) ||
       (st = dalloc(&h->bslot, (size_t)n_nodes)) ||
@@ -849,6 +849,12 @@ int sfem_create(const double* nodes, int64_t n_nodes, const int32_t* tets_in, in
   UP(h->pnode, pbld.pnode.data(), pbld.pnode.size() * sizeof(int32_t));
   UP(h->lptr, pbld.lptr.data(), pbld.lptr.size() * sizeof(uint16_t));
   UP(h->lent, pbld.lent.data(), pbld.lent.size() * sizeof(uint16_t));
+  {  // the same entries for 12-value result rows (kFeStride i + 3 j -> 12 i + 3 j)
+    std::vector<uint16_t> l12(pbld.lent.size());
+    for (size_t t = 0; t < l12.size(); t++) l12[t] = (uint16_t)(pbld.lent[t] - pbld.lent[t] / kFeStride);
+    UP(h->lent12, l12.data(), l12.size() * sizeof(uint16_t));
+    TRY(sync(h));
+  }
   UP(h->lidx, pbld.lidx.data(), pbld.lidx.size() * sizeof(ushort4));
   UP(h->pdest, pbld.pdest.data(), pbld.pdest.size() * sizeof(int32_t));
   if (h->n_shared > 0) UP(h->bnode, pbld.bnode.data(), pbld.bnode.size() * sizeof(int32_t));
@@ -886,7 +892,7 @@ int sfem_destroy(sfem_handle* h) {
                    h->sell_col16, h->sell_vals64, h->sell_ke64};
   for (void* b : ibufs)
     if (b) cudaFree(b);
-  void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lidx,
+  void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lent12, h->lidx,
                    h->partial, h->bnode, h->bptr, h->bidx, h->dmap, h->bslot};
   for (void* b : pbufs)
     if (b) cudaFree(b);

@@ -92,6 +92,8 @@ struct PatchView {
   const T* nhc;  // neo-Hookean tangent cache (k_nh_cache, 12 E values) valid for this solve, or nullptr
   int max_nodes;  // the largest node count of a patch (sizes the shared-memory node arrays)
   const T* rec;   // per element 12 values: X (9), vol, the local corners' 8 bytes, padding (16-byte rows)
+  const uint16_t* lent12;  // the local CSR entries as offsets 12 * local element + 3 * corner (FP32 neo-Hookean
+                           // product, results over the 12-value records), or nullptr
 };
 
 // Implicit-dynamics terms of the residual (FemPhysicsMatrixFree::ComputeGradients :546-557):
@@ -125,6 +127,12 @@ constexpr int kMaxBlocks = 2048;
 template <typename T, int MAT>
 void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* fe, Reduce red,
                     double* result, int* n_inverted, const CgScalars* s, cudaStream_t st);
+
+// FP32 neo-Hookean patch product with the records staged by a bulk asynchronous copy (sfem_patch_nh32.cu)
+size_t patch_hvp_nh32_smem(int max_nodes);
+void launch_patch_hvp_nh32(const PatchView<float>& pv, const float* u, const float* p, float* q, float* partial,
+                           Reduce red, CgScalars* s, cudaStream_t st, const float* r, const float* dinv, float* p_new,
+                           const float* z);
 
 constexpr int kPatchElems = 768;
 constexpr int kPatchNodes = 512;

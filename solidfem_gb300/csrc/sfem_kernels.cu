@@ -2207,6 +2207,16 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
     }
     attr_set = true;
   }
+  if constexpr (std::is_same<T, float>::value && kNH) {
+    if (!cached && pv.lent12 != nullptr) {  // the FP32 neo-Hookean product (sfem_patch_nh32.cu)
+      launch_patch_hvp_nh32(pv, u, p, q, partial, red, s, st, r, dinv, p_new, z);
+      if (mid) cudaEventRecord(mid, st);
+      if (p_new != nullptr) return;  // Krylov iteration: the fused update completes the shared nodes
+      count_launch();
+      k_patch_boundary<T><<<grid_for(pb.n), kThreads, 0, st>>>(pb, partial, q, s);
+      return;
+    }
+  }
   const unsigned grid = (unsigned)pv.n_patches;
   count_launch();
   if (p_new != nullptr) {
