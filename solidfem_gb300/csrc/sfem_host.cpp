@@ -133,6 +133,16 @@ struct sfem_handle {
   int64_t *sell_base = nullptr, *sell_cptr = nullptr;
   int32_t *sell_col = nullptr, *sell_dslot = nullptr;
   int16_t* sell_col16 = nullptr;  // the columns as differences to the row, when all fit (else sell_col)
+  // symmetric tangents: only the diagonal and upper blocks are stored (the slots above); each row's
+  // lower blocks are read transposed from their mirror rows: per slice of 32 rows, lower entry
+  // (row r, position k) at lbase[r / 32] + 32 k + r % 32 holds the column j (difference j - r, or j)
+  // and the position of block (j, r) among row j's stored blocks (0xff: padding)
+  bool sell_sym = false;
+  int64_t sell_nlow = 0;
+  int64_t* sell_lbase = nullptr;
+  int16_t* sell_lcol16 = nullptr;
+  int32_t* sell_lcol = nullptr;
+  uint8_t* sell_lpos = nullptr;
   uint32_t* sell_code = nullptr;
   float *sell_vals32 = nullptr, *sell_ke32 = nullptr;
   double *sell_vals64 = nullptr, *sell_ke64 = nullptr;
@@ -312,8 +322,12 @@ void krylov_hvp(sfem_handle* h, const T* u, const T* p, T* q, cudaEvent_t mid, c
       vals = h->sell_vals32;
     else
       vals = h->sell_vals64;
-    launch_sell_hvp<T>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, vals, p, q, h->red(), h->scal,
-                       h->stream, r, dinv, p_new, z);
+    if (h->sell_sym)
+      launch_ssell_hvp<T>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, h->sell_lbase, h->sell_lcol,
+                          h->sell_lcol16, h->sell_lpos, vals, p, q, h->red(), h->scal, h->stream, r, dinv, p_new, z);
+    else
+      launch_sell_hvp<T>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, vals, p, q, h->red(), h->scal,
+                         h->stream, r, dinv, p_new, z);
     if (mid) cudaEventRecord(mid, h->stream);
     return;
   }
@@ -889,7 +903,8 @@ int sfem_destroy(sfem_handle* h) {
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
                    h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32, h->sell_ke32,
-                   h->sell_col16, h->sell_vals64, h->sell_ke64};
+                   h->sell_col16, h->sell_vals64, h->sell_ke64, h->sell_lbase, h->sell_lcol16, h->sell_lcol,
+                   h->sell_lpos};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lent12, h->lidx,
@@ -936,7 +951,8 @@ int sfem_get_profile(const sfem_handle* h, sfem_profile* out) {
   const double sz = h->prof_precision == SFEM_FP32 ? 4.0 : 8.0;
   if (h->prof_op == 1)  // assembled tangent: blocks and their column indices, and per free node the
                         // direction inputs (z or r, p_old) and outputs (p, q)
-    out->algo_bytes_hvp = (double)h->sell_nnzb * (9.0 * sz + (h->sell_col16 ? 2.0 : 4.0)) + (double)h->nf * 12.0 * sz;
+    out->algo_bytes_hvp = (double)h->sell_nnzb * (9.0 * sz + (h->sell_col16 ? 2.0 : 4.0)) +
+                          (double)h->sell_nlow * ((h->sell_col16 ? 2.0 : 4.0) + 1.0) + (double)h->nf * 12.0 * sz;
   else
     out->algo_bytes_hvp = (double)h->E * (16.0 + 10.0 * sz) + (double)h->N * 9.0 * sz;
   out->precision = h->prof_precision;
@@ -1088,9 +1104,16 @@ static int sell_alloc(sfem_handle* h, T** p, size_t count) {
 // free every buffer of the assembled operator (also the ones a failed build left behind)
 static void sell_release(sfem_handle* h) {
   void* bufs[] = {h->sell_base, h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32,
-                  h->sell_ke32, h->sell_col16, h->sell_vals64, h->sell_ke64};
+                  h->sell_ke32, h->sell_col16, h->sell_vals64, h->sell_ke64, h->sell_lbase, h->sell_lcol16,
+                  h->sell_lcol, h->sell_lpos};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  h->sell_lbase = nullptr;
+  h->sell_lcol16 = nullptr;
+  h->sell_lcol = nullptr;
+  h->sell_lpos = nullptr;
+  h->sell_sym = false;
+  h->sell_nlow = 0;
   h->sell_base = h->sell_cptr = nullptr;
   h->sell_col = h->sell_dslot = nullptr;
   h->sell_code = nullptr;
@@ -1104,6 +1127,9 @@ static void sell_release(sfem_handle* h) {
 
 static int sell_structure(sfem_handle* h) {
   if (h->sell_T >= 0) return 0;
+  // the symmetric tangents (linear, StVK, neo-Hookean) store the diagonal and upper blocks only
+  const int mat = mat_id(h);
+  bool sym = mat == 0 || mat == 1 || mat == 3;
   const int64_t E = h->E, N = h->N, nbc = h->nbc, nf = h->nf, ns = (nf + 31) / 32;
   if (E >= (int64_t(1) << 28)) return fail(SFEM_ERR_INVALID, "too many elements for the assembled operator");
   std::vector<int4> tt((size_t)E);
@@ -1124,6 +1150,11 @@ static int sell_structure(sfem_handle* h) {
     std::sort(cols.begin(), cols.end());
     cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
   };
+  // the blocks a row stores: all of its columns, or (symmetric) those >= the row, the diagonal first
+  auto stored = [&](int64_t r, std::vector<int32_t>& cols) {
+    columns(r, cols);
+    if (sym) cols.erase(cols.begin(), std::lower_bound(cols.begin(), cols.end(), (int32_t)r));
+  };
   std::vector<int32_t> len((size_t)nf);
   parallel_rows(nf, [&](int64_t a, int64_t b) {
     std::vector<int32_t> cols;
@@ -1132,6 +1163,16 @@ static int sell_structure(sfem_handle* h) {
       len[r] = (int32_t)cols.size();
     }
   });
+  // a lower entry names its mirror's position in one byte: rows of at most 255 columns
+  if (sym && nf > 0 && *std::max_element(len.begin(), len.end()) > 255) sym = false;
+  if (sym)
+    parallel_rows(nf, [&](int64_t a, int64_t b) {
+      std::vector<int32_t> cols;
+      for (int64_t r = a; r < b; r++) {
+        stored(r, cols);
+        len[r] = (int32_t)cols.size();
+      }
+    });
   std::vector<int64_t> base((size_t)ns + 1, 0);
   int64_t nnzb = 0;
   for (int64_t sl = 0; sl < ns; sl++) {
@@ -1154,7 +1195,7 @@ static int sell_structure(sfem_handle* h) {
       const int a = (int)(ent & 3);
       const int32_t v[4] = {tt[e].x, tt[e].y, tt[e].z, tt[e].w};
       for (int b = 0; b < 4; b++) {
-        if (v[b] < nbc) continue;
+        if (v[b] < nbc || (sym && v[b] - nbc < r)) continue;  // fixed node, or a block stored by its mirror
         const int64_t pos = std::lower_bound(cols.begin(), cols.end(), v[b] - (int32_t)nbc) - cols.begin();
         emit(base[sl] + 32 * pos + l, (uint32_t)(16 * e + 4 * a + b));
       }
@@ -1163,7 +1204,7 @@ static int sell_structure(sfem_handle* h) {
   parallel_rows(nf, [&](int64_t a, int64_t b) {
     std::vector<int32_t> cols;
     for (int64_t r = a; r < b; r++) {
-      columns(r, cols);
+      stored(r, cols);
       const int64_t sl = r / 32, l = r % 32, w = (base[sl + 1] - base[sl]) / 32;
       for (int64_t k = 0; k < w; k++) {
         const int64_t t = base[sl] + 32 * k + l;
@@ -1179,7 +1220,7 @@ static int sell_structure(sfem_handle* h) {
     std::vector<int32_t> cols;
     std::vector<int64_t> fill;
     for (int64_t r = a; r < b; r++) {
-      columns(r, cols);
+      stored(r, cols);
       for_contrib(r, cols, [&](int64_t t, uint32_t c) {
         // slots of one row are visited only by this thread: cnt[t] advances as the slot's cursor
         code[cnt[t]++] = c;
@@ -1189,8 +1230,66 @@ static int sell_structure(sfem_handle* h) {
   // the fill advanced cnt[t] to the end of slot t's list: shift back to start offsets
   for (int64_t t = T; t > 0; t--) cnt[t] = cnt[t - 1];
   cnt[0] = 0;
+  // symmetric: the lower entries, each naming its mirror block (j, r) by j and its position in row j
+  std::vector<int64_t> lbase((size_t)ns + 1, 0);
+  std::vector<int32_t> lcol;
+  std::vector<uint8_t> lpos;
+  int64_t nlow = 0;
+  if (sym) {
+    std::vector<int32_t> llen((size_t)nf);
+    parallel_rows(nf, [&](int64_t a, int64_t b) {
+      std::vector<int32_t> cols;
+      for (int64_t r = a; r < b; r++) {
+        columns(r, cols);
+        llen[r] = (int32_t)(std::lower_bound(cols.begin(), cols.end(), (int32_t)r) - cols.begin());
+      }
+    });
+    for (int64_t sl = 0; sl < ns; sl++) {
+      int64_t w = 0;
+      for (int64_t r = 32 * sl; r < std::min(nf, 32 * sl + 32); r++) {
+        w = std::max<int64_t>(w, llen[r]);
+        nlow += llen[r];
+      }
+      lbase[sl + 1] = lbase[sl] + 32 * w;
+    }
+    const int64_t L = lbase[ns];
+    lcol.assign((size_t)L, 0);
+    lpos.assign((size_t)L, 0xff);
+    parallel_rows(nf, [&](int64_t a, int64_t b) {
+      std::vector<int32_t> cols;
+      for (int64_t r = a; r < b; r++) {
+        columns(r, cols);
+        const int64_t sl = r / 32, l = r % 32, w = (lbase[sl + 1] - lbase[sl]) / 32;
+        for (int64_t k = 0; k < w; k++) {
+          const int64_t t = lbase[sl] + 32 * k + l;
+          if (k < llen[r]) {
+            const int32_t jc = cols[k];
+            // row jc's stored columns ascend over its first len[jc] positions
+            const int64_t js = jc / 32, jl = jc % 32;
+            int lo = 0, hi = len[jc];
+            while (lo < hi) {
+              const int mid = (lo + hi) / 2;
+              if (scol[base[js] + 32 * mid + jl] < (int32_t)r) lo = mid + 1; else hi = mid;
+            }
+            lcol[t] = jc;
+            lpos[t] = (uint8_t)lo;
+          } else {
+            lcol[t] = (int32_t)r;  // padding (lpos 0xff): skipped
+          }
+        }
+      }
+    });
+  }
   // 16-bit column differences (2 instead of 4 bytes per block) when every |column - row| fits
   bool fits16 = true;
+  for (int64_t r = 0; r < nf && fits16 && sym; r++) {
+    const int64_t sl = r / 32, l = r % 32, w = (lbase[sl + 1] - lbase[sl]) / 32;
+    for (int64_t k = 0; k < w; k++)
+      if ((int64_t)lcol[lbase[sl] + 32 * k + l] - r < -32768) {
+        fits16 = false;
+        break;
+      }
+  }
   for (int64_t r = 0; r < nf && fits16; r++) {
     const int64_t sl = r / 32, l = r % 32, w = (base[sl + 1] - base[sl]) / 32;
     for (int64_t k = 0; k < w; k++) {
@@ -1228,9 +1327,35 @@ static int sell_structure(sfem_handle* h) {
     CU(cudaMemcpyAsync(h->sell_code, code.data(), code.size() * 4, cudaMemcpyHostToDevice, h->stream));
   if (nf > 0) CU(cudaMemcpyAsync(h->sell_dslot, dslot.data(), dslot.size() * 4, cudaMemcpyHostToDevice, h->stream));
 
+  if (sym) {
+    const int64_t L = lbase[ns];
+    TRY(sell_alloc(h, &h->sell_lbase, lbase.size()));
+    TRY(sell_alloc(h, &h->sell_lpos, std::max<size_t>(lpos.size(), 1)));
+    CU(cudaMemcpyAsync(h->sell_lbase, lbase.data(), lbase.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       h->stream));
+    if (L > 0) CU(cudaMemcpyAsync(h->sell_lpos, lpos.data(), lpos.size(), cudaMemcpyHostToDevice, h->stream));
+    if (fits16) {
+      std::vector<int16_t> d16((size_t)L, 0);
+      for (int64_t r = 0; r < nf; r++) {
+        const int64_t sl = r / 32, l = r % 32, w = (lbase[sl + 1] - lbase[sl]) / 32;
+        for (int64_t k = 0; k < w; k++) {
+          const int64_t t = lbase[sl] + 32 * k + l;
+          d16[t] = (int16_t)((int64_t)lcol[t] - r);
+        }
+      }
+      TRY(sell_alloc(h, &h->sell_lcol16, std::max<size_t>(d16.size(), 1)));
+      if (L > 0) CU(cudaMemcpyAsync(h->sell_lcol16, d16.data(), d16.size() * 2, cudaMemcpyHostToDevice, h->stream));
+      TRY(sync(h));
+    } else {
+      TRY(sell_alloc(h, &h->sell_lcol, std::max<size_t>(lcol.size(), 1)));
+      if (L > 0) CU(cudaMemcpyAsync(h->sell_lcol, lcol.data(), lcol.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    }
+  }
   TRY(sync(h));
   h->sell_T = T;
   h->sell_nnzb = nnzb;
+  h->sell_sym = sym;
+  h->sell_nlow = nlow;
   return 0;
 }
 

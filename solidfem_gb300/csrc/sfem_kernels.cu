@@ -1314,6 +1314,172 @@ template void launch_sell_hvp<double>(int64_t, int64_t, const int64_t*, const in
                                       const double*, double*, Reduce, CgScalars*, cudaStream_t, const double*,
                                       const double*, double*, const double*);
 
+// q = K p from the symmetric tangent's diagonal and upper blocks, one thread per row (a warp per slice).
+// The row's lower blocks K_rj = K_jr^T are read from their mirror slots in row j (lower entries in
+// column order, then the stored blocks: the order of the full row), so each stored block streams
+// from HBM once and its mirror read, by a row up to the mesh's bandwidth away processed at about the
+// same time, hits L2.  DIR and the p.q / alpha finish as in k_sell_hvp.
+template <typename T, bool DIR, typename CI>
+__global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
+                                                        const CI* __restrict__ col, const int64_t* __restrict__ lbase,
+                                                        const CI* __restrict__ lcol, const uint8_t* __restrict__ lpos,
+                                                        const T* __restrict__ vals, const T* __restrict__ p,
+                                                        T* __restrict__ q, Reduce red, CgScalars* s,
+                                                        const T* __restrict__ r, const T* __restrict__ dinv,
+                                                        T* __restrict__ p_new, const T* __restrict__ z) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (s != nullptr && s->done) return;
+  T beta = T(0);
+  bool use_z = false;
+  if (DIR) {
+    beta = (T)s->beta;
+    use_z = z != nullptr && s->jac == 0;
+  }
+  T acc = T(0);
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nf; row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sl = row >> 5;
+    const int lane = (int)(row & 31);
+    const int64_t cbase = sizeof(CI) == 2 ? row : 0;
+    auto xdir = [&](int64_t jf, T& x0, T& x1, T& x2) {
+      const int64_t j = 3 * (nbc + jf);
+      if (DIR) {
+        x0 = (use_z ? z[j] : dinv[j] * r[j]) + beta * p[j];
+        x1 = (use_z ? z[j + 1] : dinv[j + 1] * r[j + 1]) + beta * p[j + 1];
+        x2 = (use_z ? z[j + 2] : dinv[j + 2] * r[j + 2]) + beta * p[j + 2];
+      } else {
+        x0 = p[j];
+        x1 = p[j + 1];
+        x2 = p[j + 2];
+      }
+    };
+    T y0 = T(0), y1 = T(0), y2 = T(0);
+    // lower blocks, transposed from the mirror rows
+    {
+      const int64_t lb0 = lbase[sl];
+      const int wl = (int)((lbase[sl + 1] - lb0) >> 5);
+      const CI* lc = lcol + lb0 + lane;
+      const uint8_t* lp = lpos + lb0 + lane;
+      for (int k = 0; k < wl; k++) {
+        const int kp = lp[32 * k];
+        if (kp == 0xff) break;  // padding follows the row's last lower block
+        const int64_t j = cbase + lc[32 * k];
+        const int64_t jl = j & 31;
+        const T* V = vals + 9 * (base[j >> 5] + 32 * kp) + jl;
+        T v[9];
+#pragma unroll
+        for (int qq = 0; qq < 9; qq++) v[qq] = V[32 * qq];
+        T x0, x1, x2;
+        xdir(j, x0, x1, x2);
+        y0 += v[0] * x0 + v[3] * x1 + v[6] * x2;
+        y1 += v[1] * x0 + v[4] * x1 + v[7] * x2;
+        y2 += v[2] * x0 + v[5] * x1 + v[8] * x2;
+      }
+    }
+    // the diagonal and upper blocks of the row itself
+    const int64_t b0 = base[sl];
+    const int w = (int)((base[sl + 1] - b0) >> 5);
+    const CI* cl = col + b0 + lane;
+    const T* Vb = vals + 9 * b0 + lane;
+    int k = 0;
+    for (; k + 2 <= w; k += 2) {
+      const int64_t ja = cbase + cl[32 * k], jb = cbase + cl[32 * k + 32];
+      const T* Va = Vb + 288 * k;
+      const T* Wb = Va + 288;
+      T va[9], vb[9];
+#pragma unroll
+      for (int qq = 0; qq < 9; qq++) {
+        va[qq] = Va[32 * qq];
+        vb[qq] = Wb[32 * qq];
+      }
+      T xa0, xa1, xa2, xb0, xb1, xb2;
+      xdir(ja, xa0, xa1, xa2);
+      xdir(jb, xb0, xb1, xb2);
+      y0 += va[0] * xa0 + va[1] * xa1 + va[2] * xa2;
+      y1 += va[3] * xa0 + va[4] * xa1 + va[5] * xa2;
+      y2 += va[6] * xa0 + va[7] * xa1 + va[8] * xa2;
+      y0 += vb[0] * xb0 + vb[1] * xb1 + vb[2] * xb2;
+      y1 += vb[3] * xb0 + vb[4] * xb1 + vb[5] * xb2;
+      y2 += vb[6] * xb0 + vb[7] * xb1 + vb[8] * xb2;
+    }
+    if (k < w) {
+      const T* Va = Vb + 288 * k;
+      T x0, x1, x2;
+      xdir(cbase + cl[32 * k], x0, x1, x2);
+      y0 += Va[0] * x0 + Va[32] * x1 + Va[64] * x2;
+      y1 += Va[96] * x0 + Va[128] * x1 + Va[160] * x2;
+      y2 += Va[192] * x0 + Va[224] * x1 + Va[256] * x2;
+    }
+    const int64_t o = 3 * (nbc + row);
+    T p0, p1, p2;
+    if (DIR) {
+      p0 = (use_z ? z[o] : dinv[o] * r[o]) + beta * p[o];
+      p1 = (use_z ? z[o + 1] : dinv[o + 1] * r[o + 1]) + beta * p[o + 1];
+      p2 = (use_z ? z[o + 2] : dinv[o + 2] * r[o + 2]) + beta * p[o + 2];
+      p_new[o] = p0;
+      p_new[o + 1] = p1;
+      p_new[o + 2] = p2;
+    } else {
+      p0 = p[o];
+      p1 = p[o + 1];
+      p2 = p[o + 2];
+    }
+    q[o] = y0;
+    q[o + 1] = y1;
+    q[o + 2] = y2;
+    acc += p0 * y0 + p1 * y1 + p2 * y2;
+  }
+  if (s == nullptr) return;
+  T v[1] = {acc}, tot[1];
+  if (reduce_last<T, 1>(v, red, tot) && threadIdx.x == 0) {
+    const double pq = (double)tot[0];
+    s->pq = pq;
+    if (!isfinite(pq)) {
+      s->done = 1;
+      s->status = -3;
+      s->alpha = 0.0;
+    } else if (!(pq > 0.0)) {
+      s->done = 1;
+      s->status = 2;
+      s->alpha = 0.0;
+    } else {
+      s->alpha = s->rz / pq;
+    }
+  }
+}
+template <typename T>
+void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const int16_t* col16,
+                      const int64_t* lbase, const int32_t* lcol, const int16_t* lcol16, const uint8_t* lpos,
+                      const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st, const T* r,
+                      const T* dinv, T* p_new, const T* z) {
+  static const int wave = std::min(std::min(resident_ctas(k_ssell_hvp<T, true, int32_t>, kThreads, 0),
+                                            resident_ctas(k_ssell_hvp<T, false, int32_t>, kThreads, 0)),
+                                   std::min(resident_ctas(k_ssell_hvp<T, true, int16_t>, kThreads, 0),
+                                            resident_ctas(k_ssell_hvp<T, false, int16_t>, kThreads, 0)));
+  const int grid = std::max(1, std::min(wave, (int)((nf + kThreads - 1) / kThreads)));
+  count_launch();
+  if (col16 && p_new != nullptr)
+    launch_pdl(k_ssell_hvp<T, true, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, lbase, lcol16, lpos, vals,
+               p, q, red, s, r, dinv, p_new, z);
+  else if (col16)
+    launch_pdl(k_ssell_hvp<T, false, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, lbase, lcol16, lpos,
+               vals, p, q, red, s, nullptr, nullptr, nullptr, nullptr);
+  else if (p_new != nullptr)
+    launch_pdl(k_ssell_hvp<T, true, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, lbase, lcol, lpos, vals, p,
+               q, red, s, r, dinv, p_new, z);
+  else
+    launch_pdl(k_ssell_hvp<T, false, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, lbase, lcol, lpos, vals,
+               p, q, red, s, nullptr, nullptr, nullptr, nullptr);
+}
+template void launch_ssell_hvp<float>(int64_t, int64_t, const int64_t*, const int32_t*, const int16_t*,
+                                      const int64_t*, const int32_t*, const int16_t*, const uint8_t*, const float*,
+                                      const float*, float*, Reduce, CgScalars*, cudaStream_t, const float*,
+                                      const float*, float*, const float*);
+template void launch_ssell_hvp<double>(int64_t, int64_t, const int64_t*, const int32_t*, const int16_t*,
+                                       const int64_t*, const int32_t*, const int16_t*, const uint8_t*, const double*,
+                                       const double*, double*, Reduce, CgScalars*, cudaStream_t, const double*,
+                                       const double*, double*, const double*);
+
 // y = A x for a block-CSR matrix with 3 x 3 blocks (one thread per block row)
 __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int64_t nrows, const int32_t* __restrict__ rowptr,
                                                        const int32_t* __restrict__ col,
