@@ -40,6 +40,7 @@ extern "C" {
 #define SFEM_ERR_OOM (-5)
 #define SFEM_ERR_BREAKDOWN (-6)         /* CG curvature p.Ap <= 0 */
 #define SFEM_ERR_NO_DEVICE (-7)
+#define SFEM_ERR_TIMEOUT (-8)           /* a bounded device-side wait gave up */
 
 /* ---- material models: values of MaterialModelType, Include/FemDataStructures.h:90-105 ---- */
 #define SFEM_MMT_LINEAR 0
@@ -187,6 +188,21 @@ int sfem_set_element_lame(sfem_handle* h, const double* mu_e, const double* lamb
 int sfem_set_instances(sfem_handle* h, int32_t k, const int64_t* node_offsets);
 /* per-body |r_q| / |r_q(x_0)| and Newton iterations of the last sfem_newton_solve */
 int sfem_instance_stats(const sfem_handle* h, double* rel_res, int32_t* newton_iters);
+/* Krylov solves of a handle with instances (materials 0, 1, 3): mode 1 (default) runs every
+ * instance's own PCG recurrence -- its own alpha, beta, r.z and stop test rr <= tol^2 bb, as
+ * SolveConjugateGradientMF (Math/IterativeSolvers.h:115-195) runs per body -- in one persistent
+ * cooperative kernel per solve (element products, node gather, updates and directions between grid
+ * barriers whose waits are bounded); mode 0 runs one recurrence over all instances (converged
+ * instances masked between Newton steps). */
+int sfem_set_batched_pcg(sfem_handle* h, int32_t mode);
+/* Per instance, of the last batched PCG solve: iterations, status (1 converged, 2 non-positive
+ * curvature, 3 iteration cap) and |r| / |b|. */
+int sfem_instance_pcg_stats(const sfem_handle* h, int32_t* iters, int32_t* status, double* rel_res);
+/* Bound of the device-side waits (grid barriers) of the persistent kernels: `limit` polls of at
+ * least 64 ns each (default 2e7), after which the kernel stops and the call returns
+ * SFEM_ERR_TIMEOUT; test != 0 makes the next launches first wait for a flag that nothing sets, so
+ * that the limit is reached (a self-test of the error path that faults nothing). */
+int sfem_set_device_wait(sfem_handle* h, int64_t limit, int32_t test);
 /* Extension (FemPhysicsBase::SetExternalForces is an ASSERT stub, Include/FemPhysicsBase.h:68):
  * dead nodal loads, N x 3 original order, added to the residual scaled by mForceFraction. */
 int sfem_set_nodal_loads(sfem_handle* h, const double* f);

@@ -21,6 +21,7 @@ SFEM_ERR_INVERTED = -4
 SFEM_ERR_OOM = -5
 SFEM_ERR_BREAKDOWN = -6
 SFEM_ERR_NO_DEVICE = -7
+SFEM_ERR_TIMEOUT = -8
 
 MMT_LINEAR, MMT_STVK, MMT_COROTATIONAL, MMT_NEO_HOOKEAN = 0, 1, 2, 3
 # the other MaterialModelType values (FemDataStructures.h:93-107; FP64 handles)
@@ -130,6 +131,9 @@ SIGNATURES = {
     "sfem_gnn_set_inference": [_vp, C.c_int32],
     "sfem_set_operator": [_vp, C.c_int32],
     "sfem_set_operator_memory_limit": [_vp, C.c_int64],
+    "sfem_set_batched_pcg": [_vp, C.c_int32],
+    "sfem_instance_pcg_stats": [_vp, _ip, _ip, _dp],
+    "sfem_set_device_wait": [_vp, C.c_int64, C.c_int32],
     "sfem_set_newton_trace": [_vp, _dp, C.c_int32, _ip],
     "sfem_operator_info": [_vp, _i64p, _ip],
     "sfem_gnn_graph_form": [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],

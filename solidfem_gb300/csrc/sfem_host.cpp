@@ -111,6 +111,19 @@ struct sfem_handle {
   double* inst_norm = nullptr;
   std::vector<double> inst_r0, inst_rel;
   std::vector<int32_t> inst_its;
+  // instances' own PCG recurrences in one persistent launch (launch_batched_pcg): element instance,
+  // node tiles of at most 32 free nodes within one instance, per-tile partials and per-instance scalars
+  int bt_mode = 1;  // 1: per-instance persistent PCG (materials 0, 1, 3); 0: one recurrence over all
+  int bt_ntiles = 0;
+  int32_t *bt_einst = nullptr, *bt_tile_node = nullptr, *bt_tile_cnt = nullptr, *bt_tile_inst = nullptr,
+          *bt_inst_tile = nullptr;
+  double *bt_part = nullptr, *bt_rz = nullptr, *bt_tol2bb = nullptr, *bt_rr = nullptr;
+  int32_t *bt_done = nullptr, *bt_iters = nullptr, *bt_err = nullptr;
+  unsigned* bt_bar = nullptr;
+  long long bt_wait_limit = 20000000;  // polls of 64 ns or more: about a second at least
+  int bt_wait_test = 0;
+  std::vector<int32_t> bt_iters_h, bt_status_h;
+  std::vector<double> bt_rr_h, bt_bb_h;
   // node data (reshuffled, 3N)
   double *x0 = nullptr, *u = nullptr, *mass = nullptr, *fext = nullptr, *grav_d = nullptr;
   // dynamics (FemPhysicsMatrixFree mTimeStep, node vel, pos0 at the step start)
@@ -651,6 +664,10 @@ int upload_nodes(sfem_handle* h, const double* src, double* dst) {
   return sync(h);
 }
 
+void batch_release(sfem_handle* h);
+template <typename T>
+int batched_pcg(sfem_handle* h, const T* u, const T* rhs, KrylovWs<T>& w, const T* dinv, double tol, int max_it,
+                int* its);
 }  // namespace
 
 // =============================================================================
@@ -899,6 +916,7 @@ int sfem_destroy(sfem_handle* h) {
   if (!h) return SFEM_OK;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  batch_release(h);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
@@ -1806,7 +1824,77 @@ int sfem_set_instances(sfem_handle* h, int32_t k, const int64_t* node_offsets) {
   h->n_inst = k;
   h->inst_rel.assign(k, 1.0);
   h->inst_its.assign(k, 0);
+  // the persistent per-instance PCG: each element's instance (from its first corner), free-node tiles
+  TRY(sync(h));
+  batch_release(h);
+  {
+    std::vector<int32_t> inst_of((size_t)h->N, 0);  // reshuffled node -> instance
+    for (int q = 0; q < k; q++)
+      for (int64_t i = node_offsets[q]; i < node_offsets[q + 1]; i++) inst_of[h->map[i]] = q;
+    std::vector<int4> tt((size_t)h->E);
+    CU(cudaMemcpyAsync(tt.data(), h->tets, tt.size() * sizeof(int4), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    std::vector<int32_t> einst((size_t)h->E);
+    for (int64_t e = 0; e < h->E; e++) einst[e] = inst_of[tt[e].x];
+    std::vector<int32_t> tnode, tcnt, tinst, itile(k + 1, 0);
+    for (int q = 0; q < k; q++) {
+      const int64_t a = seg[q] / 3, b = seg[q + 1] / 3;
+      for (int64_t f = a; f < b; f += 32) {
+        tnode.push_back((int32_t)f);
+        tcnt.push_back((int32_t)std::min<int64_t>(32, b - f));
+        tinst.push_back(q);
+      }
+      itile[q + 1] = (int32_t)tnode.size();
+    }
+    const int nt = (int)tnode.size();
+    TRY(dalloc(&h->bt_einst, (size_t)h->E));
+    TRY(dalloc(&h->bt_tile_node, std::max(nt, 1)));
+    TRY(dalloc(&h->bt_tile_cnt, std::max(nt, 1)));
+    TRY(dalloc(&h->bt_tile_inst, std::max(nt, 1)));
+    TRY(dalloc(&h->bt_inst_tile, (size_t)k + 1));
+    TRY(dalloc(&h->bt_part, 3 * (size_t)std::max(nt, 1)));
+    TRY(dalloc(&h->bt_rz, 2 * (size_t)k));
+    TRY(dalloc(&h->bt_tol2bb, (size_t)k));
+    TRY(dalloc(&h->bt_rr, (size_t)k));
+    TRY(dalloc(&h->bt_done, 3 * (size_t)k));
+    TRY(dalloc(&h->bt_iters, (size_t)k));
+    TRY(dalloc(&h->bt_err, 1));
+    TRY(dalloc(&h->bt_bar, 4));
+    CU(cudaMemcpyAsync(h->bt_einst, einst.data(), einst.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    if (nt > 0) {
+      CU(cudaMemcpyAsync(h->bt_tile_node, tnode.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, h->stream));
+      CU(cudaMemcpyAsync(h->bt_tile_cnt, tcnt.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, h->stream));
+      CU(cudaMemcpyAsync(h->bt_tile_inst, tinst.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, h->stream));
+    }
+    CU(cudaMemcpyAsync(h->bt_inst_tile, itile.data(), itile.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    h->bt_ntiles = nt;
+  }
   return sync(h);
+}
+
+int sfem_set_batched_pcg(sfem_handle* h, int32_t mode) {
+  TRY(check_handle(h));
+  if (mode != 0 && mode != 1) return fail(SFEM_ERR_INVALID, "mode is 0 (one recurrence) or 1 (per instance)");
+  h->bt_mode = mode;
+  return SFEM_OK;
+}
+
+int sfem_set_device_wait(sfem_handle* h, int64_t limit, int32_t test) {
+  TRY(check_handle(h));
+  if (limit < 1) return fail(SFEM_ERR_INVALID, "the wait limit is a positive poll count");
+  h->bt_wait_limit = limit;
+  h->bt_wait_test = test ? 1 : 0;
+  return SFEM_OK;
+}
+
+int sfem_instance_pcg_stats(const sfem_handle* h, int32_t* iters, int32_t* status, double* rel_res) {
+  TRY(check_handle(h));
+  for (size_t q = 0; q < h->bt_iters_h.size(); q++) {
+    if (iters) iters[q] = h->bt_iters_h[q];
+    if (status) status[q] = h->bt_status_h[q];
+    if (rel_res) rel_res[q] = h->bt_bb_h[q] > 0 ? std::sqrt(h->bt_rr_h[q] / h->bt_bb_h[q]) : 0.0;
+  }
+  return SFEM_OK;
 }
 
 int sfem_instance_stats(const sfem_handle* h, double* rel_res, int32_t* newton_iters) {
@@ -1955,6 +2043,19 @@ int sfem_force_param_grads(sfem_handle* h, double* gmu, double* glambda, double*
   return SFEM_OK;
 }
 
+// stats of a batched solve: the largest instance iteration count, the largest instance relative
+// residual, status 1 if any instance reached the iteration cap
+static sfem_pcg_stats batched_stats(const sfem_handle* h, int its) {
+  sfem_pcg_stats s{};
+  s.iters = its;
+  for (size_t q = 0; q < h->bt_iters_h.size(); q++) {
+    const double rel = h->bt_bb_h[q] > 0 ? std::sqrt(h->bt_rr_h[q] / h->bt_bb_h[q]) : 0.0;
+    s.rel_res = std::max(s.rel_res, rel);
+    if (h->bt_status_h[q] == 3) s.status = 1;
+  }
+  return s;
+}
+
 int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* opts, sfem_pcg_stats* stats) {
   TRY(check_handle(h));
   TRY(set_device(h));
@@ -1969,8 +2070,13 @@ int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* op
     TRY(ops.st);
     CU(cudaMemcpyAsync(w.b + o, b, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (pc) TRY(jacobi<double>(h, w.dinv, nullptr));
-    st = pcg_device<double>(h, h->u, w.b, w.x, pc ? w.dinv : nullptr, opts->rel_tol, opts->max_iters,
-                            opts->check_every, stats);
+    int its = 0;
+    const int bst = batched_pcg<double>(h, h->u, w.b, w, pc ? w.dinv : w.ones, opts->rel_tol, opts->max_iters, &its);
+    if (bst < 0) return bst;
+    if (bst == 0 && stats) *stats = batched_stats(h, its);
+    if (bst != 0)
+      st = pcg_device<double>(h, h->u, w.b, w.x, pc ? w.dinv : nullptr, opts->rel_tol, opts->max_iters,
+                              opts->check_every, stats);
     if (st == SFEM_NEGATIVE_CURVATURE) return SFEM_ERR_BREAKDOWN;
     if (st < 0) return st;
     CU(cudaMemcpyAsync(x, w.x + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1982,8 +2088,13 @@ int sfem_pcg(sfem_handle* h, const double* b, double* x, const sfem_pcg_opts* op
     launch_convert<double, float>((int64_t)n, h->tmp64 + o, w.b + o, h->stream);
     const float* u32 = disp<float>(h);
     if (pc) TRY(jacobi<float>(h, w.dinv, nullptr));
-    st = pcg_device<float>(h, u32, w.b, w.x, pc ? w.dinv : nullptr, opts->rel_tol, opts->max_iters,
-                           opts->check_every, stats);
+    int its = 0;
+    const int bst = batched_pcg<float>(h, u32, w.b, w, pc ? w.dinv : w.ones, opts->rel_tol, opts->max_iters, &its);
+    if (bst < 0) return bst;
+    if (bst == 0 && stats) *stats = batched_stats(h, its);
+    if (bst != 0)
+      st = pcg_device<float>(h, u32, w.b, w.x, pc ? w.dinv : nullptr, opts->rel_tol, opts->max_iters,
+                             opts->check_every, stats);
     if (st == SFEM_NEGATIVE_CURVATURE) return SFEM_ERR_BREAKDOWN;
     if (st < 0) return st;
     launch_convert<float, double>((int64_t)n, w.x + o, h->tmp64 + o, h->stream);
@@ -2004,6 +2115,86 @@ namespace {
 
 // one inner solve K dx = r64 at the current state, in the handle's precision;
 // the step ends up in h->tmp64 (FP64, full length).
+void batch_release(sfem_handle* h) {
+  void* bufs[] = {h->bt_einst, h->bt_tile_node, h->bt_tile_cnt, h->bt_tile_inst, h->bt_inst_tile, h->bt_part,
+                  h->bt_rz, h->bt_tol2bb, h->bt_rr, h->bt_done, h->bt_iters, h->bt_err, h->bt_bar};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  h->bt_einst = h->bt_tile_node = h->bt_tile_cnt = h->bt_tile_inst = h->bt_inst_tile = nullptr;
+  h->bt_part = h->bt_rz = h->bt_tol2bb = h->bt_rr = nullptr;
+  h->bt_done = h->bt_iters = h->bt_err = nullptr;
+  h->bt_bar = nullptr;
+  h->bt_ntiles = 0;
+}
+
+// The instances' PCG solves of K x = rhs, each with its own recurrence and tolerance, in one
+// persistent launch.  *its = the largest instance iteration count.  Returns 1 when the handle does
+// not take this path (no instances, mode 0, or a material outside 0, 1, 3).
+template <typename T>
+int batched_pcg(sfem_handle* h, const T* u, const T* rhs, KrylovWs<T>& w, const T* dinv, double tol, int max_it,
+                int* its) {
+  const int mat = mat_id(h);
+  if (h->n_inst == 0 || h->bt_mode == 0 || !(mat == 0 || mat == 1 || mat == 3)) return 1;
+  const int K = h->n_inst;
+  CU(cudaMemsetAsync(h->bt_bar, 0, 4 * sizeof(unsigned), h->stream));
+  CU(cudaMemsetAsync(h->bt_err, 0, sizeof(int32_t), h->stream));
+  BatchPcg b{};
+  b.K = K;
+  b.n_tiles = h->bt_ntiles;
+  b.nbc = h->nbc;
+  b.N = h->N;
+  b.einst = h->bt_einst;
+  b.tile_node = h->bt_tile_node;
+  b.tile_cnt = h->bt_tile_cnt;
+  b.tile_inst = h->bt_tile_inst;
+  b.inst_tile = h->bt_inst_tile;
+  b.part = h->bt_part;
+  b.rz = h->bt_rz;
+  b.tol2bb = h->bt_tol2bb;
+  b.done = h->bt_done;
+  b.iters = h->bt_iters;
+  b.rr = h->bt_rr;
+  b.bar = h->bt_bar;
+  b.err = h->bt_err;
+  b.tol = tol;
+  b.max_it = max_it;
+  b.wait_limit = h->bt_wait_limit;
+  b.wait_test = h->bt_wait_test;
+  ElemView<T> ev;
+  if constexpr (std::is_same<T, float>::value)
+    ev = h->ev32();
+  else
+    ev = h->ev64();
+  const int lst = launch_batched_pcg<T>(mat, ev, h->csr(), b, u, rhs, w.x, w.r, w.p2, w.p, w.q, dinv,
+                                        reinterpret_cast<T*>(h->fe), h->stream);
+  if (lst == -2) return fail(SFEM_ERR_CUDA, "cooperative launch not available on this device");
+  if (lst != 0) return fail(SFEM_ERR_CUDA, "batched PCG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+  int32_t err = 0;
+  h->bt_iters_h.assign(K, 0);
+  h->bt_status_h.assign(K, 0);
+  h->bt_rr_h.assign(K, 0.0);
+  h->bt_bb_h.assign(K, 0.0);
+  std::vector<double> t2((size_t)K);
+  CU(cudaMemcpyAsync(&err, h->bt_err, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(h->bt_iters_h.data(), h->bt_iters, K * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(h->bt_status_h.data(), h->bt_done + 2 * K, K * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                     h->stream));
+  CU(cudaMemcpyAsync(h->bt_rr_h.data(), h->bt_rr, K * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(t2.data(), h->bt_tol2bb, K * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  for (int q = 0; q < K; q++) h->bt_bb_h[q] = tol > 0 ? t2[q] / (tol * tol) : 0.0;
+  if (err != 0)
+    return fail(SFEM_ERR_TIMEOUT, "a device wait of the batched PCG gave up after %lld polls%s", h->bt_wait_limit,
+                err == 2 ? " (wait self-test)" : "");
+  int mx = 0;
+  for (int q = 0; q < K; q++) {
+    mx = std::max(mx, h->bt_iters_h[q]);
+    if (h->bt_status_h[q] == 4) return fail(SFEM_ERR_NAN, "non-finite value in the Krylov recurrence of instance %d", q);
+  }
+  *its = mx;
+  return 0;
+}
+
 int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
   if (precond == SFEM_PC_LEARNED) return sfem_gnn_inner_solve(h, eta, max_cg, its);
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
@@ -2022,6 +2213,13 @@ int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
       if (!pc) CU(cudaMemcpyAsync(w.dinv, w.ones, 3 * (size_t)h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
       launch_segment_mask<double>(h->n_inst, h->inst_seg, h->inst_active, w.dinv + o, h->stream);
     }
+    int bst = masked ? batched_pcg<double>(h, h->u, h->r64, w, w.dinv, eta, max_cg, its) : 1;
+    if (bst < 0) return bst;
+    if (bst == 0) {
+      CU(cudaMemcpyAsync(h->tmp64 + o, w.x + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+      CU(cudaGetLastError());
+      return 0;
+    }
     st = pcg_device<double>(h, h->u, h->r64, w.x, (pc || masked) ? w.dinv : nullptr, eta, max_cg, 0, &ps);
     if (st < 0) return st;
     CU(cudaMemcpyAsync(h->tmp64 + o, w.x + o, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -2035,6 +2233,13 @@ int inner_solve(sfem_handle* h, double eta, int max_cg, int precond, int* its) {
     if (masked) {
       if (!pc) CU(cudaMemcpyAsync(w.dinv, w.ones, 3 * (size_t)h->N * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
       launch_segment_mask<float>(h->n_inst, h->inst_seg, h->inst_active, w.dinv + o, h->stream);
+    }
+    int bst = masked ? batched_pcg<float>(h, u32, w.b, w, w.dinv, eta, max_cg, its) : 1;
+    if (bst < 0) return bst;
+    if (bst == 0) {
+      launch_convert<float, double>((int64_t)n, w.x + o, h->tmp64 + o, h->stream);
+      CU(cudaGetLastError());
+      return 0;
     }
     st = pcg_device<float>(h, u32, w.b, w.x, (pc || masked) ? w.dinv : nullptr, eta, max_cg, 0, &ps);
     if (st < 0) return st;

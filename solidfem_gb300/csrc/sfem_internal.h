@@ -252,6 +252,38 @@ void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_
                       const int64_t* lbase, const int32_t* lcol, const int16_t* lcol16, const uint8_t* lpos,
                       const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st,
                       const T* r = nullptr, const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
+// ---- batched independent bodies: one persistent kernel per Krylov solve ----
+// Each instance (body) runs its own preconditioned CG recurrence (its own alpha, beta, r.z and
+// convergence test: SolveConjugateGradientMF, Math/IterativeSolvers.h:115-195, per body) inside one
+// cooperative launch; phases (element products, node gather + p.q, updates, directions) are separated
+// by grid barriers whose waits give up after wait_limit polls and set *err.  Free nodes are grouped
+// in tiles of at most 32 (one warp each) that never straddle two instances, so every per-instance sum
+// is a fixed-order sum of tile partials (deterministic).
+struct BatchPcg {
+  int K;                    // instances
+  int n_tiles;
+  int64_t nbc, N;
+  const int32_t* einst;     // E: instance of each element (element order of the handle)
+  const int32_t* tile_node; // n_tiles: first free node (0-based among the free nodes)
+  const int32_t* tile_cnt;  // n_tiles: nodes in the tile (1..32)
+  const int32_t* tile_inst; // n_tiles: the tile's instance
+  const int32_t* inst_tile; // K + 1: the tiles of instance k are inst_tile[k] .. inst_tile[k + 1] - 1
+  double* part;             // 3 n_tiles: per-tile p.q, r.z, r.r
+  double* rz;               // 2 K: r.z of the current / next iteration (by parity)
+  double* tol2bb;           // K: tol^2 |b_k|^2
+  int32_t* done;            // 2 K: 0 running, 1 converged, 2 non-positive curvature, 3 iteration cap, 4 non-finite
+  int32_t* iters;           // K
+  double* rr;               // K: final |r_k|^2
+  unsigned* bar;            // 2: barrier arrival count and generation
+  int32_t* err;             // 1: a wait gave up (0 ok)
+  double tol;
+  int max_it;
+  long long wait_limit;     // polls of one barrier wait before it gives up
+  int wait_test;            // 1: block 0 first waits for a flag that nothing sets (exercises the limit)
+};
+template <typename T>
+int launch_batched_pcg(int mat, const ElemView<T>& ev, NodeCsr csr, const BatchPcg& b, const T* u, const T* rhs, T* x,
+                       T* r, T* z, T* p, T* q, const T* dinv, T* fe, cudaStream_t st);
 // implicit dynamics: per patch-node slot mass share m_g / (h^2 k_g) (k_g patches touch g)
 template <typename T>
 void launch_patch_mass(int64_t n_slots, int64_t nbc, const int32_t* pnode, const int32_t* bidx, PatchBoundary pb,

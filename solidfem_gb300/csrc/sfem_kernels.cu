@@ -2716,6 +2716,295 @@ void launch_convert(int64_t n, const Tin* a, Tout* b, cudaStream_t st) {
 template void launch_convert<double, float>(int64_t, const double*, float*, cudaStream_t);
 template void launch_convert<float, double>(int64_t, const float*, double*, cudaStream_t);
 
+// ---------------------------------------------------------------------------
+// Batched independent bodies: every instance's PCG in one persistent cooperative launch
+// ---------------------------------------------------------------------------
+// Grid-wide barrier of a cooperative launch whose wait is bounded: after `limit` polls (or once
+// another block has reported a failure) it sets *err and returns false; every block then leaves.
+__device__ __forceinline__ bool grid_sync_bounded(unsigned* bar, int32_t* err, long long limit) {
+  __shared__ int fail;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fail = 0;
+    volatile unsigned* gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long it = 0;
+      while (*gen == g) {
+        if (*(volatile int32_t*)err != 0 || ++it > limit) {
+          atomicCAS(err, 0, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    fail = *(volatile int32_t*)err != 0;
+  }
+  __syncthreads();
+  return fail == 0;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// fixed-order sum of component c of instance k's tile partials (every warp gets the same bits)
+__device__ __forceinline__ double inst_sum(const BatchPcg& b, int k, int c, int lane) {
+  double v = 0.0;
+  const int t1 = __ldcg(b.inst_tile + k + 1);
+  for (int t = __ldcg(b.inst_tile + k) + lane; t < t1; t += 32) v += __ldcg(b.part + 3 * t + c);
+  return warp_sum_d(v);
+}
+
+template <typename T>
+__device__ __forceinline__ void load3cg(const T* a, int g, T* o) {
+  o[0] = __ldcg(a + 3 * (int64_t)g);
+  o[1] = __ldcg(a + 3 * (int64_t)g + 1);
+  o[2] = __ldcg(a + 3 * (int64_t)g + 2);
+}
+
+// Phases per iteration (each followed by a grid barrier): A element products K_e p of the running
+// instances; B q = K p at every free node (node->element CSR, element order) and the tiles' p.q;
+// C alpha_k = r.z_k / p.q_k, x += alpha p, r -= alpha q, z = D^-1 r and the tiles' r.z, r.r;
+// D beta_k, the instance's convergence test (r.r <= tol^2 b.b) and p = z + beta p.  Data written by
+// other blocks during the launch is read with L2 loads (__ldcg).
+template <typename T, int MAT>
+__global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCsr csr, BatchPcg b,
+                                                          const T* __restrict__ u, const T* __restrict__ rhs, T* x,
+                                                          T* r, T* z, T* p, T* q, const T* __restrict__ dinv, T* fe) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), nw = (int)((gridDim.x * blockDim.x) >> 5);
+  const int K = b.K;
+  const int64_t nbc = b.nbc, E = ev.E;
+  if (b.wait_test && blockIdx.x == 0 && threadIdx.x == 0) {
+    // a flag that nothing sets: the bounded wait gives up and reports it
+    volatile unsigned* never = b.bar + 2;
+    long long it = 0;
+    while (*never == 0u) {
+      if (++it > b.wait_limit) {
+        atomicCAS(b.err, 0, 2);
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  // x = 0, r = b, z = D^-1 r, p = z; tile partials of r.z and r.r
+  for (int t = gw; t < b.n_tiles; t += nw) {
+    double rz = 0.0, rr = 0.0;
+    if (lane < b.tile_cnt[t]) {
+      const int64_t o = 3 * (nbc + b.tile_node[t] + lane);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const T ri = rhs[o + c], zi = dinv[o + c] * ri;
+        x[o + c] = T(0);
+        r[o + c] = ri;
+        z[o + c] = zi;
+        p[o + c] = zi;
+        rz += (double)ri * (double)zi;
+        rr += (double)ri * (double)ri;
+      }
+    }
+    rz = warp_sum_d(rz);
+    rr = warp_sum_d(rr);
+    if (lane == 0) {
+      b.part[3 * t] = 0.0;
+      b.part[3 * t + 1] = rz;
+      b.part[3 * t + 2] = rr;
+    }
+  }
+  if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
+  for (int k = gw; k < K; k += nw) {  // one warp per instance writes its start values
+    const double rz = inst_sum(b, k, 1, lane), rr = inst_sum(b, k, 2, lane);
+    if (lane == 0) {
+      b.rz[k] = rz;
+      b.tol2bb[k] = b.tol * b.tol * rr;
+      b.done[k] = rr > 0.0 ? 0 : 1;
+      b.done[2 * K + k] = rr > 0.0 ? 0 : 1;
+      b.iters[k] = 0;
+      b.rr[k] = rr;
+    }
+  }
+  if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
+  for (int it = 0; it < b.max_it; it++) {
+    const int cur = it & 1, nxt = cur ^ 1;
+    const int32_t* done = b.done + cur * K;
+    // A: element products
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+      if (__ldcg(done + b.einst[e]) != 0) continue;
+      const int4 t4 = ev.tets[e];
+      M3<T> X;
+#pragma unroll
+      for (int k9 = 0; k9 < 9; k9++) X.a[k9] = ev.X[k9 * E + e];
+      const T vol = ev.vol[e];
+      T mu = ev.mu, la = ev.lambda;
+      if (ev.scale) {
+        const T sc = ev.scale[e];
+        mu *= sc;
+        la *= ev.scale_la ? ev.scale_la[e] : sc;
+      }
+      M3<T> F = grad_of(u, t4, X);
+      F.a[0] += T(1);
+      F.a[4] += T(1);
+      F.a[8] += T(1);
+      Tangent<T, MAT> tg;
+      tg.init(F, mu, la);
+      T a0[3], a1[3], a2[3], a3[3];
+      load3cg(p, t4.x, a0);
+      load3cg(p, t4.y, a1);
+      load3cg(p, t4.z, a2);
+      load3cg(p, t4.w, a3);
+      M3<T> D;
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        D.a[3 * i] = a1[i] - a0[i];
+        D.a[3 * i + 1] = a2[i] - a0[i];
+        D.a[3 * i + 2] = a3[i] - a0[i];
+      }
+      const M3<T> dP = tg.apply(mul(D, X));
+      T f[12];
+      nodal_forces(dP, X, -vol, f);
+      store12(fe, e, f);
+    }
+    if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
+    // B: q at the free nodes of the running instances, tile p.q
+    for (int t = gw; t < b.n_tiles; t += nw) {
+      const int k = b.tile_inst[t];
+      double pq = 0.0;
+      if (__ldcg(done + k) == 0 && lane < b.tile_cnt[t]) {
+        const int64_t g = nbc + b.tile_node[t] + lane;
+        T f0 = T(0), f1 = T(0), f2 = T(0);
+        for (int64_t c = csr.ptr[g]; c < csr.ptr[g + 1]; c++) {
+          const int64_t ent = csr.ent[c];
+          const T* src = fe + 12 * (ent >> 2) + 3 * (ent & 3);
+          f0 += __ldcg(src);
+          f1 += __ldcg(src + 1);
+          f2 += __ldcg(src + 2);
+        }
+        const int64_t o = 3 * g;
+        q[o] = -f0;
+        q[o + 1] = -f1;
+        q[o + 2] = -f2;
+        pq = -((double)__ldcg(p + o) * f0 + (double)__ldcg(p + o + 1) * f1 + (double)__ldcg(p + o + 2) * f2);
+      }
+      pq = warp_sum_d(pq);
+      if (lane == 0) b.part[3 * t] = pq;
+    }
+    if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
+    // C: alpha and the updates, tile r.z and r.r
+    for (int t = gw; t < b.n_tiles; t += nw) {
+      const int k = b.tile_inst[t];
+      double rz = 0.0, rr = 0.0;
+      if (__ldcg(done + k) == 0) {
+        const double pq = inst_sum(b, k, 0, lane);
+        const double alpha = (isfinite(pq) && pq > 0.0) ? __ldcg(b.rz + cur * K + k) / pq : 0.0;
+        if (lane < b.tile_cnt[t]) {
+          const int64_t o = 3 * (nbc + b.tile_node[t] + lane);
+          const T a = (T)alpha;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const T pi = __ldcg(p + o + c), qi = __ldcg(q + o + c);
+            x[o + c] = __ldcg(x + o + c) + a * pi;
+            const T ri = __ldcg(r + o + c) - a * qi, zi = dinv[o + c] * ri;
+            r[o + c] = ri;
+            z[o + c] = zi;
+            rz += (double)ri * (double)zi;
+            rr += (double)ri * (double)ri;
+          }
+        }
+      }
+      rz = warp_sum_d(rz);
+      rr = warp_sum_d(rr);
+      if (lane == 0) {
+        b.part[3 * t + 1] = rz;
+        b.part[3 * t + 2] = rr;
+      }
+    }
+    if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
+    // D: beta, convergence, directions
+    for (int t = gw; t < b.n_tiles; t += nw) {
+      const int k = b.tile_inst[t];
+      const bool lead = t == b.inst_tile[k] && lane == 0;
+      if (__ldcg(done + k) != 0) {
+        if (lead) b.done[nxt * K + k] = __ldcg(done + k);
+        continue;
+      }
+      const double pq = inst_sum(b, k, 0, lane), rzn = inst_sum(b, k, 1, lane), rr = inst_sum(b, k, 2, lane);
+      int st = 0;
+      if (!isfinite(pq) || !isfinite(rzn)) st = 4;
+      else if (!(pq > 0.0)) st = 2;
+      else if (rr <= __ldcg(b.tol2bb + k)) st = 1;
+      else if (it + 1 >= b.max_it) st = 3;
+      if (st == 2 && it == 0 && lane < b.tile_cnt[t]) {  // truncated at once: the preconditioned residual
+        const int64_t o = 3 * (nbc + b.tile_node[t] + lane);
+#pragma unroll
+        for (int c = 0; c < 3; c++) x[o + c] = __ldcg(p + o + c);
+      }
+      if (st == 0 && lane < b.tile_cnt[t]) {
+        const T beta = (T)(rzn / __ldcg(b.rz + cur * K + k));
+        const int64_t o = 3 * (nbc + b.tile_node[t] + lane);
+#pragma unroll
+        for (int c = 0; c < 3; c++) p[o + c] = __ldcg(z + o + c) + beta * __ldcg(p + o + c);
+      }
+      if (lead) {
+        b.done[nxt * K + k] = st;
+        b.done[2 * K + k] = st;
+        b.rz[nxt * K + k] = rzn;
+        b.iters[k] = st == 2 ? it : it + 1;
+        b.rr[k] = rr;
+      }
+    }
+    if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
+    __shared__ int all_done;
+    if (threadIdx.x == 0) {
+      int a = 1;
+      for (int k = 0; k < K && a; k++) a = __ldcg(b.done + nxt * K + k) != 0;
+      all_done = a;
+    }
+    __syncthreads();
+    if (all_done) break;
+  }
+}
+
+template <typename T>
+int launch_batched_pcg(int mat, const ElemView<T>& ev, NodeCsr csr, const BatchPcg& b, const T* u, const T* rhs, T* x,
+                       T* r, T* z, T* p, T* q, const T* dinv, T* fe, cudaStream_t st) {
+  void (*kern)(ElemView<T>, NodeCsr, BatchPcg, const T*, const T*, T*, T*, T*, T*, T*, const T*, T*) = nullptr;
+  switch (mat) {
+    case kLinear: kern = k_batched_pcg<T, kLinear>; break;
+    case kStvk: kern = k_batched_pcg<T, kStvk>; break;
+    case kNeoHookean: kern = k_batched_pcg<T, kNeoHookean>; break;
+    default: return -1;
+  }
+  int dev = 0, sms = 0, per = 0, coop = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (!coop) return -2;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, 0);
+  if (per < 1) return -2;
+  const unsigned grid = (unsigned)(per * sms);
+  ElemView<T> ev_ = ev;
+  NodeCsr csr_ = csr;
+  BatchPcg b_ = b;
+  const T *u_ = u, *rhs_ = rhs, *dinv_ = dinv;
+  T *x_ = x, *r_ = r, *z_ = z, *p_ = p, *q_ = q, *fe_ = fe;
+  void* args[] = {&ev_, &csr_, &b_, &u_, &rhs_, &x_, &r_, &z_, &p_, &q_, &dinv_, &fe_};
+  count_launch();
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kThreads), args, 0, st) == cudaSuccess ? 0 : -3;
+}
+template int launch_batched_pcg<float>(int, const ElemView<float>&, NodeCsr, const BatchPcg&, const float*, const float*,
+                                       float*, float*, float*, float*, float*, const float*, float*, cudaStream_t);
+template int launch_batched_pcg<double>(int, const ElemView<double>&, NodeCsr, const BatchPcg&, const double*,
+                                        const double*, double*, double*, double*, double*, double*, const double*,
+                                        double*, cudaStream_t);
+
 template <typename T>
 __global__ void k_axpy_state(int64_t n, double a, const T* __restrict__ d, const double* __restrict__ base,
                              double* __restrict__ x) {

@@ -182,6 +182,24 @@ class FemPhysicsMatrixFree:
         o = np.ascontiguousarray(node_offsets, dtype=np.int64)
         nat.check(self._lib.sfem_set_instances(self._h, o.size - 1, o.ctypes.data_as(nat._i64p)))
 
+    def set_batched_pcg(self, per_instance=True):
+        """Krylov solves with instances: every instance's own PCG in one persistent launch (True) or one
+        recurrence over all instances (False)."""
+        nat.check(self._lib.sfem_set_batched_pcg(self._h, 1 if per_instance else 0))
+
+    def instance_pcg_stats(self, k):
+        """Per instance, of the last per-instance PCG solve: (iterations, status, |r|/|b|)."""
+        its = np.zeros(k, dtype=np.int32)
+        st = np.zeros(k, dtype=np.int32)
+        rel = np.zeros(k)
+        nat.check(self._lib.sfem_instance_pcg_stats(self._h, its.ctypes.data_as(nat._ip), st.ctypes.data_as(nat._ip),
+                                                    _dp(rel)))
+        return its, st, rel
+
+    def set_device_wait(self, limit, test=False):
+        """Bound (polls) of the persistent kernels' device-side waits; test=True makes the waits run out."""
+        nat.check(self._lib.sfem_set_device_wait(self._h, int(limit), 1 if test else 0))
+
     def instance_stats(self, k):
         rel = np.zeros(k)
         its = np.zeros(k, dtype=np.int32)

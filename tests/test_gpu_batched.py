@@ -48,3 +48,68 @@ def test_c4_sixty_four_bodies_fp32_refined():
           f"max body rel res {st['instance_rel_res'].max():.2e}")
     assert st["status"] == 0
     assert (st["instance_rel_res"] <= 1e-8).all()
+
+
+def _separate(b, k, precision):
+    from solidfem_gb300 import FemPhysicsMatrixFree
+
+    m, sp = b.meshes[k], b.specs[k]
+    x = m.nodes.copy()
+    x[:, 1] += b.spacing * k
+    return FemPhysicsMatrixFree(m.tets, x, m.face_nodes(0, 0), young=sp.young, poisson=sp.poisson, density=1070.0,
+                                gravity=(0, 0, -9.81), material=3, precision=precision)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-5)])
+def test_per_instance_pcg_runs_each_body_own_recurrence(precision, tol):
+    """One persistent launch runs every body's PCG with its own alpha, beta and stop test: each body's
+    iteration count and solution equal its separate single-body PCG solve (SolveConjugateGradientMF,
+    Math/IterativeSolvers.h:115-195, per body); the bodies stop at different iterations."""
+    from solidfem_gb300.batch import BatchedBodies, c4_specs
+
+    specs = c4_specs(12, seed=3)
+    for sp in specs:
+        sp.n = min(sp.n, 32)
+        sp.n -= sp.n % 4
+    b = BatchedBodies(specs, precision=precision)
+    rng = np.random.default_rng(5)
+    rhs = rng.normal(size=(b.phys.n_free, 3))
+    x, st = b.phys.pcg(rhs, rel_tol=tol, max_iters=20000)
+    its, status, rel = b.phys.instance_pcg_stats(len(specs))
+    assert st["status"] == 0 and (status == 1).all() and (rel <= tol).all(), (status, rel)
+    seg = np.cumsum([0] + [_separate(b, k, precision).n_free for k in range(len(specs))])
+    for k in range(len(specs)):
+        p = _separate(b, k, precision)
+        xs, ss = p.pcg(rhs[seg[k]:seg[k + 1]], rel_tol=tol, max_iters=20000)
+        err = np.linalg.norm(x[seg[k]:seg[k + 1]] - xs) / np.linalg.norm(xs)
+        print(f"body {k} (n={specs[k].n}, E={specs[k].young:.3g}): batched {its[k]} its, separate {ss['iters']} its, "
+              f"solution difference {err:.1e}")
+        # the same recurrence; partial sums in another order can move the stop by an iteration
+        assert abs(int(its[k]) - ss["iters"]) <= 2
+        assert err <= (1e-8 if precision == "fp64" else 2e-3)
+        p.close()
+    assert len(set(its.tolist())) > 1  # every body stops on its own test
+
+
+def test_persistent_kernel_wait_gives_up_and_reports():
+    """The grid barriers' waits are bounded: with the self-test flag the first wait polls a flag that
+    nothing sets, gives up after the limit and the solve reports SFEM_ERR_TIMEOUT; the context stays
+    usable and the next solve converges."""
+    from solidfem_gb300 import SfemError
+    from solidfem_gb300 import _native as nat
+    from solidfem_gb300.batch import BatchedBodies, c4_specs
+
+    specs = c4_specs(4, seed=2)
+    for sp in specs:
+        sp.n = 8
+    b = BatchedBodies(specs, precision="fp32")
+    b.phys.set_device_wait(200000, test=True)
+    rhs = np.ones((b.phys.n_free, 3))
+    with pytest.raises(SfemError) as e:
+        b.phys.pcg(rhs, rel_tol=1e-5, max_iters=1000)
+    assert f"sfem error {nat.SFEM_ERR_TIMEOUT}" in str(e.value)
+    b.phys.set_device_wait(20000000, test=False)
+    x, st = b.phys.pcg(rhs, rel_tol=1e-5, max_iters=20000)
+    assert st["status"] == 0 and np.isfinite(x).all()
+    st = b.solve(rel_tol=1e-8, max_newton=100)
+    assert st["status"] == 0 and (st["instance_rel_res"] <= 1e-8).all()
