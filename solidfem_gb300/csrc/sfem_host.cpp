@@ -149,13 +149,13 @@ struct sfem_handle {
   // symmetric tangents: only the diagonal and upper blocks are stored (the slots above); each row's
   // lower blocks are read transposed from their mirror rows: per slice of 32 rows, lower entry
   // (row r, position k) at lbase[r / 32] + 32 k + r % 32 holds the column j (difference j - r, or j)
-  // and the position of block (j, r) among row j's stored blocks (0xff: padding)
+  // and the block-slot of block (j, r) in row j (-1: padding)
   bool sell_sym = false;
   int64_t sell_nlow = 0;
   int64_t* sell_lbase = nullptr;
   int16_t* sell_lcol16 = nullptr;
   int32_t* sell_lcol = nullptr;
-  uint8_t* sell_lpos = nullptr;
+  int32_t* sell_lslot = nullptr;
   uint32_t* sell_code = nullptr;
   float *sell_vals32 = nullptr, *sell_ke32 = nullptr;
   double *sell_vals64 = nullptr, *sell_ke64 = nullptr;
@@ -337,7 +337,7 @@ void krylov_hvp(sfem_handle* h, const T* u, const T* p, T* q, cudaEvent_t mid, c
       vals = h->sell_vals64;
     if (h->sell_sym)
       launch_ssell_hvp<T>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, h->sell_lbase, h->sell_lcol,
-                          h->sell_lcol16, h->sell_lpos, vals, p, q, h->red(), h->scal, h->stream, r, dinv, p_new, z);
+                          h->sell_lcol16, h->sell_lslot, vals, p, q, h->red(), h->scal, h->stream, r, dinv, p_new, z);
     else
       launch_sell_hvp<T>(h->nbc, h->nf, h->sell_base, h->sell_col, h->sell_col16, vals, p, q, h->red(), h->scal,
                          h->stream, r, dinv, p_new, z);
@@ -922,7 +922,7 @@ int sfem_destroy(sfem_handle* h) {
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
                    h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32, h->sell_ke32,
                    h->sell_col16, h->sell_vals64, h->sell_ke64, h->sell_lbase, h->sell_lcol16, h->sell_lcol,
-                   h->sell_lpos};
+                   h->sell_lslot};
   for (void* b : ibufs)
     if (b) cudaFree(b);
   void* pbufs[] = {h->perm, h->etmp, h->elem_off, h->node_off, h->pnode, h->pdest, h->lptr, h->lent, h->lent12, h->lidx,
@@ -970,7 +970,7 @@ int sfem_get_profile(const sfem_handle* h, sfem_profile* out) {
   if (h->prof_op == 1)  // assembled tangent: blocks and their column indices, and per free node the
                         // direction inputs (z or r, p_old) and outputs (p, q)
     out->algo_bytes_hvp = (double)h->sell_nnzb * (9.0 * sz + (h->sell_col16 ? 2.0 : 4.0)) +
-                          (double)h->sell_nlow * ((h->sell_col16 ? 2.0 : 4.0) + 1.0) + (double)h->nf * 12.0 * sz;
+                          (double)h->sell_nlow * ((h->sell_col16 ? 2.0 : 4.0) + 4.0) + (double)h->nf * 12.0 * sz;
   else
     out->algo_bytes_hvp = (double)h->E * (16.0 + 10.0 * sz) + (double)h->N * 9.0 * sz;
   out->precision = h->prof_precision;
@@ -1123,13 +1123,13 @@ static int sell_alloc(sfem_handle* h, T** p, size_t count) {
 static void sell_release(sfem_handle* h) {
   void* bufs[] = {h->sell_base, h->sell_cptr, h->sell_col, h->sell_dslot, h->sell_code, h->sell_vals32,
                   h->sell_ke32, h->sell_col16, h->sell_vals64, h->sell_ke64, h->sell_lbase, h->sell_lcol16,
-                  h->sell_lcol, h->sell_lpos};
+                  h->sell_lcol, h->sell_lslot};
   for (void* b : bufs)
     if (b) cudaFree(b);
   h->sell_lbase = nullptr;
   h->sell_lcol16 = nullptr;
   h->sell_lcol = nullptr;
-  h->sell_lpos = nullptr;
+  h->sell_lslot = nullptr;
   h->sell_sym = false;
   h->sell_nlow = 0;
   h->sell_base = h->sell_cptr = nullptr;
@@ -1181,8 +1181,6 @@ static int sell_structure(sfem_handle* h) {
       len[r] = (int32_t)cols.size();
     }
   });
-  // a lower entry names its mirror's position in one byte: rows of at most 255 columns
-  if (sym && nf > 0 && *std::max_element(len.begin(), len.end()) > 255) sym = false;
   if (sym)
     parallel_rows(nf, [&](int64_t a, int64_t b) {
       std::vector<int32_t> cols;
@@ -1248,10 +1246,9 @@ static int sell_structure(sfem_handle* h) {
   // the fill advanced cnt[t] to the end of slot t's list: shift back to start offsets
   for (int64_t t = T; t > 0; t--) cnt[t] = cnt[t - 1];
   cnt[0] = 0;
-  // symmetric: the lower entries, each naming its mirror block (j, r) by j and its position in row j
+  // symmetric: the lower entries, each naming its column j and the block-slot of its mirror (j, r)
   std::vector<int64_t> lbase((size_t)ns + 1, 0);
-  std::vector<int32_t> lcol;
-  std::vector<uint8_t> lpos;
+  std::vector<int32_t> lcol, lslot;
   int64_t nlow = 0;
   if (sym) {
     std::vector<int32_t> llen((size_t)nf);
@@ -1272,7 +1269,7 @@ static int sell_structure(sfem_handle* h) {
     }
     const int64_t L = lbase[ns];
     lcol.assign((size_t)L, 0);
-    lpos.assign((size_t)L, 0xff);
+    lslot.assign((size_t)L, -1);
     parallel_rows(nf, [&](int64_t a, int64_t b) {
       std::vector<int32_t> cols;
       for (int64_t r = a; r < b; r++) {
@@ -1290,9 +1287,9 @@ static int sell_structure(sfem_handle* h) {
               if (scol[base[js] + 32 * mid + jl] < (int32_t)r) lo = mid + 1; else hi = mid;
             }
             lcol[t] = jc;
-            lpos[t] = (uint8_t)lo;
+            lslot[t] = (int32_t)(base[js] + 32 * lo + jl);
           } else {
-            lcol[t] = (int32_t)r;  // padding (lpos 0xff): skipped
+            lcol[t] = (int32_t)r;  // padding (slot -1): skipped
           }
         }
       }
@@ -1348,10 +1345,10 @@ static int sell_structure(sfem_handle* h) {
   if (sym) {
     const int64_t L = lbase[ns];
     TRY(sell_alloc(h, &h->sell_lbase, lbase.size()));
-    TRY(sell_alloc(h, &h->sell_lpos, std::max<size_t>(lpos.size(), 1)));
+    TRY(sell_alloc(h, &h->sell_lslot, std::max<size_t>(lslot.size(), 1)));
     CU(cudaMemcpyAsync(h->sell_lbase, lbase.data(), lbase.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
                        h->stream));
-    if (L > 0) CU(cudaMemcpyAsync(h->sell_lpos, lpos.data(), lpos.size(), cudaMemcpyHostToDevice, h->stream));
+    if (L > 0) CU(cudaMemcpyAsync(h->sell_lslot, lslot.data(), lslot.size() * 4, cudaMemcpyHostToDevice, h->stream));
     if (fits16) {
       std::vector<int16_t> d16((size_t)L, 0);
       for (int64_t r = 0; r < nf; r++) {

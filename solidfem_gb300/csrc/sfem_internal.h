@@ -245,11 +245,11 @@ void launch_sell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t
                      const T* r = nullptr, const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
 // the same product from a symmetric tangent stored as its diagonal and upper blocks (base/col/col16, as
 // above), each row's lower blocks read transposed from their mirror rows: lower entry (row r, position k)
-// at lbase[r / 32] + 32 k + r % 32 names the column j (lcol, or lcol16 = j - r) and the position of block
-// (j, r) among row j's stored blocks (lpos; 0xff: padding)
+// at lbase[r / 32] + 32 k + r % 32 names the column j (lcol, or lcol16 = j - r) and the block-slot of
+// block (j, r) in row j (lslot; -1: padding)
 template <typename T>
 void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const int16_t* col16,
-                      const int64_t* lbase, const int32_t* lcol, const int16_t* lcol16, const uint8_t* lpos,
+                      const int64_t* lbase, const int32_t* lcol, const int16_t* lcol16, const int32_t* lslot,
                       const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st,
                       const T* r = nullptr, const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
 // ---- batched independent bodies: one persistent kernel per Krylov solve ----

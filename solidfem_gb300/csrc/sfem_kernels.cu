@@ -1322,7 +1322,7 @@ template void launch_sell_hvp<double>(int64_t, int64_t, const int64_t*, const in
 template <typename T, bool DIR, typename CI>
 __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
                                                         const CI* __restrict__ col, const int64_t* __restrict__ lbase,
-                                                        const CI* __restrict__ lcol, const uint8_t* __restrict__ lpos,
+                                                        const CI* __restrict__ lcol, const int32_t* __restrict__ lslot,
                                                         const T* __restrict__ vals, const T* __restrict__ p,
                                                         T* __restrict__ q, Reduce red, CgScalars* s,
                                                         const T* __restrict__ r, const T* __restrict__ dinv,
@@ -1354,26 +1354,54 @@ __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf,
       }
     };
     T y0 = T(0), y1 = T(0), y2 = T(0);
-    // lower blocks, transposed from the mirror rows
+    // lower blocks, transposed from the mirror rows (two entries per step: both slots, values and
+    // directions in flight; padding, slot -1, follows the row's last lower block)
     {
       const int64_t lb0 = lbase[sl];
       const int wl = (int)((lbase[sl + 1] - lb0) >> 5);
       const CI* lc = lcol + lb0 + lane;
-      const uint8_t* lp = lpos + lb0 + lane;
-      for (int k = 0; k < wl; k++) {
-        const int kp = lp[32 * k];
-        if (kp == 0xff) break;  // padding follows the row's last lower block
-        const int64_t j = cbase + lc[32 * k];
-        const int64_t jl = j & 31;
-        const T* V = vals + 9 * (base[j >> 5] + 32 * kp) + jl;
-        T v[9];
+      const int32_t* ls = lslot + lb0 + lane;
+      auto mirror = [&](int64_t t, T (&v)[9]) {
+        const T* V = vals + 9 * (t & ~(int64_t)31) + (t & 31);
 #pragma unroll
         for (int qq = 0; qq < 9; qq++) v[qq] = V[32 * qq];
-        T x0, x1, x2;
-        xdir(j, x0, x1, x2);
-        y0 += v[0] * x0 + v[3] * x1 + v[6] * x2;
-        y1 += v[1] * x0 + v[4] * x1 + v[7] * x2;
-        y2 += v[2] * x0 + v[5] * x1 + v[8] * x2;
+      };
+      int k = 0;
+      for (; k + 2 <= wl; k += 2) {
+        const int ta = ls[32 * k], tb = ls[32 * k + 32];
+        if (ta < 0) break;
+        const int64_t ja = cbase + lc[32 * k], jb = cbase + lc[32 * k + 32];
+        T va[9], vb[9], xa0, xa1, xa2, xb0 = T(0), xb1 = T(0), xb2 = T(0);
+        mirror(ta, va);
+        xdir(ja, xa0, xa1, xa2);
+        if (tb >= 0) {
+          mirror(tb, vb);
+          xdir(jb, xb0, xb1, xb2);
+        } else {
+#pragma unroll
+          for (int qq = 0; qq < 9; qq++) vb[qq] = T(0);
+        }
+        y0 += va[0] * xa0 + va[3] * xa1 + va[6] * xa2;
+        y1 += va[1] * xa0 + va[4] * xa1 + va[7] * xa2;
+        y2 += va[2] * xa0 + va[5] * xa1 + va[8] * xa2;
+        y0 += vb[0] * xb0 + vb[3] * xb1 + vb[6] * xb2;
+        y1 += vb[1] * xb0 + vb[4] * xb1 + vb[7] * xb2;
+        y2 += vb[2] * xb0 + vb[5] * xb1 + vb[8] * xb2;
+        if (tb < 0) {
+          k = wl;
+          break;
+        }
+      }
+      if (k < wl) {
+        const int ta = ls[32 * k];
+        if (ta >= 0) {
+          T va[9], x0, x1, x2;
+          mirror(ta, va);
+          xdir(cbase + lc[32 * k], x0, x1, x2);
+          y0 += va[0] * x0 + va[3] * x1 + va[6] * x2;
+          y1 += va[1] * x0 + va[4] * x1 + va[7] * x2;
+          y2 += va[2] * x0 + va[5] * x1 + va[8] * x2;
+        }
       }
     }
     // the diagonal and upper blocks of the row itself
@@ -1449,7 +1477,7 @@ __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf,
 }
 template <typename T>
 void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_t* col, const int16_t* col16,
-                      const int64_t* lbase, const int32_t* lcol, const int16_t* lcol16, const uint8_t* lpos,
+                      const int64_t* lbase, const int32_t* lcol, const int16_t* lcol16, const int32_t* lslot,
                       const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st, const T* r,
                       const T* dinv, T* p_new, const T* z) {
   static const int wave = std::min(std::min(resident_ctas(k_ssell_hvp<T, true, int32_t>, kThreads, 0),
@@ -1459,24 +1487,24 @@ void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_
   const int grid = std::max(1, std::min(wave, (int)((nf + kThreads - 1) / kThreads)));
   count_launch();
   if (col16 && p_new != nullptr)
-    launch_pdl(k_ssell_hvp<T, true, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, lbase, lcol16, lpos, vals,
+    launch_pdl(k_ssell_hvp<T, true, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, lbase, lcol16, lslot, vals,
                p, q, red, s, r, dinv, p_new, z);
   else if (col16)
-    launch_pdl(k_ssell_hvp<T, false, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, lbase, lcol16, lpos,
+    launch_pdl(k_ssell_hvp<T, false, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, lbase, lcol16, lslot,
                vals, p, q, red, s, nullptr, nullptr, nullptr, nullptr);
   else if (p_new != nullptr)
-    launch_pdl(k_ssell_hvp<T, true, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, lbase, lcol, lpos, vals, p,
+    launch_pdl(k_ssell_hvp<T, true, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, lbase, lcol, lslot, vals, p,
                q, red, s, r, dinv, p_new, z);
   else
-    launch_pdl(k_ssell_hvp<T, false, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, lbase, lcol, lpos, vals,
+    launch_pdl(k_ssell_hvp<T, false, int32_t>, grid, kThreads, 0, st, nbc, nf, base, col, lbase, lcol, lslot, vals,
                p, q, red, s, nullptr, nullptr, nullptr, nullptr);
 }
 template void launch_ssell_hvp<float>(int64_t, int64_t, const int64_t*, const int32_t*, const int16_t*,
-                                      const int64_t*, const int32_t*, const int16_t*, const uint8_t*, const float*,
+                                      const int64_t*, const int32_t*, const int16_t*, const int32_t*, const float*,
                                       const float*, float*, Reduce, CgScalars*, cudaStream_t, const float*,
                                       const float*, float*, const float*);
 template void launch_ssell_hvp<double>(int64_t, int64_t, const int64_t*, const int32_t*, const int16_t*,
-                                       const int64_t*, const int32_t*, const int16_t*, const uint8_t*, const double*,
+                                       const int64_t*, const int32_t*, const int16_t*, const int32_t*, const double*,
                                        const double*, double*, Reduce, CgScalars*, cudaStream_t, const double*,
                                        const double*, double*, const double*);
 

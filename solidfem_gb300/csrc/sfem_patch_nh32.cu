@@ -157,7 +157,7 @@ __device__ __forceinline__ void nh_element_forces(const float (&X)[9], float vol
 }
 
 template <bool DIR>
-__global__ void __launch_bounds__(kNT, 4) k_patch_hvp_nh32(PatchView<float> pv, const float* __restrict__ u,
+__global__ void __launch_bounds__(kNT, 5) k_patch_hvp_nh32(PatchView<float> pv, const float* __restrict__ u,
                                                            const float* __restrict__ p, float* __restrict__ q,
                                                            float* __restrict__ partial, Reduce red, CgScalars* s,
                                                            const float* __restrict__ r, const float* __restrict__ dinv,
