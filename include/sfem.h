@@ -395,6 +395,16 @@ int sfem_dot_noalloc_dev(const double* a_dev, const double* b_dev, int64_t n, do
 int sfem_coarse_factors(const double* X, int64_t n, double cell, double rtol, int32_t* aid, double* d,
                         double* R, int64_t* n_agg);
 
+/* Two-level preconditioner for the learned flexible CG of FP32 handles (extension: the reference's
+ * SolveConjugateGradientMF, Math/IterativeSolvers.h:115-195, has no coarse space):
+ * z = M(r) + P Kc^-1 P^T r, P the rigid-body modes of grid-cell aggregates of the free nodes (cell:
+ * the grid spacing; rtol as in sfem_coarse_factors), Kc = P^T K P from the FP64 tangent at the rest
+ * state, inverted once here (dense, FP64 Cholesky on the host threads) and applied in FP32 as one
+ * matrix-vector product per iteration.  cell <= 0 turns it off.  At most 4096 aggregates. */
+int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol);
+/* z = P Kc^-1 P^T r alone (free DOFs, host arrays), for checking the coarse correction. */
+int sfem_coarse_apply(sfem_handle* h, const double* r, double* z);
+
 /* ---- device-pointer variants (stream-ordered on the handle's stream) ---- */
 int sfem_compute_gradients_dev(sfem_handle* h, double* r_dev);
 int sfem_matvec_dev(sfem_handle* h, const double* d_dev, double* Kd_dev);

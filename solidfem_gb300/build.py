@@ -21,7 +21,8 @@ OBJ_DIR = os.path.join(PKG, "lib", "obj")
 LIB = os.path.join(OUT_DIR, "libsfem_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["sfem_kernels.cu", "sfem_host.cpp", "sfem_gnn.cu", "sfem_noalloc.cu", "sfem_coarse.cpp", "sfem_patch_nh32.cu"]
+SOURCES = ["sfem_kernels.cu", "sfem_host.cpp", "sfem_gnn.cu", "sfem_noalloc.cu", "sfem_coarse.cpp", "sfem_patch_nh32.cu",
+           "sfem_coarse_kernels.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,115 @@
+// Coarse-space correction of the two-level preconditioner inside the flexible-CG inner solves:
+// z += P Kc^-1 P^T r with P the aggregates' rigid-body modes (an extension: the reference's
+// SolveConjugateGradientMF, Math/IterativeSolvers.h:115-195, has no coarse space).
+//
+// In the modes' own basis B (node i's 3 x 6 block [I, -[d_i]x], d_i its offset from its aggregate's
+// centroid) the correction is z_i += B_i y_a(i), y = W s with s_a = B_a^T r = (sum r_i, sum d_i x r_i)
+// over the aggregate's nodes and W = R Kc^-1 R^T (6 n_agg square, formed once on the host; R the
+// per-aggregate orthonormalisation with dropped modes).  Three launches per application:
+//   k_coarse_restrict  one CTA per aggregate, fixed-order block sums of its node list
+//   k_coarse_gemv      one warp per row of W (the one dense contraction: a bandwidth-bound GEMV)
+//   k_coarse_prolong   one thread per free node, z_i += u_a + w_a x d_i   ((u_a, w_a) = y_a)
+// All sums run in a fixed order, so the correction is bit-identical run to run.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "sfem_internal.h"
+
+namespace sfem {
+namespace {
+
+constexpr int kCT = 256;
+
+__device__ __forceinline__ double warp_sum_c(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// s_a (6 values) from the aggregate's nodes agg_node[agg_ptr[a] .. agg_ptr[a+1]) (free-node indices)
+__global__ void __launch_bounds__(kCT) k_coarse_restrict(const int32_t* __restrict__ agg_ptr,
+                                                         const int32_t* __restrict__ agg_node,
+                                                         const float4* __restrict__ d, const float* __restrict__ r,
+                                                         float* __restrict__ s) {
+  const int a = blockIdx.x;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = agg_ptr[a] + threadIdx.x; k < agg_ptr[a + 1]; k += kCT) {
+    const int i = agg_node[k];
+    const float4 di = d[i];
+    const float r0 = r[3 * (int64_t)i], r1 = r[3 * (int64_t)i + 1], r2 = r[3 * (int64_t)i + 2];
+    acc[0] += r0;
+    acc[1] += r1;
+    acc[2] += r2;
+    acc[3] += (double)(di.y * r2 - di.z * r1);
+    acc[4] += (double)(di.z * r0 - di.x * r2);
+    acc[5] += (double)(di.x * r1 - di.y * r0);
+  }
+  __shared__ double sm[6][kCT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 6; c++) {
+    const double v = warp_sum_c(acc[c]);
+    if (lane == 0) sm[c][w] = v;
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+      const double v = warp_sum_c(lane < kCT / 32 ? sm[c][lane] : 0.0);
+      if (lane == 0) s[6 * a + c] = (float)v;
+    }
+  }
+}
+
+// y = W s, W row-major nc x ld (FP32, ld a multiple of 4, zero beyond nc; s zero beyond nc), one warp
+// per row reading 16-byte column groups
+__global__ void __launch_bounds__(kCT) k_coarse_gemv(int nc, int ld, const float* __restrict__ W,
+                                                     const float* __restrict__ s, float* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int row = (int)((blockIdx.x * (int64_t)kCT + threadIdx.x) >> 5);
+  if (row >= nc) return;
+  const float4* Wr = reinterpret_cast<const float4*>(W + (int64_t)row * ld);
+  const float4* s4 = reinterpret_cast<const float4*>(s);
+  double acc = 0.0;
+  for (int c = lane; c < ld / 4; c += 32) {
+    const float4 wv = Wr[c], sv = s4[c];
+    acc += (double)(wv.x * sv.x + wv.y * sv.y + wv.z * sv.z + wv.w * sv.w);
+  }
+  acc = warp_sum_c(acc);
+  if (lane == 0) y[row] = (float)acc;
+}
+
+// z_i += u_a + w_a x d_i over the free nodes
+__global__ void __launch_bounds__(kCT) k_coarse_prolong(int64_t nf, const int32_t* __restrict__ aid,
+                                                        const float4* __restrict__ d, const float* __restrict__ y,
+                                                        float* __restrict__ z) {
+  for (int64_t i = (int64_t)blockIdx.x * kCT + threadIdx.x; i < nf; i += (int64_t)gridDim.x * kCT) {
+    const float* ya = y + 6 * (int64_t)aid[i];
+    const float4 di = d[i];
+    const float u0 = ya[0], u1 = ya[1], u2 = ya[2], w0 = ya[3], w1 = ya[4], w2 = ya[5];
+    z[3 * i] += u0 + (w1 * di.z - w2 * di.y);
+    z[3 * i + 1] += u1 + (w2 * di.x - w0 * di.z);
+    z[3 * i + 2] += u2 + (w0 * di.y - w1 * di.x);
+  }
+}
+
+}  // namespace
+
+void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st) {
+  count_launch();
+  k_coarse_restrict<<<cv.n_agg, kCT, 0, st>>>(cv.agg_ptr, cv.agg_node, cv.d, r, cv.s);
+  count_launch();
+  const int nc = 6 * cv.n_agg;
+  k_coarse_gemv<<<(unsigned)((nc * 32 + kCT - 1) / kCT), kCT, 0, st>>>(nc, cv.ld, cv.W, cv.s, cv.y);
+  count_launch();
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want = (cv.nf + kCT - 1) / kCT;
+  const unsigned grid = (unsigned)std::min<int64_t>(want > 0 ? want : 1, (int64_t)sms * 8);
+  k_coarse_prolong<<<grid, kCT, 0, st>>>(cv.nf, cv.aid, cv.d, cv.y, z);
+}
+
+}  // namespace sfem

@@ -124,6 +124,15 @@ struct sfem_handle {
   int bt_wait_test = 0;
   std::vector<int32_t> bt_iters_h, bt_status_h;
   std::vector<double> bt_rr_h, bt_bb_h;
+  // two-level preconditioner: the coarse-space correction of the learned flexible CG
+  bool cs_on = false;
+  int cs_n_agg = 0, cs_ld = 0;
+  int32_t *cs_agg_ptr = nullptr, *cs_agg_node = nullptr, *cs_aid = nullptr;
+  float4* cs_d = nullptr;
+  float *cs_W = nullptr, *cs_s = nullptr, *cs_y = nullptr;
+  CoarseView cv() const {
+    return CoarseView{cs_n_agg, cs_ld, nf, cs_agg_ptr, cs_agg_node, cs_aid, cs_d, cs_W, cs_s, cs_y};
+  }
   // node data (reshuffled, 3N)
   double *x0 = nullptr, *u = nullptr, *mass = nullptr, *fext = nullptr, *grav_d = nullptr;
   // dynamics (FemPhysicsMatrixFree mTimeStep, node vel, pos0 at the step start)
@@ -665,6 +674,7 @@ int upload_nodes(sfem_handle* h, const double* src, double* dst) {
 }
 
 void batch_release(sfem_handle* h);
+void coarse_release(sfem_handle* h);
 template <typename T>
 int batched_pcg(sfem_handle* h, const T* u, const T* rhs, KrylovWs<T>& w, const T* dinv, double tol, int max_it,
                 int* its);
@@ -917,6 +927,7 @@ int sfem_destroy(sfem_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   batch_release(h);
+  coarse_release(h);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
@@ -1082,9 +1093,9 @@ static int bsr_structure(sfem_handle* h) {
 extern "C++" {
 // rows [0, n) split over the host's threads
 template <typename F>
-static void parallel_rows(int64_t n, F&& f) {
+static void parallel_rows(int64_t n, F&& f, int64_t min_rows = 4096) {
   const int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-  if (nt == 1 || n < 4096) {
+  if (nt == 1 || n < min_rows) {
     f((int64_t)0, n);
     return;
   }
@@ -1451,6 +1462,250 @@ int sfem_set_operator(sfem_handle* h, int32_t op) {
     sell_release(h);
   }
   return SFEM_OK;
+}
+
+}  // extern "C"
+
+extern "C++" {
+// In-place Cholesky A = L L^T of a dense symmetric positive definite n x n matrix (row-major; L in
+// the lower triangle), right-looking in blocks of 64 with the panel and trailing updates split over
+// the host's threads.  False if a pivot is not positive.
+static bool cholesky_lower(std::vector<double>& A, int n) {
+  const int bs = 64;
+  for (int k0 = 0; k0 < n; k0 += bs) {
+    const int k1 = std::min(n, k0 + bs);
+    for (int k = k0; k < k1; k++) {
+      double d = A[(size_t)k * n + k];
+      for (int p = k0; p < k; p++) d -= A[(size_t)k * n + p] * A[(size_t)k * n + p];
+      if (!(d > 0.0) || !std::isfinite(d)) return false;
+      d = std::sqrt(d);
+      A[(size_t)k * n + k] = d;
+      for (int i = k + 1; i < k1; i++) {
+        double t = A[(size_t)i * n + k];
+        for (int p = k0; p < k; p++) t -= A[(size_t)i * n + p] * A[(size_t)k * n + p];
+        A[(size_t)i * n + k] = t / d;
+      }
+    }
+    parallel_rows(n - k1, [&](int64_t a, int64_t b) {
+      for (int64_t i = k1 + a; i < k1 + b; i++) {
+        double* Ai = &A[(size_t)i * n];
+        for (int k = k0; k < k1; k++) {
+          const double* Ak = &A[(size_t)k * n];
+          double t = Ai[k];
+          for (int p = k0; p < k; p++) t -= Ai[p] * Ak[p];
+          Ai[k] = t / Ak[k];
+        }
+        for (int64_t j = k1; j <= i; j++) {
+          const double* Aj = &A[(size_t)j * n];
+          double t = 0.0;
+          for (int p = k0; p < k1; p++) t += Ai[p] * Aj[p];
+          Ai[j] -= t;
+        }
+      }
+    }, 64);
+  }
+  return true;
+}
+}
+
+extern "C" {
+
+int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  TRY(sync(h));
+  coarse_release(h);
+  if (!(cell > 0.0)) return SFEM_OK;  // off
+  if (h->precision != SFEM_FP32) return fail(SFEM_ERR_INVALID, "the coarse space serves the FP32 flexible CG");
+  if (!(rtol >= 0.0)) return fail(SFEM_ERR_INVALID, "rtol >= 0");
+  const int64_t nf = h->nf, nbc = h->nbc;
+  if (nf == 0) return SFEM_OK;
+  // aggregates of the free nodes' rest positions and their rigid-body factors
+  std::vector<double> X((size_t)3 * nf);
+  CU(cudaMemcpyAsync(X.data(), h->x0 + 3 * nbc, X.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  std::vector<int32_t> aid((size_t)nf);
+  std::vector<double> d((size_t)3 * nf);
+  int64_t na = 0;
+  TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), nullptr, &na));
+  if (na > 4096) return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates (at most 4096)", (long long)na);
+  std::vector<double> R((size_t)36 * na);
+  TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
+  // the FP64 tangent at the rest state, as block CSR over the free nodes
+  std::vector<double> u_save((size_t)3 * h->N);
+  CU(cudaMemcpyAsync(u_save.data(), h->u, u_save.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemsetAsync(h->u, 0, u_save.size() * sizeof(double), h->stream));
+  const int ast = bsr_assemble(h);
+  CU(cudaMemcpyAsync(h->u, u_save.data(), u_save.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TRY(sync(h));
+  TRY(ast);
+  std::vector<int32_t> rowptr((size_t)nf + 1), col((size_t)h->bsr_nnzb);
+  std::vector<double> vals((size_t)9 * h->bsr_nnzb);
+  CU(cudaMemcpyAsync(rowptr.data(), h->bsr_rowptr, rowptr.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(col.data(), h->bsr_col, col.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(vals.data(), h->bsr_vals, vals.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  // kept (non-zero) columns of every R_a and their positions in the compact coarse index
+  std::vector<std::vector<int>> kc((size_t)na);
+  std::vector<int> first((size_t)na + 1, 0);
+  for (int64_t a = 0; a < na; a++) {
+    for (int c = 0; c < 6; c++) {
+      double nz = 0.0;
+      for (int r = 0; r < 6; r++) nz += std::fabs(R[36 * a + 6 * r + c]);
+      if (nz > 0.0) kc[a].push_back(c);
+    }
+    first[a + 1] = first[a] + (int)kc[a].size();
+  }
+  const int nk = first[na];
+  // aggregate node lists (free-node indices, increasing)
+  std::vector<int32_t> aptr((size_t)na + 1, 0), anode((size_t)nf);
+  for (int64_t i = 0; i < nf; i++) aptr[aid[i] + 1]++;
+  for (int64_t a = 0; a < na; a++) aptr[a + 1] += aptr[a];
+  {
+    std::vector<int32_t> fill(aptr.begin(), aptr.end() - 1);
+    for (int64_t i = 0; i < nf; i++) anode[fill[aid[i]]++] = (int32_t)i;
+  }
+  // Kc = R^T (B^T K B) R by aggregate pairs: row aggregate a sums B_i^T K_ij B_j over its nodes i
+  // and their blocks j in a fixed order (one thread per aggregate row: deterministic)
+  std::vector<double> Kc((size_t)nk * nk, 0.0);
+  auto Bmat = [&](int64_t i, double (&B)[3][6]) {  // [I, -[d]x]: columns e_c and e_k x d
+    const double* di = &d[3 * i];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 6; c++) B[r][c] = (c == r) ? 1.0 : 0.0;
+    B[1][3] = -di[2]; B[2][3] = di[1];
+    B[2][4] = -di[0]; B[0][4] = di[2];
+    B[0][5] = -di[1]; B[1][5] = di[0];
+  };
+  parallel_rows(na, [&](int64_t a0, int64_t a1) {
+    std::vector<int> slot((size_t)na, -1);
+    std::vector<int> touched;
+    std::vector<double> G;
+    for (int64_t a = a0; a < a1; a++) {
+      touched.clear();
+      G.clear();
+      for (int32_t k = aptr[a]; k < aptr[a + 1]; k++) {
+        const int64_t i = anode[k];
+        double Bi[3][6];
+        Bmat(i, Bi);
+        for (int32_t e = rowptr[i]; e < rowptr[i + 1]; e++) {
+          const int64_t j = col[e];
+          const int b = aid[j];
+          if (slot[b] < 0) {
+            slot[b] = (int)touched.size();
+            touched.push_back(b);
+            G.resize(G.size() + 36, 0.0);
+          }
+          double Bj[3][6], KB[3][6];
+          Bmat(j, Bj);
+          const double* Kij = &vals[9 * (size_t)e];
+          for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 6; c++) KB[r][c] = Kij[3 * r] * Bj[0][c] + Kij[3 * r + 1] * Bj[1][c] + Kij[3 * r + 2] * Bj[2][c];
+          double* g = &G[36 * (size_t)slot[b]];
+          for (int x = 0; x < 6; x++)
+            for (int c = 0; c < 6; c++) g[6 * x + c] += Bi[0][x] * KB[0][c] + Bi[1][x] * KB[1][c] + Bi[2][x] * KB[2][c];
+        }
+      }
+      for (size_t t = 0; t < touched.size(); t++) {
+        const int b = touched[t];
+        const double* g = &G[36 * t];
+        const double* Ra = &R[36 * a];
+        const double* Rb = &R[36 * (size_t)b];
+        for (size_t p = 0; p < kc[a].size(); p++)
+          for (size_t q = 0; q < kc[b].size(); q++) {
+            double v = 0.0;
+            for (int x = 0; x < 6; x++)
+              for (int y = 0; y < 6; y++) v += Ra[6 * x + kc[a][p]] * g[6 * x + y] * Rb[6 * y + kc[b][q]];
+            Kc[(size_t)(first[a] + p) * nk + first[b] + q] = v;
+          }
+        slot[b] = -1;
+      }
+    }
+  }, 1);
+  // Kc^-1 by Cholesky, one column per task (forward then backward substitution)
+  if (!cholesky_lower(Kc, nk)) return fail(SFEM_ERR_INVALID, "the coarse matrix is not positive definite");
+  std::vector<double> U((size_t)nk * nk);  // L^T, row-major, for contiguous backward substitution
+  for (int i = 0; i < nk; i++)
+    for (int j = 0; j <= i; j++) U[(size_t)j * nk + i] = Kc[(size_t)i * nk + j];
+  std::vector<double> Kinv((size_t)nk * nk);
+  parallel_rows(nk, [&](int64_t c0, int64_t c1) {
+    std::vector<double> y((size_t)nk);
+    for (int64_t c = c0; c < c1; c++) {
+      std::fill(y.begin(), y.end(), 0.0);
+      for (int64_t i = c; i < nk; i++) {  // L y = e_c (zero above c)
+        double t = i == c ? 1.0 : 0.0;
+        const double* Li = &Kc[(size_t)i * nk];
+        for (int64_t p = c; p < i; p++) t -= Li[p] * y[p];
+        y[i] = t / Li[i];
+      }
+      for (int64_t i = nk - 1; i >= 0; i--) {  // L^T x = y
+        const double* Ui = &U[(size_t)i * nk];
+        double t = y[i];
+        for (int64_t p = i + 1; p < nk; p++) t -= Ui[p] * y[p];
+        y[i] = t / Ui[i];
+      }
+      for (int64_t i = 0; i < nk; i++) Kinv[(size_t)i * nk + c] = y[i];
+    }
+  }, 16);
+  // W = R Kc^-1 R^T in the modes' basis (6 n_agg square, rows padded to a multiple of 4)
+  const int nc = (int)(6 * na), ld = (nc + 3) / 4 * 4;
+  std::vector<float> W((size_t)nc * ld, 0.f);
+  parallel_rows(na, [&](int64_t a0, int64_t a1) {
+    for (int64_t a = a0; a < a1; a++)
+      for (int64_t b = 0; b < na; b++) {
+        const double* Ra = &R[36 * a];
+        const double* Rb = &R[36 * b];
+        for (int x = 0; x < 6; x++)
+          for (int y = 0; y < 6; y++) {
+            double v = 0.0;
+            for (size_t p = 0; p < kc[a].size(); p++) {
+              const double rx = Ra[6 * x + kc[a][p]];
+              if (rx == 0.0) continue;
+              const double* Ki = &Kinv[(size_t)(first[a] + p) * nk + first[b]];
+              for (size_t q = 0; q < kc[b].size(); q++) v += rx * Ki[q] * Rb[6 * y + kc[b][q]];
+            }
+            W[(size_t)(6 * a + x) * ld + 6 * b + y] = (float)v;
+          }
+      }
+  }, 1);
+  // device copies
+  std::vector<float4> d4((size_t)nf);
+  for (int64_t i = 0; i < nf; i++) d4[i] = make_float4((float)d[3 * i], (float)d[3 * i + 1], (float)d[3 * i + 2], 0.f);
+  TRY(dalloc(&h->cs_agg_ptr, aptr.size()));
+  TRY(dalloc(&h->cs_agg_node, anode.size()));
+  TRY(dalloc(&h->cs_aid, aid.size()));
+  TRY(dalloc(&h->cs_d, d4.size()));
+  TRY(dalloc(&h->cs_W, W.size()));
+  TRY(dalloc(&h->cs_s, (size_t)ld));
+  TRY(dalloc(&h->cs_y, (size_t)ld));
+  CU(cudaMemcpyAsync(h->cs_agg_ptr, aptr.data(), aptr.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_agg_node, anode.data(), anode.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_aid, aid.data(), aid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_d, d4.data(), d4.size() * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_W, W.data(), W.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemsetAsync(h->cs_s, 0, (size_t)ld * 4, h->stream));
+  CU(cudaMemsetAsync(h->cs_y, 0, (size_t)ld * 4, h->stream));
+  TRY(sync(h));
+  h->cs_n_agg = (int)na;
+  h->cs_ld = ld;
+  h->cs_on = true;
+  return SFEM_OK;
+}
+
+int sfem_coarse_apply(sfem_handle* h, const double* r, double* z) {
+  TRY(check_handle(h));
+  TRY(set_device(h));
+  if (!r || !z) return fail(SFEM_ERR_INVALID, "null");
+  if (!h->cs_on) return fail(SFEM_ERR_INVALID, "no coarse space (sfem_set_coarse_space)");
+  const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
+  TRY(alloc_ws(h, h->k32));
+  KrylovWs<float>& w = h->k32;
+  CU(cudaMemcpyAsync(h->tmp64 + o, r, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_convert<double, float>((int64_t)n, h->tmp64 + o, w.b + o, h->stream);
+  CU(cudaMemsetAsync(w.q + o, 0, n * sizeof(float), h->stream));
+  launch_coarse_apply(h->cv(), w.b + o, w.q + o, h->stream);
+  launch_convert<float, double>((int64_t)n, w.q + o, h->tmp64 + o, h->stream);
+  CU(cudaMemcpyAsync(z, h->tmp64 + o, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
 }
 
 int sfem_set_newton_trace(sfem_handle* h, double* trace, int32_t cap, int32_t* count) {
@@ -2122,6 +2377,17 @@ void batch_release(sfem_handle* h) {
   h->bt_done = h->bt_iters = h->bt_err = nullptr;
   h->bt_bar = nullptr;
   h->bt_ntiles = 0;
+}
+
+void coarse_release(sfem_handle* h) {
+  void* bufs[] = {h->cs_agg_ptr, h->cs_agg_node, h->cs_aid, h->cs_d, h->cs_W, h->cs_s, h->cs_y};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  h->cs_agg_ptr = h->cs_agg_node = h->cs_aid = nullptr;
+  h->cs_d = nullptr;
+  h->cs_W = h->cs_s = h->cs_y = nullptr;
+  h->cs_on = false;
+  h->cs_n_agg = h->cs_ld = 0;
 }
 
 // The instances' PCG solves of K x = rhs, each with its own recurrence and tolerance, in one
@@ -2853,6 +3119,18 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   // the polynomial's input rows D^-1/2 r, formed by the update kernel from the second pass on
   float4* xs = g->infer_mode == 0 ? g->px : nullptr;
   auto precondition = [&](bool with_beta) {
+    if (h->cs_on) {
+      // two-level: z = M(r) + P Kc^-1 P^T r, then beta and z.r from the complete z
+      if (g->infer_mode == 0)
+        gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->z + o, done,
+                               h->stream, nullptr, g->bpart, h->counter, nullptr, with_beta);
+      else
+        gnn::launch_apply(g->graph(), w.r + o, dinv, g->params, g->Wb, g->h, g->z + o, done, h->stream);
+      launch_coarse_apply(h->cv(), w.r + o, g->z + o, h->stream);
+      if (with_beta)
+        gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, dinv, part, h->counter, h->scal, h->stream);
+      return;
+    }
     if (g->infer_mode == 0) {
       gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->z + o, done,
                              h->stream, with_beta ? g->rprev + o : nullptr, g->bpart, h->counter,

@@ -252,6 +252,24 @@ void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_
                       const int64_t* lbase, const int32_t* lcol, const int16_t* lcol16, const int32_t* lslot,
                       const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st,
                       const T* r = nullptr, const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
+// ---- coarse-space correction of the two-level preconditioner (sfem_coarse_kernels.cu) ----
+// z += B W B^T r over the free block: aggregates' node lists (agg_ptr / agg_node, free-node indices),
+// per free node its aggregate and offset d_i from the aggregate's centroid (x, y, z, 0), W the
+// 6 n_agg square FP32 matrix R Kc^-1 R^T, s and y two 6 n_agg scratch vectors
+struct CoarseView {
+  int n_agg;
+  int ld;  // row stride of W: 6 n_agg rounded up to a multiple of 4
+  int64_t nf;
+  const int32_t* agg_ptr;
+  const int32_t* agg_node;
+  const int32_t* aid;
+  const float4* d;
+  const float* W;
+  float* s;
+  float* y;
+};
+void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st);
+
 // ---- batched independent bodies: one persistent kernel per Krylov solve ----
 // Each instance (body) runs its own preconditioned CG recurrence (its own alpha, beta, r.z and
 // convergence test: SolveConjugateGradientMF, Math/IterativeSolvers.h:115-195, per body) inside one

@@ -182,6 +182,18 @@ class FemPhysicsMatrixFree:
         o = np.ascontiguousarray(node_offsets, dtype=np.int64)
         nat.check(self._lib.sfem_set_instances(self._h, o.size - 1, o.ctypes.data_as(nat._i64p)))
 
+    def set_coarse_space(self, cell, rtol=1e-8):
+        """Two-level learned preconditioner: add the coarse correction P Kc^-1 P^T r of grid-cell
+        aggregates of spacing `cell` (rest-state tangent, set up once); cell <= 0 turns it off."""
+        nat.check(self._lib.sfem_set_coarse_space(self._h, float(cell), float(rtol)))
+
+    def coarse_apply(self, r):
+        """P Kc^-1 P^T r (free DOFs, (N_f, 3))."""
+        r = _f64(r).reshape(-1, 3)
+        z = np.zeros_like(r)
+        nat.check(self._lib.sfem_coarse_apply(self._h, _dp(r), _dp(z)))
+        return z
+
     def set_batched_pcg(self, per_instance=True):
         """Krylov solves with instances: every instance's own PCG in one persistent launch (True) or one
         recurrence over all instances (False)."""
