@@ -296,6 +296,7 @@ def run_gpu_arm(args):
     p32 = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision="fp32", **kw)
     p32.set_operator(args.operator)
     method = "jacobi"
+    coarse_setup_s = None
     weights = args.weights if args.weights else os.path.join(ROOT, "solidfem_gb300", "data", "gnn_slab.bin")
     if args.precond in ("learned", "auto") and os.path.exists(weights):
         from solidfem_gb300.learned import LearnedPreconditioner
@@ -303,11 +304,18 @@ def run_gpu_arm(args):
         net = LearnedPreconditioner(p32)
         net.load(weights)
         method = "learned"
+        if args.coarse_cells > 0:
+            # two-level: the coarse space of cells of coarse_cells hexes, set up once per mesh
+            # (rest-state tangent) like the network's weights, outside the timed solves
+            t_cs = time.perf_counter()
+            p32.set_coarse_space(args.coarse_cells * EXTENT[0] / dims[0])
+            coarse_setup_s = time.perf_counter() - t_cs
+            method = "learned+coarse"
     elif args.precond == "learned":
         raise SystemExit(f"no trained weights at {weights}")
     from solidfem_gb300 import PC_JACOBI, PC_LEARNED
 
-    main_pc = PC_LEARNED if method == "learned" else PC_JACOBI
+    main_pc = PC_LEARNED if method.startswith("learned") else PC_JACOBI
     rest = p32.get_free_positions()
     nf = p32.n_free
     # stage every step's inputs in HBM before the timed region (device-pointer API)
@@ -382,7 +390,8 @@ def run_gpu_arm(args):
     # and per free node z, p_old in and p, q out), reported beside the unit above
     achieved_own = prof["algo_bytes_hvp"] / (ms * 1e-3) / 1e9 if prof["samples"] else None
     if args.operator == "assembled":
-        kernel = "k_sell_hvp<float> (tangent assembled per Newton step, sliced-ELL sparse product)"
+        kernel = ("k_ssell_hvp<float> (symmetric tangent assembled per Newton step: diagonal and upper blocks in "
+                  "sliced ELL, lower blocks read transposed from their mirror rows)")
         # DRAM bytes per launch: an ncu capture of the 3,145,728-tet case, scaled by the streamed bytes
         traffic = args.traffic if args.traffic else SELL_DRAM_PER_ALGO_BYTE * prof["algo_bytes_hvp"]
         traffic_source = ("ncu capture at 3,145,728 tets scaled by the streamed bytes" if not args.traffic
@@ -396,7 +405,7 @@ def run_gpu_arm(args):
     # Jacobi-PCG FP32 of the first timed load (what the learned preconditioner replaces)
     s_ref = seeds[args.warmup]
     st_j32 = None
-    if method == "learned":
+    if method.startswith("learned"):
         st_j32 = solve(p32, s_ref, PC_JACOBI)
     # the main method on the first timed load again: its equilibrium for the oracle and FP64 checks
     st_main = solve(p32, s_ref)
@@ -461,8 +470,12 @@ def run_gpu_arm(args):
             "config": {
                 "workload": WORKLOAD if dims == DIMS else f"reduced {dims} variant of: " + WORKLOAD,
                 "method": ("inexact Newton (Eisenstat-Walker), " +
-                           ("learned-preconditioner flexible PCG" if method == "learned" else "Jacobi-PCG") +
+                           {"learned": "learned-preconditioner flexible PCG",
+                            "learned+coarse": "two-level (learned + rigid-body coarse space) flexible PCG",
+                            "jacobi": "Jacobi-PCG"}[method] +
                            " inner solves in FP32, FP64 residual and convergence test"),
+                "coarse_cells": args.coarse_cells if method == "learned+coarse" else None,
+                "coarse_setup_s": coarse_setup_s,
                 "operator": args.operator,
                 "preconditioner": method, "l2": "inputs larger than L2 (element data 0.35 GB FP32)",
                 "converged": ok, "newton_iters": [s_["newton_iters"] for s_ in stats],
@@ -672,6 +685,8 @@ def main():
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per HVP launch, if captured")
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")
+    ap.add_argument("--coarse-cells", type=int, default=0,
+                    help="two-level preconditioner: coarse-space cells of this many hexes per axis (0: off)")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")
     ap.add_argument("--operator", default="assembled", choices=["matrix-free", "assembled"],
                     help="operator of the FP32 Krylov solves: the tangent assembled per Newton step "

@@ -1486,6 +1486,7 @@ static bool cholesky_lower(std::vector<double>& A, int n) {
         A[(size_t)i * n + k] = t / d;
       }
     }
+    // the panel below the diagonal block, then (all of it known) the trailing update
     parallel_rows(n - k1, [&](int64_t a, int64_t b) {
       for (int64_t i = k1 + a; i < k1 + b; i++) {
         double* Ai = &A[(size_t)i * n];
@@ -1495,6 +1496,11 @@ static bool cholesky_lower(std::vector<double>& A, int n) {
           for (int p = k0; p < k; p++) t -= Ai[p] * Ak[p];
           Ai[k] = t / Ak[k];
         }
+      }
+    }, 64);
+    parallel_rows(n - k1, [&](int64_t a, int64_t b) {
+      for (int64_t i = k1 + a; i < k1 + b; i++) {
+        double* Ai = &A[(size_t)i * n];
         for (int64_t j = k1; j <= i; j++) {
           const double* Aj = &A[(size_t)j * n];
           double t = 0.0;
@@ -1528,7 +1534,8 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   std::vector<double> d((size_t)3 * nf);
   int64_t na = 0;
   TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), nullptr, &na));
-  if (na > 4096) return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates (at most 4096)", (long long)na);
+  // the dense factorisation costs ~(6 n_agg)^3 flops on the host: at most 1024 aggregates
+  if (na > 1024) return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates (at most 1024)", (long long)na);
   std::vector<double> R((size_t)36 * na);
   TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
   // the FP64 tangent at the rest state, as block CSR over the free nodes

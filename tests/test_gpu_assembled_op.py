@@ -233,7 +233,9 @@ def test_randomly_numbered_mesh_fp64_assembled():
     x_as, st_as = p.pcg(b, rel_tol=1e-10, max_iters=50000)
     prof = p.get_profile()
     p.set_profiling(False)
-    col_bytes = (prof["algo_bytes_hvp"] - 96.0 * p.n_free) / len(rows) - 72.0
+    # stored blocks: 72 B of values + c B of column; lower blocks: c B of column + a 4 B mirror slot
+    n_up, n_low = (len(rows) + p.n_free) // 2, (len(rows) - p.n_free) // 2
+    col_bytes = (prof["algo_bytes_hvp"] - 96.0 * p.n_free - 72.0 * n_up - 4.0 * n_low) / (n_up + n_low)
     print(f"FP64 PCG {st_mf['iters']} / {st_as['iters']}, column bytes {col_bytes:.3f}, "
           f"rel diff {rel(x_as, x_mf):.2e}")
     assert abs(col_bytes - 4.0) < 1e-6
