@@ -1320,7 +1320,7 @@ template void launch_sell_hvp<double>(int64_t, int64_t, const int64_t*, const in
 // from HBM once and its mirror read, by a row up to the mesh's bandwidth away processed at about the
 // same time, hits L2.  DIR and the p.q / alpha finish as in k_sell_hvp.
 template <typename T, bool DIR, typename CI>
-__global__ void __launch_bounds__(kThreads, 5) k_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
+__global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
                                                         const CI* __restrict__ col, const int64_t* __restrict__ lbase,
                                                         const CI* __restrict__ lcol, const int32_t* __restrict__ lslot,
                                                         const T* __restrict__ vals, const T* __restrict__ p,
