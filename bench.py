@@ -56,10 +56,10 @@ FP64_JACOBI_COUNTS = {"newton_iters": 5, "cg_iters": 10166, "residual_evals": 6}
 
 
 HVP_DRAM_BYTES_PER_TET = 220.1e6 / 3145728  # k_patch_hvp<float, NH, DIR> (ncu, see the traffic note below)
-# k_sell_hvp<float, DIR> (16-bit columns): ncu dram__bytes_read.sum + dram__bytes_write.sum on the 128x64x64
-# case, 317.0 + 7.1 MB per launch (mean of two), against its 325.3 MB of algorithmic bytes
-# (7,884,222 blocks x 38 B + 536,640 free nodes x 48 B)
-SELL_DRAM_PER_ALGO_BYTE = (317.02e6 + 7.12e6) / 325.2855e6
+# k_ssell_hvp<float, DIR> (symmetric tangent, 16-bit columns, mirror slots): ncu dram__bytes_read.sum +
+# dram__bytes_write.sum on the 128x64x64 case, 196.95 + 10.41 MB per launch, against the 207.80 MB the
+# launch streams (stored blocks x 38 B + lower entries x 6 B + free nodes x 48 B)
+SELL_DRAM_PER_ALGO_BYTE = (196.95e6 + 10.41e6) / 207.797844e6
 
 
 def peaks():

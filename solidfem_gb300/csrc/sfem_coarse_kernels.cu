@@ -6,9 +6,10 @@
 // centroid) the correction is z_i += B_i y_a(i), y = W s with s_a = B_a^T r = (sum r_i, sum d_i x r_i)
 // over the aggregate's nodes and W = R Kc^-1 R^T (6 n_agg square, formed once on the host; R the
 // per-aggregate orthonormalisation with dropped modes).  Three launches per application:
-//   k_coarse_restrict  one CTA per aggregate, fixed-order block sums of its node list
+//   k_coarse_restrict  one CTA per chunk of <= 256 nodes of an aggregate, fixed-order sums
 //   k_coarse_gemv      one warp per row of W (the one dense contraction: a bandwidth-bound GEMV)
-//   k_coarse_prolong   one thread per free node, z_i += u_a + w_a x d_i   ((u_a, w_a) = y_a)
+//   k_coarse_prolong   one thread per free node, z_i += u_a + w_a x d_i   ((u_a, w_a) = y_a); inside the
+//                      flexible CG the learned preconditioner's last pass adds this term instead
 // All sums run in a fixed order, so the correction is bit-identical run to run.
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -28,39 +29,55 @@ __device__ __forceinline__ double warp_sum_c(double v) {
   return v;
 }
 
-// s_a (6 values) from the aggregate's nodes agg_node[agg_ptr[a] .. agg_ptr[a+1]) (free-node indices)
-__global__ void __launch_bounds__(kCT) k_coarse_restrict(const int32_t* __restrict__ agg_ptr,
-                                                         const int32_t* __restrict__ agg_node,
-                                                         const float4* __restrict__ d, const float* __restrict__ r,
-                                                         float* __restrict__ s) {
-  const int a = blockIdx.x;
+// s_a = (sum r_i, sum d_i x r_i) over aggregate a's nodes: one CTA per chunk of at most 256 nodes of
+// one aggregate (one node per thread), the chunk's six sums to cpart; the aggregate's last chunk to
+// finish adds its chunks' sums in chunk order (a fixed order, so s is the same on every run) and
+// resets the aggregate's counter
+__global__ void __launch_bounds__(kCT) k_coarse_restrict(CoarseView cv, const float* __restrict__ r) {
+  const int c = blockIdx.x;
+  const int a = cv.chunk_agg[c];
   double acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int k = agg_ptr[a] + threadIdx.x; k < agg_ptr[a + 1]; k += kCT) {
-    const int i = agg_node[k];
-    const float4 di = d[i];
+  if ((int)threadIdx.x < cv.chunk_cnt[c]) {
+    const int i = cv.agg_node[cv.chunk_start[c] + threadIdx.x];
+    const float4 di = cv.d[i];
     const float r0 = r[3 * (int64_t)i], r1 = r[3 * (int64_t)i + 1], r2 = r[3 * (int64_t)i + 2];
-    acc[0] += r0;
-    acc[1] += r1;
-    acc[2] += r2;
-    acc[3] += (double)(di.y * r2 - di.z * r1);
-    acc[4] += (double)(di.z * r0 - di.x * r2);
-    acc[5] += (double)(di.x * r1 - di.y * r0);
+    acc[0] = r0;
+    acc[1] = r1;
+    acc[2] = r2;
+    acc[3] = (double)(di.y * r2 - di.z * r1);
+    acc[4] = (double)(di.z * r0 - di.x * r2);
+    acc[5] = (double)(di.x * r1 - di.y * r0);
   }
   __shared__ double sm[6][kCT / 32];
+  __shared__ bool is_last;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int c = 0; c < 6; c++) {
-    const double v = warp_sum_c(acc[c]);
-    if (lane == 0) sm[c][w] = v;
+  for (int k = 0; k < 6; k++) {
+    const double v = warp_sum_c(acc[k]);
+    if (lane == 0) sm[k][w] = v;
   }
   __syncthreads();
   if (w == 0) {
 #pragma unroll
-    for (int c = 0; c < 6; c++) {
-      const double v = warp_sum_c(lane < kCT / 32 ? sm[c][lane] : 0.0);
-      if (lane == 0) s[6 * a + c] = (float)v;
+    for (int k = 0; k < 6; k++) {
+      const double v = warp_sum_c(lane < kCT / 32 ? sm[k][lane] : 0.0);
+      if (lane == 0) cv.cpart[6 * (int64_t)c + k] = v;
+    }
+    if (lane == 0) {
+      __threadfence();
+      const unsigned n = (unsigned)(cv.agg_chunk[a + 1] - cv.agg_chunk[a]);
+      is_last = atomicAdd(cv.ccount + a, 1u) == n - 1;
     }
   }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (threadIdx.x < 6) {
+    double v = 0.0;
+    for (int k = cv.agg_chunk[a]; k < cv.agg_chunk[a + 1]; k++) v += __ldcg(cv.cpart + 6 * (int64_t)k + threadIdx.x);
+    cv.s[6 * a + threadIdx.x] = (float)v;
+  }
+  if (threadIdx.x == 0) cv.ccount[a] = 0u;
 }
 
 // y = W s, W row-major nc x ld (FP32, ld a multiple of 4, zero beyond nc; s zero beyond nc), one warp
@@ -97,12 +114,16 @@ __global__ void __launch_bounds__(kCT) k_coarse_prolong(int64_t nf, const int32_
 
 }  // namespace
 
-void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st) {
+void launch_coarse_restrict_gemv(const CoarseView& cv, const float* r, cudaStream_t st) {
   count_launch();
-  k_coarse_restrict<<<cv.n_agg, kCT, 0, st>>>(cv.agg_ptr, cv.agg_node, cv.d, r, cv.s);
+  k_coarse_restrict<<<cv.n_chunks, kCT, 0, st>>>(cv, r);
   count_launch();
   const int nc = 6 * cv.n_agg;
   k_coarse_gemv<<<(unsigned)((nc * 32 + kCT - 1) / kCT), kCT, 0, st>>>(nc, cv.ld, cv.W, cv.s, cv.y);
+}
+
+void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st) {
+  launch_coarse_restrict_gemv(cv, r, st);
   count_launch();
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);

@@ -78,7 +78,7 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float4* x4, float4* y1,
                        float4* y2, float4* w, float* out, const int* done, cudaStream_t st, const float* rprev,
-                       float* partials, unsigned* counter, CgScalars* s, bool x_ready) {
+                       float* partials, unsigned* counter, CgScalars* s, bool x_ready, CoarseAdd ca) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
   // grid-stride passes sized to one resident wave (no partly filled last wave; the BETA pass
   // then finishes with one block partial per resident CTA, 4 values each)
@@ -103,10 +103,10 @@ void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const 
   const int grid_last = std::min(blocks, wave_last);
   if (s)
     launch_pdl(k_poly_last<true>, grid_last, 256, 0, st, g, y2, w, r, dinv, pc.c, out, done, rprev, partials, counter,
-               s);
+               s, ca);
   else
     launch_pdl(k_poly_last<false>, grid_last, 256, 0, st, g, y2, w, r, dinv, pc.c, out, done, nullptr, nullptr,
-               nullptr, nullptr);
+               nullptr, nullptr, ca);
 }
 
 // the training forward: activations h0..h3 of S at x (kept, with x), then S^T through the

@@ -757,7 +757,8 @@ __global__ void __launch_bounds__(256) k_poly_last(Graph g, const float4* __rest
                                                    const float4* __restrict__ w0, const float* __restrict__ r,
                                                    const float* __restrict__ dinv, float cc, float* __restrict__ out,
                                                    const int* done, const float* __restrict__ rprev,
-                                                   float* __restrict__ partials, unsigned* counter, CgScalars* s) {
+                                                   float* __restrict__ partials, unsigned* counter, CgScalars* s,
+                                                   CoarseAdd ca) {
   pdl_wait();
   pdl_launch_dependents();
   if (done && *done) return;
@@ -766,11 +767,20 @@ __global__ void __launch_bounds__(256) k_poly_last(Graph g, const float4* __rest
     const float3 a = node_gather4(g, i, ud);
     const float4 wa = w0[i];
     const float v[3] = {a.x + wa.x, a.y + wa.y, a.z + wa.z};
+    // two-level: the coarse correction u_a + w_a x d_i of the node's aggregate
+    float cz[3] = {0.f, 0.f, 0.f};
+    if (ca.aid) {
+      const float* ya = ca.y + 6 * (int64_t)ca.aid[i];
+      const float4 di = ca.d[i];
+      cz[0] = ya[0] + (ya[4] * di.z - ya[5] * di.y);
+      cz[1] = ya[1] + (ya[5] * di.x - ya[3] * di.z);
+      cz[2] = ya[2] + (ya[3] * di.y - ya[4] * di.x);
+    }
     const int64_t o = 3 * i;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const float d = dinv[o + c], ri = r[o + c];
-      const float z = cc * d * ri + sqrtf(d) * v[c];
+      const float z = cc * d * ri + sqrtf(d) * v[c] + cz[c];
       out[o + c] = z;
       if (BETA) {
         const float dr = ri - rprev[o + c], zj = d * ri;

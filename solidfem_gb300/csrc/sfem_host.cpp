@@ -130,8 +130,14 @@ struct sfem_handle {
   int32_t *cs_agg_ptr = nullptr, *cs_agg_node = nullptr, *cs_aid = nullptr;
   float4* cs_d = nullptr;
   float *cs_W = nullptr, *cs_s = nullptr, *cs_y = nullptr;
+  int cs_n_chunks = 0;
+  int32_t *cs_chunk_start = nullptr, *cs_chunk_cnt = nullptr, *cs_chunk_agg = nullptr, *cs_agg_chunk = nullptr;
+  double* cs_cpart = nullptr;
+  unsigned* cs_ccount = nullptr;
   CoarseView cv() const {
-    return CoarseView{cs_n_agg, cs_ld, nf, cs_agg_ptr, cs_agg_node, cs_aid, cs_d, cs_W, cs_s, cs_y};
+    return CoarseView{cs_n_agg,       cs_ld,        nf,           cs_agg_ptr,     cs_agg_node,    cs_aid,
+                      cs_d,           cs_W,         cs_s,         cs_y,           cs_n_chunks,    cs_chunk_start,
+                      cs_chunk_cnt,   cs_chunk_agg, cs_agg_chunk, cs_cpart,       cs_ccount};
   }
   // node data (reshuffled, 3N)
   double *x0 = nullptr, *u = nullptr, *mass = nullptr, *fext = nullptr, *grav_d = nullptr;
@@ -1674,6 +1680,16 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
           }
       }
   }, 1);
+  // restriction chunks: at most 256 nodes of one aggregate's list each
+  std::vector<int32_t> cstart, ccnt, cagg, achunk((size_t)na + 1, 0);
+  for (int64_t a = 0; a < na; a++) {
+    for (int32_t k = aptr[a]; k < aptr[a + 1]; k += 256) {
+      cstart.push_back(k);
+      ccnt.push_back(std::min<int32_t>(256, aptr[a + 1] - k));
+      cagg.push_back((int32_t)a);
+    }
+    achunk[a + 1] = (int32_t)cstart.size();
+  }
   // device copies
   std::vector<float4> d4((size_t)nf);
   for (int64_t i = 0; i < nf; i++) d4[i] = make_float4((float)d[3 * i], (float)d[3 * i + 1], (float)d[3 * i + 2], 0.f);
@@ -1691,6 +1707,19 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   CU(cudaMemcpyAsync(h->cs_W, W.data(), W.size() * 4, cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(h->cs_s, 0, (size_t)ld * 4, h->stream));
   CU(cudaMemsetAsync(h->cs_y, 0, (size_t)ld * 4, h->stream));
+  const size_t nch = cstart.size();
+  TRY(dalloc(&h->cs_chunk_start, nch));
+  TRY(dalloc(&h->cs_chunk_cnt, nch));
+  TRY(dalloc(&h->cs_chunk_agg, nch));
+  TRY(dalloc(&h->cs_agg_chunk, achunk.size()));
+  TRY(dalloc(&h->cs_cpart, 6 * nch));
+  TRY(dalloc(&h->cs_ccount, (size_t)na));
+  CU(cudaMemcpyAsync(h->cs_chunk_start, cstart.data(), nch * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_chunk_cnt, ccnt.data(), nch * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_chunk_agg, cagg.data(), nch * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_agg_chunk, achunk.data(), achunk.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemsetAsync(h->cs_ccount, 0, (size_t)na * sizeof(unsigned), h->stream));
+  h->cs_n_chunks = (int)nch;
   TRY(sync(h));
   h->cs_n_agg = (int)na;
   h->cs_ld = ld;
@@ -2387,9 +2416,15 @@ void batch_release(sfem_handle* h) {
 }
 
 void coarse_release(sfem_handle* h) {
-  void* bufs[] = {h->cs_agg_ptr, h->cs_agg_node, h->cs_aid, h->cs_d, h->cs_W, h->cs_s, h->cs_y};
+  void* bufs[] = {h->cs_agg_ptr,     h->cs_agg_node,  h->cs_aid,       h->cs_d,        h->cs_W,
+                  h->cs_s,          h->cs_y,         h->cs_chunk_start, h->cs_chunk_cnt, h->cs_chunk_agg,
+                  h->cs_agg_chunk,  h->cs_cpart,     h->cs_ccount};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  h->cs_chunk_start = h->cs_chunk_cnt = h->cs_chunk_agg = h->cs_agg_chunk = nullptr;
+  h->cs_cpart = nullptr;
+  h->cs_ccount = nullptr;
+  h->cs_n_chunks = 0;
   h->cs_agg_ptr = h->cs_agg_node = h->cs_aid = nullptr;
   h->cs_d = nullptr;
   h->cs_W = h->cs_s = h->cs_y = nullptr;
@@ -3126,13 +3161,17 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   // the polynomial's input rows D^-1/2 r, formed by the update kernel from the second pass on
   float4* xs = g->infer_mode == 0 ? g->px : nullptr;
   auto precondition = [&](bool with_beta) {
+    if (h->cs_on && g->infer_mode == 0) {
+      // two-level: y = W B^T r, then the polynomial's last pass adds B y to M(r) and forms beta, z.r
+      launch_coarse_restrict_gemv(h->cv(), w.r + o, h->stream);
+      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->z + o, done,
+                             h->stream, with_beta ? g->rprev + o : nullptr, g->bpart, h->counter,
+                             with_beta ? h->scal : nullptr, with_beta, CoarseAdd{h->cs_aid, h->cs_d, h->cs_y});
+      return;
+    }
     if (h->cs_on) {
-      // two-level: z = M(r) + P Kc^-1 P^T r, then beta and z.r from the complete z
-      if (g->infer_mode == 0)
-        gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->z + o, done,
-                               h->stream, nullptr, g->bpart, h->counter, nullptr, with_beta);
-      else
-        gnn::launch_apply(g->graph(), w.r + o, dinv, g->params, g->Wb, g->h, g->z + o, done, h->stream);
+      // two-level through the layer kernels: z = M(r) + P Kc^-1 P^T r, then beta and z.r from the complete z
+      gnn::launch_apply(g->graph(), w.r + o, dinv, g->params, g->Wb, g->h, g->z + o, done, h->stream);
       launch_coarse_apply(h->cv(), w.r + o, g->z + o, h->stream);
       if (with_beta)
         gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, dinv, part, h->counter, h->scal, h->stream);

@@ -256,6 +256,10 @@ void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_
 // z += B W B^T r over the free block: aggregates' node lists (agg_ptr / agg_node, free-node indices),
 // per free node its aggregate and offset d_i from the aggregate's centroid (x, y, z, 0), W the
 // 6 n_agg square FP32 matrix R Kc^-1 R^T, s and y two 6 n_agg scratch vectors
+// The restriction runs over chunks of at most 256 nodes of one aggregate's list (chunk c: nodes
+// agg_node[chunk_start[c] .. + chunk_cnt[c]) of aggregate chunk_agg[c]; aggregate a owns the chunks
+// agg_chunk[a] .. agg_chunk[a+1]); the last chunk of an aggregate to finish (counter ccount[a]) sums
+// the aggregate's chunk partials cpart (6 per chunk) in chunk order.
 struct CoarseView {
   int n_agg;
   int ld;  // row stride of W: 6 n_agg rounded up to a multiple of 4
@@ -267,8 +271,25 @@ struct CoarseView {
   const float* W;
   float* s;
   float* y;
+  int n_chunks;
+  const int32_t* chunk_start;
+  const int32_t* chunk_cnt;
+  const int32_t* chunk_agg;
+  const int32_t* agg_chunk;
+  double* cpart;
+  unsigned* ccount;
 };
+// the correction's prolongation, z_i += u_a + w_a x d_i with (u_a, w_a) = y_a, as a term of another
+// kernel's node loop (aid == nullptr: none)
+struct CoarseAdd {
+  const int32_t* aid;
+  const float4* d;
+  const float* y;
+};
+// z += B W B^T r (restriction, coarse product, prolongation)
 void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st);
+// y = W B^T r only (the prolongation then runs inside the preconditioner's last pass)
+void launch_coarse_restrict_gemv(const CoarseView& cv, const float* r, cudaStream_t st);
 
 // ---- batched independent bodies: one persistent kernel per Krylov solve ----
 // Each instance (body) runs its own preconditioned CG recurrence (its own alpha, beta, r.z and
@@ -344,7 +365,7 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float4* x4, float4* y1,
                        float4* y2, float4* w, float* out, const int* done, cudaStream_t st,
                        const float* rprev = nullptr, float* partials = nullptr, unsigned* counter = nullptr,
-                       CgScalars* s = nullptr, bool x_ready = false);
+                       CgScalars* s = nullptr, bool x_ready = false, CoarseAdd ca = CoarseAdd{nullptr, nullptr, nullptr});
 // x4 rows = D^-1/2 r (r, dinv: 3n)
 void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float4* x4, cudaStream_t st);
 // the same M(r) keeping the activations h0..h3 of S and x = D^-1/2 r (training)
