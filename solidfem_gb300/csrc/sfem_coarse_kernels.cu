@@ -34,9 +34,10 @@ __device__ __forceinline__ double warp_sum_c(double v) {
 // finish adds its chunks' sums in chunk order (a fixed order, so s is the same on every run) and
 // resets the aggregate's counter
 __global__ void __launch_bounds__(kCT) k_coarse_restrict(CoarseView cv, const float* __restrict__ r) {
+  // FP32 within a warp (GB300's FP64 rate is a small fraction of FP32), the eight warp sums in FP64
   const int c = blockIdx.x;
   const int a = cv.chunk_agg[c];
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if ((int)threadIdx.x < cv.chunk_cnt[c]) {
     const int i = cv.agg_node[cv.chunk_start[c] + threadIdx.x];
     const float4 di = cv.d[i];
@@ -44,27 +45,31 @@ __global__ void __launch_bounds__(kCT) k_coarse_restrict(CoarseView cv, const fl
     acc[0] = r0;
     acc[1] = r1;
     acc[2] = r2;
-    acc[3] = (double)(di.y * r2 - di.z * r1);
-    acc[4] = (double)(di.z * r0 - di.x * r2);
-    acc[5] = (double)(di.x * r1 - di.y * r0);
+    acc[3] = di.y * r2 - di.z * r1;
+    acc[4] = di.z * r0 - di.x * r2;
+    acc[5] = di.x * r1 - di.y * r0;
   }
-  __shared__ double sm[6][kCT / 32];
+  __shared__ float sm[6][kCT / 32];
   __shared__ bool is_last;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < 6; k++) {
-    const double v = warp_sum_c(acc[k]);
+    float v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) sm[k][w] = v;
   }
   __syncthreads();
   if (w == 0) {
+    if (lane < 6) {
+      double v = 0.0;
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-      const double v = warp_sum_c(lane < kCT / 32 ? sm[k][lane] : 0.0);
-      if (lane == 0) cv.cpart[6 * (int64_t)c + k] = v;
+      for (int q = 0; q < kCT / 32; q++) v += (double)sm[lane][q];
+      cv.cpart[6 * (int64_t)c + lane] = v;
+      __threadfence();  // each writer orders its own partial before the count below
     }
+    __syncwarp();
     if (lane == 0) {
-      __threadfence();
       const unsigned n = (unsigned)(cv.agg_chunk[a + 1] - cv.agg_chunk[a]);
       is_last = atomicAdd(cv.ccount + a, 1u) == n - 1;
     }

@@ -2783,6 +2783,12 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 // fixed-order sum of component c of instance k's tile partials (every warp gets the same bits)
 __device__ __forceinline__ double inst_sum(const BatchPcg& b, int k, int c, int lane) {
   double v = 0.0;
@@ -2823,9 +2829,9 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
       __nanosleep(64);
     }
   }
-  // x = 0, r = b, z = D^-1 r, p = z; tile partials of r.z and r.r
+  // x = 0, r = b, z = D^-1 r, p = z; tile partials of r.z and r.r (a warp sums in T, the tiles in FP64)
   for (int t = gw; t < b.n_tiles; t += nw) {
-    double rz = 0.0, rr = 0.0;
+    T rz = T(0), rr = T(0);
     if (lane < b.tile_cnt[t]) {
       const int64_t o = 3 * (nbc + b.tile_node[t] + lane);
 #pragma unroll
@@ -2835,16 +2841,16 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
         r[o + c] = ri;
         z[o + c] = zi;
         p[o + c] = zi;
-        rz += (double)ri * (double)zi;
-        rr += (double)ri * (double)ri;
+        rz += ri * zi;
+        rr += ri * ri;
       }
     }
-    rz = warp_sum_d(rz);
-    rr = warp_sum_d(rr);
+    rz = warp_sum_t(rz);
+    rr = warp_sum_t(rr);
     if (lane == 0) {
       b.part[3 * t] = 0.0;
-      b.part[3 * t + 1] = rz;
-      b.part[3 * t + 2] = rr;
+      b.part[3 * t + 1] = (double)rz;
+      b.part[3 * t + 2] = (double)rr;
     }
   }
   if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
@@ -2904,7 +2910,7 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
     // B: q at the free nodes of the running instances, tile p.q
     for (int t = gw; t < b.n_tiles; t += nw) {
       const int k = b.tile_inst[t];
-      double pq = 0.0;
+      T pq = T(0);
       if (__ldcg(done + k) == 0 && lane < b.tile_cnt[t]) {
         const int64_t g = nbc + b.tile_node[t] + lane;
         T f0 = T(0), f1 = T(0), f2 = T(0);
@@ -2919,16 +2925,16 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
         q[o] = -f0;
         q[o + 1] = -f1;
         q[o + 2] = -f2;
-        pq = -((double)__ldcg(p + o) * f0 + (double)__ldcg(p + o + 1) * f1 + (double)__ldcg(p + o + 2) * f2);
+        pq = -(__ldcg(p + o) * f0 + __ldcg(p + o + 1) * f1 + __ldcg(p + o + 2) * f2);
       }
-      pq = warp_sum_d(pq);
-      if (lane == 0) b.part[3 * t] = pq;
+      pq = warp_sum_t(pq);
+      if (lane == 0) b.part[3 * t] = (double)pq;
     }
     if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
     // C: alpha and the updates, tile r.z and r.r
     for (int t = gw; t < b.n_tiles; t += nw) {
       const int k = b.tile_inst[t];
-      double rz = 0.0, rr = 0.0;
+      T rz = T(0), rr = T(0);
       if (__ldcg(done + k) == 0) {
         const double pq = inst_sum(b, k, 0, lane);
         const double alpha = (isfinite(pq) && pq > 0.0) ? __ldcg(b.rz + cur * K + k) / pq : 0.0;
@@ -2942,16 +2948,16 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
             const T ri = __ldcg(r + o + c) - a * qi, zi = dinv[o + c] * ri;
             r[o + c] = ri;
             z[o + c] = zi;
-            rz += (double)ri * (double)zi;
-            rr += (double)ri * (double)ri;
+            rz += ri * zi;
+            rr += ri * ri;
           }
         }
       }
-      rz = warp_sum_d(rz);
-      rr = warp_sum_d(rr);
+      rz = warp_sum_t(rz);
+      rr = warp_sum_t(rr);
       if (lane == 0) {
-        b.part[3 * t + 1] = rz;
-        b.part[3 * t + 2] = rr;
+        b.part[3 * t + 1] = (double)rz;
+        b.part[3 * t + 2] = (double)rr;
       }
     }
     if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
