@@ -1314,15 +1314,11 @@ template void launch_sell_hvp<double>(int64_t, int64_t, const int64_t*, const in
                                       const double*, double*, Reduce, CgScalars*, cudaStream_t, const double*,
                                       const double*, double*, const double*);
 
-// q = K p from the symmetric tangent's diagonal and upper blocks.  Two warps per slice of 32 rows: warp
-// half h = 0 takes the even block positions of each of its rows, h = 1 the odd ones (lower entries and
-// stored blocks alike), so twice as many independent loads are in flight per row at the same registers
-// per thread; the odd half's partial reaches the even half through shared memory (one 64-thread named
-// barrier per slice, the buffer alternating by round), which adds it and finishes the row.  The row's
-// lower blocks K_rj = K_jr^T are read from their mirror slots in row j, so each stored block streams
+// q = K p from the symmetric tangent's diagonal and upper blocks, one thread per row (a warp per slice).
+// The row's lower blocks K_rj = K_jr^T are read from their mirror slots in row j (lower entries in
+// column order, then the stored blocks: the order of the full row), so each stored block streams
 // from HBM once and its mirror read, by a row up to the mesh's bandwidth away processed at about the
-// same time, hits L2.  Sums in a fixed order (deterministic).  DIR and the p.q / alpha finish as in
-// k_sell_hvp.
+// same time, hits L2.  DIR and the p.q / alpha finish as in k_sell_hvp.
 template <typename T, bool DIR, typename CI>
 __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
                                                         const CI* __restrict__ col, const int64_t* __restrict__ lbase,
@@ -1340,96 +1336,126 @@ __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf,
     beta = (T)s->beta;
     use_z = z != nullptr && s->jac == 0;
   }
-  __shared__ T ys[2][kThreads / 64][32][3];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, half = warp & 1, pair = warp >> 1;
-  constexpr int kPairs = kThreads / 64;
-  const int64_t ns = (nf + 31) >> 5;
-  auto xdir = [&](int64_t jf, T& x0, T& x1, T& x2) {
-    const int64_t j = 3 * (nbc + jf);
-    if (DIR) {
-      x0 = (use_z ? z[j] : dinv[j] * r[j]) + beta * p[j];
-      x1 = (use_z ? z[j + 1] : dinv[j + 1] * r[j + 1]) + beta * p[j + 1];
-      x2 = (use_z ? z[j + 2] : dinv[j + 2] * r[j + 2]) + beta * p[j + 2];
-    } else {
-      x0 = p[j];
-      x1 = p[j + 1];
-      x2 = p[j + 2];
-    }
-  };
   T acc = T(0);
-  int round = 0;
-  for (int64_t sl0 = (int64_t)blockIdx.x * kPairs; sl0 < ns; sl0 += (int64_t)gridDim.x * kPairs, round ^= 1) {
-    const int64_t sl = sl0 + pair;
-    const int64_t row = sl * 32 + lane;
-    const bool active = sl < ns && row < nf;
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nf; row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sl = row >> 5;
+    const int lane = (int)(row & 31);
     const int64_t cbase = sizeof(CI) == 2 ? row : 0;
+    auto xdir = [&](int64_t jf, T& x0, T& x1, T& x2) {
+      const int64_t j = 3 * (nbc + jf);
+      if (DIR) {
+        x0 = (use_z ? z[j] : dinv[j] * r[j]) + beta * p[j];
+        x1 = (use_z ? z[j + 1] : dinv[j + 1] * r[j + 1]) + beta * p[j + 1];
+        x2 = (use_z ? z[j + 2] : dinv[j + 2] * r[j + 2]) + beta * p[j + 2];
+      } else {
+        x0 = p[j];
+        x1 = p[j + 1];
+        x2 = p[j + 2];
+      }
+    };
     T y0 = T(0), y1 = T(0), y2 = T(0);
-    if (active) {
-      // lower blocks of this half, transposed from the mirror rows
+    // lower blocks, transposed from the mirror rows (two entries per step: both slots, values and
+    // directions in flight; padding, slot -1, follows the row's last lower block)
+    {
       const int64_t lb0 = lbase[sl];
       const int wl = (int)((lbase[sl + 1] - lb0) >> 5);
       const CI* lc = lcol + lb0 + lane;
       const int32_t* ls = lslot + lb0 + lane;
-      for (int k = half; k < wl; k += 2) {
-        const int t = ls[32 * k];
-        if (t < 0) break;  // padding follows the row's last lower block
-        const T* V = vals + 9 * ((int64_t)t & ~(int64_t)31) + (t & 31);
-        T v[9];
+      auto mirror = [&](int64_t t, T (&v)[9]) {
+        const T* V = vals + 9 * (t & ~(int64_t)31) + (t & 31);
 #pragma unroll
         for (int qq = 0; qq < 9; qq++) v[qq] = V[32 * qq];
-        T x0, x1, x2;
-        xdir(cbase + lc[32 * k], x0, x1, x2);
-        y0 += v[0] * x0 + v[3] * x1 + v[6] * x2;
-        y1 += v[1] * x0 + v[4] * x1 + v[7] * x2;
-        y2 += v[2] * x0 + v[5] * x1 + v[8] * x2;
-      }
-      // the stored (diagonal and upper) blocks of this half
-      const int64_t b0 = base[sl];
-      const int w = (int)((base[sl + 1] - b0) >> 5);
-      const CI* cl = col + b0 + lane;
-      const T* Vb = vals + 9 * b0 + lane;
-      for (int k = half; k < w; k += 2) {
-        const T* Va = Vb + 288 * k;
-        T va[9];
+      };
+      int k = 0;
+      for (; k + 2 <= wl; k += 2) {
+        const int ta = ls[32 * k], tb = ls[32 * k + 32];
+        if (ta < 0) break;
+        const int64_t ja = cbase + lc[32 * k], jb = cbase + lc[32 * k + 32];
+        T va[9], vb[9], xa0, xa1, xa2, xb0 = T(0), xb1 = T(0), xb2 = T(0);
+        mirror(ta, va);
+        xdir(ja, xa0, xa1, xa2);
+        if (tb >= 0) {
+          mirror(tb, vb);
+          xdir(jb, xb0, xb1, xb2);
+        } else {
 #pragma unroll
-        for (int qq = 0; qq < 9; qq++) va[qq] = Va[32 * qq];
-        T x0, x1, x2;
-        xdir(cbase + cl[32 * k], x0, x1, x2);
-        y0 += va[0] * x0 + va[1] * x1 + va[2] * x2;
-        y1 += va[3] * x0 + va[4] * x1 + va[5] * x2;
-        y2 += va[6] * x0 + va[7] * x1 + va[8] * x2;
+          for (int qq = 0; qq < 9; qq++) vb[qq] = T(0);
+        }
+        y0 += va[0] * xa0 + va[3] * xa1 + va[6] * xa2;
+        y1 += va[1] * xa0 + va[4] * xa1 + va[7] * xa2;
+        y2 += va[2] * xa0 + va[5] * xa1 + va[8] * xa2;
+        y0 += vb[0] * xb0 + vb[3] * xb1 + vb[6] * xb2;
+        y1 += vb[1] * xb0 + vb[4] * xb1 + vb[7] * xb2;
+        y2 += vb[2] * xb0 + vb[5] * xb1 + vb[8] * xb2;
+        if (tb < 0) {
+          k = wl;
+          break;
+        }
+      }
+      if (k < wl) {
+        const int ta = ls[32 * k];
+        if (ta >= 0) {
+          T va[9], x0, x1, x2;
+          mirror(ta, va);
+          xdir(cbase + lc[32 * k], x0, x1, x2);
+          y0 += va[0] * x0 + va[3] * x1 + va[6] * x2;
+          y1 += va[1] * x0 + va[4] * x1 + va[7] * x2;
+          y2 += va[2] * x0 + va[5] * x1 + va[8] * x2;
+        }
       }
     }
-    if (half == 1) {
-      ys[round][pair][lane][0] = y0;
-      ys[round][pair][lane][1] = y1;
-      ys[round][pair][lane][2] = y2;
-    }
-    // the slice's two warps meet (the buffers alternate by round, so one meeting per round suffices)
-    asm volatile("bar.sync %0, 64;" ::"r"(1 + pair) : "memory");
-    if (half == 0 && active) {
-      y0 += ys[round][pair][lane][0];
-      y1 += ys[round][pair][lane][1];
-      y2 += ys[round][pair][lane][2];
-      const int64_t o = 3 * (nbc + row);
-      T p0, p1, p2;
-      if (DIR) {
-        p0 = (use_z ? z[o] : dinv[o] * r[o]) + beta * p[o];
-        p1 = (use_z ? z[o + 1] : dinv[o + 1] * r[o + 1]) + beta * p[o + 1];
-        p2 = (use_z ? z[o + 2] : dinv[o + 2] * r[o + 2]) + beta * p[o + 2];
-        p_new[o] = p0;
-        p_new[o + 1] = p1;
-        p_new[o + 2] = p2;
-      } else {
-        p0 = p[o];
-        p1 = p[o + 1];
-        p2 = p[o + 2];
+    // the diagonal and upper blocks of the row itself
+    const int64_t b0 = base[sl];
+    const int w = (int)((base[sl + 1] - b0) >> 5);
+    const CI* cl = col + b0 + lane;
+    const T* Vb = vals + 9 * b0 + lane;
+    int k = 0;
+    for (; k + 2 <= w; k += 2) {
+      const int64_t ja = cbase + cl[32 * k], jb = cbase + cl[32 * k + 32];
+      const T* Va = Vb + 288 * k;
+      const T* Wb = Va + 288;
+      T va[9], vb[9];
+#pragma unroll
+      for (int qq = 0; qq < 9; qq++) {
+        va[qq] = Va[32 * qq];
+        vb[qq] = Wb[32 * qq];
       }
-      q[o] = y0;
-      q[o + 1] = y1;
-      q[o + 2] = y2;
-      acc += p0 * y0 + p1 * y1 + p2 * y2;
+      T xa0, xa1, xa2, xb0, xb1, xb2;
+      xdir(ja, xa0, xa1, xa2);
+      xdir(jb, xb0, xb1, xb2);
+      y0 += va[0] * xa0 + va[1] * xa1 + va[2] * xa2;
+      y1 += va[3] * xa0 + va[4] * xa1 + va[5] * xa2;
+      y2 += va[6] * xa0 + va[7] * xa1 + va[8] * xa2;
+      y0 += vb[0] * xb0 + vb[1] * xb1 + vb[2] * xb2;
+      y1 += vb[3] * xb0 + vb[4] * xb1 + vb[5] * xb2;
+      y2 += vb[6] * xb0 + vb[7] * xb1 + vb[8] * xb2;
     }
+    if (k < w) {
+      const T* Va = Vb + 288 * k;
+      T x0, x1, x2;
+      xdir(cbase + cl[32 * k], x0, x1, x2);
+      y0 += Va[0] * x0 + Va[32] * x1 + Va[64] * x2;
+      y1 += Va[96] * x0 + Va[128] * x1 + Va[160] * x2;
+      y2 += Va[192] * x0 + Va[224] * x1 + Va[256] * x2;
+    }
+    const int64_t o = 3 * (nbc + row);
+    T p0, p1, p2;
+    if (DIR) {
+      p0 = (use_z ? z[o] : dinv[o] * r[o]) + beta * p[o];
+      p1 = (use_z ? z[o + 1] : dinv[o + 1] * r[o + 1]) + beta * p[o + 1];
+      p2 = (use_z ? z[o + 2] : dinv[o + 2] * r[o + 2]) + beta * p[o + 2];
+      p_new[o] = p0;
+      p_new[o + 1] = p1;
+      p_new[o + 2] = p2;
+    } else {
+      p0 = p[o];
+      p1 = p[o + 1];
+      p2 = p[o + 2];
+    }
+    q[o] = y0;
+    q[o + 1] = y1;
+    q[o + 2] = y2;
+    acc += p0 * y0 + p1 * y1 + p2 * y2;
   }
   if (s == nullptr) return;
   T v[1] = {acc}, tot[1];
@@ -1458,9 +1484,7 @@ void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_
                                             resident_ctas(k_ssell_hvp<T, false, int32_t>, kThreads, 0)),
                                    std::min(resident_ctas(k_ssell_hvp<T, true, int16_t>, kThreads, 0),
                                             resident_ctas(k_ssell_hvp<T, false, int16_t>, kThreads, 0)));
-  // two warps per slice of 32 rows: kThreads / 64 slices per CTA and round
-  const int64_t slices = (nf + 31) / 32, per = kThreads / 64;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(wave, (slices + per - 1) / per));
+  const int grid = std::max(1, std::min(wave, (int)((nf + kThreads - 1) / kThreads)));
   count_launch();
   if (col16 && p_new != nullptr)
     launch_pdl(k_ssell_hvp<T, true, int16_t>, grid, kThreads, 0, st, nbc, nf, base, col16, lbase, lcol16, lslot, vals,
