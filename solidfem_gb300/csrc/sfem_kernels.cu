@@ -2797,15 +2797,12 @@ __device__ __forceinline__ double inst_sum(const BatchPcg& b, int k, int c, int 
   return warp_sum_d(v);
 }
 
-// The CTA's fixed-order sums of the first nc components of the tile partials of each instance of the
-// round's tiles tb .. tb + kThreads / 32 - 1 (sorted by instance), into gs[c][w] for the first warp w of
-// that instance: thread j adds the instance's tiles t0 + j, t0 + j + kThreads, ..., then a warp tree and
-// the warp sums in order, so every CTA gets the same bits for the same instance.
-__device__ __forceinline__ void group_sums(const BatchPcg& b, int tb, int nc, double (&gs)[3][kThreads / 32],
-                                           double (&wsm)[3][kThreads / 32]) {
-  for (int w0 = 0; w0 < kThreads / 32 && tb + w0 < b.n_tiles; w0++) {
-    const int k = b.tile_inst[tb + w0];
-    if (w0 > 0 && b.tile_inst[tb + w0 - 1] == k) continue;
+// The CTA's fixed-order sums of the first nc components of the tile partials of instances k_lo .. k_hi
+// (at most kThreads / 32 of them: a round's tiles), into gs[c][k - k_lo]: thread j adds the tiles
+// t0 + j, t0 + j + kThreads, ..., then a warp tree and the warp sums in order (the same bits in every CTA).
+__device__ __forceinline__ void group_sums(const BatchPcg& b, int k_lo, int k_hi, int nc,
+                                           double (&gs)[3][kThreads / 32], double (&wsm)[3][kThreads / 32]) {
+  for (int k = k_lo; k <= k_hi; k++) {
     double v[3] = {0.0, 0.0, 0.0};
     const int t1 = b.inst_tile[k + 1];
     for (int t = b.inst_tile[k] + threadIdx.x; t < t1; t += kThreads)
@@ -2818,16 +2815,10 @@ __device__ __forceinline__ void group_sums(const BatchPcg& b, int tb, int nc, do
     if ((int)threadIdx.x < nc) {
       double sum = 0.0;
       for (int w = 0; w < kThreads / 32; w++) sum += wsm[threadIdx.x][w];
-      gs[threadIdx.x][w0] = sum;
+      gs[threadIdx.x][k - k_lo] = sum;
     }
     __syncthreads();
   }
-}
-// the slot of group_sums that holds tile tb + w's instance: its round's first warp of that instance
-__device__ __forceinline__ int group_slot(const BatchPcg& b, int tb, int w) {
-  const int k = b.tile_inst[tb + w];
-  while (w > 0 && b.tile_inst[tb + w - 1] == k) w--;
-  return w;
 }
 
 template <typename T>
@@ -2970,12 +2961,13 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
     // once per instance of the round's tiles (at most one per warp).
     for (int tb = blockIdx.x * wpb; tb < b.n_tiles; tb += nw) {
       const int t = tb + wid;
-      group_sums(b, tb, 1, gs, wsm);
+      const int k_lo = b.tile_inst[tb], k_hi = b.tile_inst[min(tb + wpb, b.n_tiles) - 1];
+      group_sums(b, k_lo, k_hi, 1, gs, wsm);
       if (t >= b.n_tiles) continue;
       const int k = b.tile_inst[t];
       T rz = T(0), rr = T(0);
       if (__ldcg(done + k) == 0) {
-        const double pq = gs[0][group_slot(b, tb, wid)];
+        const double pq = gs[0][k - k_lo];
         const double alpha = (isfinite(pq) && pq > 0.0) ? __ldcg(b.rz + cur * K + k) / pq : 0.0;
         if (lane < b.tile_cnt[t]) {
           const int64_t o = 3 * (nbc + b.tile_node[t] + lane);
@@ -3003,7 +2995,8 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
     // D: beta, convergence, directions (the CTA sums p.q, r.z, r.r once per instance of the round)
     for (int tb = blockIdx.x * wpb; tb < b.n_tiles; tb += nw) {
       const int t = tb + wid;
-      group_sums(b, tb, 3, gs, wsm);
+      const int k_lo = b.tile_inst[tb], k_hi = b.tile_inst[min(tb + wpb, b.n_tiles) - 1];
+      group_sums(b, k_lo, k_hi, 3, gs, wsm);
       if (t >= b.n_tiles) continue;
       const int k = b.tile_inst[t];
       const bool lead = t == b.inst_tile[k] && lane == 0;
@@ -3011,8 +3004,7 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
         if (lead) b.done[nxt * K + k] = __ldcg(done + k);
         continue;
       }
-      const int slot = group_slot(b, tb, wid);
-      const double pq = gs[0][slot], rzn = gs[1][slot], rr = gs[2][slot];
+      const double pq = gs[0][k - k_lo], rzn = gs[1][k - k_lo], rr = gs[2][k - k_lo];
       int st = 0;
       if (!isfinite(pq) || !isfinite(rzn)) st = 4;
       else if (!(pq > 0.0)) st = 2;
