@@ -300,7 +300,11 @@ def run_gpu_arm(args):
     p32.set_operator(args.operator)
     method = "jacobi"
     coarse_setup_s = None
-    weights = args.weights if args.weights else os.path.join(ROOT, "solidfem_gb300", "data", "gnn_slab.bin")
+    # the two-level method's network was fine-tuned with the coarse correction in the loop
+    data = os.path.join(ROOT, "solidfem_gb300", "data")
+    weights = args.weights if args.weights else os.path.join(data, "gnn_slab.bin")
+    if not args.weights and args.coarse_cells > 0 and os.path.exists(os.path.join(data, "gnn_two_level.bin")):
+        weights = os.path.join(data, "gnn_two_level.bin")
     if args.precond in ("learned", "auto") and os.path.exists(weights):
         from solidfem_gb300.learned import LearnedPreconditioner
 
@@ -478,6 +482,7 @@ def run_gpu_arm(args):
                             "jacobi": "Jacobi-PCG"}[method] +
                            " inner solves in FP32, FP64 residual and convergence test"),
                 "coarse_cells": args.coarse_cells if method == "learned+coarse" else None,
+                "weights": os.path.basename(weights) if method.startswith("learned") else None,
                 "coarse_setup_s": coarse_setup_s,
                 "operator": args.operator,
                 "preconditioner": method, "l2": "inputs larger than L2 (element data 0.35 GB FP32)",

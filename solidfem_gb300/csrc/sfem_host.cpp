@@ -3583,6 +3583,13 @@ int sfem_gnn_collect(sfem_handle* h, const double* b_free, int32_t every, int32_
     CU(cudaMemcpyAsync(&rf, g->spart + 4002, sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     TRY(sync(h));
     if (cf > 0.f && std::isfinite(cf) && rf > 0.f && std::isfinite(rf)) {
+      if (h->cs_on) {
+        // two-level: the network supplies M(r) beside the coarse correction C r, so it learns
+        // e_j - C r_j (the loss keeps e_j . r_j as its scale)
+        CU(cudaMemsetAsync(w.q + o, 0, n * sizeof(float), h->stream));
+        launch_coarse_apply(h->cv(), rs[j], w.q + o, h->stream);
+        gnn::launch_sub(n, xs[j], w.q + o, xs[j], h->stream);
+      }
       g->R.push_back(rs[j]);
       g->Ee.push_back(xs[j]);
       g->cinv.push_back(1.f / cf);

@@ -2797,30 +2797,6 @@ __device__ __forceinline__ double inst_sum(const BatchPcg& b, int k, int c, int 
   return warp_sum_d(v);
 }
 
-// The CTA's fixed-order sums of the first nc components of the tile partials of instances k_lo .. k_hi
-// (at most kThreads / 32 of them: a round's tiles), into gs[c][k - k_lo]: thread j adds the tiles
-// t0 + j, t0 + j + kThreads, ..., then a warp tree and the warp sums in order (the same bits in every CTA).
-__device__ __forceinline__ void group_sums(const BatchPcg& b, int k_lo, int k_hi, int nc,
-                                           double (&gs)[3][kThreads / 32], double (&wsm)[3][kThreads / 32]) {
-  for (int k = k_lo; k <= k_hi; k++) {
-    double v[3] = {0.0, 0.0, 0.0};
-    const int t1 = b.inst_tile[k + 1];
-    for (int t = b.inst_tile[k] + threadIdx.x; t < t1; t += kThreads)
-      for (int c = 0; c < nc; c++) v[c] += __ldcg(b.part + 3 * t + c);
-    for (int c = 0; c < nc; c++) {
-      v[c] = warp_sum_d(v[c]);
-      if ((threadIdx.x & 31) == 0) wsm[c][threadIdx.x >> 5] = v[c];
-    }
-    __syncthreads();
-    if ((int)threadIdx.x < nc) {
-      double sum = 0.0;
-      for (int w = 0; w < kThreads / 32; w++) sum += wsm[threadIdx.x][w];
-      gs[threadIdx.x][k - k_lo] = sum;
-    }
-    __syncthreads();
-  }
-}
-
 template <typename T>
 __device__ __forceinline__ void load3cg(const T* a, int g, T* o) {
   o[0] = __ldcg(a + 3 * (int64_t)g);
@@ -2839,8 +2815,6 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
                                                           T* r, T* z, T* p, T* q, const T* __restrict__ dinv, T* fe) {
   const int lane = threadIdx.x & 31;
   const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), nw = (int)((gridDim.x * blockDim.x) >> 5);
-  const int wid = threadIdx.x >> 5, wpb = kThreads / 32;
-  __shared__ double gs[3][kThreads / 32], wsm[3][kThreads / 32];
   const int K = b.K;
   const int64_t nbc = b.nbc, E = ev.E;
   if (b.wait_test && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -2957,17 +2931,12 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
       if (lane == 0) b.part[3 * t] = (double)pq;
     }
     if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
-    // C: alpha and the updates, tile r.z and r.r.  Rounds of one tile per warp; the CTA first sums p.q
-    // once per instance of the round's tiles (at most one per warp).
-    for (int tb = blockIdx.x * wpb; tb < b.n_tiles; tb += nw) {
-      const int t = tb + wid;
-      const int k_lo = b.tile_inst[tb], k_hi = b.tile_inst[min(tb + wpb, b.n_tiles) - 1];
-      group_sums(b, k_lo, k_hi, 1, gs, wsm);
-      if (t >= b.n_tiles) continue;
+    // C: alpha and the updates, tile r.z and r.r
+    for (int t = gw; t < b.n_tiles; t += nw) {
       const int k = b.tile_inst[t];
       T rz = T(0), rr = T(0);
       if (__ldcg(done + k) == 0) {
-        const double pq = gs[0][k - k_lo];
+        const double pq = inst_sum(b, k, 0, lane);
         const double alpha = (isfinite(pq) && pq > 0.0) ? __ldcg(b.rz + cur * K + k) / pq : 0.0;
         if (lane < b.tile_cnt[t]) {
           const int64_t o = 3 * (nbc + b.tile_node[t] + lane);
@@ -2992,19 +2961,15 @@ __global__ void __launch_bounds__(kThreads) k_batched_pcg(ElemView<T> ev, NodeCs
       }
     }
     if (!grid_sync_bounded(b.bar, b.err, b.wait_limit)) return;
-    // D: beta, convergence, directions (the CTA sums p.q, r.z, r.r once per instance of the round)
-    for (int tb = blockIdx.x * wpb; tb < b.n_tiles; tb += nw) {
-      const int t = tb + wid;
-      const int k_lo = b.tile_inst[tb], k_hi = b.tile_inst[min(tb + wpb, b.n_tiles) - 1];
-      group_sums(b, k_lo, k_hi, 3, gs, wsm);
-      if (t >= b.n_tiles) continue;
+    // D: beta, convergence, directions
+    for (int t = gw; t < b.n_tiles; t += nw) {
       const int k = b.tile_inst[t];
       const bool lead = t == b.inst_tile[k] && lane == 0;
       if (__ldcg(done + k) != 0) {
         if (lead) b.done[nxt * K + k] = __ldcg(done + k);
         continue;
       }
-      const double pq = gs[0][k - k_lo], rzn = gs[1][k - k_lo], rr = gs[2][k - k_lo];
+      const double pq = inst_sum(b, k, 0, lane), rzn = inst_sum(b, k, 1, lane), rr = inst_sum(b, k, 2, lane);
       int st = 0;
       if (!isfinite(pq) || !isfinite(rzn)) st = 4;
       else if (!(pq > 0.0)) st = 2;

@@ -6,6 +6,13 @@
     python -m solidfem_gb300.train_preconditioner --init tuned1.bin --first-seed 256 --every 15 \
         --max-snaps 60 --lr 1e-4 --init-seed 2 --out solidfem_gb300/data/gnn_slab.bin
 
+The two-level preconditioner's network (the bench's default method) is the one-level network
+fine-tuned on the corrections minus the coarse correction:
+
+    python -m solidfem_gb300.train_preconditioner --init solidfem_gb300/data/gnn_slab.bin --coarse-cells 16 \
+        --first-seed 512 --every 15 --max-snaps 60 --lr 3e-4 --init-seed 3 \
+        --out solidfem_gb300/data/gnn_two_level.bin
+
 Training meshes are slabs with the benchmark's element size (h = 1/64), jitter,
 material (neo-Hookean E = 1e5 Pa, nu = 0.49) and boundary conditions (bottom face
 clamped, random normal traction on the top face, load seeds 0..seeds-1).  For each
@@ -33,9 +40,11 @@ def slab_mesh(nx, ny, nz, jitter=0.2, seed=0):
 
 
 def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1e-3, init_seed=0, verbose=True,
-          loss="energy", batch=16, init=None, first_seed=0):
+          loss="energy", batch=16, init=None, first_seed=0, coarse_cells=0):
     """Collect pairs from load seeds first_seed .. first_seed + seeds - 1 and train; init: weights
-    to start from (a previous run's output) instead of the seeded random initialisation."""
+    to start from (a previous run's output) instead of the seeded random initialisation;
+    coarse_cells > 0: train the network as the one-level part of the two-level preconditioner
+    (coarse space of cells of that many hexes), i.e. on the corrections minus the coarse correction."""
     m = slab_mesh(*dims)
     fixed = m.face_nodes(2, 0)
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
@@ -43,6 +52,8 @@ def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1
     net = LearnedPreconditioner(p, seed=init_seed)
     if init:
         net.load(init)
+    if coarse_cells > 0:
+        p.set_coarse_space(coarse_cells / 64.0)
     net.set_loss(loss)
     net.set_batch(batch)
     t0 = time.time()
@@ -55,7 +66,7 @@ def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1
     t_train = time.time() - t0
     info = {"dims": list(dims), "load_seeds": [first_seed, first_seed + seeds - 1], "pairs": net.dataset_size(),
             "every": every, "max_snaps": max_snaps, "loss": loss, "batch": batch, "init": init, "init_seed": init_seed,
-            "steps": steps, "lr": lr, "loss_first50": float(np.mean(losses[:50])),
+            "steps": steps, "lr": lr, "coarse_cells": coarse_cells, "loss_first50": float(np.mean(losses[:50])),
             "loss_last50": float(np.mean(losses[-50:])), "collect_s": t_collect, "train_s": t_train,
             "material": "neo-Hookean E=1e5 nu=0.49, h=1/64, jitter 0.2h, bottom clamped, random top traction"}
     if verbose:
@@ -77,10 +88,12 @@ def main():
     ap.add_argument("--init", default=None, help="start from these weights (fine-tuning)")
     ap.add_argument("--first-seed", type=int, default=0, help="first load seed of the collected pairs")
     ap.add_argument("--init-seed", type=int, default=0, help="seed of the initialisation and of the minibatches")
+    ap.add_argument("--coarse-cells", type=int, default=0,
+                    help="train for the two-level preconditioner with coarse cells of this many hexes (0: one-level)")
     a = ap.parse_args()
     dims = tuple(int(v) for v in a.dims.split(","))
     net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr, init_seed=a.init_seed, loss=a.loss,
-                              batch=a.batch, init=a.init, first_seed=a.first_seed)
+                              batch=a.batch, init=a.init, first_seed=a.first_seed, coarse_cells=a.coarse_cells)
     net.save(a.out, meta=info)
     np.save(a.out.rsplit(".", 1)[0] + "_losses.npy", losses)
 
