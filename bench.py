@@ -417,7 +417,7 @@ def run_gpu_arm(args):
     # the main method on the first timed load again: its equilibrium for the oracle and FP64 checks
     st_main = solve(p32, s_ref)
     x32 = p32.get_positions()
-    # the same method through the matrix-free patch product (second record; the SURVEY's operator)
+    # the same method through the matrix-free patch product (second record: the reference's operator form)
     mf = None
     if args.operator == "assembled" and not args.skip_matrix_free:
         p32.set_operator("matrix-free")
