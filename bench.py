@@ -300,6 +300,7 @@ def run_gpu_arm(args):
     p32.set_operator(args.operator)
     method = "jacobi"
     coarse_setup_s = None
+    coarse_info = None
     # the two-level method's network was fine-tuned with the coarse correction in the loop
     data = os.path.join(ROOT, "solidfem_gb300", "data")
     weights = args.weights if args.weights else os.path.join(data, "gnn_slab.bin")
@@ -317,6 +318,7 @@ def run_gpu_arm(args):
             t_cs = time.perf_counter()
             p32.set_coarse_space(args.coarse_cells * EXTENT[0] / dims[0])
             coarse_setup_s = time.perf_counter() - t_cs
+            coarse_info = p32.coarse_info()
             method = "learned+coarse"
     elif args.precond == "learned":
         raise SystemExit(f"no trained weights at {weights}")
@@ -484,6 +486,7 @@ def run_gpu_arm(args):
                 "coarse_cells": args.coarse_cells if method == "learned+coarse" else None,
                 "weights": os.path.basename(weights) if method.startswith("learned") else None,
                 "coarse_setup_s": coarse_setup_s,
+                "coarse_setup": coarse_info,
                 "operator": args.operator,
                 "preconditioner": method, "l2": "inputs larger than L2 (element data 0.35 GB FP32)",
                 "converged": ok, "newton_iters": [s_["newton_iters"] for s_ in stats],
@@ -693,7 +696,7 @@ def main():
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per HVP launch, if captured")
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")
-    ap.add_argument("--coarse-cells", type=int, default=16,
+    ap.add_argument("--coarse-cells", type=int, default=12,
                     help="two-level preconditioner with the learned one: coarse-space cells of this many hexes "
                          "per axis (0: the learned preconditioner alone)")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")

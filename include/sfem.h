@@ -404,6 +404,11 @@ int sfem_coarse_factors(const double* X, int64_t n, double cell, double rtol, in
 int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol);
 /* z = P Kc^-1 P^T r alone (free DOFs, host arrays), for checking the coarse correction. */
 int sfem_coarse_apply(sfem_handle* h, const double* r, double* z);
+/* The coarse space's size and the wall-clock seconds of its setup (any pointer may be NULL):
+ * n_agg aggregates, n_coarse kept modes (the order of Kc); seconds[0] the rest-state FP64 tangent
+ * (pattern, assembly, copy to the host), seconds[1] Kc, seconds[2] the Cholesky factorisation, the
+ * inverse and W.  Zeros when the handle has no coarse space. */
+int sfem_coarse_info(sfem_handle* h, int32_t* n_agg, int32_t* n_coarse, double* seconds);
 
 /* ---- device-pointer variants (stream-ordered on the handle's stream) ---- */
 int sfem_compute_gradients_dev(sfem_handle* h, double* r_dev);

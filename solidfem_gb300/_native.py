@@ -134,6 +134,7 @@ SIGNATURES = {
     "sfem_set_batched_pcg": [_vp, C.c_int32],
     "sfem_set_coarse_space": [_vp, C.c_double, C.c_double],
     "sfem_coarse_apply": [_vp, _dp, _dp],
+    "sfem_coarse_info": [_vp, _ip, _ip, _dp],
     "sfem_instance_pcg_stats": [_vp, _ip, _ip, _dp],
     "sfem_set_device_wait": [_vp, C.c_int64, C.c_int32],
     "sfem_set_newton_trace": [_vp, _dp, C.c_int32, _ip],

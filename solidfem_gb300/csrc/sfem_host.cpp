@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <type_traits>
 #include <cmath>
@@ -126,7 +127,8 @@ struct sfem_handle {
   std::vector<double> bt_rr_h, bt_bb_h;
   // two-level preconditioner: the coarse-space correction of the learned flexible CG
   bool cs_on = false;
-  int cs_n_agg = 0, cs_ld = 0;
+  int cs_n_agg = 0, cs_ld = 0, cs_nk = 0;
+  double cs_setup_s[3] = {0.0, 0.0, 0.0};
   int32_t *cs_agg_ptr = nullptr, *cs_agg_node = nullptr, *cs_aid = nullptr;
   float4* cs_d = nullptr;
   float *cs_W = nullptr, *cs_s = nullptr, *cs_y = nullptr;
@@ -1032,48 +1034,109 @@ int sfem_set_stream(sfem_handle* h, void* stream) {
   return SFEM_OK;
 }
 
+extern "C++" {
+// rows [0, n) split over the host's threads
+template <typename F>
+static void parallel_rows(int64_t n, F&& f, int64_t min_rows = 4096) {
+  const int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  if (nt == 1 || n < min_rows) {
+    f((int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const int64_t chunk = (n + nt - 1) / nt;
+  for (int k = 0; k < nt; k++) {
+    const int64_t a = k * chunk, b = std::min(n, a + chunk);
+    if (a < b) pool.emplace_back([&f, a, b] { f(a, b); });
+  }
+  for (auto& th : pool) th.join();
+}
+
+// items [0, n) handed out to the host's threads in chunks of `grain` as they finish (for work
+// that grows along the range); each item's result does not depend on which thread ran it
+template <typename F>
+static void parallel_dynamic(int64_t n, int64_t grain, F&& f) {
+  const int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  if (nt == 1 || n <= grain) {
+    f((int64_t)0, n);
+    return;
+  }
+  std::atomic<int64_t> next{0};
+  auto work = [&] {
+    for (;;) {
+      const int64_t a = next.fetch_add(grain);
+      if (a >= n) return;
+      f(a, std::min(n, a + grain));
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int k = 0; k < nt; k++) pool.emplace_back(work);
+  for (auto& th : pool) th.join();
+}
+
+// the sorted free columns of free row r: r and the free corners of the elements at node nbc + r
+// (cp / ce: the node->element CSR, entries 4 e + corner)
+static void row_columns(int64_t r, int64_t nbc, const std::vector<int4>& tt, const std::vector<int64_t>& cp,
+                        const std::vector<int64_t>& ce, std::vector<int32_t>& cols) {
+  cols.clear();
+  cols.push_back((int32_t)r);
+  for (int64_t k = cp[nbc + r]; k < cp[nbc + r + 1]; k++) {
+    const int4 t4 = tt[ce[k] >> 2];
+    const int32_t v[4] = {t4.x, t4.y, t4.z, t4.w};
+    for (int b = 0; b < 4; b++)
+      if (v[b] >= nbc) cols.push_back((int32_t)(v[b] - nbc));
+  }
+  std::sort(cols.begin(), cols.end());
+  cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+}
+}
+
 // ---- assembled tangent (ElasticEnergy::AssembleStiffnessMatrix, Source/ElasticEnergy.cpp:573-635) ----
 // block-CSR pattern of the tangent over the free nodes (sorted columns per row), the block of
 // every (element, corner a, corner b) with both corners free (-1 otherwise) and each row's diagonal
 static int tangent_pattern(sfem_handle* h, std::vector<int32_t>& rowptr, std::vector<int32_t>& col,
                            std::vector<int32_t>& slot, std::vector<int32_t>& dslot) {
-  const int64_t E = h->E, nbc = h->nbc, nf = h->nf;
+  const int64_t E = h->E, N = h->N, nbc = h->nbc, nf = h->nf;
   std::vector<int4> tt((size_t)E);
+  std::vector<int64_t> cp((size_t)N + 1), ce((size_t)4 * E);
   CU(cudaMemcpyAsync(tt.data(), h->tets, tt.size() * sizeof(int4), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(cp.data(), h->csr_ptr, cp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(ce.data(), h->csr_ent, ce.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
-  std::vector<uint64_t> keys;
-  keys.reserve((size_t)E * 16 + (size_t)nf);
-  for (int64_t i = 0; i < nf; i++) keys.push_back(((uint64_t)i << 32) | (uint32_t)i);
-  for (const int4& t4 : tt) {
-    const int32_t v[4] = {t4.x, t4.y, t4.z, t4.w};
-    for (int a = 0; a < 4; a++)
-      for (int b = 0; b < 4; b++)
-        if (v[a] >= nbc && v[b] >= nbc) keys.push_back(((uint64_t)(v[a] - nbc) << 32) | (uint32_t)(v[b] - nbc));
-  }
-  std::sort(keys.begin(), keys.end());
-  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-  if (keys.size() > (size_t)INT32_MAX) return fail(SFEM_ERR_INVALID, "tangent too large for 32-bit block indices");
-  rowptr.assign((size_t)nf + 1, 0);
-  col.resize(keys.size());
+  // row lengths, then (rows in parallel) each row's columns, its diagonal and the blocks of the
+  // (element, corner) entries at its node: every (e, a) belongs to exactly one row
+  std::vector<int64_t> len((size_t)nf + 1, 0);
+  parallel_rows(nf, [&](int64_t a, int64_t b) {
+    std::vector<int32_t> cols;
+    for (int64_t r = a; r < b; r++) {
+      row_columns(r, nbc, tt, cp, ce, cols);
+      len[r + 1] = (int64_t)cols.size();
+    }
+  });
+  for (int64_t i = 0; i < nf; i++) len[i + 1] += len[i];
+  if (len[nf] > (int64_t)INT32_MAX) return fail(SFEM_ERR_INVALID, "tangent too large for 32-bit block indices");
+  rowptr.resize((size_t)nf + 1);
+  for (int64_t i = 0; i <= nf; i++) rowptr[i] = (int32_t)len[i];
+  col.resize((size_t)len[nf]);
   slot.assign((size_t)E * 16, -1);
   dslot.resize((size_t)nf);
-  for (size_t k = 0; k < keys.size(); k++) {
-    rowptr[(keys[k] >> 32) + 1]++;
-    col[k] = (int32_t)(keys[k] & 0xffffffffu);
-  }
-  for (int64_t i = 0; i < nf; i++) rowptr[i + 1] += rowptr[i];
-  auto find = [&](int64_t r, int32_t c) {
-    const int32_t* b = col.data() + rowptr[r];
-    const int32_t* e = col.data() + rowptr[r + 1];
-    return (int32_t)(std::lower_bound(b, e, c) - col.data());
-  };
-  for (int64_t e = 0; e < E; e++) {
-    const int32_t v[4] = {tt[e].x, tt[e].y, tt[e].z, tt[e].w};
-    for (int a = 0; a < 4; a++)
-      for (int b = 0; b < 4; b++)
-        if (v[a] >= nbc && v[b] >= nbc) slot[16 * e + 4 * a + b] = find(v[a] - nbc, v[b] - nbc);
-  }
-  for (int64_t i = 0; i < nf; i++) dslot[i] = find(i, (int32_t)i);
+  parallel_rows(nf, [&](int64_t a, int64_t b) {
+    std::vector<int32_t> cols;
+    for (int64_t r = a; r < b; r++) {
+      row_columns(r, nbc, tt, cp, ce, cols);
+      const int32_t base = rowptr[r];
+      std::copy(cols.begin(), cols.end(), col.begin() + base);
+      auto find = [&](int32_t c) { return base + (int32_t)(std::lower_bound(cols.begin(), cols.end(), c) - cols.begin()); };
+      dslot[r] = find((int32_t)r);
+      for (int64_t k = cp[nbc + r]; k < cp[nbc + r + 1]; k++) {
+        const int64_t e = ce[k] >> 2;
+        const int corner = (int)(ce[k] & 3);
+        const int32_t v[4] = {tt[e].x, tt[e].y, tt[e].z, tt[e].w};
+        for (int q = 0; q < 4; q++)
+          if (v[q] >= nbc) slot[16 * e + 4 * corner + q] = find(v[q] - (int32_t)nbc);
+      }
+    }
+  });
   return 0;
 }
 
@@ -1094,25 +1157,6 @@ static int bsr_structure(sfem_handle* h) {
   TRY(sync(h));
   h->bsr_nnzb = (int64_t)col.size();
   return 0;
-}
-
-extern "C++" {
-// rows [0, n) split over the host's threads
-template <typename F>
-static void parallel_rows(int64_t n, F&& f, int64_t min_rows = 4096) {
-  const int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-  if (nt == 1 || n < min_rows) {
-    f((int64_t)0, n);
-    return;
-  }
-  std::vector<std::thread> pool;
-  const int64_t chunk = (n + nt - 1) / nt;
-  for (int k = 0; k < nt; k++) {
-    const int64_t a = k * chunk, b = std::min(n, a + chunk);
-    if (a < b) pool.emplace_back([&f, a, b] { f(a, b); });
-  }
-  for (auto& th : pool) th.join();
-}
 }
 
 // The tangent's pattern in sliced ELL, built row by row from the node->element CSR: a free row's
@@ -1173,18 +1217,7 @@ static int sell_structure(sfem_handle* h) {
   CU(cudaMemcpyAsync(cp.data(), h->csr_ptr, cp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
   CU(cudaMemcpyAsync(ce.data(), h->csr_ent, ce.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
-  auto columns = [&](int64_t r, std::vector<int32_t>& cols) {
-    cols.clear();
-    cols.push_back((int32_t)r);
-    for (int64_t k = cp[nbc + r]; k < cp[nbc + r + 1]; k++) {
-      const int4 t4 = tt[ce[k] >> 2];
-      const int32_t v[4] = {t4.x, t4.y, t4.z, t4.w};
-      for (int b = 0; b < 4; b++)
-        if (v[b] >= nbc) cols.push_back((int32_t)(v[b] - nbc));
-    }
-    std::sort(cols.begin(), cols.end());
-    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-  };
+  auto columns = [&](int64_t r, std::vector<int32_t>& cols) { row_columns(r, nbc, tt, cp, ce, cols); };
   // the blocks a row stores: all of its columns, or (symmetric) those >= the row, the diagonal first
   auto stored = [&](int64_t r, std::vector<int32_t>& cols) {
     columns(r, cols);
@@ -1474,8 +1507,10 @@ int sfem_set_operator(sfem_handle* h, int32_t op) {
 
 extern "C++" {
 // In-place Cholesky A = L L^T of a dense symmetric positive definite n x n matrix (row-major; L in
-// the lower triangle), right-looking in blocks of 64 with the panel and trailing updates split over
-// the host's threads.  False if a pivot is not positive.
+// the lower triangle), right-looking in blocks of 64: the diagonal block, then the panel below it,
+// then the trailing update, the last two over the host's threads.  The trailing update takes four
+// columns at a time with two partial sums each (eight independent chains of multiply-adds).  False
+// if a pivot is not positive.
 static bool cholesky_lower(std::vector<double>& A, int n) {
   const int bs = 64;
   for (int k0 = 0; k0 < n; k0 += bs) {
@@ -1492,7 +1527,6 @@ static bool cholesky_lower(std::vector<double>& A, int n) {
         A[(size_t)i * n + k] = t / d;
       }
     }
-    // the panel below the diagonal block, then (all of it known) the trailing update
     parallel_rows(n - k1, [&](int64_t a, int64_t b) {
       for (int64_t i = k1 + a; i < k1 + b; i++) {
         double* Ai = &A[(size_t)i * n];
@@ -1504,19 +1538,94 @@ static bool cholesky_lower(std::vector<double>& A, int n) {
         }
       }
     }, 64);
-    parallel_rows(n - k1, [&](int64_t a, int64_t b) {
+    // row i takes i - k1 + 1 dot products: rows handed out dynamically
+    parallel_dynamic(n - k1, 8, [&](int64_t a, int64_t b) {
       for (int64_t i = k1 + a; i < k1 + b; i++) {
         double* Ai = &A[(size_t)i * n];
-        for (int64_t j = k1; j <= i; j++) {
+        int64_t j = k1;
+        for (; j + 3 <= i; j += 4) {
+          const double *A0 = &A[(size_t)j * n], *A1 = A0 + n, *A2 = A1 + n, *A3 = A2 + n;
+          double s0 = 0, s1 = 0, s2 = 0, s3 = 0, t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+          int p = k0;
+          for (; p + 1 < k1; p += 2) {
+            const double x = Ai[p], y = Ai[p + 1];
+            s0 += x * A0[p]; s1 += x * A1[p]; s2 += x * A2[p]; s3 += x * A3[p];
+            t0 += y * A0[p + 1]; t1 += y * A1[p + 1]; t2 += y * A2[p + 1]; t3 += y * A3[p + 1];
+          }
+          if (p < k1) {
+            const double x = Ai[p];
+            s0 += x * A0[p]; s1 += x * A1[p]; s2 += x * A2[p]; s3 += x * A3[p];
+          }
+          Ai[j] -= s0 + t0; Ai[j + 1] -= s1 + t1; Ai[j + 2] -= s2 + t2; Ai[j + 3] -= s3 + t3;
+        }
+        for (; j <= i; j++) {
           const double* Aj = &A[(size_t)j * n];
           double t = 0.0;
           for (int p = k0; p < k1; p++) t += Ai[p] * Aj[p];
           Ai[j] -= t;
         }
       }
-    }, 64);
+    });
   }
   return true;
+}
+
+// The inverse of A = L L^T (L from cholesky_lower, lower triangle of a row-major n x n array) into
+// Ainv (n x n, full, exactly symmetric).  Columns are solved 16 at a time, stored interleaved so
+// that each substitution step is 16 independent multiply-adds: L y = e_c from row c0 down, then
+// L^T x = y from row n - 1 up to row c0 (the rows of x at and below the group's first column are
+// the lower triangle's entries; the rest come from the symmetry).  Groups run on the host's threads.
+static void cholesky_inverse(const std::vector<double>& L, int n, std::vector<double>& Ainv) {
+  constexpr int G = 16;
+  std::vector<double> U((size_t)n * n);  // L^T row-major: column i of L contiguous
+  parallel_rows(n, [&](int64_t a, int64_t b) {
+    for (int64_t j = a; j < b; j++)
+      for (int64_t i = j; i < n; i++) U[(size_t)j * n + i] = L[(size_t)i * n + j];
+  }, 64);
+  Ainv.assign((size_t)n * n, 0.0);
+  const int64_t ng = (n + G - 1) / G;
+  parallel_dynamic(ng, 1, [&](int64_t g0, int64_t g1) {
+    std::vector<double> Y((size_t)n * G);
+    for (int64_t g = g0; g < g1; g++) {
+      const int c0 = (int)(g * G), w = std::min(G, n - c0);
+      std::fill(Y.begin() + (size_t)c0 * G, Y.end(), 0.0);
+      for (int i = c0; i < n; i++) {  // L y = e_c
+        double t[G];
+        for (int k = 0; k < G; k++) t[k] = (i == c0 + k) ? 1.0 : 0.0;
+        const double* Li = &L[(size_t)i * n];
+        for (int p = c0; p < i; p++) {
+          const double l = Li[p];
+          const double* Yp = &Y[(size_t)p * G];
+          for (int k = 0; k < G; k++) t[k] -= l * Yp[k];
+        }
+        const double inv = 1.0 / Li[i];
+        double* Yi = &Y[(size_t)i * G];
+        for (int k = 0; k < G; k++) Yi[k] = t[k] * inv;
+      }
+      for (int i = n - 1; i >= c0; i--) {  // L^T x = y
+        double t[G];
+        const double* Yi = &Y[(size_t)i * G];
+        for (int k = 0; k < G; k++) t[k] = Yi[k];
+        const double* Ui = &U[(size_t)i * n];
+        for (int p = i + 1; p < n; p++) {
+          const double u = Ui[p];
+          const double* Yp = &Y[(size_t)p * G];
+          for (int k = 0; k < G; k++) t[k] -= u * Yp[k];
+        }
+        const double inv = 1.0 / Ui[i];
+        double* Xi = &Y[(size_t)i * G];
+        for (int k = 0; k < G; k++) Xi[k] = t[k] * inv;
+      }
+      for (int k = 0; k < w; k++) {
+        const int c = c0 + k;
+        for (int i = c; i < n; i++) {
+          const double v = Y[(size_t)i * G + k];
+          Ainv[(size_t)i * n + c] = v;
+          Ainv[(size_t)c * n + i] = v;
+        }
+      }
+    }
+  });
 }
 }
 
@@ -1544,6 +1653,9 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   if (na > 1024) return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates (at most 1024)", (long long)na);
   std::vector<double> R((size_t)36 * na);
   TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
+  using clk = std::chrono::steady_clock;
+  auto secs = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+  const clk::time_point t0 = clk::now();
   // the FP64 tangent at the rest state, as block CSR over the free nodes
   std::vector<double> u_save((size_t)3 * h->N);
   CU(cudaMemcpyAsync(u_save.data(), h->u, u_save.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1558,6 +1670,7 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   CU(cudaMemcpyAsync(col.data(), h->bsr_col, col.size() * 4, cudaMemcpyDeviceToHost, h->stream));
   CU(cudaMemcpyAsync(vals.data(), h->bsr_vals, vals.size() * 8, cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
+  const clk::time_point t1 = clk::now();
   // kept (non-zero) columns of every R_a and their positions in the compact coarse index
   std::vector<std::vector<int>> kc((size_t)na);
   std::vector<int> first((size_t)na + 1, 0);
@@ -1634,31 +1747,11 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
       }
     }
   }, 1);
-  // Kc^-1 by Cholesky, one column per task (forward then backward substitution)
+  const clk::time_point t2 = clk::now();
+  // Kc^-1 by Cholesky
   if (!cholesky_lower(Kc, nk)) return fail(SFEM_ERR_INVALID, "the coarse matrix is not positive definite");
-  std::vector<double> U((size_t)nk * nk);  // L^T, row-major, for contiguous backward substitution
-  for (int i = 0; i < nk; i++)
-    for (int j = 0; j <= i; j++) U[(size_t)j * nk + i] = Kc[(size_t)i * nk + j];
-  std::vector<double> Kinv((size_t)nk * nk);
-  parallel_rows(nk, [&](int64_t c0, int64_t c1) {
-    std::vector<double> y((size_t)nk);
-    for (int64_t c = c0; c < c1; c++) {
-      std::fill(y.begin(), y.end(), 0.0);
-      for (int64_t i = c; i < nk; i++) {  // L y = e_c (zero above c)
-        double t = i == c ? 1.0 : 0.0;
-        const double* Li = &Kc[(size_t)i * nk];
-        for (int64_t p = c; p < i; p++) t -= Li[p] * y[p];
-        y[i] = t / Li[i];
-      }
-      for (int64_t i = nk - 1; i >= 0; i--) {  // L^T x = y
-        const double* Ui = &U[(size_t)i * nk];
-        double t = y[i];
-        for (int64_t p = i + 1; p < nk; p++) t -= Ui[p] * y[p];
-        y[i] = t / Ui[i];
-      }
-      for (int64_t i = 0; i < nk; i++) Kinv[(size_t)i * nk + c] = y[i];
-    }
-  }, 16);
+  std::vector<double> Kinv;
+  cholesky_inverse(Kc, nk, Kinv);
   // W = R Kc^-1 R^T in the modes' basis (6 n_agg square, rows padded to a multiple of 4)
   const int nc = (int)(6 * na), ld = (nc + 3) / 4 * 4;
   std::vector<float> W((size_t)nc * ld, 0.f);
@@ -1680,6 +1773,7 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
           }
       }
   }, 1);
+  const clk::time_point t3 = clk::now();
   // restriction chunks: at most 256 nodes of one aggregate's list each
   std::vector<int32_t> cstart, ccnt, cagg, achunk((size_t)na + 1, 0);
   for (int64_t a = 0; a < na; a++) {
@@ -1723,7 +1817,20 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   TRY(sync(h));
   h->cs_n_agg = (int)na;
   h->cs_ld = ld;
+  h->cs_nk = nk;
+  h->cs_setup_s[0] = secs(t0, t1);
+  h->cs_setup_s[1] = secs(t1, t2);
+  h->cs_setup_s[2] = secs(t2, t3);
   h->cs_on = true;
+  return SFEM_OK;
+}
+
+int sfem_coarse_info(sfem_handle* h, int32_t* n_agg, int32_t* n_coarse, double* seconds) {
+  TRY(check_handle(h));
+  if (n_agg) *n_agg = h->cs_on ? h->cs_n_agg : 0;
+  if (n_coarse) *n_coarse = h->cs_on ? h->cs_nk : 0;
+  if (seconds)
+    for (int k = 0; k < 3; k++) seconds[k] = h->cs_on ? h->cs_setup_s[k] : 0.0;
   return SFEM_OK;
 }
 

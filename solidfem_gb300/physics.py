@@ -194,6 +194,15 @@ class FemPhysicsMatrixFree:
         nat.check(self._lib.sfem_coarse_apply(self._h, _dp(r), _dp(z)))
         return z
 
+    def coarse_info(self):
+        """The coarse space's aggregates, kept modes and setup seconds (rest-state tangent, Kc,
+        factorisation + inverse); zeros without one."""
+        na, nk = C.c_int32(0), C.c_int32(0)
+        secs = np.zeros(3)
+        nat.check(self._lib.sfem_coarse_info(self._h, C.byref(na), C.byref(nk), _dp(secs)))
+        return {"aggregates": na.value, "coarse_dofs": nk.value, "tangent_s": float(secs[0]),
+                "coarse_matrix_s": float(secs[1]), "factorisation_s": float(secs[2])}
+
     def set_batched_pcg(self, per_instance=True):
         """Krylov solves with instances: every instance's own PCG in one persistent launch (True) or one
         recurrence over all instances (False)."""
