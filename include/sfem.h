@@ -399,8 +399,9 @@ int sfem_coarse_factors(const double* X, int64_t n, double cell, double rtol, in
  * SolveConjugateGradientMF, Math/IterativeSolvers.h:115-195, has no coarse space):
  * z = M(r) + P Kc^-1 P^T r, P the rigid-body modes of grid-cell aggregates of the free nodes (cell:
  * the grid spacing; rtol as in sfem_coarse_factors), Kc = P^T K P from the FP64 tangent at the rest
- * state, inverted once here (dense, FP64 Cholesky on the host threads) and applied in FP32 as one
- * matrix-vector product per iteration.  cell <= 0 turns it off.  At most 1024 aggregates. */
+ * state, inverted once here (dense, FP64 Cholesky on the host threads) and applied as one
+ * matrix-vector product per iteration (W = R Kc^-1 R^T stored in FP16 times a power of two, FP32 sums).
+ * cell <= 0 turns it off.  At most 2048 aggregates. */
 int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol);
 /* z = P Kc^-1 P^T r alone (free DOFs, host arrays), for checking the coarse correction. */
 int sfem_coarse_apply(sfem_handle* h, const double* r, double* z);

@@ -4,9 +4,11 @@
 //
 // In the modes' own basis B (node i's 3 x 6 block [I, -[d_i]x], d_i its offset from its aggregate's
 // centroid) the correction is z_i += B_i y_a(i), y = W s with s_a = B_a^T r = (sum r_i, sum d_i x r_i)
-// over the aggregate's nodes and W = R Kc^-1 R^T (6 n_agg square, formed once on the host; R the
-// per-aggregate orthonormalisation with dropped modes).  Three launches per application:
-//   k_coarse_restrict  one CTA per chunk of <= 256 nodes of an aggregate, fixed-order sums
+// over the aggregate's nodes and W = R Kc^-1 R^T (6 n_agg square, formed once on the host in FP64 and
+// stored in FP16 times a power of two; R the per-aggregate orthonormalisation with dropped modes).  Four launches per application:
+//   k_coarse_runs      one CTA per block of 1024 consecutive free nodes (coalesced loads of r and d into
+//                      shared memory), one thread per run of the block: the run's six sums
+//   k_coarse_aggsum    one CTA per aggregate: the sums of its runs, s_a
 //   k_coarse_gemv      one warp per row of W (the one dense contraction: a bandwidth-bound GEMV)
 //   k_coarse_prolong   one thread per free node, z_i += u_a + w_a x d_i   ((u_a, w_a) = y_a); inside the
 //                      flexible CG the learned preconditioner's last pass adds this term instead
@@ -23,84 +25,102 @@ namespace {
 
 constexpr int kCT = 256;
 
-__device__ __forceinline__ double warp_sum_c(double v) {
+// Run sums of s_a = (sum r_i, sum d_i x r_i): block b of kCoarseBlock free nodes, four nodes per
+// thread (coalesced), their six terms staged in shared memory; then each run of the block summed
+// in node order by one thread, to runpart[c * n_runs + k]
+__global__ void __launch_bounds__(kCT) k_coarse_runs(CoarseView cv, const float* __restrict__ r) {
+  __shared__ float sv[6][kCoarseBlock];
+  const int64_t base = (int64_t)blockIdx.x * kCoarseBlock;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+  for (int m = 0; m < kCoarseBlock / kCT; m++) {
+    const int t = threadIdx.x + kCT * m;
+    const int64_t i = base + t;
+    if (i < cv.nf) {
+      const float4 di = cv.d[i];
+      const float r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
+      sv[0][t] = r0;
+      sv[1][t] = r1;
+      sv[2][t] = r2;
+      sv[3][t] = di.y * r2 - di.z * r1;
+      sv[4][t] = di.z * r0 - di.x * r2;
+      sv[5][t] = di.x * r1 - di.y * r0;
+    }
+  }
+  __syncthreads();
+  const int k1 = cv.blk_run[blockIdx.x + 1];
+  for (int k = cv.blk_run[blockIdx.x] + threadIdx.x; k < k1; k += kCT) {
+    const int j0 = (int)(cv.run_start[k] - base), j1 = (int)(cv.run_start[k + 1] - base);
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int j = j0; j < j1; j++)
+#pragma unroll
+      for (int c = 0; c < 6; c++) acc[c] += sv[c][j];
+#pragma unroll
+    for (int c = 0; c < 6; c++) cv.runpart[(int64_t)c * cv.n_runs + k] = acc[c];
+  }
 }
 
-// s_a = (sum r_i, sum d_i x r_i) over aggregate a's nodes: one CTA per chunk of at most 256 nodes of
-// one aggregate (one node per thread), the chunk's six sums to cpart; the aggregate's last chunk to
-// finish adds its chunks' sums in chunk order (a fixed order, so s is the same on every run) and
-// resets the aggregate's counter
-__global__ void __launch_bounds__(kCT) k_coarse_restrict(CoarseView cv, const float* __restrict__ r) {
-  // FP32 within a warp (GB300's FP64 rate is a small fraction of FP32), the eight warp sums in FP64
-  const int c = blockIdx.x;
-  const int a = cv.chunk_agg[c];
-  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  if ((int)threadIdx.x < cv.chunk_cnt[c]) {
-    const int i = cv.agg_node[cv.chunk_start[c] + threadIdx.x];
-    const float4 di = cv.d[i];
-    const float r0 = r[3 * (int64_t)i], r1 = r[3 * (int64_t)i + 1], r2 = r[3 * (int64_t)i + 2];
-    acc[0] = r0;
-    acc[1] = r1;
-    acc[2] = r2;
-    acc[3] = di.y * r2 - di.z * r1;
-    acc[4] = di.z * r0 - di.x * r2;
-    acc[5] = di.x * r1 - di.y * r0;
-  }
-  __shared__ float sm[6][kCT / 32];
-  __shared__ bool is_last;
+// s_a from aggregate a's run sums: one CTA per aggregate, thread t adding runs t, t + 256, ... of the
+// aggregate's list in order (one run each for aggregates of up to 256 runs), then fixed butterflies
+// within the warps and the eight warp sums in warp order (the same order on every run)
+__global__ void __launch_bounds__(kCT) k_coarse_aggsum(CoarseView cv) {
+  __shared__ float ws[6][kCT / 32];
+  const int a = blockIdx.x;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const int q1 = cv.agg_run_ptr[a + 1];
+  for (int q = cv.agg_run_ptr[a] + threadIdx.x; q < q1; q += kCT) {
+    const int k = cv.agg_run[q];
 #pragma unroll
-  for (int k = 0; k < 6; k++) {
-    float v = acc[k];
+    for (int c = 0; c < 6; c++) acc[c] += cv.runpart[(int64_t)c * cv.n_runs + k];
+  }
+#pragma unroll
+  for (int c = 0; c < 6; c++) {
+    float v = acc[c];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sm[k][w] = v;
+    if (lane == 0) ws[c][w] = v;
   }
   __syncthreads();
-  if (w == 0) {
-    if (lane < 6) {
-      double v = 0.0;
-#pragma unroll
-      for (int q = 0; q < kCT / 32; q++) v += (double)sm[lane][q];
-      cv.cpart[6 * (int64_t)c + lane] = v;
-      __threadfence();  // each writer orders its own partial before the count below
-    }
-    __syncwarp();
-    if (lane == 0) {
-      const unsigned n = (unsigned)(cv.agg_chunk[a + 1] - cv.agg_chunk[a]);
-      is_last = atomicAdd(cv.ccount + a, 1u) == n - 1;
-    }
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
   if (threadIdx.x < 6) {
-    double v = 0.0;
-    for (int k = cv.agg_chunk[a]; k < cv.agg_chunk[a + 1]; k++) v += __ldcg(cv.cpart + 6 * (int64_t)k + threadIdx.x);
-    cv.s[6 * a + threadIdx.x] = (float)v;
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < kCT / 32; k++) v += ws[threadIdx.x][k];
+    cv.s[6 * a + threadIdx.x] = v;
   }
-  if (threadIdx.x == 0) cv.ccount[a] = 0u;
 }
 
-// y = W s, W row-major nc x ld (FP32, ld a multiple of 4, zero beyond nc; s zero beyond nc), one warp
-// per row reading 16-byte column groups
-__global__ void __launch_bounds__(kCT) k_coarse_gemv(int nc, int ld, const float* __restrict__ W,
+// y = W s: W row-major nc x ld FP16 (scaled by 1 / inv_scale; ld a multiple of 8, zero beyond nc), s FP32
+// (zero beyond nc).  One warp per row, each lane eight columns per 16-byte load and four loads in
+// flight; FP32 sums in a fixed order (lane partials, then a butterfly)
+__device__ __forceinline__ float dot8(const uint4& w, const float4& a, const float4& b) {
+  const float2 w0 = __half22float2(*reinterpret_cast<const __half2*>(&w.x));
+  const float2 w1 = __half22float2(*reinterpret_cast<const __half2*>(&w.y));
+  const float2 w2 = __half22float2(*reinterpret_cast<const __half2*>(&w.z));
+  const float2 w3 = __half22float2(*reinterpret_cast<const __half2*>(&w.w));
+  return ((w0.x * a.x + w0.y * a.y) + (w1.x * a.z + w1.y * a.w)) + ((w2.x * b.x + w2.y * b.y) + (w3.x * b.z + w3.y * b.w));
+}
+__global__ void __launch_bounds__(kCT) k_coarse_gemv(int nc, int ld, const __half* __restrict__ W, float inv_scale,
                                                      const float* __restrict__ s, float* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int row = (int)((blockIdx.x * (int64_t)kCT + threadIdx.x) >> 5);
   if (row >= nc) return;
-  const float4* Wr = reinterpret_cast<const float4*>(W + (int64_t)row * ld);
+  const uint4* Wr = reinterpret_cast<const uint4*>(W + (int64_t)row * ld);
   const float4* s4 = reinterpret_cast<const float4*>(s);
-  double acc = 0.0;
-  for (int c = lane; c < ld / 4; c += 32) {
-    const float4 wv = Wr[c], sv = s4[c];
-    acc += (double)(wv.x * sv.x + wv.y * sv.y + wv.z * sv.z + wv.w * sv.w);
+  const int n8 = ld / 8;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  int c = lane;
+  for (; c + 96 < n8; c += 128) {
+    uint4 w[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) w[u] = __ldcs(Wr + c + 32 * u);
+#pragma unroll
+    for (int u = 0; u < 4; u++) acc[u] += dot8(w[u], s4[2 * (c + 32 * u)], s4[2 * (c + 32 * u) + 1]);
   }
-  acc = warp_sum_c(acc);
-  if (lane == 0) y[row] = (float)acc;
+  for (; c < n8; c += 32) acc[0] += dot8(__ldcs(Wr + c), s4[2 * c], s4[2 * c + 1]);
+  float v = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) y[row] = v * inv_scale;
 }
 
 // z_i += u_a + w_a x d_i over the free nodes
@@ -120,11 +140,16 @@ __global__ void __launch_bounds__(kCT) k_coarse_prolong(int64_t nf, const int32_
 }  // namespace
 
 void launch_coarse_restrict_gemv(const CoarseView& cv, const float* r, cudaStream_t st) {
+  // ordinary launches: with programmatic dependent launch the next kernel's waiting CTAs took the
+  // slots of these grids' later CTAs (measured: 73 us more per flexible-CG iteration at 6.3M tets)
+  if (cv.n_blocks <= 0) return;
   count_launch();
-  k_coarse_restrict<<<cv.n_chunks, kCT, 0, st>>>(cv, r);
+  k_coarse_runs<<<(unsigned)cv.n_blocks, kCT, 0, st>>>(cv, r);
+  count_launch();
+  k_coarse_aggsum<<<(unsigned)cv.n_agg, kCT, 0, st>>>(cv);
   count_launch();
   const int nc = 6 * cv.n_agg;
-  k_coarse_gemv<<<(unsigned)((nc * 32 + kCT - 1) / kCT), kCT, 0, st>>>(nc, cv.ld, cv.W, cv.s, cv.y);
+  k_coarse_gemv<<<(unsigned)((nc * 32 + kCT - 1) / kCT), kCT, 0, st>>>(nc, cv.ld, cv.W, cv.w_inv_scale, cv.s, cv.y);
 }
 
 void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st) {

@@ -129,17 +129,18 @@ struct sfem_handle {
   bool cs_on = false;
   int cs_n_agg = 0, cs_ld = 0, cs_nk = 0;
   double cs_setup_s[3] = {0.0, 0.0, 0.0};
-  int32_t *cs_agg_ptr = nullptr, *cs_agg_node = nullptr, *cs_aid = nullptr;
+  int32_t* cs_aid = nullptr;
   float4* cs_d = nullptr;
-  float *cs_W = nullptr, *cs_s = nullptr, *cs_y = nullptr;
-  int cs_n_chunks = 0;
-  int32_t *cs_chunk_start = nullptr, *cs_chunk_cnt = nullptr, *cs_chunk_agg = nullptr, *cs_agg_chunk = nullptr;
-  double* cs_cpart = nullptr;
-  unsigned* cs_ccount = nullptr;
+  __half* cs_W = nullptr;
+  float cs_w_inv_scale = 1.f;
+  float *cs_s = nullptr, *cs_y = nullptr;
+  int cs_n_runs = 0, cs_n_blocks = 0;
+  int32_t *cs_run_start = nullptr, *cs_blk_run = nullptr, *cs_agg_run_ptr = nullptr, *cs_agg_run = nullptr;
+  float* cs_runpart = nullptr;
   CoarseView cv() const {
-    return CoarseView{cs_n_agg,       cs_ld,        nf,           cs_agg_ptr,     cs_agg_node,    cs_aid,
-                      cs_d,           cs_W,         cs_s,         cs_y,           cs_n_chunks,    cs_chunk_start,
-                      cs_chunk_cnt,   cs_chunk_agg, cs_agg_chunk, cs_cpart,       cs_ccount};
+    return CoarseView{cs_n_agg,   cs_ld,     nf,        cs_aid,      cs_d,         cs_W,           cs_w_inv_scale,
+                      cs_s,       cs_y,      cs_n_runs, cs_n_blocks, cs_run_start, cs_blk_run,     cs_agg_run_ptr,
+                      cs_agg_run, cs_runpart};
   }
   // node data (reshuffled, 3N)
   double *x0 = nullptr, *u = nullptr, *mass = nullptr, *fext = nullptr, *grav_d = nullptr;
@@ -1649,8 +1650,9 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   std::vector<double> d((size_t)3 * nf);
   int64_t na = 0;
   TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), nullptr, &na));
-  // the dense factorisation costs ~(6 n_agg)^3 flops on the host: at most 1024 aggregates
-  if (na > 1024) return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates (at most 1024)", (long long)na);
+  // the dense factorisation costs ~(6 n_agg)^3 / 2 multiply-adds on the host and W (6 n_agg)^2 halves:
+  // at most 2048 aggregates
+  if (na > 2048) return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates (at most 2048)", (long long)na);
   std::vector<double> R((size_t)36 * na);
   TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
   using clk = std::chrono::steady_clock;
@@ -1752,8 +1754,8 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   if (!cholesky_lower(Kc, nk)) return fail(SFEM_ERR_INVALID, "the coarse matrix is not positive definite");
   std::vector<double> Kinv;
   cholesky_inverse(Kc, nk, Kinv);
-  // W = R Kc^-1 R^T in the modes' basis (6 n_agg square, rows padded to a multiple of 4)
-  const int nc = (int)(6 * na), ld = (nc + 3) / 4 * 4;
+  // W = R Kc^-1 R^T in the modes' basis (6 n_agg square, rows padded to a multiple of 8)
+  const int nc = (int)(6 * na), ld = (nc + 7) / 8 * 8;
   std::vector<float> W((size_t)nc * ld, 0.f);
   parallel_rows(na, [&](int64_t a0, int64_t a1) {
     for (int64_t a = a0; a < a1; a++)
@@ -1773,47 +1775,63 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
           }
       }
   }, 1);
+  // stored in FP16 (11-bit significand) times 2^k, k putting the largest magnitude in [2^13, 2^14): half
+  // the bytes of the per-iteration product, relative rounding <= 2^-11 on every entry above 2^-14 / 2^k
+  float wmax = 0.f;
+  for (float v : W) wmax = std::max(wmax, std::fabs(v));
+  const int wexp = wmax > 0.f ? 13 - std::ilogb(wmax) : 0;
+  std::vector<__half> Wh(W.size());
+  parallel_rows((int64_t)W.size(), [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; i++) Wh[i] = __float2half_rn(std::ldexp(W[i], wexp));
+  });
+  h->cs_w_inv_scale = std::ldexp(1.f, -wexp);
   const clk::time_point t3 = clk::now();
-  // restriction chunks: at most 256 nodes of one aggregate's list each
-  std::vector<int32_t> cstart, ccnt, cagg, achunk((size_t)na + 1, 0);
-  for (int64_t a = 0; a < na; a++) {
-    for (int32_t k = aptr[a]; k < aptr[a + 1]; k += 256) {
-      cstart.push_back(k);
-      ccnt.push_back(std::min<int32_t>(256, aptr[a + 1] - k));
-      cagg.push_back((int32_t)a);
-    }
-    achunk[a + 1] = (int32_t)cstart.size();
+  // restriction runs: blocks of kCoarseBlock consecutive free nodes, split where the aggregate
+  // changes and after kCoarseRun nodes; then every aggregate's runs in increasing order
+  const int64_t nblk = (nf + kCoarseBlock - 1) / kCoarseBlock;
+  std::vector<int32_t> rstart, rblk((size_t)nblk + 1, 0), ragg;
+  for (int64_t b = 0; b < nblk; b++) {
+    const int64_t i0 = b * kCoarseBlock, i1 = std::min<int64_t>(nf, i0 + kCoarseBlock);
+    for (int64_t i = i0; i < i1; i++)
+      if (i == i0 || aid[i] != aid[i - 1] || i - rstart.back() == kCoarseRun) {
+        rstart.push_back((int32_t)i);
+        ragg.push_back(aid[i]);
+      }
+    rblk[b + 1] = (int32_t)rstart.size();
+  }
+  const int64_t nrun = (int64_t)rstart.size();
+  rstart.push_back((int32_t)nf);
+  std::vector<int32_t> arptr((size_t)na + 1, 0), arun((size_t)nrun);
+  for (int64_t k = 0; k < nrun; k++) arptr[ragg[k] + 1]++;
+  for (int64_t a = 0; a < na; a++) arptr[a + 1] += arptr[a];
+  {
+    std::vector<int32_t> fill(arptr.begin(), arptr.end() - 1);
+    for (int64_t k = 0; k < nrun; k++) arun[fill[ragg[k]]++] = (int32_t)k;
   }
   // device copies
   std::vector<float4> d4((size_t)nf);
   for (int64_t i = 0; i < nf; i++) d4[i] = make_float4((float)d[3 * i], (float)d[3 * i + 1], (float)d[3 * i + 2], 0.f);
-  TRY(dalloc(&h->cs_agg_ptr, aptr.size()));
-  TRY(dalloc(&h->cs_agg_node, anode.size()));
   TRY(dalloc(&h->cs_aid, aid.size()));
   TRY(dalloc(&h->cs_d, d4.size()));
-  TRY(dalloc(&h->cs_W, W.size()));
+  TRY(dalloc(&h->cs_W, Wh.size()));
   TRY(dalloc(&h->cs_s, (size_t)ld));
   TRY(dalloc(&h->cs_y, (size_t)ld));
-  CU(cudaMemcpyAsync(h->cs_agg_ptr, aptr.data(), aptr.size() * 4, cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemcpyAsync(h->cs_agg_node, anode.data(), anode.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  TRY(dalloc(&h->cs_run_start, rstart.size()));
+  TRY(dalloc(&h->cs_blk_run, rblk.size()));
+  TRY(dalloc(&h->cs_agg_run_ptr, arptr.size()));
+  TRY(dalloc(&h->cs_agg_run, std::max<size_t>(arun.size(), 1)));
+  TRY(dalloc(&h->cs_runpart, std::max<size_t>(6 * (size_t)nrun, 1)));
   CU(cudaMemcpyAsync(h->cs_aid, aid.data(), aid.size() * 4, cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemcpyAsync(h->cs_d, d4.data(), d4.size() * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemcpyAsync(h->cs_W, W.data(), W.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_W, Wh.data(), Wh.size() * sizeof(__half), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(h->cs_s, 0, (size_t)ld * 4, h->stream));
   CU(cudaMemsetAsync(h->cs_y, 0, (size_t)ld * 4, h->stream));
-  const size_t nch = cstart.size();
-  TRY(dalloc(&h->cs_chunk_start, nch));
-  TRY(dalloc(&h->cs_chunk_cnt, nch));
-  TRY(dalloc(&h->cs_chunk_agg, nch));
-  TRY(dalloc(&h->cs_agg_chunk, achunk.size()));
-  TRY(dalloc(&h->cs_cpart, 6 * nch));
-  TRY(dalloc(&h->cs_ccount, (size_t)na));
-  CU(cudaMemcpyAsync(h->cs_chunk_start, cstart.data(), nch * 4, cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemcpyAsync(h->cs_chunk_cnt, ccnt.data(), nch * 4, cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemcpyAsync(h->cs_chunk_agg, cagg.data(), nch * 4, cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemcpyAsync(h->cs_agg_chunk, achunk.data(), achunk.size() * 4, cudaMemcpyHostToDevice, h->stream));
-  CU(cudaMemsetAsync(h->cs_ccount, 0, (size_t)na * sizeof(unsigned), h->stream));
-  h->cs_n_chunks = (int)nch;
+  CU(cudaMemcpyAsync(h->cs_run_start, rstart.data(), rstart.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_blk_run, rblk.data(), rblk.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemcpyAsync(h->cs_agg_run_ptr, arptr.data(), arptr.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if (nrun > 0) CU(cudaMemcpyAsync(h->cs_agg_run, arun.data(), arun.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  h->cs_n_runs = (int)nrun;
+  h->cs_n_blocks = (int)nblk;
   TRY(sync(h));
   h->cs_n_agg = (int)na;
   h->cs_ld = ld;
@@ -2523,18 +2541,18 @@ void batch_release(sfem_handle* h) {
 }
 
 void coarse_release(sfem_handle* h) {
-  void* bufs[] = {h->cs_agg_ptr,     h->cs_agg_node,  h->cs_aid,       h->cs_d,        h->cs_W,
-                  h->cs_s,          h->cs_y,         h->cs_chunk_start, h->cs_chunk_cnt, h->cs_chunk_agg,
-                  h->cs_agg_chunk,  h->cs_cpart,     h->cs_ccount};
+  void* bufs[] = {h->cs_aid,       h->cs_d,          h->cs_W,         h->cs_s,      h->cs_y,
+                  h->cs_run_start, h->cs_blk_run,    h->cs_agg_run_ptr, h->cs_agg_run, h->cs_runpart};
   for (void* b : bufs)
     if (b) cudaFree(b);
-  h->cs_chunk_start = h->cs_chunk_cnt = h->cs_chunk_agg = h->cs_agg_chunk = nullptr;
-  h->cs_cpart = nullptr;
-  h->cs_ccount = nullptr;
-  h->cs_n_chunks = 0;
-  h->cs_agg_ptr = h->cs_agg_node = h->cs_aid = nullptr;
+  h->cs_aid = nullptr;
   h->cs_d = nullptr;
-  h->cs_W = h->cs_s = h->cs_y = nullptr;
+  h->cs_W = nullptr;
+  h->cs_w_inv_scale = 1.f;
+  h->cs_s = h->cs_y = nullptr;
+  h->cs_run_start = h->cs_blk_run = h->cs_agg_run_ptr = h->cs_agg_run = nullptr;
+  h->cs_runpart = nullptr;
+  h->cs_n_runs = h->cs_n_blocks = 0;
   h->cs_on = false;
   h->cs_n_agg = h->cs_ld = 0;
 }

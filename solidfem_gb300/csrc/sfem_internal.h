@@ -1,6 +1,7 @@
 // Internal declarations shared by the host driver (sfem_host.cpp) and the
 // CUDA kernels (sfem_kernels.cu).  Not part of the public ABI.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -253,31 +254,33 @@ void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_
                       const T* vals, const T* p, T* q, Reduce red, CgScalars* s, cudaStream_t st,
                       const T* r = nullptr, const T* dinv = nullptr, T* p_new = nullptr, const T* z = nullptr);
 // ---- coarse-space correction of the two-level preconditioner (sfem_coarse_kernels.cu) ----
-// z += B W B^T r over the free block: aggregates' node lists (agg_ptr / agg_node, free-node indices),
-// per free node its aggregate and offset d_i from the aggregate's centroid (x, y, z, 0), W the
-// 6 n_agg square FP32 matrix R Kc^-1 R^T, s and y two 6 n_agg scratch vectors
-// The restriction runs over chunks of at most 256 nodes of one aggregate's list (chunk c: nodes
-// agg_node[chunk_start[c] .. + chunk_cnt[c]) of aggregate chunk_agg[c]; aggregate a owns the chunks
-// agg_chunk[a] .. agg_chunk[a+1]); the last chunk of an aggregate to finish (counter ccount[a]) sums
-// the aggregate's chunk partials cpart (6 per chunk) in chunk order.
+// z += B W B^T r over the free block: per free node its aggregate aid[i] and offset d_i from the
+// aggregate's centroid (x, y, z, 0); W the 6 n_agg square matrix R Kc^-1 R^T in FP16, scaled by a
+// power of two (w_inv_scale undoes it; rows of ld halves, ld a multiple of 8); s and y two ld-long
+// FP32 scratch vectors.  The restriction reads the free nodes in order, in
+// blocks of kCoarseBlock: block b's nodes split into runs (consecutive nodes of one aggregate, at
+// most kCoarseRun each), runs blk_run[b] .. blk_run[b+1] - 1, run k the nodes run_start[k] ..
+// run_start[k+1] - 1.  A run's six sums go to runpart (six arrays of n_runs floats); aggregate a's runs
+// are agg_run[agg_run_ptr[a] .. agg_run_ptr[a+1] - 1], in increasing order.
+constexpr int kCoarseBlock = 1024;
+constexpr int kCoarseRun = 32;
 struct CoarseView {
   int n_agg;
-  int ld;  // row stride of W: 6 n_agg rounded up to a multiple of 4
+  int ld;
   int64_t nf;
-  const int32_t* agg_ptr;
-  const int32_t* agg_node;
   const int32_t* aid;
   const float4* d;
-  const float* W;
+  const __half* W;
+  float w_inv_scale;
   float* s;
   float* y;
-  int n_chunks;
-  const int32_t* chunk_start;
-  const int32_t* chunk_cnt;
-  const int32_t* chunk_agg;
-  const int32_t* agg_chunk;
-  double* cpart;
-  unsigned* ccount;
+  int n_runs;
+  int n_blocks;
+  const int32_t* run_start;
+  const int32_t* blk_run;
+  const int32_t* agg_run_ptr;
+  const int32_t* agg_run;
+  float* runpart;
 };
 // the correction's prolongation, z_i += u_a + w_a x d_i with (u_a, w_a) = y_a, as a term of another
 // kernel's node loop (aid == nullptr: none)
