@@ -696,7 +696,7 @@ def main():
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per HVP launch, if captured")
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")
-    ap.add_argument("--coarse-cells", type=int, default=12,
+    ap.add_argument("--coarse-cells", type=int, default=11,
                     help="two-level preconditioner with the learned one: coarse-space cells of this many hexes "
                          "per axis (0: the learned preconditioner alone)")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")
