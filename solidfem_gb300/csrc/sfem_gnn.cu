@@ -76,9 +76,10 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
   k_gnn_layer_inf<false, true, true><<<grid, LT, 0, st>>>(g, h[2], r, dinv, params, Wsb, nullptr, out, done);
 }
 
-void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float4* x4, float4* y1,
-                       float4* y2, float4* w, float* out, const int* done, cudaStream_t st, const float* rprev,
-                       float* partials, unsigned* counter, CgScalars* s, bool x_ready, CoarseAdd ca) {
+void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, Row16* x4, Row16* y1,
+                       Row16* y2, Row16* w, float* xstat, float* out, const int* done, cudaStream_t st,
+                       float* partials, unsigned* counter, const float* rprev, CgScalars* s, bool x_ready,
+                       CoarseAdd ca) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
   // grid-stride passes sized to one resident wave (no partly filled last wave; the BETA pass
   // then finishes with one block partial per resident CTA, 4 values each)
@@ -87,26 +88,29 @@ void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const 
                    wave_last = std::min(resident_ctas(k_poly_last<true>, 256, 0),
                                         resident_ctas(k_poly_last<false>, 256, 0));
   const int blocks = blocks_for(g.n, 256);
-  if (!x_ready) launch_scale_sqrt4(g.n, r, dinv, x4, st);
+  if (!x_ready) launch_scale_sqrt4(g.n, r, dinv, xstat, partials, counter, x4, st);
   count_launch();
-  launch_pdl(k_poly_fwd, std::min(blocks, wave_fwd), 256, 0, st, g, x4, y1, done);
+  launch_pdl(k_poly_fwd, std::min(blocks, wave_fwd), 256, 0, st, g, (const Row16*)x4, y1, done);
   count_launch();
-  launch_pdl(k_poly_fwd, std::min(blocks, wave_fwd), 256, 0, st, g, y1, y2, done);
+  launch_pdl(k_poly_fwd, std::min(blocks, wave_fwd), 256, 0, st, g, (const Row16*)y1, y2, done);
   count_launch();
-  launch_pdl(k_poly_mid, std::min(blocks, wave_mid), 256, 0, st, g, x4, y1, y2, pc, w, done);
+  launch_pdl(k_poly_mid, std::min(blocks, wave_mid), 256, 0, st, g, (const Row16*)x4, (const Row16*)y1,
+             (const Row16*)y2, pc, w, done);
   // Horner in A^T: w3 -> A^T u + w2 (into y1) -> A^T u + w1 (into y2) -> out
   count_launch();
-  launch_pdl(k_poly_bwd, std::min(blocks, wave_bwd), 256, 0, st, g, w + 3 * g.n, w + 2 * g.n, y1, done);
+  launch_pdl(k_poly_bwd, std::min(blocks, wave_bwd), 256, 0, st, g, (const Row16*)(w + 3 * g.n),
+             (const Row16*)(w + 2 * g.n), y1, done);
   count_launch();
-  launch_pdl(k_poly_bwd, std::min(blocks, wave_bwd), 256, 0, st, g, y1, w + g.n, y2, done);
+  launch_pdl(k_poly_bwd, std::min(blocks, wave_bwd), 256, 0, st, g, (const Row16*)y1, (const Row16*)(w + g.n), y2,
+             done);
   count_launch();
   const int grid_last = std::min(blocks, wave_last);
   if (s)
-    launch_pdl(k_poly_last<true>, grid_last, 256, 0, st, g, y2, w, r, dinv, pc.c, out, done, rprev, partials, counter,
-               s, ca);
+    launch_pdl(k_poly_last<true>, grid_last, 256, 0, st, g, (const Row16*)y2, (const Row16*)w, (const float*)xstat,
+               r, dinv, pc.c, out, done, rprev, partials, counter, s, ca);
   else
-    launch_pdl(k_poly_last<false>, grid_last, 256, 0, st, g, y2, w, r, dinv, pc.c, out, done, nullptr, nullptr,
-               nullptr, nullptr, ca);
+    launch_pdl(k_poly_last<false>, grid_last, 256, 0, st, g, (const Row16*)y2, (const Row16*)w, (const float*)xstat,
+               r, dinv, pc.c, out, done, nullptr, nullptr, nullptr, nullptr, ca);
 }
 
 // the training forward: activations h0..h3 of S at x (kept, with x), then S^T through the
@@ -195,11 +199,16 @@ void launch_pack(const float* prm, __nv_bfloat16* Wb, cudaStream_t st) {
 namespace sfem {
 namespace gnn {
 
-// xs = r D^-1/2 (the input of the polynomial passes), elementwise
-void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float4* x4, cudaStream_t st) {
+// xs = sigma r D^-1/2 (the input of the polynomial passes): sigma from sum d r^2, then the rows
+void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float* xstat, float* partials, unsigned* counter,
+                        Row16* x4, cudaStream_t st) {
+  static const int wave = resident_ctas(k_poly_xscale, 256, 0);
+  const int g3 = (int)std::max<int64_t>(1, std::min<int64_t>((3 * n + 255) / 256, wave));
+  count_launch();
+  launch_pdl(k_poly_xscale, g3, 256, 0, st, 3 * n, r, dinv, xstat, partials, counter);
   int grid = (int)std::min<int64_t>((n + 255) / 256, 2048);
   count_launch();
-  launch_pdl(k_scale_sqrt4, grid < 1 ? 1 : grid, 256, 0, st, n, r, dinv, x4);
+  launch_pdl(k_scale_sqrt4, grid < 1 ? 1 : grid, 256, 0, st, n, r, dinv, (const float*)xstat, x4);
 }
 
 // d = a - b

@@ -30,6 +30,14 @@ struct PolyCoef {
   float c;                     // weight of the Jacobi term
 };
 
+// A node row of the polynomial passes: (x, y, z) in FP16 and a zero pad, 8 bytes.  The rows hold
+// the polynomial's input D^-1/2 r (and what the passes make of it) times a power of two, sigma, that
+// puts their RMS in [1/8, 1/4): xstat[0] is the sum of d r^2 over the last rows formed, xstat[1]
+// their sigma, which the last pass divides out.
+struct alignas(8) Row16 {
+  uint32_t xy, z0;
+};
+
 struct Graph {
   int64_t n;              // free nodes
   const int32_t* ptr;     // n + 1

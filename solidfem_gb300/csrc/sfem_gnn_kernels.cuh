@@ -18,6 +18,7 @@
 #include "sfem_gnn.h"
 #include "sfem_pdl.cuh"
 #include "sfem_reduce.cuh"
+#include "sfem_row16.cuh"
 
 namespace sfem {
 namespace gnn {
@@ -633,16 +634,17 @@ __global__ void __launch_bounds__(LT) k_gnn_layer_inf(Graph g, const __nv_bfloat
 // ======================= inference through the folded polynomial =======================
 // y_{k+1} = A y_k (mean over neighbours), y_0 = x = D^-1/2 r; then w_j = sum_k y_k G[k][j]
 // and M(r) = D^-1/2 (c x + w_0 + A^T (w_1 + A^T (w_2 + A^T w_3)))   (Horner in A^T).
-// Six passes, one thread per node, over node rows of 16 bytes (x, y, z, 0) so that one
-// neighbour costs one vector load.  A^T u = sum_j u_j / deg_j: the pass that writes a Horner
-// operand stores u_i / deg_i, so every gather is a plain neighbour sum.  The neighbour loop
-// is unrolled by four (four loads in flight) and adds in neighbour order (deterministic).
+// Six passes, one thread per node, over FP16 node rows of 8 bytes (Row16: x, y, z, 0, scaled by
+// sigma) so that one neighbour costs one 8-byte load; sums and products in FP32.
+// A^T u = sum_j u_j / deg_j: the pass that writes a Horner operand stores u_i / deg_i, so every
+// gather is a plain neighbour sum.  The neighbour loop is unrolled by four (four loads in
+// flight) and adds in neighbour order (deterministic).
 
 // sum over the neighbours j of node i of v_j.  The neighbours come from the pattern table when
 // there is one (a 2-byte id per node; the table's few hundred deltas stay in L1 and a warp of
 // interior nodes reads one address), else from the 16-bit deltas or the 32-bit CSR; the three
 // list the same neighbours in the same order.
-__device__ __forceinline__ float3 node_gather4(const Graph& g, int64_t i, const float4* __restrict__ v) {
+__device__ __forceinline__ float3 node_gather16(const Graph& g, int64_t i, const Row16* __restrict__ v) {
   float3 a = make_float3(0.f, 0.f, 0.f);
   int e, p1;
   const int16_t* dl = g.d16;
@@ -660,60 +662,80 @@ __device__ __forceinline__ float3 node_gather4(const Graph& g, int64_t i, const 
     int jn[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) jn[u] = dl ? ii + (int)__ldg(&dl[e + u]) : g.idx[e + u];
-    float4 x[4];
+    Row16 x[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) x[u] = v[jn[u]];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      a.x += x[u].x;
-      a.y += x[u].y;
-      a.z += x[u].z;
+      const float3 f = unpack16(x[u]);
+      a.x += f.x;
+      a.y += f.y;
+      a.z += f.z;
     }
   }
   for (; e < p1; e++) {
-    const float4 x = v[dl ? ii + (int)__ldg(&dl[e]) : g.idx[e]];
-    a.x += x.x;
-    a.y += x.y;
-    a.z += x.z;
+    const float3 f = unpack16(v[dl ? ii + (int)__ldg(&dl[e]) : g.idx[e]]);
+    a.x += f.x;
+    a.y += f.y;
+    a.z += f.z;
   }
   return a;
 }
 
-__device__ __forceinline__ float4 row4(float3 a, float s) { return make_float4(a.x * s, a.y * s, a.z * s, 0.f); }
+__device__ __forceinline__ Row16 row16(float3 a, float s) { return pack16(a.x * s, a.y * s, a.z * s); }
 
-// x rows = D^-1/2 r
-__global__ void __launch_bounds__(256) k_scale_sqrt4(int64_t n, const float* __restrict__ r,
-                                                     const float* __restrict__ dinv, float4* __restrict__ x4) {
+// the rows' scale for a pass that forms x = D^-1/2 r itself: xstat[0] = sum d r^2 (fixed-order
+// sums), xstat[1] = sigma (row16_scale)
+__global__ void __launch_bounds__(256) k_poly_xscale(int64_t n3, const float* __restrict__ r,
+                                                     const float* __restrict__ dinv, float* __restrict__ xstat,
+                                                     float* __restrict__ partials, unsigned* counter) {
   pdl_wait();
   pdl_launch_dependents();
+  float acc[1] = {0.f};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x)
+    acc[0] += dinv[i] * r[i] * r[i];
+  double t[1];
+  if (last_block_sums<1>(acc, partials, counter, t) && threadIdx.x == 0) {
+    xstat[0] = (float)t[0];
+    xstat[1] = row16_scale((float)t[0], n3);
+  }
+}
+
+// x rows = sigma D^-1/2 r
+__global__ void __launch_bounds__(256) k_scale_sqrt4(int64_t n, const float* __restrict__ r,
+                                                     const float* __restrict__ dinv, const float* __restrict__ xstat,
+                                                     Row16* __restrict__ x4) {
+  pdl_wait();
+  pdl_launch_dependents();
+  const float sg = xstat[1];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * i;
-    x4[i] = make_float4(r[o] * sqrtf(dinv[o]), r[o + 1] * sqrtf(dinv[o + 1]), r[o + 2] * sqrtf(dinv[o + 2]), 0.f);
+    x4[i] = pack16(sg * r[o] * sqrtf(dinv[o]), sg * r[o + 1] * sqrtf(dinv[o + 1]), sg * r[o + 2] * sqrtf(dinv[o + 2]));
   }
 }
 
 // yout = A yin
-__global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const float4* __restrict__ yin,
-                                                  float4* __restrict__ yout, const int* done) {
+__global__ void __launch_bounds__(256) k_poly_fwd(Graph g, const Row16* __restrict__ yin, Row16* __restrict__ yout,
+                                                  const int* done) {
   pdl_wait();
   pdl_launch_dependents();
   if (done && *done) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
-    yout[i] = row4(node_gather4(g, i, yin), g.inv_deg[i]);
+    yout[i] = row16(node_gather16(g, i, yin), g.inv_deg[i]);
 }
 
 // y_3 = A y_2 at the node, then w_j = sum_k y_k G[k][j] for j = 0..3 (w: 4 blocks of n rows;
 // w_3, the first Horner operand, stored divided by the node's degree)
-__global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float4* __restrict__ x4,
-                                                  const float4* __restrict__ y1, const float4* __restrict__ y2,
-                                                  PolyCoef pc, float4* __restrict__ w, const int* done) {
+__global__ void __launch_bounds__(256) k_poly_mid(Graph g, const Row16* __restrict__ x4,
+                                                  const Row16* __restrict__ y1, const Row16* __restrict__ y2,
+                                                  PolyCoef pc, Row16* __restrict__ w, const int* done) {
   pdl_wait();
   pdl_launch_dependents();
   if (done && *done) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float3 a = node_gather4(g, i, y2);
+    const float3 a = node_gather16(g, i, y2);
     const float id = g.inv_deg[i];
-    const float4 v0 = x4[i], v1 = y1[i], v2 = y2[i];
+    const float3 v0 = unpack16(x4[i]), v1 = unpack16(y1[i]), v2 = unpack16(y2[i]);
     const float y[NL + 1][3] = {{v0.x, v0.y, v0.z}, {v1.x, v1.y, v1.z}, {v2.x, v2.y, v2.z},
                                 {a.x * id, a.y * id, a.z * id}};
 #pragma unroll
@@ -728,45 +750,46 @@ __global__ void __launch_bounds__(256) k_poly_mid(Graph g, const float4* __restr
           for (int b = 0; b < 3; b++) acc += y[k][b] * pc.G[k][jj][3 * b + c];
         o[c] = acc;
       }
-      w[jj * g.n + i] = row4(make_float3(o[0], o[1], o[2]), jj == NL ? id : 1.f);
+      w[jj * g.n + i] = row16(make_float3(o[0], o[1], o[2]), jj == NL ? id : 1.f);
     }
   }
 }
 
 // u_i = sum_{j in N(i)} ud_j + wadd_i, stored as u_i / deg_i (ud_j = u_j / deg_j on input)
-__global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const float4* __restrict__ ud,
-                                                  const float4* __restrict__ wadd, float4* __restrict__ out,
+__global__ void __launch_bounds__(256) k_poly_bwd(Graph g, const Row16* __restrict__ ud,
+                                                  const Row16* __restrict__ wadd, Row16* __restrict__ out,
                                                   const int* done) {
   pdl_wait();
   pdl_launch_dependents();
   if (done && *done) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float3 a = node_gather4(g, i, ud);
-    const float4 wa = wadd[i];
-    out[i] = row4(make_float3(a.x + wa.x, a.y + wa.y, a.z + wa.z), g.inv_deg[i]);
+    const float3 a = node_gather16(g, i, ud);
+    const float3 wa = unpack16(wadd[i]);
+    out[i] = row16(make_float3(a.x + wa.x, a.y + wa.y, a.z + wa.z), g.inv_deg[i]);
   }
 }
 
-// the last Horner pass: z = D^-1/2 (c x + w_0 + A^T u) = c D^-1 r + D^-1/2 (w_0 + A^T u), 3n.
+// the last Horner pass: z = D^-1/2 (c x + w_0 + A^T u) = c D^-1 r + D^-1/2 (w_0 + A^T u) / sigma, 3n.
 // BETA (inside flexible CG): also the Polak-Ribiere sums of the new z,
 //   z.(r - rprev), z.r and the same for z_J = D^-1 r, finished by the last block into
 //   s->beta, s->rz and s->jac (Jacobi direction when z.r <= 0), like k_fcg_beta.
 //   partials: 4 gridDim floats.
 template <bool BETA>
-__global__ void __launch_bounds__(256) k_poly_last(Graph g, const float4* __restrict__ ud,
-                                                   const float4* __restrict__ w0, const float* __restrict__ r,
-                                                   const float* __restrict__ dinv, float cc, float* __restrict__ out,
-                                                   const int* done, const float* __restrict__ rprev,
-                                                   float* __restrict__ partials, unsigned* counter, CgScalars* s,
-                                                   CoarseAdd ca) {
+__global__ void __launch_bounds__(256) k_poly_last(Graph g, const Row16* __restrict__ ud,
+                                                   const Row16* __restrict__ w0, const float* __restrict__ xstat,
+                                                   const float* __restrict__ r, const float* __restrict__ dinv,
+                                                   float cc, float* __restrict__ out, const int* done,
+                                                   const float* __restrict__ rprev, float* __restrict__ partials,
+                                                   unsigned* counter, CgScalars* s, CoarseAdd ca) {
   pdl_wait();
   pdl_launch_dependents();
   if (done && *done) return;
+  const float isg = 1.f / xstat[1];  // a power of two: exact
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float3 a = node_gather4(g, i, ud);
-    const float4 wa = w0[i];
-    const float v[3] = {a.x + wa.x, a.y + wa.y, a.z + wa.z};
+    const float3 a = node_gather16(g, i, ud);
+    const float3 wa = unpack16(w0[i]);
+    const float v[3] = {(a.x + wa.x) * isg, (a.y + wa.y) * isg, (a.z + wa.z) * isg};
     // two-level: the coarse correction u_a + w_a x d_i of the node's aggregate
     float cz[3] = {0.f, 0.f, 0.f};
     if (ca.aid) {

@@ -3083,8 +3083,10 @@ struct GnnState {
   int infer_mode = 0;                    // 0: folded polynomial, 1: tensor-core layers
   gnn::PolyCoef pc{};                    // folded coefficients of the current weights
   bool pc_dirty = true;
-  // polynomial-form node rows (x, y, z, 0): the input D^-1/2 r, y1, y2 (n each) and w (4 x n)
-  float4 *px = nullptr, *py1 = nullptr, *py2 = nullptr, *pw = nullptr;
+  // polynomial-form FP16 node rows (gnn::Row16): the input sigma D^-1/2 r, y1, y2 (n each) and w
+  // (4 x n); xstat: the rows' sum of d r^2 and sigma
+  gnn::Row16 *px = nullptr, *py1 = nullptr, *py2 = nullptr, *pw = nullptr;
+  float* xstat = nullptr;
   float* bpart = nullptr;  // block partials of the fused beta pass (4 per 256 nodes)
   int adam_t = 0;
   bool train_bufs = false;
@@ -3099,7 +3101,7 @@ struct GnnState {
 void gnn_free(GnnState* g) {
   void* bufs[] = {g->ptr, g->idx, g->inv_deg, g->params, g->grad, g->m, g->v, g->Wb, g->x, g->xg,
                   g->G0, g->G1, g->G2, g->wpart, g->spart, g->scount, g->losses, g->z, g->rprev, g->tmp,
-                  g->px, g->py1, g->py2, g->pw, g->bpart, g->d16, g->pid, g->pptr, g->ptab};
+                  g->px, g->py1, g->py2, g->pw, g->xstat, g->bpart, g->d16, g->pid, g->pptr, g->ptab};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int l = 0; l <= gnn::NL; l++) {
@@ -3217,7 +3219,8 @@ void gnn_apply_dev(sfem_handle* h, const float* r, float* out, const int* done, 
   if (train)
     gnn::launch_apply_train(g->graph(), r, dinv, g->params, g->Wb, g->h, g->x, g->G0, g->G1, g->G2, out, h->stream);
   else if (g->infer_mode == 0)
-    gnn::launch_apply_poly(g->graph(), r, dinv, g->pc, g->px, g->py1, g->py2, g->pw, out, done, h->stream);
+    gnn::launch_apply_poly(g->graph(), r, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->xstat, out, done, h->stream,
+                           g->bpart, h->counter);
   else
     gnn::launch_apply(g->graph(), r, dinv, g->params, g->Wb, g->h, out, done, h->stream);
 }
@@ -3284,13 +3287,13 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   float* part = reinterpret_cast<float*>(h->partials);
   const float* dinv = w.dinv + o;
   // the polynomial's input rows D^-1/2 r, formed by the update kernel from the second pass on
-  float4* xs = g->infer_mode == 0 ? g->px : nullptr;
+  gnn::Row16* xs = g->infer_mode == 0 ? g->px : nullptr;
   auto precondition = [&](bool with_beta) {
     if (h->cs_on && g->infer_mode == 0) {
       // two-level: y = W B^T r, then the polynomial's last pass adds B y to M(r) and forms beta, z.r
       launch_coarse_restrict_gemv(h->cv(), w.r + o, h->stream);
-      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->z + o, done,
-                             h->stream, with_beta ? g->rprev + o : nullptr, g->bpart, h->counter,
+      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->xstat, g->z + o,
+                             done, h->stream, g->bpart, h->counter, with_beta ? g->rprev + o : nullptr,
                              with_beta ? h->scal : nullptr, with_beta, CoarseAdd{h->cs_aid, h->cs_d, h->cs_y});
       return;
     }
@@ -3303,8 +3306,8 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
       return;
     }
     if (g->infer_mode == 0) {
-      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->z + o, done,
-                             h->stream, with_beta ? g->rprev + o : nullptr, g->bpart, h->counter,
+      gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->xstat, g->z + o,
+                             done, h->stream, g->bpart, h->counter, with_beta ? g->rprev + o : nullptr,
                              with_beta ? h->scal : nullptr, with_beta);
     } else {
       gnn::launch_apply(g->graph(), w.r + o, dinv, g->params, g->Wb, g->h, g->z + o, done, h->stream);
@@ -3347,7 +3350,8 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
       }
       if (h->profiling) h->prof_launches++;
       launch_fcg_update_patch<float>(h->nbc, h->N, krylov_bslot<float>(h), reinterpret_cast<const float*>(h->partial), x,
-                                     w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream, xs ? w.dinv : nullptr, xs);
+                                     w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream, xs ? w.dinv : nullptr, xs,
+                                     g->xstat);
       precondition(true);
     }
   }
@@ -3499,6 +3503,12 @@ int sfem_gnn_init(sfem_handle* h, uint64_t seed) {
   TRY(dalloc(&g->py1, (size_t)n));
   TRY(dalloc(&g->py2, (size_t)n));
   TRY(dalloc(&g->pw, 4 * (size_t)n));
+  TRY(dalloc(&g->xstat, 2));
+  {
+    const float xs0[2] = {0.f, 1.f};
+    CU(cudaMemcpyAsync(g->xstat, xs0, sizeof(xs0), cudaMemcpyHostToDevice, h->stream));
+    TRY(sync(h));
+  }
   TRY(dalloc(&g->bpart, 4 * (size_t)((n + 255) / 256) + 64));
   TRY(dalloc(&g->spart, 4096));
   TRY(dalloc(&g->scount, 1));

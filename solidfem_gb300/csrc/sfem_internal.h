@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "sfem_gnn.h"
+
 namespace sfem {
 
 enum Mode {
@@ -153,11 +155,13 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
 
 // fused Krylov update for the patch product (assembles q at shared nodes: bslot[g] = (first
 // partial slot, count), count 0 for nodes of one patch); with xs, also the preconditioner's
-// input rows D^-1/2 r (x, y, z, 0) of the free nodes
+// input rows sigma D^-1/2 r of the free nodes (FP16, gnn::Row16), sigma from the sum of d r^2 that
+// the previous update left in xstat[0]; the update leaves sigma in xstat[1] and its own sum in
+// xstat[0]
 template <typename T>
 void launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x, T* r, T* rprev,
                              const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
-                             const T* dinv = nullptr, float4* xs = nullptr);
+                             const T* dinv = nullptr, gnn::Row16* xs = nullptr, float* xstat = nullptr);
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x, T* r, const T* p,
                             const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
@@ -361,16 +365,18 @@ namespace gnn {
 // fused into the first and last); Wb holds the 3 packed BF16 weight sets (k_gnn_pack)
 void launch_apply(const Graph& g, const float* r, const float* dinv, const float* params, const __nv_bfloat16* Wb,
                   __nv_bfloat16* const* h, float* out, const int* done, cudaStream_t st);
-// the same M(r) through the folded polynomial: six gather passes over node rows of 16 bytes
-// (x, y, z, 0); x4, y1, y2: n rows, w: 4 x n rows.  x4 = D^-1/2 r is formed first unless
-// x_ready (the flexible-CG update wrote it).  With s (flexible CG), the last pass also forms
-// the Polak-Ribiere beta from r, rprev (like k_fcg_beta).
-void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, float4* x4, float4* y1,
-                       float4* y2, float4* w, float* out, const int* done, cudaStream_t st,
-                       const float* rprev = nullptr, float* partials = nullptr, unsigned* counter = nullptr,
-                       CgScalars* s = nullptr, bool x_ready = false, CoarseAdd ca = CoarseAdd{nullptr, nullptr, nullptr});
-// x4 rows = D^-1/2 r (r, dinv: 3n)
-void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float4* x4, cudaStream_t st);
+// the same M(r) through the folded polynomial: six gather passes over FP16 node rows (Row16)
+// scaled by sigma (xstat); x4, y1, y2: n rows, w: 4 x n rows.  x4 = sigma D^-1/2 r is formed first
+// (with sigma from sum d r^2) unless x_ready (the flexible-CG update wrote it and xstat).
+// partials / counter: scratch of the fixed-order sums.  With s (flexible CG), the last pass also
+// forms the Polak-Ribiere beta from r, rprev (like k_fcg_beta).
+void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, Row16* x4, Row16* y1,
+                       Row16* y2, Row16* w, float* xstat, float* out, const int* done, cudaStream_t st,
+                       float* partials, unsigned* counter, const float* rprev = nullptr, CgScalars* s = nullptr,
+                       bool x_ready = false, CoarseAdd ca = CoarseAdd{nullptr, nullptr, nullptr});
+// x4 rows = sigma D^-1/2 r (r, dinv: 3n), sigma and sum d r^2 into xstat
+void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float* xstat, float* partials, unsigned* counter,
+                        Row16* x4, cudaStream_t st);
 // the same M(r) keeping the activations h0..h3 of S and x = D^-1/2 r (training)
 void launch_apply_train(const Graph& g, const float* r, const float* dinv, const float* params,
                         const __nv_bfloat16* Wb, __nv_bfloat16* const* h, float* x, float* G0, float* G1, float* G2,

@@ -26,6 +26,7 @@
 #include "sfem_internal.h"
 #include "sfem_pdl.cuh"
 #include "sfem_reduce.cuh"
+#include "sfem_row16.cuh"
 
 namespace sfem {
 
@@ -2115,12 +2116,17 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
                                                                T* __restrict__ r, T* __restrict__ rprev,
                                                                const T* __restrict__ p, const T* __restrict__ q,
                                                                Reduce red, CgScalars* s, const T* __restrict__ dinv,
-                                                               float4* __restrict__ xs) {
+                                                               gnn::Row16* __restrict__ xs, float* __restrict__ xstat) {
   pdl_wait();
   pdl_launch_dependents();
   if (s->done) return;
   const T a = (T)s->alpha;
   T rr = T(0);
+  float xx = 0.f;
+  // the rows' scale from the previous rows' sum (xstat[0] is overwritten by the last block only,
+  // after every block has read it)
+  const float sg = xs ? gnn::row16_scale(xstat[0], 3 * (N - nbc)) : 1.f;
+  if (xs && blockIdx.x == 0 && threadIdx.x == 0) xstat[1] = sg;
   for (int64_t g = nbc + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = 3 * g;
     T qq[3];
@@ -2135,12 +2141,20 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
       r[o + c2] = rn[c2];
       rr += rn[c2] * rn[c2];
     }
-    if (xs)  // the preconditioner's input D^-1/2 r
-      xs[g - nbc] = make_float4((float)(rn[0] * sqrt(dinv[o])), (float)(rn[1] * sqrt(dinv[o + 1])),
-                                (float)(rn[2] * sqrt(dinv[o + 2])), 0.f);
+    if (xs) {  // the preconditioner's input sigma D^-1/2 r
+      float xv[3];
+#pragma unroll
+      for (int c2 = 0; c2 < 3; c2++) {
+        const float d = (float)dinv[o + c2], rv = (float)rn[c2];
+        xx += d * rv * rv;
+        xv[c2] = sg * rv * sqrtf(d);
+      }
+      xs[g - nbc] = gnn::pack16(xv[0], xv[1], xv[2]);
+    }
   }
-  T v[1] = {rr}, tot[1];
-  if (reduce_last<T, 1>(v, red, tot) && threadIdx.x == 0) {
+  T v[2] = {rr, (T)xx}, tot[2];
+  if (reduce_last<T, 2>(v, red, tot) && threadIdx.x == 0) {
+    if (xs) xstat[0] = (float)tot[1];
     s->rr = (double)tot[0];
     s->it += 1;
     if (!isfinite(s->rr)) {
@@ -2162,7 +2176,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
 __device__ __forceinline__ void fcg_node(int64_t g, float a, float* __restrict__ x, float* __restrict__ r,
                                          float* __restrict__ rprev, const float* __restrict__ p,
                                          const float* __restrict__ q, const float* __restrict__ dinv,
-                                         float4* __restrict__ xs, int64_t nbc, float& rr) {
+                                         gnn::Row16* __restrict__ xs, float sg, int64_t nbc, float& rr, float& xx) {
   const int64_t o = 3 * g;
   float rn[3];
 #pragma unroll
@@ -2174,7 +2188,16 @@ __device__ __forceinline__ void fcg_node(int64_t g, float a, float* __restrict__
     r[o + c] = rn[c];
     rr += rn[c] * rn[c];
   }
-  if (xs) xs[g - nbc] = make_float4(rn[0] * sqrtf(dinv[o]), rn[1] * sqrtf(dinv[o + 1]), rn[2] * sqrtf(dinv[o + 2]), 0.f);
+  if (xs) {
+    float xv[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float d = dinv[o + c];
+      xx += d * rn[c] * rn[c];
+      xv[c] = sg * rn[c] * sqrtf(d);
+    }
+    xs[g - nbc] = gnn::pack16(xv[0], xv[1], xv[2]);
+  }
 }
 __device__ __forceinline__ void ld12(const float* __restrict__ a, float (&v)[12]) {
   const float4* a4 = reinterpret_cast<const float4*>(a);
@@ -2196,12 +2219,16 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_vec(int64_t nbc, int64_
                                                              float* __restrict__ r, float* __restrict__ rprev,
                                                              const float* __restrict__ p, const float* __restrict__ q,
                                                              Reduce red, CgScalars* s, const float* __restrict__ dinv,
-                                                             float4* __restrict__ xs) {
+                                                             gnn::Row16* __restrict__ xs, float* __restrict__ xstat) {
   pdl_wait();
   pdl_launch_dependents();
   if (s->done) return;
   const float a = (float)s->alpha;
-  float rr = 0.f;
+  float rr = 0.f, xx = 0.f;
+  // the rows' scale from the previous rows' sum (xstat[0] is overwritten by the last block only,
+  // after every block has read it)
+  const float sg = xs ? gnn::row16_scale(xstat[0], 3 * (N - nbc)) : 1.f;
+  if (xs && blockIdx.x == 0 && threadIdx.x == 0) xstat[1] = sg;
   const int64_t g0a = (nbc + 3) & ~(int64_t)3, g0 = g0a < N ? g0a : N;
   const int64_t ng = (N - g0) / 4, gend = g0 + 4 * ng;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
@@ -2225,17 +2252,20 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_vec(int64_t nbc, int64_
     st12(r + o, rn);
     if (xs) {
 #pragma unroll
+      for (int i = 0; i < 12; i++) xx += dv[i] * rn[i] * rn[i];
+#pragma unroll
       for (int m = 0; m < 4; m++)
-        xs[g + m - nbc] = make_float4(rn[3 * m] * sqrtf(dv[3 * m]), rn[3 * m + 1] * sqrtf(dv[3 * m + 1]),
-                                      rn[3 * m + 2] * sqrtf(dv[3 * m + 2]), 0.f);
+        xs[g + m - nbc] = gnn::pack16(sg * rn[3 * m] * sqrtf(dv[3 * m]), sg * rn[3 * m + 1] * sqrtf(dv[3 * m + 1]),
+                                      sg * rn[3 * m + 2] * sqrtf(dv[3 * m + 2]));
     }
   }
   // the nodes before the first group and after the last
   const int64_t nhead = g0 - nbc, ntail = N - gend;
-  if (tid < nhead) fcg_node(nbc + tid, a, x, r, rprev, p, q, dinv, xs, nbc, rr);
-  else if (tid < nhead + ntail) fcg_node(gend + (tid - nhead), a, x, r, rprev, p, q, dinv, xs, nbc, rr);
-  float v[1] = {rr}, tot[1];
-  if (reduce_last<float, 1>(v, red, tot) && threadIdx.x == 0) {
+  if (tid < nhead) fcg_node(nbc + tid, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx);
+  else if (tid < nhead + ntail) fcg_node(gend + (tid - nhead), a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx);
+  float v[2] = {rr, xx}, tot[2];
+  if (reduce_last<float, 2>(v, red, tot) && threadIdx.x == 0) {
+    if (xs) xstat[0] = tot[1];
     s->rr = (double)tot[0];
     s->it += 1;
     if (!isfinite(s->rr)) {
@@ -2253,25 +2283,25 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_vec(int64_t nbc, int64_
 template <typename T>
 void launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x,
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
-                             const T* dinv, float4* xs) {
+                             const T* dinv, gnn::Row16* xs, float* xstat) {
   if constexpr (std::is_same<T, float>::value) {
     if (bslot == nullptr) {  // q complete: the grouped update
       static const int wave_v = resident_ctas(k_fcg_update_vec, kThreads, 0);
       const int64_t groups = (N - nbc) / 4 + 1;
       count_launch();
       launch_pdl(k_fcg_update_vec, std::max(1, (int)std::min<int64_t>(wave_v, (groups + kThreads - 1) / kThreads)),
-                 kThreads, 0, st, nbc, N, x, r, rprev, p, q, red, s, dinv, xs);
+                 kThreads, 0, st, nbc, N, x, r, rprev, p, q, red, s, dinv, xs, xstat);
       return;
     }
   }
   count_launch();
   static const int wave = resident_ctas(k_fcg_update_patch<T>, kThreads, 0);
   launch_pdl(k_fcg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bslot, partial, x, r,
-             rprev, p, q, red, s, dinv, xs);
+             rprev, p, q, red, s, dinv, xs, xstat);
 }
 template void launch_fcg_update_patch<float>(int64_t, int64_t, const int2*, const float*, float*,
                                              float*, float*, const float*, const float*, Reduce, CgScalars*,
-                                             cudaStream_t, const float*, float4*);
+                                             cudaStream_t, const float*, gnn::Row16*, float*);
 
 // 12 consecutive values (4 nodes) with 16-byte loads and stores, FP64
 __device__ __forceinline__ void ld12(const double* __restrict__ a, double (&v)[12]) {

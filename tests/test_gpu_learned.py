@@ -53,8 +53,9 @@ def test_forward_matches_fp64_oracle(mode):
     err_ss = rel(ss_g, ss_o)
     print(f"M(r) GPU ({mode}) vs FP64 oracle: rel err {err:.2e}; S^T S part {err_ss:.2e}; {net.graph_form()}")
     assert err < 2e-2 and err_ss < 3e-2
-    if mode == "poly":  # FP32 arithmetic on the folded coefficients: no BF16 activations
-        assert err_ss < 1e-4
+    if mode == "poly":  # FP32 arithmetic on the folded coefficients over FP16 node rows (11-bit
+        # significand, scaled into range): about 3.5e-4 here in a numpy model of the same rounding
+        assert err_ss < 2e-3
         # a lattice's free nodes fall in 3 x 3 x 3 neighbour patterns (interior, faces, edges,
         # corners; the layer above the clamped face is a class of its own)
         assert net.graph_form()[0] == "patterns"
@@ -84,7 +85,7 @@ def test_forward_without_shared_patterns():
     c = np.exp(net.get_params().astype(np.float64)[go.OFF_C])
     err_ss = rel(out_g - c * dinv * r, out_o - c * dinv * r)
     print(f"M(r) GPU (poly, per-node deltas) vs FP64 oracle: S^T S part {err_ss:.2e}")
-    assert err_ss < 1e-4
+    assert err_ss < 2e-3  # FP16 node rows, as above
 
 
 @pytest.mark.parametrize("mode", ["energy", "residual"])
