@@ -18,6 +18,7 @@
 
 #include <algorithm>
 
+#include "sfem_coarse.cuh"
 #include "sfem_internal.h"
 
 namespace sfem {
@@ -25,38 +26,19 @@ namespace {
 
 constexpr int kCT = 256;
 
-// Run sums of s_a = (sum r_i, sum d_i x r_i): block b of kCoarseBlock free nodes, four nodes per
-// thread (coalesced), their six terms staged in shared memory; then each run of the block summed
-// in node order by one thread, to runpart[c * n_runs + k]
+// Run sums of s_a = (sum r_i, sum d_i x r_i): restriction block b (coarse_block_start, up to
+// kCoarseSpan free nodes), its nodes' six terms staged in shared memory by coalesced loads; then each
+// run of the block summed in node order by one thread, to runpart[c * n_runs + k]
 __global__ void __launch_bounds__(kCT) k_coarse_runs(CoarseView cv, const float* __restrict__ r) {
-  __shared__ float sv[6][kCoarseBlock];
-  const int64_t base = (int64_t)blockIdx.x * kCoarseBlock;
-#pragma unroll
-  for (int m = 0; m < kCoarseBlock / kCT; m++) {
-    const int t = threadIdx.x + kCT * m;
+  __shared__ float sv[6][kCoarseSpan];
+  const int64_t base = coarse_block_start(blockIdx.x, cv.n_blocks, cv.blk_off, cv.nf);
+  const int cnt = (int)(coarse_block_start(blockIdx.x + 1, cv.n_blocks, cv.blk_off, cv.nf) - base);
+  for (int t = threadIdx.x; t < cnt; t += kCT) {
     const int64_t i = base + t;
-    if (i < cv.nf) {
-      const float4 di = cv.d[i];
-      const float r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
-      sv[0][t] = r0;
-      sv[1][t] = r1;
-      sv[2][t] = r2;
-      sv[3][t] = di.y * r2 - di.z * r1;
-      sv[4][t] = di.z * r0 - di.x * r2;
-      sv[5][t] = di.x * r1 - di.y * r0;
-    }
+    coarse_stage(cv, i, base, r[3 * i], r[3 * i + 1], r[3 * i + 2], sv);
   }
   __syncthreads();
-  const int k1 = cv.blk_run[blockIdx.x + 1];
-  for (int k = cv.blk_run[blockIdx.x] + threadIdx.x; k < k1; k += kCT) {
-    const int j0 = (int)(cv.run_start[k] - base), j1 = (int)(cv.run_start[k + 1] - base);
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int j = j0; j < j1; j++)
-#pragma unroll
-      for (int c = 0; c < 6; c++) acc[c] += sv[c][j];
-#pragma unroll
-    for (int c = 0; c < 6; c++) cv.runpart[(int64_t)c * cv.n_runs + k] = acc[c];
-  }
+  coarse_block_runs(cv, blockIdx.x, base, sv);
 }
 
 // s_a from aggregate a's run sums: one CTA per aggregate, thread t adding runs t, t + 256, ... of the
@@ -145,6 +127,11 @@ void launch_coarse_restrict_gemv(const CoarseView& cv, const float* r, cudaStrea
   if (cv.n_blocks <= 0) return;
   count_launch();
   k_coarse_runs<<<(unsigned)cv.n_blocks, kCT, 0, st>>>(cv, r);
+  launch_coarse_sum_gemv(cv, st);
+}
+
+void launch_coarse_sum_gemv(const CoarseView& cv, cudaStream_t st) {
+  if (cv.n_blocks <= 0) return;
   count_launch();
   k_coarse_aggsum<<<(unsigned)cv.n_agg, kCT, 0, st>>>(cv);
   count_launch();

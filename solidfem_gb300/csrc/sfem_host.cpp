@@ -134,12 +134,12 @@ struct sfem_handle {
   __half* cs_W = nullptr;
   float cs_w_inv_scale = 1.f;
   float *cs_s = nullptr, *cs_y = nullptr;
-  int cs_n_runs = 0, cs_n_blocks = 0;
+  int cs_n_runs = 0, cs_n_blocks = 0, cs_blk_off = 0;
   int32_t *cs_run_start = nullptr, *cs_blk_run = nullptr, *cs_agg_run_ptr = nullptr, *cs_agg_run = nullptr;
   float* cs_runpart = nullptr;
   CoarseView cv() const {
     return CoarseView{cs_n_agg,   cs_ld,     nf,        cs_aid,      cs_d,         cs_W,           cs_w_inv_scale,
-                      cs_s,       cs_y,      cs_n_runs, cs_n_blocks, cs_run_start, cs_blk_run,     cs_agg_run_ptr,
+                      cs_s,       cs_y,      cs_n_runs, cs_n_blocks, cs_blk_off,   cs_run_start,   cs_blk_run,     cs_agg_run_ptr,
                       cs_agg_run, cs_runpart};
   }
   // node data (reshuffled, 3N)
@@ -1786,12 +1786,14 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   });
   h->cs_w_inv_scale = std::ldexp(1.f, -wexp);
   const clk::time_point t3 = clk::now();
-  // restriction runs: blocks of kCoarseBlock consecutive free nodes, split where the aggregate
-  // changes and after kCoarseRun nodes; then every aggregate's runs in increasing order
-  const int64_t nblk = (nf + kCoarseBlock - 1) / kCoarseBlock;
+  // restriction runs: the blocks of the flexible-CG update's CTAs (coarse_block_start), split where
+  // the aggregate changes and after kCoarseRun nodes; then every aggregate's runs in increasing order
+  const int64_t N = h->N, g0a = (nbc + 3) & ~(int64_t)3, g0 = g0a < N ? g0a : N, ngrp = (N - g0) / 4;
+  const int64_t nblk = std::max<int64_t>(1, (ngrp + 255) / 256);
+  const int blk_off = (int)(g0 - nbc);
   std::vector<int32_t> rstart, rblk((size_t)nblk + 1, 0), ragg;
   for (int64_t b = 0; b < nblk; b++) {
-    const int64_t i0 = b * kCoarseBlock, i1 = std::min<int64_t>(nf, i0 + kCoarseBlock);
+    const int64_t i0 = coarse_block_start(b, nblk, blk_off, nf), i1 = coarse_block_start(b + 1, nblk, blk_off, nf);
     for (int64_t i = i0; i < i1; i++)
       if (i == i0 || aid[i] != aid[i - 1] || i - rstart.back() == kCoarseRun) {
         rstart.push_back((int32_t)i);
@@ -1832,6 +1834,7 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   if (nrun > 0) CU(cudaMemcpyAsync(h->cs_agg_run, arun.data(), arun.size() * 4, cudaMemcpyHostToDevice, h->stream));
   h->cs_n_runs = (int)nrun;
   h->cs_n_blocks = (int)nblk;
+  h->cs_blk_off = blk_off;
   TRY(sync(h));
   h->cs_n_agg = (int)na;
   h->cs_ld = ld;
@@ -2552,7 +2555,7 @@ void coarse_release(sfem_handle* h) {
   h->cs_s = h->cs_y = nullptr;
   h->cs_run_start = h->cs_blk_run = h->cs_agg_run_ptr = h->cs_agg_run = nullptr;
   h->cs_runpart = nullptr;
-  h->cs_n_runs = h->cs_n_blocks = 0;
+  h->cs_n_runs = h->cs_n_blocks = h->cs_blk_off = 0;
   h->cs_on = false;
   h->cs_n_agg = h->cs_ld = 0;
 }
@@ -3288,10 +3291,15 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   const float* dinv = w.dinv + o;
   // the polynomial's input rows D^-1/2 r, formed by the update kernel from the second pass on
   gnn::Row16* xs = g->infer_mode == 0 ? g->px : nullptr;
-  auto precondition = [&](bool with_beta) {
+  const CoarseView cvw = h->cv();
+  auto precondition = [&](bool with_beta, bool runs_done) {
     if (h->cs_on && g->infer_mode == 0) {
-      // two-level: y = W B^T r, then the polynomial's last pass adds B y to M(r) and forms beta, z.r
-      launch_coarse_restrict_gemv(h->cv(), w.r + o, h->stream);
+      // two-level: y = W B^T r (the update may have formed the restriction's run sums), then the
+      // polynomial's last pass adds B y to M(r) and forms beta, z.r
+      if (runs_done)
+        launch_coarse_sum_gemv(cvw, h->stream);
+      else
+        launch_coarse_restrict_gemv(cvw, w.r + o, h->stream);
       gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->xstat, g->z + o,
                              done, h->stream, g->bpart, h->counter, with_beta ? g->rprev + o : nullptr,
                              with_beta ? h->scal : nullptr, with_beta, CoarseAdd{h->cs_aid, h->cs_d, h->cs_y});
@@ -3315,7 +3323,7 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
         gnn::launch_fcg_beta(n, w.r + o, g->rprev + o, g->z + o, dinv, part, h->counter, h->scal, h->stream);
     }
   };
-  precondition(false);
+  precondition(false, false);
   gnn::launch_fcg_init(n, w.r + o, g->z + o, w.p + o, part, h->counter, h->scal, h->stream);  // p_old = 0
   float* pbuf[2] = {w.p, w.p2};
   const int check_every = 16;
@@ -3349,10 +3357,11 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
         pending = true;
       }
       if (h->profiling) h->prof_launches++;
-      launch_fcg_update_patch<float>(h->nbc, h->N, krylov_bslot<float>(h), reinterpret_cast<const float*>(h->partial), x,
-                                     w.r, g->rprev, pnew, w.q, h->red(), h->scal, h->stream, xs ? w.dinv : nullptr, xs,
-                                     g->xstat);
-      precondition(true);
+      const bool runs = launch_fcg_update_patch<float>(
+          h->nbc, h->N, krylov_bslot<float>(h), reinterpret_cast<const float*>(h->partial), x, w.r, g->rprev, pnew, w.q,
+          h->red(), h->scal, h->stream, xs ? w.dinv : nullptr, xs, g->xstat,
+          h->cs_on && g->infer_mode == 0 ? &cvw : nullptr);
+      precondition(true, runs);
     }
   }
   if (pending) {

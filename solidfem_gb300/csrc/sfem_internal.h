@@ -157,11 +157,14 @@ void launch_patch_hvp(const PatchView<T>& pv, PatchBoundary pb, const T* u, cons
 // partial slot, count), count 0 for nodes of one patch); with xs, also the preconditioner's
 // input rows sigma D^-1/2 r of the free nodes (FP16, gnn::Row16), sigma from the sum of d r^2 that
 // the previous update left in xstat[0]; the update leaves sigma in xstat[1] and its own sum in
-// xstat[0]
+// xstat[0].  With cv (the two-level preconditioner) and q complete (bslot null), the same pass also
+// forms the coarse restriction's run sums (k_coarse_runs' output) and the call returns true.
+struct CoarseView;
 template <typename T>
-void launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x, T* r, T* rprev,
+bool launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x, T* r, T* rprev,
                              const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
-                             const T* dinv = nullptr, gnn::Row16* xs = nullptr, float* xstat = nullptr);
+                             const T* dinv = nullptr, gnn::Row16* xs = nullptr, float* xstat = nullptr,
+                             const CoarseView* cv = nullptr);
 template <typename T>
 void launch_cg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x, T* r, const T* p,
                             const T* q, const T* dinv, Reduce red, CgScalars* s, cudaStream_t st);
@@ -261,13 +264,22 @@ void launch_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* base, const int32_
 // z += B W B^T r over the free block: per free node its aggregate aid[i] and offset d_i from the
 // aggregate's centroid (x, y, z, 0); W the 6 n_agg square matrix R Kc^-1 R^T in FP16, scaled by a
 // power of two (w_inv_scale undoes it; rows of ld halves, ld a multiple of 8); s and y two ld-long
-// FP32 scratch vectors.  The restriction reads the free nodes in order, in
-// blocks of kCoarseBlock: block b's nodes split into runs (consecutive nodes of one aggregate, at
-// most kCoarseRun each), runs blk_run[b] .. blk_run[b+1] - 1, run k the nodes run_start[k] ..
-// run_start[k+1] - 1.  A run's six sums go to runpart (six arrays of n_runs floats); aggregate a's runs
-// are agg_run[agg_run_ptr[a] .. agg_run_ptr[a+1] - 1], in increasing order.
+// FP32 scratch vectors.  The restriction reads the free nodes in order, in n_blocks
+// blocks that match the flexible-CG update's CTAs (256 groups of four nodes, the groups starting at
+// the first node index that is a multiple of four): block b > 0 starts at free node blk_off + 1024 b,
+// block 0 at 0 and the last block ends at nf (so the first also takes the blk_off <= 3 nodes before the
+// first group and the last the <= 3 after the last group; at most kCoarseSpan nodes each).  Block b's
+// nodes split into runs (consecutive nodes of one aggregate, at most kCoarseRun each), runs
+// blk_run[b] .. blk_run[b+1] - 1, run k the nodes run_start[k] .. run_start[k+1] - 1.  A run's six sums
+// go to runpart (six arrays of n_runs floats); aggregate a's runs are agg_run[agg_run_ptr[a] ..
+// agg_run_ptr[a+1] - 1], in increasing order.
 constexpr int kCoarseBlock = 1024;
+constexpr int kCoarseSpan = 1032;
 constexpr int kCoarseRun = 32;
+// first free node of restriction block b (n_blocks blocks; b == n_blocks gives nf)
+__host__ __device__ inline int64_t coarse_block_start(int64_t b, int64_t n_blocks, int blk_off, int64_t nf) {
+  return b == 0 ? 0 : (b >= n_blocks ? nf : blk_off + (int64_t)kCoarseBlock * b);
+}
 struct CoarseView {
   int n_agg;
   int ld;
@@ -280,6 +292,7 @@ struct CoarseView {
   float* y;
   int n_runs;
   int n_blocks;
+  int blk_off;
   const int32_t* run_start;
   const int32_t* blk_run;
   const int32_t* agg_run_ptr;
@@ -297,6 +310,8 @@ struct CoarseAdd {
 void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st);
 // y = W B^T r only (the prolongation then runs inside the preconditioner's last pass)
 void launch_coarse_restrict_gemv(const CoarseView& cv, const float* r, cudaStream_t st);
+// the same after the run sums are in place (the flexible-CG update formed them)
+void launch_coarse_sum_gemv(const CoarseView& cv, cudaStream_t st);
 
 // ---- batched independent bodies: one persistent kernel per Krylov solve ----
 // Each instance (body) runs its own preconditioned CG recurrence (its own alpha, beta, r.z and

@@ -27,6 +27,7 @@
 #include "sfem_pdl.cuh"
 #include "sfem_reduce.cuh"
 #include "sfem_row16.cuh"
+#include "sfem_coarse.cuh"
 
 namespace sfem {
 
@@ -2176,9 +2177,9 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_patch(int64_t nbc, int6
 __device__ __forceinline__ void fcg_node(int64_t g, float a, float* __restrict__ x, float* __restrict__ r,
                                          float* __restrict__ rprev, const float* __restrict__ p,
                                          const float* __restrict__ q, const float* __restrict__ dinv,
-                                         gnn::Row16* __restrict__ xs, float sg, int64_t nbc, float& rr, float& xx) {
+                                         gnn::Row16* __restrict__ xs, float sg, int64_t nbc, float& rr, float& xx,
+                                         float (&rn)[3]) {
   const int64_t o = 3 * g;
-  float rn[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     x[o + c] += a * p[o + c];
@@ -2261,8 +2262,93 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_vec(int64_t nbc, int64_
   }
   // the nodes before the first group and after the last
   const int64_t nhead = g0 - nbc, ntail = N - gend;
-  if (tid < nhead) fcg_node(nbc + tid, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx);
-  else if (tid < nhead + ntail) fcg_node(gend + (tid - nhead), a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx);
+  float rn1[3];
+  if (tid < nhead) fcg_node(nbc + tid, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
+  else if (tid < nhead + ntail) fcg_node(gend + (tid - nhead), a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
+  float v[2] = {rr, xx}, tot[2];
+  if (reduce_last<float, 2>(v, red, tot) && threadIdx.x == 0) {
+    if (xs) xstat[0] = tot[1];
+    s->rr = (double)tot[0];
+    s->it += 1;
+    if (!isfinite(s->rr)) {
+      s->done = 1;
+      s->status = -3;
+    } else if (s->rr <= s->tol2) {
+      s->done = 1;
+    } else if (s->it >= s->max_it) {
+      s->done = 1;
+      s->status = 1;
+    }
+  }
+}
+
+// k_fcg_update_vec with the coarse restriction's run sums fused in (two-level preconditioner): CTA b
+// takes the 256 groups of restriction block b, one group per thread (block 0 also the nodes before
+// the first group, the last block those after the last group; coarse_block_start), stages each
+// node's six restriction terms from the new r in shared memory and sums the block's runs like
+// k_coarse_runs, so that r is not read again for the restriction.  One CTA per block, no grid stride.
+__global__ void __launch_bounds__(kThreads) k_fcg_update_runs(int64_t nbc, int64_t N, float* __restrict__ x,
+                                                              float* __restrict__ r, float* __restrict__ rprev,
+                                                              const float* __restrict__ p, const float* __restrict__ q,
+                                                              Reduce red, CgScalars* s, const float* __restrict__ dinv,
+                                                              gnn::Row16* __restrict__ xs, float* __restrict__ xstat,
+                                                              CoarseView cv) {
+  __shared__ float sv[6][kCoarseSpan];
+  pdl_wait();
+  pdl_launch_dependents();
+  if (s->done) return;
+  const float a = (float)s->alpha;
+  float rr = 0.f, xx = 0.f;
+  const float sg = xs ? gnn::row16_scale(xstat[0], 3 * (N - nbc)) : 1.f;
+  if (xs && blockIdx.x == 0 && threadIdx.x == 0) xstat[1] = sg;
+  const int64_t g0a = (nbc + 3) & ~(int64_t)3, g0 = g0a < N ? g0a : N;
+  const int64_t ng = (N - g0) / 4, gend = g0 + 4 * ng;
+  const int64_t base = coarse_block_start(blockIdx.x, cv.n_blocks, cv.blk_off, cv.nf);
+  const int64_t k = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (k < ng) {
+    const int64_t g = g0 + 4 * k, o = 3 * g;
+    float xv[12], rv[12], pv[12], qv[12], dv[12];
+    ld12(x + o, xv);
+    ld12(r + o, rv);
+    ld12(p + o, pv);
+    ld12(q + o, qv);
+    if (xs) ld12(dinv + o, dv);
+    st12(rprev + o, rv);
+    float rn[12];
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      xv[i] += a * pv[i];
+      rn[i] = rv[i] - a * qv[i];
+      rr += rn[i] * rn[i];
+    }
+    st12(x + o, xv);
+    st12(r + o, rn);
+    if (xs) {
+#pragma unroll
+      for (int i = 0; i < 12; i++) xx += dv[i] * rn[i] * rn[i];
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+        xs[g + m - nbc] = gnn::pack16(sg * rn[3 * m] * sqrtf(dv[3 * m]), sg * rn[3 * m + 1] * sqrtf(dv[3 * m + 1]),
+                                      sg * rn[3 * m + 2] * sqrtf(dv[3 * m + 2]));
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) coarse_stage(cv, g + m - nbc, base, rn[3 * m], rn[3 * m + 1], rn[3 * m + 2], sv);
+  }
+  // the nodes before the first group (block 0) and after the last (the last block)
+  const int64_t nhead = g0 - nbc, ntail = N - gend;
+  float rn1[3];
+  if (blockIdx.x == 0 && threadIdx.x < nhead) {
+    const int64_t g = nbc + threadIdx.x;
+    fcg_node(g, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
+    coarse_stage(cv, g - nbc, base, rn1[0], rn1[1], rn1[2], sv);
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x < ntail) {
+    const int64_t g = gend + threadIdx.x;
+    fcg_node(g, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
+    coarse_stage(cv, g - nbc, base, rn1[0], rn1[1], rn1[2], sv);
+  }
+  __syncthreads();
+  coarse_block_runs(cv, blockIdx.x, base, sv);
   float v[2] = {rr, xx}, tot[2];
   if (reduce_last<float, 2>(v, red, tot) && threadIdx.x == 0) {
     if (xs) xstat[0] = tot[1];
@@ -2281,27 +2367,36 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_vec(int64_t nbc, int64_
 }
 
 template <typename T>
-void launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x,
+bool launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T* partial, T* x,
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
-                             const T* dinv, gnn::Row16* xs, float* xstat) {
+                             const T* dinv, gnn::Row16* xs, float* xstat, const CoarseView* cv) {
   if constexpr (std::is_same<T, float>::value) {
+    if (bslot == nullptr && cv && cv->n_blocks > 0 && cv->n_blocks <= 4 * kMaxBlocks) {
+      // q complete, with the coarse run sums: one CTA per restriction block (the reduction's
+      // partials hold 2 floats per block: 8 kMaxBlocks floats of the 4 kMaxBlocks doubles)
+      count_launch();
+      launch_pdl(k_fcg_update_runs, (unsigned)cv->n_blocks, kThreads, 0, st, nbc, N, x, r, rprev, p, q, red, s, dinv,
+                 xs, xstat, *cv);
+      return true;
+    }
     if (bslot == nullptr) {  // q complete: the grouped update
       static const int wave_v = resident_ctas(k_fcg_update_vec, kThreads, 0);
       const int64_t groups = (N - nbc) / 4 + 1;
       count_launch();
       launch_pdl(k_fcg_update_vec, std::max(1, (int)std::min<int64_t>(wave_v, (groups + kThreads - 1) / kThreads)),
                  kThreads, 0, st, nbc, N, x, r, rprev, p, q, red, s, dinv, xs, xstat);
-      return;
+      return false;
     }
   }
   count_launch();
   static const int wave = resident_ctas(k_fcg_update_patch<T>, kThreads, 0);
   launch_pdl(k_fcg_update_patch<T>, std::min(grid_for(N - nbc), wave), kThreads, 0, st, nbc, N, bslot, partial, x, r,
              rprev, p, q, red, s, dinv, xs, xstat);
+  return false;
 }
-template void launch_fcg_update_patch<float>(int64_t, int64_t, const int2*, const float*, float*,
+template bool launch_fcg_update_patch<float>(int64_t, int64_t, const int2*, const float*, float*,
                                              float*, float*, const float*, const float*, Reduce, CgScalars*,
-                                             cudaStream_t, const float*, gnn::Row16*, float*);
+                                             cudaStream_t, const float*, gnn::Row16*, float*, const CoarseView*);
 
 // 12 consecutive values (4 nodes) with 16-byte loads and stores, FP64
 __device__ __forceinline__ void ld12(const double* __restrict__ a, double (&v)[12]) {
