@@ -72,8 +72,9 @@ __global__ void __launch_bounds__(kCT) k_coarse_aggsum(CoarseView cv) {
 }
 
 // y = W s: W row-major nc x ld FP16 (scaled by 1 / inv_scale; ld a multiple of 8, zero beyond nc), s FP32
-// (zero beyond nc).  One warp per row, each lane eight columns per 16-byte load and four loads in
-// flight; FP32 sums in a fixed order (lane partials, then a butterfly)
+// (zero beyond nc).  One warp per row, each lane eight columns per 16-byte load and eight loads in
+// flight (a row of 5,184 columns is three rounds); FP32 sums in a fixed order (lane partials, then a
+// butterfly)
 __device__ __forceinline__ float dot8(const uint4& w, const float4& a, const float4& b) {
   const float2 w0 = __half22float2(*reinterpret_cast<const __half2*>(&w.x));
   const float2 w1 = __half22float2(*reinterpret_cast<const __half2*>(&w.y));
@@ -91,6 +92,13 @@ __global__ void __launch_bounds__(kCT) k_coarse_gemv(int nc, int ld, const __hal
   const int n8 = ld / 8;
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   int c = lane;
+  for (; c + 224 < n8; c += 256) {
+    uint4 w[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) w[u] = __ldcs(Wr + c + 32 * u);
+#pragma unroll
+    for (int u = 0; u < 8; u++) acc[u & 3] += dot8(w[u], s4[2 * (c + 32 * u)], s4[2 * (c + 32 * u) + 1]);
+  }
   for (; c + 96 < n8; c += 128) {
     uint4 w[4];
 #pragma unroll

@@ -1433,14 +1433,24 @@ static int sell_assemble(sfem_handle* h) {
   T** vals = reinterpret_cast<T**>(sizeof(T) == 4 ? (void*)&h->sell_vals32 : (void*)&h->sell_vals64);
   T** ke = reinterpret_cast<T**>(sizeof(T) == 4 ? (void*)&h->sell_ke32 : (void*)&h->sell_ke64);
   if (!*vals) TRY(sell_alloc(h, vals, std::max<size_t>(9 * (size_t)h->sell_T, 1)));
+  const int mat = mat_id(h);
+  if (mat > 4) return fail(SFEM_ERR_INVALID, "the assembled operator covers materials 0-3");
+  const T* uT = disp<T>(h);
+  const ElemView<T> ev = ev_of<T>(h);
+  if constexpr (sizeof(T) == 4) {
+    if (mat == 3) {  // FP32 neo-Hookean: 24 factors per element instead of ten 12-slot blocks
+      if (!*ke) TRY(sell_alloc(h, ke, (size_t)h->E * kNhFactorsHost));
+      launch_assemble_sell_nh32(ev, uT, *ke, h->sell_T, h->sell_cptr, h->sell_code, h->nbc, h->nf, h->sell_dslot,
+                                h->dt > 0 ? h->mass : nullptr, h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0, *vals,
+                                h->stream);
+      CU(cudaGetLastError());
+      return 0;
+    }
+  }
   // 12-slot blocks per element: 16 for the corotational tangents (not symmetric), 10 otherwise
   const int nb_alloc = (h->material == SFEM_MMT_COROTATIONAL) ? 16 : 10;
   if (!*ke) TRY(sell_alloc(h, ke, (size_t)h->E * 12 * nb_alloc));
-  const T* uT = disp<T>(h);
-  const ElemView<T> ev = ev_of<T>(h);
   int nb = 10;
-  const int mat = mat_id(h);
-  if (mat > 4) return fail(SFEM_ERR_INVALID, "the assembled operator covers materials 0-3");
   with_mat<float>(mat, [&](auto m) {  // the materials 0-4 (dispatch list shared by both precisions)
     nb = launch_element_stiffness_sym<T, decltype(m)::value>(ev, uT, *ke, h->stream);
   });

@@ -244,6 +244,12 @@ template <typename T>
 void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* code, const T* Ke, int nb,
                           int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass, double inv_h2, T* vals,
                           cudaStream_t st);
+// the FP32 neo-Hookean tangent the same way through 24 factors per element (Kf: 24 E floats)
+// instead of its blocks: h_a = F^-T g_a, vol mu (g_a . g_b), vol (mu - lambda log J), vol lambda
+constexpr int kNhFactorsHost = 24;
+void launch_assemble_sell_nh32(const ElemView<float>& ev, const float* u, float* Kf, int64_t nslots, const int64_t* cptr,
+                               const uint32_t* code, int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass,
+                               double inv_h2, float* vals, cudaStream_t st);
 // q = K p over the free rows (+ p.q, alpha with s); with p_new the direction is formed on the fly,
 // p = (z or D^-1 r) + beta p_old, as the patch product does
 // (columns: col, free-node indices, or col16, differences to the row when every one fits 16 bits)

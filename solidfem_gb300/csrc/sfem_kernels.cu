@@ -1145,6 +1145,89 @@ __global__ void __launch_bounds__(kThreads) k_assemble_sell(int64_t nslots, cons
     for (int q = 0; q < 9; q++) V[32 * q] = acc[q];
   }
 }
+// FP32 neo-Hookean factors of the element tangent for the sliced-ELL assembly, kNhFactors floats per
+// element (six 16-byte stores) instead of its ten 3x3 blocks: h_a = F^-T g_a (corner-major, 12), vol mu
+// (g_a . g_b) for the ten pairs a <= b (in the blocks' order of k_element_stiffness_sym), vol (mu -
+// lambda log J), vol lambda.  Block (a, b) of any corner pair is then
+//   K_ab[i][c] = vol mu (g_a . g_b) d_ic + vol c1 (h_b)_i (h_a)_c + vol lambda (h_a)_i (h_b)_c,
+// formed where the assembly sums it (k_assemble_sell_nh): a fifth of the bytes written and read.
+constexpr int kNhFactors = 24;
+__global__ void __launch_bounds__(kThreads) k_element_factors_nh(ElemView<float> ev, const float* __restrict__ u,
+                                                                 float* __restrict__ Kf) {
+  const int64_t E = ev.E;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int4 t = ev.tets[e];
+    M3<float> X;
+#pragma unroll
+    for (int k = 0; k < 9; k++) X.a[k] = ev.X[k * E + e];
+    const float vol = ev.vol[e];
+    float mu = ev.mu, la = ev.lambda;
+    if (ev.scale) {
+      const float sc = ev.scale[e];
+      mu *= sc;
+      la *= ev.scale_la ? ev.scale_la[e] : sc;
+    }
+    M3<float> F = grad_of(u, t, X);
+    F.a[0] += 1.f;
+    F.a[4] += 1.f;
+    F.a[8] += 1.f;
+    float g[4][3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      g[0][j] = -(X.a[j] + X.a[3 + j] + X.a[6 + j]);
+      g[1][j] = X.a[j];
+      g[2][j] = X.a[3 + j];
+      g[3][j] = X.a[6 + j];
+    }
+    float J;
+    const M3<float> Fi = inverse(F, &J);
+    float f[kNhFactors];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) f[3 * a + i] = Fi.a[i] * g[a][0] + Fi.a[3 + i] * g[a][1] + Fi.a[6 + i] * g[a][2];
+    int blk = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = a; b < 4; b++, blk++) f[12 + blk] = vol * mu * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]);
+    f[22] = vol * (mu - la * dev_log<float>(J));
+    f[23] = vol * la;
+    float4* K4 = reinterpret_cast<float4*>(Kf + kNhFactors * e);
+#pragma unroll
+    for (int k = 0; k < kNhFactors / 4; k++) K4[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+  }
+}
+
+// assembly from the neo-Hookean factors: one thread per block-slot, its contributions (code = 16 e +
+// 4 a + b) formed from element e's factors and summed in the order of k_assemble_sell (deterministic)
+__global__ void __launch_bounds__(kThreads) k_assemble_sell_nh(int64_t nslots, const int64_t* __restrict__ cptr,
+                                                               const uint32_t* __restrict__ code,
+                                                               const float* __restrict__ Kf, float* __restrict__ vals) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nslots; t += (int64_t)gridDim.x * blockDim.x) {
+    float acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) acc[q] = 0.f;
+    for (int64_t c = cptr[t]; c < cptr[t + 1]; c++) {
+      const uint32_t v = code[c];
+      const int a = (int)((v >> 2) & 3), b = (int)(v & 3);
+      const int lo = a < b ? a : b, hi = a < b ? b : a;
+      const int blk = lo == 0 ? hi : lo == 1 ? 3 + hi : lo == 2 ? 5 + hi : 9;
+      const float* f = Kf + (int64_t)kNhFactors * (v >> 4);
+      const float ha[3] = {__ldg(f + 3 * a), __ldg(f + 3 * a + 1), __ldg(f + 3 * a + 2)};
+      const float hb[3] = {__ldg(f + 3 * b), __ldg(f + 3 * b + 1), __ldg(f + 3 * b + 2)};
+      const float gg = __ldg(f + 12 + blk), c1 = __ldg(f + 22), la = __ldg(f + 23);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) acc[3 * i + cc] += (i == cc ? gg : 0.f) + c1 * hb[i] * ha[cc] + la * ha[i] * hb[cc];
+    }
+    float* V = vals + 9 * (t & ~(int64_t)31) + (t & 31);
+#pragma unroll
+    for (int q = 0; q < 9; q++) V[32 * q] = acc[q];
+  }
+}
+
 // implicit dynamics: (m / h^2) I added to each free row's diagonal block
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_sell_mass(int64_t nbc, int64_t nf, const int32_t* __restrict__ dslot,
@@ -1159,6 +1242,19 @@ __global__ void __launch_bounds__(kThreads) k_sell_mass(int64_t nbc, int64_t nf,
     V[32 * 8] += m;
   }
 }
+void launch_assemble_sell_nh32(const ElemView<float>& ev, const float* u, float* Kf, int64_t nslots, const int64_t* cptr,
+                               const uint32_t* code, int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass,
+                               double inv_h2, float* vals, cudaStream_t st) {
+  count_launch();
+  k_element_factors_nh<<<grid_for(ev.E), kThreads, 0, st>>>(ev, u, Kf);
+  count_launch();
+  k_assemble_sell_nh<<<grid_for(nslots), kThreads, 0, st>>>(nslots, cptr, code, Kf, vals);
+  if (mass) {
+    count_launch();
+    k_sell_mass<float><<<grid_for(nf), kThreads, 0, st>>>(nbc, nf, dslot, mass, inv_h2, vals);
+  }
+}
+
 template <typename T>
 void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* code, const T* Ke, int nb,
                           int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass, double inv_h2, T* vals,
@@ -2282,12 +2378,13 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_vec(int64_t nbc, int64_
   }
 }
 
-// k_fcg_update_vec with the coarse restriction's run sums fused in (two-level preconditioner): CTA b
-// takes the 256 groups of restriction block b, one group per thread (block 0 also the nodes before
-// the first group, the last block those after the last group; coarse_block_start), stages each
-// node's six restriction terms from the new r in shared memory and sums the block's runs like
-// k_coarse_runs, so that r is not read again for the restriction.  One CTA per block, no grid stride.
-__global__ void __launch_bounds__(kThreads) k_fcg_update_runs(int64_t nbc, int64_t N, float* __restrict__ x,
+// k_fcg_update_vec with the coarse restriction's run sums fused in (two-level preconditioner): CTA c
+// takes restriction blocks 2c and 2c + 1 in turn (so the grid is one resident wave at the bench's
+// size), each block's 256 groups one per thread (block 0 also the nodes before the first group, the
+// last block those after the last group; coarse_block_start); it stages each node's six restriction
+// terms from the new r in shared memory and sums the block's runs like k_coarse_runs, so that r is
+// not read again for the restriction.  Four CTAs per SM (at most 64 registers).
+__global__ void __launch_bounds__(kThreads, 4) k_fcg_update_runs(int64_t nbc, int64_t N, float* __restrict__ x,
                                                               float* __restrict__ r, float* __restrict__ rprev,
                                                               const float* __restrict__ p, const float* __restrict__ q,
                                                               Reduce red, CgScalars* s, const float* __restrict__ dinv,
@@ -2303,52 +2400,57 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update_runs(int64_t nbc, int64
   if (xs && blockIdx.x == 0 && threadIdx.x == 0) xstat[1] = sg;
   const int64_t g0a = (nbc + 3) & ~(int64_t)3, g0 = g0a < N ? g0a : N;
   const int64_t ng = (N - g0) / 4, gend = g0 + 4 * ng;
-  const int64_t base = coarse_block_start(blockIdx.x, cv.n_blocks, cv.blk_off, cv.nf);
-  const int64_t k = (int64_t)blockIdx.x * kThreads + threadIdx.x;
-  if (k < ng) {
-    const int64_t g = g0 + 4 * k, o = 3 * g;
-    float xv[12], rv[12], pv[12], qv[12], dv[12];
-    ld12(x + o, xv);
-    ld12(r + o, rv);
-    ld12(p + o, pv);
-    ld12(q + o, qv);
-    if (xs) ld12(dinv + o, dv);
-    st12(rprev + o, rv);
-    float rn[12];
-#pragma unroll
-    for (int i = 0; i < 12; i++) {
-      xv[i] += a * pv[i];
-      rn[i] = rv[i] - a * qv[i];
-      rr += rn[i] * rn[i];
-    }
-    st12(x + o, xv);
-    st12(r + o, rn);
-    if (xs) {
-#pragma unroll
-      for (int i = 0; i < 12; i++) xx += dv[i] * rn[i] * rn[i];
-#pragma unroll
-      for (int m = 0; m < 4; m++)
-        xs[g + m - nbc] = gnn::pack16(sg * rn[3 * m] * sqrtf(dv[3 * m]), sg * rn[3 * m + 1] * sqrtf(dv[3 * m + 1]),
-                                      sg * rn[3 * m + 2] * sqrtf(dv[3 * m + 2]));
-    }
-#pragma unroll
-    for (int m = 0; m < 4; m++) coarse_stage(cv, g + m - nbc, base, rn[3 * m], rn[3 * m + 1], rn[3 * m + 2], sv);
-  }
-  // the nodes before the first group (block 0) and after the last (the last block)
   const int64_t nhead = g0 - nbc, ntail = N - gend;
-  float rn1[3];
-  if (blockIdx.x == 0 && threadIdx.x < nhead) {
-    const int64_t g = nbc + threadIdx.x;
-    fcg_node(g, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
-    coarse_stage(cv, g - nbc, base, rn1[0], rn1[1], rn1[2], sv);
+  for (int half = 0; half < 2; half++) {
+    const int b = 2 * blockIdx.x + half;  // the same for the whole CTA
+    if (b >= cv.n_blocks) break;
+    if (half) __syncthreads();  // the previous block's runs have read sv
+    const int64_t base = coarse_block_start(b, cv.n_blocks, cv.blk_off, cv.nf);
+    const int64_t k = (int64_t)b * kThreads + threadIdx.x;
+    if (k < ng) {
+      const int64_t g = g0 + 4 * k, o = 3 * g;
+      float xv[12], rv[12], pv[12], qv[12], dv[12];
+      ld12(x + o, xv);
+      ld12(r + o, rv);
+      ld12(p + o, pv);
+      ld12(q + o, qv);
+      if (xs) ld12(dinv + o, dv);
+      st12(rprev + o, rv);
+      float rn[12];
+#pragma unroll
+      for (int i = 0; i < 12; i++) {
+        xv[i] += a * pv[i];
+        rn[i] = rv[i] - a * qv[i];
+        rr += rn[i] * rn[i];
+      }
+      st12(x + o, xv);
+      st12(r + o, rn);
+      if (xs) {
+#pragma unroll
+        for (int i = 0; i < 12; i++) xx += dv[i] * rn[i] * rn[i];
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+          xs[g + m - nbc] = gnn::pack16(sg * rn[3 * m] * sqrtf(dv[3 * m]), sg * rn[3 * m + 1] * sqrtf(dv[3 * m + 1]),
+                                        sg * rn[3 * m + 2] * sqrtf(dv[3 * m + 2]));
+      }
+#pragma unroll
+      for (int m = 0; m < 4; m++) coarse_stage(cv, g + m - nbc, base, rn[3 * m], rn[3 * m + 1], rn[3 * m + 2], sv);
+    }
+    // the nodes before the first group (block 0) and after the last (the last block)
+    float rn1[3];
+    if (b == 0 && threadIdx.x < nhead) {
+      const int64_t g = nbc + threadIdx.x;
+      fcg_node(g, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
+      coarse_stage(cv, g - nbc, base, rn1[0], rn1[1], rn1[2], sv);
+    }
+    if (b == cv.n_blocks - 1 && threadIdx.x < ntail) {
+      const int64_t g = gend + threadIdx.x;
+      fcg_node(g, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
+      coarse_stage(cv, g - nbc, base, rn1[0], rn1[1], rn1[2], sv);
+    }
+    __syncthreads();
+    coarse_block_runs(cv, b, base, sv);
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x < ntail) {
-    const int64_t g = gend + threadIdx.x;
-    fcg_node(g, a, x, r, rprev, p, q, dinv, xs, sg, nbc, rr, xx, rn1);
-    coarse_stage(cv, g - nbc, base, rn1[0], rn1[1], rn1[2], sv);
-  }
-  __syncthreads();
-  coarse_block_runs(cv, blockIdx.x, base, sv);
   float v[2] = {rr, xx}, tot[2];
   if (reduce_last<float, 2>(v, red, tot) && threadIdx.x == 0) {
     if (xs) xstat[0] = tot[1];
@@ -2371,12 +2473,12 @@ bool launch_fcg_update_patch(int64_t nbc, int64_t N, const int2* bslot, const T*
                              T* r, T* rprev, const T* p, const T* q, Reduce red, CgScalars* s, cudaStream_t st,
                              const T* dinv, gnn::Row16* xs, float* xstat, const CoarseView* cv) {
   if constexpr (std::is_same<T, float>::value) {
-    if (bslot == nullptr && cv && cv->n_blocks > 0 && cv->n_blocks <= 4 * kMaxBlocks) {
-      // q complete, with the coarse run sums: one CTA per restriction block (the reduction's
-      // partials hold 2 floats per block: 8 kMaxBlocks floats of the 4 kMaxBlocks doubles)
+    if (bslot == nullptr && cv && cv->n_blocks > 0 && cv->n_blocks <= 8 * kMaxBlocks) {
+      // q complete, with the coarse run sums: one CTA per two restriction blocks (the reduction's
+      // partials hold 2 floats per CTA: 8 kMaxBlocks floats of the 4 kMaxBlocks doubles)
       count_launch();
-      launch_pdl(k_fcg_update_runs, (unsigned)cv->n_blocks, kThreads, 0, st, nbc, N, x, r, rprev, p, q, red, s, dinv,
-                 xs, xstat, *cv);
+      launch_pdl(k_fcg_update_runs, (unsigned)((cv->n_blocks + 1) / 2), kThreads, 0, st, nbc, N, x, r, rprev, p, q, red,
+                 s, dinv, xs, xstat, *cv);
       return true;
     }
     if (bslot == nullptr) {  // q complete: the grouped update
