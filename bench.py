@@ -316,7 +316,7 @@ def run_gpu_arm(args):
             # two-level: the coarse space of cells of coarse_cells hexes, set up once per mesh
             # (rest-state tangent) like the network's weights, outside the timed solves
             t_cs = time.perf_counter()
-            p32.set_coarse_space(args.coarse_cells * EXTENT[0] / dims[0])
+            p32.set_coarse_space(args.coarse_cells * EXTENT[0] / dims[0], modes=args.coarse_modes)
             coarse_setup_s = time.perf_counter() - t_cs
             coarse_info = p32.coarse_info()
             method = "learned+coarse"
@@ -484,6 +484,7 @@ def run_gpu_arm(args):
                             "jacobi": "Jacobi-PCG"}[method] +
                            " inner solves in FP32, FP64 residual and convergence test"),
                 "coarse_cells": args.coarse_cells if method == "learned+coarse" else None,
+                "coarse_modes": args.coarse_modes if method == "learned+coarse" else None,
                 "weights": os.path.basename(weights) if method.startswith("learned") else None,
                 "coarse_setup_s": coarse_setup_s,
                 "coarse_setup": coarse_info,
@@ -696,7 +697,9 @@ def main():
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per HVP launch, if captured")
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")
-    ap.add_argument("--coarse-cells", type=int, default=11,
+    ap.add_argument("--coarse-modes", type=int, default=12, choices=[6, 12],
+                    help="modes per coarse aggregate: 6 rigid-body, 12 affine")
+    ap.add_argument("--coarse-cells", type=int, default=13,
                     help="two-level preconditioner with the learned one: coarse-space cells of this many hexes "
                          "per axis (0: the learned preconditioner alone)")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")

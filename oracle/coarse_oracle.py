@@ -87,13 +87,15 @@ def rigid_body_basis(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8) -> sp.c
 
 
 def basis_from_factors(aid: np.ndarray, d: np.ndarray, R: np.ndarray) -> sp.csr_matrix:
-    """P from a compact form: node i's block B(d_i) R_a, the nonzero columns of R_a kept in order."""
+    """P from a compact form: node i's block B(d_i) R_a, the nonzero columns of R_a kept in order
+    (B the rigid-body modes for 6 x 6 factors, the affine ones for 12 x 12)."""
     kept = (np.abs(R).sum(axis=1) > 0).sum(axis=1)  # columns per aggregate
     first = np.concatenate([[0], np.cumsum(kept)])
+    Bf = modes if R.shape[1] == 6 else affine_modes
     rows, cols, vals = [], [], []
     for i in range(d.shape[0]):
         a = aid[i]
-        blk = modes(d[i:i + 1]) @ R[a][:, :kept[a]]
+        blk = Bf(d[i:i + 1]) @ R[a][:, :kept[a]]
         for c in range(3):
             rows.append(np.full(kept[a], 3 * i + c))
             cols.append(first[a] + np.arange(kept[a]))
@@ -110,6 +112,17 @@ def modes(d: np.ndarray) -> np.ndarray:
     for r, (i, j) in enumerate(((1, 2), (2, 0), (0, 1))):
         B[i::3, 3 + r] = -d[:, j]
         B[j::3, 3 + r] = d[:, i]
+    return B
+
+
+def affine_modes(d: np.ndarray) -> np.ndarray:
+    """B of the affine modes for nodes at offsets d: (3 n x 12), translations, then column 3 + 3 k + l
+    giving component k the coordinate d[l]."""
+    B = np.zeros((3 * d.shape[0], 12))
+    for k in range(3):
+        B[k::3, k] = 1.0
+        for l in range(3):
+            B[k::3, 3 + 3 * k + l] = d[:, l]
     return B
 
 
@@ -137,6 +150,41 @@ def rigid_body_factors(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8):
         k = int(keep.sum())
         R[a, 3:, 3:3 + k] = V[a][:, keep] / np.sqrt(lam[a][keep])
     return d, R
+
+
+def affine_basis(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8) -> sp.csr_matrix:
+    """P of the affine coarse space: per aggregate the twelve modes u_i = t + A d_i (three translations,
+    the nine entries of A), orthonormalised by a QR factorisation of the aggregate's block; modes along
+    directions where the offsets' second moment S = sum d d^T has an eigenvalue <= rtol times the largest
+    are left out (one node: all nine linear modes; collinear nodes: six).  The correction P Kc^-1 P^T
+    depends on the span only, so any orthonormal basis of it serves."""
+    na = int(aid.max()) + 1
+    cnt = np.bincount(aid, minlength=na).astype(np.float64)
+    cen = np.zeros((na, 3))
+    np.add.at(cen, aid, X)
+    cen /= cnt[:, None]
+    d = X - cen[aid]
+    rows, cols, vals = [], [], []
+    ncol = 0
+    for a in range(na):
+        idx = np.where(aid == a)[0]
+        da = d[idx]
+        lam, V = np.linalg.eigh(da.T @ da)  # ascending
+        keep = lam > rtol * max(lam[-1], 0.0)
+        e = da @ V[:, keep]  # offsets along the kept directions
+        B = np.zeros((3 * len(idx), 3 + 3 * e.shape[1]))
+        for c in range(3):
+            B[c::3, c] = 1.0
+            for m in range(e.shape[1]):
+                B[c::3, 3 + 3 * m + c] = e[:, m]
+        Q, _ = np.linalg.qr(B)
+        r_ = (3 * idx[:, None] + np.arange(3)[None, :]).ravel()
+        for j in range(Q.shape[1]):
+            rows.append(r_)
+            cols.append(np.full(len(r_), ncol))
+            vals.append(Q[:, j])
+            ncol += 1
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(3 * len(X), ncol))
 
 
 def coarse_matrix(K: sp.spmatrix, P: sp.spmatrix) -> np.ndarray:

@@ -133,3 +133,46 @@ extern "C" int sfem_coarse_factors(const double* X, int64_t n, double cell, doub
   }
   return SFEM_OK;
 }
+
+// Affine modes (twelve per aggregate): u_i = t + A d_i, columns B_i = [I, L(d_i)] with L's column
+// 3 + 3 k + l giving component k the coordinate d_i[l].  B^T B = diag(n I, S (x) I) blockwise per
+// component, S = sum d d^T, so P = B R_a is orthonormal for the translations scaled by 1 / sqrt(n) and,
+// per kept eigenpair (lambda_m, v_m) of S (ascending; lambda_m > rtol times the largest) and component
+// k, the column 3 + 3 j + k (j: the pair's rank among the kept ones) with entries v_m[l] / sqrt(lambda_m)
+// in rows 3 + 3 k + l.  R: 144 doubles per aggregate, row-major 12 x 12, dropped columns zero.
+extern "C" int sfem_coarse_factors_affine(const double* X, int64_t n, double cell, double rtol, int32_t* aid,
+                                          double* d, double* R, int64_t* n_agg) {
+  const int st = sfem_coarse_factors(X, n, cell, rtol, aid, d, nullptr, n_agg);
+  if (st != SFEM_OK || !R) return st;
+  const int64_t na = *n_agg;
+  std::vector<double> S((size_t)9 * na, 0.0), cnt((size_t)na, 0.0);
+  for (int64_t i = 0; i < n; i++) {
+    const double* di = d + 3 * i;
+    double* Sa = S.data() + 9 * aid[i];
+    cnt[aid[i]] += 1.0;
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) Sa[3 * r + c] += di[r] * di[c];
+  }
+  for (int64_t a = 0; a < na; a++) {
+    double* Ra = R + 144 * a;
+    std::fill(Ra, Ra + 144, 0.0);
+    const double inv = 1.0 / std::sqrt(cnt[a]);
+    for (int c = 0; c < 3; c++) Ra[12 * c + c] = inv;
+    double A[3][3], w[3], V[3][3];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) A[r][c] = S[9 * a + 3 * r + c];
+    symmetric_eigen3(A, w, V);
+    int order[3] = {0, 1, 2};
+    std::sort(order, order + 3, [&](int x, int y) { return w[x] < w[y]; });
+    const double wmax = std::max(w[order[2]], 0.0);
+    int j = 0;
+    for (int m : order) {
+      if (!(w[m] > rtol * wmax)) continue;
+      const double sc = 1.0 / std::sqrt(w[m]);
+      for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++) Ra[12 * (3 + 3 * k + l) + 3 + 3 * j + k] = V[l][m] * sc;
+      j++;
+    }
+  }
+  return SFEM_OK;
+}

@@ -26,9 +26,9 @@ namespace {
 
 constexpr int kCT = 256;
 
-// Run sums of s_a = (sum r_i, sum d_i x r_i): restriction block b (coarse_block_start, up to
-// kCoarseSpan free nodes), its nodes' six terms staged in shared memory by coalesced loads; then each
-// run of the block summed in node order by one thread, to runpart[c * n_runs + k]
+// Run sums of s_a = B_a^T r: restriction block b (coarse_block_start, up to kCoarseSpan free nodes), its
+// nodes' r and d staged in shared memory by coalesced loads; then each run of the block summed in node
+// order by one thread (coarse_block_runs), to runpart[c * n_runs + k]
 __global__ void __launch_bounds__(kCT) k_coarse_runs(CoarseView cv, const float* __restrict__ r) {
   __shared__ float sv[6][kCoarseSpan];
   const int64_t base = coarse_block_start(blockIdx.x, cv.n_blocks, cv.blk_off, cv.nf);
@@ -41,33 +41,35 @@ __global__ void __launch_bounds__(kCT) k_coarse_runs(CoarseView cv, const float*
   coarse_block_runs(cv, blockIdx.x, base, sv);
 }
 
-// s_a from aggregate a's run sums: one CTA per aggregate, thread t adding runs t, t + 256, ... of the
-// aggregate's list in order (one run each for aggregates of up to 256 runs), then fixed butterflies
-// within the warps and the eight warp sums in warp order (the same order on every run)
+// s_a from aggregate a's run sums (nm per run): one CTA per aggregate, thread t adding runs t, t + 256,
+// ... of the aggregate's list in order (one run each for aggregates of up to 256 runs), then fixed
+// butterflies within the warps and the eight warp sums in warp order (the same order on every run)
 __global__ void __launch_bounds__(kCT) k_coarse_aggsum(CoarseView cv) {
-  __shared__ float ws[6][kCT / 32];
+  __shared__ float ws[12][kCT / 32];
   const int a = blockIdx.x;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const int nm = cv.nm;
+  float acc[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   const int q1 = cv.agg_run_ptr[a + 1];
   for (int q = cv.agg_run_ptr[a] + threadIdx.x; q < q1; q += kCT) {
     const int k = cv.agg_run[q];
 #pragma unroll
-    for (int c = 0; c < 6; c++) acc[c] += cv.runpart[(int64_t)c * cv.n_runs + k];
+    for (int c = 0; c < 12; c++)
+      if (c < nm) acc[c] += cv.runpart[(int64_t)c * cv.n_runs + k];
   }
 #pragma unroll
-  for (int c = 0; c < 6; c++) {
+  for (int c = 0; c < 12; c++) {
     float v = acc[c];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) ws[c][w] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 6) {
+  if ((int)threadIdx.x < nm) {
     float v = 0.f;
 #pragma unroll
     for (int k = 0; k < kCT / 32; k++) v += ws[threadIdx.x][k];
-    cv.s[6 * a + threadIdx.x] = v;
+    cv.s[nm * a + threadIdx.x] = v;
   }
 }
 
@@ -113,17 +115,15 @@ __global__ void __launch_bounds__(kCT) k_coarse_gemv(int nc, int ld, const __hal
   if (lane == 0) y[row] = v * inv_scale;
 }
 
-// z_i += u_a + w_a x d_i over the free nodes
-__global__ void __launch_bounds__(kCT) k_coarse_prolong(int64_t nf, const int32_t* __restrict__ aid,
+// z_i += B_i y_a over the free nodes (coarse_prolong_term)
+__global__ void __launch_bounds__(kCT) k_coarse_prolong(int64_t nf, int nm, const int32_t* __restrict__ aid,
                                                         const float4* __restrict__ d, const float* __restrict__ y,
                                                         float* __restrict__ z) {
   for (int64_t i = (int64_t)blockIdx.x * kCT + threadIdx.x; i < nf; i += (int64_t)gridDim.x * kCT) {
-    const float* ya = y + 6 * (int64_t)aid[i];
-    const float4 di = d[i];
-    const float u0 = ya[0], u1 = ya[1], u2 = ya[2], w0 = ya[3], w1 = ya[4], w2 = ya[5];
-    z[3 * i] += u0 + (w1 * di.z - w2 * di.y);
-    z[3 * i + 1] += u1 + (w2 * di.x - w0 * di.z);
-    z[3 * i + 2] += u2 + (w0 * di.y - w1 * di.x);
+    const float3 t = coarse_prolong_term(y + (int64_t)nm * aid[i], d[i], nm);
+    z[3 * i] += t.x;
+    z[3 * i + 1] += t.y;
+    z[3 * i + 2] += t.z;
   }
 }
 
@@ -143,7 +143,7 @@ void launch_coarse_sum_gemv(const CoarseView& cv, cudaStream_t st) {
   count_launch();
   k_coarse_aggsum<<<(unsigned)cv.n_agg, kCT, 0, st>>>(cv);
   count_launch();
-  const int nc = 6 * cv.n_agg;
+  const int nc = cv.nm * cv.n_agg;
   k_coarse_gemv<<<(unsigned)((nc * 32 + kCT - 1) / kCT), kCT, 0, st>>>(nc, cv.ld, cv.W, cv.w_inv_scale, cv.s, cv.y);
 }
 
@@ -155,7 +155,7 @@ void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStr
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t want = (cv.nf + kCT - 1) / kCT;
   const unsigned grid = (unsigned)std::min<int64_t>(want > 0 ? want : 1, (int64_t)sms * 8);
-  k_coarse_prolong<<<grid, kCT, 0, st>>>(cv.nf, cv.aid, cv.d, cv.y, z);
+  k_coarse_prolong<<<grid, kCT, 0, st>>>(cv.nf, cv.nm, cv.aid, cv.d, cv.y, z);
 }
 
 }  // namespace sfem

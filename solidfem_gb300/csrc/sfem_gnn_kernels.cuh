@@ -19,6 +19,7 @@
 #include "sfem_pdl.cuh"
 #include "sfem_reduce.cuh"
 #include "sfem_row16.cuh"
+#include "sfem_coarse.cuh"
 
 namespace sfem {
 namespace gnn {
@@ -790,14 +791,13 @@ __global__ void __launch_bounds__(256) k_poly_last(Graph g, const Row16* __restr
     const float3 a = node_gather16(g, i, ud);
     const float3 wa = unpack16(w0[i]);
     const float v[3] = {(a.x + wa.x) * isg, (a.y + wa.y) * isg, (a.z + wa.z) * isg};
-    // two-level: the coarse correction u_a + w_a x d_i of the node's aggregate
+    // two-level: the coarse correction B_i y_a of the node's aggregate
     float cz[3] = {0.f, 0.f, 0.f};
     if (ca.aid) {
-      const float* ya = ca.y + 6 * (int64_t)ca.aid[i];
-      const float4 di = ca.d[i];
-      cz[0] = ya[0] + (ya[4] * di.z - ya[5] * di.y);
-      cz[1] = ya[1] + (ya[5] * di.x - ya[3] * di.z);
-      cz[2] = ya[2] + (ya[3] * di.y - ya[4] * di.x);
+      const float3 t = coarse_prolong_term(ca.y + (int64_t)ca.nm * ca.aid[i], ca.d[i], ca.nm);
+      cz[0] = t.x;
+      cz[1] = t.y;
+      cz[2] = t.z;
     }
     const int64_t o = 3 * i;
 #pragma unroll

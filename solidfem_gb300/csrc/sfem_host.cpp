@@ -127,7 +127,7 @@ struct sfem_handle {
   std::vector<double> bt_rr_h, bt_bb_h;
   // two-level preconditioner: the coarse-space correction of the learned flexible CG
   bool cs_on = false;
-  int cs_n_agg = 0, cs_ld = 0, cs_nk = 0;
+  int cs_n_agg = 0, cs_ld = 0, cs_nk = 0, cs_nm = 6;
   double cs_setup_s[3] = {0.0, 0.0, 0.0};
   int32_t* cs_aid = nullptr;
   float4* cs_d = nullptr;
@@ -138,7 +138,7 @@ struct sfem_handle {
   int32_t *cs_run_start = nullptr, *cs_blk_run = nullptr, *cs_agg_run_ptr = nullptr, *cs_agg_run = nullptr;
   float* cs_runpart = nullptr;
   CoarseView cv() const {
-    return CoarseView{cs_n_agg,   cs_ld,     nf,        cs_aid,      cs_d,         cs_W,           cs_w_inv_scale,
+    return CoarseView{cs_n_agg,   cs_nm,     cs_ld,     nf,          cs_aid,       cs_d,           cs_W,           cs_w_inv_scale,
                       cs_s,       cs_y,      cs_n_runs, cs_n_blocks, cs_blk_off,   cs_run_start,   cs_blk_run,     cs_agg_run_ptr,
                       cs_agg_run, cs_runpart};
   }
@@ -1642,7 +1642,9 @@ static void cholesky_inverse(const std::vector<double>& L, int n, std::vector<do
 
 extern "C" {
 
-int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
+int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) { return sfem_set_coarse_space_modes(h, cell, rtol, 6); }
+
+int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_t modes) {
   TRY(check_handle(h));
   TRY(set_device(h));
   TRY(sync(h));
@@ -1650,9 +1652,11 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   if (!(cell > 0.0)) return SFEM_OK;  // off
   if (h->precision != SFEM_FP32) return fail(SFEM_ERR_INVALID, "the coarse space serves the FP32 flexible CG");
   if (!(rtol >= 0.0)) return fail(SFEM_ERR_INVALID, "rtol >= 0");
+  if (modes != 6 && modes != 12) return fail(SFEM_ERR_INVALID, "modes is 6 (rigid) or 12 (affine)");
+  const int nm = modes;
   const int64_t nf = h->nf, nbc = h->nbc;
   if (nf == 0) return SFEM_OK;
-  // aggregates of the free nodes' rest positions and their rigid-body factors
+  // aggregates of the free nodes' rest positions and their modes' factors
   std::vector<double> X((size_t)3 * nf);
   CU(cudaMemcpyAsync(X.data(), h->x0 + 3 * nbc, X.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
@@ -1660,11 +1664,16 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   std::vector<double> d((size_t)3 * nf);
   int64_t na = 0;
   TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), nullptr, &na));
-  // the dense factorisation costs ~(6 n_agg)^3 / 2 multiply-adds on the host and W (6 n_agg)^2 halves:
-  // at most 2048 aggregates
-  if (na > 2048) return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates (at most 2048)", (long long)na);
-  std::vector<double> R((size_t)36 * na);
-  TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
+  // the dense factorisation costs ~(nm n_agg)^3 / 2 multiply-adds on the host and W (nm n_agg)^2 halves:
+  // at most 2048 aggregates and 12,288 modes
+  if (na > 2048 || na * nm > 12288)
+    return fail(SFEM_ERR_INVALID, "the coarse space has %lld aggregates of %d modes (at most 2048 and 12,288 modes)",
+                (long long)na, nm);
+  std::vector<double> R((size_t)nm * nm * na);
+  if (nm == 6)
+    TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
+  else
+    TRY(sfem_coarse_factors_affine(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
   using clk = std::chrono::steady_clock;
   auto secs = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
   const clk::time_point t0 = clk::now();
@@ -1686,10 +1695,11 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   // kept (non-zero) columns of every R_a and their positions in the compact coarse index
   std::vector<std::vector<int>> kc((size_t)na);
   std::vector<int> first((size_t)na + 1, 0);
+  const int nm2 = nm * nm;
   for (int64_t a = 0; a < na; a++) {
-    for (int c = 0; c < 6; c++) {
+    for (int c = 0; c < nm; c++) {
       double nz = 0.0;
-      for (int r = 0; r < 6; r++) nz += std::fabs(R[36 * a + 6 * r + c]);
+      for (int r = 0; r < nm; r++) nz += std::fabs(R[nm2 * a + nm * r + c]);
       if (nz > 0.0) kc[a].push_back(c);
     }
     first[a + 1] = first[a] + (int)kc[a].size();
@@ -1706,13 +1716,18 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   // Kc = R^T (B^T K B) R by aggregate pairs: row aggregate a sums B_i^T K_ij B_j over its nodes i
   // and their blocks j in a fixed order (one thread per aggregate row: deterministic)
   std::vector<double> Kc((size_t)nk * nk, 0.0);
-  auto Bmat = [&](int64_t i, double (&B)[3][6]) {  // [I, -[d]x]: columns e_c and e_k x d
+  auto Bmat = [&](int64_t i, double (&B)[3][12]) {  // [I, -[d]x] (rigid) or [I, L(d)] (affine)
     const double* di = &d[3 * i];
     for (int r = 0; r < 3; r++)
-      for (int c = 0; c < 6; c++) B[r][c] = (c == r) ? 1.0 : 0.0;
-    B[1][3] = -di[2]; B[2][3] = di[1];
-    B[2][4] = -di[0]; B[0][4] = di[2];
-    B[0][5] = -di[1]; B[1][5] = di[0];
+      for (int c = 0; c < nm; c++) B[r][c] = (c == r) ? 1.0 : 0.0;
+    if (nm == 6) {
+      B[1][3] = -di[2]; B[2][3] = di[1];
+      B[2][4] = -di[0]; B[0][4] = di[2];
+      B[0][5] = -di[1]; B[1][5] = di[0];
+    } else {
+      for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++) B[k][3 + 3 * k + l] = di[l];
+    }
   };
   parallel_rows(na, [&](int64_t a0, int64_t a1) {
     std::vector<int> slot((size_t)na, -1);
@@ -1723,7 +1738,7 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
       G.clear();
       for (int32_t k = aptr[a]; k < aptr[a + 1]; k++) {
         const int64_t i = anode[k];
-        double Bi[3][6];
+        double Bi[3][12];
         Bmat(i, Bi);
         for (int32_t e = rowptr[i]; e < rowptr[i + 1]; e++) {
           const int64_t j = col[e];
@@ -1731,28 +1746,28 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
           if (slot[b] < 0) {
             slot[b] = (int)touched.size();
             touched.push_back(b);
-            G.resize(G.size() + 36, 0.0);
+            G.resize(G.size() + nm2, 0.0);
           }
-          double Bj[3][6], KB[3][6];
+          double Bj[3][12], KB[3][12];
           Bmat(j, Bj);
           const double* Kij = &vals[9 * (size_t)e];
           for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 6; c++) KB[r][c] = Kij[3 * r] * Bj[0][c] + Kij[3 * r + 1] * Bj[1][c] + Kij[3 * r + 2] * Bj[2][c];
-          double* g = &G[36 * (size_t)slot[b]];
-          for (int x = 0; x < 6; x++)
-            for (int c = 0; c < 6; c++) g[6 * x + c] += Bi[0][x] * KB[0][c] + Bi[1][x] * KB[1][c] + Bi[2][x] * KB[2][c];
+            for (int c = 0; c < nm; c++) KB[r][c] = Kij[3 * r] * Bj[0][c] + Kij[3 * r + 1] * Bj[1][c] + Kij[3 * r + 2] * Bj[2][c];
+          double* g = &G[nm2 * (size_t)slot[b]];
+          for (int x = 0; x < nm; x++)
+            for (int c = 0; c < nm; c++) g[nm * x + c] += Bi[0][x] * KB[0][c] + Bi[1][x] * KB[1][c] + Bi[2][x] * KB[2][c];
         }
       }
       for (size_t t = 0; t < touched.size(); t++) {
         const int b = touched[t];
-        const double* g = &G[36 * t];
-        const double* Ra = &R[36 * a];
-        const double* Rb = &R[36 * (size_t)b];
+        const double* g = &G[nm2 * t];
+        const double* Ra = &R[nm2 * a];
+        const double* Rb = &R[nm2 * (size_t)b];
         for (size_t p = 0; p < kc[a].size(); p++)
           for (size_t q = 0; q < kc[b].size(); q++) {
             double v = 0.0;
-            for (int x = 0; x < 6; x++)
-              for (int y = 0; y < 6; y++) v += Ra[6 * x + kc[a][p]] * g[6 * x + y] * Rb[6 * y + kc[b][q]];
+            for (int x = 0; x < nm; x++)
+              for (int y = 0; y < nm; y++) v += Ra[nm * x + kc[a][p]] * g[nm * x + y] * Rb[nm * y + kc[b][q]];
             Kc[(size_t)(first[a] + p) * nk + first[b] + q] = v;
           }
         slot[b] = -1;
@@ -1764,24 +1779,24 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   if (!cholesky_lower(Kc, nk)) return fail(SFEM_ERR_INVALID, "the coarse matrix is not positive definite");
   std::vector<double> Kinv;
   cholesky_inverse(Kc, nk, Kinv);
-  // W = R Kc^-1 R^T in the modes' basis (6 n_agg square, rows padded to a multiple of 8)
-  const int nc = (int)(6 * na), ld = (nc + 7) / 8 * 8;
+  // W = R Kc^-1 R^T in the modes' basis (nm n_agg square, rows padded to a multiple of 8)
+  const int nc = (int)(nm * na), ld = (nc + 7) / 8 * 8;
   std::vector<float> W((size_t)nc * ld, 0.f);
   parallel_rows(na, [&](int64_t a0, int64_t a1) {
     for (int64_t a = a0; a < a1; a++)
       for (int64_t b = 0; b < na; b++) {
-        const double* Ra = &R[36 * a];
-        const double* Rb = &R[36 * b];
-        for (int x = 0; x < 6; x++)
-          for (int y = 0; y < 6; y++) {
+        const double* Ra = &R[nm2 * a];
+        const double* Rb = &R[nm2 * b];
+        for (int x = 0; x < nm; x++)
+          for (int y = 0; y < nm; y++) {
             double v = 0.0;
             for (size_t p = 0; p < kc[a].size(); p++) {
-              const double rx = Ra[6 * x + kc[a][p]];
+              const double rx = Ra[nm * x + kc[a][p]];
               if (rx == 0.0) continue;
               const double* Ki = &Kinv[(size_t)(first[a] + p) * nk + first[b]];
-              for (size_t q = 0; q < kc[b].size(); q++) v += rx * Ki[q] * Rb[6 * y + kc[b][q]];
+              for (size_t q = 0; q < kc[b].size(); q++) v += rx * Ki[q] * Rb[nm * y + kc[b][q]];
             }
-            W[(size_t)(6 * a + x) * ld + 6 * b + y] = (float)v;
+            W[(size_t)(nm * a + x) * ld + nm * b + y] = (float)v;
           }
       }
   }, 1);
@@ -1832,7 +1847,7 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   TRY(dalloc(&h->cs_blk_run, rblk.size()));
   TRY(dalloc(&h->cs_agg_run_ptr, arptr.size()));
   TRY(dalloc(&h->cs_agg_run, std::max<size_t>(arun.size(), 1)));
-  TRY(dalloc(&h->cs_runpart, std::max<size_t>(6 * (size_t)nrun, 1)));
+  TRY(dalloc(&h->cs_runpart, std::max<size_t>((size_t)nm * nrun, 1)));
   CU(cudaMemcpyAsync(h->cs_aid, aid.data(), aid.size() * 4, cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemcpyAsync(h->cs_d, d4.data(), d4.size() * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemcpyAsync(h->cs_W, Wh.data(), Wh.size() * sizeof(__half), cudaMemcpyHostToDevice, h->stream));
@@ -1849,6 +1864,7 @@ int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol) {
   h->cs_n_agg = (int)na;
   h->cs_ld = ld;
   h->cs_nk = nk;
+  h->cs_nm = nm;
   h->cs_setup_s[0] = secs(t0, t1);
   h->cs_setup_s[1] = secs(t1, t2);
   h->cs_setup_s[2] = secs(t2, t3);
@@ -3312,7 +3328,7 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
         launch_coarse_restrict_gemv(cvw, w.r + o, h->stream);
       gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->xstat, g->z + o,
                              done, h->stream, g->bpart, h->counter, with_beta ? g->rprev + o : nullptr,
-                             with_beta ? h->scal : nullptr, with_beta, CoarseAdd{h->cs_aid, h->cs_d, h->cs_y});
+                             with_beta ? h->scal : nullptr, with_beta, CoarseAdd{h->cs_aid, h->cs_d, h->cs_y, h->cs_nm});
       return;
     }
     if (h->cs_on) {

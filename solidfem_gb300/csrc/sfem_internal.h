@@ -288,6 +288,8 @@ __host__ __device__ inline int64_t coarse_block_start(int64_t b, int64_t n_block
 }
 struct CoarseView {
   int n_agg;
+  int nm;  // modes per aggregate: 6 (rigid: y_a = (u, w), z_i += u + w x d_i) or 12 (affine: y_a = (u, A
+           // row-major), z_i += u + A d_i); s_a = (sum r_i, sum d_i x r_i) or (sum r_i, sum r_i[k] d_i[l])
   int ld;
   int64_t nf;
   const int32_t* aid;
@@ -311,6 +313,7 @@ struct CoarseAdd {
   const int32_t* aid;
   const float4* d;
   const float* y;
+  int nm;
 };
 // z += B W B^T r (restriction, coarse product, prolongation)
 void launch_coarse_apply(const CoarseView& cv, const float* r, float* z, cudaStream_t st);
@@ -394,7 +397,7 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, Row16* x4, Row16* y1,
                        Row16* y2, Row16* w, float* xstat, float* out, const int* done, cudaStream_t st,
                        float* partials, unsigned* counter, const float* rprev = nullptr, CgScalars* s = nullptr,
-                       bool x_ready = false, CoarseAdd ca = CoarseAdd{nullptr, nullptr, nullptr});
+                       bool x_ready = false, CoarseAdd ca = CoarseAdd{nullptr, nullptr, nullptr, 6});
 // x4 rows = sigma D^-1/2 r (r, dinv: 3n), sigma and sum d r^2 into xstat
 void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float* xstat, float* partials, unsigned* counter,
                         Row16* x4, cudaStream_t st);

@@ -182,10 +182,11 @@ class FemPhysicsMatrixFree:
         o = np.ascontiguousarray(node_offsets, dtype=np.int64)
         nat.check(self._lib.sfem_set_instances(self._h, o.size - 1, o.ctypes.data_as(nat._i64p)))
 
-    def set_coarse_space(self, cell, rtol=1e-8):
+    def set_coarse_space(self, cell, rtol=1e-8, modes=6):
         """Two-level learned preconditioner: add the coarse correction P Kc^-1 P^T r of grid-cell
-        aggregates of spacing `cell` (rest-state tangent, set up once); cell <= 0 turns it off."""
-        nat.check(self._lib.sfem_set_coarse_space(self._h, float(cell), float(rtol)))
+        aggregates of spacing `cell` (rest-state tangent, set up once), P the aggregates' six
+        rigid-body modes (modes=6) or twelve affine modes (modes=12); cell <= 0 turns it off."""
+        nat.check(self._lib.sfem_set_coarse_space_modes(self._h, float(cell), float(rtol), int(modes)))
 
     def coarse_apply(self, r):
         """P Kc^-1 P^T r (free DOFs, (N_f, 3))."""

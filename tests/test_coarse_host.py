@@ -34,6 +34,35 @@ def test_factors_match_the_oracle_on_a_slab(cell):
     assert same_span(P, P_o) < 1e-12
 
 
+@pytest.mark.parametrize("cell", [4 / 64, 16 / 64])
+def test_affine_factors_span_the_oracles_affine_modes(cell):
+    m = box_lattice(32, 8, 8, extent=(0.5, 0.125, 0.125), jitter=0.2, seed=0)
+    o = Oracle(m.nodes, m.tets, m.face_nodes(2, 0), 1e5, 0.49)
+    X = o.free_positions().reshape(-1, 3)
+    aid, d, R = coarse_factors(X, cell, modes=12)
+    np.testing.assert_array_equal(aid, co.aggregate_cells(X, cell))
+    P = co.basis_from_factors(aid, d, R)
+    P_o = co.affine_basis(X, aid)
+    assert P.shape == P_o.shape
+    np.testing.assert_allclose((P.T @ P).toarray(), np.eye(P.shape[1]), atol=1e-12)
+    assert same_span(P, P_o) < 1e-12
+
+
+def test_degenerate_aggregates_drop_affine_modes():
+    rng = np.random.default_rng(4)
+    X = np.vstack([
+        rng.uniform(0.0, 1.0, size=(20, 3)),              # a full aggregate: 12 modes
+        [[2.5, 0.5, 0.5]],                                 # one point: translations only
+        [[4.2, 0.5, 0.5], [4.5, 0.5, 0.5], [4.8, 0.5, 0.5]],  # collinear: one direction, 3 + 3 modes
+    ])
+    aid, d, R = coarse_factors(X, 1.0, modes=12)
+    kept = (np.abs(R).sum(axis=1) > 0).sum(axis=1)
+    np.testing.assert_array_equal(kept[aid[[0, 20, 21]]], [12, 3, 6])
+    P = co.basis_from_factors(aid, d, R)
+    np.testing.assert_allclose((P.T @ P).toarray(), np.eye(P.shape[1]), atol=1e-12)
+    assert same_span(P, co.affine_basis(X, co.aggregate_cells(X, 1.0))) < 1e-12
+
+
 def test_degenerate_aggregates_drop_rotations():
     rng = np.random.default_rng(4)
     X = np.vstack([

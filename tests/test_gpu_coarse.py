@@ -51,24 +51,52 @@ def test_coarse_correction_matches_oracle():
         assert err <= 1e-3
 
 
+def test_affine_coarse_correction_matches_oracle():
+    """The twelve affine modes per aggregate (sfem_set_coarse_space_modes(..., 12)) against the oracle's
+    affine basis (a QR of each aggregate's block: the same span, so the same correction)."""
+    from solidfem_gb300 import FemPhysicsMatrixFree
+
+    m, fixed, f, h = slab(16, 8, 8)
+    p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
+                             material=3, precision="fp32")
+    cell = 4 * h
+    p.set_coarse_space(cell, modes=12)
+    info = p.coarse_info()
+    o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.49, 1070.0, (0, 0, 0), 3)
+    X = o.free_positions().reshape(-1, 3)
+    aid = co.aggregate_cells(X, cell)
+    P = co.affine_basis(X, aid)
+    assert info["coarse_dofs"] == P.shape[1], (info, P.shape)
+    K = co.probe_tangent(o)
+    Kc = co.coarse_matrix(K, P)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        r = rng.normal(size=3 * o.n_free)
+        z_ref = P @ np.linalg.solve(Kc, P.T @ r)
+        z = p.coarse_apply(r.reshape(-1, 3)).ravel()
+        err = np.linalg.norm(z - z_ref) / np.linalg.norm(z_ref)
+        print(f"affine coarse correction vs oracle ({P.shape[1]} coarse DOFs): {err:.2e}")
+        assert err <= 1e-3  # W in FP16, as above
+
+
 def test_two_level_learned_solve_fewer_iterations_same_equilibrium():
     from solidfem_gb300 import PC_LEARNED, FemPhysicsMatrixFree
     from solidfem_gb300.learned import LearnedPreconditioner
 
     m, fixed, f, h = slab(64, 16, 16)
     res = {}
-    for cell in (0.0, 8 * h):
+    for cell, modes in ((0.0, 6), (8 * h, 6), (8 * h, 12)):
         p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
                                  material=3, precision="fp32")
         p.set_operator("assembled")
         LearnedPreconditioner(p).load(WEIGHTS)
-        p.set_coarse_space(cell)
+        p.set_coarse_space(cell, modes=modes)
         p.set_nodal_loads(f)
         st = p.newton_solve(rel_tol=1e-8, max_newton=30, max_cg=100000, precond=PC_LEARNED)
         assert st["status"] == 0 and st["rel_res"] <= 1e-8, (cell, st)
-        res[cell] = (p.get_positions(), st)
+        res[(cell, modes)] = (p.get_positions(), st)
         p.close()
-    (x1, s1), (x2, s2) = res[0.0], res[8 * h]
+    (x1, s1), (x2, s2), (x3, s3) = res[(0.0, 6)], res[(8 * h, 6)], res[(8 * h, 12)]
     o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.49, 1070.0, (0, 0, 0), 3)
     o.set_nodal_loads(f)
     r0 = np.linalg.norm(o.gradients())
@@ -76,10 +104,16 @@ def test_two_level_learned_solve_fewer_iterations_same_equilibrium():
     sh[o.reshuffle_map()] = x2
     o.set_positions_shuffled(sh)
     r2 = np.linalg.norm(o.gradients()) / r0
+    sh[o.reshuffle_map()] = x3
+    o.set_positions_shuffled(sh)
+    r3 = np.linalg.norm(o.gradients()) / r0
     err = np.linalg.norm(x2 - x1) / np.linalg.norm(x1 - m.nodes)
+    err3 = np.linalg.norm(x3 - x1) / np.linalg.norm(x1 - m.nodes)
     print(f"learned: {s1['cg_iters']} CG its in {s1['newton_iters']} Newton, {s1['seconds']:.3f} s; with the coarse "
           f"space (cells of 8h): {s2['cg_iters']} CG its in {s2['newton_iters']} Newton, {s2['seconds']:.3f} s; "
-          f"oracle |r|/|r0| {r2:.2e}, solutions differ by {err:.1e}")
-    assert r2 <= 1.5e-8
-    assert err <= 1e-6
+          f"affine modes: {s3['cg_iters']} CG its, {s3['seconds']:.3f} s; oracle |r|/|r0| {r2:.2e} / {r3:.2e}, "
+          f"solutions differ by {err:.1e} / {err3:.1e}")
+    assert r2 <= 1.5e-8 and r3 <= 1.5e-8
+    assert err <= 1e-6 and err3 <= 1e-6
     assert s2["cg_iters"] < 0.8 * s1["cg_iters"]
+    assert s3["cg_iters"] < s2["cg_iters"]
