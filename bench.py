@@ -697,9 +697,9 @@ def main():
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per HVP launch, if captured")
     ap.add_argument("--precond", default="auto", choices=["auto", "jacobi", "learned"],
                     help="auto: the learned preconditioner when trained weights exist, else Jacobi")
-    ap.add_argument("--coarse-modes", type=int, default=12, choices=[6, 12],
-                    help="modes per coarse aggregate: 6 rigid-body, 12 affine")
-    ap.add_argument("--coarse-cells", type=int, default=13,
+    ap.add_argument("--coarse-modes", type=int, default=30, choices=[6, 12, 30],
+                    help="modes per coarse aggregate: 6 rigid-body, 12 affine, 30 quadratic")
+    ap.add_argument("--coarse-cells", type=int, default=17,
                     help="two-level preconditioner with the learned one: coarse-space cells of this many hexes "
                          "per axis (0: the learned preconditioner alone)")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")

@@ -394,12 +394,16 @@ int sfem_dot_noalloc_dev(const double* a_dev, const double* b_dev, int64_t n, do
  * columns).  Call with R = NULL to learn n_agg.  No device work. */
 int sfem_coarse_factors(const double* X, int64_t n, double cell, double rtol, int32_t* aid, double* d,
                         double* R, int64_t* n_agg);
-/* The same aggregates with twelve affine modes each (u_i = t + A d_i: three translations and the nine
- * entries of A, column 3 + 3 k + l giving component k the coordinate d_i[l]), orthonormalised: R (optional,
- * 144 * n_agg doubles, row-major 12 x 12 per aggregate) from the eigenpairs of S = sum d_i d_i^T, linear
- * modes of eigenvalue <= rtol * the largest dropped (zero columns).  No device work. */
-int sfem_coarse_factors_affine(const double* X, int64_t n, double cell, double rtol, int32_t* aid, double* d,
-                               double* R, int64_t* n_agg);
+/* The same aggregates with polynomial modes: per displacement component k the F features of the offset
+ * (degree 1: F = 4, 1, dx, dy, dz, the affine motions u = t + A d_i; degree 2: F = 10, also dx^2, dy^2,
+ * dz^2, dx dy, dy dz, dz dx), column F k + m of node i's block giving component k the feature f_m(d_i),
+ * orthonormalised: R (optional, (3F)^2 * n_agg doubles, row-major per aggregate) = I (x) V L^-1/2 from
+ * the eigenpairs of the features' Gram matrix (formed on d / the aggregate's largest |d|, the scaling
+ * folded into R; column 3 j + k: component k of the j-th eigenvector, largest first), modes of eigenvalue
+ * <= max(rtol, 1e-3) * the largest dropped (zero columns, last: the floor drops nearly dependent modes,
+ * e.g. a quadratic feature along an aggregate's thin direction).  No device work. */
+int sfem_coarse_factors_poly(const double* X, int64_t n, double cell, double rtol, int32_t degree, int32_t* aid,
+                             double* d, double* R, int64_t* n_agg);
 
 /* Two-level preconditioner for the learned flexible CG of FP32 handles (extension: the reference's
  * SolveConjugateGradientMF, Math/IterativeSolvers.h:115-195, has no coarse space):
@@ -409,8 +413,9 @@ int sfem_coarse_factors_affine(const double* X, int64_t n, double cell, double r
  * matrix-vector product per iteration (W = R Kc^-1 R^T stored in FP16 times a power of two, FP32 sums).
  * cell <= 0 turns it off.  At most 2048 aggregates. */
 int sfem_set_coarse_space(sfem_handle* h, double cell, double rtol);
-/* The same with the aggregates' twelve affine modes (modes = 12, sfem_coarse_factors_affine) or their six
- * rigid-body modes (modes = 6: sfem_set_coarse_space).  At most 2048 aggregates, 12,288 coarse modes. */
+/* The same with the aggregates' six rigid-body modes (modes = 6: sfem_set_coarse_space), twelve affine
+ * modes (modes = 12) or thirty quadratic ones (modes = 30; sfem_coarse_factors_poly of degree 1 or 2).
+ * At most 2048 aggregates and 12,288 coarse modes. */
 int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_t modes);
 /* z = P Kc^-1 P^T r alone (free DOFs, host arrays), for checking the coarse correction. */
 int sfem_coarse_apply(sfem_handle* h, const double* r, double* z);

@@ -91,7 +91,7 @@ def basis_from_factors(aid: np.ndarray, d: np.ndarray, R: np.ndarray) -> sp.csr_
     (B the rigid-body modes for 6 x 6 factors, the affine ones for 12 x 12)."""
     kept = (np.abs(R).sum(axis=1) > 0).sum(axis=1)  # columns per aggregate
     first = np.concatenate([[0], np.cumsum(kept)])
-    Bf = modes if R.shape[1] == 6 else affine_modes
+    Bf = modes if R.shape[1] == 6 else (lambda dd: poly_modes(dd, 1 if R.shape[1] == 12 else 2))
     rows, cols, vals = [], [], []
     for i in range(d.shape[0]):
         a = aid[i]
@@ -115,14 +115,14 @@ def modes(d: np.ndarray) -> np.ndarray:
     return B
 
 
-def affine_modes(d: np.ndarray) -> np.ndarray:
-    """B of the affine modes for nodes at offsets d: (3 n x 12), translations, then column 3 + 3 k + l
-    giving component k the coordinate d[l]."""
-    B = np.zeros((3 * d.shape[0], 12))
+def poly_modes(d: np.ndarray, degree: int) -> np.ndarray:
+    """B of the polynomial modes for nodes at offsets d: (3 n x 3F), column F k + m giving component k
+    the feature f_m(d) (poly_features)."""
+    f = poly_features(d, degree)
+    F = f.shape[1]
+    B = np.zeros((3 * d.shape[0], 3 * F))
     for k in range(3):
-        B[k::3, k] = 1.0
-        for l in range(3):
-            B[k::3, 3 + 3 * k + l] = d[:, l]
+        B[k::3, F * k:F * (k + 1)] = f
     return B
 
 
@@ -152,12 +152,22 @@ def rigid_body_factors(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8):
     return d, R
 
 
-def affine_basis(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8) -> sp.csr_matrix:
-    """P of the affine coarse space: per aggregate the twelve modes u_i = t + A d_i (three translations,
-    the nine entries of A), orthonormalised by a QR factorisation of the aggregate's block; modes along
-    directions where the offsets' second moment S = sum d d^T has an eigenvalue <= rtol times the largest
-    are left out (one node: all nine linear modes; collinear nodes: six).  The correction P Kc^-1 P^T
-    depends on the span only, so any orthonormal basis of it serves."""
+def poly_features(d: np.ndarray, degree: int) -> np.ndarray:
+    """The node offsets' features (n x F): 1, dx, dy, dz (degree 1: F = 4), and dx^2, dy^2, dz^2,
+    dx dy, dy dz, dz dx (degree 2: F = 10)."""
+    f = [np.ones(len(d)), d[:, 0], d[:, 1], d[:, 2]]
+    if degree == 2:
+        f += [d[:, 0] ** 2, d[:, 1] ** 2, d[:, 2] ** 2, d[:, 0] * d[:, 1], d[:, 1] * d[:, 2], d[:, 2] * d[:, 0]]
+    return np.stack(f, axis=1)
+
+
+def poly_basis(X: np.ndarray, aid: np.ndarray, degree: int, rtol: float = 1e-3) -> sp.csr_matrix:
+    """P of the polynomial coarse space: per aggregate and displacement component the features of the
+    nodes' offsets from the centroid (degree 1: the twelve affine motions u = t + A d; degree 2: thirty
+    modes), orthonormalised per aggregate from the eigenpairs of the features' Gram matrix (formed on
+    d / the aggregate's largest |d|), features of eigenvalue <= rtol times the largest left out (1e-3:
+    nearly dependent modes, e.g. a quadratic feature along a thin aggregate's short direction).  The
+    correction P Kc^-1 P^T depends on the span only, so any orthonormal basis of it serves."""
     na = int(aid.max()) + 1
     cnt = np.bincount(aid, minlength=na).astype(np.float64)
     cen = np.zeros((na, 3))
@@ -168,22 +178,20 @@ def affine_basis(X: np.ndarray, aid: np.ndarray, rtol: float = 1e-8) -> sp.csr_m
     ncol = 0
     for a in range(na):
         idx = np.where(aid == a)[0]
-        da = d[idx]
-        lam, V = np.linalg.eigh(da.T @ da)  # ascending
+        h = np.abs(d[idx]).max()
+        f = poly_features(d[idx] / (h if h > 0 else 1.0), degree)
+        lam, V = np.linalg.eigh(f.T @ f)
         keep = lam > rtol * max(lam[-1], 0.0)
-        e = da @ V[:, keep]  # offsets along the kept directions
-        B = np.zeros((3 * len(idx), 3 + 3 * e.shape[1]))
-        for c in range(3):
-            B[c::3, c] = 1.0
-            for m in range(e.shape[1]):
-                B[c::3, 3 + 3 * m + c] = e[:, m]
-        Q, _ = np.linalg.qr(B)
+        Q = f @ (V[:, keep] / np.sqrt(lam[keep]))  # orthonormal feature columns
         r_ = (3 * idx[:, None] + np.arange(3)[None, :]).ravel()
-        for j in range(Q.shape[1]):
-            rows.append(r_)
-            cols.append(np.full(len(r_), ncol))
-            vals.append(Q[:, j])
-            ncol += 1
+        for k in range(3):
+            for j in range(Q.shape[1]):
+                v = np.zeros((len(idx), 3))
+                v[:, k] = Q[:, j]
+                rows.append(r_)
+                cols.append(np.full(len(r_), ncol))
+                vals.append(v.ravel())
+                ncol += 1
     return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(3 * len(X), ncol))
 
 

@@ -142,7 +142,7 @@ SIGNATURES = {
     "sfem_operator_info": [_vp, _i64p, _ip],
     "sfem_gnn_graph_form": [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "sfem_coarse_factors": [_dp, C.c_int64, C.c_double, C.c_double, _ip, _dp, _dp, _i64p],
-    "sfem_coarse_factors_affine": [_dp, C.c_int64, C.c_double, C.c_double, _ip, _dp, _dp, _i64p],
+    "sfem_coarse_factors_poly": [_dp, C.c_int64, C.c_double, C.c_double, C.c_int32, _ip, _dp, _dp, _i64p],
     "sfem_gnn_get_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_set_params": [_vp, C.POINTER(C.c_float)],
     "sfem_gnn_apply": [_vp, _dp, _dp],

@@ -134,43 +134,116 @@ extern "C" int sfem_coarse_factors(const double* X, int64_t n, double cell, doub
   return SFEM_OK;
 }
 
-// Affine modes (twelve per aggregate): u_i = t + A d_i, columns B_i = [I, L(d_i)] with L's column
-// 3 + 3 k + l giving component k the coordinate d_i[l].  B^T B = diag(n I, S (x) I) blockwise per
-// component, S = sum d d^T, so P = B R_a is orthonormal for the translations scaled by 1 / sqrt(n) and,
-// per kept eigenpair (lambda_m, v_m) of S (ascending; lambda_m > rtol times the largest) and component
-// k, the column 3 + 3 j + k (j: the pair's rank among the kept ones) with entries v_m[l] / sqrt(lambda_m)
-// in rows 3 + 3 k + l.  R: 144 doubles per aggregate, row-major 12 x 12, dropped columns zero.
-extern "C" int sfem_coarse_factors_affine(const double* X, int64_t n, double cell, double rtol, int32_t* aid,
-                                          double* d, double* R, int64_t* n_agg) {
+// Polynomial modes: per aggregate and displacement component k, the F features of the node's offset
+// (F = 4 for degree 1: 1, dx, dy, dz; F = 10 for degree 2: also dx^2, dy^2, dz^2, dx dy, dy dz, dz dx),
+// column F k + m of B_i giving component k the feature f_m(d_i) (degree 1: the affine motions
+// u = t + A d_i).  B^T B is block diagonal over the components with the features' Gram matrix
+// G = sum f f^T in every block, so P = B R_a is orthonormal for R_a = I (x) V L^-1/2 from G's eigenpairs
+// (L, V), eigenvalues <= max(rtol, 1e-3) times the largest dropped: column 3 j + k of R_a is component
+// k of the j-th kept eigenvector (largest eigenvalue first), so the zero columns of dropped ones come
+// last.  The floor drops nearly dependent modes (in an aggregate two node layers thick, the quadratic
+// feature along the thin direction is almost a linear one): kept, they make W's entries large and
+// cancelling, which its FP16 storage cannot carry (measured: 3,274 instead of ≈ 350 iterations).  The features are formed from d_i / h_a (h_a the aggregate's largest |d|) for the
+// eigenproblem and the scaling is folded into R_a, which therefore acts on the unscaled features.
+namespace {
+
+// eigenpairs of a symmetric n x n matrix (n <= 10, row-major), A = V diag(w) V^T, by cyclic Jacobi
+void symmetric_eigen(int n, double* A, double* w, double* V) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) V[n * i + j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 64; sweep++) {
+    double off = 0.0, dia = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) (i == j ? dia : off) += A[n * i + j] * A[n * i + j];
+    if (off == 0.0 || off <= 1e-30 * dia) break;
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double apq = A[n * p + q];
+        if (apq == 0.0) continue;
+        const double theta = (A[n * q + q] - A[n * p + p]) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < n; k++) {  // columns p, q of A
+          const double akp = A[n * k + p], akq = A[n * k + q];
+          A[n * k + p] = c * akp - sn * akq;
+          A[n * k + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < n; k++) {  // rows p, q
+          const double apk = A[n * p + k], aqk = A[n * q + k];
+          A[n * p + k] = c * apk - sn * aqk;
+          A[n * q + k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < n; k++) {
+          const double vkp = V[n * k + p], vkq = V[n * k + q];
+          V[n * k + p] = c * vkp - sn * vkq;
+          V[n * k + q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < n; i++) w[i] = A[n * i + i];
+}
+
+}  // namespace
+
+// the F features of offset d (F = 4 or 10)
+static inline void poly_features(const double* d, int F, double* f) {
+  f[0] = 1.0;
+  f[1] = d[0];
+  f[2] = d[1];
+  f[3] = d[2];
+  if (F == 10) {
+    f[4] = d[0] * d[0];
+    f[5] = d[1] * d[1];
+    f[6] = d[2] * d[2];
+    f[7] = d[0] * d[1];
+    f[8] = d[1] * d[2];
+    f[9] = d[2] * d[0];
+  }
+}
+
+constexpr double kPolyModeFloor = 1e-3;
+
+extern "C" int sfem_coarse_factors_poly(const double* X, int64_t n, double cell, double rtol, int32_t degree,
+                                        int32_t* aid, double* d, double* R, int64_t* n_agg) {
+  if (degree != 1 && degree != 2) return sfem::set_error(SFEM_ERR_INVALID, "sfem_coarse_factors_poly: degree 1 or 2");
   const int st = sfem_coarse_factors(X, n, cell, rtol, aid, d, nullptr, n_agg);
   if (st != SFEM_OK || !R) return st;
+  const int F = degree == 1 ? 4 : 10, nm = 3 * F;
   const int64_t na = *n_agg;
-  std::vector<double> S((size_t)9 * na, 0.0), cnt((size_t)na, 0.0);
+  std::vector<double> hs((size_t)na, 0.0);
+  for (int64_t i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) hs[aid[i]] = std::max(hs[aid[i]], std::fabs(d[3 * i + c]));
+  std::vector<double> G((size_t)F * F * na, 0.0);
   for (int64_t i = 0; i < n; i++) {
-    const double* di = d + 3 * i;
-    double* Sa = S.data() + 9 * aid[i];
-    cnt[aid[i]] += 1.0;
-    for (int r = 0; r < 3; r++)
-      for (int c = 0; c < 3; c++) Sa[3 * r + c] += di[r] * di[c];
+    const double h = hs[aid[i]] > 0.0 ? hs[aid[i]] : 1.0;
+    const double e[3] = {d[3 * i] / h, d[3 * i + 1] / h, d[3 * i + 2] / h};
+    double f[10];
+    poly_features(e, F, f);
+    double* Ga = G.data() + (size_t)F * F * aid[i];
+    for (int r = 0; r < F; r++)
+      for (int c = 0; c < F; c++) Ga[F * r + c] += f[r] * f[c];
   }
   for (int64_t a = 0; a < na; a++) {
-    double* Ra = R + 144 * a;
-    std::fill(Ra, Ra + 144, 0.0);
-    const double inv = 1.0 / std::sqrt(cnt[a]);
-    for (int c = 0; c < 3; c++) Ra[12 * c + c] = inv;
-    double A[3][3], w[3], V[3][3];
-    for (int r = 0; r < 3; r++)
-      for (int c = 0; c < 3; c++) A[r][c] = S[9 * a + 3 * r + c];
-    symmetric_eigen3(A, w, V);
-    int order[3] = {0, 1, 2};
-    std::sort(order, order + 3, [&](int x, int y) { return w[x] < w[y]; });
-    const double wmax = std::max(w[order[2]], 0.0);
+    double* Ra = R + (size_t)nm * nm * a;
+    std::fill(Ra, Ra + (size_t)nm * nm, 0.0);
+    double A[100], w[10], V[100];
+    std::copy(G.begin() + (size_t)F * F * a, G.begin() + (size_t)F * F * (a + 1), A);
+    symmetric_eigen(F, A, w, V);
+    int order[10];
+    for (int k = 0; k < F; k++) order[k] = k;
+    std::sort(order, order + F, [&](int x, int y) { return w[x] < w[y]; });
+    const double wmax = std::max(w[order[F - 1]], 0.0), wtol = std::max(rtol, kPolyModeFloor) * wmax;
+    // the scaling of feature m by h^-deg(m), folded into R (features act on the unscaled offsets)
+    const double h = hs[a] > 0.0 ? hs[a] : 1.0;
+    double fs[10];
+    for (int m = 0; m < F; m++) fs[m] = m == 0 ? 1.0 : (m < 4 ? 1.0 / h : 1.0 / (h * h));
     int j = 0;
-    for (int m : order) {
-      if (!(w[m] > rtol * wmax)) continue;
-      const double sc = 1.0 / std::sqrt(w[m]);
+    for (int e = F - 1; e >= 0; e--) {  // the largest first, so that a dropped mode is always the last
+      const int mm = order[e];
+      if (!(w[mm] > wtol)) continue;
+      const double sc = 1.0 / std::sqrt(w[mm]);
       for (int k = 0; k < 3; k++)
-        for (int l = 0; l < 3; l++) Ra[12 * (3 + 3 * k + l) + 3 + 3 * j + k] = V[l][m] * sc;
+        for (int m = 0; m < F; m++) Ra[(size_t)nm * (F * k + m) + 3 * j + k] = V[F * m + mm] * sc * fs[m];
       j++;
     }
   }

@@ -45,20 +45,23 @@ __global__ void __launch_bounds__(kCT) k_coarse_runs(CoarseView cv, const float*
 // ... of the aggregate's list in order (one run each for aggregates of up to 256 runs), then fixed
 // butterflies within the warps and the eight warp sums in warp order (the same order on every run)
 __global__ void __launch_bounds__(kCT) k_coarse_aggsum(CoarseView cv) {
-  __shared__ float ws[12][kCT / 32];
+  __shared__ float ws[30][kCT / 32];
   const int a = blockIdx.x;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nm = cv.nm;
-  float acc[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float acc[30];
+#pragma unroll
+  for (int c = 0; c < 30; c++) acc[c] = 0.f;
   const int q1 = cv.agg_run_ptr[a + 1];
   for (int q = cv.agg_run_ptr[a] + threadIdx.x; q < q1; q += kCT) {
     const int k = cv.agg_run[q];
 #pragma unroll
-    for (int c = 0; c < 12; c++)
+    for (int c = 0; c < 30; c++)
       if (c < nm) acc[c] += cv.runpart[(int64_t)c * cv.n_runs + k];
   }
 #pragma unroll
-  for (int c = 0; c < 12; c++) {
+  for (int c = 0; c < 30; c++) {
+    if (c >= nm) break;
     float v = acc[c];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

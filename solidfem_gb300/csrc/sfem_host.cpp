@@ -1652,7 +1652,8 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
   if (!(cell > 0.0)) return SFEM_OK;  // off
   if (h->precision != SFEM_FP32) return fail(SFEM_ERR_INVALID, "the coarse space serves the FP32 flexible CG");
   if (!(rtol >= 0.0)) return fail(SFEM_ERR_INVALID, "rtol >= 0");
-  if (modes != 6 && modes != 12) return fail(SFEM_ERR_INVALID, "modes is 6 (rigid) or 12 (affine)");
+  if (modes != 6 && modes != 12 && modes != 30)
+    return fail(SFEM_ERR_INVALID, "modes is 6 (rigid), 12 (affine) or 30 (quadratic)");
   const int nm = modes;
   const int64_t nf = h->nf, nbc = h->nbc;
   if (nf == 0) return SFEM_OK;
@@ -1673,7 +1674,7 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
   if (nm == 6)
     TRY(sfem_coarse_factors(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
   else
-    TRY(sfem_coarse_factors_affine(X.data(), nf, cell, rtol, aid.data(), d.data(), R.data(), &na));
+    TRY(sfem_coarse_factors_poly(X.data(), nf, cell, rtol, nm == 12 ? 1 : 2, aid.data(), d.data(), R.data(), &na));
   using clk = std::chrono::steady_clock;
   auto secs = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
   const clk::time_point t0 = clk::now();
@@ -1716,17 +1717,20 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
   // Kc = R^T (B^T K B) R by aggregate pairs: row aggregate a sums B_i^T K_ij B_j over its nodes i
   // and their blocks j in a fixed order (one thread per aggregate row: deterministic)
   std::vector<double> Kc((size_t)nk * nk, 0.0);
-  auto Bmat = [&](int64_t i, double (&B)[3][12]) {  // [I, -[d]x] (rigid) or [I, L(d)] (affine)
+  auto Bmat = [&](int64_t i, double (&B)[3][30]) {  // [I, -[d]x] (rigid) or I (x) features (polynomial)
     const double* di = &d[3 * i];
     for (int r = 0; r < 3; r++)
-      for (int c = 0; c < nm; c++) B[r][c] = (c == r) ? 1.0 : 0.0;
+      for (int c = 0; c < nm; c++) B[r][c] = (nm == 6 && c == r) ? 1.0 : 0.0;
     if (nm == 6) {
       B[1][3] = -di[2]; B[2][3] = di[1];
       B[2][4] = -di[0]; B[0][4] = di[2];
       B[0][5] = -di[1]; B[1][5] = di[0];
     } else {
+      const int F = nm / 3;
+      const double f[10] = {1.0, di[0], di[1], di[2], di[0] * di[0], di[1] * di[1], di[2] * di[2],
+                            di[0] * di[1], di[1] * di[2], di[2] * di[0]};
       for (int k = 0; k < 3; k++)
-        for (int l = 0; l < 3; l++) B[k][3 + 3 * k + l] = di[l];
+        for (int m = 0; m < F; m++) B[k][F * k + m] = f[m];
     }
   };
   parallel_rows(na, [&](int64_t a0, int64_t a1) {
@@ -1738,7 +1742,7 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
       G.clear();
       for (int32_t k = aptr[a]; k < aptr[a + 1]; k++) {
         const int64_t i = anode[k];
-        double Bi[3][12];
+        double Bi[3][30];
         Bmat(i, Bi);
         for (int32_t e = rowptr[i]; e < rowptr[i + 1]; e++) {
           const int64_t j = col[e];
@@ -1748,7 +1752,7 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
             touched.push_back(b);
             G.resize(G.size() + nm2, 0.0);
           }
-          double Bj[3][12], KB[3][12];
+          double Bj[3][30], KB[3][30];
           Bmat(j, Bj);
           const double* Kij = &vals[9 * (size_t)e];
           for (int r = 0; r < 3; r++)

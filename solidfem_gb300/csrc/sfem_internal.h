@@ -288,8 +288,9 @@ __host__ __device__ inline int64_t coarse_block_start(int64_t b, int64_t n_block
 }
 struct CoarseView {
   int n_agg;
-  int nm;  // modes per aggregate: 6 (rigid: y_a = (u, w), z_i += u + w x d_i) or 12 (affine: y_a = (u, A
-           // row-major), z_i += u + A d_i); s_a = (sum r_i, sum d_i x r_i) or (sum r_i, sum r_i[k] d_i[l])
+  int nm;  // modes per aggregate: 6 (rigid: y_a = (u, w), z_i += u + w x d_i, s_a = (sum r_i, sum d_i x r_i))
+           // or 3 F = 12 / 30 (polynomial, F features f(d) = 1, d (, its quadratic terms): z_i[k] +=
+           // sum_m y_a[F k + m] f_m(d_i), s_a[F k + m] = sum r_i[k] f_m(d_i))
   int ld;
   int64_t nf;
   const int32_t* aid;

@@ -34,33 +34,34 @@ def test_factors_match_the_oracle_on_a_slab(cell):
     assert same_span(P, P_o) < 1e-12
 
 
-@pytest.mark.parametrize("cell", [4 / 64, 16 / 64])
-def test_affine_factors_span_the_oracles_affine_modes(cell):
+@pytest.mark.parametrize("cell,modes", [(4 / 64, 12), (16 / 64, 12), (4 / 64, 30), (16 / 64, 30)])
+def test_polynomial_factors_span_the_oracles_modes(cell, modes):
     m = box_lattice(32, 8, 8, extent=(0.5, 0.125, 0.125), jitter=0.2, seed=0)
     o = Oracle(m.nodes, m.tets, m.face_nodes(2, 0), 1e5, 0.49)
     X = o.free_positions().reshape(-1, 3)
-    aid, d, R = coarse_factors(X, cell, modes=12)
+    aid, d, R = coarse_factors(X, cell, modes=modes)
     np.testing.assert_array_equal(aid, co.aggregate_cells(X, cell))
     P = co.basis_from_factors(aid, d, R)
-    P_o = co.affine_basis(X, aid)
+    P_o = co.poly_basis(X, aid, 1 if modes == 12 else 2)
     assert P.shape == P_o.shape
-    np.testing.assert_allclose((P.T @ P).toarray(), np.eye(P.shape[1]), atol=1e-12)
-    assert same_span(P, P_o) < 1e-12
+    np.testing.assert_allclose((P.T @ P).toarray(), np.eye(P.shape[1]), atol=1e-10)
+    assert same_span(P, P_o) < 1e-10
 
 
-def test_degenerate_aggregates_drop_affine_modes():
+@pytest.mark.parametrize("modes,full,line", [(12, 12, 6), (30, 30, 9)])
+def test_degenerate_aggregates_drop_polynomial_modes(modes, full, line):
     rng = np.random.default_rng(4)
     X = np.vstack([
-        rng.uniform(0.0, 1.0, size=(20, 3)),              # a full aggregate: 12 modes
+        rng.uniform(0.0, 1.0, size=(40, 3)),              # a full aggregate: every mode
         [[2.5, 0.5, 0.5]],                                 # one point: translations only
-        [[4.2, 0.5, 0.5], [4.5, 0.5, 0.5], [4.8, 0.5, 0.5]],  # collinear: one direction, 3 + 3 modes
+        [[4.2, 0.5, 0.5], [4.5, 0.5, 0.5], [4.8, 0.5, 0.5]],  # collinear: 1, x (and x^2) per component
     ])
-    aid, d, R = coarse_factors(X, 1.0, modes=12)
+    aid, d, R = coarse_factors(X, 1.0, modes=modes)
     kept = (np.abs(R).sum(axis=1) > 0).sum(axis=1)
-    np.testing.assert_array_equal(kept[aid[[0, 20, 21]]], [12, 3, 6])
+    np.testing.assert_array_equal(kept[aid[[0, 40, 41]]], [full, 3, line])
     P = co.basis_from_factors(aid, d, R)
-    np.testing.assert_allclose((P.T @ P).toarray(), np.eye(P.shape[1]), atol=1e-12)
-    assert same_span(P, co.affine_basis(X, co.aggregate_cells(X, 1.0))) < 1e-12
+    np.testing.assert_allclose((P.T @ P).toarray(), np.eye(P.shape[1]), atol=1e-10)
+    assert same_span(P, co.poly_basis(X, co.aggregate_cells(X, 1.0), 1 if modes == 12 else 2)) < 1e-10
 
 
 def test_degenerate_aggregates_drop_rotations():

@@ -51,21 +51,23 @@ def test_coarse_correction_matches_oracle():
         assert err <= 1e-3
 
 
-def test_affine_coarse_correction_matches_oracle():
-    """The twelve affine modes per aggregate (sfem_set_coarse_space_modes(..., 12)) against the oracle's
-    affine basis (a QR of each aggregate's block: the same span, so the same correction)."""
+@pytest.mark.parametrize("modes", [12, 30])
+def test_polynomial_coarse_correction_matches_oracle(modes):
+    """The affine (12) and quadratic (30) modes per aggregate (sfem_set_coarse_space_modes) against the
+    oracle's polynomial basis (orthonormalised per aggregate its own way: the same span, so the same
+    correction)."""
     from solidfem_gb300 import FemPhysicsMatrixFree
 
     m, fixed, f, h = slab(16, 8, 8)
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
                              material=3, precision="fp32")
     cell = 4 * h
-    p.set_coarse_space(cell, modes=12)
+    p.set_coarse_space(cell, modes=modes)
     info = p.coarse_info()
     o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.49, 1070.0, (0, 0, 0), 3)
     X = o.free_positions().reshape(-1, 3)
     aid = co.aggregate_cells(X, cell)
-    P = co.affine_basis(X, aid)
+    P = co.poly_basis(X, aid, 1 if modes == 12 else 2)
     assert info["coarse_dofs"] == P.shape[1], (info, P.shape)
     K = co.probe_tangent(o)
     Kc = co.coarse_matrix(K, P)
@@ -75,7 +77,7 @@ def test_affine_coarse_correction_matches_oracle():
         z_ref = P @ np.linalg.solve(Kc, P.T @ r)
         z = p.coarse_apply(r.reshape(-1, 3)).ravel()
         err = np.linalg.norm(z - z_ref) / np.linalg.norm(z_ref)
-        print(f"affine coarse correction vs oracle ({P.shape[1]} coarse DOFs): {err:.2e}")
+        print(f"{modes}-mode coarse correction vs oracle ({P.shape[1]} coarse DOFs): {err:.2e}")
         assert err <= 1e-3  # W in FP16, as above
 
 
@@ -85,7 +87,7 @@ def test_two_level_learned_solve_fewer_iterations_same_equilibrium():
 
     m, fixed, f, h = slab(64, 16, 16)
     res = {}
-    for cell, modes in ((0.0, 6), (8 * h, 6), (8 * h, 12)):
+    for cell, modes in ((0.0, 6), (8 * h, 6), (8 * h, 12), (8 * h, 30)):
         p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
                                  material=3, precision="fp32")
         p.set_operator("assembled")
@@ -96,7 +98,7 @@ def test_two_level_learned_solve_fewer_iterations_same_equilibrium():
         assert st["status"] == 0 and st["rel_res"] <= 1e-8, (cell, st)
         res[(cell, modes)] = (p.get_positions(), st)
         p.close()
-    (x1, s1), (x2, s2), (x3, s3) = res[(0.0, 6)], res[(8 * h, 6)], res[(8 * h, 12)]
+    (x1, s1), (x2, s2), (x3, s3), (x4, s4) = res[(0.0, 6)], res[(8 * h, 6)], res[(8 * h, 12)], res[(8 * h, 30)]
     o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.49, 1070.0, (0, 0, 0), 3)
     o.set_nodal_loads(f)
     r0 = np.linalg.norm(o.gradients())
@@ -107,13 +109,18 @@ def test_two_level_learned_solve_fewer_iterations_same_equilibrium():
     sh[o.reshuffle_map()] = x3
     o.set_positions_shuffled(sh)
     r3 = np.linalg.norm(o.gradients()) / r0
+    sh[o.reshuffle_map()] = x4
+    o.set_positions_shuffled(sh)
+    r4 = np.linalg.norm(o.gradients()) / r0
     err = np.linalg.norm(x2 - x1) / np.linalg.norm(x1 - m.nodes)
     err3 = np.linalg.norm(x3 - x1) / np.linalg.norm(x1 - m.nodes)
     print(f"learned: {s1['cg_iters']} CG its in {s1['newton_iters']} Newton, {s1['seconds']:.3f} s; with the coarse "
           f"space (cells of 8h): {s2['cg_iters']} CG its in {s2['newton_iters']} Newton, {s2['seconds']:.3f} s; "
-          f"affine modes: {s3['cg_iters']} CG its, {s3['seconds']:.3f} s; oracle |r|/|r0| {r2:.2e} / {r3:.2e}, "
-          f"solutions differ by {err:.1e} / {err3:.1e}")
-    assert r2 <= 1.5e-8 and r3 <= 1.5e-8
-    assert err <= 1e-6 and err3 <= 1e-6
+          f"affine modes: {s3['cg_iters']} CG its, {s3['seconds']:.3f} s; quadratic modes: {s4['cg_iters']} CG its, "
+          f"{s4['seconds']:.3f} s; oracle |r|/|r0| {r2:.2e} / {r3:.2e} / {r4:.2e}, solutions differ by {err:.1e} / "
+          f"{err3:.1e}")
+    err4 = np.linalg.norm(x4 - x1) / np.linalg.norm(x1 - m.nodes)
+    assert r2 <= 1.5e-8 and r3 <= 1.5e-8 and r4 <= 1.5e-8
+    assert err <= 1e-6 and err3 <= 1e-6 and err4 <= 1e-6
     assert s2["cg_iters"] < 0.8 * s1["cg_iters"]
-    assert s3["cg_iters"] < s2["cg_iters"]
+    assert s4["cg_iters"] < s3["cg_iters"] < s2["cg_iters"]
