@@ -40,11 +40,12 @@ def slab_mesh(nx, ny, nz, jitter=0.2, seed=0):
 
 
 def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1e-3, init_seed=0, verbose=True,
-          loss="energy", batch=16, init=None, first_seed=0, coarse_cells=0):
+          loss="energy", batch=16, init=None, first_seed=0, coarse_cells=0, coarse_modes=6):
     """Collect pairs from load seeds first_seed .. first_seed + seeds - 1 and train; init: weights
     to start from (a previous run's output) instead of the seeded random initialisation;
     coarse_cells > 0: train the network as the one-level part of the two-level preconditioner
-    (coarse space of cells of that many hexes), i.e. on the corrections minus the coarse correction."""
+    (coarse space of cells of that many hexes, coarse_modes modes per aggregate: 6 rigid, 12 affine, 30
+    quadratic), i.e. on the corrections minus the coarse correction."""
     m = slab_mesh(*dims)
     fixed = m.face_nodes(2, 0)
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
@@ -53,7 +54,7 @@ def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1
     if init:
         net.load(init)
     if coarse_cells > 0:
-        p.set_coarse_space(coarse_cells / 64.0)
+        p.set_coarse_space(coarse_cells / 64.0, modes=coarse_modes)
     net.set_loss(loss)
     net.set_batch(batch)
     t0 = time.time()
@@ -66,7 +67,7 @@ def train(dims=(64, 16, 16), seeds=128, every=25, max_snaps=40, steps=6000, lr=1
     t_train = time.time() - t0
     info = {"dims": list(dims), "load_seeds": [first_seed, first_seed + seeds - 1], "pairs": net.dataset_size(),
             "every": every, "max_snaps": max_snaps, "loss": loss, "batch": batch, "init": init, "init_seed": init_seed,
-            "steps": steps, "lr": lr, "coarse_cells": coarse_cells, "loss_first50": float(np.mean(losses[:50])),
+            "steps": steps, "lr": lr, "coarse_cells": coarse_cells, "coarse_modes": coarse_modes, "loss_first50": float(np.mean(losses[:50])),
             "loss_last50": float(np.mean(losses[-50:])), "collect_s": t_collect, "train_s": t_train,
             "material": "neo-Hookean E=1e5 nu=0.49, h=1/64, jitter 0.2h, bottom clamped, random top traction"}
     if verbose:
@@ -90,10 +91,12 @@ def main():
     ap.add_argument("--init-seed", type=int, default=0, help="seed of the initialisation and of the minibatches")
     ap.add_argument("--coarse-cells", type=int, default=0,
                     help="train for the two-level preconditioner with coarse cells of this many hexes (0: one-level)")
+    ap.add_argument("--coarse-modes", type=int, default=6, choices=[6, 12, 30], help="modes per coarse aggregate")
     a = ap.parse_args()
     dims = tuple(int(v) for v in a.dims.split(","))
     net, info, losses = train(dims, a.seeds, a.every, a.max_snaps, a.steps, a.lr, init_seed=a.init_seed, loss=a.loss,
-                              batch=a.batch, init=a.init, first_seed=a.first_seed, coarse_cells=a.coarse_cells)
+                              batch=a.batch, init=a.init, first_seed=a.first_seed, coarse_cells=a.coarse_cells,
+                              coarse_modes=a.coarse_modes)
     net.save(a.out, meta=info)
     np.save(a.out.rsplit(".", 1)[0] + "_losses.npy", losses)
 
