@@ -415,9 +415,23 @@ int residual(sfem_handle* h, double* rnorm, int* n_inverted, double* energy = nu
   return 0;
 }
 
-// Jacobi diagonal (inverse) of the tangent at the current state, precision T
+// Jacobi diagonal (inverse) of the tangent at the current state, precision T.  With the assembled
+// operator in use (and only the inverse asked for), from its diagonal blocks: the same sums, formed
+// once by the assembly, instead of an element pass.
 template <typename T>
 int jacobi(sfem_handle* h, T* dinv, T* diag) {
+  if (h->sell_on && dinv && !diag) {
+    const T* vals;
+    if constexpr (std::is_same<T, float>::value)
+      vals = h->sell_vals32;
+    else
+      vals = h->sell_vals64;
+    if (vals) {
+      launch_sell_diag_inv<T>(h->nbc, h->nf, h->sell_dslot, vals, dinv, h->stream);
+      CU(cudaGetLastError());
+      return 0;
+    }
+  }
   const T* u = disp<T>(h);
   T* fe = reinterpret_cast<T*>(h->fe);
   element_pass<T>(h, MODE_DIAG, u, nullptr, fe, nullptr, nullptr, nullptr);
@@ -2751,12 +2765,14 @@ void trace_trial(sfem_handle* h, int iter, double step, double rnorm) {
   (*h->ls_trace_count)++;
 }
 
+// e_init (optional): the total energy at the starting state, computed with its residual
 int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, double* rn_io, int* nit, int* cgit,
-                 int* cuts, int max_newton) {
+                 int* cuts, int max_newton, const double* e_init = nullptr) {
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
   double rn = *rn_io, rprev = rn, eta = op.eta_max;
-  bool have_e = false;  // e_acc holds the total energy at the current state
-  double e_acc = 0.0;
+  const bool inst0 = h->n_inst > 0;
+  bool have_e = e_init != nullptr && op.ls_condition == SFEM_LSC_ARMIJO && !inst0;  // e_acc: the energy here
+  double e_acc = have_e ? *e_init : 0.0;
   const int max_bis = op.max_bisection > 0 ? op.max_bisection : 30;
   const bool inst = h->n_inst > 0;
   if (inst) h->inst_rel.assign(h->n_inst, 1.0);
@@ -2932,8 +2948,11 @@ int sfem_newton_solve(sfem_handle* h, const sfem_newton_opts* opts, sfem_newton_
   int nit = 0, cgit = 0, cuts = 0, st = SFEM_OK;
   double r0 = 0, rn = 0;
   const int steps = op.load_steps > 1 ? op.load_steps : 1;
-  // |r(x_0)| of the full load defines the relative tolerance
-  TRY(residual(h, &r0, nullptr));
+  // |r(x_0)| of the full load defines the relative tolerance; for a one-step Armijo solve the same
+  // element pass also gives the starting energy the first line search compares against
+  const bool e_first = steps == 1 && op.ls_condition == SFEM_LSC_ARMIJO && h->n_inst == 0;
+  double e0[2] = {0.0, 0.0};
+  TRY(residual(h, &r0, nullptr, e_first ? e0 : nullptr));
   for (int s = 1; s <= steps; s++) {
     h->ff = ff_final * (double)s / steps;
     double r_ref = r0;
@@ -2949,7 +2968,7 @@ int sfem_newton_solve(sfem_handle* h, const sfem_newton_opts* opts, sfem_newton_
     } else {
       rn = r0;
     }
-    st = newton_stage(h, so, r_ref, &rn, &nit, &cgit, &cuts, op.max_newton - nit);
+    st = newton_stage(h, so, r_ref, &rn, &nit, &cgit, &cuts, op.max_newton - nit, e_first ? &e0[1] : nullptr);
     if (st < 0 || st == SFEM_LINESEARCH_FAILED) break;
   }
   h->ff = ff_final;

@@ -244,6 +244,9 @@ template <typename T>
 void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* code, const T* Ke, int nb,
                           int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass, double inv_h2, T* vals,
                           cudaStream_t st);
+// dinv = 1 / diag over the free rows from the assembled operator's diagonal blocks
+template <typename T>
+void launch_sell_diag_inv(int64_t nbc, int64_t nf, const int32_t* dslot, const T* vals, T* dinv, cudaStream_t st);
 // the FP32 neo-Hookean tangent the same way through 24 factors per element (Kf: 24 E floats)
 // instead of its blocks: h_a = F^-T g_a, vol mu (g_a . g_b), vol (mu - lambda log J), vol lambda
 constexpr int kNhFactorsHost = 24;

@@ -1255,6 +1255,28 @@ void launch_assemble_sell_nh32(const ElemView<float>& ev, const float* u, float*
   }
 }
 
+// the Jacobi diagonal's inverse from the assembled operator: each free row's diagonal block (slot
+// dslot[r]) holds the row's three diagonal entries (with the mass term of implicit dynamics)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_sell_diag_inv(int64_t nbc, int64_t nf, const int32_t* __restrict__ dslot,
+                                                            const T* __restrict__ vals, T* __restrict__ dinv) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nf; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = dslot[r];
+    const T* V = vals + 9 * (t & ~(int64_t)31) + (t & 31);
+    const int64_t o = 3 * (nbc + r);
+    dinv[o] = T(1) / V[0];
+    dinv[o + 1] = T(1) / V[32 * 4];
+    dinv[o + 2] = T(1) / V[32 * 8];
+  }
+}
+template <typename T>
+void launch_sell_diag_inv(int64_t nbc, int64_t nf, const int32_t* dslot, const T* vals, T* dinv, cudaStream_t st) {
+  count_launch();
+  k_sell_diag_inv<T><<<grid_for(nf), kThreads, 0, st>>>(nbc, nf, dslot, vals, dinv);
+}
+template void launch_sell_diag_inv<float>(int64_t, int64_t, const int32_t*, const float*, float*, cudaStream_t);
+template void launch_sell_diag_inv<double>(int64_t, int64_t, const int32_t*, const double*, double*, cudaStream_t);
+
 template <typename T>
 void launch_assemble_sell(int64_t nslots, const int64_t* cptr, const uint32_t* code, const T* Ke, int nb,
                           int64_t nbc, int64_t nf, const int32_t* dslot, const double* mass, double inv_h2, T* vals,
