@@ -1532,14 +1532,15 @@ int sfem_set_operator(sfem_handle* h, int32_t op) {
 
 extern "C++" {
 // In-place Cholesky A = L L^T of a dense symmetric positive definite n x n matrix (row-major; L in
-// the lower triangle), right-looking in blocks of 64: the diagonal block, then the panel below it,
-// then the trailing update, the last two over the host's threads.  The trailing update takes four
-// columns at a time with two partial sums each (eight independent chains of multiply-adds).  False
-// if a pivot is not positive.
+// the lower triangle), right-looking in blocks of 64: the diagonal block, then the panel below it
+// (rows in parallel), then the trailing update A22 -= P P^T as 4 x 8 register tiles over the panel
+// packed transposed (tiles in parallel, the order of every sum fixed).  False if a pivot is not
+// positive.
 static bool cholesky_lower(std::vector<double>& A, int n) {
   const int bs = 64;
+  std::vector<double> Pt;
   for (int k0 = 0; k0 < n; k0 += bs) {
-    const int k1 = std::min(n, k0 + bs);
+    const int k1 = std::min(n, k0 + bs), w = k1 - k0;
     for (int k = k0; k < k1; k++) {
       double d = A[(size_t)k * n + k];
       for (int p = k0; p < k; p++) d -= A[(size_t)k * n + p] * A[(size_t)k * n + p];
@@ -1552,7 +1553,9 @@ static bool cholesky_lower(std::vector<double>& A, int n) {
         A[(size_t)i * n + k] = t / d;
       }
     }
-    parallel_rows(n - k1, [&](int64_t a, int64_t b) {
+    const int m = n - k1;
+    if (m <= 0) break;
+    parallel_rows(m, [&](int64_t a, int64_t b) {
       for (int64_t i = k1 + a; i < k1 + b; i++) {
         double* Ai = &A[(size_t)i * n];
         for (int k = k0; k < k1; k++) {
@@ -1563,31 +1566,40 @@ static bool cholesky_lower(std::vector<double>& A, int n) {
         }
       }
     }, 64);
-    // row i takes i - k1 + 1 dot products: rows handed out dynamically
-    parallel_dynamic(n - k1, 8, [&](int64_t a, int64_t b) {
-      for (int64_t i = k1 + a; i < k1 + b; i++) {
-        double* Ai = &A[(size_t)i * n];
-        int64_t j = k1;
-        for (; j + 3 <= i; j += 4) {
-          const double *A0 = &A[(size_t)j * n], *A1 = A0 + n, *A2 = A1 + n, *A3 = A2 + n;
-          double s0 = 0, s1 = 0, s2 = 0, s3 = 0, t0 = 0, t1 = 0, t2 = 0, t3 = 0;
-          int p = k0;
-          for (; p + 1 < k1; p += 2) {
-            const double x = Ai[p], y = Ai[p + 1];
-            s0 += x * A0[p]; s1 += x * A1[p]; s2 += x * A2[p]; s3 += x * A3[p];
-            t0 += y * A0[p + 1]; t1 += y * A1[p + 1]; t2 += y * A2[p + 1]; t3 += y * A3[p + 1];
+    // P^T: Pt[p][r] = A[k1 + r][k0 + p], rows padded with zeros past every tile read (8 beyond m, to a
+    // multiple of 8)
+    const int mp = (m + 7) / 8 * 8 + 8;
+    Pt.assign((size_t)w * mp, 0.0);
+    parallel_rows(m, [&](int64_t a, int64_t b) {
+      for (int64_t r = a; r < b; r++)
+        for (int p = 0; p < w; p++) Pt[(size_t)p * mp + r] = A[(size_t)(k1 + r) * n + k0 + p];
+    }, 256);
+    // the lower trailing block in tiles of 4 rows x 8 columns (j <= i), row tiles handed out dynamically
+    const int nti = (m + 3) / 4;
+    parallel_dynamic(nti, 4, [&](int64_t t0, int64_t t1) {
+      for (int64_t ti = t0; ti < t1; ti++) {
+        const int i0 = (int)(4 * ti);
+        const int jmax = std::min(m, i0 + 4);  // columns 0 .. jmax - 1 reach the tile's rows
+        for (int j0 = 0; j0 < jmax; j0 += 8) {
+          double acc[4][8];
+          for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 8; c++) acc[r][c] = 0.0;
+          for (int p = 0; p < w; p++) {
+            const double* pr = &Pt[(size_t)p * mp];
+            const double a0 = pr[i0], a1 = pr[i0 + 1], a2 = pr[i0 + 2], a3 = pr[i0 + 3];
+            const double* pb = pr + j0;
+            for (int c = 0; c < 8; c++) {
+              const double bv = pb[c];
+              acc[0][c] += a0 * bv;
+              acc[1][c] += a1 * bv;
+              acc[2][c] += a2 * bv;
+              acc[3][c] += a3 * bv;
+            }
           }
-          if (p < k1) {
-            const double x = Ai[p];
-            s0 += x * A0[p]; s1 += x * A1[p]; s2 += x * A2[p]; s3 += x * A3[p];
+          for (int r = 0; r < 4 && i0 + r < m; r++) {
+            double* Ai = &A[(size_t)(k1 + i0 + r) * n + k1];
+            for (int c = 0; c < 8 && j0 + c <= i0 + r; c++) Ai[j0 + c] -= acc[r][c];
           }
-          Ai[j] -= s0 + t0; Ai[j + 1] -= s1 + t1; Ai[j + 2] -= s2 + t2; Ai[j + 3] -= s3 + t3;
-        }
-        for (; j <= i; j++) {
-          const double* Aj = &A[(size_t)j * n];
-          double t = 0.0;
-          for (int p = k0; p < k1; p++) t += Ai[p] * Aj[p];
-          Ai[j] -= t;
         }
       }
     });
@@ -1596,12 +1608,14 @@ static bool cholesky_lower(std::vector<double>& A, int n) {
 }
 
 // The inverse of A = L L^T (L from cholesky_lower, lower triangle of a row-major n x n array) into
-// Ainv (n x n, full, exactly symmetric).  Columns are solved 16 at a time, stored interleaved so
-// that each substitution step is 16 independent multiply-adds: L y = e_c from row c0 down, then
-// L^T x = y from row n - 1 up to row c0 (the rows of x at and below the group's first column are
-// the lower triangle's entries; the rest come from the symmetry).  Groups run on the host's threads.
+// Ainv (n x n, full, exactly symmetric).  Columns in groups of 8, each group on one host thread: the
+// forward substitution L y = e_c from the group's first row down, then the backward substitution
+// L^T x = y from row n - 1 up to the group's first row (the rows of x at and below it are the lower
+// triangle's entries; the rest come from the symmetry).  Both run over rows in tiles of 4: the terms
+// of rows already solved as 4 x 8 register tiles (four rows share every load of y or x), then the
+// tile's own 4 x 4 triangle in order.  Every sum has a fixed order.
 static void cholesky_inverse(const std::vector<double>& L, int n, std::vector<double>& Ainv) {
-  constexpr int G = 16;
+  constexpr int G = 8;
   std::vector<double> U((size_t)n * n);  // L^T row-major: column i of L contiguous
   parallel_rows(n, [&](int64_t a, int64_t b) {
     for (int64_t j = a; j < b; j++)
@@ -1614,32 +1628,68 @@ static void cholesky_inverse(const std::vector<double>& L, int n, std::vector<do
     for (int64_t g = g0; g < g1; g++) {
       const int c0 = (int)(g * G), w = std::min(G, n - c0);
       std::fill(Y.begin() + (size_t)c0 * G, Y.end(), 0.0);
-      for (int i = c0; i < n; i++) {  // L y = e_c
-        double t[G];
-        for (int k = 0; k < G; k++) t[k] = (i == c0 + k) ? 1.0 : 0.0;
-        const double* Li = &L[(size_t)i * n];
-        for (int p = c0; p < i; p++) {
-          const double l = Li[p];
-          const double* Yp = &Y[(size_t)p * G];
-          for (int k = 0; k < G; k++) t[k] -= l * Yp[k];
+      // L y = e_c, rows c0 .. n - 1 in tiles of 4 going down
+      for (int i0 = c0; i0 < n; i0 += 4) {
+        const int ni = std::min(4, n - i0);
+        double acc[4][G];
+        for (int r = 0; r < 4; r++)
+          for (int k = 0; k < G; k++) acc[r][k] = (i0 + r == c0 + k) ? 1.0 : 0.0;
+        const double* R0 = &L[(size_t)i0 * n];
+        const double* R1 = ni > 1 ? R0 + n : R0;
+        const double* R2 = ni > 2 ? R0 + 2 * (size_t)n : R0;
+        const double* R3 = ni > 3 ? R0 + 3 * (size_t)n : R0;
+        for (int p = c0; p < i0; p++) {
+          const double l0 = R0[p], l1 = R1[p], l2 = R2[p], l3 = R3[p];
+          const double* yp = &Y[(size_t)p * G];
+          for (int k = 0; k < G; k++) {
+            const double yv = yp[k];
+            acc[0][k] -= l0 * yv;
+            acc[1][k] -= l1 * yv;
+            acc[2][k] -= l2 * yv;
+            acc[3][k] -= l3 * yv;
+          }
         }
-        const double inv = 1.0 / Li[i];
-        double* Yi = &Y[(size_t)i * G];
-        for (int k = 0; k < G; k++) Yi[k] = t[k] * inv;
+        for (int r = 0; r < ni; r++) {
+          const double* Lr = &L[(size_t)(i0 + r) * n];
+          for (int q = 0; q < r; q++) {
+            const double l = Lr[i0 + q];
+            for (int k = 0; k < G; k++) acc[r][k] -= l * Y[(size_t)(i0 + q) * G + k];
+          }
+          const double inv = 1.0 / Lr[i0 + r];
+          for (int k = 0; k < G; k++) Y[(size_t)(i0 + r) * G + k] = acc[r][k] * inv;
+        }
       }
-      for (int i = n - 1; i >= c0; i--) {  // L^T x = y
-        double t[G];
-        const double* Yi = &Y[(size_t)i * G];
-        for (int k = 0; k < G; k++) t[k] = Yi[k];
-        const double* Ui = &U[(size_t)i * n];
-        for (int p = i + 1; p < n; p++) {
-          const double u = Ui[p];
-          const double* Yp = &Y[(size_t)p * G];
-          for (int k = 0; k < G; k++) t[k] -= u * Yp[k];
+      // L^T x = y, rows n - 1 .. c0 in tiles of 4 going up (x overwrites y)
+      for (int i1 = n - 1; i1 >= c0; i1 -= 4) {  // the tile's rows i1, i1 - 1, ... (at most 4, >= c0)
+        const int ni = std::min(4, i1 - c0 + 1);
+        double acc[4][G];
+        for (int r = 0; r < 4; r++)
+          for (int k = 0; k < G; k++) acc[r][k] = r < ni ? Y[(size_t)(i1 - r) * G + k] : 0.0;
+        const double* R0 = &U[(size_t)i1 * n];
+        const double* R1 = ni > 1 ? R0 - n : R0;
+        const double* R2 = ni > 2 ? R0 - 2 * (size_t)n : R0;
+        const double* R3 = ni > 3 ? R0 - 3 * (size_t)n : R0;
+        for (int p = i1 + 1; p < n; p++) {
+          const double u0 = R0[p], u1 = R1[p], u2 = R2[p], u3 = R3[p];
+          const double* xp = &Y[(size_t)p * G];
+          for (int k = 0; k < G; k++) {
+            const double xv = xp[k];
+            acc[0][k] -= u0 * xv;
+            acc[1][k] -= u1 * xv;
+            acc[2][k] -= u2 * xv;
+            acc[3][k] -= u3 * xv;
+          }
         }
-        const double inv = 1.0 / Ui[i];
-        double* Xi = &Y[(size_t)i * G];
-        for (int k = 0; k < G; k++) Xi[k] = t[k] * inv;
+        for (int r = 0; r < ni; r++) {  // row i1 - r needs the rows i1 - r + 1 .. i1 of this tile
+          const int i = i1 - r;
+          const double* Ur = &U[(size_t)i * n];
+          for (int q = 0; q < r; q++) {
+            const double u = Ur[i1 - q];
+            for (int k = 0; k < G; k++) acc[r][k] -= u * Y[(size_t)(i1 - q) * G + k];
+          }
+          const double inv = 1.0 / Ur[i];
+          for (int k = 0; k < G; k++) Y[(size_t)i * G + k] = acc[r][k] * inv;
+        }
       }
       for (int k = 0; k < w; k++) {
         const int c = c0 + k;
@@ -1750,7 +1800,7 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
   parallel_rows(na, [&](int64_t a0, int64_t a1) {
     std::vector<int> slot((size_t)na, -1);
     std::vector<int> touched;
-    std::vector<double> G;
+    std::vector<double> G, Tg((size_t)nm * nm);
     for (int64_t a = a0; a < a1; a++) {
       touched.clear();
       G.clear();
@@ -1766,14 +1816,33 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
             touched.push_back(b);
             G.resize(G.size() + nm2, 0.0);
           }
-          double Bj[3][30], KB[3][30];
-          Bmat(j, Bj);
           const double* Kij = &vals[9 * (size_t)e];
-          for (int r = 0; r < 3; r++)
-            for (int c = 0; c < nm; c++) KB[r][c] = Kij[3 * r] * Bj[0][c] + Kij[3 * r + 1] * Bj[1][c] + Kij[3 * r + 2] * Bj[2][c];
           double* g = &G[nm2 * (size_t)slot[b]];
-          for (int x = 0; x < nm; x++)
-            for (int c = 0; c < nm; c++) g[nm * x + c] += Bi[0][x] * KB[0][c] + Bi[1][x] * KB[1][c] + Bi[2][x] * KB[2][c];
+          if (nm == 6) {
+            double Bj[3][30], KB[3][30];
+            Bmat(j, Bj);
+            for (int r = 0; r < 3; r++)
+              for (int c = 0; c < nm; c++)
+                KB[r][c] = Kij[3 * r] * Bj[0][c] + Kij[3 * r + 1] * Bj[1][c] + Kij[3 * r + 2] * Bj[2][c];
+            for (int x = 0; x < nm; x++)
+              for (int c = 0; c < nm; c++) g[nm * x + c] += Bi[0][x] * KB[0][c] + Bi[1][x] * KB[1][c] + Bi[2][x] * KB[2][c];
+          } else {
+            // polynomial modes: B_i = I (x) f(d_i), so (B_i^T K_ij B_j)[F r + m][F s + l] = f_m(d_i) K_ij[r][s] f_l(d_j)
+            const int F = nm / 3;
+            const double* dj = &d[3 * j];
+            const double fj[10] = {1.0, dj[0], dj[1], dj[2], dj[0] * dj[0], dj[1] * dj[1], dj[2] * dj[2],
+                                   dj[0] * dj[1], dj[1] * dj[2], dj[2] * dj[0]};
+            double KB[3][30];
+            for (int r = 0; r < 3; r++)
+              for (int s2 = 0; s2 < 3; s2++)
+                for (int l = 0; l < F; l++) KB[r][F * s2 + l] = Kij[3 * r + s2] * fj[l];
+            for (int r = 0; r < 3; r++)
+              for (int m = 0; m < F; m++) {
+                const double fm = Bi[r][F * r + m];
+                double* gr = g + (size_t)nm * (F * r + m);
+                for (int c = 0; c < nm; c++) gr[c] += fm * KB[r][c];
+              }
+          }
         }
       }
       for (size_t t = 0; t < touched.size(); t++) {
@@ -1781,12 +1850,19 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
         const double* g = &G[nm2 * t];
         const double* Ra = &R[nm2 * a];
         const double* Rb = &R[nm2 * (size_t)b];
-        for (size_t p = 0; p < kc[a].size(); p++)
-          for (size_t q = 0; q < kc[b].size(); q++) {
+        const int kpa = (int)kc[a].size(), kqb = (int)kc[b].size();
+        // Kc_ab = R_a^T g R_b in two products: T = g R_b (nm x kept of b), then R_a^T T
+        for (int x = 0; x < nm; x++)
+          for (int q = 0; q < kqb; q++) {
             double v = 0.0;
-            for (int x = 0; x < nm; x++)
-              for (int y = 0; y < nm; y++) v += Ra[nm * x + kc[a][p]] * g[nm * x + y] * Rb[nm * y + kc[b][q]];
-            Kc[(size_t)(first[a] + p) * nk + first[b] + q] = v;
+            for (int y = 0; y < nm; y++) v += g[nm * x + y] * Rb[nm * y + kc[b][q]];
+            Tg[(size_t)nm * x + q] = v;
+          }
+        for (int p2 = 0; p2 < kpa; p2++)
+          for (int q = 0; q < kqb; q++) {
+            double v = 0.0;
+            for (int x = 0; x < nm; x++) v += Ra[nm * x + kc[a][p2]] * Tg[(size_t)nm * x + q];
+            Kc[(size_t)(first[a] + p2) * nk + first[b] + q] = v;
           }
         slot[b] = -1;
       }
@@ -1800,24 +1876,34 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
   // W = R Kc^-1 R^T in the modes' basis (nm n_agg square, rows padded to a multiple of 8)
   const int nc = (int)(nm * na), ld = (nc + 7) / 8 * 8;
   std::vector<float> W((size_t)nc * ld, 0.f);
-  parallel_rows(na, [&](int64_t a0, int64_t a1) {
-    for (int64_t a = a0; a < a1; a++)
+  // per aggregate pair (a, b): T = Kinv_ab R_b^T (kept columns of a x nm), then W_ab = R_a T
+  parallel_dynamic(na, 1, [&](int64_t a0, int64_t a1) {
+    std::vector<double> T((size_t)nm * nm);
+    for (int64_t a = a0; a < a1; a++) {
+      const double* Ra = &R[nm2 * a];
+      const int kpa = (int)kc[a].size();
       for (int64_t b = 0; b < na; b++) {
-        const double* Ra = &R[nm2 * a];
         const double* Rb = &R[nm2 * b];
-        for (int x = 0; x < nm; x++)
+        const int kqb = (int)kc[b].size();
+        for (int p = 0; p < kpa; p++) {
+          const double* Ki = &Kinv[(size_t)(first[a] + p) * nk + first[b]];
           for (int y = 0; y < nm; y++) {
             double v = 0.0;
-            for (size_t p = 0; p < kc[a].size(); p++) {
-              const double rx = Ra[nm * x + kc[a][p]];
-              if (rx == 0.0) continue;
-              const double* Ki = &Kinv[(size_t)(first[a] + p) * nk + first[b]];
-              for (size_t q = 0; q < kc[b].size(); q++) v += rx * Ki[q] * Rb[nm * y + kc[b][q]];
-            }
-            W[(size_t)(nm * a + x) * ld + nm * b + y] = (float)v;
+            for (int q = 0; q < kqb; q++) v += Ki[q] * Rb[nm * y + kc[b][q]];
+            T[(size_t)nm * p + y] = v;
           }
+        }
+        for (int x = 0; x < nm; x++) {
+          float* Wr = &W[(size_t)(nm * a + x) * ld + nm * b];
+          for (int y = 0; y < nm; y++) {
+            double v = 0.0;
+            for (int p = 0; p < kpa; p++) v += Ra[nm * x + kc[a][p]] * T[(size_t)nm * p + y];
+            Wr[y] = (float)v;
+          }
+        }
       }
-  }, 1);
+    }
+  });
   // stored in FP16 (11-bit significand) times 2^k, k putting the largest magnitude in [2^13, 2^14): half
   // the bytes of the per-iteration product, relative rounding <= 2^-11 on every entry above 2^-14 / 2^k
   float wmax = 0.f;
