@@ -85,3 +85,16 @@ def test_invalid_arguments():
         coarse_factors(X, 0.0)
     with pytest.raises(nat.SfemError):
         coarse_factors(np.full((2, 3), np.nan), 1.0)
+    with pytest.raises(nat.SfemError):
+        coarse_factors(X, 0.0, modes=30)
+    with pytest.raises(ValueError):
+        coarse_factors(X, 1.0, modes=9)
+    # the C entry point checks the degree itself
+    import ctypes as C
+    lib = nat.load()
+    aid = np.empty(4, dtype=np.int32)
+    d = np.empty((4, 3))
+    na = C.c_int64()
+    st = lib.sfem_coarse_factors_poly(np.ascontiguousarray(X).ctypes.data_as(nat._dp), 4, 1.0, 1e-8, 3,
+                                      aid.ctypes.data_as(nat._ip), d.ctypes.data_as(nat._dp), None, C.byref(na))
+    assert st != 0

@@ -62,8 +62,14 @@ def test_polynomial_coarse_correction_matches_oracle(modes):
     p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, young=1e5, poisson=0.49, density=1070.0, gravity=(0, 0, 0),
                              material=3, precision="fp32")
     cell = 4 * h
+    from solidfem_gb300 import _native as nat
+
+    with pytest.raises(nat.SfemError):
+        p.set_coarse_space(cell, modes=7)
+    assert p.coarse_info()["aggregates"] == 0  # a failed set-up leaves none
     p.set_coarse_space(cell, modes=modes)
     info = p.coarse_info()
+    assert info["aggregates"] > 0 and min(info["tangent_s"], info["coarse_matrix_s"], info["factorisation_s"]) >= 0
     o = Oracle(m.nodes, m.tets, fixed, 1e5, 0.49, 1070.0, (0, 0, 0), 3)
     X = o.free_positions().reshape(-1, 3)
     aid = co.aggregate_cells(X, cell)
