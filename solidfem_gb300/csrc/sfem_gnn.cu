@@ -79,7 +79,7 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, Row16* x4, Row16* y1,
                        Row16* y2, Row16* w, float* xstat, float* out, const int* done, cudaStream_t st,
                        float* partials, unsigned* counter, const float* rprev, CgScalars* s, bool x_ready,
-                       CoarseAdd ca) {
+                       CoarseAdd ca, cudaEvent_t before_last) {
   static_assert(NL == 3, "the launch sequence below is written for three layers");
   // grid-stride passes sized to one resident wave (no partly filled last wave; the BETA pass
   // then finishes with one block partial per resident CTA, 4 values each)
@@ -103,6 +103,7 @@ void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const 
   count_launch();
   launch_pdl(k_poly_bwd, std::min(blocks, wave_bwd), 256, 0, st, g, (const Row16*)y1, (const Row16*)(w + g.n), y2,
              done);
+  if (before_last) cudaStreamWaitEvent(st, before_last, 0);
   count_launch();
   const int grid_last = std::min(blocks, wave_last);
   if (s)

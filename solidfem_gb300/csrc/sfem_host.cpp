@@ -137,6 +137,10 @@ struct sfem_handle {
   int cs_n_runs = 0, cs_n_blocks = 0, cs_blk_off = 0;
   int32_t *cs_run_start = nullptr, *cs_blk_run = nullptr, *cs_agg_run_ptr = nullptr, *cs_agg_run = nullptr;
   float* cs_runpart = nullptr;
+  // a second stream for the coarse chain's aggregate sums and product, which overlap the first five
+  // polynomial passes; events fork and join it
+  cudaStream_t cs_stream = nullptr;
+  cudaEvent_t cs_fork = nullptr, cs_join = nullptr;
   CoarseView cv() const {
     return CoarseView{cs_n_agg,   cs_nm,     cs_ld,     nf,          cs_aid,       cs_d,           cs_W,           cs_w_inv_scale,
                       cs_s,       cs_y,      cs_n_runs, cs_n_blocks, cs_blk_off,   cs_run_start,   cs_blk_run,     cs_agg_run_ptr,
@@ -951,6 +955,12 @@ int sfem_destroy(sfem_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   batch_release(h);
   coarse_release(h);
+  if (h->cs_stream) {
+    cudaStreamSynchronize(h->cs_stream);
+    cudaStreamDestroy(h->cs_stream);
+  }
+  if (h->cs_fork) cudaEventDestroy(h->cs_fork);
+  if (h->cs_join) cudaEventDestroy(h->cs_join);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
@@ -1963,6 +1973,9 @@ int sfem_set_coarse_space_modes(sfem_handle* h, double cell, double rtol, int32_
   if (nrun > 0) CU(cudaMemcpyAsync(h->cs_agg_run, arun.data(), arun.size() * 4, cudaMemcpyHostToDevice, h->stream));
   h->cs_n_runs = (int)nrun;
   h->cs_n_blocks = (int)nblk;
+  if (!h->cs_stream) CU(cudaStreamCreateWithFlags(&h->cs_stream, cudaStreamNonBlocking));
+  if (!h->cs_fork) CU(cudaEventCreateWithFlags(&h->cs_fork, cudaEventDisableTiming));
+  if (!h->cs_join) CU(cudaEventCreateWithFlags(&h->cs_join, cudaEventDisableTiming));
   h->cs_blk_off = blk_off;
   TRY(sync(h));
   h->cs_n_agg = (int)na;
@@ -3429,15 +3442,20 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   const CoarseView cvw = h->cv();
   auto precondition = [&](bool with_beta, bool runs_done) {
     if (h->cs_on && g->infer_mode == 0) {
-      // two-level: y = W B^T r (the update may have formed the restriction's run sums), then the
-      // polynomial's last pass adds B y to M(r) and forms beta, z.r
+      // two-level: y = W B^T r (the update may have formed the restriction's run sums) on the coarse
+      // chain's own stream, beside the polynomial's first five passes; the last pass waits for it,
+      // adds B y to M(r) and forms beta, z.r
+      cudaEventRecord(h->cs_fork, h->stream);  // errors surface at the loop's next check
+      cudaStreamWaitEvent(h->cs_stream, h->cs_fork, 0);
       if (runs_done)
-        launch_coarse_sum_gemv(cvw, h->stream);
+        launch_coarse_sum_gemv(cvw, h->cs_stream);
       else
-        launch_coarse_restrict_gemv(cvw, w.r + o, h->stream);
+        launch_coarse_restrict_gemv(cvw, w.r + o, h->cs_stream);
+      cudaEventRecord(h->cs_join, h->cs_stream);
       gnn::launch_apply_poly(g->graph(), w.r + o, dinv, g->pc, g->px, g->py1, g->py2, g->pw, g->xstat, g->z + o,
                              done, h->stream, g->bpart, h->counter, with_beta ? g->rprev + o : nullptr,
-                             with_beta ? h->scal : nullptr, with_beta, CoarseAdd{h->cs_aid, h->cs_d, h->cs_y, h->cs_nm});
+                             with_beta ? h->scal : nullptr, with_beta, CoarseAdd{h->cs_aid, h->cs_d, h->cs_y, h->cs_nm},
+                             h->cs_join);
       return;
     }
     if (h->cs_on) {

@@ -401,7 +401,8 @@ void launch_apply(const Graph& g, const float* r, const float* dinv, const float
 void launch_apply_poly(const Graph& g, const float* r, const float* dinv, const PolyCoef& pc, Row16* x4, Row16* y1,
                        Row16* y2, Row16* w, float* xstat, float* out, const int* done, cudaStream_t st,
                        float* partials, unsigned* counter, const float* rprev = nullptr, CgScalars* s = nullptr,
-                       bool x_ready = false, CoarseAdd ca = CoarseAdd{nullptr, nullptr, nullptr, 6});
+                       bool x_ready = false, CoarseAdd ca = CoarseAdd{nullptr, nullptr, nullptr, 6},
+                       cudaEvent_t before_last = nullptr);
 // x4 rows = sigma D^-1/2 r (r, dinv: 3n), sigma and sum d r^2 into xstat
 void launch_scale_sqrt4(int64_t n, const float* r, const float* dinv, float* xstat, float* partials, unsigned* counter,
                         Row16* x4, cudaStream_t st);
