@@ -480,9 +480,12 @@ def run_gpu_arm(args):
                 "workload": WORKLOAD if dims == DIMS else f"reduced {dims} variant of: " + WORKLOAD,
                 "method": ("inexact Newton (Eisenstat-Walker), " +
                            {"learned": "learned-preconditioner flexible PCG",
-                            "learned+coarse": "two-level (learned + rigid-body coarse space) flexible PCG",
+                            "learned+coarse": "two-level (learned + " +
+                                              {6: "rigid-body", 12: "affine", 30: "quadratic"}.get(
+                                                  args.coarse_modes, str(args.coarse_modes)) +
+                                              " coarse modes per aggregate) flexible PCG",
                             "jacobi": "Jacobi-PCG"}[method] +
-                           " inner solves in FP32, FP64 residual and convergence test"),
+                           " inner solves in FP32, FP64-accurate residual and convergence test"),
                 "coarse_cells": args.coarse_cells if method == "learned+coarse" else None,
                 "coarse_modes": args.coarse_modes if method == "learned+coarse" else None,
                 "weights": os.path.basename(weights) if method.startswith("learned") else None,
