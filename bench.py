@@ -298,6 +298,7 @@ def run_gpu_arm(args):
 
     p32 = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision="fp32", **kw)
     p32.set_operator(args.operator)
+    p32.set_residual_arithmetic(args.residual)
     method = "jacobi"
     coarse_setup_s = None
     coarse_info = None
@@ -492,6 +493,7 @@ def run_gpu_arm(args):
                 "coarse_setup_s": coarse_setup_s,
                 "coarse_setup": coarse_info,
                 "operator": args.operator,
+                "residual_arithmetic": args.residual,
                 "preconditioner": method, "l2": "inputs larger than L2 (element data 0.35 GB FP32)",
                 "converged": ok, "newton_iters": [s_["newton_iters"] for s_ in stats],
                 "cg_iters": [s_["cg_iters"] for s_ in stats],
@@ -706,6 +708,9 @@ def main():
                     help="two-level preconditioner with the learned one: coarse-space cells of this many hexes "
                          "per axis (0: the learned preconditioner alone)")
     ap.add_argument("--weights", default=None, help="trained weights (default solidfem_gb300/data/gnn_slab.bin)")
+    ap.add_argument("--residual", default="two-term", choices=["two-term", "fp64"],
+                    help="arithmetic of the FP32 solves' nonlinear residual: two-term FP32 (default, "
+                         "FP64-accurate) or FP64 instructions")
     ap.add_argument("--operator", default="assembled", choices=["matrix-free", "assembled"],
                     help="operator of the FP32 Krylov solves: the tangent assembled per Newton step "
                          "(default, faster) or the matrix-free patch product; the FP64 baseline stays "

@@ -278,6 +278,17 @@ int sfem_set_operator_memory_limit(sfem_handle* h, int64_t bytes);
 /* Device bytes the assembled operator holds, and 1 in *fallback after an assembly ran out of memory. */
 int sfem_operator_info(sfem_handle* h, int64_t* bytes, int32_t* fallback);
 
+/* ---- arithmetic of the nonlinear residual (ElasticEnergy::ComputeForces, Source/ElasticEnergy.cpp:170-186
+ * neo-Hookean stress; the energy of :80-86 for the line search) ----
+ * SFEM_RESIDUAL_TWO_TERM (default for SFEM_FP32 handles, neo-Hookean, no batched instances): the element
+ * forces and energy in two-term FP32 arithmetic (about 48 significant bits, evaluated on H = F - I so
+ * that no term of order one cancels), summed per node in the same arithmetic and converted to FP64 once;
+ * as accurate as the FP64 pass, on the FP32 pipes.  SFEM_RESIDUAL_FP64: FP64 instructions throughout
+ * (always so for SFEM_FP64 handles and the other materials).  Returns SFEM_ERR_INVALID for other modes. */
+#define SFEM_RESIDUAL_FP64 0
+#define SFEM_RESIDUAL_TWO_TERM 1
+int sfem_set_residual_arithmetic(sfem_handle* h, int32_t mode);
+
 /* ---- assembled tangent (ElasticEnergy::AssembleStiffnessMatrix, Source/ElasticEnergy.cpp:573-635;
  * FemPhysicsMatrixFree::ComputeSystemMatrix :700-722 adds M/h^2 for implicit dynamics) ----
  * Block CSR over the free nodes in the reshuffled free order (3 x 3 blocks, row-major), FP64,

@@ -33,6 +33,7 @@ FP64, FP32 = 0, 1
 PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
 SIM_EXPLICIT, SIM_IMPLICIT = 2, 3
 OP_MATRIX_FREE, OP_ASSEMBLED = 0, 1
+RESIDUAL_FP64, RESIDUAL_TWO_TERM = 0, 1
 LSC_ARMIJO, LSC_ENGINEERING, LSC_RESIDUAL = 0, 1, 2
 TANGENT_REFERENCE, TANGENT_EXACT = 0, 1
 
@@ -130,6 +131,7 @@ SIGNATURES = {
     "sfem_gnn_set_batch": [_vp, C.c_int32],
     "sfem_gnn_set_inference": [_vp, C.c_int32],
     "sfem_set_operator": [_vp, C.c_int32],
+    "sfem_set_residual_arithmetic": [_vp, C.c_int32],
     "sfem_set_operator_memory_limit": [_vp, C.c_int64],
     "sfem_set_batched_pcg": [_vp, C.c_int32],
     "sfem_set_coarse_space": [_vp, C.c_double, C.c_double],

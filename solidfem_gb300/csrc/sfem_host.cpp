@@ -105,6 +105,9 @@ struct sfem_handle {
   double *X64 = nullptr, *vol64 = nullptr, *scale64 = nullptr, *young_e = nullptr, *scale_la64 = nullptr;
   float *X32 = nullptr, *vol32 = nullptr, *scale32 = nullptr, *scale_la32 = nullptr;
   bool has_scale_la = false;
+  // two-term residual: the low parts of X (9 x E) and V (E) beside X32 / vol32, made on first use
+  float* df_lo = nullptr;
+  int32_t resid_arith = SFEM_RESIDUAL_TWO_TERM;
   // independent instances: free-DOF segments, per-instance activity and residual norms
   int n_inst = 0;
   int64_t* inst_seg = nullptr;   // device, n_inst + 1 (offsets into a free-DOF vector)
@@ -399,15 +402,32 @@ int sync(sfem_handle* h) {
 // FP64 residual r64 = f_int + m g ff + f_ext ff; returns |r| and the number of inverted elements.
 // With energy (elastic, total), the element pass also sums the elastic energy and a node pass
 // the potential of the loads (the values sfem_energy returns, from the same kernels' arithmetic).
+// the FP32 handle's neo-Hookean residual in two-term FP32 arithmetic (FP64-accurate; k_element_nh_df)
+bool residual_two_term(const sfem_handle* h) {
+  return h->resid_arith == SFEM_RESIDUAL_TWO_TERM && h->precision == SFEM_FP32 && mat_id(h) == 3 && h->n_inst == 0;
+}
 int residual(sfem_handle* h, double* rnorm, int* n_inverted, double* energy = nullptr) {
   CU(cudaMemsetAsync(h->ninv, 0, sizeof(int), h->stream));
-  element_pass<double>(h, energy ? MODE_FORCE_ENERGY : MODE_FORCE, h->u, nullptr, h->fe, energy ? h->dres + 3 : nullptr,
-                       h->ninv, nullptr);
+  const bool tt = residual_two_term(h);
+  if (tt) {
+    const int64_t E = h->E;
+    if (!h->df_lo) {
+      TRY(dalloc(&h->df_lo, 10 * (size_t)E));
+      launch_split_geom(9 * E, h->X64, h->X32, h->df_lo, h->stream);
+      launch_split_geom(E, h->vol64, h->vol32, h->df_lo + 9 * E, h->stream);
+    }
+    const DfGeom dg{h->X32, h->df_lo, h->vol32, h->df_lo + 9 * E};
+    launch_element_nh_df(energy != nullptr, h->ev64(), dg, h->u, reinterpret_cast<float2*>(h->fe), h->red(),
+                         energy ? h->dres + 3 : nullptr, h->ninv, h->stream);
+  } else {
+    element_pass<double>(h, energy ? MODE_FORCE_ENERGY : MODE_FORCE, h->u, nullptr, h->fe,
+                         energy ? h->dres + 3 : nullptr, h->ninv, nullptr);
+  }
   const PressureView pv = h->pres();
   if (h->n_tris > 0) launch_pressure_tris(pv, h->x0, h->u, h->ff, h->stream);
   const DynView dv = h->dyn();
   launch_gather_force(h->nbc, h->N, h->csr(), h->fe, h->mass, h->fext, h->grav, h->ff, h->r64, h->red(),
-                      h->dres, h->stream, h->n_tris > 0 ? &pv : nullptr, h->dt > 0 ? &dv : nullptr, h->u);
+                      h->dres, h->stream, h->n_tris > 0 ? &pv : nullptr, h->dt > 0 ? &dv : nullptr, h->u, tt);
   if (energy)
     launch_potential(h->nbc, h->N, h->x0, h->u, h->mass, h->fext, h->grav, h->ff, h->red(), h->dres + 4, h->stream,
                      h->dt > 0 ? &dv : nullptr);
@@ -988,7 +1008,7 @@ int sfem_destroy(sfem_handle* h) {
                   h->mass, h->fext, h->grav_d, h->csr_ptr, h->csr_ent, h->fe, h->partials, h->counter, h->scal,
                   h->dres, h->ninv, h->r64, h->ubase, h->tmp64, h->tmp64b, h->k64.b, h->k64.x, h->k64.r, h->k64.p,
                   h->k64.q, h->k64.dinv, h->k64.u, h->k32.b, h->k32.x, h->k32.r, h->k32.p, h->k32.q, h->k32.dinv,
-                  h->k32.u, h->k64.p2, h->k64.ones, h->k32.p2, h->k32.ones};
+                  h->k32.u, h->k64.p2, h->k64.ones, h->k32.p2, h->k32.ones, h->df_lo};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->scal_h) cudaFreeHost(h->scal_h);
@@ -2081,6 +2101,14 @@ int sfem_set_operator_memory_limit(sfem_handle* h, int64_t bytes) {
   if (bytes < 0) return fail(SFEM_ERR_INVALID, "the limit is a byte count (0: no limit)");
   h->sell_limit = bytes;
   h->sell_oom = false;
+  return SFEM_OK;
+}
+
+int sfem_set_residual_arithmetic(sfem_handle* h, int32_t mode) {
+  TRY(check_handle(h));
+  if (mode != SFEM_RESIDUAL_FP64 && mode != SFEM_RESIDUAL_TWO_TERM)
+    return fail(SFEM_ERR_INVALID, "residual arithmetic %d (0: FP64, 1: two-term FP32)", (int)mode);
+  h->resid_arith = mode;
   return SFEM_OK;
 }
 

@@ -184,7 +184,19 @@ void launch_pressure_tris(PressureView pv, const double* x0, const double* u, do
 void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
                          const double* fext, const double* grav, double ff, double* r, Reduce red,
                          double* rr_out, cudaStream_t st, const PressureView* pv = nullptr,
-                         const DynView* dv = nullptr, const double* u = nullptr);
+                         const DynView* dv = nullptr, const double* u = nullptr, bool fe_df = false);
+// The element geometry as two-term FP32 values: the FP32 copies of X and V and their low parts.
+struct DfGeom {
+  const float* Xhi;    // 9 x E
+  const float* Xlo;    // 9 x E, RN(X - Xhi)
+  const float* volhi;  // E
+  const float* vollo;  // E
+};
+// neo-Hookean element forces (+ energy sum) to FP64 accuracy in two-term FP32 arithmetic; fe holds
+// 12 (hi, lo) pairs per element
+void launch_element_nh_df(bool energy, const ElemView<double>& ev, const DfGeom& dg, const double* u, float2* fe,
+                          Reduce red, double* result, int* n_inverted, cudaStream_t st);
+void launch_split_geom(int64_t n, const double* x, const float* hi, float* lo, cudaStream_t st);
 template <typename T>
 void launch_gather_hvp(int64_t nbc, int64_t N, NodeCsr csr, const T* fe, const T* p, T* q, Reduce red,
                        CgScalars* s, cudaStream_t st);

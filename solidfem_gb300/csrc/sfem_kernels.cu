@@ -28,6 +28,7 @@
 #include "sfem_reduce.cuh"
 #include "sfem_row16.cuh"
 #include "sfem_coarse.cuh"
+#include "sfem_df32.cuh"
 
 namespace sfem {
 
@@ -844,6 +845,85 @@ void launch_element(int mode, const ElemView<T>& ev, const T* u, const T* p, T* 
       k_element<T, MAT, MODE_NODALVOL><<<grid, kThreads, 0, st>>>(ev, u, p, fe, red, result, n_inverted, s);
       break;
   }
+}
+
+// ---- the neo-Hookean residual's element pass in two-term FP32 arithmetic ----
+//
+// Forces -V P X^T (and the energy sum of V psi) of the neo-Hookean material to FP64 accuracy on the
+// FP32 pipes (df32::nh_element: ElasticEnergy.cpp:170-186 and :80-86 on H = F - I), from the FP64
+// displacement: the differences u_a - u_0 are taken in FP64 (nine subtractions per element) and
+// split exactly; X and V are the FP32 copies plus their low parts (DfGeom).  Each element writes its
+// 12 forces as (hi, lo) pairs, which k_gather_force<float2> sums per node in element order.
+template <bool ENERGY>
+__global__ void __launch_bounds__(kThreads) k_element_nh_df(ElemView<double> ev, DfGeom dg,
+                                                            const double* __restrict__ u, float2* __restrict__ fe,
+                                                            Reduce red, double* result, int* n_inv) {
+  using df32::df;
+  using df32::DfSum;
+  DfSum eacc;
+  int ninv = 0;
+  const int64_t E = ev.E;
+  const df mu0 = df32::split_f64(ev.mu), la0 = df32::split_f64(ev.lambda);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int4 t = ev.tets[e];
+    double a0[3], a1[3], a2[3], a3[3];
+    load3(u, t.x, a0);
+    load3(u, t.y, a1);
+    load3(u, t.z, a2);
+    load3(u, t.w, a3);
+    df D[9], X[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      D[3 * i] = df32::split_f64(a1[i] - a0[i]);
+      D[3 * i + 1] = df32::split_f64(a2[i] - a0[i]);
+      D[3 * i + 2] = df32::split_f64(a3[i] - a0[i]);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) X[k] = df{dg.Xhi[k * E + e], dg.Xlo[k * E + e]};
+    const df vol = {dg.volhi[e], dg.vollo[e]};
+    df mu = mu0, la = la0;
+    if (ev.scale) {
+      const double sc = ev.scale[e];
+      mu = df32::split_f64(ev.mu * sc);
+      la = df32::split_f64(ev.lambda * (ev.scale_la ? ev.scale_la[e] : sc));
+    }
+    df f[12], psi = {0.0f, 0.0f};
+    if (df32::nh_element(D, X, vol, mu, la, ENERGY, f, &psi)) ninv++;
+    float4* o = reinterpret_cast<float4*>(fe + 12 * e);
+#pragma unroll
+    for (int k = 0; k < 6; k++) o[k] = make_float4(f[2 * k].hi, f[2 * k].lo, f[2 * k + 1].hi, f[2 * k + 1].lo);
+    if (ENERGY) eacc.add(psi);
+  }
+  if (ENERGY) {
+    double v[1] = {df32::to_f64(eacc.value())}, tot[1];
+    if (reduce_last<double, 1>(v, red, tot) && threadIdx.x == 0) *result = tot[0];
+  }
+  if (n_inv != nullptr) {
+    int v[1] = {ninv};
+    block_sum<int, 1>(v);
+    if (threadIdx.x == 0 && v[0] != 0) atomicAdd(n_inv, v[0]);
+  }
+}
+
+void launch_element_nh_df(bool energy, const ElemView<double>& ev, const DfGeom& dg, const double* u, float2* fe,
+                          Reduce red, double* result, int* n_inverted, cudaStream_t st) {
+  count_launch();
+  const int grid = grid_for(ev.E, 152 * 12);
+  if (energy)
+    k_element_nh_df<true><<<grid, kThreads, 0, st>>>(ev, dg, u, fe, red, result, n_inverted);
+  else
+    k_element_nh_df<false><<<grid, kThreads, 0, st>>>(ev, dg, u, fe, red, result, n_inverted);
+}
+
+// low parts of the element geometry: lo = RN(x - hi) for the FP32 copies hi = RN(x) of X and V
+__global__ void __launch_bounds__(kThreads) k_split_geom(int64_t n, const double* __restrict__ x,
+                                                         const float* __restrict__ hi, float* __restrict__ lo) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    lo[i] = (float)(x[i] - (double)hi[i]);
+}
+void launch_split_geom(int64_t n, const double* x, const float* hi, float* lo, cudaStream_t st) {
+  count_launch();
+  k_split_geom<<<grid_for(n), kThreads, 0, st>>>(n, x, hi, lo);
 }
 
 // Element stiffness (12 x 12, row-major, per element) from the tangent:
@@ -1717,8 +1797,27 @@ void launch_pressure_tris(PressureView pv, const double* x0, const double* u, do
   k_pressure_tris<<<grid_for(pv.n_tris), kThreads, 0, st>>>(pv, x0, u, ff);
 }
 
+// the nodal sums of two-term (hi, lo) element forces, in element order, converted to FP64 once
+__device__ __forceinline__ void gather_node(NodeCsr csr, const float2* __restrict__ fe, int64_t g, double* acc) {
+  df32::df a[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+  const int64_t b = csr.ptr[g], en = csr.ptr[g + 1];
+  for (int64_t k = b; k < en; k++) {
+    const int64_t x = csr.ent[k];
+    const float2* src = fe + 12 * (x >> 2) + 3 * (x & 3);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float2 v = src[c];
+      a[c] = df32::df_add(a[c], df32::df{v.x, v.y});
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) acc[c] = df32::to_f64(a[c]);
+}
+
+// FE = double: FP64 element forces; FE = float2: two-term ones (k_element_nh_df)
+template <typename FE>
 __global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t N, NodeCsr csr,
-                                                           const double* __restrict__ fe,
+                                                           const FE* __restrict__ fe,
                                                            const double* __restrict__ mass,
                                                            const double* __restrict__ fext, double g0, double g1,
                                                            double g2, double ff, double* __restrict__ r,
@@ -1756,12 +1855,18 @@ __global__ void __launch_bounds__(kThreads) k_gather_force(int64_t nbc, int64_t 
 
 void launch_gather_force(int64_t nbc, int64_t N, NodeCsr csr, const double* fe, const double* mass,
                          const double* fext, const double* grav, double ff, double* r, Reduce red, double* rr_out,
-                         cudaStream_t st, const PressureView* pv, const DynView* dv, const double* u) {
+                         cudaStream_t st, const PressureView* pv, const DynView* dv, const double* u, bool fe_df) {
   count_launch();
   PressureView none{0, nullptr, nullptr, nullptr, nullptr, 0.0};
   DynView nodyn{nullptr, nullptr, 0.0, 0.0};
-  k_gather_force<<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, mass, fext, grav[0], grav[1], grav[2], ff,
-                                                        r, red, rr_out, pv ? *pv : none, dv ? *dv : nodyn, u);
+  if (fe_df)
+    k_gather_force<float2><<<grid_for(N - nbc), kThreads, 0, st>>>(
+        nbc, N, csr, reinterpret_cast<const float2*>(fe), mass, fext, grav[0], grav[1], grav[2], ff, r, red, rr_out,
+        pv ? *pv : none, dv ? *dv : nodyn, u);
+  else
+    k_gather_force<double><<<grid_for(N - nbc), kThreads, 0, st>>>(nbc, N, csr, fe, mass, fext, grav[0], grav[1],
+                                                                  grav[2], ff, r, red, rr_out, pv ? *pv : none,
+                                                                  dv ? *dv : nodyn, u);
 }
 
 template <typename T>

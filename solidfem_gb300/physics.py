@@ -394,6 +394,13 @@ class FemPhysicsMatrixFree:
         nat.check(self._lib.sfem_set_operator(self._h, {"matrix-free": nat.OP_MATRIX_FREE,
                                                          "assembled": nat.OP_ASSEMBLED}[op]))
 
+    def set_residual_arithmetic(self, mode: str) -> None:
+        """Arithmetic of the nonlinear residual's element pass for FP32 neo-Hookean handles: 'two-term'
+        (default: two-term FP32, FP64-accurate, on the FP32 pipes) or 'fp64' (FP64 instructions).  FP64
+        handles and the other materials always use FP64."""
+        nat.check(self._lib.sfem_set_residual_arithmetic(self._h, {"fp64": nat.RESIDUAL_FP64,
+                                                                    "two-term": nat.RESIDUAL_TWO_TERM}[mode]))
+
     def set_operator_memory_limit(self, nbytes: int) -> None:
         """Cap on the device memory of the assembled operator (0: none); beyond it the Krylov solves
         keep the matrix-free product."""
