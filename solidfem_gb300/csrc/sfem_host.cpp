@@ -144,11 +144,6 @@ struct sfem_handle {
   // polynomial passes; events fork and join it
   cudaStream_t cs_stream = nullptr;
   cudaEvent_t cs_fork = nullptr, cs_join = nullptr;
-  // speculative assembly: the FP32 neo-Hookean operator at a line-search trial state, built on its own
-  // stream while the main stream evaluates the FP64 residual there; sell_spec marks it current
-  bool sell_spec = false;
-  cudaStream_t spec_stream = nullptr;
-  cudaEvent_t spec_fork = nullptr, spec_join = nullptr;
   CoarseView cv() const {
     return CoarseView{cs_n_agg,   cs_nm,     cs_ld,     nf,          cs_aid,       cs_d,           cs_W,           cs_w_inv_scale,
                       cs_s,       cs_y,      cs_n_runs, cs_n_blocks, cs_blk_off,   cs_run_start,   cs_blk_run,     cs_agg_run_ptr,
@@ -986,12 +981,6 @@ int sfem_destroy(sfem_handle* h) {
   }
   if (h->cs_fork) cudaEventDestroy(h->cs_fork);
   if (h->cs_join) cudaEventDestroy(h->cs_join);
-  if (h->spec_stream) {
-    cudaStreamSynchronize(h->spec_stream);
-    cudaStreamDestroy(h->spec_stream);
-  }
-  if (h->spec_fork) cudaEventDestroy(h->spec_fork);
-  if (h->spec_join) cudaEventDestroy(h->spec_join);
   void* ibufs[] = {h->scale_la64, h->scale_la32, h->inst_seg, h->inst_active, h->inst_norm, h->tri, h->tptr, h->tent,
                    h->ptf, h->vel, h->ustart, h->pm64, h->pm32, h->bsr_rowptr, h->bsr_col, h->bsr_slot,
                    h->bsr_dslot, h->bsr_vals, h->nhc64, h->nhc32, h->rec64, h->rec32, h->sell_base,
@@ -1523,11 +1512,6 @@ struct OperatorScope {
   sfem_handle* h;
   int st = 0;
   explicit OperatorScope(sfem_handle* hh) : h(hh) {
-    if (h->sell_spec) {  // assembled at this state beside the line search's residual (spec_begin)
-      h->sell_spec = false;
-      h->sell_on = true;
-      return;
-    }
     if (h->op_mode == 1 && h->n_inst == 0 && mat_id(h) <= 4 && !h->sell_oom) {
       st = h->precision == SFEM_FP32 ? sell_assemble<float>(h) : sell_assemble<double>(h);
       h->sell_on = st == 0;
@@ -1543,41 +1527,6 @@ struct OperatorScope {
     }
   }
   ~OperatorScope() { h->sell_on = false; }
-};
-
-// Speculative assembly of the FP32 neo-Hookean operator at the current state on the handle's second
-// stream (forked from the main stream, so after the state's update), for an inner solve that will
-// need it at this state: the main stream meanwhile evaluates the FP64 residual there (FP64-bound, so
-// the FP32 assembly fills the idle FP32 pipes).  Only once an earlier assembly has built the structure
-// and buffers.  spec_join makes the main stream wait for it before its next work; a state change
-// clears sell_spec (the next trial of a line search, the end of a Newton stage).
-static void spec_begin(sfem_handle* h) {
-  h->sell_spec = false;
-  if (h->precision != SFEM_FP32 || h->op_mode != 1 || h->n_inst > 0 || mat_id(h) != 3 || h->sell_oom) return;
-  if (h->sell_T < 0 || !h->sell_vals32 || !h->sell_ke32 || !h->k32.u) return;
-  if (!h->spec_stream) {
-    if (cudaStreamCreateWithFlags(&h->spec_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->spec_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->spec_join, cudaEventDisableTiming) != cudaSuccess) {
-      cudaGetLastError();
-      return;
-    }
-  }
-  cudaEventRecord(h->spec_fork, h->stream);
-  cudaStreamWaitEvent(h->spec_stream, h->spec_fork, 0);
-  launch_convert<double, float>(3 * h->N, h->u, h->k32.u, h->spec_stream);
-  launch_assemble_sell_nh32(ev_of<float>(h), h->k32.u, h->sell_ke32, h->sell_T, h->sell_cptr, h->sell_code, h->nbc,
-                            h->nf, h->sell_dslot, h->dt > 0 ? h->mass : nullptr,
-                            h->dt > 0 ? 1.0 / (h->dt * h->dt) : 0.0, h->sell_vals32, h->spec_stream);
-  cudaEventRecord(h->spec_join, h->spec_stream);
-  h->sell_spec = true;
-}
-static void spec_join(sfem_handle* h) {
-  if (h->spec_stream) cudaStreamWaitEvent(h->stream, h->spec_join, 0);
-}
-struct SpecClear {  // no speculative assembly outlives the Newton stage that made it
-  sfem_handle* h;
-  ~SpecClear() { h->sell_spec = false; }
 };
 
 // assemble the FP64 tangent at the current state into h->bsr_vals
@@ -2946,7 +2895,6 @@ void trace_trial(sfem_handle* h, int iter, double step, double rnorm) {
 // e_init (optional): the total energy at the starting state, computed with its residual
 int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, double* rn_io, int* nit, int* cgit,
                  int* cuts, int max_newton, const double* e_init = nullptr) {
-  SpecClear spec_clear{h};
   const size_t o = 3 * (size_t)h->nbc, n = 3 * (size_t)h->nf;
   double rn = *rn_io, rprev = rn, eta = op.eta_max;
   const bool inst0 = h->n_inst > 0;
@@ -3037,16 +2985,9 @@ int newton_stage(sfem_handle* h, const sfem_newton_opts& op, double r_ref, doubl
       int bis = 0;
       for (;;) {
         launch_axpy_state<double>((int64_t)n, a, h->tmp64 + o, h->ubase + o, h->u + o, h->stream);
-        // the full step is usually accepted: assemble the next inner solve's operator at it meanwhile
-        if (a == 1.0 && bis == 0)
-          spec_begin(h);
-        else
-          h->sell_spec = false;
         int ninv = 0;
         double en[2] = {0.0, 0.0};  // elastic and total energy, with the residual (Armijo)
-        const int rst = residual(h, &rnew, &ninv, op.ls_condition == SFEM_LSC_ARMIJO ? en : nullptr);
-        spec_join(h);
-        TRY(rst);
+        TRY(residual(h, &rnew, &ninv, op.ls_condition == SFEM_LSC_ARMIJO ? en : nullptr));
         trace_trial(h, *nit - 1, a, rnew);
         bool cond = false;
         if (ninv == 0 && std::isfinite(rnew)) {
@@ -3138,11 +3079,7 @@ int sfem_newton_solve(sfem_handle* h, const sfem_newton_opts* opts, sfem_newton_
   // element pass also gives the starting energy the first line search compares against
   const bool e_first = steps == 1 && op.ls_condition == SFEM_LSC_ARMIJO && h->n_inst == 0;
   double e0[2] = {0.0, 0.0};
-  SpecClear spec_clear{h};
-  if (steps == 1) spec_begin(h);  // the first inner solve assembles at this state
-  const int rst0 = residual(h, &r0, nullptr, e_first ? e0 : nullptr);
-  spec_join(h);
-  TRY(rst0);
+  TRY(residual(h, &r0, nullptr, e_first ? e0 : nullptr));
   for (int s = 1; s <= steps; s++) {
     h->ff = ff_final * (double)s / steps;
     double r_ref = r0;
@@ -3570,8 +3507,12 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
   precondition(false, false);
   gnn::launch_fcg_init(n, w.r + o, g->z + o, w.p + o, part, h->counter, h->scal, h->stream);  // p_old = 0
   float* pbuf[2] = {w.p, w.p2};
+  // iterations between the host's looks at the stop flag: 16, or fewer once the residual's decay
+  // over the last look predicts convergence sooner (the launches queued past convergence return at
+  // once, but each still costs a launch)
   const int check_every = 16;
-  int it = 0;
+  int chunk = check_every, it = 0, it_prev = -1;
+  double rr_prev = 0.0;
   bool pending = false;
   if (h->profiling) {
     h->prof_precision = SFEM_FP32;
@@ -3581,6 +3522,17 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
     CU(cudaMemcpyAsync(h->scal_h, h->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
     TRY(sync(h));
     if (h->scal_h->done || it >= max_it) break;
+    {
+      const double rr = h->scal_h->rr, goal = h->scal_h->tol2;
+      chunk = check_every;
+      if (it_prev >= 0 && rr > 0.0 && goal > 0.0 && rr_prev > rr && h->scal_h->it > it_prev) {
+        const double rate = std::log(rr_prev / rr) / (double)(h->scal_h->it - it_prev);
+        const double need = std::log(rr / goal) / rate;
+        if (need < check_every - 2) chunk = std::max(2, (int)std::ceil(need * 1.1) + 1);
+      }
+      it_prev = h->scal_h->it;
+      rr_prev = rr;
+    }
     if (pending) {
       float a = 0, bms = 0;
       cudaEventElapsedTime(&a, h->pev[0], h->pev[1]);
@@ -3590,7 +3542,7 @@ int fcg_device(sfem_handle* h, const float* b, float* x, double tol, int max_it,
       h->prof_samples++;
       pending = false;
     }
-    for (int k = 0; k < check_every && it < max_it; k++, it++) {
+    for (int k = 0; k < chunk && it < max_it; k++, it++) {
       const bool sample = h->profiling && k == 0;
       float* pold = pbuf[it % 2];
       float* pnew = pbuf[(it + 1) % 2];
