@@ -395,7 +395,8 @@ int sfem_kernel_launches(int64_t* count);
 int sfem_dot_noalloc_dev(const double* a_dev, const double* b_dev, int64_t n, double* out_dev, void* stream);
 
 /* ---- coarse space (extension; the reference's SolveConjugateGradientMF,
- * Math/IterativeSolvers.h:115-195, has none): host-side groundwork of a two-level preconditioner.
+ * Math/IterativeSolvers.h:115-195, has none): the host-side factors of the two-level preconditioner
+ * (sfem_set_coarse_space below), exposed for checking.
  * X: n points (3n doubles, e.g. free-node rest positions); aggregates are the cells of a uniform
  * grid of spacing `cell` anchored at the points' minimum corner, numbered in increasing cell order
  * (aid: n).  d: 3n, each point's offset from its aggregate's centroid.  R (optional, 36 * n_agg
