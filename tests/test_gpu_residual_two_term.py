@@ -73,6 +73,39 @@ def test_equilibrium_residual_and_newton_iterates():
     assert np.linalg.norm(u_t - u_6) <= 1e-7 * np.linalg.norm(u_6)
 
 
+def test_gradients_vs_oracle_with_element_scales():
+    """The two-term gradients against the FP64 oracle (ComputeGradients, FemPhysicsMatrixFree.cpp:536-560) at
+    random positions, also with per-element Young's moduli (the scaled branch of the kernel)."""
+    from solidfem_gb300 import FemPhysicsMatrixFree
+    from solidfem_gb300.mesh import box_lattice, lumped_face_load
+    from oracle.oracle import Oracle
+
+    rng = np.random.default_rng(103)
+    m = box_lattice(12, 5, 4, extent=(3.0, 1.0, 0.8), jitter=0.2, seed=3)
+    fixed = m.face_nodes(0, 0)
+    f = lumped_face_load(m, 2, 1, (0.0, 0.0, -700.0))
+    orc = Oracle(m.nodes, m.tets, fixed, 3e5, 0.43, 1100.0, (0.0, -2.0, -9.81), 3)
+    orc.set_nodal_loads(f)
+    p = FemPhysicsMatrixFree(m.tets, m.nodes, fixed, precision="fp32", young=3e5, poisson=0.43, density=1100.0,
+                             gravity=(0.0, -2.0, -9.81), material=3)
+    p.set_nodal_loads(f)
+    x = orc.free_positions() + 0.02 * rng.normal(size=3 * orc.n_free)
+    orc.set_free_positions(x)
+    p.set_free_positions(x)
+
+    def rel(a, b):
+        return np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b))
+
+    e0 = rel(p.ComputeGradients(), orc.gradients())
+    ye = 3e5 * np.exp(0.5 * rng.normal(size=m.n_tets))
+    p.set_element_youngs(ye)
+    orc.set_element_scale(ye / 3e5)
+    e1 = rel(p.ComputeGradients(), orc.gradients())
+    print(f"two-term gradients vs the FP64 oracle: {e0:.2e}; with element moduli {e1:.2e}")
+    assert e0 <= 1e-11 and e1 <= 1e-11
+    p.close()
+
+
 def test_inversion_detected():
     m, p = _slab()
     assert p.count_inverted() == 0
