@@ -6,7 +6,7 @@ Workload (one "step" = one complete static solve from the rest configuration):
   (seed 0), compressible neo-Hookean E=1e5 Pa, nu=0.49, bottom face z=0 clamped,
   per-node normal traction on the top face drawn from N(0, 200 Pa), smoothed by a
   Gaussian of width 4h and rescaled to 200 Pa std (load seeds 10000 + step).
-  Relative residual = |r(x_k)|_2 / |r(x_0)|_2 of the FP64 nonlinear residual.
+  Relative residual = |r(x_k)|_2 / |r(x_0)|_2 of the FP64-accurate nonlinear residual.
 
 Arms (one JSON line each):
   default          the repository's fastest method on the GPU: inexact Newton with FP32 flexible-CG

@@ -61,7 +61,7 @@ extern "C" {
 
 /* ---- precision of the element kernels and the inner Krylov solve ---- */
 #define SFEM_FP64 0
-#define SFEM_FP32 1 /* FP32 element kernels + CG; FP64 Newton residual and convergence test */
+#define SFEM_FP32 1 /* FP32 element kernels + CG; FP64-accurate Newton residual, FP64 convergence test */
 
 /* ---- tangent used by the Hessian-vector product ---- */
 #define SFEM_TANGENT_REFERENCE 0 /* the reference's force differential (FemPhysicsMatrixFree.cpp:436-470) */
