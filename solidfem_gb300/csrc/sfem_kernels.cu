@@ -1520,7 +1520,7 @@ template void launch_sell_hvp<double>(int64_t, int64_t, const int64_t*, const in
 // from HBM once and its mirror read, by a row up to the mesh's bandwidth away processed at about the
 // same time, hits L2.  DIR and the p.q / alpha finish as in k_sell_hvp.
 template <typename T, bool DIR, typename CI>
-__global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
+__global__ void __launch_bounds__(kThreads, 4) k_ssell_hvp(int64_t nbc, int64_t nf, const int64_t* __restrict__ base,
                                                         const CI* __restrict__ col, const int64_t* __restrict__ lbase,
                                                         const CI* __restrict__ lcol, const int32_t* __restrict__ lslot,
                                                         const T* __restrict__ vals, const T* __restrict__ p,
@@ -1566,11 +1566,23 @@ __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf,
 #pragma unroll
         for (int qq = 0; qq < 9; qq++) v[qq] = V[32 * qq];
       };
+      // the next pair's slots and columns are loaded while this pair's values are (one dependent
+      // round trip per pair instead of two)
       int k = 0;
+      int ta = -1, tb = -1;
+      int64_t ja = 0, jb = 0;
+      if (wl >= 2) {
+        ta = ls[0], tb = ls[32];
+        ja = cbase + lc[0], jb = cbase + lc[32];
+      }
       for (; k + 2 <= wl; k += 2) {
-        const int ta = ls[32 * k], tb = ls[32 * k + 32];
         if (ta < 0) break;
-        const int64_t ja = cbase + lc[32 * k], jb = cbase + lc[32 * k + 32];
+        int tan = -1, tbn = -1;
+        int64_t jan = 0, jbn = 0;
+        if (tb >= 0 && k + 4 <= wl) {
+          tan = ls[32 * k + 64], tbn = ls[32 * k + 96];
+          jan = cbase + lc[32 * k + 64], jbn = cbase + lc[32 * k + 96];
+        }
         T va[9], vb[9], xa0, xa1, xa2, xb0 = T(0), xb1 = T(0), xb2 = T(0);
         mirror(ta, va);
         xdir(ja, xa0, xa1, xa2);
@@ -1591,6 +1603,7 @@ __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf,
           k = wl;
           break;
         }
+        ta = tan, tb = tbn, ja = jan, jb = jbn;
       }
       if (k < wl) {
         const int ta = ls[32 * k];
@@ -1610,8 +1623,11 @@ __global__ void __launch_bounds__(kThreads) k_ssell_hvp(int64_t nbc, int64_t nf,
     const CI* cl = col + b0 + lane;
     const T* Vb = vals + 9 * b0 + lane;
     int k = 0;
+    CI ca = 0, cb = 0;
+    if (w >= 2) ca = cl[0], cb = cl[32];
     for (; k + 2 <= w; k += 2) {
-      const int64_t ja = cbase + cl[32 * k], jb = cbase + cl[32 * k + 32];
+      const int64_t ja = cbase + ca, jb = cbase + cb;
+      if (k + 4 <= w) ca = cl[32 * k + 64], cb = cl[32 * k + 96];
       const T* Va = Vb + 288 * k;
       const T* Wb = Va + 288;
       T va[9], vb[9];
