@@ -403,14 +403,22 @@ bool residual_two_term(const sfem_handle* h) {
 }
 int residual(sfem_handle* h, double* rnorm, int* n_inverted, double* energy = nullptr) {
   CU(cudaMemsetAsync(h->ninv, 0, sizeof(int), h->stream));
-  const bool tt = residual_two_term(h);
-  if (tt) {
+  bool tt = residual_two_term(h);
+  if (tt && !h->df_lo) {
     const int64_t E = h->E;
-    if (!h->df_lo) {
-      TRY(dalloc(&h->df_lo, 10 * (size_t)E));
+    if (dalloc(&h->df_lo, 10 * (size_t)E) == 0) {
       launch_split_geom(9 * E, h->X64, h->X32, h->df_lo, h->stream);
       launch_split_geom(E, h->vol64, h->vol32, h->df_lo + 9 * E, h->stream);
+    } else {  // without room for the low parts: the FP64 pass, for this handle from now on
+      cudaGetLastError();
+      h->df_lo = nullptr;
+      h->resid_arith = SFEM_RESIDUAL_FP64;
+      g_err.clear();
+      tt = false;
     }
+  }
+  if (tt) {
+    const int64_t E = h->E;
     const DfGeom dg{h->X32, h->df_lo, h->vol32, h->df_lo + 9 * E};
     launch_element_nh_df(energy != nullptr, h->ev64(), dg, h->u, reinterpret_cast<float2*>(h->fe), h->red(),
                          energy ? h->dres + 3 : nullptr, h->ninv, h->stream);
