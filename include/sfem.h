@@ -283,7 +283,9 @@ int sfem_operator_info(sfem_handle* h, int64_t* bytes, int32_t* fallback);
  * SFEM_RESIDUAL_TWO_TERM (default for SFEM_FP32 handles, neo-Hookean, no batched instances): the element
  * forces and energy in two-term FP32 arithmetic (about 48 significant bits, evaluated on H = F - I so
  * that no term of order one cancels), summed per node in the same arithmetic and converted to FP64 once;
- * as accurate as the FP64 pass, on the FP32 pipes; it keeps the low parts of X and V (40 B per element)
+ * element forces within about 1e-12 of their largest entry at any strain (the FP64 pass: about 1e-15 at
+ * large strains, 1e-8 at strains of 1e-6, where F - F^-T cancels), on the FP32 pipes; it keeps the low
+ * parts of X and V (40 B per element)
  * on the device, and a handle whose device has no room for them uses the FP64 pass from then on.
  * SFEM_RESIDUAL_FP64: FP64 instructions throughout (always so for SFEM_FP64 handles and the other
  * materials).  Returns SFEM_ERR_INVALID for other modes. */

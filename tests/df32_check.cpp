@@ -161,7 +161,33 @@ int main() {
   printf("force_rel_two_term %.3e\nforce_rel_fp64 %.3e\nenergy_rel_two_term %.3e\nenergy_rel_fp64 %.3e\n",
          (double)fe_tt, (double)fe_64, (double)pe_tt, (double)pe_64);
 
-  // 4. an inverted element reports itself and gives non-finite forces
+  // 4. node sums (the two-term gather): 24 element contributions that cancel to a small net force, added
+  //    in order with the accurate two-term addition; error relative to the largest contribution, beside
+  //    FP64 recursive summation of the same (FP64-rounded) contributions
+  ld gs_tt = 0, gs_64 = 0;
+  for (int i = 0; i < 100000; i++) {
+    double v[24];
+    double sum = 0;
+    for (int k = 0; k < 23; k++) v[k] = U(rng) * pow(10.0, 2.0 * U(rng)), sum += v[k];
+    v[23] = -sum + 1e-6 * U(rng);  // nearly in equilibrium
+    df acc = {0.0f, 0.0f};
+    double acc64 = 0;
+    ld exact = 0, vmax = 0;
+    for (int k = 0; k < 24; k++) {
+      const df t = sfem::df32::split_f64(v[k]);
+      acc = sfem::df32::df_add(acc, t);
+      acc64 += v[k];
+      exact += val(t);  // the two-term inputs exactly
+      vmax = fmaxl(vmax, fabsl((ld)v[k]));
+    }
+    ld exact64 = 0;
+    for (int k = 0; k < 24; k++) exact64 += (ld)v[k];
+    gs_tt = fmaxl(gs_tt, fabsl(val(acc) - exact) / vmax);
+    gs_64 = fmaxl(gs_64, fabsl((ld)acc64 - exact64) / vmax);
+  }
+  printf("node_sum_rel_two_term %.3e\nnode_sum_rel_fp64 %.3e\n", (double)gs_tt, (double)gs_64);
+
+  // 5. an inverted element reports itself and gives non-finite forces
   {
     double X[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, D[9] = {-2, 0, 0, 0, 0, 0, 0, 0, 0};
     df Dd[9], Xd[9], f[12], psi;

@@ -49,6 +49,13 @@ def test_energy(measured):
     assert measured["energy_rel_two_term"] <= measured["energy_rel_fp64"]
 
 
+def test_node_sums(measured):
+    # the gather's accurate two-term addition over 24 cancelling contributions: about 3u^2 (u = 2^-24) per
+    # addition relative to the partial sums, so ~25x FP64 recursive summation's error, far below the
+    # element forces' own
+    assert measured["node_sum_rel_two_term"] <= 1e-13
+
+
 def test_inverted_element(measured):
     assert measured["inverted_flag"] == 1
     assert measured["forces_nan"] == 1
